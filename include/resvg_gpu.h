@@ -1,0 +1,149 @@
+/*
+ * resvg_gpu.h — C ABI of the GB300 rendering backend (libresvg_gb300.so).
+ *
+ * Drop-in surface: `resvg_render` / `resvg_render_node` keep the signatures
+ * of resvg's C API (crates/c-api/resvg.h:485-489 and :505-510, implemented at
+ * crates/c-api/lib.rs:875-893 and :908-942): the caller owns a host pixmap of
+ * width*height*4 bytes of premultiplied RGBA8, and rendering draws onto its
+ * existing content.  Rendering runs on the GPU through hand-written sm_103a
+ * kernels; there is no CPU fallback — when no device is usable the call logs
+ * the error (resvg_gpu_last_error) and leaves the pixmap untouched, the way
+ * the reference logs and skips on internal failures (crates/resvg/src/render.rs:108).
+ *
+ * `resvg_render_tree` here wraps the backend's resolved tree (rgpu_tree.h),
+ * the counterpart of the usvg::Tree that resvg_render_tree wraps in the
+ * reference (crates/c-api/lib.rs:839-844).  Parsing SVG text stays outside
+ * this library, as usvg stays on the host in the reference.
+ *
+ * Every function other than the two drop-ins returns an rgpu_status and
+ * never aborts.
+ */
+#ifndef RESVG_GPU_H
+#define RESVG_GPU_H
+
+#include <stdbool.h>
+#include <stddef.h>
+#include <stdint.h>
+#include "rgpu_tree.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum rgpu_status {
+    RGPU_OK = 0,
+    RGPU_ERR_INVALID_ARG = 1,
+    RGPU_ERR_NO_DEVICE = 2,
+    RGPU_ERR_CUDA = 3,
+    RGPU_ERR_OUT_OF_MEMORY = 4,
+    RGPU_ERR_CAPACITY = 5,      /* a work buffer was too small; the host resizes and retries */
+    RGPU_ERR_DEVICE_FAULT = 6,  /* a kernel reported an error word (bounds/timeout), output untouched */
+    RGPU_ERR_UNSUPPORTED = 7
+} rgpu_status;
+
+/* resvg_transform (crates/c-api/resvg.h, lib.rs:67-81): {a,b,c,d,e,f}. */
+typedef struct resvg_transform {
+    float a, b, c, d, e, f;
+} resvg_transform;
+
+typedef struct rgpu_tree resvg_render_tree;
+
+/* ---- tree building (the usvg::Tree stand-in) ---------------------------- */
+resvg_render_tree *rgpu_tree_new(float width, float height);
+void rgpu_tree_free(resvg_render_tree *tree);
+/* Adds a group under `parent` (-1: detached, e.g. a clip/mask root). */
+int32_t rgpu_tree_add_group(resvg_render_tree *tree, int32_t parent, const rgpu_group *group);
+int32_t rgpu_tree_add_path(resvg_render_tree *tree, int32_t parent, const rgpu_path *path, const uint8_t *verbs,
+                           uint32_t verb_count, const float *points, uint32_t point_count, const float *dashes,
+                           uint32_t dash_count);
+int32_t rgpu_tree_add_paint(resvg_render_tree *tree, const rgpu_paint *paint, const rgpu_stop *stops,
+                            uint32_t stop_count);
+int32_t rgpu_tree_add_clip(resvg_render_tree *tree, const rgpu_clip *clip);
+int32_t rgpu_tree_add_mask(resvg_render_tree *tree, const rgpu_mask *mask);
+int32_t rgpu_tree_add_filter(resvg_render_tree *tree, const rgpu_filter *filter, const rgpu_primitive *prims,
+                             uint32_t prim_count, const int32_t *merge_inputs, uint32_t merge_count);
+/* Attaches filters (indices from rgpu_tree_add_filter) to a group. */
+int rgpu_tree_set_group_filters(resvg_render_tree *tree, int32_t group, const uint32_t *filters, uint32_t count);
+/* Computes path and layer bounding boxes; call once after building. */
+int rgpu_tree_finalize(resvg_render_tree *tree);
+const rgpu_tree_view *rgpu_tree_get_view(resvg_render_tree *tree);
+/* Seeded synthetic workloads (see resvg_gb300/csrc/host/gen.cpp):
+ * config 0..3; `scale` multiplies path counts (1.0 = full workload). */
+resvg_render_tree *rgpu_tree_generate(int config, uint64_t seed, uint64_t index, float scale);
+
+/* ---- drop-in render (host pixmap) --------------------------------------- */
+/* resvg_render: crates/c-api/resvg.h:485, lib.rs:875-893. */
+void resvg_render(const resvg_render_tree *tree, resvg_transform transform, uint32_t width, uint32_t height,
+                  char *pixmap);
+/* resvg_render_node: crates/c-api/resvg.h:505, lib.rs:908-942.  `id` is the
+ * index of a root child given as a decimal string (the tree keeps no SVG ids). */
+bool resvg_render_node(const resvg_render_tree *tree, const char *id, resvg_transform transform, uint32_t width,
+                       uint32_t height, char *pixmap);
+
+/* ---- GPU-native entry points --------------------------------------------- */
+/* Selects the CUDA device (no counterpart in the reference: resvg is CPU-only). */
+int rgpu_init(int device);
+/* Last error message of the calling thread ("" when none). */
+const char *rgpu_last_error(void);
+/* Render into a DEVICE pixmap on `stream` (cudaStream_t; 0 = default).  The
+ * pixmap is premultiplied RGBA8, `stride` bytes per row; rendering draws onto
+ * its content.  Asynchronous: returns after enqueueing.  Counterpart of
+ * resvg::render (crates/resvg/src/lib.rs:34) without host copies. */
+int rgpu_render_device(const resvg_render_tree *tree, resvg_transform transform, uint32_t width, uint32_t height,
+                       uint8_t *device_pixmap, uint32_t stride, void *stream);
+/* Batched form: renders `count` independent trees.  pixmaps[i] are DEVICE
+ * pointers of widths[i]*heights[i]*4 bytes, cleared to transparent by the
+ * caller or not (rendering draws onto content).  One submission; the work is
+ * spread over persistent work-queue kernels replayed from a captured CUDA
+ * graph.  No counterpart in the reference (resvg renders one tree per call). */
+int rgpu_render_batch(const resvg_render_tree *const *trees, const resvg_transform *transforms, uint32_t count,
+                      const uint32_t *widths, const uint32_t *heights, uint8_t *const *device_pixmaps, void *stream);
+
+/* Tuning knobs of the raster kernels (chosen by the autotuner). */
+typedef struct rgpu_tuning {
+    uint32_t band_rows;          /* pixel rows per raster work item: 0 (auto), 1, 2, 4 or 8 */
+    uint32_t pixels_per_thread;  /* consecutive pixels per raster thread: 0 (auto), 4, 8 or 16 */
+    uint32_t reserved;
+} rgpu_tuning;
+int rgpu_set_tuning(const rgpu_tuning *t);
+int rgpu_get_tuning(rgpu_tuning *t);
+
+/* Per-call statistics of the last render on this thread (for benchmarking). */
+typedef struct rgpu_stats {
+    uint64_t draws, edges, crossings_capacity, work_items, kernel_launches;
+    uint64_t h2d_bytes, d2h_bytes;
+    float raster_ms;         /* device time of the raster kernel (CUDA events) */
+} rgpu_stats;
+int rgpu_get_stats(rgpu_stats *s);
+
+/* ---- filter kernels on device images (filter module primitives) --------- */
+/* Box blur, 5 passes of (vertical, horizontal) box sums: crates/resvg/src/filter/box_blur.rs:23. */
+int rgpu_filter_box_blur(uint8_t *device_img, uint32_t width, uint32_t height, double sigma_x, double sigma_y,
+                         void *stream);
+/* IIR (recursive Gaussian) blur in f64: crates/resvg/src/filter/iir_blur.rs:47. */
+int rgpu_filter_iir_blur(uint8_t *device_img, uint32_t width, uint32_t height, double sigma_x, double sigma_y,
+                         void *stream);
+/* Morphology erode (0) / dilate (1): crates/resvg/src/filter/morphology.rs:15. */
+int rgpu_filter_morphology(uint8_t *device_img, uint32_t width, uint32_t height, int dilate, float rx, float ry,
+                           void *stream);
+/* sRGB <-> linearRGB on premultiplied pixels: crates/resvg/src/filter/mod.rs:115-125. */
+int rgpu_filter_color_space(uint8_t *device_img, uint32_t width, uint32_t height, int to_linear, void *stream);
+
+/* ---- differentiable soft-coverage form ---------------------------------- */
+/* Scene parameters for the analytic-area soft rasteriser (no counterpart in
+ * the reference).  See resvg_gb300/csrc/kernels/soft.cu. */
+typedef struct rgpu_soft_scene {
+    uint32_t width, height;     /* canvas */
+    uint32_t path_count;        /* closed cubic paths */
+    const uint32_t *seg_offset; /* path i owns cubic segments [seg_offset[i], seg_offset[i+1]) */
+    float *points;              /* 3 control points (x,y) per segment + implicit start: see soft.cu */
+    float *colors;              /* RGBA per path (straight alpha) */
+    float *stops;               /* 4 stops x (offset, r, g, b, a) per path, linear gradient */
+    float *grad_line;           /* (x1,y1,x2,y2) per path */
+    float *sigma;               /* blur sigma (1 per scene) */
+} rgpu_soft_scene;
+
+#ifdef __cplusplus
+}
+#endif
+#endif

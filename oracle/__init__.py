@@ -1,0 +1,84 @@
+"""CPU oracle — TEST INFRASTRUCTURE ONLY.
+
+A C++ restatement of resvg 0.48.1's render path (crates/resvg/src/{render,path,
+clip,mask,geom}.rs, crates/resvg/src/filter/*.rs) over a restatement of the
+tiny-skia 0.12.0 raster pipeline (not vendored in the reference; Skia's
+published algorithms).  Parity with resvg is pinned against resvg's own golden
+PNGs (crates/resvg/tests/tests/**, see tests/test_golden.py).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may load
+this module.  The product (resvg_gb300) never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+_lib = None
+
+
+def build() -> str:
+    subprocess.run([os.path.join(HERE, "build.sh")], check=True)
+    return LIB_PATH
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = C.CDLL(LIB_PATH)
+        L.oracle_render.restype = C.c_int
+        L.oracle_render.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.c_uint32, C.c_uint32, C.c_void_p]
+        for n in ("oracle_box_blur", "oracle_iir_blur"):
+            getattr(L, n).argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_double, C.c_double]
+        L.oracle_morphology.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_int, C.c_float, C.c_float]
+        L.oracle_to_linear.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32]
+        L.oracle_to_srgb.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32]
+        _lib = L
+    return _lib
+
+
+def render(tree_view_ptr, transform, width: int, height: int, pixmap: np.ndarray | None = None) -> np.ndarray:
+    """Renders a tree (pointer to an rgpu_tree_view) onto `pixmap` (premultiplied
+    RGBA8, (h, w, 4)); a fresh transparent pixmap when None.  Returns it."""
+    if pixmap is None:
+        pixmap = np.zeros((height, width, 4), dtype=np.uint8)
+    assert pixmap.dtype == np.uint8 and pixmap.shape == (height, width, 4) and pixmap.flags.c_contiguous
+    ts = (C.c_float * 6)(*[float(v) for v in transform])
+    r = lib().oracle_render(C.cast(tree_view_ptr, C.c_void_p), ts, width, height, pixmap.ctypes.data)
+    if r != 0:
+        raise RuntimeError("oracle_render failed")
+    return pixmap
+
+
+def _img_op(name, img, *args):
+    assert img.dtype == np.uint8 and img.ndim == 3 and img.shape[2] == 4
+    out = np.ascontiguousarray(img).copy()
+    getattr(lib(), name)(out.ctypes.data, out.shape[1], out.shape[0], *args)
+    return out
+
+
+def box_blur(img, sx, sy):
+    return _img_op("oracle_box_blur", img, C.c_double(sx), C.c_double(sy))
+
+
+def iir_blur(img, sx, sy):
+    return _img_op("oracle_iir_blur", img, C.c_double(sx), C.c_double(sy))
+
+
+def morphology(img, dilate, rx, ry):
+    return _img_op("oracle_morphology", img, int(dilate), C.c_float(rx), C.c_float(ry))
+
+
+def to_linear(img):
+    return _img_op("oracle_to_linear", img)
+
+
+def to_srgb(img):
+    return _img_op("oracle_to_srgb", img)

@@ -1,0 +1,563 @@
+// CPU oracle — test infrastructure only.
+//
+// Restatement of resvg 0.48.1's filter module:
+//   crates/resvg/src/filter/mod.rs:115-308   colour spaces, multiply/demultiply, LUTs, Image
+//   crates/resvg/src/filter/mod.rs:335-564   apply / apply_inner / get_input, subregion crop
+//   crates/resvg/src/filter/mod.rs:645-666   apply_blur, :1119-1147 resolve_std_dev
+//   crates/resvg/src/filter/mod.rs:731-793   apply_composite, :795-818 apply_merge
+//   crates/resvg/src/filter/mod.rs:905-956   colour matrix, convolve, morphology drivers
+//   crates/resvg/src/filter/mod.rs:1100-1114 apply_to_canvas
+//   crates/resvg/src/filter/box_blur.rs       box blur (5 box passes, V then H)
+//   crates/resvg/src/filter/iir_blur.rs       IIR blur (f64)
+//   crates/resvg/src/filter/color_matrix.rs, morphology.rs, composite.rs, convolve_matrix.rs
+// The two sRGB <-> linearRGB tables are resvg's (mod.rs:161-238): both are
+// the standard transfer functions evaluated and rounded to u8 (a data table
+// has to be identical to give identical output).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+#include "raster.h"
+
+namespace ora {
+
+namespace {
+
+const uint8_t SRGB_TO_LINEAR[256] = {
+    0,   0,   0,   0,   0,   0,   0,   1,   1,   1,   1,   1,   1,   1,   1,   1,   1,   1,   2,   2,   2,   2,
+    2,   2,   2,   2,   3,   3,   3,   3,   3,   3,   4,   4,   4,   4,   4,   5,   5,   5,   5,   6,   6,   6,
+    6,   7,   7,   7,   8,   8,   8,   8,   9,   9,   9,   10,  10,  10,  11,  11,  12,  12,  12,  13,  13,  13,
+    14,  14,  15,  15,  16,  16,  17,  17,  17,  18,  18,  19,  19,  20,  20,  21,  22,  22,  23,  23,  24,  24,
+    25,  25,  26,  27,  27,  28,  29,  29,  30,  30,  31,  32,  32,  33,  34,  35,  35,  36,  37,  37,  38,  39,
+    40,  41,  41,  42,  43,  44,  45,  45,  46,  47,  48,  49,  50,  51,  51,  52,  53,  54,  55,  56,  57,  58,
+    59,  60,  61,  62,  63,  64,  65,  66,  67,  68,  69,  70,  71,  72,  73,  74,  76,  77,  78,  79,  80,  81,
+    82,  84,  85,  86,  87,  88,  90,  91,  92,  93,  95,  96,  97,  99,  100, 101, 103, 104, 105, 107, 108, 109,
+    111, 112, 114, 115, 116, 118, 119, 121, 122, 124, 125, 127, 128, 130, 131, 133, 134, 136, 138, 139, 141, 142,
+    144, 146, 147, 149, 151, 152, 154, 156, 157, 159, 161, 163, 164, 166, 168, 170, 171, 173, 175, 177, 179, 181,
+    183, 184, 186, 188, 190, 192, 194, 196, 198, 200, 202, 204, 206, 208, 210, 212, 214, 216, 218, 220, 222, 224,
+    226, 229, 231, 233, 235, 237, 239, 242, 244, 246, 248, 250, 253, 255};
+const uint8_t LINEAR_TO_SRGB[256] = {
+    0,   13,  22,  28,  34,  38,  42,  46,  50,  53,  56,  59,  61,  64,  66,  69,  71,  73,  75,  77,  79,  81,
+    83,  85,  86,  88,  90,  92,  93,  95,  96,  98,  99,  101, 102, 104, 105, 106, 108, 109, 110, 112, 113, 114,
+    115, 117, 118, 119, 120, 121, 122, 124, 125, 126, 127, 128, 129, 130, 131, 132, 133, 134, 135, 136, 137, 138,
+    139, 140, 141, 142, 143, 144, 145, 146, 147, 148, 148, 149, 150, 151, 152, 153, 154, 155, 155, 156, 157, 158,
+    159, 159, 160, 161, 162, 163, 163, 164, 165, 166, 167, 167, 168, 169, 170, 170, 171, 172, 173, 173, 174, 175,
+    175, 176, 177, 178, 178, 179, 180, 180, 181, 182, 182, 183, 184, 185, 185, 186, 187, 187, 188, 189, 189, 190,
+    190, 191, 192, 192, 193, 194, 194, 195, 196, 196, 197, 197, 198, 199, 199, 200, 200, 201, 202, 202, 203, 203,
+    204, 205, 205, 206, 206, 207, 208, 208, 209, 209, 210, 210, 211, 212, 212, 213, 213, 214, 214, 215, 215, 216,
+    216, 217, 218, 218, 219, 219, 220, 220, 221, 221, 222, 222, 223, 223, 224, 224, 225, 226, 226, 227, 227, 228,
+    228, 229, 229, 230, 230, 231, 231, 232, 232, 233, 233, 234, 234, 235, 235, 236, 236, 237, 237, 238, 238, 238,
+    239, 239, 240, 240, 241, 241, 242, 242, 243, 243, 244, 244, 245, 245, 246, 246, 246, 247, 247, 248, 248, 249,
+    249, 250, 250, 251, 251, 251, 252, 252, 253, 253, 254, 254, 255, 255};
+
+inline uint8_t sat_u8f(float v) {
+    if (!(v > 0.0f)) return 0;
+    if (v >= 255.0f) return 255;
+    return (uint8_t)v;
+}
+inline uint8_t sat_u8d(double v) {
+    if (!(v > 0.0)) return 0;
+    if (v >= 255.0) return 255;
+    return (uint8_t)v;
+}
+// mod.rs:242-254
+inline float f32_bound(float mn, float v, float mx) {
+    if (v > mx) return mx;
+    if (v >= mn) return v;
+    return mn;
+}
+void multiply_alpha(std::vector<uint8_t> &d) {
+    for (size_t i = 0; i < d.size(); i += 4) {
+        float a = d[i + 3] / 255.0f;
+        d[i + 2] = sat_u8f(d[i + 2] * a + 0.5f);
+        d[i + 1] = sat_u8f(d[i + 1] * a + 0.5f);
+        d[i + 0] = sat_u8f(d[i + 0] * a + 0.5f);
+    }
+}
+void demultiply_alpha(std::vector<uint8_t> &d) {
+    for (size_t i = 0; i < d.size(); i += 4) {
+        float a = d[i + 3] / 255.0f;
+        d[i + 2] = sat_u8f(d[i + 2] / a + 0.5f);
+        d[i + 1] = sat_u8f(d[i + 1] / a + 0.5f);
+        d[i + 0] = sat_u8f(d[i + 0] / a + 0.5f);
+    }
+}
+void into_linear(Pixmap &p) {
+    demultiply_alpha(p.data);
+    for (size_t i = 0; i < p.data.size(); i += 4)
+        for (int k = 0; k < 3; k++) p.data[i + k] = SRGB_TO_LINEAR[p.data[i + k]];
+    multiply_alpha(p.data);
+}
+void into_srgb(Pixmap &p) {
+    demultiply_alpha(p.data);
+    for (size_t i = 0; i < p.data.size(); i += 4)
+        for (int k = 0; k < 3; k++) p.data[i + k] = LINEAR_TO_SRGB[p.data[i + k]];
+    multiply_alpha(p.data);
+}
+
+struct Image {
+    std::shared_ptr<Pixmap> image;
+    IntRect region;
+    bool linear;
+};
+
+Image into_cs(const Image &im, bool linear) {
+    if (im.linear == linear) return im;
+    auto p = std::make_shared<Pixmap>(*im.image);
+    if (linear) into_linear(*p); else into_srgb(*p);
+    return Image{p, im.region, linear};
+}
+
+// ---- box blur (box_blur.rs)
+inline float fround(float x) {
+    volatile float y = x + 12582912.0f;
+    return y - 12582912.0f;
+}
+void create_box_gauss(float sigma, int sizes[5]) {
+    if (sigma > 0.0f) {
+        float n = 5.0f;
+        float w_ideal = std::sqrt(12.0f * sigma * sigma / n) + 1.0f;
+        int wl = (int)std::floor(w_ideal);
+        if (wl % 2 == 0) wl -= 1;
+        int wu = wl + 2;
+        float wlf = (float)wl;
+        float m_ideal = (12.0f * sigma * sigma - n * wlf * wlf - 4.0f * n * wlf - 3.0f * n) / (-4.0f * wlf - 4.0f);
+        float mr = std::round(m_ideal);  // Rust f32::round: half away from zero
+        int m = mr <= 0.0f ? 0 : (int)mr;  // `as usize` saturates at 0
+        for (int i = 0; i < 5; i++) sizes[i] = i < m ? wl : wu;
+    } else {
+        for (int i = 0; i < 5; i++) sizes[i] = 1;
+    }
+}
+// One direction of the sliding-window box sum with zero padding; `stride`
+// walks along the line, `lines`/`lstride` across lines.
+void box_pass(const uint8_t *src, uint8_t *dst, int len, int lines, size_t stride, size_t lstride, int r) {
+    if (r == 0) {
+        for (int l = 0; l < lines; l++)
+            for (int i = 0; i < len; i++) std::memcpy(dst + l * lstride + i * stride, src + l * lstride + i * stride, 4);
+        return;
+    }
+    float iarr = 1.0f / (float)(r + r + 1);
+    for (int l = 0; l < lines; l++) {
+        const uint8_t *s = src + l * lstride;
+        uint8_t *d = dst + l * lstride;
+        long val[4] = {0, 0, 0, 0};
+        for (int j = 0; j < std::min(r, len); j++)
+            for (int k = 0; k < 4; k++) val[k] += s[j * stride + k];
+        for (int i = 0; i < len; i++) {
+            int add = i + r, sub = i - r - 1;
+            if (add < len) for (int k = 0; k < 4; k++) val[k] += s[add * stride + k];
+            if (sub >= 0) for (int k = 0; k < 4; k++) val[k] -= s[sub * stride + k];
+            for (int k = 0; k < 4; k++) d[i * stride + k] = sat_u8f(fround((float)val[k] * iarr));
+        }
+    }
+}
+void box_blur(double sx, double sy, Pixmap &src) {
+    int bh[5], bv[5];
+    create_box_gauss((float)sx, bh);
+    create_box_gauss((float)sy, bv);
+    std::vector<uint8_t> back = src.data;
+    int w = (int)src.width, h = (int)src.height;
+    for (int i = 0; i < 5; i++) {
+        int rh = (bh[i] - 1) / 2, rv = (bv[i] - 1) / 2;
+        box_pass(src.data.data(), back.data(), h, w, (size_t)w * 4, 4, rv);   // vertical: src -> back
+        box_pass(back.data(), src.data.data(), w, h, 4, (size_t)w * 4, rh);   // horizontal: back -> src
+    }
+}
+
+// ---- IIR blur (iir_blur.rs)
+void gen_coefficients(double sigma, int steps, double *lambda, double *dnu) {
+    *lambda = (sigma * sigma) / (2.0 * steps);
+    *dnu = (1.0 + 2.0 * *lambda - std::sqrt(1.0 + 4.0 * *lambda)) / (2.0 * *lambda);
+}
+void gaussianiir2d(int width, int height, double sx, double sy, std::vector<double> &buf) {
+    const int steps = 4;
+    double lx = 1.0, dx = 1.0, ly = 1.0, dy = 1.0;
+    if (sx > 0.0) {
+        gen_coefficients(sx, steps, &lx, &dx);
+        for (int y = 0; y < height; y++)
+            for (int s = 0; s < steps; s++) {
+                size_t idx = (size_t)width * y;
+                for (int x = 1; x < width; x++) buf[idx + x] += dx * buf[idx + x - 1];
+                for (int x = width - 1; x > 0; x--) buf[idx + x - 1] += dx * buf[idx + x];
+            }
+    }
+    if (sy > 0.0) {
+        gen_coefficients(sy, steps, &ly, &dy);
+        for (int x = 0; x < width; x++)
+            for (int s = 0; s < steps; s++) {
+                size_t idx = x;
+                for (size_t y = width; y < buf.size(); y += width) buf[idx + y] += dy * buf[idx + y - width];
+                for (size_t y = buf.size() - width; y > 0; y -= width) buf[idx + y - width] += dy * buf[idx + y];
+            }
+    }
+    double post = std::pow(std::sqrt(dx * dy) / std::sqrt(lx * ly), 2 * steps);
+    for (auto &v : buf) v *= post;
+}
+void iir_blur(double sx, double sy, Pixmap &src) {
+    size_t n = (size_t)src.width * src.height;
+    std::vector<double> buf(n);
+    for (int ch = 0; ch < 4; ch++) {
+        for (size_t i = 0; i < n; i++) buf[i] = src.data[i * 4 + ch] / 255.0;
+        gaussianiir2d((int)src.width, (int)src.height, sx, sy, buf);
+        for (size_t i = 0; i < n; i++) src.data[i * 4 + ch] = sat_u8d(buf[i] * 255.0);
+    }
+}
+
+bool approx_zero_ulps(float v) {
+    // ApproxEqUlps against 0.0 with 4 ulps
+    int32_t a, b = 0;
+    std::memcpy(&a, &v, 4);
+    if ((a < 0) != (b < 0)) return v == 0.0f;
+    return std::abs(a - b) <= 4;
+}
+
+bool resolve_std_dev(float sdx, float sdy, const Transform &ts, double *ox, double *oy, bool *box) {
+    float sx, sy;
+    ts.get_scale(&sx, &sy);
+    float x = sdx * sx, y = sdy * sy;
+    if (approx_zero_ulps(x) && approx_zero_ulps(y)) return false;
+    if (x < 0.05f) x = 0.0f;
+    if (y < 0.05f) y = 0.0f;
+    *box = x >= 2.0f || y >= 2.0f;
+    *ox = x; *oy = y;
+    return true;
+}
+
+// ---- colour matrix (color_matrix.rs)
+inline uint8_t from_normalized(float c) { return sat_u8f(f32_bound(0.0f, c, 1.0f) * 255.0f); }
+void color_matrix(const rgpu_primitive &p, Pixmap &pm) {
+    auto &d = pm.data;
+    int kind = p.i[0];
+    if (kind == RGPU_CM_MATRIX) {
+        const float *m = p.f;
+        for (size_t i = 0; i < d.size(); i += 4) {
+            float r = d[i] / 255.0f, g = d[i + 1] / 255.0f, b = d[i + 2] / 255.0f, a = d[i + 3] / 255.0f;
+            float nr = r * m[0] + g * m[1] + b * m[2] + a * m[3] + m[4];
+            float ng = r * m[5] + g * m[6] + b * m[7] + a * m[8] + m[9];
+            float nb = r * m[10] + g * m[11] + b * m[12] + a * m[13] + m[14];
+            float na = r * m[15] + g * m[16] + b * m[17] + a * m[18] + m[19];
+            d[i] = from_normalized(nr); d[i + 1] = from_normalized(ng);
+            d[i + 2] = from_normalized(nb); d[i + 3] = from_normalized(na);
+        }
+    } else if (kind == RGPU_CM_SATURATE || kind == RGPU_CM_HUE_ROTATE) {
+        float m[9];
+        if (kind == RGPU_CM_SATURATE) {
+            float v = std::max(p.f[0], 0.0f);
+            float mm[9] = {0.213f + 0.787f * v, 0.715f - 0.715f * v, 0.072f - 0.072f * v,
+                           0.213f - 0.213f * v, 0.715f + 0.285f * v, 0.072f - 0.072f * v,
+                           0.213f - 0.213f * v, 0.715f - 0.715f * v, 0.072f + 0.928f * v};
+            std::memcpy(m, mm, sizeof(m));
+        } else {
+            float angle = p.f[0] * (float)(M_PI / 180.0);
+            float a1 = std::cos(angle), a2 = std::sin(angle);
+            float mm[9] = {0.213f + 0.787f * a1 - 0.213f * a2, 0.715f - 0.715f * a1 - 0.715f * a2,
+                           0.072f - 0.072f * a1 + 0.928f * a2, 0.213f - 0.213f * a1 + 0.143f * a2,
+                           0.715f + 0.285f * a1 + 0.140f * a2, 0.072f - 0.072f * a1 - 0.283f * a2,
+                           0.213f - 0.213f * a1 - 0.787f * a2, 0.715f - 0.715f * a1 + 0.715f * a2,
+                           0.072f + 0.928f * a1 + 0.072f * a2};
+            std::memcpy(m, mm, sizeof(m));
+        }
+        for (size_t i = 0; i < d.size(); i += 4) {
+            float r = d[i] / 255.0f, g = d[i + 1] / 255.0f, b = d[i + 2] / 255.0f;
+            d[i] = from_normalized(r * m[0] + g * m[1] + b * m[2]);
+            d[i + 1] = from_normalized(r * m[3] + g * m[4] + b * m[5]);
+            d[i + 2] = from_normalized(r * m[6] + g * m[7] + b * m[8]);
+        }
+    } else {
+        for (size_t i = 0; i < d.size(); i += 4) {
+            float r = d[i] / 255.0f, g = d[i + 1] / 255.0f, b = d[i + 2] / 255.0f;
+            float na = r * 0.2125f + g * 0.7154f + b * 0.0721f;
+            d[i] = d[i + 1] = d[i + 2] = 0;
+            d[i + 3] = from_normalized(na);
+        }
+    }
+}
+
+// ---- morphology (morphology.rs)
+void morphology(bool dilate, float rx, float ry, Pixmap &src) {
+    uint32_t columns = std::min((uint32_t)std::ceil(rx) * 2, src.width);
+    uint32_t rows = std::min((uint32_t)std::ceil(ry) * 2, src.height);
+    uint32_t tx0 = (uint32_t)std::floor(columns / 2.0f), ty0 = (uint32_t)std::floor(rows / 2.0f);
+    int32_t wmax = (int32_t)src.width - 1, hmax = (int32_t)src.height - 1;
+    std::vector<uint8_t> buf(src.data.size(), 0);
+    for (uint32_t y = 0; y < src.height; y++)
+        for (uint32_t x = 0; x < src.width; x++) {
+            uint8_t np[4];
+            for (int k = 0; k < 4; k++) np[k] = dilate ? 0 : 255;
+            for (uint32_t oy = 0; oy < rows; oy++)
+                for (uint32_t ox = 0; ox < columns; ox++) {
+                    int32_t tx = (int32_t)x - (int32_t)tx0 + (int32_t)ox, ty = (int32_t)y - (int32_t)ty0 + (int32_t)oy;
+                    if (tx < 0 || tx > wmax || ty < 0 || ty > hmax) continue;
+                    const uint8_t *p = src.px((uint32_t)tx, (uint32_t)ty);
+                    for (int k = 0; k < 4; k++) np[k] = dilate ? std::max(np[k], p[k]) : std::min(np[k], p[k]);
+                }
+            std::memcpy(&buf[((size_t)y * src.width + x) * 4], np, 4);
+        }
+    src.data = buf;
+}
+
+// ---- arithmetic composite (composite.rs)
+void arithmetic(float k1, float k2, float k3, float k4, const Pixmap &s1, const Pixmap &s2, Pixmap &dst) {
+    auto calc = [&](uint8_t i1, uint8_t i2, float mx) {
+        float a = i1 / 255.0f, b = i2 / 255.0f;
+        float r = k1 * a * b + k2 * a + k3 * b + k4;
+        return f32_bound(0.0f, r, mx);
+    };
+    size_t n = (size_t)dst.width * dst.height;
+    for (size_t i = 0; i < n; i++) {
+        const uint8_t *c1 = &s1.data[i * 4], *c2 = &s2.data[i * 4];
+        float a = calc(c1[3], c2[3], 1.0f);
+        if (approx_zero_ulps(a)) continue;
+        uint8_t *d = &dst.data[i * 4];
+        d[0] = sat_u8f(calc(c1[0], c2[0], a) * 255.0f);
+        d[1] = sat_u8f(calc(c1[1], c2[1], a) * 255.0f);
+        d[2] = sat_u8f(calc(c1[2], c2[2], a) * 255.0f);
+        d[3] = sat_u8f(a * 255.0f);
+    }
+}
+
+// ---- convolve matrix (convolve_matrix.rs)
+void convolve(const rgpu_primitive &p, Pixmap &src) {
+    int cols = p.i[0], rows = p.i[1], tx0 = p.i[2], ty0 = p.i[3], edge = p.i[4];
+    bool preserve = p.i[5] != 0;
+    float divisor = p.f[0], bias = p.f[1];
+    const float *k = p.f + 2;
+    int32_t wmax = (int32_t)src.width - 1, hmax = (int32_t)src.height - 1;
+    std::vector<uint8_t> buf(src.data.size(), 0);
+    for (uint32_t y = 0; y < src.height; y++)
+        for (uint32_t x = 0; x < src.width; x++) {
+            float nr = 0, ng = 0, nb = 0, na = 0;
+            for (int oy = 0; oy < rows; oy++)
+                for (int ox = 0; ox < cols; ox++) {
+                    int32_t tx = (int32_t)x - tx0 + ox, ty = (int32_t)y - ty0 + oy;
+                    if (edge == RGPU_EDGE_NONE) {
+                        if (tx < 0 || tx > wmax || ty < 0 || ty > hmax) continue;
+                    } else if (edge == RGPU_EDGE_DUPLICATE) {
+                        tx = std::max(0, std::min(wmax, tx));
+                        ty = std::max(0, std::min(hmax, ty));
+                    } else {
+                        while (tx < 0) tx += (int32_t)src.width;
+                        tx %= (int32_t)src.width;
+                        while (ty < 0) ty += (int32_t)src.height;
+                        ty %= (int32_t)src.height;
+                    }
+                    float kv = k[(rows - oy - 1) * cols + (cols - ox - 1)];
+                    const uint8_t *pp = src.px((uint32_t)tx, (uint32_t)ty);
+                    nr += (float)pp[0] / 255.0f * kv;
+                    ng += (float)pp[1] / 255.0f * kv;
+                    nb += (float)pp[2] / 255.0f * kv;
+                    if (!preserve) na += (float)pp[3] / 255.0f * kv;
+                }
+            const uint8_t *in_p = src.px(x, y);
+            if (preserve) na = in_p[3] / 255.0f;
+            else na = na / divisor + bias;
+            float bna = f32_bound(0.0f, na, 1.0f);
+            auto calc = [&](float v) {
+                float q = v / divisor + bias * na;
+                q = preserve ? f32_bound(0.0f, q, 1.0f) * bna : f32_bound(0.0f, q, bna);
+                return sat_u8f(q * 255.0f + 0.5f);
+            };
+            uint8_t *o = &buf[((size_t)y * src.width + x) * 4];
+            o[0] = calc(nr); o[1] = calc(ng); o[2] = calc(nb);
+            o[3] = sat_u8f(bna * 255.0f + 0.5f);
+        }
+    src.data = buf;
+}
+
+bool int_rect_eq(const IntRect &a, const IntRect &b) { return a.x == b.x && a.y == b.y && a.w == b.w && a.h == b.h; }
+
+struct Result { Image image; };
+
+}  // namespace
+
+// mod.rs:335-521 apply/apply_inner + mod.rs:1100-1114 apply_to_canvas
+bool filter_apply(const rgpu_tree_view &t, const rgpu_filter &f, const Transform &ts, Pixmap &source) {
+    auto fail = [&]() { pixmap_fill(source, ColorF{0, 0, 0, 0}); return false; };
+    bool ok;
+    Rect fr = rect_transform(Rect{f.x, f.y, f.x + f.w, f.y + f.h}, ts, &ok);
+    if (!ok) return fail();
+    IntRect region;
+    if (!rect_to_int_rect(fr, &region)) return fail();
+    {
+        IntRect src_rect{0, 0, (int32_t)source.width, (int32_t)source.height};
+        int32_t l = std::max(region.x, 0), tt = std::max(region.y, 0);
+        int32_t r = std::min(region.right(), src_rect.right()), b = std::min(region.bottom(), src_rect.bottom());
+        if (r <= l || b <= tt) return fail();
+        region = IntRect{l, tt, r - l, b - tt};
+    }
+    std::vector<Image> results;
+    auto get_input = [&](int32_t in) -> Image {
+        if (in >= 0 && (size_t)in < results.size()) return results[in];
+        auto p = std::make_shared<Pixmap>(source);
+        if (in == RGPU_IN_SOURCE_ALPHA)
+            for (size_t i = 0; i < p->data.size(); i += 4) p->data[i] = p->data[i + 1] = p->data[i + 2] = 0;
+        return Image{p, region, false};
+    };
+    for (uint32_t pi = 0; pi < f.prim_count; pi++) {
+        const rgpu_primitive &p = t.prims[f.prim_offset + pi];
+        Rect pr = rect_transform(Rect{p.x, p.y, p.x + p.w, p.y + p.h}, ts, &ok);
+        if (!ok) return fail();
+        IntRect subregion;
+        if (!rect_to_int_rect(pr, &subregion)) return fail();
+        bool lin = p.linear_rgb != 0;
+        Image res;
+        switch (p.kind) {
+        case RGPU_FE_BLUR: {
+            Image in = get_input(p.in1);
+            double sx, sy;
+            bool box;
+            if (!resolve_std_dev(p.f[0], p.f[1], ts, &sx, &sy, &box)) { res = in; break; }
+            Image c = into_cs(in, lin);
+            auto pm = std::make_shared<Pixmap>(*c.image);
+            if (box) box_blur(sx, sy, *pm); else iir_blur(sx, sy, *pm);
+            res = Image{pm, IntRect{0, 0, (int32_t)pm->width, (int32_t)pm->height}, lin};
+            break;
+        }
+        case RGPU_FE_COLOR_MATRIX: {
+            Image c = into_cs(get_input(p.in1), lin);
+            auto pm = std::make_shared<Pixmap>(*c.image);
+            demultiply_alpha(pm->data);
+            color_matrix(p, *pm);
+            multiply_alpha(pm->data);
+            res = Image{pm, IntRect{0, 0, (int32_t)pm->width, (int32_t)pm->height}, lin};
+            break;
+        }
+        case RGPU_FE_MORPHOLOGY: {
+            Image c = into_cs(get_input(p.in1), lin);
+            auto pm = std::make_shared<Pixmap>(*c.image);
+            float sx, sy;
+            ts.get_scale(&sx, &sy);
+            float rx = p.f[0] * sx, ry = p.f[1] * sy;
+            if (!(rx > 0.0f && ry > 0.0f)) pixmap_fill(*pm, ColorF{0, 0, 0, 0});
+            else morphology(p.i[0] == 1, rx, ry, *pm);
+            res = Image{pm, IntRect{0, 0, (int32_t)pm->width, (int32_t)pm->height}, lin};
+            break;
+        }
+        case RGPU_FE_COMPOSITE: {
+            Image i1 = into_cs(get_input(p.in1), lin), i2 = into_cs(get_input(p.in2), lin);
+            auto pm = std::make_shared<Pixmap>((uint32_t)region.w, (uint32_t)region.h);
+            if (p.i[0] == RGPU_OP_ARITHMETIC) {
+                arithmetic(p.f[0], p.f[1], p.f[2], p.f[3], *i1.image, *i2.image, *pm);
+            } else {
+                draw_pixmap(*pm, 0, 0, *i2.image, 1.0f, RGPU_BLEND_SOURCE_OVER);
+                uint32_t bm = RGPU_BLEND_SOURCE_OVER;
+                switch (p.i[0]) {
+                case RGPU_OP_IN: bm = RGPU_BLEND_SOURCE_IN; break;
+                case RGPU_OP_OUT: bm = RGPU_BLEND_SOURCE_OUT; break;
+                case RGPU_OP_ATOP: bm = RGPU_BLEND_SOURCE_ATOP; break;
+                case RGPU_OP_XOR: bm = RGPU_BLEND_XOR; break;
+                default: break;
+                }
+                draw_pixmap(*pm, 0, 0, *i1.image, 1.0f, bm);
+            }
+            res = Image{pm, IntRect{0, 0, (int32_t)pm->width, (int32_t)pm->height}, lin};
+            break;
+        }
+        case RGPU_FE_CONVOLVE: {
+            Image c = into_cs(get_input(p.in1), lin);
+            auto pm = std::make_shared<Pixmap>(*c.image);
+            if (p.i[5]) demultiply_alpha(pm->data);
+            convolve(p, *pm);
+            res = Image{pm, IntRect{0, 0, (int32_t)pm->width, (int32_t)pm->height}, lin};
+            break;
+        }
+        case RGPU_FE_FLOOD: {
+            auto pm = std::make_shared<Pixmap>((uint32_t)region.w, (uint32_t)region.h);
+            pixmap_fill(*pm, color_from_rgba8((uint8_t)p.i[0], (uint8_t)p.i[1], (uint8_t)p.i[2], to_u8_norm(p.f[0])));
+            res = Image{pm, IntRect{0, 0, (int32_t)pm->width, (int32_t)pm->height}, false};
+            break;
+        }
+        case RGPU_FE_OFFSET: {
+            Image in = get_input(p.in1);
+            float sx, sy;
+            ts.get_scale(&sx, &sy);
+            float dx = p.f[0] * sx, dy = p.f[1] * sy;
+            if (approx_zero_ulps(dx) && approx_zero_ulps(dy)) { res = in; break; }
+            auto pm = std::make_shared<Pixmap>(in.image->width, in.image->height);
+            draw_pixmap(*pm, sat_i32(dx), sat_i32(dy), *in.image, 1.0f, RGPU_BLEND_SOURCE_OVER);
+            res = Image{pm, IntRect{0, 0, (int32_t)pm->width, (int32_t)pm->height}, in.linear};
+            break;
+        }
+        case RGPU_FE_MERGE: {
+            auto pm = std::make_shared<Pixmap>((uint32_t)region.w, (uint32_t)region.h);
+            for (int32_t k = 0; k < p.i[1]; k++) {
+                Image c = into_cs(get_input(t.merge_inputs[p.i[0] + k]), lin);
+                draw_pixmap(*pm, 0, 0, *c.image, 1.0f, RGPU_BLEND_SOURCE_OVER);
+            }
+            res = Image{pm, IntRect{0, 0, (int32_t)pm->width, (int32_t)pm->height}, lin};
+            break;
+        }
+        case RGPU_FE_BLEND: {
+            Image i1 = into_cs(get_input(p.in1), lin), i2 = into_cs(get_input(p.in2), lin);
+            auto pm = std::make_shared<Pixmap>((uint32_t)region.w, (uint32_t)region.h);
+            draw_pixmap(*pm, 0, 0, *i2.image, 1.0f, RGPU_BLEND_SOURCE_OVER);
+            draw_pixmap(*pm, 0, 0, *i1.image, 1.0f, (uint32_t)p.i[0]);
+            res = Image{pm, IntRect{0, 0, (int32_t)pm->width, (int32_t)pm->height}, lin};
+            break;
+        }
+        default:
+            return fail();
+        }
+        if (!int_rect_eq(region, subregion)) {
+            IntRect sub2 = p.kind == RGPU_FE_OFFSET ? IntRect{0, 0, region.w, region.h}
+                                                     : IntRect{subregion.x - region.x, subregion.y - region.y,
+                                                               subregion.w, subregion.h};
+            auto pm = std::make_shared<Pixmap>(*res.image);
+            float w = (float)pm->width, h = (float)pm->height;
+            Paint clear;
+            clear.shader.color = ColorF{0, 0, 0, 1};
+            clear.blend = RGPU_BLEND_CLEAR;
+            if (sub2.y > 0) fill_rect(*pm, Rect{0, 0, w, (float)sub2.y}, clear);
+            if (sub2.x > 0) fill_rect(*pm, Rect{0, 0, (float)sub2.x, h}, clear);
+            fill_rect(*pm, Rect{(float)sub2.right(), 0, (float)sub2.right() + w, h}, clear);
+            fill_rect(*pm, Rect{0, (float)sub2.bottom(), w, (float)sub2.bottom() + h}, clear);
+            res = Image{pm, subregion, res.linear};
+        }
+        results.push_back(res);
+    }
+    if (results.empty()) return fail();
+    Image last = into_cs(results.back(), false);
+    pixmap_fill(source, ColorF{0, 0, 0, 0});
+    draw_pixmap(source, 0, 0, *last.image, 1.0f, RGPU_BLEND_SOURCE_OVER);
+    return true;
+}
+
+}  // namespace ora
+
+extern "C" {
+// Direct filter-kernel oracles (tests only): operate on a premultiplied RGBA8
+// image in place.
+void oracle_box_blur(uint8_t *img, uint32_t w, uint32_t h, double sx, double sy) {
+    ora::Pixmap p(w, h);
+    std::memcpy(p.data.data(), img, (size_t)w * h * 4);
+    ora::box_blur(sx, sy, p);
+    std::memcpy(img, p.data.data(), (size_t)w * h * 4);
+}
+void oracle_iir_blur(uint8_t *img, uint32_t w, uint32_t h, double sx, double sy) {
+    ora::Pixmap p(w, h);
+    std::memcpy(p.data.data(), img, (size_t)w * h * 4);
+    ora::iir_blur(sx, sy, p);
+    std::memcpy(img, p.data.data(), (size_t)w * h * 4);
+}
+void oracle_morphology(uint8_t *img, uint32_t w, uint32_t h, int dilate, float rx, float ry) {
+    ora::Pixmap p(w, h);
+    std::memcpy(p.data.data(), img, (size_t)w * h * 4);
+    ora::morphology(dilate != 0, rx, ry, p);
+    std::memcpy(img, p.data.data(), (size_t)w * h * 4);
+}
+void oracle_to_linear(uint8_t *img, uint32_t w, uint32_t h) {
+    ora::Pixmap p(w, h);
+    std::memcpy(p.data.data(), img, (size_t)w * h * 4);
+    ora::into_linear(p);
+    std::memcpy(img, p.data.data(), (size_t)w * h * 4);
+}
+void oracle_to_srgb(uint8_t *img, uint32_t w, uint32_t h) {
+    ora::Pixmap p(w, h);
+    std::memcpy(p.data.data(), img, (size_t)w * h * 4);
+    ora::into_srgb(p);
+    std::memcpy(img, p.data.data(), (size_t)w * h * 4);
+}
+}

@@ -1,0 +1,210 @@
+"""resvg_gb300 — GB300-native rendering backend for resvg (host-side Python API).
+
+The native library (libresvg_gb300.so, built in-tree by resvg_gb300.build)
+holds the tree builder, the host flattener and the sm_103a CUDA kernels; this
+module is a thin ctypes layer over its C ABI (include/resvg_gpu.h).  Rendering
+always runs on the GPU; there is no CPU fallback, and a missing or unusable
+device raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _abi
+from ._abi import (Clip, Filter, Group, Mask, Paint, Path, Primitive, Stop, Transform)  # noqa: F401
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_native", "libresvg_gb300.so")
+_lib = None
+
+
+class RenderError(RuntimeError):
+    pass
+
+
+def lib() -> C.CDLL:
+    """Loads libresvg_gb300.so (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RenderError("libresvg_gb300.so is not built; run `python -m resvg_gb300.build`")
+        L = C.CDLL(LIB_PATH)
+        _abi.declare(L)
+        _declare_render(L)
+        _lib = L
+    return _lib
+
+
+def _declare_render(L):
+    P = C.c_void_p
+    L.resvg_render.restype = None
+    L.resvg_render.argtypes = [P, _abi.ResvgTransform, C.c_uint32, C.c_uint32, P]
+    L.resvg_render_node.restype = C.c_bool
+    L.resvg_render_node.argtypes = [P, C.c_char_p, _abi.ResvgTransform, C.c_uint32, C.c_uint32, P]
+    L.rgpu_init.restype = C.c_int
+    L.rgpu_init.argtypes = [C.c_int]
+    L.rgpu_last_error.restype = C.c_char_p
+    L.rgpu_render_device.restype = C.c_int
+    L.rgpu_render_device.argtypes = [P, _abi.ResvgTransform, C.c_uint32, C.c_uint32, P, C.c_uint32, P]
+    L.rgpu_render_batch.restype = C.c_int
+    L.rgpu_render_batch.argtypes = [C.POINTER(P), C.POINTER(_abi.ResvgTransform), C.c_uint32,
+                                    C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(P), P]
+    L.rgpu_set_tuning.restype = C.c_int
+    L.rgpu_set_tuning.argtypes = [C.POINTER(_abi.Tuning)]
+    L.rgpu_get_tuning.restype = C.c_int
+    L.rgpu_get_tuning.argtypes = [C.POINTER(_abi.Tuning)]
+    L.rgpu_get_stats.restype = C.c_int
+    L.rgpu_get_stats.argtypes = [C.POINTER(_abi.Stats)]
+    for n in ("rgpu_filter_box_blur", "rgpu_filter_iir_blur"):
+        if hasattr(L, n):
+            getattr(L, n).restype = C.c_int
+            getattr(L, n).argtypes = [P, C.c_uint32, C.c_uint32, C.c_double, C.c_double, P]
+    if hasattr(L, "rgpu_filter_morphology"):
+        L.rgpu_filter_morphology.restype = C.c_int
+        L.rgpu_filter_morphology.argtypes = [P, C.c_uint32, C.c_uint32, C.c_int, C.c_float, C.c_float, P]
+    if hasattr(L, "rgpu_filter_color_space"):
+        L.rgpu_filter_color_space.restype = C.c_int
+        L.rgpu_filter_color_space.argtypes = [P, C.c_uint32, C.c_uint32, C.c_int, P]
+
+
+def check(status: int, what: str = "") -> None:
+    if status != 0:
+        msg = lib().rgpu_last_error().decode(errors="replace")
+        raise RenderError("%s failed (status %d): %s" % (what, status, msg))
+
+
+class Tree:
+    """A resolved render tree (the usvg::Tree stand-in), built node by node or
+    generated.  Group 0 is the root."""
+
+    def __init__(self, width: float = 0, height: float = 0, _handle=None):
+        self._h = _handle if _handle is not None else lib().rgpu_tree_new(float(width), float(height))
+        if not self._h:
+            raise ValueError("invalid tree size")
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            _lib.rgpu_tree_free(h)
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    @staticmethod
+    def generate(config: int, seed: int = 0, index: int = 0, scale: float = 1.0) -> "Tree":
+        h = lib().rgpu_tree_generate(int(config), int(seed), int(index), float(scale))
+        if not h:
+            raise ValueError("unknown config %r" % config)
+        return Tree(_handle=h)
+
+    def add_group(self, parent: int, group: Group) -> int:
+        return lib().rgpu_tree_add_group(self._h, parent, C.byref(group))
+
+    def add_paint(self, paint: Paint, stops=()) -> int:
+        arr = (Stop * max(1, len(stops)))(*stops)
+        return lib().rgpu_tree_add_paint(self._h, C.byref(paint), arr, len(stops))
+
+    def add_path(self, parent: int, path: Path, verbs, points, dashes=()) -> int:
+        v = np.ascontiguousarray(np.asarray(verbs, dtype=np.uint8))
+        p = np.ascontiguousarray(np.asarray(points, dtype=np.float32).reshape(-1))
+        d = np.ascontiguousarray(np.asarray(dashes, dtype=np.float32).reshape(-1))
+        return lib().rgpu_tree_add_path(
+            self._h, parent, C.byref(path), v.ctypes.data_as(C.POINTER(C.c_uint8)), len(v),
+            p.ctypes.data_as(C.POINTER(C.c_float)), len(p) // 2,
+            d.ctypes.data_as(C.POINTER(C.c_float)) if len(d) else None, len(d))
+
+    def add_clip(self, clip: Clip) -> int:
+        return lib().rgpu_tree_add_clip(self._h, C.byref(clip))
+
+    def add_mask(self, mask: Mask) -> int:
+        return lib().rgpu_tree_add_mask(self._h, C.byref(mask))
+
+    def add_filter(self, filt: Filter, prims, merge_inputs=()) -> int:
+        arr = (Primitive * max(1, len(prims)))(*prims)
+        m = (C.c_int32 * max(1, len(merge_inputs)))(*merge_inputs)
+        return lib().rgpu_tree_add_filter(self._h, C.byref(filt), arr, len(prims), m, len(merge_inputs))
+
+    def set_group_filters(self, group: int, filters) -> None:
+        arr = (C.c_uint32 * max(1, len(filters)))(*filters)
+        check(lib().rgpu_tree_set_group_filters(self._h, group, arr, len(filters)), "set_group_filters")
+
+    def finalize(self) -> None:
+        check(lib().rgpu_tree_finalize(self._h), "finalize")
+
+    def view(self):
+        """Pointer to the rgpu_tree_view (finalizes first if needed)."""
+        return lib().rgpu_tree_get_view(self._h)
+
+    @property
+    def size(self):
+        v = self.view().contents
+        return v.width, v.height
+
+
+def _rt(transform) -> _abi.ResvgTransform:
+    return _abi.ResvgTransform(*[float(x) for x in transform])
+
+
+def init(device: int = 0) -> None:
+    check(lib().rgpu_init(device), "rgpu_init")
+
+
+def render(tree: Tree, transform=(1, 0, 0, 1, 0, 0), width: int | None = None, height: int | None = None,
+           pixmap: np.ndarray | None = None) -> np.ndarray:
+    """resvg_render through the C ABI: draws `tree` onto a host pixmap
+    (premultiplied RGBA8, (h, w, 4); transparent when None) and returns it."""
+    if pixmap is None:
+        w = int(width if width is not None else tree.size[0])
+        h = int(height if height is not None else tree.size[1])
+        pixmap = np.zeros((h, w, 4), dtype=np.uint8)
+    h, w = pixmap.shape[:2]
+    assert pixmap.dtype == np.uint8 and pixmap.flags.c_contiguous and pixmap.shape[2] == 4
+    tree.view()
+    lib().resvg_render(tree.handle, _rt(transform), w, h, pixmap.ctypes.data)
+    err = lib().rgpu_last_error()
+    if err:
+        raise RenderError(err.decode(errors="replace"))
+    return pixmap
+
+
+def render_device(tree: Tree, transform, width: int, height: int, device_ptr: int, stride: int,
+                  stream: int = 0) -> None:
+    """Renders onto a device pixmap (e.g. a torch.uint8 CUDA tensor's data_ptr())."""
+    tree.view()
+    check(lib().rgpu_render_device(tree.handle, _rt(transform), width, height, C.c_void_p(device_ptr), stride,
+                                   C.c_void_p(stream)), "rgpu_render_device")
+
+
+def render_batch(trees, transforms, widths, heights, device_ptrs, stream: int = 0) -> None:
+    n = len(trees)
+    for t in trees:
+        t.view()
+    th = (C.c_void_p * n)(*[t.handle for t in trees])
+    ts = (_abi.ResvgTransform * n)(*[_rt(t) for t in transforms])
+    ws = (C.c_uint32 * n)(*widths)
+    hs = (C.c_uint32 * n)(*heights)
+    ps = (C.c_void_p * n)(*device_ptrs)
+    check(lib().rgpu_render_batch(th, ts, n, ws, hs, ps, C.c_void_p(stream)), "rgpu_render_batch")
+
+
+def set_tuning(band_rows: int = 0, pixels_per_thread: int = 0) -> None:
+    """Raster work decomposition; 0 = automatic."""
+    t = _abi.Tuning(band_rows, pixels_per_thread, 0)
+    check(lib().rgpu_set_tuning(C.byref(t)), "rgpu_set_tuning")
+
+
+def get_tuning():
+    t = _abi.Tuning()
+    check(lib().rgpu_get_tuning(C.byref(t)), "rgpu_get_tuning")
+    return t.band_rows, t.pixels_per_thread
+
+
+def stats():
+    s = _abi.Stats()
+    check(lib().rgpu_get_stats(C.byref(s)), "rgpu_get_stats")
+    return {k: getattr(s, k) for k, _ in _abi.Stats._fields_}

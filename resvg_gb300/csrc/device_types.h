@@ -1,0 +1,122 @@
+// Device-side data layout shared by the host flattener and the CUDA kernels.
+//
+// The host walks the render tree the way resvg's render.rs does and emits,
+// per scene:
+//   * DrawRec   — one per filled path (strokes arrive as host-stroked outlines),
+//                 holding the path's geometry range, its full transform into its
+//                 target layer, the layer size (the tiny-skia clip rect) and paint;
+//   * PaintRec  — the resolved paint in the form the raster pipeline consumes;
+//   * LayerRec  — isolated-group layers / clip and mask pixmaps (integer rects);
+//   * Cmd       — the command stream the band VM executes in order.
+// Geometry (verbs, f32 points) is uploaded as-is; the device transforms points,
+// builds fixed-point edges, bins them into row bands and rasterises.
+#pragma once
+#include <stdint.h>
+
+namespace rgpu {
+
+constexpr int kMaxGradStops = 16;   // intervals incl. the two constant ends
+
+struct GradRec {
+    float ts[6];         // device pixel -> unit gradient space (sx, ky, kx, sy, tx, ty)
+    uint32_t flags;      // see GRAD_* below
+    uint32_t spread;     // rgpu_spread
+    uint32_t n;          // number of t_values / factors / biases
+    float fr0, fr1, cdx, cdy;  // two-point conical parameters (unit space)
+    float t[kMaxGradStops];
+    float f[kMaxGradStops][4];
+    float b[kMaxGradStops][4];
+};
+enum : uint32_t {
+    GRAD_TWO_STOP = 1, GRAD_PAD_CLAMP = 2, GRAD_PREMUL = 4, GRAD_RADIAL_SIMPLE = 8, GRAD_RADIAL_CONICAL = 16
+};
+
+struct PaintRec {
+    uint32_t kind;       // 0 solid, 1 gradient
+    uint32_t blend;      // rgpu_blend after tiny-skia's strength reduction
+    uint32_t flags;      // PAINT_* below
+    uint32_t grad;       // index into GradRec when kind == 1
+    uint16_t rgba16[4];  // lowp uniform colour
+    float colorf[4];     // highp uniform colour (premultiplied)
+    uint8_t memset_rgba[4];
+    uint32_t _pad;
+};
+enum : uint32_t { PAINT_LOWP = 1, PAINT_MEMSET = 2, PAINT_SKIP = 4 };
+
+struct DrawRec {
+    // ---- set by the host
+    uint32_t verb_off, verb_cnt, pt_off, pt_cnt;  // geometry ranges
+    float ts[6];
+    int32_t clip_w, clip_h;      // target pixmap size (tiny-skia clip rect)
+    int32_t ox, oy;              // target pixmap origin in the stream's output space
+    uint32_t flags;              // DRAW_* below
+    uint32_t paint;
+    uint32_t seg_base;           // segment slots: [seg_base, seg_base + verb_cnt + 1)
+    uint32_t tpt_base;           // transformed points: [tpt_base, tpt_base + pt_cnt)
+    uint32_t stream;             // stream the draw belongs to
+    // ---- set by the setup kernel
+    int32_t valid;
+    int32_t shift;               // 2: anti-aliased (4x4 supersampling), 0: aliased
+    int32_t contained;           // path inside the clip: edges are not clipped
+    int32_t sect_l, sect_t, sect_r, sect_b;      // pixel rect coverage may land in
+    int32_t start_y, stop_y, right_clip, super_left;  // scan range in (sub)scanline units
+    uint32_t edge_base, edge_count;
+};
+enum : uint32_t { DRAW_EVENODD = 1, DRAW_AA = 2 };
+
+struct SegRec {
+    uint32_t draw;
+    uint32_t kind;   // 0 empty, 1 line, 2 quad, 3 cubic
+    uint32_t p0;     // index of the first point in tpts
+    uint32_t p1;     // line end point index (close lines point back to the move point)
+};
+
+// A fixed-point line edge (SkEdge after curve forward differencing).
+struct EdgeRec {
+    int32_t x;        // 16.16 at first_y
+    int32_t dx;       // 16.16 per (sub)scanline
+    int32_t first_y;  // first (sub)scanline, target pixmap coordinates
+    int32_t hw;       // (last_y - first_y) << 8 | (winding & 0xff)
+};
+
+struct LayerRec {
+    int32_t x, y, w, h;   // in the stream's output space
+};
+
+enum CmdOp : uint32_t {
+    CMD_FILL = 0,         // a = draw
+    CMD_PUSH = 1,         // a = layer, b = init (0 transparent, 1 opaque black, 2 load buffer)
+    CMD_POP_COMPOSITE = 2,// a = popped layer, b = blend, f = opacity
+    CMD_POP_CLIP = 3,     // a = popped layer: mask = 255 - alpha, applied to the new top
+    CMD_POP_MASK = 4,     // a = popped layer, b = 0 luminance / 1 alpha
+    CMD_APPLY_REGION = 5, // a = draw: top *= coverage(draw)
+    CMD_CLEAR = 6,        // top = transparent
+    CMD_END = 7
+};
+
+struct Cmd {
+    uint32_t op, a, b;
+    float f;
+};
+
+// One unit of raster work: a band of output rows [band*band_rows, +band_rows)
+// and the x range [x0, x1) of one stream.
+struct WorkItem {
+    uint32_t stream, band;
+    int32_t x0, x1;
+};
+
+// One stream = one target surface rendered by the band VM.
+struct StreamRec {
+    uint32_t cmd_off, cmd_cnt;
+    uint32_t draw_off, draw_cnt;   // draws referenced by this stream
+    uint32_t layer_off;
+    int32_t out_w, out_h;          // target surface size
+    uint32_t out_stride;           // bytes per row
+    uint64_t out_ptr;              // device pointer of the target surface
+    uint32_t band_rows, nbands;    // band height and count
+    uint32_t bin_off;              // dense (band, draw) counters for this stream
+    uint32_t max_depth;            // layer-stack depth needed
+};
+
+}  // namespace rgpu

@@ -1,0 +1,461 @@
+// Host flattener (see flatten.h).
+//
+// Paint conversion follows resvg's path.rs:118-177 (stop colours with
+// (stop_opacity * opacity).to_u8() alpha) and the tiny-skia shader/blitter
+// set-up it calls (Gradient::new stop normalisation, points_to_unit transforms,
+// RasterPipelineBlitter::new strength reduction of SourceOver to Source for
+// opaque paints and the memset fast path).
+#include "flatten.h"
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+namespace rgpu {
+namespace {
+
+struct ColorF { float r, g, b, a; };
+
+inline uint8_t sat_u8(float v) {
+    if (!(v > 0.0f)) return 0;
+    if (v >= 255.0f) return 255;
+    return (uint8_t)v;
+}
+inline uint16_t sat_u16(float v) {
+    if (!(v > 0.0f)) return 0;
+    if (v >= 65535.0f) return 65535;
+    return (uint16_t)v;
+}
+inline uint8_t to_u8_norm(float v) { return sat_u8(v * 255.0f + 0.5f); }
+inline ColorF rgba8(uint8_t r, uint8_t g, uint8_t b, uint8_t a) { return ColorF{r / 255.0f, g / 255.0f, b / 255.0f, a / 255.0f}; }
+inline int32_t sat_i32(float v) {
+    if (std::isnan(v)) return 0;
+    if (v >= 2147483648.0f) return INT32_MAX;
+    if (v <= -2147483648.0f) return INT32_MIN;
+    return (int32_t)v;
+}
+inline ColorF premul(ColorF c) {
+    if (c.a == 1.0f) return c;
+    auto cl = [](float v) { return std::min(std::max(v, 0.0f), 1.0f); };
+    return ColorF{cl(c.r * c.a), cl(c.g * c.a), cl(c.b * c.a), c.a};
+}
+
+struct Stop { float pos; ColorF c; };
+
+enum ShKind { SH_NONE, SH_SOLID, SH_LINEAR, SH_RADIAL };
+struct Shader {
+    ShKind kind = SH_NONE;
+    ColorF color{0, 0, 0, 1};
+    std::vector<Stop> stops;
+    uint32_t spread = 0;
+    Xf ts;
+    float x0 = 0, y0 = 0, x1 = 0, y1 = 0, r0 = 0, r1 = 0;
+    bool opaque() const {
+        if (kind == SH_SOLID) return color.a == 1.0f;
+        for (auto &s : stops) if (s.c.a != 1.0f) return false;
+        return true;
+    }
+};
+
+// path.rs:118-177 + LinearGradient::new / RadialGradient::new
+bool make_shader(const rgpu_tree_view &t, int32_t pi, float opacity, Shader &sh) {
+    const rgpu_paint &pp = t.paints[pi];
+    uint8_t a8 = to_u8_norm(opacity);
+    if (pp.kind == RGPU_PAINT_SOLID) { sh.kind = SH_SOLID; sh.color = rgba8(pp.r, pp.g, pp.b, a8); return true; }
+    for (uint32_t i = 0; i < pp.stop_count; i++) {
+        const rgpu_stop &s = t.stops[pp.stop_offset + i];
+        sh.stops.push_back(Stop{s.offset, rgba8(s.r, s.g, s.b, to_u8_norm(s.opacity * opacity))});
+    }
+    if (sh.stops.empty()) return false;
+    if (sh.stops.size() == 1) { sh.kind = SH_SOLID; sh.color = sh.stops[0].c; return true; }
+    Xf gts = Xf::of(pp.transform), inv;
+    if (pp.kind == RGPU_PAINT_LINEAR) {
+        float dx = pp.x2 - pp.x1, dy = pp.y2 - pp.y1;
+        float len = std::sqrt(dx * dx + dy * dy);
+        if (!std::isfinite(len)) return false;
+        if (len <= 1.0f / (1 << 15)) { sh.kind = SH_SOLID; sh.color = sh.stops.back().c; return true; }
+        if (!invert(gts, &inv)) return false;
+        sh.kind = SH_LINEAR;
+        sh.x0 = pp.x1; sh.y0 = pp.y1; sh.x1 = pp.x2; sh.y1 = pp.y2;
+    } else {
+        if (!(pp.r_ > 0)) return false;
+        if (!invert(gts, &inv)) return false;
+        sh.kind = SH_RADIAL;
+        sh.x0 = pp.fx; sh.y0 = pp.fy; sh.r0 = pp.fr;
+        sh.x1 = pp.cx; sh.y1 = pp.cy; sh.r1 = pp.r_;
+    }
+    sh.spread = pp.spread;
+    sh.ts = gts;
+    return true;
+}
+
+// Gradient::new + push_stages, producing the device GradRec.
+bool make_grad(const Shader &sh, GradRec &g) {
+    std::memset(&g, 0, sizeof(g));
+    std::vector<Stop> st = sh.stops;
+    bool dummy_first = st[0].pos != 0.0f, dummy_last = st.back().pos != 1.0f;
+    if (dummy_first) st.insert(st.begin(), Stop{0.0f, st[0].c});
+    if (dummy_last) st.push_back(Stop{1.0f, st.back().c});
+    bool opaque = true;
+    for (auto &s : st) if (s.c.a != 1.0f) opaque = false;
+    size_t start = dummy_first ? 0 : 1;
+    float prev = 0.0f;
+    bool uniform = true;
+    float step = st[start].pos - prev;
+    for (size_t i = start; i < st.size(); i++) {
+        float curr;
+        if (i + 1 == st.size()) curr = 1.0f;
+        else { float v = st[i].pos; curr = v > 1.0f ? 1.0f : (v >= prev ? v : prev); }
+        uniform = uniform && std::fabs(step - (curr - prev)) <= 1.0f / 4096.0f;
+        st[i].pos = std::min(std::max(curr, 0.0f), 1.0f);
+        prev = curr;
+    }
+    g.flags = 0;
+    if (!opaque) g.flags |= GRAD_PREMUL;
+    if (sh.spread == RGPU_SPREAD_PAD && uniform) g.flags |= GRAD_PAD_CLAMP;
+    g.spread = sh.spread;
+    if (st.size() == 2) {
+        g.flags |= GRAD_TWO_STOP;
+        ColorF c0 = st[0].c, c1 = st[1].c;
+        g.n = 1;
+        g.t[0] = 0;
+        g.f[0][0] = c1.r - c0.r; g.f[0][1] = c1.g - c0.g; g.f[0][2] = c1.b - c0.b; g.f[0][3] = c1.a - c0.a;
+        g.b[0][0] = c0.r; g.b[0][1] = c0.g; g.b[0][2] = c0.b; g.b[0][3] = c0.a;
+    } else {
+        auto eq = [](ColorF a, ColorF b) { return a.r == b.r && a.g == b.g && a.b == b.b && a.a == b.a; };
+        size_t first = eq(st[0].c, st[1].c) ? 1 : 0;
+        size_t last = eq(st.back().c, st[st.size() - 2].c) ? st.size() - 2 : st.size() - 1;
+        uint32_t n = 0;
+        auto push = [&](const float f[4], const float b[4], float t) {
+            if (n >= (uint32_t)kMaxGradStops) return;
+            for (int k = 0; k < 4; k++) { g.f[n][k] = f[k]; g.b[n][k] = b[k]; }
+            g.t[n] = t;
+            n++;
+        };
+        float tl = st[first].pos;
+        ColorF cl = st[first].c;
+        float zero[4] = {0, 0, 0, 0};
+        { float b[4] = {cl.r, cl.g, cl.b, cl.a}; push(zero, b, 0.0f); }
+        for (size_t i = first; i < last; i++) {
+            float tr = st[i + 1].pos;
+            ColorF cr = st[i + 1].c;
+            if (tl < tr) {
+                float d = tr - tl;
+                float f[4] = {(cr.r - cl.r) / d, (cr.g - cl.g) / d, (cr.b - cl.b) / d, (cr.a - cl.a) / d};
+                float b[4] = {cl.r - f[0] * tl, cl.g - f[1] * tl, cl.b - f[2] * tl, cl.a - f[3] * tl};
+                push(f, b, std::min(std::max(tl, 0.0f), 1.0f));
+            }
+            tl = tr;
+            cl = cr;
+        }
+        { float b[4] = {cl.r, cl.g, cl.b, cl.a}; push(zero, b, std::min(std::max(tl, 0.0f), 1.0f)); }
+        g.n = n;
+    }
+    // device pixel -> unit space
+    Xf inv;
+    if (!invert(sh.ts, &inv)) return false;
+    Xf unit;
+    if (sh.kind == SH_LINEAR) {
+        float vx = sh.x1 - sh.x0, vy = sh.y1 - sh.y0;
+        float mag = std::sqrt(vx * vx + vy * vy);
+        float invm = mag != 0.0f ? 1.0f / mag : 0.0f;
+        vx *= invm; vy *= invm;
+        float sn = -vy, cs = vx, ci = 1.0f - cs;
+        unit = Xf::row(cs, sn, -sn, cs, sn * sh.y0 + ci * sh.x0, -sn * sh.x0 + ci * sh.y0);
+        unit = post_concat(unit, Xf::translate(-sh.x0, -sh.y0));
+        unit = post_concat(unit, Xf::scale(invm, invm));
+    } else {
+        float ir = 1.0f / sh.r1;
+        unit = post_concat(Xf::translate(-sh.x0, -sh.y0), Xf::scale(ir, ir));
+        if (sh.x0 == sh.x1 && sh.y0 == sh.y1 && sh.r0 == 0.0f) {
+            g.flags |= GRAD_RADIAL_SIMPLE;
+        } else {
+            g.flags |= GRAD_RADIAL_CONICAL;
+            g.fr0 = sh.r0 * ir;
+            g.fr1 = 1.0f;
+            g.cdx = (sh.x1 - sh.x0) * ir;
+            g.cdy = (sh.y1 - sh.y0) * ir;
+        }
+    }
+    Xf full = post_concat(inv, unit);
+    g.ts[0] = full.sx; g.ts[1] = full.ky; g.ts[2] = full.kx; g.ts[3] = full.sy; g.ts[4] = full.tx; g.ts[5] = full.ty;
+    return true;
+}
+
+struct Target {
+    int32_t w, h;    // pixmap size
+    int32_t ox, oy;  // origin in the stream's output space
+};
+
+struct Flattener {
+    SceneBuild &sb;
+    Tree &tree;
+    const rgpu_tree_view &t;
+    uint32_t stream;
+    uint32_t tree_verb_base, tree_pt_base;
+    int32_t max_x, max_y, max_w, max_h;  // max_filter_bbox
+    uint32_t depth = 0, max_depth = 0;
+    bool unsupported = false;
+
+    uint32_t add_paint(const PaintRec &p) { sb.paints.push_back(p); return (uint32_t)sb.paints.size() - 1; }
+
+    // RasterPipelineBlitter::new for the paint; false when nothing is drawn.
+    bool paint_rec(const Shader &sh0, uint32_t blend, bool aa, const Xf &ts, PaintRec &pr) {
+        std::memset(&pr, 0, sizeof(pr));
+        Shader sh = sh0;
+        if (sh.kind == SH_LINEAR || sh.kind == SH_RADIAL) sh.ts = post_concat(sh.ts, ts);
+        bool opaque = sh.opaque();
+        if (blend == RGPU_BLEND_DESTINATION) return false;
+        if (blend == RGPU_BLEND_DESTINATION_IN && opaque && sh.kind == SH_SOLID) return false;
+        if (opaque && blend == RGPU_BLEND_SOURCE_OVER) blend = RGPU_BLEND_SOURCE;
+        bool memset_ok = false;
+        if (sh.kind == SH_SOLID) {
+            pr.kind = 0;
+            ColorF c = premul(sh.color);
+            float cf[4] = {c.r, c.g, c.b, c.a};
+            for (int i = 0; i < 4; i++) {
+                pr.colorf[i] = cf[i];
+                pr.rgba16[i] = sat_u16(cf[i] * 255.0f + 0.5f);
+                pr.memset_rgba[i] = sat_u8(cf[i] * 255.0f + 0.5f);
+            }
+            if (blend == RGPU_BLEND_SOURCE) memset_ok = true;
+        } else {
+            GradRec g;
+            if (!make_grad(sh, g)) return false;
+            sb.grads.push_back(g);
+            pr.kind = 1;
+            pr.grad = (uint32_t)sb.grads.size() - 1;
+        }
+        if (blend == RGPU_BLEND_CLEAR && !aa) {
+            blend = RGPU_BLEND_SOURCE;
+            memset_ok = true;
+            std::memset(pr.memset_rgba, 0, 4);
+        }
+        bool lowp = sh.kind == SH_SOLID &&
+                    (blend == RGPU_BLEND_SOURCE || blend == RGPU_BLEND_SOURCE_OVER || blend == RGPU_BLEND_CLEAR ||
+                     blend == RGPU_BLEND_DESTINATION_OUT || blend == RGPU_BLEND_XOR || blend == RGPU_BLEND_SOURCE_ATOP ||
+                     blend == RGPU_BLEND_PLUS || blend == RGPU_BLEND_MODULATE || blend == RGPU_BLEND_SCREEN);
+        pr.blend = blend;
+        pr.flags = (lowp ? PAINT_LOWP : 0) | (memset_ok ? PAINT_MEMSET : 0);
+        return true;
+    }
+
+    void emit_draw(uint32_t op, uint32_t verb_off, uint32_t verb_cnt, uint32_t pt_off, uint32_t pt_cnt, const Xf &ts,
+                   const Target &tg, uint32_t rule, bool aa, uint32_t paint) {
+        DrawRec d;
+        std::memset(&d, 0, sizeof(d));
+        d.verb_off = verb_off; d.verb_cnt = verb_cnt; d.pt_off = pt_off; d.pt_cnt = pt_cnt;
+        d.ts[0] = ts.sx; d.ts[1] = ts.ky; d.ts[2] = ts.kx; d.ts[3] = ts.sy; d.ts[4] = ts.tx; d.ts[5] = ts.ty;
+        d.clip_w = tg.w; d.clip_h = tg.h;
+        d.ox = tg.ox; d.oy = tg.oy;
+        d.flags = (rule == RGPU_EVENODD ? DRAW_EVENODD : 0) | (aa ? DRAW_AA : 0);
+        d.paint = paint;
+        d.seg_base = (uint32_t)sb.nsegs;
+        d.tpt_base = (uint32_t)sb.ntpts;
+        d.stream = stream;
+        sb.nsegs += verb_cnt + 1;
+        sb.ntpts += pt_cnt;
+        sb.draws.push_back(d);
+        sb.cmds.push_back(Cmd{op, (uint32_t)sb.draws.size() - 1, 0, 0.0f});
+    }
+
+    bool path_bounds_empty(const rgpu_path &p) {
+        if (p.point_count == 0) return true;
+        const float *pts = t.points + 2 * (size_t)p.point_offset;
+        float l = pts[0], r = pts[0], tp = pts[1], b = pts[1];
+        for (uint32_t i = 1; i < p.point_count; i++) {
+            l = std::min(l, pts[2 * i]); r = std::max(r, pts[2 * i]);
+            tp = std::min(tp, pts[2 * i + 1]); b = std::max(b, pts[2 * i + 1]);
+        }
+        return r - l == 0.0f || b - tp == 0.0f;
+    }
+
+    // path.rs:26-75
+    void fill_path(const rgpu_path &p, uint32_t blend, const Xf &ts, const Target &tg) {
+        if (p.fill_paint < 0) return;
+        if (path_bounds_empty(p)) return;
+        Shader sh;
+        if (!make_shader(t, p.fill_paint, p.fill_opacity, sh)) return;
+        PaintRec pr;
+        if (!paint_rec(sh, blend, p.anti_alias != 0, ts, pr)) return;
+        emit_draw(CMD_FILL, tree_verb_base + p.verb_offset, p.verb_count, tree_pt_base + p.point_offset, p.point_count,
+                  ts, tg, p.fill_rule, p.anti_alias != 0, add_paint(pr));
+    }
+    // path.rs:77-116 (outline from the host stroker, filled non-zero)
+    void stroke_path(uint32_t pi, uint32_t blend, const Xf &ts, const Target &tg) {
+        const rgpu_path &p = t.paths[pi];
+        if (p.stroke_paint < 0) return;
+        Shader sh;
+        if (!make_shader(t, p.stroke_paint, p.stroke_opacity, sh)) return;
+        float rs = resolution_scale(ts.sx, ts.ky, ts.kx, ts.sy);
+        auto outline = tree.stroke_outline(pi, rs);
+        if (!outline || outline->verbs.empty()) return;
+        PaintRec pr;
+        if (!paint_rec(sh, blend, p.anti_alias != 0, ts, pr)) return;
+        uint32_t vo = (uint32_t)sb.verbs.size(), po = (uint32_t)(sb.pts.size() / 2);
+        sb.verbs.insert(sb.verbs.end(), outline->verbs.begin(), outline->verbs.end());
+        sb.pts.insert(sb.pts.end(), outline->pts.begin(), outline->pts.end());
+        emit_draw(CMD_FILL, vo, (uint32_t)outline->verbs.size(), po, (uint32_t)(outline->pts.size() / 2), ts, tg,
+                  RGPU_NONZERO, p.anti_alias != 0, add_paint(pr));
+    }
+    void render_path(uint32_t pi, const Xf &ts, const Target &tg) {
+        const rgpu_path &p = t.paths[pi];
+        if (!p.visible) return;
+        if (!p.stroke_first) {
+            fill_path(p, RGPU_BLEND_SOURCE_OVER, ts, tg);
+            stroke_path(pi, RGPU_BLEND_SOURCE_OVER, ts, tg);
+        } else {
+            stroke_path(pi, RGPU_BLEND_SOURCE_OVER, ts, tg);
+            fill_path(p, RGPU_BLEND_SOURCE_OVER, ts, tg);
+        }
+    }
+    uint32_t push_layer(const Target &tg, uint32_t init) {
+        sb.layers.push_back(LayerRec{tg.ox, tg.oy, tg.w, tg.h});
+        uint32_t li = (uint32_t)(sb.layers.size() - 1 - sb.streams.back().layer_off);
+        sb.cmds.push_back(Cmd{CMD_PUSH, li, init, 0.0f});
+        depth++;
+        max_depth = std::max(max_depth, depth);
+        return li;
+    }
+    void pop(uint32_t op, uint32_t li, uint32_t b, float f) {
+        sb.cmds.push_back(Cmd{op, li, b, f});
+        depth--;
+    }
+    // clip.rs:30-68
+    void draw_children(uint32_t gi, uint32_t mode, const Xf &ts, const Target &tg) {
+        const rgpu_group &g = t.groups[gi];
+        for (uint32_t k = 0; k < g.child_count; k++) {
+            const rgpu_node &n = t.children[g.child_offset + k];
+            if (n.kind == RGPU_NODE_PATH) {
+                const rgpu_path &p = t.paths[n.index];
+                if (!p.visible) continue;
+                fill_path(p, mode, ts, tg);
+            } else {
+                const rgpu_group &cg = t.groups[n.index];
+                Xf t2 = pre_concat(ts, Xf::of(cg.transform));
+                if (cg.clip_path >= 0) {
+                    // clip_group (clip.rs:70-98)
+                    uint32_t li = push_layer(tg, 0);
+                    draw_children(n.index, RGPU_BLEND_SOURCE_OVER, t2, tg);
+                    clip_apply(t.clips[cg.clip_path], t2, tg);
+                    pop(CMD_POP_COMPOSITE, li, RGPU_BLEND_XOR, 1.0f);
+                } else {
+                    draw_children(n.index, mode, t2, tg);
+                }
+            }
+        }
+    }
+    // clip.rs:6-28; the nested clip is applied to the layer first, then this
+    // clip's own mask (the same order resvg applies them in).
+    void clip_apply(const rgpu_clip &clip, const Xf &ts, const Target &tg) {
+        if (clip.clip_path >= 0) clip_apply(t.clips[clip.clip_path], ts, tg);
+        uint32_t li = push_layer(tg, 1);
+        draw_children(clip.root, RGPU_BLEND_CLEAR, pre_concat(ts, Xf::of(clip.transform)), tg);
+        pop(CMD_POP_CLIP, li, 0, 0.0f);
+    }
+    // mask.rs:6-46
+    void mask_apply(const rgpu_mask &mask, const Xf &ts, const Target &tg) {
+        if (t.groups[mask.root].child_count == 0) {
+            sb.cmds.push_back(Cmd{CMD_CLEAR, 0, 0, 0.0f});
+            return;
+        }
+        if (mask.mask >= 0) mask_apply(t.masks[mask.mask], ts, tg);
+        uint32_t li = push_layer(tg, 0);
+        render_nodes(mask.root, ts, tg);
+        // region: Mask::fill_path(rect, winding, aa, ts), then apply_mask
+        uint32_t vo = (uint32_t)sb.verbs.size(), po = (uint32_t)(sb.pts.size() / 2);
+        uint8_t v[5] = {RGPU_MOVE, RGPU_LINE, RGPU_LINE, RGPU_LINE, RGPU_CLOSE};
+        sb.verbs.insert(sb.verbs.end(), v, v + 5);
+        float r[8] = {mask.x, mask.y, mask.x + mask.w, mask.y, mask.x + mask.w, mask.y + mask.h, mask.x, mask.y + mask.h};
+        sb.pts.insert(sb.pts.end(), r, r + 8);
+        PaintRec pr;
+        std::memset(&pr, 0, sizeof(pr));
+        pr.flags = PAINT_SKIP;
+        emit_draw(CMD_APPLY_REGION, vo, 5, po, 4, ts, tg, RGPU_NONZERO, true, add_paint(pr));
+        pop(CMD_POP_MASK, li, mask.kind == RGPU_MASK_LUMINANCE ? 0 : 1, 0.0f);
+    }
+    static bool fit(int64_t x, int64_t y, int64_t w, int64_t h, int32_t bx, int32_t by, int32_t bw, int32_t bh,
+                    int32_t out[4]) {
+        int64_t l = std::max<int64_t>(x, bx), tp = std::max<int64_t>(y, by);
+        int64_t r = std::min<int64_t>(x + w, (int64_t)bx + bw), b = std::min<int64_t>(y + h, (int64_t)by + bh);
+        if (r <= l || b <= tp) return false;
+        out[0] = (int32_t)l; out[1] = (int32_t)tp; out[2] = (int32_t)(r - l); out[3] = (int32_t)(b - tp);
+        return true;
+    }
+    // render.rs:49-142
+    void render_group(uint32_t gi, const Xf &ts_in, const Target &tg) {
+        const rgpu_group &g = t.groups[gi];
+        Xf ts = pre_concat(ts_in, Xf::of(g.transform));
+        bool isolate = g.isolate || g.opacity != 1.0f || g.clip_path >= 0 || g.mask >= 0 || g.filter_count > 0 ||
+                       g.blend != RGPU_BLEND_SOURCE_OVER;
+        if (!isolate) { render_nodes(gi, ts, tg); return; }
+        if (!g.has_layer_bbox) return;
+        float bb[4];
+        if (!map_rect(ts, g.layer_x, g.layer_y, g.layer_x + g.layer_w, g.layer_y + g.layer_h, bb)) return;
+        float bw = bb[2] - bb[0], bh = bb[3] - bb[1];
+        int32_t ib[4];
+        if (g.filter_count == 0) {
+            int64_t x = (int64_t)sat_i32(std::floor(bb[0])) - 2, y = (int64_t)sat_i32(std::floor(bb[1])) - 2;
+            int64_t w = (int64_t)(uint32_t)std::max(0.0f, std::ceil(bw)) + 4;
+            int64_t h = (int64_t)(uint32_t)std::max(0.0f, std::ceil(bh)) + 4;
+            if (x < INT32_MIN || y < INT32_MIN || x + w > INT32_MAX || y + h > INT32_MAX) return;
+            if (!fit(x, y, w, h, max_x, max_y, max_w, max_h, ib)) return;
+        } else {
+            int64_t x = sat_i32(std::floor(bb[0])), y = sat_i32(std::floor(bb[1]));
+            int64_t w = (int64_t)std::max(1.0f, std::ceil(bw)), h = (int64_t)std::max(1.0f, std::ceil(bh));
+            if (x + w > INT32_MAX || y + h > INT32_MAX) return;
+            if (!fit(x, y, w, h, max_x, max_y, max_w, max_h, ib)) return;
+            unsupported = true;  // filters run through the filter pass (not in this stream)
+            return;
+        }
+        float dx = bb[0], dy = bb[1];
+        dx -= bb[0] - (float)ib[0];
+        dy -= bb[1] - (float)ib[1];
+        Xf lts = pre_concat(Xf::translate(-dx, -dy), ts);
+        Target lt{ib[2], ib[3], tg.ox + ib[0], tg.oy + ib[1]};
+        uint32_t li = push_layer(lt, 0);
+        render_nodes(gi, lts, lt);
+        if (g.clip_path >= 0) clip_apply(t.clips[g.clip_path], lts, lt);
+        if (g.mask >= 0) mask_apply(t.masks[g.mask], lts, lt);
+        pop(CMD_POP_COMPOSITE, li, g.blend, g.opacity);
+    }
+    void render_nodes(uint32_t gi, const Xf &ts, const Target &tg) {
+        const rgpu_group &g = t.groups[gi];
+        for (uint32_t k = 0; k < g.child_count; k++) {
+            const rgpu_node &n = t.children[g.child_offset + k];
+            if (n.kind == RGPU_NODE_PATH) render_path(n.index, ts, tg);
+            else render_group(n.index, ts, tg);
+        }
+    }
+};
+
+}  // namespace
+
+int SceneBuild::add_tree(Tree &tree, const Xf &ts, int32_t w, int32_t h, uint64_t out_ptr, uint32_t stride) {
+    const rgpu_tree_view &t = *tree.get_view();
+    StreamRec st;
+    std::memset(&st, 0, sizeof(st));
+    st.cmd_off = (uint32_t)cmds.size();
+    st.draw_off = (uint32_t)draws.size();
+    st.layer_off = (uint32_t)layers.size();
+    st.out_w = w; st.out_h = h;
+    st.out_stride = stride;
+    st.out_ptr = out_ptr;
+    streams.push_back(st);
+    Flattener f{*this, tree, t, (uint32_t)streams.size() - 1, (uint32_t)verbs.size(), (uint32_t)(pts.size() / 2)};
+    verbs.insert(verbs.end(), t.verbs, t.verbs + t.verb_count);
+    pts.insert(pts.end(), t.points, t.points + 2 * (size_t)t.point_count);
+    int64_t mx = -2 * (int64_t)w, my = -2 * (int64_t)h, mw = 5 * (int64_t)w, mh = 5 * (int64_t)h;
+    f.max_x = (int32_t)mx; f.max_y = (int32_t)my; f.max_w = (int32_t)mw; f.max_h = (int32_t)mh;
+    if (t.group_count) f.render_nodes(0, ts, Target{w, h, 0, 0});
+    StreamRec &s = streams.back();
+    s.cmd_cnt = (uint32_t)cmds.size() - s.cmd_off;
+    s.draw_cnt = (uint32_t)draws.size() - s.draw_off;
+    s.max_depth = f.max_depth;
+    if (f.unsupported) {
+        error = "filters are not supported by this build of the stream renderer";
+        return -1;
+    }
+    return (int)streams.size() - 1;
+}
+
+}  // namespace rgpu

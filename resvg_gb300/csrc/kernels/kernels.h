@@ -1,0 +1,36 @@
+// Host-side launchers of the CUDA kernels (implemented in the .cu files).
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+#include "../device_types.h"
+#include "rgpu_tree.h"
+
+namespace rgpu {
+
+// edges.cu
+cudaError_t launch_draw_setup(DrawRec *draws, uint32_t ndraws, const uint8_t *verbs, const float *pts, void *tpts,
+                              SegRec *segs, cudaStream_t s);
+cudaError_t launch_edges(bool emit, const SegRec *segs, uint32_t nsegs, const DrawRec *draws, const void *tpts,
+                         uint32_t *counts, const uint32_t *offsets, EdgeRec *edges, uint32_t *edge_draw,
+                         uint32_t edge_cap, cudaStream_t s);
+cudaError_t launch_draw_edges(DrawRec *draws, uint32_t ndraws, const uint32_t *seg_offsets, cudaStream_t s);
+cudaError_t launch_bin(bool scatter, const EdgeRec *edges, const uint32_t *edge_draw, uint32_t nedges,
+                       const DrawRec *draws, const StreamRec *streams, uint32_t *bin_counts,
+                       const uint32_t *bin_offsets, EdgeRec *bins, cudaStream_t s);
+size_t scan_scratch_words(uint64_t n);
+cudaError_t launch_exclusive_scan(const uint32_t *in, uint32_t *out, uint64_t n, uint32_t *scratch, uint32_t *total,
+                                  cudaStream_t s);
+
+// raster.cu
+size_t raster_smem_bytes();
+size_t raster_stack_words_per_cta(int px);
+int raster_threads();
+cudaError_t launch_raster(int px, uint32_t grid, uint32_t stack_depth, const StreamRec *streams, const WorkItem *items, uint32_t nitems,
+                          uint32_t *item_counter, const Cmd *cmds, const DrawRec *draws, const PaintRec *paints,
+                          const GradRec *grads, const LayerRec *layers, const EdgeRec *bins,
+                          const uint32_t *bin_offsets, const uint32_t *bin_counts, uint32_t *stack, int2 *span_ovf,
+                          uint32_t ovf_cap, uint32_t *err, cudaStream_t s);
+int raster_max_blocks_per_sm(int px);
+
+}  // namespace rgpu

@@ -1,0 +1,321 @@
+// Per-pixel raster-pipeline arithmetic on the device: tiny-skia's lowp (u16
+// lanes, div255 = (v+255)>>8) and highp (f32, store = round-to-nearest-even of
+// clamp(v)*255) stage math for the paints and blend modes resvg uses
+// (tiny-skia 0.12.0 pipeline/lowp.rs, pipeline/highp.rs, shaders/gradient.rs).
+// Compiled with --fmad=false so every product and sum rounds separately.
+#pragma once
+#include <stdint.h>
+#include "../device_types.h"
+#include "rgpu_tree.h"
+
+namespace rgpu {
+namespace dev {
+
+__device__ __forceinline__ uint16_t div255(uint32_t v) { return (uint16_t)(((uint16_t)(v + 255u)) >> 8); }
+__device__ __forceinline__ uint16_t u16(uint32_t v) { return (uint16_t)v; }
+__device__ __forceinline__ uint16_t inv16(uint16_t v) { return (uint16_t)(255 - v); }
+
+__device__ __forceinline__ uint8_t unnorm(float v) {
+    v = fmaxf(v, 0.0f);
+    v = fminf(v, 1.0f);
+    return (uint8_t)__float2int_rn(v * 255.0f);
+}
+__device__ __forceinline__ uint16_t sat_u16(float v) {
+    if (!(v > 0.0f)) return 0;
+    if (v >= 65535.0f) return 65535;
+    return (uint16_t)v;
+}
+constexpr float kInv255 = 1.0f / 255.0f;
+
+__device__ __forceinline__ uint32_t pack(uint32_t r, uint32_t g, uint32_t b, uint32_t a) {
+    return (r & 0xff) | ((g & 0xff) << 8) | ((b & 0xff) << 16) | ((a & 0xff) << 24);
+}
+__device__ __forceinline__ uint32_t ch(uint32_t p, int i) { return (p >> (8 * i)) & 0xff; }
+
+__device__ __forceinline__ bool pre_scale(uint32_t blend) {
+    return blend == RGPU_BLEND_DESTINATION || blend == RGPU_BLEND_DESTINATION_OVER || blend == RGPU_BLEND_PLUS ||
+           blend == RGPU_BLEND_DESTINATION_OUT || blend == RGPU_BLEND_SOURCE_ATOP ||
+           blend == RGPU_BLEND_SOURCE_OVER || blend == RGPU_BLEND_XOR;
+}
+
+__device__ __forceinline__ void lowp_blend(uint32_t blend, const uint16_t s[4], const uint16_t d[4], uint16_t o[4]) {
+    uint16_t sa = s[3];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        switch (blend) {
+        case RGPU_BLEND_CLEAR: o[i] = 0; break;
+        case RGPU_BLEND_SOURCE_OVER: o[i] = u16(s[i] + div255(u16(d[i] * inv16(sa)))); break;
+        case RGPU_BLEND_DESTINATION_OUT: o[i] = div255(u16(d[i] * inv16(sa))); break;
+        case RGPU_BLEND_SOURCE_ATOP: o[i] = div255(u16(s[i] * d[3] + d[i] * inv16(sa))); break;
+        case RGPU_BLEND_XOR: o[i] = div255(u16(s[i] * inv16(d[3]) + d[i] * inv16(sa))); break;
+        case RGPU_BLEND_PLUS: o[i] = min((uint16_t)u16(s[i] + d[i]), (uint16_t)255); break;
+        case RGPU_BLEND_MODULATE: o[i] = div255(u16(s[i] * d[i])); break;
+        case RGPU_BLEND_SCREEN: o[i] = u16(s[i] + d[i] - div255(u16(s[i] * d[i]))); break;
+        default: o[i] = s[i]; break;
+        }
+    }
+}
+
+__device__ __forceinline__ float hinv(float v) { return 1.0f - v; }
+
+__device__ __noinline__ void blend_sep(uint32_t mode, const float *s, const float *d, float *o) {
+    float sa = s[3], da = d[3];
+    switch (mode) {
+    case RGPU_BLEND_CLEAR: for (int i = 0; i < 4; i++) o[i] = 0.0f; return;
+    case RGPU_BLEND_SOURCE: for (int i = 0; i < 4; i++) o[i] = s[i]; return;
+    case RGPU_BLEND_DESTINATION: for (int i = 0; i < 4; i++) o[i] = d[i]; return;
+    case RGPU_BLEND_SOURCE_OVER: for (int i = 0; i < 4; i++) o[i] = d[i] * hinv(sa) + s[i]; return;
+    case RGPU_BLEND_DESTINATION_OVER: for (int i = 0; i < 4; i++) o[i] = s[i] * hinv(da) + d[i]; return;
+    case RGPU_BLEND_SOURCE_IN: for (int i = 0; i < 4; i++) o[i] = s[i] * da; return;
+    case RGPU_BLEND_DESTINATION_IN: for (int i = 0; i < 4; i++) o[i] = d[i] * sa; return;
+    case RGPU_BLEND_SOURCE_OUT: for (int i = 0; i < 4; i++) o[i] = s[i] * hinv(da); return;
+    case RGPU_BLEND_DESTINATION_OUT: for (int i = 0; i < 4; i++) o[i] = d[i] * hinv(sa); return;
+    case RGPU_BLEND_SOURCE_ATOP: for (int i = 0; i < 4; i++) o[i] = s[i] * da + d[i] * hinv(sa); return;
+    case RGPU_BLEND_DESTINATION_ATOP: for (int i = 0; i < 4; i++) o[i] = d[i] * sa + s[i] * hinv(da); return;
+    case RGPU_BLEND_XOR: for (int i = 0; i < 4; i++) o[i] = s[i] * hinv(da) + d[i] * hinv(sa); return;
+    case RGPU_BLEND_PLUS: for (int i = 0; i < 4; i++) o[i] = fminf(s[i] + d[i], 1.0f); return;
+    case RGPU_BLEND_MODULATE: for (int i = 0; i < 4; i++) o[i] = s[i] * d[i]; return;
+    case RGPU_BLEND_SCREEN: for (int i = 0; i < 4; i++) o[i] = s[i] + d[i] - s[i] * d[i]; return;
+    case RGPU_BLEND_MULTIPLY:
+        for (int i = 0; i < 4; i++) o[i] = s[i] * hinv(da) + d[i] * hinv(sa) + s[i] * d[i];
+        return;
+    default: break;
+    }
+    if (mode <= RGPU_BLEND_MULTIPLY) {
+        // separable modes with alpha = source-over
+        for (int i = 0; i < 3; i++) {
+            float s_ = s[i], d_ = d[i], x;
+            switch (mode) {
+            case RGPU_BLEND_DARKEN: x = s_ + d_ - fmaxf(s_ * da, d_ * sa); break;
+            case RGPU_BLEND_LIGHTEN: x = s_ + d_ - fminf(s_ * da, d_ * sa); break;
+            case RGPU_BLEND_DIFFERENCE: { float m = fminf(s_ * da, d_ * sa); x = s_ + d_ - (m + m); break; }
+            case RGPU_BLEND_EXCLUSION: { float m = s_ * d_; x = s_ + d_ - (m + m); break; }
+            case RGPU_BLEND_COLOR_BURN:
+                if (d_ == da) x = d_ + s_ * hinv(da);
+                else if (s_ == 0.0f) x = d_ * hinv(sa);
+                else x = sa * (da - fminf(da, (da - d_) * sa * __fdiv_rn(1.0f, s_))) + s_ * hinv(da) + d_ * hinv(sa);
+                break;
+            case RGPU_BLEND_COLOR_DODGE:
+                if (d_ == 0.0f) x = s_ * hinv(da);
+                else if (s_ == sa) x = s_ + d_ * hinv(sa);
+                else x = sa * fminf(da, (d_ * sa) * __fdiv_rn(1.0f, sa - s_)) + s_ * hinv(da) + d_ * hinv(sa);
+                break;
+            case RGPU_BLEND_HARD_LIGHT: {
+                float y = (s_ + s_ <= sa) ? (s_ * d_) + (s_ * d_) : sa * da - 2.0f * ((da - d_) * (sa - s_));
+                x = s_ * hinv(da) + d_ * hinv(sa) + y;
+                break;
+            }
+            case RGPU_BLEND_OVERLAY: {
+                float y = (d_ + d_ <= da) ? (s_ * d_) + (s_ * d_) : sa * da - 2.0f * ((da - d_) * (sa - s_));
+                x = s_ * hinv(da) + d_ * hinv(sa) + y;
+                break;
+            }
+            case RGPU_BLEND_SOFT_LIGHT: {
+                float m = da > 0.0f ? __fdiv_rn(d_, da) : 0.0f;
+                float s2 = s_ + s_;
+                float m4 = (m + m) + (m + m);
+                float dark_src = d_ * (sa + (s2 - sa) * (1.0f - m));
+                float dark_dst = (m4 * m4 + m4) * (m - 1.0f) + 7.0f * m;
+                float lite_dst = __fsqrt_rn(m) - m;
+                float lite_src = d_ * sa + da * (s2 - sa) * ((d_ + d_) + (d_ + d_) <= da ? dark_dst : lite_dst);
+                x = s_ * hinv(da) + d_ * hinv(sa) + (s2 <= sa ? dark_src : lite_src);
+                break;
+            }
+            default: x = s_; break;
+            }
+            o[i] = x;
+        }
+        o[3] = sa + da * hinv(sa);
+        return;
+    }
+    // non-separable modes
+    auto lum = [](float r, float g, float b) { return r * 0.30f + g * 0.59f + b * 0.11f; };
+    auto sat = [](float r, float g, float b) { return fmaxf(fmaxf(r, g), b) - fminf(fminf(r, g), b); };
+    float r, g, b;
+    auto set_sat = [&](float s_) {
+        float mn = fminf(fminf(r, g), b), mx = fmaxf(fmaxf(r, g), b);
+        float st = mx - mn;
+        r = st == 0.0f ? 0.0f : __fdiv_rn((r - mn) * s_, st);
+        g = st == 0.0f ? 0.0f : __fdiv_rn((g - mn) * s_, st);
+        b = st == 0.0f ? 0.0f : __fdiv_rn((b - mn) * s_, st);
+    };
+    auto set_lum = [&](float l) {
+        float diff = l - lum(r, g, b);
+        r += diff; g += diff; b += diff;
+    };
+    auto clip_color = [&](float a) {
+        float mn = fminf(fminf(r, g), b), mx = fmaxf(fmaxf(r, g), b);
+        float l = lum(r, g, b);
+        auto clip = [&](float c) {
+            if (mn < 0.0f && l - mn != 0.0f) c = l + __fdiv_rn((c - l) * l, l - mn);
+            if (mx > a && mx - l != 0.0f) c = l + __fdiv_rn((c - l) * (a - l), mx - l);
+            return fmaxf(c, 0.0f);
+        };
+        r = clip(r); g = clip(g); b = clip(b);
+    };
+    if (mode == RGPU_BLEND_HUE) {
+        r = s[0] * sa; g = s[1] * sa; b = s[2] * sa;
+        set_sat(sat(d[0], d[1], d[2]) * sa);
+        set_lum(lum(d[0], d[1], d[2]) * sa);
+        clip_color(sa * da);
+    } else if (mode == RGPU_BLEND_SATURATION) {
+        r = d[0] * sa; g = d[1] * sa; b = d[2] * sa;
+        set_sat(sat(s[0], s[1], s[2]) * da);
+        set_lum(lum(d[0], d[1], d[2]) * sa);
+        clip_color(sa * da);
+    } else if (mode == RGPU_BLEND_COLOR) {
+        r = s[0] * da; g = s[1] * da; b = s[2] * da;
+        set_lum(lum(d[0], d[1], d[2]) * sa);
+        clip_color(sa * da);
+    } else {
+        r = d[0] * sa; g = d[1] * sa; b = d[2] * sa;
+        set_lum(lum(s[0], s[1], s[2]) * da);
+        clip_color(sa * da);
+    }
+    o[0] = r + d[0] * hinv(sa) + s[0] * hinv(da);
+    o[1] = g + d[1] * hinv(sa) + s[1] * hinv(da);
+    o[2] = b + d[2] * hinv(sa) + s[2] * hinv(da);
+    o[3] = sa + da - sa * da;
+}
+
+// Gradient colour at device pixel (px, py) (premultiplied f32); false when the
+// pixel lies in a two-point-conical region with no circle through it.
+__device__ __forceinline__ bool gradient_eval(const GradRec &g, int32_t px, int32_t py, float *c) {
+    float x = (float)px + 0.5f, y = (float)py + 0.5f;
+    float tx = x * g.ts[0] + y * g.ts[2] + g.ts[4];
+    float ty = x * g.ts[1] + y * g.ts[3] + g.ts[5];
+    float t;
+    if (g.flags & GRAD_RADIAL_SIMPLE) {
+        t = __fsqrt_rn(tx * tx + ty * ty);
+    } else if (g.flags & GRAD_RADIAL_CONICAL) {
+        float dr = g.fr1 - g.fr0;
+        float a = g.cdx * g.cdx + g.cdy * g.cdy - dr * dr;
+        float b = tx * g.cdx + ty * g.cdy + g.fr0 * dr;
+        float cc = tx * tx + ty * ty - g.fr0 * g.fr0;
+        if (a == 0.0f) {
+            if (b == 0.0f) return false;
+            t = __fdiv_rn(cc, 2.0f * b);
+            if (g.fr0 + t * dr < 0.0f) return false;
+        } else {
+            float disc = b * b - a * cc;
+            if (disc < 0.0f) return false;
+            float sq = __fsqrt_rn(disc);
+            float t1 = __fdiv_rn(b + sq, a), t2 = __fdiv_rn(b - sq, a);
+            float hi = fmaxf(t1, t2), lo = fminf(t1, t2);
+            if (g.fr0 + hi * dr >= 0.0f) t = hi;
+            else if (g.fr0 + lo * dr >= 0.0f) t = lo;
+            else return false;
+        }
+    } else {
+        t = tx;
+    }
+    if (g.spread == RGPU_SPREAD_REFLECT) {
+        float u = t - 1.0f;
+        t = fabsf(u - 2.0f * floorf(u * 0.5f) - 1.0f);
+        t = fminf(fmaxf(t, 0.0f), 1.0f);
+    } else if (g.spread == RGPU_SPREAD_REPEAT) {
+        t = t - floorf(t);
+        t = fminf(fmaxf(t, 0.0f), 1.0f);
+    } else if (g.flags & GRAD_PAD_CLAMP) {
+        t = fminf(fmaxf(t, 0.0f), 1.0f);
+    }
+    uint32_t idx = 0;
+    if (!(g.flags & GRAD_TWO_STOP)) {
+        for (uint32_t i = 1; i < g.n; i++)
+            if (t >= g.t[i]) idx++;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) c[k] = t * g.f[idx][k] + g.b[idx][k];
+    if (g.flags & GRAD_PREMUL) { c[0] *= c[3]; c[1] *= c[3]; c[2] *= c[3]; }
+    return true;
+}
+
+// Blits one pixel of a fill with coverage `cov` (1..255) onto `dst`.
+__device__ __forceinline__ uint32_t shade_pixel(const PaintRec &pr, const GradRec *grads, int32_t lx, int32_t ly,
+                                                uint32_t cov, uint32_t dst) {
+    if (cov == 255 && (pr.flags & PAINT_MEMSET))
+        return pack(pr.memset_rgba[0], pr.memset_rgba[1], pr.memset_rgba[2], pr.memset_rgba[3]);
+    uint32_t blend = pr.blend;
+    if (pr.flags & PAINT_LOWP) {
+        uint16_t s[4] = {pr.rgba16[0], pr.rgba16[1], pr.rgba16[2], pr.rgba16[3]};
+        uint16_t d[4] = {(uint16_t)ch(dst, 0), (uint16_t)ch(dst, 1), (uint16_t)ch(dst, 2), (uint16_t)ch(dst, 3)};
+        uint16_t o[4];
+        if (cov == 255) {
+            if (blend == RGPU_BLEND_SOURCE) { for (int i = 0; i < 4; i++) o[i] = s[i]; }
+            else lowp_blend(blend, s, d, o);
+        } else {
+            uint16_t c = sat_u16(((float)cov * kInv255) * 255.0f + 0.5f);
+            if (pre_scale(blend)) {
+                for (int i = 0; i < 4; i++) s[i] = div255(u16(s[i] * c));
+                lowp_blend(blend, s, d, o);
+            } else {
+                uint16_t b[4];
+                lowp_blend(blend, s, d, b);
+                for (int i = 0; i < 4; i++) o[i] = div255(u16(d[i] * inv16(c) + b[i] * c));
+            }
+        }
+        return pack(o[0], o[1], o[2], o[3]);
+    }
+    float s[4];
+    if (pr.kind == 0) {
+        for (int i = 0; i < 4; i++) s[i] = pr.colorf[i];
+    } else {
+        if (!gradient_eval(grads[pr.grad], lx, ly, s)) { s[0] = s[1] = s[2] = s[3] = 0.0f; }
+    }
+    float d[4] = {(float)ch(dst, 0) * kInv255, (float)ch(dst, 1) * kInv255, (float)ch(dst, 2) * kInv255,
+                  (float)ch(dst, 3) * kInv255};
+    float o[4];
+    if (cov == 255) {
+        if (blend == RGPU_BLEND_SOURCE) { for (int i = 0; i < 4; i++) o[i] = s[i]; }
+        else blend_sep(blend, s, d, o);
+    } else {
+        float c = (float)cov * kInv255;
+        if (pre_scale(blend)) {
+            for (int i = 0; i < 4; i++) s[i] = s[i] * c;
+            blend_sep(blend, s, d, o);
+        } else {
+            float b[4];
+            blend_sep(blend, s, d, b);
+            for (int i = 0; i < 4; i++) o[i] = (b[i] - d[i]) * c + d[i];
+        }
+    }
+    return pack(unnorm(o[0]), unnorm(o[1]), unnorm(o[2]), unnorm(o[3]));
+}
+
+// draw_pixmap of one pixel: highp pattern (already at the right pixel),
+// opacity scale, blend, store.
+__device__ __forceinline__ uint32_t composite_pixel(uint32_t src, uint32_t dst, float opacity, uint32_t blend) {
+    if (blend == RGPU_BLEND_DESTINATION) return dst;
+    float s[4] = {(float)ch(src, 0) * kInv255, (float)ch(src, 1) * kInv255, (float)ch(src, 2) * kInv255,
+                  (float)ch(src, 3) * kInv255};
+    if (opacity != 1.0f)
+        for (int i = 0; i < 4; i++) s[i] = s[i] * opacity;
+    float d[4] = {(float)ch(dst, 0) * kInv255, (float)ch(dst, 1) * kInv255, (float)ch(dst, 2) * kInv255,
+                  (float)ch(dst, 3) * kInv255};
+    float o[4];
+    if (blend == RGPU_BLEND_SOURCE) { for (int i = 0; i < 4; i++) o[i] = s[i]; }
+    else blend_sep(blend, s, d, o);
+    return pack(unnorm(o[0]), unnorm(o[1]), unnorm(o[2]), unnorm(o[3]));
+}
+
+// Pixmap::apply_mask (lowp): every channel *= m / 255 via div255.
+__device__ __forceinline__ uint32_t mask_pixel(uint32_t p, uint32_t m) {
+    return pack(div255(ch(p, 0) * m), div255(ch(p, 1) * m), div255(ch(p, 2) * m), div255(ch(p, 3) * m));
+}
+
+// Mask::from_pixmap value for one pixel.
+__device__ __forceinline__ uint32_t mask_value(uint32_t p, bool luminance) {
+    uint32_t a8 = ch(p, 3);
+    if (!luminance) return a8;
+    float r = (float)ch(p, 0) / 255.0f, g = (float)ch(p, 1) / 255.0f, b = (float)ch(p, 2) / 255.0f;
+    float a = (float)a8 / 255.0f;
+    if (a8 != 0) { r = __fdiv_rn(r, a); g = __fdiv_rn(g, a); b = __fdiv_rn(b, a); }
+    float luma = r * 0.2125f + g * 0.7154f + b * 0.0721f;
+    float v = ceilf(fminf(fmaxf((luma * a) * 255.0f, 0.0f), 255.0f));
+    if (!(v > 0.0f)) return 0;
+    if (v >= 255.0f) return 255;
+    return (uint32_t)v;
+}
+
+}  // namespace dev
+}  // namespace rgpu
