@@ -1,0 +1,303 @@
+"""Benchmark of the GB300 rendering backend (one JSON line on stdout).
+
+Workload (default): the 1024x1024 plain-render scene — 2000 gradient fills
+(linear/radial, 2-8 stops, pad/reflect/repeat, affine gradientTransform),
+500 stroked open cubics, 20 nested clip groups and 10 luminance masks — from
+the seeded generator (resvg_gb300/csrc/host/gen.cpp).  One step = one render of
+that scene.
+
+  value  scenes/s of the device path: a prepared scene (records resident in
+         HBM) rendered into a device pixmap; every pipeline kernel runs each
+         step (edge build, binning, band raster), replayed from a CUDA graph.
+         Timed per step with CUDA events; L2 is flushed between steps.
+  e2e    scenes/s through the drop-in C ABI call resvg_render with a host
+         pixmap: host flattening, record + pixmap upload, kernels, pixmap
+         download, all inside the timed region.
+
+With --gpus N under torchrun each rank renders its own scene (replicas; the
+units are independent scenes, no collective on the data path).
+--impl reference times the CPU restatement of resvg's renderer on all host
+cores (resvg itself cannot be built without a Rust toolchain).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CONFIG_DESC = {
+    0: "512x512, 200 solid cubic loops (non-zero/even-odd), source-over",
+    1: "1024x1024, 2000 gradient fills + 500 strokes + 20 nested clips + 10 luminance masks",
+    2: "2048x2048, 500 cubic loops + blur/saturate/morphology/arithmetic filter chain (linearRGB)",
+}
+SEED = 2026
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", type=int, default=1)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--scale", type=float, default=1.0,
+                    help="path-count scale of the workload (1.0 = the full workload; smaller only for profiling)")
+    return ap.parse_args()
+
+
+def dist_setup(n):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world > 1:
+        import torch.distributed as dist
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
+    return rank, world
+
+
+def _smi_index():
+    lr = int(os.environ.get("LOCAL_RANK", "0"))
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+    if vis:
+        ids = [v.strip() for v in vis.split(",") if v.strip()]
+        if lr < len(ids):
+            return ids[lr]
+    return str(lr)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", _smi_index(),
+                                      "--query-gpu=" + self.Q, "--format=csv,noheader,nounits"],
+                                     capture_output=True, text=True, timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([v.strip() for v in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if len(s) > 3 + i and s[3 + i].strip() == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            p = json.load(fh)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic(config):
+    """DRAM bytes per raster launch from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "raster_traffic.json")
+    try:
+        with open(path) as fh:
+            return json.load(fh).get("config%d" % config)
+    except Exception:
+        return None
+
+
+def cpu_baseline(tree, w, h):
+    import oracle
+    t0 = time.perf_counter()
+    oracle.render(tree.view(), (1, 0, 0, 1, 0, 0), w, h)
+    dt = time.perf_counter() - t0
+    return {"value": 1.0 / dt, "unit": "scenes/s", "cores": 1, "kind": "port",
+            "sample": "one full scene rendered single-threaded by the C++ restatement of resvg+tiny-skia "
+                      "(%.1f s)" % dt}
+
+
+def run_reference(args, rank, world):
+    """CPU restatement of resvg's renderer on all host cores."""
+    if rank != 0:
+        return
+    import oracle
+    import resvg_gb300 as R
+    oracle.lib()
+    tree = R.Tree.generate(args.config, seed=SEED, index=0, scale=1.0)
+    w, h = (int(v) for v in tree.size)
+    threads = os.cpu_count() or 1
+    times = []
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        oracle.render_parallel(tree.view(), (1, 0, 0, 1, 0, 0), w, h, threads)
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            times.append(dt)
+    ms = 1e3 * sum(times) / len(times)
+    value = 1e3 / ms
+    line = {"metric": "scenes/s (plain render, config %d)" % args.config, "value": value, "unit": "scenes/s",
+            "impl": "reference", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+            "data": "synthetic (seeded generator)",
+            "config": {"workload": "config%d: %s" % (args.config, CONFIG_DESC.get(args.config, "")),
+                       "mpix_per_scene": w * h / 1e6},
+            "mpix_s": value * w * h / 1e6,
+            "cpu_baseline": {"value": value, "unit": "scenes/s", "cores": threads, "kind": "port",
+                             "sample": "one full scene per step, canvas split into %d row strips rendered on %d "
+                                       "threads by the C++ restatement of resvg+tiny-skia" % (threads, threads)},
+            "e2e": {"value": value, "unit": "scenes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world = dist_setup(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    import torch
+    import resvg_gb300 as R
+    from resvg_gb300 import build as B
+    B.build()
+    R.init(0)
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    torch.cuda.set_device(dev)
+    tree = R.Tree.generate(args.config, seed=SEED, index=rank, scale=args.scale)
+    w, h = (int(v) for v in tree.size)
+    surface = torch.zeros((h, w, 4), dtype=torch.uint8, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
+    sh = stream.cuda_stream
+    scene = R.Scene([tree], [(1, 0, 0, 1, 0, 0)], [w], [h], [surface.data_ptr()])
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)  # > 129 MB L2
+
+    def step():
+        surface.zero_()
+        flush.zero_()
+        s0 = torch.cuda.Event(enable_timing=True)
+        s1 = torch.cuda.Event(enable_timing=True)
+        s0.record(stream)
+        scene.render(sh)
+        s1.record(stream)
+        return s0, s1
+
+    for _ in range(args.warmup):
+        step()
+        scene.check()
+    info = scene.info()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    step_ms = []
+    with ClockSampler() as clk:
+        t_wall0 = time.perf_counter()
+        for _ in range(args.steps):
+            s0, s1 = step()
+            scene.check()
+            step_ms.append(s0.elapsed_time(s1))
+        torch.cuda.synchronize()
+        t_wall = time.perf_counter() - t_wall0
+    # raster-kernel device time for the roofline: un-captured renders with
+    # events around the kernel (same buffers and inputs)
+    scene.set_timing(True)
+    raster_ms = []
+    for _ in range(max(3, args.steps // 4)):
+        step()
+        raster_ms.append(scene.check())
+    scene.set_timing(False)
+    if world > 1:
+        torch.distributed.barrier()
+    ms = sum(step_ms) / len(step_ms)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * 1e3 / ms
+    rms = sum(raster_ms) / len(raster_ms)
+
+    # ---- end to end through the drop-in C ABI (host pixmap)
+    host = np.zeros((h, w, 4), dtype=np.uint8)
+    for _ in range(2):
+        R.render(tree, (1, 0, 0, 1, 0, 0), pixmap=host)
+    e2e_t = [float("nan")]
+    if args.e2e_steps:
+        e2e_t = []
+    for _ in range(args.e2e_steps):
+        host[:] = 0
+        t0 = time.perf_counter()
+        R.render(tree, (1, 0, 0, 1, 0, 0), pixmap=host)
+        e2e_t.append(time.perf_counter() - t0)
+    st = R.stats()
+    e2e_ms = 1e3 * sum(e2e_t) / len(e2e_t)
+
+    # ---- roofline of the raster kernel (algorithmic bytes per launch)
+    out_px = info["output_pixels"]
+    alg_bytes = out_px * 8 + info["binned_edges"] * 16 + info["record_bytes"] + info["layer_pixels"] * 8
+    peak, peak_kind = peaks()
+    achieved = alg_bytes / (rms * 1e-3) / 1e9
+    line = {
+        "metric": "scenes/s (plain render, config %d)" % args.config,
+        "value": value, "unit": "scenes/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+        "data": "synthetic (seeded generator, seed %d)" % SEED,
+        "config": {"workload": "config%d: %s" % (args.config, CONFIG_DESC.get(args.config, "")),
+                   "canvas": [w, h], "draws": info["draws"], "edges": info["edges"],
+                   "binned_edges": info["binned_edges"], "work_items": info["work_items"],
+                   "l2": "flushed between steps (256 MB write)", "graph_replay": True},
+        "mpix_s": value * out_px / 1e6,
+        "raster_ms": rms,
+        "wall_s_timed_region": t_wall,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind,
+                     "traffic": profiled_traffic(args.config),
+                     "kernel": "k_raster (band VM)", "algorithmic_bytes": alg_bytes},
+        "e2e": {"value": 1e3 / e2e_ms, "unit": "scenes/s", "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": int(st["h2d_bytes"]), "d2h_bytes_per_step": int(st["d2h_bytes"])},
+        "gpu_launches": int(info["kernel_launches"]) * args.steps,
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(tree, w, h)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -99,6 +99,30 @@ int rgpu_render_device(const resvg_render_tree *tree, resvg_transform transform,
 int rgpu_render_batch(const resvg_render_tree *const *trees, const resvg_transform *transforms, uint32_t count,
                       const uint32_t *widths, const uint32_t *heights, uint8_t *const *device_pixmaps, void *stream);
 
+/* Prepared scene ("display list"): one or many trees flattened once, with
+ * records and geometry resident in device memory and their own work buffers.
+ * The first render sizes the edge/bin buffers (two stream synchronisations);
+ * later renders are asynchronous and replay a captured CUDA graph.  The
+ * device pixmaps given at prepare time are the render targets.  The batched
+ * form (many trees) uses one persistent raster kernel over all scenes' bands. */
+typedef struct rgpu_scene rgpu_scene;
+int rgpu_scene_prepare(const resvg_render_tree *const *trees, const resvg_transform *transforms, uint32_t count,
+                       const uint32_t *widths, const uint32_t *heights, uint8_t *const *device_pixmaps,
+                       const uint32_t *strides, rgpu_scene **out);
+int rgpu_scene_render(rgpu_scene *scene, void *stream);
+/* Timing mode: renders run un-captured with CUDA events around the raster
+ * kernel so rgpu_scene_check can report its device time (-1 otherwise). */
+int rgpu_scene_set_timing(rgpu_scene *scene, int enabled);
+/* Synchronises the stream of the last render and reports kernel error flags;
+ * raster_ms = raster kernel time of the last render in timing mode, else -1. */
+int rgpu_scene_check(rgpu_scene *scene, float *raster_ms);
+typedef struct rgpu_scene_stats {
+    uint64_t streams, draws, commands, segments, edges, binned_edges, work_items;
+    uint64_t grid, pixels_per_thread, kernel_launches, output_pixels, layer_pixels, record_bytes;
+} rgpu_scene_stats;
+int rgpu_scene_info(const rgpu_scene *scene, rgpu_scene_stats *stats);
+void rgpu_scene_free(rgpu_scene *scene);
+
 /* Tuning knobs of the raster kernels (chosen by the autotuner). */
 typedef struct rgpu_tuning {
     uint32_t band_rows;          /* pixel rows per raster work item: 0 (auto), 1, 2, 4 or 8 */

@@ -35,6 +35,9 @@ def lib() -> C.CDLL:
         L = C.CDLL(LIB_PATH)
         L.oracle_render.restype = C.c_int
         L.oracle_render.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.c_uint32, C.c_uint32, C.c_void_p]
+        L.oracle_render_parallel.restype = C.c_int
+        L.oracle_render_parallel.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.c_uint32, C.c_uint32, C.c_void_p,
+                                             C.c_uint32]
         for n in ("oracle_box_blur", "oracle_iir_blur"):
             getattr(L, n).argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_double, C.c_double]
         L.oracle_morphology.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_int, C.c_float, C.c_float]
@@ -54,6 +57,19 @@ def render(tree_view_ptr, transform, width: int, height: int, pixmap: np.ndarray
     r = lib().oracle_render(C.cast(tree_view_ptr, C.c_void_p), ts, width, height, pixmap.ctypes.data)
     if r != 0:
         raise RuntimeError("oracle_render failed")
+    return pixmap
+
+
+def render_parallel(tree_view_ptr, transform, width: int, height: int, threads: int,
+                    pixmap: np.ndarray | None = None) -> np.ndarray:
+    """All-core timing variant of render(): strips of the canvas on `threads` threads."""
+    if pixmap is None:
+        pixmap = np.zeros((height, width, 4), dtype=np.uint8)
+    ts = (C.c_float * 6)(*[float(v) for v in transform])
+    r = lib().oracle_render_parallel(C.cast(tree_view_ptr, C.c_void_p), ts, width, height, pixmap.ctypes.data,
+                                     threads)
+    if r != 0:
+        raise RuntimeError("oracle_render_parallel failed")
     return pixmap
 
 

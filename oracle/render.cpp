@@ -288,3 +288,33 @@ int oracle_render(const rgpu_tree_view *tree, const float ts6[6], uint32_t w, ui
 }
 
 }
+
+#include <thread>
+extern "C" {
+// Renders with `threads` host threads, each drawing a horizontal strip of the
+// canvas through a translated transform (resvg renders one tree per thread;
+// this is the all-core CPU timing of the same workload).
+int oracle_render_parallel(const rgpu_tree_view *tree, const float ts6[6], uint32_t w, uint32_t h, uint8_t *pixmap,
+                           uint32_t threads) {
+    if (!tree || !pixmap || w == 0 || h == 0) return -1;
+    if (threads == 0) threads = 1;
+    threads = std::min(threads, h);
+    std::vector<std::thread> pool;
+    uint32_t rows = (h + threads - 1) / threads;
+    for (uint32_t k = 0; k < threads; k++) {
+        uint32_t y0 = k * rows;
+        if (y0 >= h) break;
+        uint32_t hh = std::min(rows, h - y0);
+        pool.emplace_back([=]() {
+            ora::Pixmap pm(w, hh);
+            std::memcpy(pm.data.data(), pixmap + (size_t)y0 * w * 4, (size_t)w * hh * 4);
+            ora::Transform ts = ora::Transform::from_row(ts6[0], ts6[1], ts6[2], ts6[3], ts6[4], ts6[5]);
+            ts = ora::Transform::translate(0.0f, -(float)y0).pre_concat(ts);
+            ora::render_tree(*tree, ts, pm);
+            std::memcpy(pixmap + (size_t)y0 * w * 4, pm.data.data(), (size_t)w * hh * 4);
+        });
+    }
+    for (auto &t : pool) t.join();
+    return 0;
+}
+}

@@ -208,3 +208,78 @@ def stats():
     s = _abi.Stats()
     check(lib().rgpu_get_stats(C.byref(s)), "rgpu_get_stats")
     return {k: getattr(s, k) for k, _ in _abi.Stats._fields_}
+
+
+class SceneStats(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in ("streams", "draws", "commands", "segments", "edges", "binned_edges",
+                                           "work_items", "grid", "pixels_per_thread", "kernel_launches",
+                                           "output_pixels", "layer_pixels", "record_bytes")]
+
+
+def _declare_scene(L):
+    P = C.c_void_p
+    L.rgpu_scene_prepare.restype = C.c_int
+    L.rgpu_scene_prepare.argtypes = [C.POINTER(P), C.POINTER(_abi.ResvgTransform), C.c_uint32,
+                                     C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(P),
+                                     C.POINTER(C.c_uint32), C.POINTER(P)]
+    L.rgpu_scene_render.restype = C.c_int
+    L.rgpu_scene_render.argtypes = [P, P]
+    L.rgpu_scene_set_timing.restype = C.c_int
+    L.rgpu_scene_set_timing.argtypes = [P, C.c_int]
+    L.rgpu_scene_check.restype = C.c_int
+    L.rgpu_scene_check.argtypes = [P, C.POINTER(C.c_float)]
+    L.rgpu_scene_info.restype = C.c_int
+    L.rgpu_scene_info.argtypes = [P, C.POINTER(SceneStats)]
+    L.rgpu_scene_free.restype = None
+    L.rgpu_scene_free.argtypes = [P]
+
+
+class Scene:
+    """A prepared scene (device-resident display list) over one or many trees.
+
+    `device_ptrs` are the device pixmaps rendered into (premultiplied RGBA8,
+    e.g. torch uint8 CUDA tensors' data_ptr()).  render() enqueues the whole
+    pipeline on `stream` (a cudaStream_t handle; 0 = the library's stream);
+    from the second render on it replays a captured CUDA graph."""
+
+    def __init__(self, trees, transforms, widths, heights, device_ptrs, strides=None):
+        L = lib()
+        if not hasattr(L, "_scene_declared"):
+            _declare_scene(L)
+            L._scene_declared = True
+        n = len(trees)
+        self._trees = list(trees)  # keep alive
+        for t in trees:
+            t.view()
+        th = (C.c_void_p * n)(*[t.handle for t in trees])
+        ts = (_abi.ResvgTransform * n)(*[_rt(t) for t in transforms])
+        ws = (C.c_uint32 * n)(*[int(w) for w in widths])
+        hs = (C.c_uint32 * n)(*[int(h) for h in heights])
+        ps = (C.c_void_p * n)(*[int(p) for p in device_ptrs])
+        ss = (C.c_uint32 * n)(*[int(s) for s in strides]) if strides is not None else None
+        out = C.c_void_p()
+        check(L.rgpu_scene_prepare(th, ts, n, ws, hs, ps, ss, C.byref(out)), "rgpu_scene_prepare")
+        self._h = out
+
+    def render(self, stream: int = 0) -> None:
+        check(lib().rgpu_scene_render(self._h, C.c_void_p(stream)), "rgpu_scene_render")
+
+    def set_timing(self, enabled: bool) -> None:
+        check(lib().rgpu_scene_set_timing(self._h, int(bool(enabled))), "rgpu_scene_set_timing")
+
+    def check(self) -> float:
+        """Synchronises; raises on kernel error flags; returns the raster kernel ms of the last render."""
+        ms = C.c_float(0)
+        check(lib().rgpu_scene_check(self._h, C.byref(ms)), "rgpu_scene_check")
+        return ms.value
+
+    def info(self) -> dict:
+        st = SceneStats()
+        check(lib().rgpu_scene_info(self._h, C.byref(st)), "rgpu_scene_info")
+        return {k: getattr(st, k) for k, _ in SceneStats._fields_}
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            _lib.rgpu_scene_free(h)
+            self._h = None

@@ -73,16 +73,43 @@ struct Tuning {
     uint32_t px = 0;         // pixels per thread: 0 automatic, else 4/8/16
 };
 
+struct Buffers {
+    DevBuf verbs, pts, draws, paints, grads, layers, cmds, streams, items;
+    DevBuf tpts, segs, seg_counts, seg_offsets, scan_scratch, totals;
+    DevBuf edges, edge_draw, bin_counts, bin_offsets, bins;
+    DevBuf stack, span_ovf, err, counter;
+    void release() {
+        DevBuf *all[] = {&verbs, &pts, &draws, &paints, &grads, &layers, &cmds, &streams, &items, &tpts, &segs,
+                         &seg_counts, &seg_offsets, &scan_scratch, &totals, &edges, &edge_draw, &bin_counts,
+                         &bin_offsets, &bins, &stack, &span_ovf, &err, &counter};
+        for (DevBuf *b : all) {
+            if (b->p) cudaFree(b->p);
+            b->p = nullptr;
+            b->cap = 0;
+        }
+    }
+};
+
+// A flattened submission with its work decomposition.
+struct Plan {
+    SceneBuild sb;
+    std::vector<WorkItem> items;
+    uint32_t px = 8;
+    uint64_t nbins = 0;
+    uint32_t max_depth = 1;
+    uint32_t grid = 1;
+    uint32_t nedges = 0, nbinned = 0;  // known after the first (sizing) run
+    bool sized = false;
+};
+
 struct Context {
     std::mutex mu;
     int device = -1;
     int sms = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    DevBuf verbs, pts, draws, paints, grads, layers, cmds, streams, items;
-    DevBuf tpts, segs, seg_counts, seg_offsets, scan_scratch, totals;
-    DevBuf edges, edge_draw, bin_counts, bin_offsets, bins;
-    DevBuf stack, span_ovf, err, counter, surface;
+    Buffers buf;
+    DevBuf surface;
     HostBuf staging;
     Tuning tuning;
 };
@@ -122,6 +149,7 @@ int ensure_device(Context &c) {
     CK(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
     CK(cudaEventCreate(&c.ev0));
     CK(cudaEventCreate(&c.ev1));
+    CK(raster_init());
     c.device = dev;
     return RGPU_OK;
 }
@@ -151,119 +179,141 @@ uint32_t pick_bh(int32_t w, uint32_t px, const Tuning &tu) {
     return bh;
 }
 
-// Runs the device pipeline for a flattened submission on `s`.
-int run_scene(Context &c, SceneBuild &sb, cudaStream_t s) {
-    uint32_t px = pick_px(sb, c.tuning);
-    // work items and bin layout
-    std::vector<WorkItem> items;
-    uint64_t nbins = 0;
-    uint32_t max_depth = 1;
+// Host-side work decomposition of a flattened submission.
+int plan_scene(Context &c, Plan &p) {
+    SceneBuild &sb = p.sb;
+    p.px = pick_px(sb, c.tuning);
+    p.items.clear();
+    p.nbins = 0;
+    p.max_depth = 1;
     for (uint32_t si = 0; si < sb.streams.size(); si++) {
         StreamRec &st = sb.streams[si];
-        uint32_t bh = pick_bh(st.out_w, px, c.tuning);
+        uint32_t bh = pick_bh(st.out_w, p.px, c.tuning);
         st.band_rows = bh;
         st.nbands = (uint32_t)((st.out_h + (int32_t)bh - 1) / (int32_t)bh);
-        st.bin_off = (uint32_t)nbins;
-        nbins += (uint64_t)st.nbands * st.draw_cnt;
-        max_depth = std::max(max_depth, st.max_depth + 1);
-        int32_t cw = (int32_t)((256 / bh) * px);
+        st.bin_off = (uint32_t)p.nbins;
+        p.nbins += (uint64_t)st.nbands * st.draw_cnt;
+        p.max_depth = std::max(p.max_depth, st.max_depth + 1);
+        int32_t cw = (int32_t)((256 / bh) * p.px);
         for (uint32_t b = 0; b < st.nbands; b++)
-            for (int32_t x0 = 0; x0 < st.out_w; x0 += cw) items.push_back(WorkItem{si, b, x0, std::min(x0 + cw, st.out_w)});
+            for (int32_t x0 = 0; x0 < st.out_w; x0 += cw)
+                p.items.push_back(WorkItem{si, b, x0, std::min(x0 + cw, st.out_w)});
     }
-    if (nbins > 0xF0000000ull) { set_error("too many (band, draw) bins"); return RGPU_ERR_CAPACITY; }
-    g_stats.draws += sb.draws.size();
-    g_stats.work_items += items.size();
-    // staging: all record arrays
-    size_t stage = 0;
-    auto rup = [](size_t b) { return (b + 255) & ~(size_t)255; };
-    stage += rup(sb.verbs.size()) + rup(sb.pts.size() * 4) + rup(sb.draws.size() * sizeof(DrawRec)) +
-             rup(sb.paints.size() * sizeof(PaintRec)) + rup(sb.grads.size() * sizeof(GradRec)) +
-             rup(sb.layers.size() * sizeof(LayerRec)) + rup(sb.cmds.size() * sizeof(Cmd)) +
-             rup(sb.streams.size() * sizeof(StreamRec)) + rup(items.size() * sizeof(WorkItem)) + 4096;
-    CK(c.staging.ensure(stage));
-    size_t off = 0;
-    int r;
-    if ((r = upload(c, c.verbs, sb.verbs, off, s))) return r;
-    if ((r = upload(c, c.pts, sb.pts, off, s))) return r;
-    if ((r = upload(c, c.draws, sb.draws, off, s))) return r;
-    if ((r = upload(c, c.paints, sb.paints, off, s))) return r;
-    if ((r = upload(c, c.grads, sb.grads, off, s))) return r;
-    if ((r = upload(c, c.layers, sb.layers, off, s))) return r;
-    if ((r = upload(c, c.cmds, sb.cmds, off, s))) return r;
-    if ((r = upload(c, c.streams, sb.streams, off, s))) return r;
-    if ((r = upload(c, c.items, items, off, s))) return r;
-    uint32_t ndraws = (uint32_t)sb.draws.size();
-    uint64_t nsegs = sb.nsegs;
-    CK(c.tpts.ensure(std::max<uint64_t>(sb.ntpts, 1) * 8));
-    CK(c.segs.ensure(std::max<uint64_t>(nsegs, 1) * sizeof(SegRec)));
-    CK(c.seg_counts.ensure((nsegs + 1) * 4));
-    CK(c.seg_offsets.ensure((nsegs + 1) * 4));
-    CK(c.totals.ensure(64));
-    CK(c.scan_scratch.ensure(scan_scratch_words(std::max<uint64_t>(nsegs + 1, nbins + 1)) * 4));
-    uint32_t *totals = c.totals.as<uint32_t>();
-    CK(launch_draw_setup(c.draws.as<DrawRec>(), ndraws, c.verbs.as<uint8_t>(), c.pts.as<float>(), c.tpts.p,
-                         c.segs.as<SegRec>(), s));
-    CK(cudaMemsetAsync(c.seg_counts.p, 0, (nsegs + 1) * 4, s));
-    CK(launch_edges(false, c.segs.as<SegRec>(), (uint32_t)nsegs, c.draws.as<DrawRec>(), c.tpts.p,
-                    c.seg_counts.as<uint32_t>(), nullptr, nullptr, nullptr, 0, s));
-    CK(launch_exclusive_scan(c.seg_counts.as<uint32_t>(), c.seg_offsets.as<uint32_t>(), nsegs + 1,
-                             c.scan_scratch.as<uint32_t>(), totals, s));
-    uint32_t host_tot[2] = {0, 0};
-    CK(cudaMemcpyAsync(host_tot, totals, 4, cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    uint32_t nedges = host_tot[0];
-    g_stats.edges += nedges;
-    CK(c.edges.ensure(std::max<uint32_t>(nedges, 1) * sizeof(EdgeRec)));
-    CK(c.edge_draw.ensure(std::max<uint32_t>(nedges, 1) * 4));
-    CK(launch_edges(true, c.segs.as<SegRec>(), (uint32_t)nsegs, c.draws.as<DrawRec>(), c.tpts.p,
-                    c.seg_counts.as<uint32_t>(), c.seg_offsets.as<uint32_t>(), c.edges.as<EdgeRec>(),
-                    c.edge_draw.as<uint32_t>(), nedges, s));
-    CK(launch_draw_edges(c.draws.as<DrawRec>(), ndraws, c.seg_offsets.as<uint32_t>(), s));
-    // bins
-    CK(c.bin_counts.ensure((nbins + 1) * 4));
-    CK(c.bin_offsets.ensure((nbins + 1) * 4));
-    CK(cudaMemsetAsync(c.bin_counts.p, 0, (nbins + 1) * 4, s));
-    CK(launch_bin(false, c.edges.as<EdgeRec>(), c.edge_draw.as<uint32_t>(), nedges, c.draws.as<DrawRec>(),
-                  c.streams.as<StreamRec>(), c.bin_counts.as<uint32_t>(), nullptr, nullptr, s));
-    CK(launch_exclusive_scan(c.bin_counts.as<uint32_t>(), c.bin_offsets.as<uint32_t>(), nbins + 1,
-                             c.scan_scratch.as<uint32_t>(), totals + 1, s));
-    CK(cudaMemcpyAsync(host_tot + 1, totals + 1, 4, cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    uint32_t nbinned = host_tot[1];
-    CK(c.bins.ensure(std::max<uint32_t>(nbinned, 1) * sizeof(EdgeRec)));
-    CK(cudaMemsetAsync(c.bin_counts.p, 0, (nbins + 1) * 4, s));
-    CK(launch_bin(true, c.edges.as<EdgeRec>(), c.edge_draw.as<uint32_t>(), nedges, c.draws.as<DrawRec>(),
-                  c.streams.as<StreamRec>(), c.bin_counts.as<uint32_t>(), c.bin_offsets.as<uint32_t>(),
-                  c.bins.as<EdgeRec>(), s));
-    // raster
-    uint32_t per_sm = (uint32_t)raster_max_blocks_per_sm((int)px);
-    uint32_t grid = std::min<uint32_t>((uint32_t)items.size(), (uint32_t)c.sms * per_sm);
-    if (grid == 0) grid = 1;
-    const uint32_t ovf_cap = 64;
-    size_t stack_words = (size_t)max_depth * raster_threads() * px;
-    CK(c.stack.ensure((size_t)grid * stack_words * 4));
-    CK(c.span_ovf.ensure((size_t)grid * raster_threads() * ovf_cap * 8));
-    CK(c.err.ensure(16));
-    CK(c.counter.ensure(16));
-    CK(cudaMemsetAsync(c.err.p, 0, 4, s));
-    CK(cudaMemsetAsync(c.counter.p, 0, 4, s));
-    CK(cudaEventRecord(c.ev0, s));
-    CK(launch_raster((int)px, grid, max_depth, c.streams.as<StreamRec>(), c.items.as<WorkItem>(),
-                     (uint32_t)items.size(), c.counter.as<uint32_t>(), c.cmds.as<Cmd>(), c.draws.as<DrawRec>(),
-                     c.paints.as<PaintRec>(), c.grads.as<GradRec>(), c.layers.as<LayerRec>(), c.bins.as<EdgeRec>(),
-                     c.bin_offsets.as<uint32_t>(), c.bin_counts.as<uint32_t>(), c.stack.as<uint32_t>(),
-                     c.span_ovf.as<int2>(), ovf_cap, c.err.as<uint32_t>(), s));
-    CK(cudaEventRecord(c.ev1, s));
-    g_stats.kernel_launches += 12;
+    if (p.nbins > 0xF0000000ull) { set_error("too many (band, draw) bins"); return RGPU_ERR_CAPACITY; }
+    uint32_t per_sm = (uint32_t)raster_max_blocks_per_sm((int)p.px);
+    p.grid = std::max<uint32_t>(1, std::min<uint32_t>((uint32_t)p.items.size(), (uint32_t)c.sms * per_sm));
     return RGPU_OK;
 }
 
-int check_err(Context &c, cudaStream_t s) {
+int upload_plan(Context &c, Buffers &b, Plan &p, cudaStream_t s) {
+    SceneBuild &sb = p.sb;
+    auto rup = [](size_t n) { return (n + 255) & ~(size_t)255; };
+    size_t stage = rup(sb.verbs.size()) + rup(sb.pts.size() * 4) + rup(sb.draws.size() * sizeof(DrawRec)) +
+                   rup(sb.paints.size() * sizeof(PaintRec)) + rup(sb.grads.size() * sizeof(GradRec)) +
+                   rup(sb.layers.size() * sizeof(LayerRec)) + rup(sb.cmds.size() * sizeof(Cmd)) +
+                   rup(sb.streams.size() * sizeof(StreamRec)) + rup(p.items.size() * sizeof(WorkItem)) + 4096;
+    CK(c.staging.ensure(stage));
+    size_t off = 0;
+    int r;
+    if ((r = upload(c, b.verbs, sb.verbs, off, s))) return r;
+    if ((r = upload(c, b.pts, sb.pts, off, s))) return r;
+    if ((r = upload(c, b.draws, sb.draws, off, s))) return r;
+    if ((r = upload(c, b.paints, sb.paints, off, s))) return r;
+    if ((r = upload(c, b.grads, sb.grads, off, s))) return r;
+    if ((r = upload(c, b.layers, sb.layers, off, s))) return r;
+    if ((r = upload(c, b.cmds, sb.cmds, off, s))) return r;
+    if ((r = upload(c, b.streams, sb.streams, off, s))) return r;
+    if ((r = upload(c, b.items, p.items, off, s))) return r;
+    // fixed-size work buffers
+    uint64_t nsegs = sb.nsegs;
+    CK(b.tpts.ensure(std::max<uint64_t>(sb.ntpts, 1) * 8));
+    CK(b.segs.ensure(std::max<uint64_t>(nsegs, 1) * sizeof(SegRec)));
+    CK(b.seg_counts.ensure((nsegs + 1) * 4));
+    CK(b.seg_offsets.ensure((nsegs + 1) * 4));
+    CK(b.totals.ensure(64));
+    CK(b.scan_scratch.ensure(scan_scratch_words(std::max<uint64_t>(nsegs + 1, p.nbins + 1)) * 4));
+    CK(b.bin_counts.ensure((p.nbins + 1) * 4));
+    CK(b.bin_offsets.ensure((p.nbins + 1) * 4));
+    const uint32_t ovf_cap = 64;
+    size_t stack_words = (size_t)p.max_depth * raster_threads() * p.px;
+    CK(b.stack.ensure((size_t)p.grid * stack_words * 4));
+    CK(b.span_ovf.ensure((size_t)p.grid * raster_threads() * ovf_cap * 8));
+    CK(b.err.ensure(16));
+    CK(b.counter.ensure(16));
+    return RGPU_OK;
+}
+
+// Enqueues the device pipeline.  Without known sizes it synchronises twice to
+// read the edge and bin totals; with known sizes (a prepared scene rendered
+// before) it is fully asynchronous and capturable into a CUDA graph.
+int enqueue_plan(Context &c, Buffers &b, Plan &p, cudaStream_t s, cudaEvent_t ev0, cudaEvent_t ev1) {
+    SceneBuild &sb = p.sb;
+    uint32_t ndraws = (uint32_t)sb.draws.size();
+    uint64_t nsegs = sb.nsegs;
+    uint32_t *totals = b.totals.as<uint32_t>();
+    CK(launch_draw_setup(b.draws.as<DrawRec>(), ndraws, b.verbs.as<uint8_t>(), b.pts.as<float>(), b.tpts.p,
+                         b.segs.as<SegRec>(), s));
+    CK(cudaMemsetAsync(b.seg_counts.p, 0, (nsegs + 1) * 4, s));
+    CK(launch_edges(false, b.segs.as<SegRec>(), (uint32_t)nsegs, b.draws.as<DrawRec>(), b.tpts.p,
+                    b.seg_counts.as<uint32_t>(), nullptr, nullptr, nullptr, 0, s));
+    CK(launch_exclusive_scan(b.seg_counts.as<uint32_t>(), b.seg_offsets.as<uint32_t>(), nsegs + 1,
+                             b.scan_scratch.as<uint32_t>(), totals, s));
+    if (!p.sized) {
+        uint32_t tot = 0;
+        CK(cudaMemcpyAsync(&tot, totals, 4, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        p.nedges = tot;
+        CK(b.edges.ensure(std::max<uint32_t>(tot, 1) * sizeof(EdgeRec)));
+        CK(b.edge_draw.ensure(std::max<uint32_t>(tot, 1) * 4));
+    }
+    uint32_t nedges = p.nedges;
+    g_stats.edges += nedges;
+    CK(launch_edges(true, b.segs.as<SegRec>(), (uint32_t)nsegs, b.draws.as<DrawRec>(), b.tpts.p,
+                    b.seg_counts.as<uint32_t>(), b.seg_offsets.as<uint32_t>(), b.edges.as<EdgeRec>(),
+                    b.edge_draw.as<uint32_t>(), nedges, s));
+    CK(launch_draw_edges(b.draws.as<DrawRec>(), ndraws, b.seg_offsets.as<uint32_t>(), s));
+    CK(cudaMemsetAsync(b.bin_counts.p, 0, (p.nbins + 1) * 4, s));
+    CK(launch_bin(false, b.edges.as<EdgeRec>(), b.edge_draw.as<uint32_t>(), nedges, b.draws.as<DrawRec>(),
+                  b.streams.as<StreamRec>(), b.bin_counts.as<uint32_t>(), nullptr, 0, nullptr, nullptr, s));
+    CK(launch_exclusive_scan(b.bin_counts.as<uint32_t>(), b.bin_offsets.as<uint32_t>(), p.nbins + 1,
+                             b.scan_scratch.as<uint32_t>(), totals + 1, s));
+    if (!p.sized) {
+        uint32_t tot = 0;
+        CK(cudaMemcpyAsync(&tot, totals + 1, 4, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        p.nbinned = tot;
+        CK(b.bins.ensure(std::max<uint32_t>(tot, 1) * sizeof(EdgeRec)));
+        p.sized = true;
+    }
+    CK(cudaMemsetAsync(b.bin_counts.p, 0, (p.nbins + 1) * 4, s));
+    CK(cudaMemsetAsync(b.err.p, 0, 4, s));
+    CK(launch_bin(true, b.edges.as<EdgeRec>(), b.edge_draw.as<uint32_t>(), nedges, b.draws.as<DrawRec>(),
+                  b.streams.as<StreamRec>(), b.bin_counts.as<uint32_t>(), b.bin_offsets.as<uint32_t>(), p.nbinned,
+                  b.err.as<uint32_t>(), b.bins.as<EdgeRec>(), s));
+    CK(cudaMemsetAsync(b.counter.p, 0, 4, s));
+    const uint32_t ovf_cap = 64;
+    if (ev0) CK(cudaEventRecord(ev0, s));
+    CK(launch_raster((int)p.px, p.grid, p.max_depth, b.streams.as<StreamRec>(), b.items.as<WorkItem>(),
+                     (uint32_t)p.items.size(), b.counter.as<uint32_t>(), b.cmds.as<Cmd>(), b.draws.as<DrawRec>(),
+                     b.paints.as<PaintRec>(), b.grads.as<GradRec>(), b.layers.as<LayerRec>(), b.bins.as<EdgeRec>(),
+                     b.bin_offsets.as<uint32_t>(), b.bin_counts.as<uint32_t>(), b.stack.as<uint32_t>(),
+                     b.span_ovf.as<int2>(), ovf_cap, b.err.as<uint32_t>(), s));
+    if (ev1) CK(cudaEventRecord(ev1, s));
+    g_stats.draws += ndraws;
+    g_stats.work_items += p.items.size();
+    g_stats.kernel_launches += 13;
+    return RGPU_OK;
+}
+
+int check_err(Buffers &b, cudaStream_t s, cudaEvent_t ev0, cudaEvent_t ev1) {
     uint32_t e = 0;
-    CK(cudaMemcpyAsync(&e, c.err.p, 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(&e, b.err.p, 4, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     float ms = 0;
-    if (cudaEventElapsedTime(&ms, c.ev0, c.ev1) == cudaSuccess) g_stats.raster_ms = ms;
+    if (ev0) {
+        if (cudaEventElapsedTime(&ms, ev0, ev1) == cudaSuccess) g_stats.raster_ms = ms;
+        cudaGetLastError();  // never leave a pending error behind for the caller
+    }
     if (e) {
         set_error("raster kernel reported error flags 0x%x", e);
         return RGPU_ERR_DEVICE_FAULT;
@@ -285,23 +335,23 @@ int render_host(const rgpu_tree *tree, const resvg_transform &ts, uint32_t w, ui
     cudaStream_t s = c.stream;
     size_t bytes = (size_t)w * h * 4;
     CK(c.surface.ensure(bytes));
-    SceneBuild sb;
+    Plan p;
     rgpu_tree *tr = const_cast<rgpu_tree *>(tree);
     if (!tr->finalized) tr->finalize();
-    if (sb.add_tree(*tr, Xf::row(ts.a, ts.b, ts.c, ts.d, ts.e, ts.f), (int32_t)w, (int32_t)h,
-                    (uint64_t)(uintptr_t)c.surface.p, w * 4) < 0) {
-        set_error("%s", sb.error.c_str());
+    if (p.sb.add_tree(*tr, Xf::row(ts.a, ts.b, ts.c, ts.d, ts.e, ts.f), (int32_t)w, (int32_t)h,
+                      (uint64_t)(uintptr_t)c.surface.p, w * 4) < 0) {
+        set_error("%s", p.sb.error.c_str());
         return RGPU_ERR_UNSUPPORTED;
     }
     CK(c.staging.ensure(bytes));
     std::memcpy(c.staging.p, pixmap, bytes);
     CK(cudaMemcpyAsync(c.surface.p, c.staging.p, bytes, cudaMemcpyHostToDevice, s));
-    CK(cudaStreamSynchronize(s));  // staging is reused by run_scene
+    CK(cudaStreamSynchronize(s));  // staging is reused for the records
     g_stats.h2d_bytes += bytes;
-    r = run_scene(c, sb, s);
-    if (r) return r;
-    r = check_err(c, s);
-    if (r) return r;
+    if ((r = plan_scene(c, p))) return r;
+    if ((r = upload_plan(c, c.buf, p, s))) return r;
+    if ((r = enqueue_plan(c, c.buf, p, s, c.ev0, c.ev1))) return r;
+    if ((r = check_err(c.buf, s, c.ev0, c.ev1))) return r;
     CK(c.staging.ensure(bytes));
     CK(cudaMemcpyAsync(c.staging.p, c.surface.p, bytes, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
@@ -342,6 +392,52 @@ bool resvg_render_node(const resvg_render_tree *tree, const char *id, resvg_tran
     return false;
 }
 
+}  // extern "C"
+
+// Prepared scene: flattened records resident on the device with their own
+// work buffers; renders after the first are asynchronous and replay a
+// captured CUDA graph.
+struct rgpu_scene {
+    Plan plan;
+    Buffers buf;
+    cudaGraphExec_t graph = nullptr;
+    cudaStream_t graph_stream = nullptr;
+    cudaStream_t last_stream = nullptr;
+    bool timing = false;        // un-captured renders with events around the raster kernel
+    bool timed_valid = false;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    ~rgpu_scene() {
+        if (graph) cudaGraphExecDestroy(graph);
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        buf.release();
+    }
+};
+
+static int build_batch(Plan &p, const resvg_render_tree *const *trees, const resvg_transform *transforms,
+                       uint32_t count, const uint32_t *widths, const uint32_t *heights, uint8_t *const *ptrs,
+                       const uint32_t *strides) {
+    for (uint32_t i = 0; i < count; i++) {
+        rgpu_tree *tr = const_cast<rgpu_tree *>(trees[i]);
+        if (!tr || !ptrs[i] || !widths[i] || !heights[i] || widths[i] > 32767 || heights[i] > 32767) {
+            set_error("invalid batch entry %u", i);
+            return RGPU_ERR_INVALID_ARG;
+        }
+        uint32_t stride = strides ? strides[i] : widths[i] * 4;
+        if (stride < widths[i] * 4) { set_error("invalid stride for entry %u", i); return RGPU_ERR_INVALID_ARG; }
+        if (!tr->finalized) tr->finalize();
+        const resvg_transform &ts = transforms[i];
+        if (p.sb.add_tree(*tr, Xf::row(ts.a, ts.b, ts.c, ts.d, ts.e, ts.f), (int32_t)widths[i], (int32_t)heights[i],
+                          (uint64_t)(uintptr_t)ptrs[i], stride) < 0) {
+            set_error("entry %u: %s", i, p.sb.error.c_str());
+            return RGPU_ERR_UNSUPPORTED;
+        }
+    }
+    return RGPU_OK;
+}
+
+extern "C" {
+
 int rgpu_render_device(const resvg_render_tree *tree, resvg_transform ts, uint32_t w, uint32_t h,
                        uint8_t *device_pixmap, uint32_t stride, void *stream) {
     g_last_error.clear();
@@ -355,17 +451,12 @@ int rgpu_render_device(const resvg_render_tree *tree, resvg_transform ts, uint32
     int r = ensure_device(c);
     if (r) return r;
     cudaStream_t s = stream ? (cudaStream_t)stream : c.stream;
-    SceneBuild sb;
-    rgpu_tree *tr = const_cast<rgpu_tree *>(tree);
-    if (!tr->finalized) tr->finalize();
-    if (sb.add_tree(*tr, Xf::row(ts.a, ts.b, ts.c, ts.d, ts.e, ts.f), (int32_t)w, (int32_t)h,
-                    (uint64_t)(uintptr_t)device_pixmap, stride) < 0) {
-        set_error("%s", sb.error.c_str());
-        return RGPU_ERR_UNSUPPORTED;
-    }
-    r = run_scene(c, sb, s);
-    if (r) return r;
-    return check_err(c, s);
+    Plan p;
+    if ((r = build_batch(p, &tree, &ts, 1, &w, &h, &device_pixmap, &stride))) return r;
+    if ((r = plan_scene(c, p))) return r;
+    if ((r = upload_plan(c, c.buf, p, s))) return r;
+    if ((r = enqueue_plan(c, c.buf, p, s, c.ev0, c.ev1))) return r;
+    return check_err(c.buf, s, c.ev0, c.ev1);
 }
 
 int rgpu_render_batch(const resvg_render_tree *const *trees, const resvg_transform *transforms, uint32_t count,
@@ -381,24 +472,126 @@ int rgpu_render_batch(const resvg_render_tree *const *trees, const resvg_transfo
     int r = ensure_device(c);
     if (r) return r;
     cudaStream_t s = stream ? (cudaStream_t)stream : c.stream;
-    SceneBuild sb;
-    for (uint32_t i = 0; i < count; i++) {
-        rgpu_tree *tr = const_cast<rgpu_tree *>(trees[i]);
-        if (!tr || !device_pixmaps[i] || !widths[i] || !heights[i]) {
-            set_error("invalid batch entry %u", i);
-            return RGPU_ERR_INVALID_ARG;
-        }
-        if (!tr->finalized) tr->finalize();
-        const resvg_transform &ts = transforms[i];
-        if (sb.add_tree(*tr, Xf::row(ts.a, ts.b, ts.c, ts.d, ts.e, ts.f), (int32_t)widths[i], (int32_t)heights[i],
-                        (uint64_t)(uintptr_t)device_pixmaps[i], widths[i] * 4) < 0) {
-            set_error("batch entry %u: %s", i, sb.error.c_str());
-            return RGPU_ERR_UNSUPPORTED;
-        }
+    Plan p;
+    if ((r = build_batch(p, trees, transforms, count, widths, heights, device_pixmaps, nullptr))) return r;
+    if ((r = plan_scene(c, p))) return r;
+    if ((r = upload_plan(c, c.buf, p, s))) return r;
+    if ((r = enqueue_plan(c, c.buf, p, s, c.ev0, c.ev1))) return r;
+    return check_err(c.buf, s, c.ev0, c.ev1);
+}
+
+int rgpu_scene_prepare(const resvg_render_tree *const *trees, const resvg_transform *transforms, uint32_t count,
+                       const uint32_t *widths, const uint32_t *heights, uint8_t *const *device_pixmaps,
+                       const uint32_t *strides, rgpu_scene **out) {
+    g_last_error.clear();
+    std::memset(&g_stats, 0, sizeof(g_stats));
+    if (!out || !trees || !transforms || !widths || !heights || !device_pixmaps || count == 0) {
+        set_error("invalid arguments");
+        return RGPU_ERR_INVALID_ARG;
     }
-    r = run_scene(c, sb, s);
+    *out = nullptr;
+    Context &c = ctx();
+    std::lock_guard<std::mutex> lock(c.mu);
+    int r = ensure_device(c);
     if (r) return r;
-    return check_err(c, s);
+    rgpu_scene *sc = new rgpu_scene();
+    if ((r = build_batch(sc->plan, trees, transforms, count, widths, heights, device_pixmaps, strides)) ||
+        (r = plan_scene(c, sc->plan)) || (r = upload_plan(c, sc->buf, sc->plan, c.stream))) {
+        delete sc;
+        return r;
+    }
+    cudaError_t e = cudaStreamSynchronize(c.stream);
+    if (e == cudaSuccess) e = cudaEventCreate(&sc->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&sc->ev1);
+    if (e != cudaSuccess) {
+        set_error("rgpu_scene_prepare: %s", cudaGetErrorString(e));
+        delete sc;
+        return RGPU_ERR_CUDA;
+    }
+    *out = sc;
+    return RGPU_OK;
+}
+
+int rgpu_scene_render(rgpu_scene *sc, void *stream) {
+    g_last_error.clear();
+    if (!sc) { set_error("invalid arguments"); return RGPU_ERR_INVALID_ARG; }
+    Context &c = ctx();
+    std::lock_guard<std::mutex> lock(c.mu);
+    cudaStream_t s = stream ? (cudaStream_t)stream : c.stream;
+    sc->last_stream = s;
+    int r;
+    if (!sc->plan.sized || sc->timing) {
+        // the first render sizes the edge and bin buffers (two synchronisations);
+        // timing renders run un-captured with events around the raster kernel
+        r = enqueue_plan(c, sc->buf, sc->plan, s, sc->timing ? sc->ev0 : nullptr, sc->timing ? sc->ev1 : nullptr);
+        sc->timed_valid = sc->timing && r == RGPU_OK;
+        return r;
+    }
+    sc->timed_valid = false;
+    if (!sc->graph || sc->graph_stream != s) {
+        if (sc->graph) { cudaGraphExecDestroy(sc->graph); sc->graph = nullptr; }
+        cudaGraph_t g;
+        CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        r = enqueue_plan(c, sc->buf, sc->plan, s, nullptr, nullptr);
+        cudaError_t e = cudaStreamEndCapture(s, &g);
+        if (r) return r;
+        CK(e);
+        e = cudaGraphInstantiate(&sc->graph, g, 0);
+        cudaGraphDestroy(g);
+        CK(e);
+        sc->graph_stream = s;
+    }
+    CK(cudaGraphLaunch(sc->graph, s));
+    return RGPU_OK;
+}
+
+int rgpu_scene_set_timing(rgpu_scene *sc, int enabled) {
+    if (!sc) return RGPU_ERR_INVALID_ARG;
+    sc->timing = enabled != 0;
+    return RGPU_OK;
+}
+
+int rgpu_scene_check(rgpu_scene *sc, float *raster_ms) {
+    if (!sc) return RGPU_ERR_INVALID_ARG;
+    Context &c = ctx();
+    std::lock_guard<std::mutex> lock(c.mu);
+    cudaStream_t s = sc->last_stream ? sc->last_stream : c.stream;
+    int r = check_err(sc->buf, s, sc->timed_valid ? sc->ev0 : nullptr, sc->timed_valid ? sc->ev1 : nullptr);
+    if (raster_ms) *raster_ms = sc->timed_valid ? g_stats.raster_ms : -1.0f;
+    return r;
+}
+
+int rgpu_scene_info(const rgpu_scene *sc, rgpu_scene_stats *st) {
+    if (!sc || !st) return RGPU_ERR_INVALID_ARG;
+    const Plan &p = sc->plan;
+    st->streams = p.sb.streams.size();
+    st->draws = p.sb.draws.size();
+    st->commands = p.sb.cmds.size();
+    st->segments = p.sb.nsegs;
+    st->edges = p.nedges;
+    st->binned_edges = p.nbinned;
+    st->work_items = p.items.size();
+    st->grid = p.grid;
+    st->pixels_per_thread = p.px;
+    st->kernel_launches = 13;
+    uint64_t px = 0;
+    for (auto &s : p.sb.streams) px += (uint64_t)s.out_w * s.out_h;
+    st->output_pixels = px;
+    uint64_t layer_px = 0;
+    for (auto &l : p.sb.layers) layer_px += (uint64_t)l.w * l.h;
+    st->layer_pixels = layer_px;
+    st->record_bytes = p.sb.verbs.size() + p.sb.pts.size() * 4 + p.sb.draws.size() * sizeof(DrawRec) +
+                       p.sb.paints.size() * sizeof(PaintRec) + p.sb.grads.size() * sizeof(GradRec) +
+                       p.sb.layers.size() * sizeof(LayerRec) + p.sb.cmds.size() * sizeof(Cmd);
+    return RGPU_OK;
+}
+
+void rgpu_scene_free(rgpu_scene *sc) {
+    if (!sc) return;
+    Context &c = ctx();
+    std::lock_guard<std::mutex> lock(c.mu);
+    if (c.stream) cudaStreamSynchronize(c.stream);
+    delete sc;
 }
 
 int rgpu_set_tuning(const rgpu_tuning *t) {

@@ -186,7 +186,8 @@ __global__ void k_draw_edges(DrawRec *draws, uint32_t ndraws, const uint32_t *se
 
 template <bool SCATTER>
 __global__ void k_bin(const EdgeRec *edges, const uint32_t *edge_draw, uint32_t nedges, const DrawRec *draws,
-                      const StreamRec *streams, uint32_t *bin_counts, const uint32_t *bin_offsets, EdgeRec *bins) {
+                      const StreamRec *streams, uint32_t *bin_counts, const uint32_t *bin_offsets, uint32_t bin_cap,
+                      uint32_t *err, EdgeRec *bins) {
     uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= nedges) return;
     uint32_t d = edge_draw[e];
@@ -207,7 +208,11 @@ __global__ void k_bin(const EdgeRec *edges, const uint32_t *edge_draw, uint32_t 
     for (int32_t b = b0; b <= b1; b++) {
         uint32_t slot = st.bin_off + (uint32_t)b * st.draw_cnt + ld;
         uint32_t k = atomicAdd(&bin_counts[slot], 1u);
-        if (SCATTER) bins[bin_offsets[slot] + k] = er;
+        if (SCATTER) {
+            uint32_t pos = bin_offsets[slot] + k;
+            if (pos < bin_cap) bins[pos] = er;
+            else atomicOr(err, 1u);
+        }
     }
 }
 
@@ -314,14 +319,14 @@ cudaError_t launch_draw_edges(DrawRec *draws, uint32_t ndraws, const uint32_t *s
 }
 cudaError_t launch_bin(bool scatter, const EdgeRec *edges, const uint32_t *edge_draw, uint32_t nedges,
                        const DrawRec *draws, const StreamRec *streams, uint32_t *bin_counts,
-                       const uint32_t *bin_offsets, EdgeRec *bins, cudaStream_t s) {
+                       const uint32_t *bin_offsets, uint32_t bin_cap, uint32_t *err, EdgeRec *bins, cudaStream_t s) {
     if (!nedges) return cudaSuccess;
     if (scatter)
         k_bin<true><<<blocks_for(nedges, 256), 256, 0, s>>>(edges, edge_draw, nedges, draws, streams, bin_counts,
-                                                             bin_offsets, bins);
+                                                             bin_offsets, bin_cap, err, bins);
     else
         k_bin<false><<<blocks_for(nedges, 256), 256, 0, s>>>(edges, edge_draw, nedges, draws, streams, bin_counts,
-                                                              bin_offsets, bins);
+                                                              bin_offsets, bin_cap, err, bins);
     return cudaGetLastError();
 }
 size_t scan_scratch_words(uint64_t n) { return (size_t)blocks_for(n ? n : 1, SCAN_TILE) + 1; }

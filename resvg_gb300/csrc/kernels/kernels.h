@@ -17,12 +17,13 @@ cudaError_t launch_edges(bool emit, const SegRec *segs, uint32_t nsegs, const Dr
 cudaError_t launch_draw_edges(DrawRec *draws, uint32_t ndraws, const uint32_t *seg_offsets, cudaStream_t s);
 cudaError_t launch_bin(bool scatter, const EdgeRec *edges, const uint32_t *edge_draw, uint32_t nedges,
                        const DrawRec *draws, const StreamRec *streams, uint32_t *bin_counts,
-                       const uint32_t *bin_offsets, EdgeRec *bins, cudaStream_t s);
+                       const uint32_t *bin_offsets, uint32_t bin_cap, uint32_t *err, EdgeRec *bins, cudaStream_t s);
 size_t scan_scratch_words(uint64_t n);
 cudaError_t launch_exclusive_scan(const uint32_t *in, uint32_t *out, uint64_t n, uint32_t *scratch, uint32_t *total,
                                   cudaStream_t s);
 
 // raster.cu
+cudaError_t raster_init();
 size_t raster_smem_bytes();
 size_t raster_stack_words_per_cta(int px);
 int raster_threads();

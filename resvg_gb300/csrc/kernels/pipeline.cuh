@@ -58,27 +58,29 @@ __device__ __forceinline__ void lowp_blend(uint32_t blend, const uint16_t s[4], 
 
 __device__ __forceinline__ float hinv(float v) { return 1.0f - v; }
 
-__device__ __noinline__ void blend_sep(uint32_t mode, const float *s, const float *d, float *o) {
+__device__ __noinline__ float4 blend_generic(uint32_t mode, float4 sv, float4 dv) {
+    const float s[4] = {sv.x, sv.y, sv.z, sv.w}, d[4] = {dv.x, dv.y, dv.z, dv.w};
+    float o[4];
     float sa = s[3], da = d[3];
     switch (mode) {
-    case RGPU_BLEND_CLEAR: for (int i = 0; i < 4; i++) o[i] = 0.0f; return;
-    case RGPU_BLEND_SOURCE: for (int i = 0; i < 4; i++) o[i] = s[i]; return;
-    case RGPU_BLEND_DESTINATION: for (int i = 0; i < 4; i++) o[i] = d[i]; return;
-    case RGPU_BLEND_SOURCE_OVER: for (int i = 0; i < 4; i++) o[i] = d[i] * hinv(sa) + s[i]; return;
-    case RGPU_BLEND_DESTINATION_OVER: for (int i = 0; i < 4; i++) o[i] = s[i] * hinv(da) + d[i]; return;
-    case RGPU_BLEND_SOURCE_IN: for (int i = 0; i < 4; i++) o[i] = s[i] * da; return;
-    case RGPU_BLEND_DESTINATION_IN: for (int i = 0; i < 4; i++) o[i] = d[i] * sa; return;
-    case RGPU_BLEND_SOURCE_OUT: for (int i = 0; i < 4; i++) o[i] = s[i] * hinv(da); return;
-    case RGPU_BLEND_DESTINATION_OUT: for (int i = 0; i < 4; i++) o[i] = d[i] * hinv(sa); return;
-    case RGPU_BLEND_SOURCE_ATOP: for (int i = 0; i < 4; i++) o[i] = s[i] * da + d[i] * hinv(sa); return;
-    case RGPU_BLEND_DESTINATION_ATOP: for (int i = 0; i < 4; i++) o[i] = d[i] * sa + s[i] * hinv(da); return;
-    case RGPU_BLEND_XOR: for (int i = 0; i < 4; i++) o[i] = s[i] * hinv(da) + d[i] * hinv(sa); return;
-    case RGPU_BLEND_PLUS: for (int i = 0; i < 4; i++) o[i] = fminf(s[i] + d[i], 1.0f); return;
-    case RGPU_BLEND_MODULATE: for (int i = 0; i < 4; i++) o[i] = s[i] * d[i]; return;
-    case RGPU_BLEND_SCREEN: for (int i = 0; i < 4; i++) o[i] = s[i] + d[i] - s[i] * d[i]; return;
+    case RGPU_BLEND_CLEAR: return make_float4(0.f, 0.f, 0.f, 0.f);
+    case RGPU_BLEND_SOURCE: { for (int i = 0; i < 4; i++) o[i] = s[i]; return make_float4(o[0], o[1], o[2], o[3]); }
+    case RGPU_BLEND_DESTINATION: { for (int i = 0; i < 4; i++) o[i] = d[i]; return make_float4(o[0], o[1], o[2], o[3]); }
+    case RGPU_BLEND_SOURCE_OVER: { for (int i = 0; i < 4; i++) o[i] = d[i] * hinv(sa) + s[i]; return make_float4(o[0], o[1], o[2], o[3]); }
+    case RGPU_BLEND_DESTINATION_OVER: { for (int i = 0; i < 4; i++) o[i] = s[i] * hinv(da) + d[i]; return make_float4(o[0], o[1], o[2], o[3]); }
+    case RGPU_BLEND_SOURCE_IN: { for (int i = 0; i < 4; i++) o[i] = s[i] * da; return make_float4(o[0], o[1], o[2], o[3]); }
+    case RGPU_BLEND_DESTINATION_IN: { for (int i = 0; i < 4; i++) o[i] = d[i] * sa; return make_float4(o[0], o[1], o[2], o[3]); }
+    case RGPU_BLEND_SOURCE_OUT: { for (int i = 0; i < 4; i++) o[i] = s[i] * hinv(da); return make_float4(o[0], o[1], o[2], o[3]); }
+    case RGPU_BLEND_DESTINATION_OUT: { for (int i = 0; i < 4; i++) o[i] = d[i] * hinv(sa); return make_float4(o[0], o[1], o[2], o[3]); }
+    case RGPU_BLEND_SOURCE_ATOP: { for (int i = 0; i < 4; i++) o[i] = s[i] * da + d[i] * hinv(sa); return make_float4(o[0], o[1], o[2], o[3]); }
+    case RGPU_BLEND_DESTINATION_ATOP: { for (int i = 0; i < 4; i++) o[i] = d[i] * sa + s[i] * hinv(da); return make_float4(o[0], o[1], o[2], o[3]); }
+    case RGPU_BLEND_XOR: { for (int i = 0; i < 4; i++) o[i] = s[i] * hinv(da) + d[i] * hinv(sa); return make_float4(o[0], o[1], o[2], o[3]); }
+    case RGPU_BLEND_PLUS: { for (int i = 0; i < 4; i++) o[i] = fminf(s[i] + d[i], 1.0f); return make_float4(o[0], o[1], o[2], o[3]); }
+    case RGPU_BLEND_MODULATE: { for (int i = 0; i < 4; i++) o[i] = s[i] * d[i]; return make_float4(o[0], o[1], o[2], o[3]); }
+    case RGPU_BLEND_SCREEN: { for (int i = 0; i < 4; i++) o[i] = s[i] + d[i] - s[i] * d[i]; return make_float4(o[0], o[1], o[2], o[3]); }
     case RGPU_BLEND_MULTIPLY:
-        for (int i = 0; i < 4; i++) o[i] = s[i] * hinv(da) + d[i] * hinv(sa) + s[i] * d[i];
-        return;
+        { for (int i = 0; i < 4; i++) o[i] = s[i] * hinv(da) + d[i] * hinv(sa) + s[i] * d[i];
+          return make_float4(o[0], o[1], o[2], o[3]); }
     default: break;
     }
     if (mode <= RGPU_BLEND_MULTIPLY) {
@@ -126,7 +128,7 @@ __device__ __noinline__ void blend_sep(uint32_t mode, const float *s, const floa
             o[i] = x;
         }
         o[3] = sa + da * hinv(sa);
-        return;
+        return make_float4(o[0], o[1], o[2], o[3]);
     }
     // non-separable modes
     auto lum = [](float r, float g, float b) { return r * 0.30f + g * 0.59f + b * 0.11f; };
@@ -176,6 +178,23 @@ __device__ __noinline__ void blend_sep(uint32_t mode, const float *s, const floa
     o[1] = g + d[1] * hinv(sa) + s[1] * hinv(da);
     o[2] = b + d[2] * hinv(sa) + s[2] * hinv(da);
     o[3] = sa + da - sa * da;
+    return make_float4(o[0], o[1], o[2], o[3]);
+}
+
+
+// highp blend with the common modes inlined.
+__device__ __forceinline__ float4 blend4(uint32_t mode, float4 s, float4 d) {
+    if (mode == RGPU_BLEND_SOURCE_OVER) {
+        float ia = hinv(s.w);
+        return make_float4(d.x * ia + s.x, d.y * ia + s.y, d.z * ia + s.z, d.w * ia + s.w);
+    }
+    if (mode == RGPU_BLEND_SOURCE) return s;
+    if (mode == RGPU_BLEND_CLEAR) return make_float4(0.f, 0.f, 0.f, 0.f);
+    return blend_generic(mode, s, d);
+}
+__device__ __forceinline__ void blend_sep(uint32_t mode, const float *s, const float *d, float *o) {
+    float4 r = blend4(mode, make_float4(s[0], s[1], s[2], s[3]), make_float4(d[0], d[1], d[2], d[3]));
+    o[0] = r.x; o[1] = r.y; o[2] = r.z; o[3] = r.w;
 }
 
 // Gradient colour at device pixel (px, py) (premultiplied f32); false when the
@@ -230,72 +249,74 @@ __device__ __forceinline__ bool gradient_eval(const GradRec &g, int32_t px, int3
     return true;
 }
 
+__device__ __forceinline__ float4 unpack_f(uint32_t p) {
+    return make_float4((float)ch(p, 0) * kInv255, (float)ch(p, 1) * kInv255, (float)ch(p, 2) * kInv255,
+                       (float)ch(p, 3) * kInv255);
+}
+__device__ __forceinline__ uint32_t pack_f(float4 o) { return pack(unnorm(o.x), unnorm(o.y), unnorm(o.z), unnorm(o.w)); }
+
 // Blits one pixel of a fill with coverage `cov` (1..255) onto `dst`.
-__device__ __forceinline__ uint32_t shade_pixel(const PaintRec &pr, const GradRec *grads, int32_t lx, int32_t ly,
+__device__ __forceinline__ uint32_t shade_pixel(const PaintRec &pr, const GradRec *grad, int32_t lx, int32_t ly,
                                                 uint32_t cov, uint32_t dst) {
     if (cov == 255 && (pr.flags & PAINT_MEMSET))
         return pack(pr.memset_rgba[0], pr.memset_rgba[1], pr.memset_rgba[2], pr.memset_rgba[3]);
-    uint32_t blend = pr.blend;
+    const uint32_t blend = pr.blend;
     if (pr.flags & PAINT_LOWP) {
         uint16_t s[4] = {pr.rgba16[0], pr.rgba16[1], pr.rgba16[2], pr.rgba16[3]};
         uint16_t d[4] = {(uint16_t)ch(dst, 0), (uint16_t)ch(dst, 1), (uint16_t)ch(dst, 2), (uint16_t)ch(dst, 3)};
         uint16_t o[4];
         if (cov == 255) {
-            if (blend == RGPU_BLEND_SOURCE) { for (int i = 0; i < 4; i++) o[i] = s[i]; }
-            else lowp_blend(blend, s, d, o);
+            if (blend == RGPU_BLEND_SOURCE) {
+#pragma unroll
+                for (int i = 0; i < 4; i++) o[i] = s[i];
+            } else lowp_blend(blend, s, d, o);
         } else {
             uint16_t c = sat_u16(((float)cov * kInv255) * 255.0f + 0.5f);
             if (pre_scale(blend)) {
+#pragma unroll
                 for (int i = 0; i < 4; i++) s[i] = div255(u16(s[i] * c));
                 lowp_blend(blend, s, d, o);
             } else {
                 uint16_t b[4];
                 lowp_blend(blend, s, d, b);
+#pragma unroll
                 for (int i = 0; i < 4; i++) o[i] = div255(u16(d[i] * inv16(c) + b[i] * c));
             }
         }
         return pack(o[0], o[1], o[2], o[3]);
     }
-    float s[4];
+    float4 s;
     if (pr.kind == 0) {
-        for (int i = 0; i < 4; i++) s[i] = pr.colorf[i];
+        s = make_float4(pr.colorf[0], pr.colorf[1], pr.colorf[2], pr.colorf[3]);
     } else {
-        if (!gradient_eval(grads[pr.grad], lx, ly, s)) { s[0] = s[1] = s[2] = s[3] = 0.0f; }
+        float c[4];
+        if (gradient_eval(*grad, lx, ly, c)) s = make_float4(c[0], c[1], c[2], c[3]);
+        else s = make_float4(0.f, 0.f, 0.f, 0.f);
     }
-    float d[4] = {(float)ch(dst, 0) * kInv255, (float)ch(dst, 1) * kInv255, (float)ch(dst, 2) * kInv255,
-                  (float)ch(dst, 3) * kInv255};
-    float o[4];
+    const float4 d = unpack_f(dst);
+    float4 o;
     if (cov == 255) {
-        if (blend == RGPU_BLEND_SOURCE) { for (int i = 0; i < 4; i++) o[i] = s[i]; }
-        else blend_sep(blend, s, d, o);
+        o = blend4(blend, s, d);
     } else {
-        float c = (float)cov * kInv255;
+        const float c = (float)cov * kInv255;
         if (pre_scale(blend)) {
-            for (int i = 0; i < 4; i++) s[i] = s[i] * c;
-            blend_sep(blend, s, d, o);
+            s = make_float4(s.x * c, s.y * c, s.z * c, s.w * c);
+            o = blend4(blend, s, d);
         } else {
-            float b[4];
-            blend_sep(blend, s, d, b);
-            for (int i = 0; i < 4; i++) o[i] = (b[i] - d[i]) * c + d[i];
+            float4 b = blend4(blend, s, d);
+            o = make_float4((b.x - d.x) * c + d.x, (b.y - d.y) * c + d.y, (b.z - d.z) * c + d.z, (b.w - d.w) * c + d.w);
         }
     }
-    return pack(unnorm(o[0]), unnorm(o[1]), unnorm(o[2]), unnorm(o[3]));
+    return pack_f(o);
 }
 
 // draw_pixmap of one pixel: highp pattern (already at the right pixel),
 // opacity scale, blend, store.
 __device__ __forceinline__ uint32_t composite_pixel(uint32_t src, uint32_t dst, float opacity, uint32_t blend) {
     if (blend == RGPU_BLEND_DESTINATION) return dst;
-    float s[4] = {(float)ch(src, 0) * kInv255, (float)ch(src, 1) * kInv255, (float)ch(src, 2) * kInv255,
-                  (float)ch(src, 3) * kInv255};
-    if (opacity != 1.0f)
-        for (int i = 0; i < 4; i++) s[i] = s[i] * opacity;
-    float d[4] = {(float)ch(dst, 0) * kInv255, (float)ch(dst, 1) * kInv255, (float)ch(dst, 2) * kInv255,
-                  (float)ch(dst, 3) * kInv255};
-    float o[4];
-    if (blend == RGPU_BLEND_SOURCE) { for (int i = 0; i < 4; i++) o[i] = s[i]; }
-    else blend_sep(blend, s, d, o);
-    return pack(unnorm(o[0]), unnorm(o[1]), unnorm(o[2]), unnorm(o[3]));
+    float4 s = unpack_f(src);
+    if (opacity != 1.0f) s = make_float4(s.x * opacity, s.y * opacity, s.z * opacity, s.w * opacity);
+    return pack_f(blend4(blend, s, unpack_f(dst)));
 }
 
 // Pixmap::apply_mask (lowp): every channel *= m / 255 via div255.

@@ -29,14 +29,21 @@ constexpr int kXCap = 40;        // crossings held per thread before the exact s
 constexpr int kSpanCap = 12;     // spans per (slot, sub-scanline) kept in shared memory
 constexpr int kMaxDepth = 48;    // layer stack depth
 
+constexpr int kMaxSlots = 64;   // draws per phase-A window (S >= 4 scanlines each)
+
 struct VmShared {
     int32_t win_first;           // first command index of the prepared window
     int32_t win_last;            // one past the last command index covered by the window
     int32_t nslots;
-    int32_t slot_cmd[kThreads];  // command index per slot
+    int32_t slot_cmd[kMaxSlots]; // command index per slot
     uint16_t span_cnt[kThreads];
     int2 spans[kThreads * kSpanCap];
+    int4 rects[kMaxDepth];       // layer-stack rects (x, y, w, h), uniform across the CTA
+    PaintRec paint[kMaxSlots];   // paints of the window's draws
+    int32_t grad_slot[kMaxSlots];// index into grad[] or -1
+    GradRec grad[kMaxSlots];     // gradients of the window's draws
     int32_t item;
+    // followed by the top layer: kThreads * px uint32 pixels (dynamic)
 };
 
 __device__ __forceinline__ int32_t round16(int32_t x) { return (int32_t)((uint32_t)x + 0x8000u) >> 16; }
@@ -55,7 +62,7 @@ __device__ __forceinline__ int2 load_span(const VmShared &sh, const int2 *ovf, u
     return idx < kSpanCap ? sh.spans[slot_j * kSpanCap + idx] : ovf[(size_t)slot_j * ovf_cap + (idx - kSpanCap)];
 }
 
-// Phase A for one (draw, scanline): spans into slot `sj`.
+// Phase A for one (draw, scanline): spans into slot `sj`.  
 __device__ void phase_a(VmShared &sh, int sj, const DrawRec &dr, int32_t y, const EdgeRec *bl, uint32_t nb,
                         int2 *ovf, uint32_t ovf_cap, uint32_t *err) {
     int nspans = 0;
@@ -120,14 +127,30 @@ __device__ void phase_a(VmShared &sh, int sj, const DrawRec &dr, int32_t y, cons
     sh.span_cnt[sj] = (uint16_t)min(nspans, kSpanCap + (int)ovf_cap);
 }
 
-template <int PX>
-__global__ void __launch_bounds__(kThreads, 2)
-k_raster(const StreamRec *streams, const WorkItem *items, uint32_t nitems, uint32_t *item_counter, const Cmd *cmds,
-         const DrawRec *draws, const PaintRec *paints, const GradRec *grads, const LayerRec *layers,
+
+// Coverage of pixel `lx` (layer coordinates) on one scanline's span list,
+// starting from cursor q (spans before q end left of the warp's window).
+__device__ __forceinline__ uint32_t span_cov(const VmShared &sh, const int2 *ovf, uint32_t ovf_cap, int sj, int n,
+                                             int &q, int32_t w0, int32_t w1, int32_t p0, uint32_t maxv) {
+    while (q < n && load_span(sh, ovf, ovf_cap, sj, q).y <= w0) q++;
+    uint32_t cov = 0;
+    for (int k = q; k < n; k++) {
+        int2 sp = load_span(sh, ovf, ovf_cap, sj, k);
+        if (sp.x >= w1) break;
+        int32_t ov = min(sp.y, p0 + 4) - max(sp.x, p0);
+        if (ov > 0) cov += ov == 4 ? maxv : (uint32_t)ov * 16u;
+    }
+    return cov;
+}
+
+__global__ void __launch_bounds__(kThreads, 3)
+k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitems, uint32_t *item_counter,
+         const Cmd *cmds, const DrawRec *draws, const PaintRec *paints, const GradRec *grads, const LayerRec *layers,
          const EdgeRec *bins, const uint32_t *bin_offsets, const uint32_t *bin_counts, uint32_t *stack_scratch,
          uint32_t stack_depth, int2 *span_ovf, uint32_t ovf_cap, uint32_t *err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     VmShared &sh = *reinterpret_cast<VmShared *>(smem_raw);
+    uint32_t *layer = reinterpret_cast<uint32_t *>(smem_raw + ((sizeof(VmShared) + 15) & ~(size_t)15));
     const int tid = threadIdx.x;
     uint32_t *stack = stack_scratch + (size_t)blockIdx.x * stack_depth * kThreads * PX;
     int2 *ovf = span_ovf + (size_t)blockIdx.x * kThreads * ovf_cap;
@@ -135,32 +158,28 @@ k_raster(const StreamRec *streams, const WorkItem *items, uint32_t nitems, uint3
     for (;;) {
         if (tid == 0) sh.item = (int32_t)atomicAdd(item_counter, 1u);
         __syncthreads();
-        int32_t item_idx = sh.item;
+        const int32_t item_idx = sh.item;
         __syncthreads();
         if (item_idx >= (int32_t)nitems) break;
         const WorkItem wi = items[item_idx];
         const StreamRec st = streams[wi.stream];
         const int BH = (int)st.band_rows;
         const int S = 4 * BH;                 // scanline slots per draw (sub-scanlines for AA)
-        const int K = kThreads / S;           // draws per phase-A window
+        const int K = min(kThreads / S, kMaxSlots);
         const int tpr = kThreads / BH;        // threads per pixel row
         const int row = tid / tpr;
+        const int lr = tid % tpr;             // lane within the row: pixel x = x0 + i*tpr + lr
         const int32_t cy = (int32_t)wi.band * BH + row;
-        const int32_t cx0 = wi.x0 + (tid % tpr) * PX;
         const bool row_ok = cy < st.out_h;
         uint8_t *out = (uint8_t *)(uintptr_t)st.out_ptr;
-
-        uint32_t px[PX];
-#pragma unroll
+        // pixel (i) of this thread lives in layer[i * kThreads + tid]
         for (int i = 0; i < PX; i++) {
-            int32_t x = cx0 + i;
-            px[i] = (row_ok && x < st.out_w && x < wi.x1) ? *(const uint32_t *)(out + (size_t)cy * st.out_stride + 4 * (size_t)x) : 0u;
+            int32_t x = wi.x0 + i * tpr + lr;
+            layer[i * kThreads + tid] =
+                (row_ok && x < wi.x1) ? *(const uint32_t *)(out + (size_t)cy * st.out_stride + 4 * (size_t)x) : 0u;
         }
-        // layer stack: rect of each level in output space
         int32_t depth = 0;
         int32_t top_x = 0, top_y = 0, top_w = st.out_w, top_h = st.out_h;
-        int32_t rect_x[kMaxDepth], rect_y[kMaxDepth], rect_w[kMaxDepth], rect_h[kMaxDepth];
-
         if (tid == 0) { sh.win_first = 0; sh.win_last = 0; sh.nslots = 0; }
         __syncthreads();
         int32_t slot_next = 0;
@@ -169,29 +188,66 @@ k_raster(const StreamRec *streams, const WorkItem *items, uint32_t nitems, uint3
             const Cmd c = cmds[st.cmd_off + ci];
             if (c.op == CMD_FILL || c.op == CMD_APPLY_REGION) {
                 if ((int32_t)ci >= sh.win_last) {
-                    // ---- prepare a new phase-A window starting at this command
+                    // ---- prepare a phase-A window over the next K fill commands
                     __syncthreads();
-                    if (tid == 0) {
+                    if (tid < 32) {
+                        // warp 0 finds the next K fill commands with a ballot scan
                         int ns = 0;
                         uint32_t cj = ci;
-                        for (; cj < st.cmd_cnt && ns < K; cj++) {
-                            uint32_t op = cmds[st.cmd_off + cj].op;
-                            if (op == CMD_FILL || op == CMD_APPLY_REGION) sh.slot_cmd[ns++] = (int32_t)cj;
+                        uint32_t end = st.cmd_cnt;
+                        while (cj < st.cmd_cnt && ns < K) {
+                            uint32_t idx = cj + (uint32_t)tid;
+                            bool isfill = false;
+                            if (idx < st.cmd_cnt) {
+                                uint32_t op = cmds[st.cmd_off + idx].op;
+                                isfill = op == CMD_FILL || op == CMD_APPLY_REGION;
+                            }
+                            uint32_t m = __ballot_sync(0xffffffffu, isfill);
+                            int slot = ns + __popc(m & ((1u << tid) - 1u));
+                            if (isfill && slot < K) sh.slot_cmd[slot] = (int32_t)idx;
+                            int tot = __popc(m);
+                            if (ns + tot >= K) {
+                                // the window ends after the K-th fill command
+                                uint32_t mk = __ballot_sync(0xffffffffu, isfill && slot == K - 1);
+                                uint32_t last = __shfl_sync(0xffffffffu, idx, __ffs(mk) - 1);
+                                end = last + 1;
+                                ns = K;
+                                break;
+                            }
+                            ns += tot;
+                            cj += 32;
                         }
-                        sh.win_first = (int32_t)ci;
-                        sh.win_last = (int32_t)cj;
-                        sh.nslots = ns;
+                        if (tid == 0) {
+                            sh.win_first = (int32_t)ci;
+                            sh.win_last = (int32_t)min(end, st.cmd_cnt);
+                            sh.nslots = ns;
+                        }
                     }
                     __syncthreads();
+                    if (tid < sh.nslots) {
+                        const PaintRec &pr = paints[draws[cmds[st.cmd_off + sh.slot_cmd[tid]].a].paint];
+                        sh.paint[tid] = pr;
+                        sh.grad_slot[tid] = pr.kind == 1 ? tid : -1;
+                    }
+                    __syncthreads();
+                    // stage the window's gradients cooperatively
+                    {
+                        const int words = (int)(sizeof(GradRec) / 4);
+                        const int total = sh.nslots * words;
+                        for (int w = tid; w < total; w += kThreads) {
+                            const int k = w / words, o = w - k * words;
+                            if (sh.grad_slot[k] >= 0)
+                                ((uint32_t *)&sh.grad[k])[o] = ((const uint32_t *)&grads[sh.paint[k].grad])[o];
+                        }
+                    }
                     slot_next = 0;
-                    int k = tid / S, j = tid % S;
+                    const int k = tid / S, j = tid % S;
                     if (k < sh.nslots) {
                         const Cmd fc = cmds[st.cmd_off + sh.slot_cmd[k]];
                         const DrawRec dr = draws[fc.a];
-                        uint32_t ld = fc.a - st.draw_off;
-                        uint32_t slot = st.bin_off + wi.band * st.draw_cnt + ld;
-                        // scanline for (draw, j): layer row of this band's first row
-                        int32_t lrow0 = (int32_t)wi.band * BH - dr.oy;
+                        const uint32_t ld = fc.a - st.draw_off;
+                        const uint32_t slot = st.bin_off + wi.band * st.draw_cnt + ld;
+                        const int32_t lrow0 = (int32_t)wi.band * BH - dr.oy;
                         int32_t y;
                         bool ok;
                         if (dr.shift) { y = lrow0 * 4 + j; ok = true; }
@@ -201,120 +257,116 @@ k_raster(const StreamRec *streams, const WorkItem *items, uint32_t nitems, uint3
                     }
                     __syncthreads();
                 }
-                // ---- phase B for this command's slot
+                // ---- phase B: coverage + shading, one pixel per (thread, i)
                 const int slot = slot_next++;
                 const DrawRec dr = draws[c.a];
-                uint32_t cov[PX];
-#pragma unroll
-                for (int i = 0; i < PX; i++) cov[i] = 0;
+                if (!dr.valid && c.op == CMD_FILL) continue;
                 const int32_t ly = cy - dr.oy;
-                const int32_t lx0 = cx0 - dr.ox;
-                if (dr.valid && row_ok && ly >= dr.sect_t && ly < dr.sect_b) {
-                    const int32_t lrow0 = (int32_t)wi.band * BH - dr.oy;
+                const int32_t lrow0 = (int32_t)wi.band * BH - dr.oy;
+                const bool row_in = dr.valid && row_ok && ly >= dr.sect_t && ly < dr.sect_b;
+                if (c.op == CMD_FILL && !row_in) continue;
+                const PaintRec &pr = sh.paint[slot];
+                const GradRec *gr = sh.grad_slot[slot] >= 0 ? &sh.grad[sh.grad_slot[slot]] : &grads[pr.grad];
+                int cur[4] = {0, 0, 0, 0};
+                const int sj0 = slot * S + (ly - lrow0) * (dr.shift ? 4 : 1);
+                int ncnt[4];
+                if (row_in) {
                     if (dr.shift) {
-                        for (int s = 0; s < 4; s++) {
-                            const int j = (ly - lrow0) * 4 + s;
-                            const int sj = slot * S + j;
-                            const int n = sh.span_cnt[sj];
-                            const uint32_t maxv = s == 3 ? 63u : 64u;
-                            const int32_t a0 = lx0 << 2, a1 = (lx0 + PX) << 2;
-                            for (int q = 0; q < n; q++) {
-                                int2 sp = load_span(sh, ovf, ovf_cap, sj, q);
-                                if (sp.y <= a0) continue;
-                                if (sp.x >= a1) break;
-#pragma unroll
-                                for (int i = 0; i < PX; i++) {
-                                    int32_t p0 = (lx0 + i) << 2;
-                                    int32_t ov = min(sp.y, p0 + 4) - max(sp.x, p0);
-                                    if (ov > 0) cov[i] += ov == 4 ? maxv : (uint32_t)ov * 16u;
-                                }
-                            }
-                        }
+                        for (int s = 0; s < 4; s++) ncnt[s] = sh.span_cnt[sj0 + s];
                     } else {
-                        const int j = ly - lrow0;
-                        const int sj = slot * S + j;
-                        const int n = sh.span_cnt[sj];
-                        for (int q = 0; q < n; q++) {
-                            int2 sp = load_span(sh, ovf, ovf_cap, sj, q);
-#pragma unroll
-                            for (int i = 0; i < PX; i++) {
-                                int32_t x = lx0 + i;
-                                if (x >= sp.x && x < sp.y) cov[i] = 255;
-                            }
-                        }
+                        ncnt[0] = sh.span_cnt[sj0];
                     }
                 }
-                const PaintRec pr = paints[dr.paint];
-#pragma unroll
+#pragma unroll 1
                 for (int i = 0; i < PX; i++) {
-                    int32_t lx = lx0 + i;
-                    uint32_t cv = min(cov[i], 255u);
-                    if (lx < dr.sect_l || lx >= dr.sect_r) cv = 0;
+                    const int32_t x = wi.x0 + i * tpr + lr;
+                    const int32_t lx = x - dr.ox;
+                    uint32_t cv = 0;
+                    if (row_in) {
+                        const int32_t wx = wi.x0 + i * tpr + (lr & ~31) - dr.ox;  // warp window start (layer x)
+                        if (dr.shift) {
+                            const int32_t w0 = wx << 2, w1 = (wx + 32) << 2, p0 = lx << 2;
+#pragma unroll
+                            for (int s = 0; s < 4; s++)
+                                cv += span_cov(sh, ovf, ovf_cap, sj0 + s, ncnt[s], cur[s], w0, w1, p0, s == 3 ? 63u : 64u);
+                        } else {
+                            int q = cur[0];
+                            while (q < ncnt[0] && load_span(sh, ovf, ovf_cap, sj0, q).y <= wx) q++;
+                            cur[0] = q;
+                            for (int k2 = q; k2 < ncnt[0]; k2++) {
+                                int2 sp = load_span(sh, ovf, ovf_cap, sj0, k2);
+                                if (sp.x >= wx + 32) break;
+                                if (lx >= sp.x && lx < sp.y) cv = 255;
+                            }
+                        }
+                        cv = min(cv, 255u);
+                        if (lx < dr.sect_l || lx >= dr.sect_r) cv = 0;
+                    }
+                    uint32_t &px = layer[i * kThreads + tid];
                     if (c.op == CMD_FILL) {
-                        if (cv && !(pr.flags & PAINT_SKIP)) px[i] = dev::shade_pixel(pr, grads, lx, ly, cv, px[i]);
+                        if (cv && !(pr.flags & PAINT_SKIP)) px = dev::shade_pixel(pr, gr, lx, ly, cv, px);
                     } else {
                         // region mask: Mask::fill_path coverage (lerp 0 -> 255), then apply_mask
-                        int32_t x = cx0 + i;
-                        bool in_top = row_ok && x >= top_x && x < top_x + top_w && cy >= top_y && cy < top_y + top_h;
+                        const bool in_top = row_ok && x < wi.x1 && x >= top_x && x < top_x + top_w && cy >= top_y &&
+                                            cy < top_y + top_h;
                         if (in_top) {
                             uint32_t m = cv == 255 ? 255u
                                                    : (uint32_t)dev::div255((uint32_t)dev::sat_u16(((float)cv * dev::kInv255) * 255.0f + 0.5f) * 255u);
-                            px[i] = dev::mask_pixel(px[i], m);
+                            px = dev::mask_pixel(px, m);
                         }
                     }
                 }
             } else if (c.op == CMD_PUSH) {
+                __syncthreads();
                 if (depth + 1 >= kMaxDepth || (uint32_t)depth >= stack_depth) { atomicOr(err, 4u); break; }
-                uint32_t *lvl = stack + (size_t)depth * kThreads * PX + (size_t)tid * PX;
-#pragma unroll
-                for (int i = 0; i < PX; i++) lvl[i] = px[i];
-                rect_x[depth] = top_x; rect_y[depth] = top_y; rect_w[depth] = top_w; rect_h[depth] = top_h;
+                uint32_t *lvl = stack + (size_t)depth * kThreads * PX;
+                for (int i = 0; i < PX; i++) lvl[i * kThreads + tid] = layer[i * kThreads + tid];
+                if (tid == 0) sh.rects[depth] = make_int4(top_x, top_y, top_w, top_h);
                 depth++;
                 const LayerRec L = layers[st.layer_off + c.a];
                 top_x = L.x; top_y = L.y; top_w = L.w; top_h = L.h;
-                uint32_t init = c.b == 1 ? 0xFF000000u : 0u;
-#pragma unroll
+                const uint32_t init = c.b == 1 ? 0xFF000000u : 0u;
+                const bool row_in = cy >= top_y && cy < top_y + top_h;
                 for (int i = 0; i < PX; i++) {
-                    int32_t x = cx0 + i;
-                    bool in = x >= top_x && x < top_x + top_w && cy >= top_y && cy < top_y + top_h;
-                    px[i] = in ? init : 0u;
+                    const int32_t x = wi.x0 + i * tpr + lr;
+                    layer[i * kThreads + tid] = (row_in && x >= top_x && x < top_x + top_w) ? init : 0u;
                 }
             } else if (c.op == CMD_POP_COMPOSITE || c.op == CMD_POP_CLIP || c.op == CMD_POP_MASK) {
                 if (depth == 0) { atomicOr(err, 4u); break; }
+                __syncthreads();
                 depth--;
-                const uint32_t *lvl = stack + (size_t)depth * kThreads * PX + (size_t)tid * PX;
-                int32_t px0 = rect_x[depth], py0 = rect_y[depth], pw = rect_w[depth], ph = rect_h[depth];
-#pragma unroll
+                const uint32_t *lvl = stack + (size_t)depth * kThreads * PX;
+                const int4 p4 = sh.rects[depth];
+                const bool in_child_row = cy >= top_y && cy < top_y + top_h;
+                const bool in_parent_row = cy >= p4.y && cy < p4.y + p4.w;
                 for (int i = 0; i < PX; i++) {
-                    int32_t x = cx0 + i;
-                    uint32_t parent = lvl[i];
-                    bool in_child = x >= top_x && x < top_x + top_w && cy >= top_y && cy < top_y + top_h;
-                    bool in_parent = x >= px0 && x < px0 + pw && cy >= py0 && cy < py0 + ph;
+                    const int32_t x = wi.x0 + i * tpr + lr;
+                    uint32_t parent = lvl[i * kThreads + tid];
+                    const uint32_t child = layer[i * kThreads + tid];
+                    const bool in_child = in_child_row && x >= top_x && x < top_x + top_w;
+                    const bool in_parent = in_parent_row && x >= p4.x && x < p4.x + p4.z;
                     if (in_child && in_parent) {
-                        if (c.op == CMD_POP_COMPOSITE) parent = dev::composite_pixel(px[i], parent, c.f, c.b);
-                        else if (c.op == CMD_POP_CLIP) parent = dev::mask_pixel(parent, 255u - dev::ch(px[i], 3));
-                        else parent = dev::mask_pixel(parent, dev::mask_value(px[i], c.b == 0));
+                        if (c.op == CMD_POP_COMPOSITE) parent = dev::composite_pixel(child, parent, c.f, c.b);
+                        else if (c.op == CMD_POP_CLIP) parent = dev::mask_pixel(parent, 255u - dev::ch(child, 3));
+                        else parent = dev::mask_pixel(parent, dev::mask_value(child, c.b == 0));
                     }
-                    px[i] = parent;
+                    layer[i * kThreads + tid] = parent;
                 }
-                top_x = px0; top_y = py0; top_w = pw; top_h = ph;
+                top_x = p4.x; top_y = p4.y; top_w = p4.z; top_h = p4.w;
             } else if (c.op == CMD_CLEAR) {
-#pragma unroll
+                const bool row_in = cy >= top_y && cy < top_y + top_h;
                 for (int i = 0; i < PX; i++) {
-                    int32_t x = cx0 + i;
-                    bool in = x >= top_x && x < top_x + top_w && cy >= top_y && cy < top_y + top_h;
-                    if (in) px[i] = 0u;
+                    const int32_t x = wi.x0 + i * tpr + lr;
+                    if (row_in && x >= top_x && x < top_x + top_w) layer[i * kThreads + tid] = 0u;
                 }
             } else if (c.op == CMD_END) {
                 break;
             }
         }
-        // ---- write back the root layer
         if (depth != 0) atomicOr(err, 8u);
-#pragma unroll
         for (int i = 0; i < PX; i++) {
-            int32_t x = cx0 + i;
-            if (row_ok && x < st.out_w && x < wi.x1) *(uint32_t *)(out + (size_t)cy * st.out_stride + 4 * (size_t)x) = px[i];
+            const int32_t x = wi.x0 + i * tpr + lr;
+            if (row_ok && x < wi.x1) *(uint32_t *)(out + (size_t)cy * st.out_stride + 4 * (size_t)x) = layer[i * kThreads + tid];
         }
         __syncthreads();
     }
@@ -322,51 +374,31 @@ k_raster(const StreamRec *streams, const WorkItem *items, uint32_t nitems, uint3
 
 }  // namespace
 
-size_t raster_smem_bytes() { return sizeof(VmShared); }
+size_t raster_smem_bytes_px(int px) { return ((sizeof(VmShared) + 15) & ~(size_t)15) + (size_t)kThreads * px * 4; }
+size_t raster_smem_bytes() { return raster_smem_bytes_px(16); }
 size_t raster_stack_words_per_cta(int px) { return (size_t)kMaxDepth * kThreads * px; }
 int raster_threads() { return kThreads; }
 
-cudaError_t launch_raster(int px, uint32_t grid, uint32_t stack_depth, const StreamRec *streams, const WorkItem *items, uint32_t nitems,
-                          uint32_t *item_counter, const Cmd *cmds, const DrawRec *draws, const PaintRec *paints,
-                          const GradRec *grads, const LayerRec *layers, const EdgeRec *bins,
+cudaError_t raster_init() {
+    return cudaFuncSetAttribute(k_raster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)raster_smem_bytes_px(16));
+}
+
+cudaError_t launch_raster(int px, uint32_t grid, uint32_t stack_depth, const StreamRec *streams, const WorkItem *items,
+                          uint32_t nitems, uint32_t *item_counter, const Cmd *cmds, const DrawRec *draws,
+                          const PaintRec *paints, const GradRec *grads, const LayerRec *layers, const EdgeRec *bins,
                           const uint32_t *bin_offsets, const uint32_t *bin_counts, uint32_t *stack, int2 *span_ovf,
                           uint32_t ovf_cap, uint32_t *err, cudaStream_t s) {
-    size_t smem = sizeof(VmShared);
-    cudaError_t e;
-    switch (px) {
-    case 4:
-        e = cudaFuncSetAttribute(k_raster<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        k_raster<4><<<grid, kThreads, smem, s>>>(streams, items, nitems, item_counter, cmds, draws, paints, grads, layers,
-                                                  bins, bin_offsets, bin_counts, stack, stack_depth, span_ovf, ovf_cap, err);
-        break;
-    case 8:
-        e = cudaFuncSetAttribute(k_raster<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        k_raster<8><<<grid, kThreads, smem, s>>>(streams, items, nitems, item_counter, cmds, draws, paints, grads, layers,
-                                                  bins, bin_offsets, bin_counts, stack, stack_depth, span_ovf, ovf_cap, err);
-        break;
-    default:
-        e = cudaFuncSetAttribute(k_raster<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        k_raster<16><<<grid, kThreads, smem, s>>>(streams, items, nitems, item_counter, cmds, draws, paints, grads,
-                                                   layers, bins, bin_offsets, bin_counts, stack, stack_depth, span_ovf, ovf_cap, err);
-        break;
-    }
+    k_raster<<<grid, kThreads, raster_smem_bytes_px(px), s>>>(px, streams, items, nitems, item_counter, cmds, draws, paints,
+                                                              grads, layers, bins, bin_offsets, bin_counts, stack,
+                                                              stack_depth, span_ovf, ovf_cap, err);
     return cudaGetLastError();
 }
 
-}  // namespace rgpu
-
-namespace rgpu {
 int raster_max_blocks_per_sm(int px) {
     int n = 0;
-    size_t smem = raster_smem_bytes();
-    cudaError_t e;
-    if (px == 4) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_raster<4>, raster_threads(), smem);
-    else if (px == 8) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_raster<8>, raster_threads(), smem);
-    else e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_raster<16>, raster_threads(), smem);
-    if (e != cudaSuccess || n < 1) n = 1;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_raster, kThreads, raster_smem_bytes_px(px));
+    if (e != cudaSuccess || n < 1) { cudaGetLastError(); n = 1; }
     return n;
 }
+
 }  // namespace rgpu
