@@ -15,7 +15,7 @@
 
 namespace rgpu {
 
-constexpr int kMaxGradStops = 16;   // intervals incl. the two constant ends
+constexpr int kMaxGradStops = 12;   // intervals incl. the two constant ends (<= 10 stops after padding)
 
 struct GradRec {
     float ts[6];         // device pixel -> unit gradient space (sx, ky, kx, sy, tx, ty)
@@ -81,11 +81,14 @@ struct EdgeRec {
 
 struct LayerRec {
     int32_t x, y, w, h;   // in the stream's output space
+    int32_t surf;         // internal surface holding the layer's initial content (filter result), or -1
+    int32_t _pad;
+    uint64_t buf;         // device address of that surface (patched when surfaces are allocated)
 };
 
 enum CmdOp : uint32_t {
     CMD_FILL = 0,         // a = draw
-    CMD_PUSH = 1,         // a = layer, b = init (0 transparent, 1 opaque black, 2 load buffer)
+    CMD_PUSH = 1,         // a = layer, b = init (0 transparent, 1 opaque black, 2 the layer's surface)
     CMD_POP_COMPOSITE = 2,// a = popped layer, b = blend, f = opacity
     CMD_POP_CLIP = 3,     // a = popped layer: mask = 255 - alpha, applied to the new top
     CMD_POP_MASK = 4,     // a = popped layer, b = 0 luminance / 1 alpha
@@ -117,6 +120,8 @@ struct StreamRec {
     uint32_t band_rows, nbands;    // band height and count
     uint32_t bin_off;              // dense (band, draw) counters for this stream
     uint32_t max_depth;            // layer-stack depth needed
+    int32_t surface;               // internal surface rendered into (filter content), or -1
+    uint32_t level;                // dependency level: content streams render before their parents
 };
 
 }  // namespace rgpu

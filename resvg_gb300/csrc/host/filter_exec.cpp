@@ -1,0 +1,247 @@
+// Host driver of a filter job over device images (see filter_exec.h).
+//
+// Follows crates/resvg/src/filter/mod.rs: the filter region is the filter rect
+// mapped by the layer transform (:362-373); each primitive takes its inputs
+// (SourceGraphic, SourceAlpha or an earlier result, :523-564), converts them
+// to the primitive's colour space (:286-308), runs, and is cropped to its
+// subregion (:457-508); the last result goes back to sRGB and replaces the
+// layer (:1100-1114).  On an invalid region the layer is cleared (:343-346).
+#include "filter_exec.h"
+#include <cmath>
+#include <cstring>
+#include <vector>
+#include "../kernels/kernels.h"
+#include "resvg_gpu.h"
+
+namespace rgpu {
+namespace {
+
+inline int32_t sat_i32(float v) {
+    if (std::isnan(v)) return 0;
+    if (v >= 2147483648.0f) return INT32_MAX;
+    if (v <= -2147483648.0f) return INT32_MIN;
+    return (int32_t)v;
+}
+
+struct IRect { int32_t x, y, w, h; };
+
+// rect.transform(ts).to_int_rect()
+bool map_int_rect(const Xf &ts, float x, float y, float w, float h, IRect *out) {
+    float b[4];
+    if (!map_rect(ts, x, y, x + w, y + h, b)) return false;
+    int64_t ix = sat_i32(std::floor(b[0])), iy = sat_i32(std::floor(b[1]));
+    int64_t iw = std::max<int64_t>(1, (int64_t)std::ceil(b[2] - b[0]));
+    int64_t ih = std::max<int64_t>(1, (int64_t)std::ceil(b[3] - b[1]));
+    if (ix + iw > INT32_MAX || iy + ih > INT32_MAX) return false;
+    *out = IRect{(int32_t)ix, (int32_t)iy, (int32_t)iw, (int32_t)ih};
+    return true;
+}
+
+bool approx_zero_ulps(float v) {
+    int32_t a;
+    std::memcpy(&a, &v, 4);
+    if (a < 0) return v == 0.0f;
+    return a <= 4;
+}
+
+struct Img {
+    uint32_t *p;
+    bool linear;
+};
+
+struct Runner {
+    FilterScratch &sc;
+    cudaStream_t s;
+    int32_t w, h;
+    size_t n;
+    uint32_t next = 0;
+    cudaError_t e = cudaSuccess;
+
+    uint32_t *fresh() { return sc.image(next++, n); }
+    void ck(cudaError_t x) { if (e == cudaSuccess) e = x; }
+    // a private copy of `in` in colour space `lin`
+    Img private_in(Img in, bool lin) {
+        uint32_t *o = fresh();
+        ck(filter_copy(in.p, o, n, s));
+        if (in.linear != lin) ck(filter_color_space(o, n, lin, s));
+        return Img{o, lin};
+    }
+    Img in_space(Img in, bool lin) { return in.linear == lin ? in : private_in(in, lin); }
+};
+
+}  // namespace
+
+int run_filter_job(const FilterJob &job, uint32_t *content, uint32_t *result, FilterScratch &scratch, cudaStream_t s,
+                   std::string &err) {
+    const rgpu_tree_view &t = *job.tree;
+    Runner r{scratch, s, job.w, job.h, (size_t)job.w * job.h};
+    // the layer the filters act on, in place, one filter after another
+    uint32_t *source = content;
+    for (uint32_t fi = 0; fi < job.filter_count; fi++) {
+        const rgpu_filter &f = t.filters[t.filter_refs[job.filter_ref_offset + fi]];
+        IRect region;
+        bool ok = map_int_rect(job.ts, f.x, f.y, f.w, f.h, &region);
+        if (ok) {
+            int32_t l = std::max(region.x, 0), tp = std::max(region.y, 0);
+            int32_t rr = std::min(region.x + region.w, job.w), b = std::min(region.y + region.h, job.h);
+            ok = rr > l && b > tp;
+            region = IRect{l, tp, rr - l, b - tp};
+        }
+        if (ok && (region.x != 0 || region.y != 0 || region.w != job.w || region.h != job.h)) {
+            err = "filter region smaller than its layer";
+            return RGPU_ERR_UNSUPPORTED;
+        }
+        std::vector<Img> results;
+        bool failed = !ok;
+        for (uint32_t pi = 0; pi < f.prim_count && !failed; pi++) {
+            const rgpu_primitive &p = t.prims[f.prim_offset + pi];
+            IRect sub;
+            if (!map_int_rect(job.ts, p.x, p.y, p.w, p.h, &sub)) { failed = true; break; }
+            const bool lin = p.linear_rgb != 0;
+            auto input = [&](int32_t in) -> Img {
+                if (in >= 0 && (size_t)in < results.size()) return results[in];
+                if (in == RGPU_IN_SOURCE_ALPHA) {
+                    // SourceAlpha: RGB set to zero, alpha kept
+                    uint32_t *o = r.fresh();
+                    r.ck(filter_copy(source, o, r.n, s));
+                    r.ck(filter_alpha_only(o, r.n, s));
+                    return Img{o, false};
+                }
+                return Img{source, false};
+            };
+            Img res{nullptr, lin};
+            switch (p.kind) {
+            case RGPU_FE_BLUR: {
+                Img in = input(p.in1);
+                float sx, sy;
+                sx = std::sqrt(job.ts.sx * job.ts.sx + job.ts.kx * job.ts.kx);
+                sy = std::sqrt(job.ts.ky * job.ts.ky + job.ts.sy * job.ts.sy);
+                float x = p.f[0] * sx, y = p.f[1] * sy;
+                if (approx_zero_ulps(x) && approx_zero_ulps(y)) { res = in; break; }
+                if (x < 0.05f) x = 0.0f;
+                if (y < 0.05f) y = 0.0f;
+                bool box = x >= 2.0f || y >= 2.0f;
+                res = r.private_in(in, lin);
+                if (box) r.ck(filter_box_blur(res.p, r.fresh(), r.w, r.h, x, y, s));
+                else r.ck(filter_iir_blur(res.p, scratch.plane(r.n), r.w, r.h, x, y, s));
+                break;
+            }
+            case RGPU_FE_COLOR_MATRIX: {
+                res = r.private_in(input(p.in1), lin);
+                r.ck(filter_color_matrix(res.p, r.n, p.i[0], p.f, s));
+                break;
+            }
+            case RGPU_FE_MORPHOLOGY: {
+                res = r.private_in(input(p.in1), lin);
+                float sx = std::sqrt(job.ts.sx * job.ts.sx + job.ts.kx * job.ts.kx);
+                float sy = std::sqrt(job.ts.ky * job.ts.ky + job.ts.sy * job.ts.sy);
+                float rx = p.f[0] * sx, ry = p.f[1] * sy;
+                if (!(rx > 0.0f && ry > 0.0f)) r.ck(filter_fill(res.p, r.n, 0u, s));
+                else r.ck(filter_morphology(res.p, r.fresh(), r.w, r.h, p.i[0] == 1, rx, ry, s));
+                break;
+            }
+            case RGPU_FE_COMPOSITE: {
+                Img a = r.in_space(input(p.in1), lin), b = r.in_space(input(p.in2), lin);
+                uint32_t *o = r.fresh();
+                if (p.i[0] == RGPU_OP_ARITHMETIC) {
+                    const float k[4] = {p.f[0], p.f[1], p.f[2], p.f[3]};
+                    r.ck(filter_arithmetic(a.p, b.p, o, r.n, k, s));
+                } else {
+                    uint32_t bm = RGPU_BLEND_SOURCE_OVER;
+                    switch (p.i[0]) {
+                    case RGPU_OP_IN: bm = RGPU_BLEND_SOURCE_IN; break;
+                    case RGPU_OP_OUT: bm = RGPU_BLEND_SOURCE_OUT; break;
+                    case RGPU_OP_ATOP: bm = RGPU_BLEND_SOURCE_ATOP; break;
+                    case RGPU_OP_XOR: bm = RGPU_BLEND_XOR; break;
+                    default: break;
+                    }
+                    r.ck(filter_fill(o, r.n, 0u, s));
+                    r.ck(filter_draw(b.p, o, r.w, r.h, 0, 0, RGPU_BLEND_SOURCE_OVER, s));
+                    r.ck(filter_draw(a.p, o, r.w, r.h, 0, 0, bm, s));
+                }
+                res = Img{o, lin};
+                break;
+            }
+            case RGPU_FE_BLEND: {
+                Img a = r.in_space(input(p.in1), lin), b = r.in_space(input(p.in2), lin);
+                uint32_t *o = r.fresh();
+                r.ck(filter_fill(o, r.n, 0u, s));
+                r.ck(filter_draw(b.p, o, r.w, r.h, 0, 0, RGPU_BLEND_SOURCE_OVER, s));
+                r.ck(filter_draw(a.p, o, r.w, r.h, 0, 0, (uint32_t)p.i[0], s));
+                res = Img{o, lin};
+                break;
+            }
+            case RGPU_FE_MERGE: {
+                uint32_t *o = r.fresh();
+                r.ck(filter_fill(o, r.n, 0u, s));
+                for (int32_t k = 0; k < p.i[1]; k++) {
+                    Img in = r.in_space(input(t.merge_inputs[p.i[0] + k]), lin);
+                    r.ck(filter_draw(in.p, o, r.w, r.h, 0, 0, RGPU_BLEND_SOURCE_OVER, s));
+                }
+                res = Img{o, lin};
+                break;
+            }
+            case RGPU_FE_FLOOD: {
+                uint32_t *o = r.fresh();
+                // Pixmap::fill(Color::from_rgba8(r, g, b, opacity.to_u8())): premultiplied
+                float a = (float)(uint8_t)std::min(255.0f, std::max(0.0f, p.f[0] * 255.0f + 0.5f)) / 255.0f;
+                auto pm = [&](int c) {
+                    float v = (float)(uint8_t)c / 255.0f;
+                    if (a != 1.0f) v = std::min(std::max(v * a, 0.0f), 1.0f);
+                    return (uint32_t)(uint8_t)std::min(255.0f, v * 255.0f + 0.5f);
+                };
+                uint32_t a8 = (uint32_t)(uint8_t)std::min(255.0f, a * 255.0f + 0.5f);
+                uint32_t v = pm(p.i[0]) | (pm(p.i[1]) << 8) | (pm(p.i[2]) << 16) | (a8 << 24);
+                r.ck(filter_fill(o, r.n, v, s));
+                res = Img{o, false};
+                break;
+            }
+            case RGPU_FE_OFFSET: {
+                Img in = input(p.in1);
+                float sx = std::sqrt(job.ts.sx * job.ts.sx + job.ts.kx * job.ts.kx);
+                float sy = std::sqrt(job.ts.ky * job.ts.ky + job.ts.sy * job.ts.sy);
+                float dx = p.f[0] * sx, dy = p.f[1] * sy;
+                if (approx_zero_ulps(dx) && approx_zero_ulps(dy)) { res = in; break; }
+                uint32_t *o = r.fresh();
+                r.ck(filter_fill(o, r.n, 0u, s));
+                r.ck(filter_draw(in.p, o, r.w, r.h, sat_i32(dx), sat_i32(dy), RGPU_BLEND_SOURCE_OVER, s));
+                res = Img{o, in.linear};
+                break;
+            }
+            default:
+                err = "filter primitive not supported on the device";
+                return RGPU_ERR_UNSUPPORTED;
+            }
+            if (sub.x != region.x || sub.y != region.y || sub.w != region.w || sub.h != region.h) {
+                uint32_t *o = r.fresh();
+                r.ck(filter_copy(res.p, o, r.n, s));
+                if (p.kind == RGPU_FE_OFFSET) {
+                    // feOffset is not cropped
+                } else {
+                    int32_t l = sub.x - region.x, tp = sub.y - region.y;
+                    r.ck(filter_crop(o, r.w, r.h, l, tp, l + sub.w, tp + sub.h, s));
+                }
+                res = Img{o, res.linear};
+            }
+            results.push_back(res);
+        }
+        if (results.empty()) failed = true;
+        uint32_t *dst = (fi + 1 == job.filter_count) ? result : r.fresh();
+        if (failed) {
+            r.ck(filter_fill(dst, r.n, 0u, s));
+        } else {
+            Img last = results.back();
+            r.ck(filter_copy(last.p, dst, r.n, s));
+            if (last.linear) r.ck(filter_color_space(dst, r.n, false, s));
+        }
+        source = dst;
+    }
+    if (job.filter_count == 0) r.ck(filter_copy(content, result, r.n, s));
+    if (r.e != cudaSuccess) {
+        err = cudaGetErrorString(r.e);
+        return RGPU_ERR_CUDA;
+    }
+    return RGPU_OK;
+}
+
+}  // namespace rgpu

@@ -126,7 +126,7 @@ bool make_grad(const Shader &sh, GradRec &g) {
         size_t last = eq(st.back().c, st[st.size() - 2].c) ? st.size() - 2 : st.size() - 1;
         uint32_t n = 0;
         auto push = [&](const float f[4], const float b[4], float t) {
-            if (n >= (uint32_t)kMaxGradStops) return;
+            if (n >= (uint32_t)kMaxGradStops) { n = kMaxGradStops + 1; return; }
             for (int k = 0; k < 4; k++) { g.f[n][k] = f[k]; g.b[n][k] = b[k]; }
             g.t[n] = t;
             n++;
@@ -148,6 +148,7 @@ bool make_grad(const Shader &sh, GradRec &g) {
             cl = cr;
         }
         { float b[4] = {cl.r, cl.g, cl.b, cl.a}; push(zero, b, std::min(std::max(tl, 0.0f), 1.0f)); }
+        if (n > (uint32_t)kMaxGradStops) return false;  // more stops than the device record holds
         g.n = n;
     }
     // device pixel -> unit space
@@ -190,10 +191,11 @@ struct Flattener {
     SceneBuild &sb;
     Tree &tree;
     const rgpu_tree_view &t;
-    uint32_t stream;
     uint32_t tree_verb_base, tree_pt_base;
     int32_t max_x, max_y, max_w, max_h;  // max_filter_bbox
-    uint32_t depth = 0, max_depth = 0;
+    StreamBuild *cur = nullptr;          // stream being emitted
+    uint32_t depth = 0;
+    uint32_t child_level = 0;            // max level of content streams referenced by `cur` (+1)
     bool unsupported = false;
 
     uint32_t add_paint(const PaintRec &p) { sb.paints.push_back(p); return (uint32_t)sb.paints.size() - 1; }
@@ -249,13 +251,8 @@ struct Flattener {
         d.ox = tg.ox; d.oy = tg.oy;
         d.flags = (rule == RGPU_EVENODD ? DRAW_EVENODD : 0) | (aa ? DRAW_AA : 0);
         d.paint = paint;
-        d.seg_base = (uint32_t)sb.nsegs;
-        d.tpt_base = (uint32_t)sb.ntpts;
-        d.stream = stream;
-        sb.nsegs += verb_cnt + 1;
-        sb.ntpts += pt_cnt;
-        sb.draws.push_back(d);
-        sb.cmds.push_back(Cmd{op, (uint32_t)sb.draws.size() - 1, 0, 0.0f});
+        cur->draws.push_back(d);
+        cur->cmds.push_back(Cmd{op, (uint32_t)cur->draws.size() - 1, 0, 0.0f});
     }
 
     bool path_bounds_empty(const rgpu_path &p) {
@@ -308,16 +305,20 @@ struct Flattener {
             fill_path(p, RGPU_BLEND_SOURCE_OVER, ts, tg);
         }
     }
-    uint32_t push_layer(const Target &tg, uint32_t init) {
-        sb.layers.push_back(LayerRec{tg.ox, tg.oy, tg.w, tg.h});
-        uint32_t li = (uint32_t)(sb.layers.size() - 1 - sb.streams.back().layer_off);
-        sb.cmds.push_back(Cmd{CMD_PUSH, li, init, 0.0f});
+    uint32_t push_layer(const Target &tg, uint32_t init, int32_t surf = -1) {
+        LayerRec L;
+        std::memset(&L, 0, sizeof(L));
+        L.x = tg.ox; L.y = tg.oy; L.w = tg.w; L.h = tg.h;
+        L.surf = surf;
+        cur->layers.push_back(L);
+        uint32_t li = (uint32_t)cur->layers.size() - 1;
+        cur->cmds.push_back(Cmd{CMD_PUSH, li, init, 0.0f});
         depth++;
-        max_depth = std::max(max_depth, depth);
+        cur->max_depth = std::max(cur->max_depth, depth);
         return li;
     }
     void pop(uint32_t op, uint32_t li, uint32_t b, float f) {
-        sb.cmds.push_back(Cmd{op, li, b, f});
+        cur->cmds.push_back(Cmd{op, li, b, f});
         depth--;
     }
     // clip.rs:30-68
@@ -355,7 +356,7 @@ struct Flattener {
     // mask.rs:6-46
     void mask_apply(const rgpu_mask &mask, const Xf &ts, const Target &tg) {
         if (t.groups[mask.root].child_count == 0) {
-            sb.cmds.push_back(Cmd{CMD_CLEAR, 0, 0, 0.0f});
+            cur->cmds.push_back(Cmd{CMD_CLEAR, 0, 0, 0.0f});
             return;
         }
         if (mask.mask >= 0) mask_apply(t.masks[mask.mask], ts, tg);
@@ -381,6 +382,41 @@ struct Flattener {
         out[0] = (int32_t)l; out[1] = (int32_t)tp; out[2] = (int32_t)(r - l); out[3] = (int32_t)(b - tp);
         return true;
     }
+    // Flattens a filtered group's content into its own stream and records the
+    // filter job; returns the surface holding the filtered result.
+    int32_t filtered_content(uint32_t gi, const Xf &lts, int32_t w, int32_t h) {
+        const rgpu_group &g = t.groups[gi];
+        uint32_t content = (uint32_t)sb.surfaces.size();
+        sb.surfaces.push_back(SurfaceReq{w, h});
+        uint32_t result = (uint32_t)sb.surfaces.size();
+        sb.surfaces.push_back(SurfaceReq{w, h});
+        StreamBuild sub;
+        sub.out_w = w; sub.out_h = h;
+        sub.stride = (uint32_t)w * 4;
+        sub.surface = (int32_t)content;
+        StreamBuild *saved = cur;
+        uint32_t saved_depth = depth, saved_child = child_level;
+        cur = &sub;
+        depth = 0;
+        child_level = 0;
+        render_nodes(gi, lts, Target{w, h, 0, 0});
+        sub.level = child_level;
+        cur = saved;
+        depth = saved_depth;
+        child_level = std::max(saved_child, sub.level + 1);
+        sb.append_stream(sub);
+        FilterJob job;
+        job.content = content;
+        job.result = result;
+        job.w = w; job.h = h;
+        job.ts = lts;
+        job.tree = &t;
+        job.filter_ref_offset = g.filter_offset;
+        job.filter_count = g.filter_count;
+        job.level = sub.level;
+        sb.jobs.push_back(job);
+        return (int32_t)result;
+    }
     // render.rs:49-142
     void render_group(uint32_t gi, const Xf &ts_in, const Target &tg) {
         const rgpu_group &g = t.groups[gi];
@@ -404,16 +440,21 @@ struct Flattener {
             int64_t w = (int64_t)std::max(1.0f, std::ceil(bw)), h = (int64_t)std::max(1.0f, std::ceil(bh));
             if (x + w > INT32_MAX || y + h > INT32_MAX) return;
             if (!fit(x, y, w, h, max_x, max_y, max_w, max_h, ib)) return;
-            unsupported = true;  // filters run through the filter pass (not in this stream)
-            return;
         }
         float dx = bb[0], dy = bb[1];
         dx -= bb[0] - (float)ib[0];
         dy -= bb[1] - (float)ib[1];
         Xf lts = pre_concat(Xf::translate(-dx, -dy), ts);
         Target lt{ib[2], ib[3], tg.ox + ib[0], tg.oy + ib[1]};
-        uint32_t li = push_layer(lt, 0);
-        render_nodes(gi, lts, lt);
+        uint32_t li;
+        if (g.filter_count) {
+            if ((int64_t)ib[2] * ib[3] > (int64_t)1 << 28) { unsupported = true; return; }
+            int32_t surf = filtered_content(gi, lts, ib[2], ib[3]);
+            li = push_layer(lt, 2, surf);
+        } else {
+            li = push_layer(lt, 0);
+            render_nodes(gi, lts, lt);
+        }
         if (g.clip_path >= 0) clip_apply(t.clips[g.clip_path], lts, lt);
         if (g.mask >= 0) mask_apply(t.masks[g.mask], lts, lt);
         pop(CMD_POP_COMPOSITE, li, g.blend, g.opacity);
@@ -430,32 +471,58 @@ struct Flattener {
 
 }  // namespace
 
-int SceneBuild::add_tree(Tree &tree, const Xf &ts, int32_t w, int32_t h, uint64_t out_ptr, uint32_t stride) {
-    const rgpu_tree_view &t = *tree.get_view();
+uint32_t SceneBuild::append_stream(StreamBuild &b) {
     StreamRec st;
     std::memset(&st, 0, sizeof(st));
+    uint32_t si = (uint32_t)streams.size();
     st.cmd_off = (uint32_t)cmds.size();
+    st.cmd_cnt = (uint32_t)b.cmds.size();
     st.draw_off = (uint32_t)draws.size();
+    st.draw_cnt = (uint32_t)b.draws.size();
     st.layer_off = (uint32_t)layers.size();
-    st.out_w = w; st.out_h = h;
-    st.out_stride = stride;
-    st.out_ptr = out_ptr;
+    st.out_w = b.out_w; st.out_h = b.out_h;
+    st.out_stride = b.stride;
+    st.out_ptr = b.out_ptr;
+    st.max_depth = b.max_depth;
+    st.surface = b.surface;
+    st.level = b.level;
+    max_level = std::max(max_level, b.level);
+    for (auto &d : b.draws) {
+        d.seg_base = (uint32_t)nsegs;
+        d.tpt_base = (uint32_t)ntpts;
+        d.stream = si;
+        nsegs += d.verb_cnt + 1;
+        ntpts += d.pt_cnt;
+        draws.push_back(d);
+    }
+    for (auto c : b.cmds) {
+        if (c.op == CMD_FILL || c.op == CMD_APPLY_REGION) c.a += st.draw_off;
+        cmds.push_back(c);
+    }
+    layers.insert(layers.end(), b.layers.begin(), b.layers.end());
     streams.push_back(st);
-    Flattener f{*this, tree, t, (uint32_t)streams.size() - 1, (uint32_t)verbs.size(), (uint32_t)(pts.size() / 2)};
+    return si;
+}
+
+int SceneBuild::add_tree(Tree &tree, const Xf &ts, int32_t w, int32_t h, uint64_t out_ptr, uint32_t stride) {
+    const rgpu_tree_view &t = *tree.get_view();
+    Flattener f{*this, tree, t, (uint32_t)verbs.size(), (uint32_t)(pts.size() / 2)};
     verbs.insert(verbs.end(), t.verbs, t.verbs + t.verb_count);
     pts.insert(pts.end(), t.points, t.points + 2 * (size_t)t.point_count);
     int64_t mx = -2 * (int64_t)w, my = -2 * (int64_t)h, mw = 5 * (int64_t)w, mh = 5 * (int64_t)h;
     f.max_x = (int32_t)mx; f.max_y = (int32_t)my; f.max_w = (int32_t)mw; f.max_h = (int32_t)mh;
+    StreamBuild root;
+    root.out_w = w; root.out_h = h;
+    root.stride = stride;
+    root.out_ptr = out_ptr;
+    f.cur = &root;
     if (t.group_count) f.render_nodes(0, ts, Target{w, h, 0, 0});
-    StreamRec &s = streams.back();
-    s.cmd_cnt = (uint32_t)cmds.size() - s.cmd_off;
-    s.draw_cnt = (uint32_t)draws.size() - s.draw_off;
-    s.max_depth = f.max_depth;
     if (f.unsupported) {
-        error = "filters are not supported by this build of the stream renderer";
+        error = "a filter region of more than 2^28 pixels";
         return -1;
     }
-    return (int)streams.size() - 1;
+    root.level = f.child_level;
+    return (int)append_stream(root);
 }
 
 }  // namespace rgpu

@@ -1,7 +1,13 @@
 // Host flattener: walks a render tree the way resvg's renderer does
 // (crates/resvg/src/render.rs:10-142, path.rs:6-177, clip.rs:6-98,
 // mask.rs:6-46) and emits device records (draws, paints, gradients, layers)
-// and the band VM's command stream instead of rasterising.
+// and the band VM's command streams instead of rasterising.
+//
+// A group with filters (render.rs:113-117) splits the work: its content is
+// flattened into a stream of its own that renders into an internal surface at
+// an earlier dependency level, a FilterJob runs the filter chain on that
+// surface (filter_exec.cpp), and the parent stream pushes a layer initialised
+// from the job's result before applying clip, mask and the composite.
 #pragma once
 #include <string>
 #include <vector>
@@ -11,7 +17,31 @@
 
 namespace rgpu {
 
-struct FilterJob;  // filter groups rendered in a separate pass (filter_exec.cpp)
+struct SurfaceReq {
+    int32_t w, h;
+};
+
+struct FilterJob {
+    uint32_t content;               // surface with the rendered group content (SourceGraphic)
+    uint32_t result;                // surface receiving the filtered layer
+    int32_t w, h;
+    Xf ts;                          // the layer's transform (filter regions are mapped with it)
+    const rgpu_tree_view *tree;
+    uint32_t filter_ref_offset, filter_count;
+    uint32_t level;                 // runs after the raster pass of this level
+};
+
+struct StreamBuild {
+    std::vector<DrawRec> draws;     // seg_base / tpt_base / stream assigned on append
+    std::vector<Cmd> cmds;          // FILL / APPLY_REGION: a = draw index within this stream
+    std::vector<LayerRec> layers;
+    int32_t out_w = 0, out_h = 0;
+    uint32_t stride = 0;
+    uint64_t out_ptr = 0;
+    int32_t surface = -1;
+    uint32_t max_depth = 0;
+    uint32_t level = 0;
+};
 
 struct SceneBuild {
     std::vector<DrawRec> draws;
@@ -20,14 +50,19 @@ struct SceneBuild {
     std::vector<LayerRec> layers;
     std::vector<Cmd> cmds;
     std::vector<StreamRec> streams;
+    std::vector<SurfaceReq> surfaces;
+    std::vector<FilterJob> jobs;
     std::vector<uint8_t> verbs;
     std::vector<float> pts;
     uint64_t nsegs = 0, ntpts = 0;
+    uint32_t max_level = 0;
     std::string error;
 
-    // Appends one tree as one output stream; returns the stream index or -1.
-    // `out_ptr`/`stride` describe the device surface; (w, h) its size.
+    // Appends one tree rendered onto a device surface (`out_ptr`, `stride`,
+    // size w x h); returns the index of its output stream or -1.
     int add_tree(Tree &tree, const Xf &ts, int32_t w, int32_t h, uint64_t out_ptr, uint32_t stride);
+    // internal: concatenates a finished stream
+    uint32_t append_stream(StreamBuild &sbd);
 };
 
 }  // namespace rgpu

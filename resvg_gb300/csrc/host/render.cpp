@@ -15,6 +15,7 @@
 #include <string>
 #include <vector>
 #include "../kernels/kernels.h"
+#include "filter_exec.h"
 #include "flatten.h"
 #include "resvg_gpu.h"
 #include "tree.h"
@@ -78,15 +79,38 @@ struct Buffers {
     DevBuf tpts, segs, seg_counts, seg_offsets, scan_scratch, totals;
     DevBuf edges, edge_draw, bin_counts, bin_offsets, bins;
     DevBuf stack, span_ovf, err, counter;
+    std::vector<DevBuf> surf, img;   // internal surfaces (filter content/results) and filter images
+    DevBuf plane;                    // f64 plane of the IIR blur
     void release() {
         DevBuf *all[] = {&verbs, &pts, &draws, &paints, &grads, &layers, &cmds, &streams, &items, &tpts, &segs,
                          &seg_counts, &seg_offsets, &scan_scratch, &totals, &edges, &edge_draw, &bin_counts,
-                         &bin_offsets, &bins, &stack, &span_ovf, &err, &counter};
+                         &bin_offsets, &bins, &stack, &span_ovf, &err, &counter, &plane};
         for (DevBuf *b : all) {
             if (b->p) cudaFree(b->p);
             b->p = nullptr;
             b->cap = 0;
         }
+        for (auto &b : surf) if (b.p) cudaFree(b.p);
+        for (auto &b : img) if (b.p) cudaFree(b.p);
+        surf.clear();
+        img.clear();
+    }
+};
+
+struct BufScratch : FilterScratch {
+    Buffers &b;
+    cudaError_t e = cudaSuccess;
+    explicit BufScratch(Buffers &bb) : b(bb) {}
+    uint32_t *image(uint32_t idx, size_t pixels) override {
+        if (b.img.size() <= idx) b.img.resize(idx + 1);
+        cudaError_t x = b.img[idx].ensure(pixels * 4);
+        if (x != cudaSuccess) e = x;
+        return b.img[idx].as<uint32_t>();
+    }
+    double *plane(size_t n) override {
+        cudaError_t x = b.plane.ensure(n * 8);
+        if (x != cudaSuccess) e = x;
+        return b.plane.as<double>();
     }
 };
 
@@ -94,6 +118,7 @@ struct Buffers {
 struct Plan {
     SceneBuild sb;
     std::vector<WorkItem> items;
+    std::vector<uint32_t> level_off, level_cnt;  // work items per dependency level
     uint32_t px = 8;
     uint64_t nbins = 0;
     uint32_t max_depth = 1;
@@ -194,10 +219,20 @@ int plan_scene(Context &c, Plan &p) {
         st.bin_off = (uint32_t)p.nbins;
         p.nbins += (uint64_t)st.nbands * st.draw_cnt;
         p.max_depth = std::max(p.max_depth, st.max_depth + 1);
-        int32_t cw = (int32_t)((256 / bh) * p.px);
-        for (uint32_t b = 0; b < st.nbands; b++)
-            for (int32_t x0 = 0; x0 < st.out_w; x0 += cw)
-                p.items.push_back(WorkItem{si, b, x0, std::min(x0 + cw, st.out_w)});
+    }
+    p.level_off.assign(sb.max_level + 1, 0);
+    p.level_cnt.assign(sb.max_level + 1, 0);
+    for (uint32_t lv = 0; lv <= sb.max_level; lv++) {
+        p.level_off[lv] = (uint32_t)p.items.size();
+        for (uint32_t si = 0; si < sb.streams.size(); si++) {
+            const StreamRec &st = sb.streams[si];
+            if (st.level != lv) continue;
+            int32_t cw = (int32_t)((256 / st.band_rows) * p.px);
+            for (uint32_t b = 0; b < st.nbands; b++)
+                for (int32_t x0 = 0; x0 < st.out_w; x0 += cw)
+                    p.items.push_back(WorkItem{si, b, x0, std::min(x0 + cw, st.out_w)});
+        }
+        p.level_cnt[lv] = (uint32_t)p.items.size() - p.level_off[lv];
     }
     if (p.nbins > 0xF0000000ull) { set_error("too many (band, draw) bins"); return RGPU_ERR_CAPACITY; }
     uint32_t per_sm = (uint32_t)raster_max_blocks_per_sm((int)p.px);
@@ -207,6 +242,13 @@ int plan_scene(Context &c, Plan &p) {
 
 int upload_plan(Context &c, Buffers &b, Plan &p, cudaStream_t s) {
     SceneBuild &sb = p.sb;
+    if (b.surf.size() < sb.surfaces.size()) b.surf.resize(sb.surfaces.size());
+    for (size_t i = 0; i < sb.surfaces.size(); i++)
+        CK(b.surf[i].ensure((size_t)sb.surfaces[i].w * sb.surfaces[i].h * 4));
+    for (auto &st : sb.streams)
+        if (st.surface >= 0) st.out_ptr = (uint64_t)(uintptr_t)b.surf[st.surface].p;
+    for (auto &L : sb.layers)
+        if (L.surf >= 0) L.buf = (uint64_t)(uintptr_t)b.surf[L.surf].p;
     auto rup = [](size_t n) { return (n + 255) & ~(size_t)255; };
     size_t stage = rup(sb.verbs.size()) + rup(sb.pts.size() * 4) + rup(sb.draws.size() * sizeof(DrawRec)) +
                    rup(sb.paints.size() * sizeof(PaintRec)) + rup(sb.grads.size() * sizeof(GradRec)) +
@@ -239,7 +281,7 @@ int upload_plan(Context &c, Buffers &b, Plan &p, cudaStream_t s) {
     CK(b.stack.ensure((size_t)p.grid * stack_words * 4));
     CK(b.span_ovf.ensure((size_t)p.grid * raster_threads() * ovf_cap * 8));
     CK(b.err.ensure(16));
-    CK(b.counter.ensure(16));
+    CK(b.counter.ensure(4 * (sb.max_level + 1)));
     return RGPU_OK;
 }
 
@@ -290,15 +332,31 @@ int enqueue_plan(Context &c, Buffers &b, Plan &p, cudaStream_t s, cudaEvent_t ev
     CK(launch_bin(true, b.edges.as<EdgeRec>(), b.edge_draw.as<uint32_t>(), nedges, b.draws.as<DrawRec>(),
                   b.streams.as<StreamRec>(), b.bin_counts.as<uint32_t>(), b.bin_offsets.as<uint32_t>(), p.nbinned,
                   b.err.as<uint32_t>(), b.bins.as<EdgeRec>(), s));
-    CK(cudaMemsetAsync(b.counter.p, 0, 4, s));
+    CK(cudaMemsetAsync(b.counter.p, 0, 4 * (sb.max_level + 1), s));
+    for (const auto &st : sb.streams)
+        if (st.surface >= 0) CK(cudaMemsetAsync(b.surf[st.surface].p, 0, (size_t)st.out_w * st.out_h * 4, s));
     const uint32_t ovf_cap = 64;
-    if (ev0) CK(cudaEventRecord(ev0, s));
-    CK(launch_raster((int)p.px, p.grid, p.max_depth, b.streams.as<StreamRec>(), b.items.as<WorkItem>(),
-                     (uint32_t)p.items.size(), b.counter.as<uint32_t>(), b.cmds.as<Cmd>(), b.draws.as<DrawRec>(),
-                     b.paints.as<PaintRec>(), b.grads.as<GradRec>(), b.layers.as<LayerRec>(), b.bins.as<EdgeRec>(),
-                     b.bin_offsets.as<uint32_t>(), b.bin_counts.as<uint32_t>(), b.stack.as<uint32_t>(),
-                     b.span_ovf.as<int2>(), ovf_cap, b.err.as<uint32_t>(), s));
-    if (ev1) CK(cudaEventRecord(ev1, s));
+    BufScratch scratch(b);
+    for (uint32_t lv = 0; lv <= sb.max_level; lv++) {
+        bool last = lv == sb.max_level;
+        if (ev0 && last) CK(cudaEventRecord(ev0, s));
+        if (p.level_cnt[lv])
+            CK(launch_raster((int)p.px, p.grid, p.max_depth, b.streams.as<StreamRec>(),
+                             b.items.as<WorkItem>() + p.level_off[lv], p.level_cnt[lv], b.counter.as<uint32_t>() + lv,
+                             b.cmds.as<Cmd>(), b.draws.as<DrawRec>(), b.paints.as<PaintRec>(), b.grads.as<GradRec>(),
+                             b.layers.as<LayerRec>(), b.bins.as<EdgeRec>(), b.bin_offsets.as<uint32_t>(),
+                             b.bin_counts.as<uint32_t>(), b.stack.as<uint32_t>(), b.span_ovf.as<int2>(), ovf_cap,
+                             b.err.as<uint32_t>(), s));
+        if (ev1 && last) CK(cudaEventRecord(ev1, s));
+        for (const auto &job : sb.jobs) {
+            if (job.level != lv) continue;
+            std::string ferr;
+            int r = run_filter_job(job, b.surf[job.content].as<uint32_t>(), b.surf[job.result].as<uint32_t>(), scratch,
+                                   s, ferr);
+            if (scratch.e != cudaSuccess) CK(scratch.e);
+            if (r) { set_error("filter: %s", ferr.c_str()); return r; }
+        }
+    }
     g_stats.draws += ndraws;
     g_stats.work_items += p.items.size();
     g_stats.kernel_launches += 13;
@@ -620,6 +678,69 @@ int rgpu_get_tuning(rgpu_tuning *t) {
 int rgpu_get_stats(rgpu_stats *s) {
     if (!s) return RGPU_ERR_INVALID_ARG;
     *s = g_stats;
+    return RGPU_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- filter kernels on caller images
+static DevBuf g_ftmp;
+static DevBuf g_fplane;
+
+extern "C" {
+
+int rgpu_filter_box_blur(uint8_t *img, uint32_t w, uint32_t h, double sx, double sy, void *stream) {
+    g_last_error.clear();
+    if (!img || !w || !h) { set_error("invalid arguments"); return RGPU_ERR_INVALID_ARG; }
+    Context &c = ctx();
+    std::lock_guard<std::mutex> lock(c.mu);
+    int r = ensure_device(c);
+    if (r) return r;
+    cudaStream_t s = stream ? (cudaStream_t)stream : c.stream;
+    CK(g_ftmp.ensure((size_t)w * h * 4));
+    CK(filter_box_blur((uint32_t *)img, g_ftmp.as<uint32_t>(), (int)w, (int)h, sx, sy, s));
+    CK(cudaStreamSynchronize(s));
+    return RGPU_OK;
+}
+
+int rgpu_filter_iir_blur(uint8_t *img, uint32_t w, uint32_t h, double sx, double sy, void *stream) {
+    g_last_error.clear();
+    if (!img || !w || !h) { set_error("invalid arguments"); return RGPU_ERR_INVALID_ARG; }
+    Context &c = ctx();
+    std::lock_guard<std::mutex> lock(c.mu);
+    int r = ensure_device(c);
+    if (r) return r;
+    cudaStream_t s = stream ? (cudaStream_t)stream : c.stream;
+    CK(g_fplane.ensure((size_t)w * h * 8));
+    CK(filter_iir_blur((uint32_t *)img, g_fplane.as<double>(), (int)w, (int)h, sx, sy, s));
+    CK(cudaStreamSynchronize(s));
+    return RGPU_OK;
+}
+
+int rgpu_filter_morphology(uint8_t *img, uint32_t w, uint32_t h, int dilate, float rx, float ry, void *stream) {
+    g_last_error.clear();
+    if (!img || !w || !h || !(rx > 0) || !(ry > 0)) { set_error("invalid arguments"); return RGPU_ERR_INVALID_ARG; }
+    Context &c = ctx();
+    std::lock_guard<std::mutex> lock(c.mu);
+    int r = ensure_device(c);
+    if (r) return r;
+    cudaStream_t s = stream ? (cudaStream_t)stream : c.stream;
+    CK(g_ftmp.ensure((size_t)w * h * 4));
+    CK(filter_morphology((uint32_t *)img, g_ftmp.as<uint32_t>(), (int)w, (int)h, dilate != 0, rx, ry, s));
+    CK(cudaStreamSynchronize(s));
+    return RGPU_OK;
+}
+
+int rgpu_filter_color_space(uint8_t *img, uint32_t w, uint32_t h, int to_linear, void *stream) {
+    g_last_error.clear();
+    if (!img || !w || !h) { set_error("invalid arguments"); return RGPU_ERR_INVALID_ARG; }
+    Context &c = ctx();
+    std::lock_guard<std::mutex> lock(c.mu);
+    int r = ensure_device(c);
+    if (r) return r;
+    cudaStream_t s = stream ? (cudaStream_t)stream : c.stream;
+    CK(filter_color_space((uint32_t *)img, (size_t)w * h, to_linear != 0, s));
+    CK(cudaStreamSynchronize(s));
     return RGPU_OK;
 }
 

@@ -34,4 +34,21 @@ cudaError_t launch_raster(int px, uint32_t grid, uint32_t stack_depth, const Str
                           uint32_t ovf_cap, uint32_t *err, cudaStream_t s);
 int raster_max_blocks_per_sm(int px);
 
+// filters.cu
+cudaError_t filter_color_space(uint32_t *img, size_t n, bool to_linear, cudaStream_t s);
+void box_sizes(float sigma, int sizes[5]);
+cudaError_t filter_box_blur(uint32_t *img, uint32_t *tmp, int w, int h, double sx, double sy, cudaStream_t s);
+cudaError_t filter_iir_blur(uint32_t *img, double *buf, int w, int h, double sx, double sy, cudaStream_t s);
+cudaError_t filter_color_matrix(uint32_t *img, size_t n, int kind, const float *values, cudaStream_t s);
+cudaError_t filter_morphology(uint32_t *img, uint32_t *tmp, int w, int h, bool dilate, float rx, float ry,
+                              cudaStream_t s);
+cudaError_t filter_arithmetic(const uint32_t *a, const uint32_t *b, uint32_t *dst, size_t n, const float k[4],
+                              cudaStream_t s);
+cudaError_t filter_copy(const uint32_t *src, uint32_t *dst, size_t n, cudaStream_t s);
+cudaError_t filter_crop(uint32_t *img, int w, int h, int l, int t, int r, int b, cudaStream_t s);
+cudaError_t filter_draw(const uint32_t *src, uint32_t *dst, int w, int h, int dx, int dy, uint32_t blend,
+                        cudaStream_t s);
+cudaError_t filter_fill(uint32_t *img, size_t n, uint32_t v, cudaStream_t s);
+cudaError_t filter_alpha_only(uint32_t *img, size_t n, cudaStream_t s);
+
 }  // namespace rgpu

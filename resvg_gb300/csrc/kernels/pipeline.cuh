@@ -58,7 +58,7 @@ __device__ __forceinline__ void lowp_blend(uint32_t blend, const uint16_t s[4], 
 
 __device__ __forceinline__ float hinv(float v) { return 1.0f - v; }
 
-__device__ __noinline__ float4 blend_generic(uint32_t mode, float4 sv, float4 dv) {
+static __device__ __noinline__ float4 blend_generic(uint32_t mode, float4 sv, float4 dv) {
     const float s[4] = {sv.x, sv.y, sv.z, sv.w}, d[4] = {dv.x, dv.y, dv.z, dv.w};
     float o[4];
     float sa = s[3], da = d[3];

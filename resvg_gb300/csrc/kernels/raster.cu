@@ -26,10 +26,10 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kXCap = 40;        // crossings held per thread before the exact slow path
-constexpr int kSpanCap = 12;     // spans per (slot, sub-scanline) kept in shared memory
+constexpr int kSpanCap = 8;      // spans per (slot, sub-scanline) kept in shared memory
 constexpr int kMaxDepth = 48;    // layer stack depth
 
-constexpr int kMaxSlots = 64;   // draws per phase-A window (S >= 4 scanlines each)
+constexpr int kMaxSlots = 32;   // draws per phase-A window
 
 struct VmShared {
     int32_t win_first;           // first command index of the prepared window
@@ -40,6 +40,8 @@ struct VmShared {
     int2 spans[kThreads * kSpanCap];
     int4 rects[kMaxDepth];       // layer-stack rects (x, y, w, h), uniform across the CTA
     PaintRec paint[kMaxSlots];   // paints of the window's draws
+    int4 slot_geo[kMaxSlots];    // (valid | shift << 1, ox, oy, unused) per slot
+    int4 slot_sect[kMaxSlots];   // coverage rect (l, t, r, b) per slot
     int32_t grad_slot[kMaxSlots];// index into grad[] or -1
     GradRec grad[kMaxSlots];     // gradients of the window's draws
     int32_t item;
@@ -52,14 +54,23 @@ __device__ __forceinline__ int32_t round16(int32_t x) { return (int32_t)((uint32
 // search when a sub-scanline has more than kXCap crossings.
 struct Crossing { int32_t x; int32_t w; };
 
+// Spans of one (slot, scanline) live in shared memory while they fit; a
+// longer list moves as a whole to the per-CTA global overflow area.
 __device__ void store_span(VmShared &sh, int2 *ovf, uint32_t ovf_cap, int slot_j, int idx, int32_t L, int32_t R,
                            uint32_t *err) {
-    if (idx < kSpanCap) sh.spans[slot_j * kSpanCap + idx] = make_int2(L, R);
-    else if ((uint32_t)(idx - kSpanCap) < ovf_cap) ovf[(size_t)slot_j * ovf_cap + (idx - kSpanCap)] = make_int2(L, R);
+    int2 *o = ovf + (size_t)slot_j * ovf_cap;
+    if (idx < kSpanCap) {
+        sh.spans[slot_j * kSpanCap + idx] = make_int2(L, R);
+        return;
+    }
+    if (idx == kSpanCap)
+        for (int k = 0; k < kSpanCap; k++) o[k] = sh.spans[slot_j * kSpanCap + k];
+    if ((uint32_t)idx < ovf_cap) o[idx] = make_int2(L, R);
     else atomicOr(err, 2u);
 }
-__device__ __forceinline__ int2 load_span(const VmShared &sh, const int2 *ovf, uint32_t ovf_cap, int slot_j, int idx) {
-    return idx < kSpanCap ? sh.spans[slot_j * kSpanCap + idx] : ovf[(size_t)slot_j * ovf_cap + (idx - kSpanCap)];
+__device__ __forceinline__ const int2 *span_base(const VmShared &sh, const int2 *ovf, uint32_t ovf_cap, int slot_j,
+                                                 int n) {
+    return n <= kSpanCap ? &sh.spans[slot_j * kSpanCap] : ovf + (size_t)slot_j * ovf_cap;
 }
 
 // Phase A for one (draw, scanline): spans into slot `sj`.  
@@ -124,20 +135,21 @@ __device__ void phase_a(VmShared &sh, int sj, const DrawRec &dr, int32_t y, cons
         }
     }
     if ((w & mask) != 0 && right_clip > left) emit(left, right_clip);
-    sh.span_cnt[sj] = (uint16_t)min(nspans, kSpanCap + (int)ovf_cap);
+    sh.span_cnt[sj] = (uint16_t)min(nspans, (int)ovf_cap);
 }
 
 
-// Coverage of pixel `lx` (layer coordinates) on one scanline's span list,
-// starting from cursor q (spans before q end left of the warp's window).
-__device__ __forceinline__ uint32_t span_cov(const VmShared &sh, const int2 *ovf, uint32_t ovf_cap, int sj, int n,
-                                             int &q, int32_t w0, int32_t w1, int32_t p0, uint32_t maxv) {
-    while (q < n && load_span(sh, ovf, ovf_cap, sj, q).y <= w0) q++;
+// Coverage contribution of one scanline's spans to pixel sub-column range
+// [p0, p0+4), for the warp window [w0, w1); `q` is a cursor past spans that
+// end left of the window (windows advance left to right).
+__device__ __forceinline__ uint32_t span_cov(const int2 *L, int n, int &q, int32_t w0, int32_t w1, int32_t p0,
+                                             uint32_t maxv) {
+    while (q < n && L[q].y <= w0) q++;
     uint32_t cov = 0;
     for (int k = q; k < n; k++) {
-        int2 sp = load_span(sh, ovf, ovf_cap, sj, k);
-        if (sp.x >= w1) break;
-        int32_t ov = min(sp.y, p0 + 4) - max(sp.x, p0);
+        const int2 a = L[k];
+        if (a.x >= w1) break;
+        const int32_t ov = min(a.y, p0 + 4) - max(a.x, p0);
         if (ov > 0) cov += ov == 4 ? maxv : (uint32_t)ov * 16u;
     }
     return cov;
@@ -225,9 +237,12 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
                     }
                     __syncthreads();
                     if (tid < sh.nslots) {
-                        const PaintRec &pr = paints[draws[cmds[st.cmd_off + sh.slot_cmd[tid]].a].paint];
+                        const DrawRec &d = draws[cmds[st.cmd_off + sh.slot_cmd[tid]].a];
+                        const PaintRec &pr = paints[d.paint];
                         sh.paint[tid] = pr;
                         sh.grad_slot[tid] = pr.kind == 1 ? tid : -1;
+                        sh.slot_geo[tid] = make_int4((d.valid ? 1 : 0) | (d.shift ? 2 : 0), d.ox, d.oy, 0);
+                        sh.slot_sect[tid] = make_int4(d.sect_l, d.sect_t, d.sect_r, d.sect_b);
                     }
                     __syncthreads();
                     // stage the window's gradients cooperatively
@@ -259,48 +274,62 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
                 }
                 // ---- phase B: coverage + shading, one pixel per (thread, i)
                 const int slot = slot_next++;
-                const DrawRec dr = draws[c.a];
-                if (!dr.valid && c.op == CMD_FILL) continue;
-                const int32_t ly = cy - dr.oy;
-                const int32_t lrow0 = (int32_t)wi.band * BH - dr.oy;
-                const bool row_in = dr.valid && row_ok && ly >= dr.sect_t && ly < dr.sect_b;
+                const int4 geo = sh.slot_geo[slot];
+                const bool dvalid = geo.x & 1, aa = geo.x & 2;
+                if (!dvalid && c.op == CMD_FILL) continue;
+                const int4 sect = sh.slot_sect[slot];
+                const int32_t ox = geo.y, oy = geo.z;
+                const int32_t ly = cy - oy;
+                const int32_t lrow0 = (int32_t)wi.band * BH - oy;
+                const bool row_in = dvalid && row_ok && ly >= sect.y && ly < sect.w;
                 if (c.op == CMD_FILL && !row_in) continue;
                 const PaintRec &pr = sh.paint[slot];
                 const GradRec *gr = sh.grad_slot[slot] >= 0 ? &sh.grad[sh.grad_slot[slot]] : &grads[pr.grad];
-                int cur[4] = {0, 0, 0, 0};
-                const int sj0 = slot * S + (ly - lrow0) * (dr.shift ? 4 : 1);
-                int ncnt[4];
+                const int nsl = aa ? 4 : 1;
+                const int sj0 = slot * S + (ly - lrow0) * nsl;
+                const int2 *sp[4];
+                int ns[4], cur[4] = {0, 0, 0, 0};
+                int32_t rowL = INT32_MAX, rowR = INT32_MIN;
                 if (row_in) {
-                    if (dr.shift) {
-                        for (int s = 0; s < 4; s++) ncnt[s] = sh.span_cnt[sj0 + s];
-                    } else {
-                        ncnt[0] = sh.span_cnt[sj0];
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        ns[q] = 0;
+                        sp[q] = nullptr;
+                        if (q < nsl) {
+                            ns[q] = sh.span_cnt[sj0 + q];
+                            sp[q] = span_base(sh, ovf, ovf_cap, sj0 + q, ns[q]);
+                            if (ns[q]) { rowL = min(rowL, sp[q][0].x); rowR = max(rowR, sp[q][ns[q] - 1].y); }
+                        }
                     }
                 }
+                if (c.op == CMD_FILL && rowL >= rowR) continue;  // no span on this row
+                const int sub = aa ? 2 : 0;  // sub-column shift
 #pragma unroll 1
                 for (int i = 0; i < PX; i++) {
                     const int32_t x = wi.x0 + i * tpr + lr;
-                    const int32_t lx = x - dr.ox;
+                    const int32_t lx = x - ox;
                     uint32_t cv = 0;
-                    if (row_in) {
-                        const int32_t wx = wi.x0 + i * tpr + (lr & ~31) - dr.ox;  // warp window start (layer x)
-                        if (dr.shift) {
-                            const int32_t w0 = wx << 2, w1 = (wx + 32) << 2, p0 = lx << 2;
-#pragma unroll
-                            for (int s = 0; s < 4; s++)
-                                cv += span_cov(sh, ovf, ovf_cap, sj0 + s, ncnt[s], cur[s], w0, w1, p0, s == 3 ? 63u : 64u);
+                    const int32_t wx = wi.x0 + i * tpr + (lr & ~31) - ox;  // warp window start (layer x)
+                    const int32_t w0 = wx << sub, w1 = (wx + 32) << sub;
+                    if (row_in && w1 > rowL && w0 < rowR) {
+                        if (aa) {
+                            const int32_t p0 = lx << 2;
+                            cv = span_cov(sp[0], ns[0], cur[0], w0, w1, p0, 64u) +
+                                 span_cov(sp[1], ns[1], cur[1], w0, w1, p0, 64u) +
+                                 span_cov(sp[2], ns[2], cur[2], w0, w1, p0, 64u) +
+                                 span_cov(sp[3], ns[3], cur[3], w0, w1, p0, 63u);
+                            cv = min(cv, 255u);
                         } else {
                             int q = cur[0];
-                            while (q < ncnt[0] && load_span(sh, ovf, ovf_cap, sj0, q).y <= wx) q++;
+                            while (q < ns[0] && sp[0][q].y <= w0) q++;
                             cur[0] = q;
-                            for (int k2 = q; k2 < ncnt[0]; k2++) {
-                                int2 sp = load_span(sh, ovf, ovf_cap, sj0, k2);
-                                if (sp.x >= wx + 32) break;
-                                if (lx >= sp.x && lx < sp.y) cv = 255;
+                            for (int k2 = q; k2 < ns[0]; k2++) {
+                                const int2 a2 = sp[0][k2];
+                                if (a2.x >= w1) break;
+                                if (lx >= a2.x && lx < a2.y) cv = 255;
                             }
                         }
-                        cv = min(cv, 255u);
-                        if (lx < dr.sect_l || lx >= dr.sect_r) cv = 0;
+                        if (lx < sect.x || lx >= sect.z) cv = 0;
                     }
                     uint32_t &px = layer[i * kThreads + tid];
                     if (c.op == CMD_FILL) {
@@ -327,9 +356,13 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
                 top_x = L.x; top_y = L.y; top_w = L.w; top_h = L.h;
                 const uint32_t init = c.b == 1 ? 0xFF000000u : 0u;
                 const bool row_in = cy >= top_y && cy < top_y + top_h;
+                const uint32_t *src = (c.b == 2 && L.buf) ? (const uint32_t *)(uintptr_t)L.buf : nullptr;
                 for (int i = 0; i < PX; i++) {
                     const int32_t x = wi.x0 + i * tpr + lr;
-                    layer[i * kThreads + tid] = (row_in && x >= top_x && x < top_x + top_w) ? init : 0u;
+                    uint32_t v = 0u;
+                    if (row_in && x >= top_x && x < top_x + top_w)
+                        v = src ? src[(size_t)(cy - top_y) * top_w + (x - top_x)] : init;
+                    layer[i * kThreads + tid] = v;
                 }
             } else if (c.op == CMD_POP_COMPOSITE || c.op == CMD_POP_CLIP || c.op == CMD_POP_MASK) {
                 if (depth == 0) { atomicOr(err, 4u); break; }

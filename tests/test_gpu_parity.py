@@ -125,3 +125,16 @@ def test_clip_and_mask(gpu, oracle_mod):
     g, o = _both(t, 300, 300, (1.5, 0, 0, 1.5, 0, 0))
     n, mx = diff_stats(g, o)
     assert mx <= 1, "%d px differ (max %d)" % (n, mx)
+
+
+@pytest.mark.parametrize("index", [0, 1, 2, 3, 5, 8, 13, 21])
+def test_config3_scenes(gpu, oracle_mod, index):
+    """Scenes of the batched workload (sizes 64..1024, 10..2000 paths, 10% with
+    clip + blur) rendered one at a time through resvg_render."""
+    t = R.Tree.generate(3, seed=2026, index=index)
+    w, h = (int(v) for v in t.size)
+    if w * h * t.view().contents.path_count > 3e8:
+        pytest.skip("scene too large for a quick oracle render")
+    g, o = _both(t, w, h)
+    n, mx = diff_stats(g, o)
+    assert mx <= 1, "%d px differ (max %d)" % (n, mx)
