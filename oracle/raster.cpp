@@ -1331,7 +1331,8 @@ static bool gradient_setup(const Shader &sh, GradientCtx &g) {
 
 // Evaluate a gradient at device pixel (x, y): premultiplied f32 colour.
 // Returns false when the pixel is masked out (degenerate conical region).
-static bool gradient_eval(const GradientCtx &g, uint32_t spread, int32_t px, int32_t py, ColorF *out) {
+static bool gradient_eval(const GradientCtx &g, uint32_t spread, int32_t px, int32_t py, ColorF *out,
+                          bool premul_stage = true) {
     float x = (float)px + 0.5f, y = (float)py + 0.5f;
     const Transform &ts = g.ts;
     float tx = x * ts.sx + y * ts.kx + ts.tx;
@@ -1382,9 +1383,25 @@ static bool gradient_eval(const GradientCtx &g, uint32_t spread, int32_t px, int
         const ColorF &f = g.factors[idx], &b = g.biases[idx];
         c = ColorF{t * f.r + b.r, t * f.g + b.g, t * f.b + b.b, t * f.a + b.a};
     }
-    if (g.premul) { c.r *= c.a; c.g *= c.a; c.b *= c.a; }
+    if (g.premul && premul_stage) { c.r *= c.a; c.g *= c.a; c.b *= c.a; }
     *out = c;
     return true;
+}
+
+// lowp gradient colour (pipeline/lowp.rs): the f32 stop interpolation is
+// clamped, rounded to u16 by truncating v * 255 + 0.5, and premultiplied
+// with div255 when the stops are not opaque.  Linear and simple radial
+// gradients only (the two-point conical stages exist in highp alone).
+static void gradient_eval_lowp(const GradientCtx &g, uint32_t spread, int32_t px, int32_t py, uint16_t out[4]) {
+    ColorF c;
+    gradient_eval(g, spread, px, py, &c, false);
+    float v[4] = {c.r, c.g, c.b, c.a};
+    for (int i = 0; i < 4; i++) {
+        float x = std::min(std::max(v[i], 0.0f), 1.0f) * 255.0f + 0.5f;
+        out[i] = (uint16_t)x;
+    }
+    if (g.premul)
+        for (int i = 0; i < 3; i++) out[i] = (uint16_t)(((uint32_t)out[i] * out[3] + 255) >> 8);
 }
 
 // highp blend (pipeline/highp.rs).  s/d are premultiplied f32.
@@ -1470,11 +1487,13 @@ static void blend_sep(uint32_t mode, const float s[4], const float d[4], float o
             float diff = l - lum(r, g, b);
             r += diff; g += diff; b += diff;
         };
+        // pulls channels above `a` towards the luminance and clamps negatives
+        // to zero; there is no separate pull-up of a negative minimum (pinned
+        // against resvg's mix-blend-mode goldens).
         auto clip_color = [&](float &r, float &g, float &b, float a) {
-            float mn = std::min({r, g, b}), mx = std::max({r, g, b});
+            float mx = std::max({r, g, b});
             float l = lum(r, g, b);
             auto clip = [&](float c) {
-                if (mn < 0.0f && l - mn != 0.0f) c = l + (c - l) * l / (l - mn);
                 if (mx > a && mx - l != 0.0f) c = l + (c - l) * (a - l) / (mx - l);
                 return std::max(c, 0.0f);
             };
@@ -1546,8 +1565,11 @@ struct PipelineBlitter {
             memset_ok = true;
             memset_color[0] = memset_color[1] = memset_color[2] = memset_color[3] = 0;
         }
-        // lowp is possible for a solid colour with the blend modes resvg fills with.
-        lowp = paint.shader.kind == SHADER_SOLID &&
+        // lowp is possible for a solid colour, a linear or a simple radial
+        // gradient, with the blend modes resvg fills with.
+        bool lowp_shader = paint.shader.kind == SHADER_SOLID || paint.shader.kind == SHADER_LINEAR ||
+                           (paint.shader.kind == SHADER_RADIAL && grad.radial_simple);
+        lowp = lowp_shader &&
                (blend == RGPU_BLEND_SOURCE || blend == RGPU_BLEND_SOURCE_OVER || blend == RGPU_BLEND_CLEAR ||
                 blend == RGPU_BLEND_DESTINATION_OUT || blend == RGPU_BLEND_XOR || blend == RGPU_BLEND_SOURCE_ATOP ||
                 blend == RGPU_BLEND_PLUS || blend == RGPU_BLEND_MODULATE || blend == RGPU_BLEND_SCREEN);
@@ -1579,6 +1601,7 @@ struct PipelineBlitter {
         if (cov == 255 && memset_ok) { memcpy(p, memset_color, 4); return; }
         if (lowp) {
             uint16_t s[4] = {rgba16[0], rgba16[1], rgba16[2], rgba16[3]};
+            if (shader->kind != SHADER_SOLID) gradient_eval_lowp(grad, shader->spread, x, y, s);
             uint16_t d[4] = {p[0], p[1], p[2], p[3]};
             uint16_t o[4];
             if (cov == 255) {
@@ -1705,7 +1728,8 @@ Mask mask_from_pixmap(const Pixmap &pm, bool luminance) {
         if (!luminance) { m.data[i] = p[3]; continue; }
         float r = p[0] / 255.0f, g = p[1] / 255.0f, b = p[2] / 255.0f, a = p[3] / 255.0f;
         if (p[3] != 0) { r /= a; g /= a; b /= a; }
-        float luma = r * 0.2125f + g * 0.7154f + b * 0.0721f;
+        // Rec. 709 luma coefficients (tiny-skia mask.rs from_pixmap)
+        float luma = r * 0.2126f + g * 0.7152f + b * 0.0722f;
         float v = std::ceil(std::min(std::max((luma * a) * 255.0f, 0.0f), 255.0f));
         m.data[i] = sat_u8(v);
     }

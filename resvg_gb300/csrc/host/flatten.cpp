@@ -232,7 +232,11 @@ struct Flattener {
             memset_ok = true;
             std::memset(pr.memset_rgba, 0, 4);
         }
-        bool lowp = sh.kind == SH_SOLID &&
+        // tiny-skia runs a solid colour, a linear or a simple radial gradient
+        // in the lowp pipeline (two-point conical stages are highp only).
+        bool lowp_shader = sh.kind == SH_SOLID || sh.kind == SH_LINEAR ||
+                           (sh.kind == SH_RADIAL && (sb.grads.back().flags & GRAD_RADIAL_SIMPLE));
+        bool lowp = lowp_shader &&
                     (blend == RGPU_BLEND_SOURCE || blend == RGPU_BLEND_SOURCE_OVER || blend == RGPU_BLEND_CLEAR ||
                      blend == RGPU_BLEND_DESTINATION_OUT || blend == RGPU_BLEND_XOR || blend == RGPU_BLEND_SOURCE_ATOP ||
                      blend == RGPU_BLEND_PLUS || blend == RGPU_BLEND_MODULATE || blend == RGPU_BLEND_SCREEN);

@@ -317,126 +317,4 @@ bool tight_bounds(const uint8_t *verbs, size_t nv, const float *pts, size_t npts
     return true;
 }
 
-bool stroke_path(const uint8_t *verbs, size_t nv, const float *pts, size_t npts, const StrokeStyle &st,
-                 float res_scale, PathData &out) {
-    (void)npts;
-    if (!(st.width > 0) || !std::isfinite(st.width)) return false;
-    double hw = st.width * 0.5;
-    double tol = 0.02 / std::max(res_scale, 1e-6f);
-    std::vector<Poly> polys = flatten(verbs, nv, pts, tol);
-    Out o{out};
-    for (auto &pl0 : polys) {
-        Poly pl = pl0;
-        if (!pl.has_seg) continue;
-        dedupe(pl);
-        if (pl.p.size() == 1) {
-            // zero-length contour: round/square caps draw a dot/square
-            if (st.cap == 0) continue;
-            V2 c = pl.p[0];
-            std::vector<V2> poly;
-            if (st.cap == 1) {
-                poly.push_back(c + V2{hw, 0});
-                arc(poly, c, V2{1, 0}, V2{1, 0}, hw, 1, tol);
-            } else {
-                poly = {c + V2{-hw, -hw}, c + V2{hw, -hw}, c + V2{hw, hw}, c + V2{-hw, hw}};
-            }
-            o.move(poly[0]);
-            for (size_t i = 1; i < poly.size(); i++) o.line(poly[i]);
-            o.close();
-            continue;
-        }
-        if (pl.closed && pl.p.size() < 3) pl.closed = false;
-        if (pl.closed) {
-            std::vector<V2> outer, inner;
-            offset_side(pl, hw, st, tol, 1.0, outer);
-            offset_side(pl, hw, st, tol, -1.0, inner);
-            o.move(outer[0]);
-            for (size_t i = 1; i < outer.size(); i++) o.line(outer[i]);
-            o.close();
-            o.move(inner.back());
-            for (size_t i = inner.size() - 1; i-- > 0;) o.line(inner[i]);
-            o.close();
-        } else {
-            std::vector<V2> left, right;
-            offset_side(pl, hw, st, tol, 1.0, left);
-            offset_side(pl, hw, st, tol, -1.0, right);
-            std::vector<V2> ring;
-            ring.insert(ring.end(), left.begin(), left.end());
-            size_t n = pl.p.size();
-            V2 dend = norm(pl.p[n - 1] - pl.p[n - 2]);
-            // end cap from left side to right side
-            {
-                std::vector<V2> cap;
-                V2 p = pl.p[n - 1];
-                V2 nl = perp(dend) * hw;
-                if (st.cap == 1) arc(cap, p, norm(nl), norm(nl * -1.0), hw, cross(nl, dend) >= 0 ? -1 : 1, tol);
-                else if (st.cap == 2) { cap.push_back(p + nl + dend * hw); cap.push_back(p - nl + dend * hw); }
-                ring.insert(ring.end(), cap.begin(), cap.end());
-            }
-            for (size_t i = right.size(); i-- > 0;) ring.push_back(right[i]);
-            V2 dst = norm(pl.p[0] - pl.p[1]);
-            {
-                std::vector<V2> cap;
-                V2 p = pl.p[0];
-                V2 nl = perp(dst) * hw;
-                if (st.cap == 1) arc(cap, p, norm(nl), norm(nl * -1.0), hw, cross(nl, dst) >= 0 ? -1 : 1, tol);
-                else if (st.cap == 2) { cap.push_back(p + nl + dst * hw); cap.push_back(p - nl + dst * hw); }
-                ring.insert(ring.end(), cap.begin(), cap.end());
-            }
-            o.move(ring[0]);
-            for (size_t i = 1; i < ring.size(); i++) o.line(ring[i]);
-            o.close();
-        }
-    }
-    return !out.empty();
-}
-
-bool dash_path(const uint8_t *verbs, size_t nv, const float *pts, size_t npts, const float *dashes, size_t nd,
-               float offset, float res_scale, PathData &out) {
-    (void)npts;
-    if (nd == 0) return false;
-    double total = 0;
-    for (size_t i = 0; i < nd; i++) {
-        if (dashes[i] < 0 || !std::isfinite(dashes[i])) return false;
-        total += dashes[i];
-    }
-    if (!(total > 0)) return false;
-    double tol = 0.02 / std::max(res_scale, 1e-6f);
-    std::vector<Poly> polys = flatten(verbs, nv, pts, tol);
-    for (auto &pl0 : polys) {
-        Poly pl = pl0;
-        std::vector<V2> p = pl.p;
-        if (pl.closed && !p.empty()) p.push_back(p.front());
-        // dash phase
-        double ph = std::fmod((double)offset, total);
-        if (ph < 0) ph += total;
-        size_t di = 0;
-        while (ph >= dashes[di]) { ph -= dashes[di]; di = (di + 1) % nd; }
-        double remain = dashes[di] - ph;
-        bool on = (di % 2) == 0;
-        bool started = false;
-        for (size_t s = 0; s + 1 < p.size(); s++) {
-            V2 a = p[s], b = p[s + 1];
-            double sl = len(b - a), pos = 0;
-            while (sl - pos > 1e-12) {
-                double step = std::min(remain, sl - pos);
-                V2 q0 = a + (b - a) * (pos / sl), q1 = a + (b - a) * ((pos + step) / sl);
-                if (on) {
-                    if (!started) { out.move_to((float)q0.x, (float)q0.y); started = true; }
-                    out.line_to((float)q1.x, (float)q1.y);
-                }
-                pos += step;
-                remain -= step;
-                if (remain <= 1e-12) {
-                    di = (di + 1) % nd;
-                    remain = dashes[di];
-                    on = !on;
-                    started = false;
-                }
-            }
-        }
-    }
-    return true;
-}
-
 }  // namespace rgpu

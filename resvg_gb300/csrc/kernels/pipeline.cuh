@@ -145,11 +145,13 @@ static __device__ __noinline__ float4 blend_generic(uint32_t mode, float4 sv, fl
         float diff = l - lum(r, g, b);
         r += diff; g += diff; b += diff;
     };
+    // tiny-skia's clip_color pulls channels above `a` back towards the
+    // luminance and clamps negatives to zero; it has no separate pull-up of a
+    // negative minimum (pinned against resvg's mix-blend-mode goldens).
     auto clip_color = [&](float a) {
-        float mn = fminf(fminf(r, g), b), mx = fmaxf(fmaxf(r, g), b);
+        float mx = fmaxf(fmaxf(r, g), b);
         float l = lum(r, g, b);
         auto clip = [&](float c) {
-            if (mn < 0.0f && l - mn != 0.0f) c = l + __fdiv_rn((c - l) * l, l - mn);
             if (mx > a && mx - l != 0.0f) c = l + __fdiv_rn((c - l) * (a - l), mx - l);
             return fmaxf(c, 0.0f);
         };
@@ -199,7 +201,8 @@ __device__ __forceinline__ void blend_sep(uint32_t mode, const float *s, const f
 
 // Gradient colour at device pixel (px, py) (premultiplied f32); false when the
 // pixel lies in a two-point-conical region with no circle through it.
-__device__ __forceinline__ bool gradient_eval(const GradRec &g, int32_t px, int32_t py, float *c) {
+__device__ __forceinline__ bool gradient_eval(const GradRec &g, int32_t px, int32_t py, float *c,
+                                              bool premul_stage = true) {
     float x = (float)px + 0.5f, y = (float)py + 0.5f;
     float tx = x * g.ts[0] + y * g.ts[2] + g.ts[4];
     float ty = x * g.ts[1] + y * g.ts[3] + g.ts[5];
@@ -245,8 +248,22 @@ __device__ __forceinline__ bool gradient_eval(const GradRec &g, int32_t px, int3
     }
 #pragma unroll
     for (int k = 0; k < 4; k++) c[k] = t * g.f[idx][k] + g.b[idx][k];
-    if (g.flags & GRAD_PREMUL) { c[0] *= c[3]; c[1] *= c[3]; c[2] *= c[3]; }
+    if ((g.flags & GRAD_PREMUL) && premul_stage) { c[0] *= c[3]; c[1] *= c[3]; c[2] *= c[3]; }
     return true;
+}
+
+// lowp gradient colour (pipeline/lowp.rs gradient / evenly_spaced_2_stop_gradient
+// + premultiply): the f32 interpolation is clamped, rounded to u16 by
+// truncating v * 255 + 0.5, then premultiplied with div255.
+__device__ __forceinline__ void gradient_eval_lowp(const GradRec &g, int32_t px, int32_t py, uint16_t s[4]) {
+    float c[4];
+    gradient_eval(g, px, py, c, false);
+#pragma unroll
+    for (int k = 0; k < 4; k++) s[k] = (uint16_t)(fminf(fmaxf(c[k], 0.0f), 1.0f) * 255.0f + 0.5f);
+    if (g.flags & GRAD_PREMUL) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) s[k] = div255((uint16_t)(s[k] * s[3]));
+    }
 }
 
 __device__ __forceinline__ float4 unpack_f(uint32_t p) {
@@ -263,6 +280,7 @@ __device__ __forceinline__ uint32_t shade_pixel(const PaintRec &pr, const GradRe
     const uint32_t blend = pr.blend;
     if (pr.flags & PAINT_LOWP) {
         uint16_t s[4] = {pr.rgba16[0], pr.rgba16[1], pr.rgba16[2], pr.rgba16[3]};
+        if (pr.kind != 0) gradient_eval_lowp(*grad, lx, ly, s);
         uint16_t d[4] = {(uint16_t)ch(dst, 0), (uint16_t)ch(dst, 1), (uint16_t)ch(dst, 2), (uint16_t)ch(dst, 3)};
         uint16_t o[4];
         if (cov == 255) {
@@ -331,7 +349,8 @@ __device__ __forceinline__ uint32_t mask_value(uint32_t p, bool luminance) {
     float r = (float)ch(p, 0) / 255.0f, g = (float)ch(p, 1) / 255.0f, b = (float)ch(p, 2) / 255.0f;
     float a = (float)a8 / 255.0f;
     if (a8 != 0) { r = __fdiv_rn(r, a); g = __fdiv_rn(g, a); b = __fdiv_rn(b, a); }
-    float luma = r * 0.2125f + g * 0.7154f + b * 0.0721f;
+    // Rec. 709 luma coefficients (tiny-skia mask.rs from_pixmap)
+    float luma = r * 0.2126f + g * 0.7152f + b * 0.0722f;
     float v = ceilf(fminf(fmaxf((luma * a) * 255.0f, 0.0f), 255.0f));
     if (!(v > 0.0f)) return 0;
     if (v >= 255.0f) return 255;

@@ -1,0 +1,1311 @@
+"""SVG-subset front end: parses SVG text into the backend's render tree.
+
+A stand-in for the parts of usvg (crates/usvg/src/parser/**) that produce the
+tree resvg renders: shapes to paths (parser/shapes.rs: rect with rx/ry,
+circle/ellipse as four arcs, line/polyline/polygon), path data with arcs
+converted to cubics the way usvg does it (kurbo's SvgArc -> Arc ->
+to_cubic_beziers(0.1), parser/shapes.rs:276-330), presentation attributes and
+`style`, inheritance, transforms, `use`, gradients with objectBoundingBox units
+and normalised stops (parser/paint_server.rs:277-405), clipPath, mask and the
+filter primitives the backend implements, with usvg's default regions
+(parser/filter.rs:185-214).
+
+Unsupported features raise `Unsupported`; the golden-image harness uses that
+to select the reference tests this front end can express.
+"""
+from __future__ import annotations
+
+import math
+import re
+import xml.etree.ElementTree as ET
+
+import numpy as np
+
+from . import _abi as A
+
+SVG_NS = "{http://www.w3.org/2000/svg}"
+XLINK = "{http://www.w3.org/1999/xlink}href"
+
+
+class Unsupported(Exception):
+    pass
+
+
+# ---------------------------------------------------------------- colours
+NAMED = {
+    "black": (0, 0, 0), "white": (255, 255, 255), "red": (255, 0, 0), "green": (0, 128, 0), "blue": (0, 0, 255),
+    "yellow": (255, 255, 0), "cyan": (0, 255, 255), "aqua": (0, 255, 255), "magenta": (255, 0, 255),
+    "fuchsia": (255, 0, 255), "gray": (128, 128, 128), "grey": (128, 128, 128), "silver": (192, 192, 192),
+    "maroon": (128, 0, 0), "olive": (128, 128, 0), "lime": (0, 255, 0), "teal": (0, 128, 128), "navy": (0, 0, 128),
+    "purple": (128, 0, 128), "orange": (255, 165, 0), "pink": (255, 192, 203), "brown": (165, 42, 42),
+    "gold": (255, 215, 0), "seagreen": (46, 139, 87), "darkgreen": (0, 100, 0), "lightblue": (173, 216, 230),
+    "lightgreen": (144, 238, 144), "darkblue": (0, 0, 139), "darkred": (139, 0, 0), "indigo": (75, 0, 130),
+    "violet": (238, 130, 238), "coral": (255, 127, 80), "salmon": (250, 128, 114), "khaki": (240, 230, 140),
+    "crimson": (220, 20, 60), "chocolate": (210, 105, 30), "tomato": (255, 99, 71), "orchid": (218, 112, 214),
+    "skyblue": (135, 206, 235), "steelblue": (70, 130, 180), "springgreen": (0, 255, 127),
+    "mediumseagreen": (60, 179, 113), "forestgreen": (34, 139, 34), "limegreen": (50, 205, 50),
+    "darkgray": (169, 169, 169), "darkgrey": (169, 169, 169), "lightgray": (211, 211, 211),
+    "lightgrey": (211, 211, 211), "whitesmoke": (245, 245, 245), "beige": (245, 245, 220),
+    "turquoise": (64, 224, 208), "royalblue": (65, 105, 225), "slateblue": (106, 90, 205),
+    "darkorange": (255, 140, 0), "goldenrod": (218, 165, 32), "peru": (205, 133, 63), "plum": (221, 160, 221),
+    "tan": (210, 180, 140), "wheat": (245, 222, 179), "ivory": (255, 255, 240), "lavender": (230, 230, 250),
+    "mintcream": (245, 255, 250), "honeydew": (240, 255, 240), "azure": (240, 255, 255),
+}
+
+
+def parse_color(s: str, current=(0, 0, 0)):
+    """Returns ((r, g, b), alpha) or None for 'none'."""
+    s = s.strip()
+    low = s.lower()
+    if low == "none":
+        return None
+    if low == "transparent":
+        return (0, 0, 0), 0.0
+    if low == "currentcolor":
+        return current, 1.0
+    if low in NAMED:
+        return NAMED[low], 1.0
+    if s.startswith("#"):
+        h = s[1:]
+        if len(h) == 3:
+            return tuple(int(c * 2, 16) for c in h), 1.0
+        if len(h) == 4:
+            return tuple(int(c * 2, 16) for c in h[:3]), int(h[3] * 2, 16) / 255.0
+        if len(h) == 6:
+            return (int(h[0:2], 16), int(h[2:4], 16), int(h[4:6], 16)), 1.0
+        if len(h) == 8:
+            return (int(h[0:2], 16), int(h[2:4], 16), int(h[4:6], 16)), int(h[6:8], 16) / 255.0
+        raise Unsupported("color " + s)
+    m = re.match(r"rgba?\(([^)]*)\)", low)
+    if m:
+        parts = [p.strip() for p in re.split(r"[,\s/]+", m.group(1).strip()) if p.strip()]
+        vals = []
+        for p in parts[:3]:
+            if p.endswith("%"):
+                vals.append(int(round(float(p[:-1]) * 2.55)))
+            else:
+                vals.append(int(round(float(p))))
+        vals = [max(0, min(255, v)) for v in vals]
+        a = 1.0
+        if len(parts) > 3:
+            a = float(parts[3][:-1]) / 100 if parts[3].endswith("%") else float(parts[3])
+        return tuple(vals), max(0.0, min(1.0, a))
+    raise Unsupported("color " + s)
+
+
+# ---------------------------------------------------------------- numbers, lengths, transforms
+NUM = r"[-+]?(?:\d+\.?\d*|\.\d+)(?:[eE][-+]?\d+)?"
+
+
+def numbers(s):
+    return [float(x) for x in re.findall(NUM, s or "")]
+
+
+def parse_length(s, ref=0.0, font_size=12.0):
+    s = s.strip()
+    m = re.match(r"(" + NUM + r")\s*([a-z%]*)$", s)
+    if not m:
+        raise Unsupported("length " + s)
+    v, u = float(m.group(1)), m.group(2)
+    if u in ("", "px"):
+        return v
+    if u == "%":
+        return v * ref / 100.0
+    if u == "em":
+        return v * font_size
+    if u == "ex":
+        return v * font_size / 2.0
+    if u == "in":
+        return v * 96.0
+    if u == "cm":
+        return v * 96.0 / 2.54
+    if u == "mm":
+        return v * 96.0 / 25.4
+    if u == "pt":
+        return v * 4.0 / 3.0
+    if u == "pc":
+        return v * 16.0
+    raise Unsupported("unit " + u)
+
+
+def mat_mul(a, b):
+    """a * b for (sx, ky, kx, sy, tx, ty) row-form transforms (f64)."""
+    return (a[0] * b[0] + a[2] * b[1], a[1] * b[0] + a[3] * b[1],
+            a[0] * b[2] + a[2] * b[3], a[1] * b[2] + a[3] * b[3],
+            a[0] * b[4] + a[2] * b[5] + a[4], a[1] * b[4] + a[3] * b[5] + a[5])
+
+
+IDENT = (1.0, 0.0, 0.0, 1.0, 0.0, 0.0)
+
+
+def parse_transform(s):
+    ts = IDENT
+    for name, args in re.findall(r"(\w+)\s*\(([^)]*)\)", s or ""):
+        v = numbers(args)
+        if name == "matrix" and len(v) == 6:
+            t = tuple(v)
+        elif name == "translate":
+            t = (1, 0, 0, 1, v[0], v[1] if len(v) > 1 else 0.0)
+        elif name == "scale":
+            t = (v[0], 0, 0, v[1] if len(v) > 1 else v[0], 0, 0)
+        elif name == "rotate":
+            a = math.radians(v[0])
+            c, s_ = math.cos(a), math.sin(a)
+            t = (c, s_, -s_, c, 0, 0)
+            if len(v) == 3:
+                t = mat_mul(mat_mul((1, 0, 0, 1, v[1], v[2]), t), (1, 0, 0, 1, -v[1], -v[2]))
+        elif name == "skewX":
+            t = (1, 0, math.tan(math.radians(v[0])), 1, 0, 0)
+        elif name == "skewY":
+            t = (1, math.tan(math.radians(v[0])), 0, 1, 0, 0)
+        else:
+            raise Unsupported("transform " + name)
+        ts = mat_mul(ts, t)
+    return ts
+
+
+# ---------------------------------------------------------------- path data
+class PathB:
+    """tiny-skia PathBuilder semantics (f32 points, move_to after close)."""
+
+    def __init__(self):
+        self.verbs, self.pts = [], []
+        self.move_req = True
+        self.last_move = None
+
+    def _f(self, v):
+        return float(np.float32(v))
+
+    def last(self):
+        return self.pts[-1] if self.pts else None
+
+    def move_to(self, x, y):
+        x, y = self._f(x), self._f(y)
+        if self.verbs and self.verbs[-1] == A.MOVE:
+            self.pts[-1] = (x, y)
+        else:
+            self.verbs.append(A.MOVE)
+            self.pts.append((x, y))
+        self.last_move = (x, y)
+        self.move_req = False
+
+    def _inject(self):
+        if self.move_req:
+            p = self.last_move if self.last_move is not None else (0.0, 0.0)
+            self.move_to(*p)
+
+    def line_to(self, x, y):
+        self._inject()
+        self.verbs.append(A.LINE)
+        self.pts.append((self._f(x), self._f(y)))
+
+    def quad_to(self, x1, y1, x, y):
+        self._inject()
+        self.verbs.append(A.QUAD)
+        self.pts += [(self._f(x1), self._f(y1)), (self._f(x), self._f(y))]
+
+    def cubic_to(self, x1, y1, x2, y2, x, y):
+        self._inject()
+        self.verbs.append(A.CUBIC)
+        self.pts += [(self._f(x1), self._f(y1)), (self._f(x2), self._f(y2)), (self._f(x), self._f(y))]
+
+    def close(self):
+        if self.verbs and self.verbs[-1] != A.CLOSE:
+            self.verbs.append(A.CLOSE)
+        self.move_req = True
+
+    def arc_to(self, rx, ry, rot, large, sweep, x, y, prev=None):
+        """usvg's PathBuilderExt::arc_to: kurbo arc -> cubics, or a line when
+        the arc is degenerate.  `prev` overrides the start point (f64)."""
+        if prev is None:
+            prev = self.last()
+        if prev is None:
+            return
+        cubics = svg_arc_to_cubics(prev, (x, y), rx, ry, rot, large, sweep)
+        if cubics is None:
+            self.line_to(x, y)
+            return
+        for c in cubics:
+            self.cubic_to(*c)
+
+    def finish(self):
+        if len(self.verbs) <= 1:
+            return None
+        # drop a trailing move
+        while self.verbs and self.verbs[-1] == A.MOVE:
+            self.verbs.pop()
+            self.pts.pop()
+        if len(self.verbs) <= 1:
+            return None
+        return self.verbs, [c for p in self.pts for c in p]
+
+
+def svg_arc_to_cubics(p0, p1, rx, ry, rot_deg, large, sweep, tol=0.1):
+    """kurbo::Arc::from_svg_arc + to_cubic_beziers(0.1), in f64."""
+    fx, fy = float(p0[0]), float(p0[1])
+    tx, ty = float(p1[0]), float(p1[1])
+    rx, ry = abs(float(rx)), abs(float(ry))
+    if rx <= 1e-5 or ry <= 1e-5 or (fx == tx and fy == ty):
+        return None  # SvgArc::is_straight_line: Arc::from_svg_arc gives None
+    xr = math.radians(rot_deg) % (2 * math.pi)
+    sp, cp = math.sin(xr), math.cos(xr)
+    hdx, hdy = (fx - tx) * 0.5, (fy - ty) * 0.5
+    hsx, hsy = (fx + tx) * 0.5, (fy + ty) * 0.5
+    px = cp * hdx + sp * hdy
+    py = -sp * hdx + cp * hdy
+    rf = px * px / (rx * rx) + py * py / (ry * ry)
+    if rf > 1.0:
+        rx *= math.sqrt(rf)
+        ry *= math.sqrt(rf)
+    rxry = rx * ry
+    rxpy = rx * py
+    rypx = ry * px
+    ssq = rxpy * rxpy + rypx * rypx
+    coe = (-1.0 if large == sweep else 1.0) * math.sqrt(abs((rxry * rxry - ssq) / ssq))
+    tcx = coe * rxpy / ry
+    tcy = -coe * rypx / rx
+    cx = cp * tcx - sp * tcy + hsx
+    cy = sp * tcx + cp * tcy + hsy
+    sa = math.atan2((py - tcy) / ry, (px - tcx) / rx)
+    ea = math.atan2((-py - tcy) / ry, (-px - tcx) / rx)
+    sweep_a = math.fmod(ea - sa, 2 * math.pi)
+    if sweep and sweep_a < 0:
+        sweep_a += 2 * math.pi
+    elif not sweep and sweep_a > 0:
+        sweep_a -= 2 * math.pi
+    rot = math.radians(rot_deg)
+
+    def sample(angle):
+        u, v = rx * math.cos(angle), ry * math.sin(angle)
+        s, c = math.sin(rot), math.cos(rot)
+        return u * c - v * s, u * s + v * c
+
+    sign = math.copysign(1.0, sweep_a)
+    scaled_err = max(rx, ry) / tol
+    n_err = max((1.1163 * scaled_err) ** (1.0 / 6.0), 3.999999)
+    n = math.ceil(n_err * abs(sweep_a) * (1.0 / (2.0 * math.pi)))
+    if n <= 0:
+        return []
+    step = sweep_a / n
+    arm = (4.0 / 3.0) * abs(math.tan(step / 4.0)) * sign
+    a0 = sa
+    q0 = sample(a0)
+    out = []
+    for _ in range(int(n)):
+        a1 = a0 + step
+        d0 = sample(a0 + math.pi / 2)
+        q3 = sample(a1)
+        d1 = sample(a1 + math.pi / 2)
+        p1 = (q0[0] + arm * d0[0], q0[1] + arm * d0[1])
+        p2 = (q3[0] - arm * d1[0], q3[1] - arm * d1[1])
+        out.append((cx + p1[0], cy + p1[1], cx + p2[0], cy + p2[1], cx + q3[0], cy + q3[1]))
+        a0, q0 = a1, q3
+    return out
+
+
+def parse_path_data(d: str) -> PathB:
+    """svgtypes SimplifyingPathParser semantics: absolute coordinates, H/V as
+    lines, S/T as reflected curves, arcs as cubics."""
+    toks = re.findall(r"[MmLlHhVvCcSsQqTtAaZz]|" + NUM, d or "")
+    b = PathB()
+    i, cmd = 0, None
+    cx = cy = sx = sy = 0.0
+    last_ctrl = None  # (kind, x, y) of the previous curve's second control point
+    first = True
+
+    def nums(k):
+        nonlocal i
+        out = []
+        for _ in range(k):
+            if i >= len(toks) or re.match(r"[A-Za-z]", toks[i]):
+                raise ValueError("missing number")
+            out.append(float(toks[i]))
+            i += 1
+        return out
+
+    while i < len(toks):
+        t = toks[i]
+        if re.match(r"[A-Za-z]", t):
+            cmd = t
+            i += 1
+            if first and cmd not in "Mm":
+                break
+            first = False
+            if cmd in "Zz":
+                b.close()
+                cx, cy = sx, sy
+                last_ctrl = None
+                continue
+        elif cmd is None:
+            break
+        try:
+            rel = cmd.islower()
+            c = cmd.upper()
+            if c == "M":
+                x, y = nums(2)
+                if rel:
+                    x, y = cx + x, cy + y
+                b.move_to(x, y)
+                cx, cy, sx, sy = x, y, x, y
+                cmd = "l" if rel else "L"
+                last_ctrl = None
+            elif c == "L":
+                x, y = nums(2)
+                if rel:
+                    x, y = cx + x, cy + y
+                b.line_to(x, y)
+                cx, cy = x, y
+                last_ctrl = None
+            elif c == "H":
+                (x,) = nums(1)
+                if rel:
+                    x = cx + x
+                b.line_to(x, cy)
+                cx = x
+                last_ctrl = None
+            elif c == "V":
+                (y,) = nums(1)
+                if rel:
+                    y = cy + y
+                b.line_to(cx, y)
+                cy = y
+                last_ctrl = None
+            elif c == "C":
+                x1, y1, x2, y2, x, y = nums(6)
+                if rel:
+                    x1, y1, x2, y2, x, y = cx + x1, cy + y1, cx + x2, cy + y2, cx + x, cy + y
+                b.cubic_to(x1, y1, x2, y2, x, y)
+                last_ctrl = ("C", x2, y2)
+                cx, cy = x, y
+            elif c == "S":
+                x2, y2, x, y = nums(4)
+                if rel:
+                    x2, y2, x, y = cx + x2, cy + y2, cx + x, cy + y
+                if last_ctrl and last_ctrl[0] == "C":
+                    x1, y1 = 2 * cx - last_ctrl[1], 2 * cy - last_ctrl[2]
+                else:
+                    x1, y1 = cx, cy
+                b.cubic_to(x1, y1, x2, y2, x, y)
+                last_ctrl = ("C", x2, y2)
+                cx, cy = x, y
+            elif c == "Q":
+                x1, y1, x, y = nums(4)
+                if rel:
+                    x1, y1, x, y = cx + x1, cy + y1, cx + x, cy + y
+                b.quad_to(x1, y1, x, y)
+                last_ctrl = ("Q", x1, y1)
+                cx, cy = x, y
+            elif c == "T":
+                x, y = nums(2)
+                if rel:
+                    x, y = cx + x, cy + y
+                if last_ctrl and last_ctrl[0] == "Q":
+                    x1, y1 = 2 * cx - last_ctrl[1], 2 * cy - last_ctrl[2]
+                else:
+                    x1, y1 = cx, cy
+                b.quad_to(x1, y1, x, y)
+                last_ctrl = ("Q", x1, y1)
+                cx, cy = x, y
+            elif c == "A":
+                rx, ry, rot = nums(3)
+                # flags may be glued: "A5 5 0 01 10 10"
+                flags = []
+                while len(flags) < 2:
+                    tok = toks[i]
+                    if tok in ("0", "1"):
+                        flags.append(tok == "1")
+                        i += 1
+                    elif re.match(r"[01]", tok):
+                        flags.append(tok[0] == "1")
+                        toks[i] = tok[1:]
+                    else:
+                        raise ValueError("bad arc flag")
+                x, y = nums(2)
+                if rel:
+                    x, y = cx + x, cy + y
+                b._inject()
+                b.arc_to(rx, ry, rot, flags[0], flags[1], x, y, prev=(cx, cy))
+                cx, cy = x, y
+                last_ctrl = None
+            else:
+                break
+        except (ValueError, IndexError):
+            break
+    return b
+
+
+# ---------------------------------------------------------------- tight bounds (usvg compute_tight_bounds)
+def tight_bounds(verbs, pts):
+    xs, ys = [], []
+    P = [(pts[2 * k], pts[2 * k + 1]) for k in range(len(pts) // 2)]
+    pi = 0
+    last = None
+    for v in verbs:
+        if v == A.MOVE or v == A.LINE:
+            last = P[pi]
+            pi += 1
+            xs.append(last[0])
+            ys.append(last[1])
+        elif v == A.QUAD:
+            c, e = P[pi], P[pi + 1]
+            pi += 2
+            xs.append(e[0]); ys.append(e[1])
+            for k in range(2):
+                a, b_, cc = last[k], c[k], e[k]
+                den = a - 2 * b_ + cc
+                if den != 0:
+                    t = (a - b_) / den
+                    if 0 < t < 1:
+                        m = 1 - t
+                        q = (m * m * last[0] + 2 * m * t * c[0] + t * t * e[0], m * m * last[1] + 2 * m * t * c[1] + t * t * e[1])
+                        xs.append(q[0]); ys.append(q[1])
+            last = e
+        elif v == A.CUBIC:
+            c1, c2, e = P[pi], P[pi + 1], P[pi + 2]
+            pi += 3
+            xs.append(e[0]); ys.append(e[1])
+            for k in range(2):
+                p0, p1, p2, p3 = last[k], c1[k], c2[k], e[k]
+                a = -p0 + 3 * p1 - 3 * p2 + p3
+                b_ = 2 * (p0 - 2 * p1 + p2)
+                cc = p1 - p0
+                roots = []
+                if abs(a) < 1e-12:
+                    if b_ != 0:
+                        roots.append(-cc / b_)
+                else:
+                    disc = b_ * b_ - 4 * a * cc
+                    if disc >= 0:
+                        sq = math.sqrt(disc)
+                        roots += [(-b_ + sq) / (2 * a), (-b_ - sq) / (2 * a)]
+                for t in roots:
+                    if 0 < t < 1:
+                        m = 1 - t
+                        q = [m ** 3 * last[j] + 3 * m * m * t * c1[j] + 3 * m * t * t * c2[j] + t ** 3 * e[j] for j in range(2)]
+                        xs.append(q[0]); ys.append(q[1])
+            last = e
+    if not xs:
+        return None
+    return min(xs), min(ys), max(xs), max(ys)
+
+
+# ---------------------------------------------------------------- the loader
+INHERITED = {"fill", "fill-opacity", "fill-rule", "stroke", "stroke-width", "stroke-opacity", "stroke-linecap",
+             "stroke-linejoin", "stroke-miterlimit", "stroke-dasharray", "stroke-dashoffset", "visibility",
+             "shape-rendering", "clip-rule", "color", "color-interpolation-filters", "paint-order", "font-size"}
+NON_INHERITED = {"opacity", "clip-path", "mask", "filter", "mix-blend-mode", "isolation", "display",
+                 "stop-color", "stop-opacity", "flood-color", "flood-opacity", "transform"}
+UNSUPPORTED_ELEMS = {"text", "image", "pattern", "marker", "switch", "foreignObject", "tspan", "textPath", "symbol",
+                     "feImage", "feTile", "feTurbulence", "feDisplacementMap", "feComponentTransfer",
+                     "feDropShadow", "feDiffuseLighting", "feSpecularLighting", "feConvolveMatrix", "feFuncR",
+                     "style", "animate", "set"}
+BLEND = {"normal": "source-over", "multiply": "multiply", "screen": "screen", "overlay": "overlay",
+         "darken": "darken", "lighten": "lighten", "color-dodge": "color-dodge", "color-burn": "color-burn",
+         "hard-light": "hard-light", "soft-light": "soft-light", "difference": "difference",
+         "exclusion": "exclusion", "hue": "hue", "saturation": "saturation", "color": "color",
+         "luminosity": "luminosity"}
+
+
+F = np.float32
+
+
+def _tag(e):
+    t = e.tag
+    return t[len(SVG_NS):] if t.startswith(SVG_NS) else t
+
+
+class Loader:
+    def __init__(self, text: str, tree_cls):
+        self.root = ET.fromstring(text)
+        if _tag(self.root) != "svg":
+            raise Unsupported("root is not svg")
+        self.ids = {}
+        for e in self.root.iter():
+            i = e.get("id")
+            if i is not None and i not in self.ids:
+                self.ids[i] = e
+        self.parent = {c: p for p in self.root.iter() for c in p}
+        self.tree_cls = tree_cls
+        for e in self.root.iter():
+            if _tag(e) in UNSUPPORTED_ELEMS:
+                raise Unsupported("element " + _tag(e))
+            if e.get("class") is not None or e.get("systemLanguage") is not None:
+                raise Unsupported("class/systemLanguage")
+        self.clip_cache, self.mask_cache, self.filter_cache = {}, {}, {}
+
+    # ---- attributes with style and inheritance
+    def attrs(self, e):
+        a = dict(e.attrib)
+        st = a.pop("style", None)
+        if st:
+            for part in st.split(";"):
+                if ":" in part:
+                    k, v = part.split(":", 1)
+                    a[k.strip()] = v.strip()
+        return a
+
+    def get(self, e, name, inherited=True):
+        a = self.attrs(e)
+        if name in a and a[name].strip() != "inherit":
+            return a[name]
+        if inherited or (name in a and a[name].strip() == "inherit"):
+            p = self.parent.get(e)
+            while p is not None:
+                pa = self.attrs(p)
+                if name in pa and pa[name].strip() != "inherit":
+                    return pa[name]
+                if not inherited:
+                    break
+                p = self.parent.get(p)
+        return None
+
+    def num(self, e, name, default, ref=0.0):
+        v = self.attrs(e).get(name)
+        if v is None:
+            return default
+        return parse_length(v, ref)
+
+    def href(self, e):
+        h = e.get(XLINK) or e.get("href")
+        if h and h.startswith("#"):
+            return self.ids.get(h[1:])
+        return None
+
+    def ref(self, value):
+        if not value or value.strip() == "none":
+            return None
+        m = re.match(r"url\(\s*['\"]?#([^'\")]+)['\"]?\s*\)", value.strip())
+        if not m:
+            raise Unsupported("reference " + value)
+        return self.ids.get(m.group(1), "missing")
+
+
+
+def _map_box(t, b):
+    xs = [b[0], b[2], b[2], b[0]]
+    ys = [b[1], b[1], b[3], b[3]]
+    pts = [(t[0] * x + t[2] * y + t[4], t[1] * x + t[3] * y + t[5]) for x, y in zip(xs, ys)]
+    return (min(p[0] for p in pts), min(p[1] for p in pts), max(p[0] for p in pts), max(p[1] for p in pts))
+
+
+def _group(**kw):
+    g = A.Group()
+    g.transform = A.Transform.identity()
+    g.opacity = 1.0
+    g.blend = A.BLEND["source-over"]
+    g.clip_path = -1
+    g.mask = -1
+    for k, v in kw.items():
+        setattr(g, k, v)
+    return g
+
+
+def _tf(t):
+    return A.Transform(*[float(np.float32(v)) for v in t])
+
+
+class Builder(Loader):
+    """Converts the SVG element tree into render-tree nodes."""
+
+    def load(self):
+        svg = self.root
+        vb = numbers(svg.get("viewBox"))
+        w, h = svg.get("width"), svg.get("height")
+        if vb and len(vb) == 4:
+            W = parse_length(w, vb[2]) if (w and not w.strip().endswith("%")) else vb[2]
+            H = parse_length(h, vb[3]) if (h and not h.strip().endswith("%")) else vb[3]
+            par = svg.get("preserveAspectRatio")
+            if par not in (None, "xMidYMid", "xMidYMid meet"):
+                raise Unsupported("preserveAspectRatio")
+            s = min(W / vb[2], H / vb[3])
+            root_ts = (s, 0, 0, s, -vb[0] * s + (W - vb[2] * s) / 2, -vb[1] * s + (H - vb[3] * s) / 2)
+        else:
+            W = parse_length(w, 100) if w else 100.0
+            H = parse_length(h, 100) if h else 100.0
+            root_ts = IDENT
+        self.vbw, self.vbh = (vb[2], vb[3]) if vb and len(vb) == 4 else (W, H)
+        self.W, self.H = W, H
+        self.tree = self.tree_cls(W, H)
+        root = self.tree.add_group(-1, _group())
+        if root_ts != IDENT:
+            root = self.tree.add_group(root, _group(transform=_tf(root_ts)))
+        for c in svg:
+            self.node(c, root)
+        self.tree.finalize()
+        return self.tree
+
+    def visible(self, e):
+        if self.attrs(e).get("display", "").strip() == "none":
+            return False
+        return True
+
+    def node(self, e, parent, transform_extra=IDENT):
+        tag = _tag(e)
+        if tag in ("defs", "linearGradient", "radialGradient", "clipPath", "mask", "filter", "title", "desc",
+                   "metadata", "stop"):
+            return
+        if not self.visible(e):
+            return
+        if tag not in ("g", "path", "rect", "circle", "ellipse", "line", "polyline", "polygon", "use", "svg", "a"):
+            raise Unsupported("element " + tag)
+        ts = parse_transform(self.attrs(e).get("transform", ""))
+        if transform_extra != IDENT:
+            ts = mat_mul(transform_extra, ts)
+        if tag == "use":
+            ref = self.href(e)
+            if ref is None:
+                return
+            x = self.num(e, "x", 0.0, self.vbw)
+            y = self.num(e, "y", 0.0, self.vbh)
+            ts = mat_mul(ts, (1, 0, 0, 1, x, y))
+            if _tag(ref) == "svg" or _tag(ref) == "symbol":
+                raise Unsupported("use of svg/symbol")
+        g = self.group_for(e, parent, ts)
+        if g is None:
+            return
+        if tag in ("g", "a"):
+            for c in e:
+                self.node(c, g)
+        elif tag == "use":
+            self.node(ref, g)
+        elif tag == "svg":
+            raise Unsupported("nested svg")
+        else:
+            self.shape(e, g)
+
+    def group_for(self, e, parent, ts):
+        """Creates the group an element needs (transform, opacity, clip, mask,
+        filter, blend); returns the parent to add children to."""
+        a = self.attrs(e)
+        opacity = float(a.get("opacity", "1").strip()) if "opacity" in a else 1.0
+        opacity = max(0.0, min(1.0, opacity))
+        clip = self.ref(a.get("clip-path"))
+        mask = self.ref(a.get("mask"))
+        filt = a.get("filter")
+        blend = BLEND.get(a.get("mix-blend-mode", "normal").strip(), None)
+        if blend is None:
+            raise Unsupported("blend mode")
+        isolate = a.get("isolation", "auto").strip() == "isolate"
+        if clip == "missing" or mask == "missing":
+            return None  # references to missing elements: the element is not rendered
+        needs = ts != IDENT or opacity != 1.0 or clip is not None or mask is not None or filt or \
+            blend != "source-over" or isolate
+        if not needs:
+            return parent
+        bbox = None
+        has_filter = bool(filt and filt.strip() != "none")
+        if clip is not None or mask is not None or has_filter:
+            bbox = self.element_bbox(e)
+        ci = mi = -1
+        if clip is not None:
+            ci = self.clip(clip, bbox)
+            if ci is None:
+                return None
+        if mask is not None:
+            mi = self.mask(mask, bbox)
+            if mi is None:
+                return None
+        fids = []
+        if has_filter:
+            for fref in re.findall(r"url\([^)]*\)", filt):
+                fe = self.ref(fref)
+                if fe == "missing" or fe is None:
+                    return None
+                fi = self.filter(fe, bbox)
+                if fi is None:
+                    return None
+                fids.append(fi)
+            if not fids:
+                raise Unsupported("filter functions")
+        g = _group(transform=_tf(ts), opacity=float(np.float32(opacity)), blend=A.BLEND[blend],
+                   isolate=1 if isolate else 0, clip_path=ci, mask=mi)
+        gi = self.tree.add_group(parent, g)
+        if fids:
+            self.tree.set_group_filters(gi, fids)
+        return gi
+
+    # ---- bounding boxes (object bounding box of an element, its user space)
+    def element_bbox(self, e):
+        tag = _tag(e)
+        if tag in ("g", "a"):
+            boxes = []
+            for c in e:
+                if _tag(c) in ("defs", "title", "desc") or not self.visible(c):
+                    continue
+                b = self.element_bbox(c)
+                if b is None:
+                    continue
+                boxes.append(_map_box(parse_transform(self.attrs(c).get("transform", "")), b))
+            if not boxes:
+                return None
+            return (min(b[0] for b in boxes), min(b[1] for b in boxes), max(b[2] for b in boxes),
+                    max(b[3] for b in boxes))
+        if tag == "use":
+            ref = self.href(e)
+            if ref is None:
+                return None
+            b = self.element_bbox(ref)
+            if b is None:
+                return None
+            t = parse_transform(self.attrs(ref).get("transform", ""))
+            t = mat_mul((1, 0, 0, 1, self.num(e, "x", 0.0, self.vbw), self.num(e, "y", 0.0, self.vbh)), t)
+            return _map_box(t, b)
+        geo = self.geometry(e)
+        if geo is None:
+            return None
+        return tight_bounds(*geo)
+
+    # ---- shapes
+    def geometry(self, e):
+        tag = _tag(e)
+        a = self.attrs(e)
+        L = lambda n, d, ref: parse_length(a[n], ref) if n in a else d  # noqa: E731
+        b = PathB()
+        if tag == "path":
+            b = parse_path_data(a.get("d", ""))
+        elif tag == "rect":
+            # usvg shapes.rs convert_rect: lengths and corner arithmetic in f32
+            w, h = F(L("width", 0.0, self.vbw)), F(L("height", 0.0, self.vbh))
+            if not (w > 0 and h > 0):
+                return None
+            x, y = F(L("x", 0.0, self.vbw)), F(L("y", 0.0, self.vbh))
+            rx = L("rx", None, self.vbw) if "rx" in a else None
+            ry = L("ry", None, self.vbh) if "ry" in a else None
+            rx = None if (rx is not None and math.copysign(1.0, rx) < 0) else rx
+            ry = None if (ry is not None and math.copysign(1.0, ry) < 0) else ry
+            if rx is None and ry is None:
+                rx = ry = 0.0
+            elif rx is None:
+                rx = ry
+            elif ry is None:
+                ry = rx
+            rx, ry = F(rx), F(ry)
+            two = F(2.0)
+            if rx > w / two:
+                rx = w / two
+            if ry > h / two:
+                ry = h / two
+            if abs(int(np.float32(rx).view(np.int32))) <= 4:
+                b.move_to(x, y); b.line_to(x + w, y); b.line_to(x + w, y + h); b.line_to(x, y + h); b.close()
+            else:
+                b.move_to(x + rx, y)
+                b.line_to(x + w - rx, y)
+                b.arc_to(rx, ry, 0, False, True, x + w, y + ry)
+                b.line_to(x + w, y + h - ry)
+                b.arc_to(rx, ry, 0, False, True, x + w - rx, y + h)
+                b.line_to(x + rx, y + h)
+                b.arc_to(rx, ry, 0, False, True, x, y + h - ry)
+                b.line_to(x, y + ry)
+                b.arc_to(rx, ry, 0, False, True, x + rx, y)
+                b.close()
+        elif tag in ("circle", "ellipse"):
+            cx, cy = F(L("cx", 0.0, self.vbw)), F(L("cy", 0.0, self.vbh))
+            if tag == "circle":
+                r = L("r", 0.0, math.hypot(self.vbw, self.vbh) / math.sqrt(2))
+                rx = ry = r
+            else:
+                rx = L("rx", None, self.vbw) if "rx" in a else None
+                ry = L("ry", None, self.vbh) if "ry" in a else None
+                rx = None if (rx is not None and math.copysign(1.0, rx) < 0) else rx
+                ry = None if (ry is not None and math.copysign(1.0, ry) < 0) else ry
+                if rx is None and ry is None:
+                    return None
+                rx = ry if rx is None else rx
+                ry = rx if ry is None else ry
+            rx, ry = F(rx), F(ry)
+            if not (rx > 0 and ry > 0):
+                return None
+            b.move_to(cx + rx, cy)
+            b.arc_to(rx, ry, 0, False, True, cx, cy + ry)
+            b.arc_to(rx, ry, 0, False, True, cx - rx, cy)
+            b.arc_to(rx, ry, 0, False, True, cx, cy - ry)
+            b.arc_to(rx, ry, 0, False, True, cx + rx, cy)
+            b.close()
+        elif tag == "line":
+            b.move_to(L("x1", 0.0, self.vbw), L("y1", 0.0, self.vbh))
+            b.line_to(L("x2", 0.0, self.vbw), L("y2", 0.0, self.vbh))
+        elif tag in ("polyline", "polygon"):
+            v = numbers(a.get("points", ""))
+            if len(v) % 2:
+                v = v[:-1]
+            if len(v) < 4:
+                return None
+            b.move_to(v[0], v[1])
+            for k in range(2, len(v), 2):
+                b.line_to(v[k], v[k + 1])
+            if tag == "polygon":
+                b.close()
+        else:
+            return None
+        return b.finish()
+
+    def paint(self, e, which, bbox, opacity_attr):
+        v = self.get(e, which)
+        if v is None:
+            v = "black" if which == "fill" else "none"
+        v = v.strip()
+        cur = parse_color(self.get(e, "color") or "black")
+        cur = cur[0] if cur else (0, 0, 0)
+        op = self.get(e, opacity_attr)
+        opacity = 1.0
+        if op is not None:
+            op = op.strip()
+            opacity = float(op[:-1]) / 100 if op.endswith("%") else float(op)
+        opacity = max(0.0, min(1.0, opacity))
+        if v.startswith("url("):
+            m = re.match(r"url\(\s*['\"]?#([^'\")]+)['\"]?\s*\)\s*(.*)$", v)
+            if not m:
+                raise Unsupported("paint " + v)
+            ref = self.ids.get(m.group(1))
+            fallback = m.group(2).strip()
+            if ref is None or _tag(ref) not in ("linearGradient", "radialGradient"):
+                if ref is not None and _tag(ref) == "pattern":
+                    raise Unsupported("pattern")
+                if fallback:
+                    c = parse_color(fallback, cur)
+                    if c is None:
+                        return None
+                    return self.solid(c), opacity * c[1]
+                return None
+            return self.gradient(ref, bbox, opacity)
+        c = parse_color(v, cur)
+        if c is None:
+            return None
+        return self.solid(c), opacity * c[1]
+
+    def solid(self, c):
+        p = A.Paint()
+        p.kind = A.PAINT_SOLID
+        p.r, p.g, p.b = c[0]
+        p.transform = A.Transform.identity()
+        return self.tree.add_paint(p)
+
+    def grad_attr(self, e, name, chain):
+        for g in chain:
+            v = g.get(name)
+            if v is not None:
+                return v
+        return None
+
+    def gradient(self, ref, bbox, opacity):
+        chain, g = [], ref
+        seen = set()
+        while g is not None and id(g) not in seen:
+            seen.add(id(g))
+            chain.append(g)
+            g = self.href(g)
+        stops_src = next((c for c in chain if any(_tag(s) == "stop" for s in c)), None)
+        if stops_src is None:
+            return None
+        stops = []
+        prev = 0.0
+        for s in stops_src:
+            if _tag(s) != "stop":
+                continue
+            sa = self.attrs(s)
+            off = sa.get("offset")
+            if off is None:
+                o = prev
+            else:
+                off = off.strip()
+                o = float(off[:-1]) / 100 if off.endswith("%") else float(off)
+            prev = o
+            o = max(0.0, min(1.0, o))
+            col = sa.get("stop-color", "black")
+            c = parse_color(col, (0, 0, 0)) or ((0, 0, 0), 0.0)
+            sop = sa.get("stop-opacity", "1").strip()
+            sop = float(sop[:-1]) / 100 if sop.endswith("%") else float(sop)
+            stops.append([float(np.float32(o)), c[0], c[1] * max(0.0, min(1.0, sop))])
+        if not stops:
+            return None
+        # usvg stop normalisation (paint_server.rs:334-404)
+        eps = float(np.finfo(np.float32).eps)
+
+        def ulps_eq(a, b):
+            return abs(np.float32(a).view(np.int32) - np.float32(b).view(np.int32)) <= 4 or a == b
+        if len(stops) >= 3:
+            i = 0
+            while i < len(stops) - 2:
+                if ulps_eq(stops[i][0], stops[i + 1][0]) and ulps_eq(stops[i + 1][0], stops[i + 2][0]):
+                    stops.pop(i + 1)
+                else:
+                    i += 1
+        if len(stops) >= 2:
+            for i in range(len(stops) - 1):
+                if ulps_eq(stops[i][0], 0.0) and ulps_eq(stops[i + 1][0], 0.0):
+                    stops[i + 1][0] = float(np.float32(min(1.0, max(0.0, stops[i][0] + eps))))
+        for i in range(1, len(stops)):
+            o1, o2 = stops[i - 1][0], stops[i][0]
+            if o1 > o2 or ulps_eq(o1, o2):
+                stops[i - 1][0] = float(np.float32(min(1.0, max(0.0, o1 - eps))))
+                stops[i][0] = o1
+        units = self.grad_attr(ref, "gradientUnits", chain) or "objectBoundingBox"
+        spread = {"pad": 0, "reflect": 1, "repeat": 2}.get((self.grad_attr(ref, "spreadMethod", chain) or "pad").strip(), 0)
+        gts = parse_transform(self.grad_attr(ref, "gradientTransform", chain) or "")
+        p = A.Paint()
+        p.spread = spread
+        obb = units.strip() == "objectBoundingBox"
+        if obb:
+            if bbox is None or bbox[2] - bbox[0] <= 0 or bbox[3] - bbox[1] <= 0:
+                return None
+            bts = (bbox[2] - bbox[0], 0, 0, bbox[3] - bbox[1], bbox[0], bbox[1])
+            gts = mat_mul(bts, gts)
+
+        def ln(name, default, ref_len):
+            v = self.grad_attr(ref, name, chain)
+            if v is None:
+                return default
+            v = v.strip()
+            if obb:
+                return float(v[:-1]) / 100 if v.endswith("%") else float(v)
+            return parse_length(v, ref_len)
+        if _tag(ref) == "linearGradient":
+            p.kind = A.PAINT_LINEAR
+            p.x1 = ln("x1", 0.0, self.vbw)
+            p.y1 = ln("y1", 0.0, self.vbh)
+            p.x2 = ln("x2", 1.0 if obb else self.vbw, self.vbw)
+            p.y2 = ln("y2", 0.0, self.vbh)
+        else:
+            p.kind = A.PAINT_RADIAL
+            diag = math.hypot(self.vbw, self.vbh) / math.sqrt(2)
+            p.cx = ln("cx", 0.5 if obb else self.vbw / 2, self.vbw)
+            p.cy = ln("cy", 0.5 if obb else self.vbh / 2, self.vbh)
+            p.r_ = ln("r", 0.5 if obb else diag / 2, diag)
+            p.fx = ln("fx", p.cx, self.vbw)
+            p.fy = ln("fy", p.cy, self.vbh)
+            p.fr = ln("fr", 0.0, diag)
+            if not p.r_ > 0:
+                return None
+        p.transform = _tf(gts)
+        if len(stops) == 1:
+            c = stops[0]
+            return self.solid((c[1], 1.0)), opacity * c[2]
+        st = []
+        for o, c, a in stops:
+            s = A.Stop()
+            s.offset = o
+            s.r, s.g, s.b = c
+            s.opacity = float(np.float32(a))
+            st.append(s)
+        return self.tree.add_paint(p, st), opacity
+
+    def shape(self, e, parent):
+        geo = self.geometry(e)
+        if geo is None:
+            return
+        verbs, pts = geo
+        bbox = tight_bounds(verbs, pts)
+        vis = (self.get(e, "visibility") or "visible").strip()
+        path = A.Path()
+        path.fill_paint = -1
+        path.stroke_paint = -1
+        path.visible = 1 if vis == "visible" else 0
+        sr = (self.get(e, "shape-rendering") or "geometricPrecision").strip()
+        path.anti_alias = 0 if sr in ("crispEdges", "optimizeSpeed") else 1
+        po = (self.get(e, "paint-order") or "normal").strip().split()
+        path.stroke_first = 1 if po and po[0] == "stroke" else 0
+        fill = self.paint(e, "fill", bbox, "fill-opacity")
+        if fill is not None:
+            path.fill_paint, path.fill_opacity = fill[0], float(np.float32(fill[1]))
+        path.fill_rule = A.EVENODD if (self.get(e, "fill-rule") or "nonzero").strip() == "evenodd" else A.NONZERO
+        sw = self.get(e, "stroke-width")
+        width = parse_length(sw, math.hypot(self.vbw, self.vbh) / math.sqrt(2)) if sw else 1.0
+        dashes = []
+        if width > 0:
+            stroke = self.paint(e, "stroke", bbox, "stroke-opacity")
+            if stroke is not None:
+                path.stroke_paint, path.stroke_opacity = stroke[0], float(np.float32(stroke[1]))
+                path.stroke_width = float(np.float32(width))
+                ml = self.get(e, "stroke-miterlimit")
+                path.miter_limit = float(ml) if ml else 4.0
+                if path.miter_limit < 1:
+                    path.stroke_paint = -1
+                path.line_cap = {"butt": 0, "round": 1, "square": 2}.get((self.get(e, "stroke-linecap") or "butt").strip(), 0)
+                path.line_join = {"miter": 0, "miter-clip": 1, "round": 2, "bevel": 3, "arcs": 0}.get(
+                    (self.get(e, "stroke-linejoin") or "miter").strip(), 0)
+                da = self.get(e, "stroke-dasharray")
+                if da and da.strip() != "none":
+                    dashes = [parse_length(x, self.vbw) for x in re.split(r"[\s,]+", da.strip()) if x]
+                    if any(d < 0 for d in dashes) or sum(dashes) <= 0:
+                        dashes = []
+                    elif len(dashes) % 2:
+                        dashes = dashes * 2
+                    do = self.get(e, "stroke-dashoffset")
+                    path.dash_phase = float(parse_length(do, self.vbw)) if do else 0.0
+        if path.fill_paint < 0 and path.stroke_paint < 0:
+            return
+        if path.stroke_paint < 0:
+            path.stroke_width = 1.0
+        self.tree.add_path(parent, path, verbs, pts, dashes)
+
+    # ---- clip paths
+    def clip(self, ce, bbox):
+        if _tag(ce) != "clipPath":
+            return None
+        units = (ce.get("clipPathUnits") or "userSpaceOnUse").strip()
+        ts = parse_transform(ce.get("transform", ""))
+        if units == "objectBoundingBox":
+            if bbox is None or bbox[2] <= bbox[0] or bbox[3] <= bbox[1]:
+                return None
+            ts = mat_mul(ts, (bbox[2] - bbox[0], 0, 0, bbox[3] - bbox[1], bbox[0], bbox[1]))
+        root = self.tree.add_group(-1, _group())
+        for c in ce:
+            tag = _tag(c)
+            if tag in ("title", "desc"):
+                continue
+            if tag not in ("path", "rect", "circle", "ellipse", "line", "polyline", "polygon", "use", "g"):
+                raise Unsupported("clip child " + tag)
+            if tag == "g":
+                raise Unsupported("clip child g")
+            self.clip_child(c, root)
+        c = A.Clip()
+        c.transform = _tf(ts)
+        c.clip_path = -1
+        c.root = root
+        nested = self.ref(self.attrs(ce).get("clip-path"))
+        if nested == "missing":
+            return None
+        if nested is not None:
+            ni = self.clip(nested, bbox)
+            if ni is None:
+                return None
+            c.clip_path = ni
+        return self.tree.add_clip(c)
+
+    def clip_child(self, e, root):
+        if not self.visible(e):
+            return
+        a = self.attrs(e)
+        ts = parse_transform(a.get("transform", ""))
+        target = e
+        if _tag(e) == "use":
+            target = self.href(e)
+            if target is None or _tag(target) not in ("path", "rect", "circle", "ellipse", "line", "polyline",
+                                                      "polygon"):
+                raise Unsupported("clip use")
+            ts = mat_mul(ts, (1, 0, 0, 1, self.num(e, "x", 0.0, self.vbw), self.num(e, "y", 0.0, self.vbh)))
+        parent = root
+        cp = self.ref(a.get("clip-path"))
+        ci = -1
+        if cp is not None:
+            if cp == "missing":
+                return
+            ci = self.clip(cp, self.element_bbox(target))
+            if ci is None:
+                return
+        if ts != IDENT or ci >= 0:
+            parent = self.tree.add_group(root, _group(transform=_tf(ts), clip_path=ci))
+        geo = self.geometry(target)
+        if geo is None:
+            return
+        path = A.Path()
+        path.fill_paint = self.solid(((0, 0, 0), 1.0))
+        path.fill_opacity = 1.0
+        path.stroke_paint = -1
+        path.stroke_width = 1.0
+        path.visible = 1 if (self.get(e, "visibility") or "visible").strip() == "visible" else 0
+        sr = (self.get(target, "shape-rendering") or "geometricPrecision").strip()
+        path.anti_alias = 0 if sr in ("crispEdges", "optimizeSpeed") else 1
+        path.fill_rule = A.EVENODD if (self.get(e, "clip-rule") or "nonzero").strip() == "evenodd" else A.NONZERO
+        self.tree.add_path(parent, path, geo[0], geo[1])
+
+    # ---- masks
+    def mask(self, me, bbox):
+        if _tag(me) != "mask":
+            return None
+        units = (me.get("maskUnits") or "objectBoundingBox").strip()
+        cunits = (me.get("maskContentUnits") or "userSpaceOnUse").strip()
+
+        def fr(name, default):
+            v = me.get(name)
+            if v is None:
+                return default
+            v = v.strip()
+            return float(v[:-1]) / 100 if v.endswith("%") else float(v)
+        if units == "objectBoundingBox":
+            if bbox is None or bbox[2] <= bbox[0] or bbox[3] <= bbox[1]:
+                return None
+            bw, bh = bbox[2] - bbox[0], bbox[3] - bbox[1]
+            x = bbox[0] + fr("x", -0.1) * bw
+            y = bbox[1] + fr("y", -0.1) * bh
+            w = fr("width", 1.2) * bw
+            h = fr("height", 1.2) * bh
+        else:
+            x = self.num(me, "x", -0.1 * self.vbw, self.vbw)
+            y = self.num(me, "y", -0.1 * self.vbh, self.vbh)
+            w = self.num(me, "width", 1.2 * self.vbw, self.vbw)
+            h = self.num(me, "height", 1.2 * self.vbh, self.vbh)
+        if not (w > 0 and h > 0):
+            return None
+        root = self.tree.add_group(-1, _group())
+        content = root
+        if cunits == "objectBoundingBox":
+            if bbox is None:
+                return None
+            content = self.tree.add_group(root, _group(transform=_tf(
+                (bbox[2] - bbox[0], 0, 0, bbox[3] - bbox[1], bbox[0], bbox[1]))))
+        for c in me:
+            self.node(c, content)
+        m = A.Mask()
+        m.x, m.y, m.w, m.h = x, y, w, h
+        mt = (self.attrs(me).get("mask-type") or "luminance").strip()
+        m.kind = A.MASK_ALPHA if mt == "alpha" else A.MASK_LUMINANCE
+        m.mask = -1
+        m.root = root
+        nested = self.ref(self.attrs(me).get("mask"))
+        if nested == "missing":
+            return None
+        if nested is not None:
+            ni = self.mask(nested, bbox)
+            if ni is None:
+                return None
+            m.mask = ni
+        return self.tree.add_mask(m)
+
+    # ---- filters
+    def filter(self, fe, bbox):
+        if _tag(fe) != "filter":
+            return None
+        units = (fe.get("filterUnits") or "objectBoundingBox").strip()
+        punits = (fe.get("primitiveUnits") or "userSpaceOnUse").strip()
+        if punits != "userSpaceOnUse":
+            raise Unsupported("primitiveUnits")
+
+        def fr(e, name, default):
+            v = e.get(name)
+            if v is None:
+                return default
+            v = v.strip()
+            return float(v[:-1]) / 100 if v.endswith("%") else float(v)
+        if units == "objectBoundingBox":
+            if bbox is None or bbox[2] <= bbox[0] or bbox[3] <= bbox[1]:
+                return None
+            bw, bh = bbox[2] - bbox[0], bbox[3] - bbox[1]
+            x, y = bbox[0] + fr(fe, "x", -0.1) * bw, bbox[1] + fr(fe, "y", -0.1) * bh
+            w, h = fr(fe, "width", 1.2) * bw, fr(fe, "height", 1.2) * bh
+        else:
+            x = self.num(fe, "x", -0.1 * self.vbw, self.vbw)
+            y = self.num(fe, "y", -0.1 * self.vbh, self.vbh)
+            w = self.num(fe, "width", 1.2 * self.vbw, self.vbw)
+            h = self.num(fe, "height", 1.2 * self.vbh, self.vbh)
+        if not (w > 0 and h > 0):
+            return None
+        prims, names, merge = [], {}, []
+        for c in fe:
+            tag = _tag(c)
+            if tag in ("title", "desc"):
+                continue
+            p = A.Primitive()
+            p.x = self.num(c, "x", x, self.vbw) if c.get("x") is not None else x
+            p.y = self.num(c, "y", y, self.vbh) if c.get("y") is not None else y
+            p.w = self.num(c, "width", w, self.vbw) if c.get("width") is not None else w
+            p.h = self.num(c, "height", h, self.vbh) if c.get("height") is not None else h
+            cif = (self.get(c, "color-interpolation-filters") or "linearRGB").strip()
+            p.linear_rgb = 0 if cif == "sRGB" else 1
+
+            def inp(name):
+                v = c.get(name)
+                if v is None:
+                    return len(prims) - 1 if prims else A.IN_SOURCE_GRAPHIC
+                v = v.strip()
+                if v == "SourceGraphic":
+                    return A.IN_SOURCE_GRAPHIC
+                if v == "SourceAlpha":
+                    return A.IN_SOURCE_ALPHA
+                if v in names:
+                    return names[v]
+                if v in ("BackgroundImage", "BackgroundAlpha", "FillPaint", "StrokePaint"):
+                    raise Unsupported("input " + v)
+                return len(prims) - 1 if prims else A.IN_SOURCE_GRAPHIC
+            p.in1 = inp("in")
+            if tag == "feGaussianBlur":
+                sd = numbers(c.get("stdDeviation", "0"))
+                sdx, sdy = (sd[0], sd[1]) if len(sd) > 1 else ((sd[0], sd[0]) if sd else (0.0, 0.0))
+                if sdx < 0 or sdy < 0:
+                    sdx = sdy = 0.0
+                p.kind = A.FE_BLUR
+                p.f[0], p.f[1] = sdx, sdy
+            elif tag == "feColorMatrix":
+                p.kind = A.FE_COLOR_MATRIX
+                t = (c.get("type") or "matrix").strip()
+                vals = numbers(c.get("values", ""))
+                if t == "saturate":
+                    p.i[0] = A.CM_SATURATE
+                    p.f[0] = vals[0] if vals else 1.0
+                elif t == "hueRotate":
+                    p.i[0] = A.CM_HUE_ROTATE
+                    p.f[0] = vals[0] if vals else 0.0
+                elif t == "luminanceToAlpha":
+                    p.i[0] = A.CM_LUM_TO_ALPHA
+                else:
+                    p.i[0] = A.CM_MATRIX
+                    if len(vals) != 20:
+                        vals = [1, 0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 1, 0]
+                    for k in range(20):
+                        p.f[k] = vals[k]
+            elif tag == "feMorphology":
+                p.kind = A.FE_MORPHOLOGY
+                p.i[0] = 1 if (c.get("operator") or "erode").strip() == "dilate" else 0
+                r = numbers(c.get("radius", "0"))
+                rx, ry = (r[0], r[1]) if len(r) > 1 else ((r[0], r[0]) if r else (0.0, 0.0))
+                if rx < 0 or ry < 0 or (rx == 0 and ry == 0):
+                    rx = ry = 0.0
+                p.f[0], p.f[1] = rx, ry
+            elif tag == "feComposite":
+                p.kind = A.FE_COMPOSITE
+                p.in2 = inp("in2")
+                op = (c.get("operator") or "over").strip()
+                p.i[0] = {"over": A.OP_OVER, "in": A.OP_IN, "out": A.OP_OUT, "atop": A.OP_ATOP, "xor": A.OP_XOR,
+                          "arithmetic": A.OP_ARITHMETIC}.get(op, A.OP_OVER)
+                for k, n in enumerate(("k1", "k2", "k3", "k4")):
+                    p.f[k] = float(c.get(n, "0"))
+            elif tag == "feFlood":
+                p.kind = A.FE_FLOOD
+                col = parse_color(self.attrs(c).get("flood-color", "black")) or ((0, 0, 0), 0.0)
+                p.i[0], p.i[1], p.i[2] = col[0]
+                fo = self.attrs(c).get("flood-opacity", "1").strip()
+                fo = float(fo[:-1]) / 100 if fo.endswith("%") else float(fo)
+                p.f[0] = max(0.0, min(1.0, fo)) * col[1]
+            elif tag == "feOffset":
+                p.kind = A.FE_OFFSET
+                p.f[0], p.f[1] = float(c.get("dx", "0")), float(c.get("dy", "0"))
+            elif tag == "feMerge":
+                p.kind = A.FE_MERGE
+                ins = []
+                for n in c:
+                    if _tag(n) == "feMergeNode":
+                        v = n.get("in")
+                        if v is None:
+                            ins.append(len(prims) - 1 if prims else A.IN_SOURCE_GRAPHIC)
+                        elif v == "SourceGraphic":
+                            ins.append(A.IN_SOURCE_GRAPHIC)
+                        elif v == "SourceAlpha":
+                            ins.append(A.IN_SOURCE_ALPHA)
+                        elif v in names:
+                            ins.append(names[v])
+                        else:
+                            raise Unsupported("merge input")
+                p.i[0], p.i[1] = len(merge), len(ins)
+                merge += ins
+            elif tag == "feBlend":
+                p.kind = A.FE_BLEND
+                p.in2 = inp("in2")
+                p.i[0] = A.BLEND[BLEND.get((c.get("mode") or "normal").strip(), "source-over")]
+            else:
+                raise Unsupported("filter primitive " + tag)
+            res = c.get("result")
+            if res:
+                names[res] = len(prims)
+            prims.append(p)
+        if not prims:
+            return None
+        f = A.Filter()
+        f.x, f.y, f.w, f.h = x, y, w, h
+        return self.tree.add_filter(f, prims, merge)
+
+
+def load_svg(text: str, tree_cls=None):
+    """Parses SVG text into a render tree (resvg_gb300.Tree)."""
+    if tree_cls is None:
+        from . import Tree as tree_cls
+    return Builder(text, tree_cls).load()
