@@ -12,8 +12,10 @@ pixel differs.
 
 Usage:  python tests/golden/pin_oracle.py <resvg checkout> [--write] [--verbose] [--only=<substring>]
   --write  rewrites tests/golden/oracle_pin.json (the committed summary) and
-           tests/golden/fixtures.npz (the parsed scenes and golden pixels of
-           the passing tests, replayed on the GPU by tests/test_gpu_golden.py).
+           tests/golden/fixtures.npz: for up to FIXTURES_PER_DIR passing tests
+           per test directory, the SVG text and the golden image (demultiplied
+           RGBA8), both zlib-compressed.  tests/test_oracle_golden.py replays
+           them on the oracle (CPU) and tests/test_gpu_golden.py on the GPU.
 """
 from __future__ import annotations
 
@@ -46,6 +48,7 @@ CATEGORIES = [
     "filters/filter-functions",
 ]
 IMAGE_SIZE = 300
+FIXTURES_PER_DIR = 4
 
 
 def render_size(tw, th):
@@ -133,7 +136,12 @@ def main():
             json.dump({"rule": "resvg integration suite: width 300, demultiplied, channel threshold 1, "
                                "pass = 0 differing pixels", "totals": tot, "tests": results}, f, indent=0,
                       sort_keys=True)
-        names = sorted(fixtures)
+        # a bounded subset travels with the repository: the first
+        # FIXTURES_PER_DIR passing tests of every test directory
+        by_dir = {}
+        for k in sorted(fixtures):
+            by_dir.setdefault(k.rsplit("/", 1)[0], []).append(k)
+        names = [k for v in by_dir.values() for k in v[:FIXTURES_PER_DIR]]
         blob = {}
         for i, k in enumerate(names):
             text, img = fixtures[k]

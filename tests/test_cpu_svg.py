@@ -1,0 +1,64 @@
+"""The SVG-subset front end (usvg stand-in) on its own."""
+import math
+
+import numpy as np
+import pytest
+
+from resvg_gb300 import _abi as A
+from resvg_gb300 import svg
+
+
+def test_arc_to_cubics_endpoints_and_count():
+    # a quarter circle of radius 50: kurbo needs ceil(n_err * 0.25) cubics
+    cubics = svg.svg_arc_to_cubics((100, 50), (50, 100), 50, 50, 0, False, True)
+    n_err = max((1.1163 * 50 / 0.1) ** (1 / 6), 3.999999)
+    assert len(cubics) == math.ceil(n_err * 0.25)
+    assert cubics[-1][4] == pytest.approx(50, abs=1e-9) and cubics[-1][5] == pytest.approx(100, abs=1e-9)
+    # every on-curve point lies on the circle
+    for c in cubics:
+        assert math.hypot(c[4] - 50, c[5] - 50) == pytest.approx(50, abs=1e-9)
+
+
+def test_degenerate_arc_is_a_line():
+    assert svg.svg_arc_to_cubics((0, 0), (10, 0), 0, 5, 0, False, True) is None
+    b = svg.parse_path_data("M0 0 A0 5 0 0 1 10 0")
+    assert b.verbs == [A.MOVE, A.LINE]
+
+
+def test_path_data_semantics():
+    b = svg.parse_path_data("m10 10 20 0 0 20 z l 5 5")
+    # implicit lineto after moveto; a segment after close starts at the subpath start
+    assert b.verbs == [A.MOVE, A.LINE, A.LINE, A.CLOSE, A.MOVE, A.LINE]
+    assert b.pts[-1] == (15.0, 15.0)
+    b = svg.parse_path_data("M0 0 H10 V10 h-10 Z")
+    assert b.pts == [(0, 0), (10, 0), (10, 10), (0, 10)]
+
+
+def test_smooth_curves_reflect_control_points():
+    b = svg.parse_path_data("M0 0 Q10 10 20 0 T40 0")
+    assert b.verbs == [A.MOVE, A.QUAD, A.QUAD]
+    assert b.pts[3] == (30.0, -10.0)
+
+
+def test_colors():
+    assert svg.parse_color("#0f0") == ((0, 255, 0), 1.0)
+    assert svg.parse_color("rgb(10%, 20%, 30%)")[0] == (26, 51, 76)
+    assert svg.parse_color("none") is None
+
+
+def test_transform_list():
+    t = svg.parse_transform("translate(10 20) scale(2)")
+    assert t == (2, 0, 0, 2, 10, 20)
+    t = svg.parse_transform("rotate(90)")
+    assert t[1] == pytest.approx(1) and t[2] == pytest.approx(-1)
+
+
+def test_rect_corners_in_f32(native):
+    text = ('<svg viewBox="0 0 1 1" xmlns="http://www.w3.org/2000/svg">'
+            '<rect x="0.2" y="0.2" width="0.6" height="0.6" rx="0.1"/></svg>')
+    tree = svg.load_svg(text)
+    v = tree.view().contents
+    p = v.paths[0]
+    pts = np.ctypeslib.as_array(v.points, shape=(v.point_count * 2,))[2 * p.point_offset:2 * (p.point_offset + 2)]
+    f = np.float32
+    assert pts[0] == f(0.2) + f(0.1) and pts[2] == (f(0.2) + f(0.6)) - f(0.1)
