@@ -153,6 +153,19 @@ int rgpu_filter_morphology(uint8_t *device_img, uint32_t width, uint32_t height,
 /* sRGB <-> linearRGB on premultiplied pixels: crates/resvg/src/filter/mod.rs:115-125. */
 int rgpu_filter_color_space(uint8_t *device_img, uint32_t width, uint32_t height, int to_linear, void *stream);
 
+/* Allocation-free box blur (no counterpart in the reference): the same result
+ * as rgpu_filter_box_blur, with the intermediate image in a fixed device array
+ * instead of a cudaMalloc'd buffer, for callers that may not allocate device
+ * memory (embedders that own the memory budget through their own allocator or
+ * a hard cap, and latency paths where cudaMalloc/cudaFree would synchronise
+ * the device).  At most 1,048,576 pixels per image (4 MiB of scratch); larger
+ * images return RGPU_ERR_INVALID_ARG.  The first call on a device does the
+ * set-up (looks up the array's address) and should come before any stream
+ * capture.  The scratch is shared by all calls on a device: overlapping calls
+ * race.  NULL stream = the default stream; returns after the blur finished. */
+int rgpu_filter_box_blur_noalloc(uint8_t *device_img, uint32_t width, uint32_t height, double sigma_x,
+                                 double sigma_y, void *stream);
+
 /* ---- differentiable soft-coverage form ---------------------------------- */
 /* Scene parameters for the analytic-area soft rasteriser (no counterpart in
  * the reference).  See resvg_gb300/csrc/kernels/soft.cu. */

@@ -419,6 +419,11 @@ int render_host(const rgpu_tree *tree, const resvg_transform &ts, uint32_t w, ui
 }
 
 }  // namespace
+
+// Sets the calling thread's rgpu_last_error() text (for entry points in other
+// translation units).
+void set_last_error_message(const char *msg) { g_last_error = msg ? msg : ""; }
+
 }  // namespace rgpu
 
 using namespace rgpu;
