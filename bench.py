@@ -39,7 +39,10 @@ CONFIG_DESC = {
     0: "512x512, 200 solid cubic loops (non-zero/even-odd), source-over",
     1: "1024x1024, 2000 gradient fills + 500 strokes + 20 nested clips + 10 luminance masks",
     2: "2048x2048, 500 cubic loops + blur/saturate/morphology/arithmetic filter chain (linearRGB)",
+    3: "batched: 4096 scenes, side log-uniform 64-1024, paths log-uniform 10-2000 (config-1 paint mix, "
+       "20% strokes, 10% with a clip and a blur)",
 }
+TUNING_CANDIDATES = [(1, 4), (2, 4), (4, 4), (8, 4), (2, 8), (4, 8), (8, 8), (4, 16), (8, 16)]
 SEED = 2026
 
 
@@ -52,6 +55,9 @@ def parse():
     ap.add_argument("--config", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--scenes", type=int, default=4096, help="scenes per step of the batched form (config 3)")
+    ap.add_argument("--plain-sample", type=int, default=128,
+                    help="scenes rendered one by one through the plain drop-in for the batched comparison")
     ap.add_argument("--scale", type=float, default=1.0,
                     help="path-count scale of the workload (1.0 = the full workload; smaller only for profiling)")
     return ap.parse_args()
@@ -184,11 +190,128 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def run_batched(args, rank, world):
+    """Config 3: thousands of independent scenes in one prepared submission
+    (one persistent raster kernel per stage, CUDA-graph replay), against the
+    same scenes rendered one call at a time through the plain GPU drop-in."""
+    import torch
+    import resvg_gb300 as R
+    from resvg_gb300 import build as B
+    B.build()
+    R.init(0)
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    torch.cuda.set_device(dev)
+    n = args.scenes
+    trees = [R.Tree.generate(3, seed=SEED, index=rank * n + i, scale=args.scale) for i in range(n)]
+    sizes = [tuple(int(v) for v in t.size) for t in trees]
+    offs, total = [], 0
+    for w, h in sizes:
+        offs.append(total)
+        total += ((w * h * 4 + 255) // 256) * 256
+    buf = torch.zeros(total, dtype=torch.uint8, device=dev)
+    base = buf.data_ptr()
+    ptrs = [base + o for o in offs]
+    ws = [w for w, _ in sizes]
+    hs = [h for _, h in sizes]
+    ident = [(1, 0, 0, 1, 0, 0)] * n
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
+    sh = stream.cuda_stream
+    # autotune the raster decomposition on a stratified sample of the scenes
+    samp = list(range(0, n, max(1, n // 256)))
+    t0 = time.perf_counter()
+    best, best_ms = R.autotune([trees[i] for i in samp], [ident[i] for i in samp], [ws[i] for i in samp],
+                               [hs[i] for i in samp], [ptrs[i] for i in samp], TUNING_CANDIDATES, reps=2)
+    tune_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    scene = R.Scene(trees, ident, ws, hs, ptrs)
+    prep_s = time.perf_counter() - t0
+
+    def step():
+        s0 = torch.cuda.Event(enable_timing=True)
+        s1 = torch.cuda.Event(enable_timing=True)
+        s0.record(stream)
+        scene.render(sh)
+        s1.record(stream)
+        return s0, s1
+
+    for _ in range(args.warmup):
+        step()
+        scene.check()
+    info = scene.info()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    step_ms = []
+    with ClockSampler() as clk:
+        for _ in range(args.steps):
+            s0, s1 = step()
+            scene.check()
+            step_ms.append(s0.elapsed_time(s1))
+        torch.cuda.synchronize()
+    ms = sum(step_ms) / len(step_ms)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * n * 1e3 / ms
+    out_px = sum(w * h for w, h in sizes)
+    # plain per-scene drop-in (device pixmap, one call per scene, synchronised)
+    psamp = list(range(0, n, max(1, n // max(1, args.plain_sample))))
+    for i in psamp[:4]:
+        R.render_device(trees[i], ident[i], ws[i], hs[i], ptrs[i], ws[i] * 4, sh)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in psamp:
+        R.render_device(trees[i], ident[i], ws[i], hs[i], ptrs[i], ws[i] * 4, sh)
+        stream.synchronize()
+    plain_s = time.perf_counter() - t0
+    plain_value = len(psamp) / plain_s
+    # end to end through the public batch call: flatten + upload + render + read back every output
+    pinned = torch.empty(total, dtype=torch.uint8, pin_memory=True)
+    e2e_t = []
+    for _ in range(max(1, args.e2e_steps if args.e2e_steps < 5 else 1)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        R.render_batch(trees, ident, ws, hs, ptrs, sh)
+        pinned.copy_(buf, non_blocking=True)
+        torch.cuda.synchronize()
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_ms = 1e3 * sum(e2e_t) / len(e2e_t)
+    st = R.stats()
+    line = {
+        "metric": "scenes/s (batched render, config 3)", "value": value, "unit": "scenes/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic (seeded generator, seed %d)" % SEED,
+        "config": {"workload": "config3: %s" % CONFIG_DESC[3], "scenes": n, "output_mpix": out_px / 1e6,
+                   "draws": info["draws"], "edges": info["edges"], "binned_edges": info["binned_edges"],
+                   "work_items": info["work_items"], "tuning": {"band_rows": best[0], "pixels_per_thread": best[1],
+                                                                "autotune_ms_on_sample": best_ms,
+                                                                "autotune_s": tune_s},
+                   "prepare_s": prep_s, "l2": "outputs %.1f GB > L2" % (total / 1e9), "graph_replay": True},
+        "mpix_s": value * out_px / n / 1e6 if n else 0.0,
+        "plain": {"value": plain_value, "unit": "scenes/s", "sample_scenes": len(psamp),
+                  "how": "rgpu_render_device per scene (host flatten + upload + kernels), synchronised"},
+        "batched_vs_plain": value / plain_value,
+        "e2e": {"value": n * 1e3 / e2e_ms, "unit": "scenes/s", "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": int(st["h2d_bytes"]), "d2h_bytes_per_step": int(total)},
+        "gpu_launches": int(info["kernel_launches"]) * args.steps,
+        "clocks": clk.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
 def main():
     args = parse()
     rank, world = dist_setup(args.gpus)
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.config == 3:
+        run_batched(args, rank, world)
         return
     import torch
     import resvg_gb300 as R

@@ -131,6 +131,14 @@ typedef struct rgpu_tuning {
 } rgpu_tuning;
 int rgpu_set_tuning(const rgpu_tuning *t);
 int rgpu_get_tuning(rgpu_tuning *t);
+/* Autotuner (no counterpart in the reference): prepares the given scenes once
+ * per candidate tuning, times `reps` graph replays of each with CUDA events,
+ * keeps the fastest as the current tuning and returns it (and its ms per
+ * render).  Candidates that fail are skipped. */
+int rgpu_autotune(const resvg_render_tree *const *trees, const resvg_transform *transforms, uint32_t count,
+                  const uint32_t *widths, const uint32_t *heights, uint8_t *const *device_pixmaps,
+                  const uint32_t *strides, const rgpu_tuning *candidates, uint32_t candidate_count, uint32_t reps,
+                  rgpu_tuning *best, float *best_ms);
 
 /* Per-call statistics of the last render on this thread (for benchmarking). */
 typedef struct rgpu_stats {

@@ -204,6 +204,34 @@ def get_tuning():
     return t.band_rows, t.pixels_per_thread
 
 
+def autotune(trees, transforms, widths, heights, device_ptrs, candidates, reps: int = 3, strides=None):
+    """Times each (band_rows, pixels_per_thread) candidate on the given scenes
+    (rgpu_autotune), keeps the fastest as the current tuning and returns
+    ((band_rows, pixels_per_thread), ms per render)."""
+    L = lib()
+    P = C.c_void_p
+    L.rgpu_autotune.restype = C.c_int
+    L.rgpu_autotune.argtypes = [C.POINTER(P), C.POINTER(_abi.ResvgTransform), C.c_uint32, C.POINTER(C.c_uint32),
+                                C.POINTER(C.c_uint32), C.POINTER(P), C.POINTER(C.c_uint32),
+                                C.POINTER(_abi.Tuning), C.c_uint32, C.c_uint32, C.POINTER(_abi.Tuning),
+                                C.POINTER(C.c_float)]
+    n = len(trees)
+    for t in trees:
+        t.view()
+    th = (P * n)(*[t.handle for t in trees])
+    ts = (_abi.ResvgTransform * n)(*[_rt(t) for t in transforms])
+    ws = (C.c_uint32 * n)(*[int(w) for w in widths])
+    hs = (C.c_uint32 * n)(*[int(h) for h in heights])
+    ps = (P * n)(*[int(p) for p in device_ptrs])
+    ss = (C.c_uint32 * n)(*[int(s) for s in strides]) if strides is not None else None
+    cand = (_abi.Tuning * len(candidates))(*[_abi.Tuning(b, p, 0) for b, p in candidates])
+    best = _abi.Tuning()
+    ms = C.c_float(0)
+    check(L.rgpu_autotune(th, ts, n, ws, hs, ps, ss, cand, len(candidates), reps, C.byref(best), C.byref(ms)),
+          "rgpu_autotune")
+    return (best.band_rows, best.pixels_per_thread), ms.value
+
+
 def stats():
     s = _abi.Stats()
     check(lib().rgpu_get_stats(C.byref(s)), "rgpu_get_stats")

@@ -233,6 +233,15 @@ int plan_scene(Context &c, Plan &p) {
                     p.items.push_back(WorkItem{si, b, x0, std::min(x0 + cw, st.out_w)});
         }
         p.level_cnt[lv] = (uint32_t)p.items.size() - p.level_off[lv];
+        // the persistent kernel takes items in order: heaviest first (draws x
+        // pixels) shortens the tail when scenes of very different cost share
+        // a launch
+        auto cost = [&](const WorkItem &it) {
+            const StreamRec &st = sb.streams[it.stream];
+            return (uint64_t)st.draw_cnt * (uint64_t)(it.x1 - it.x0) * st.band_rows;
+        };
+        std::stable_sort(p.items.begin() + p.level_off[lv], p.items.end(),
+                         [&](const WorkItem &a, const WorkItem &b) { return cost(a) > cost(b); });
     }
     if (p.nbins > 0xF0000000ull) { set_error("too many (band, draw) bins"); return RGPU_ERR_CAPACITY; }
     uint32_t per_sm = (uint32_t)raster_max_blocks_per_sm((int)p.px);
@@ -677,6 +686,62 @@ int rgpu_get_tuning(rgpu_tuning *t) {
     t->band_rows = c.tuning.band_rows;
     t->pixels_per_thread = c.tuning.px;
     t->reserved = 0;
+    return RGPU_OK;
+}
+
+int rgpu_autotune(const resvg_render_tree *const *trees, const resvg_transform *transforms, uint32_t count,
+                  const uint32_t *widths, const uint32_t *heights, uint8_t *const *device_pixmaps,
+                  const uint32_t *strides, const rgpu_tuning *candidates, uint32_t ncand, uint32_t reps,
+                  rgpu_tuning *best, float *best_ms) {
+    g_last_error.clear();
+    if (!candidates || !ncand || !best || !reps) { set_error("invalid arguments"); return RGPU_ERR_INVALID_ARG; }
+    rgpu_tuning saved;
+    rgpu_get_tuning(&saved);
+    cudaStream_t s;
+    {
+        Context &c = ctx();
+        std::lock_guard<std::mutex> lock(c.mu);
+        int r = ensure_device(c);
+        if (r) return r;
+        s = c.stream;
+    }
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    if (cudaEventCreate(&e1) != cudaSuccess) { cudaEventDestroy(e0); set_error("event"); return RGPU_ERR_CUDA; }
+    float best_t = 0.0f;
+    int best_i = -1, last_err = RGPU_OK;
+    for (uint32_t i = 0; i < ncand; i++) {
+        if (rgpu_set_tuning(&candidates[i]) != RGPU_OK) continue;
+        rgpu_scene *sc = nullptr;
+        int r = rgpu_scene_prepare(trees, transforms, count, widths, heights, device_pixmaps, strides, &sc);
+        // first render sizes the buffers, the second captures the graph
+        if (r == RGPU_OK) r = rgpu_scene_render(sc, s);
+        if (r == RGPU_OK) r = rgpu_scene_render(sc, s);
+        if (r == RGPU_OK) r = rgpu_scene_check(sc, nullptr);
+        float ms = 0.0f;
+        if (r == RGPU_OK) {
+            cudaEventRecord(e0, s);
+            for (uint32_t k = 0; k < reps && r == RGPU_OK; k++) r = rgpu_scene_render(sc, s);
+            cudaEventRecord(e1, s);
+            if (r == RGPU_OK) r = rgpu_scene_check(sc, nullptr);
+            if (r == RGPU_OK && cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) r = RGPU_ERR_CUDA;
+            ms /= (float)reps;
+        }
+        if (sc) rgpu_scene_free(sc);
+        if (r != RGPU_OK) { last_err = r; continue; }
+        if (best_i < 0 || ms < best_t) { best_t = ms; best_i = (int)i; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (best_i < 0) {
+        rgpu_set_tuning(&saved);
+        if (g_last_error.empty()) set_error("no candidate tuning rendered");
+        return last_err != RGPU_OK ? last_err : RGPU_ERR_INVALID_ARG;
+    }
+    rgpu_set_tuning(&candidates[best_i]);
+    *best = candidates[best_i];
+    if (best_ms) *best_ms = best_t;
+    g_last_error.clear();
     return RGPU_OK;
 }
 
