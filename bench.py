@@ -41,6 +41,8 @@ CONFIG_DESC = {
     2: "2048x2048, 500 cubic loops + blur/saturate/morphology/arithmetic filter chain (linearRGB)",
     3: "batched: 4096 scenes, side log-uniform 64-1024, paths log-uniform 10-2000 (config-1 paint mix, "
        "20% strokes, 10% with a clip and a blur)",
+    4: "differentiable: 256 scenes of 256x256, 64 closed cubic paths (4-16 segments), solid/4-stop linear "
+       "gradient paints, one Gaussian blur (learnable sigma), L2 loss against a perturbed target",
 }
 TUNING_CANDIDATES = [(1, 4), (2, 4), (4, 4), (8, 4), (2, 8), (4, 8), (8, 8), (4, 16), (8, 16)]
 SEED = 2026
@@ -304,6 +306,79 @@ def run_batched(args, rank, world):
         torch.distributed.destroy_process_group()
 
 
+def run_soft(args, rank, world):
+    """Config 4: forward soft-coverage render + hand-written adjoint of an L2
+    loss over 256 scenes; one step = forward, loss and all parameter gradients."""
+    import torch
+    from resvg_gb300 import build as B
+    from resvg_gb300 import soft
+    import resvg_gb300 as R
+    B.build()
+    R.init(0)
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    torch.cuda.set_device(dev)
+    a = soft.make_scenes(seed=SEED + rank, scenes=256, size=256, paths=64)
+    t = soft.perturb(a, seed=SEED + 1000 + rank)
+    sc, tgt = soft.Scenes(a), soft.Scenes(t)
+    _, target = soft.forward(tgt)
+
+    def step():
+        image, blurred = soft.forward(sc)
+        loss, g = soft.mse(blurred, target)
+        return loss, soft.backward(sc, image, g)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    ms_list = []
+    with ClockSampler() as clk:
+        for _ in range(args.steps):
+            s0 = torch.cuda.Event(enable_timing=True)
+            s1 = torch.cuda.Event(enable_timing=True)
+            s0.record()
+            loss, grads = step()
+            s1.record()
+            torch.cuda.synchronize()
+            ms_list.append(s0.elapsed_time(s1))
+    ms = sum(ms_list) / len(ms_list)
+    if world > 1:
+        tt = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        ms = float(tt.item())
+    value = world * 256 * 1e3 / ms
+    # end to end: parameters from pinned host memory, gradients back to the host
+    host = {k: torch.from_numpy(np.ascontiguousarray(a[k])).pin_memory() for k in soft.PARAMS}
+    e2e = []
+    for _ in range(max(1, min(args.e2e_steps, 3))):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k in soft.PARAMS:
+            sc.params[k].copy_(host[k], non_blocking=True)
+        loss, grads = step()
+        out = {k: grads[k].to("cpu", non_blocking=True) for k in soft.PARAMS}
+        torch.cuda.synchronize()
+        e2e.append(time.perf_counter() - t0)
+    e2e_ms = 1e3 * sum(e2e) / len(e2e)
+    h2d = sum(int(host[k].numel()) * 4 for k in soft.PARAMS)
+    line = {
+        "metric": "grads/s (scenes x (forward + adjoint) per second, config 4)", "value": value,
+        "unit": "scenes/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded generator, seed %d)" % SEED,
+        "config": {"workload": "config4: %s" % CONFIG_DESC[4], "scenes": 256, "canvas": [256, 256], "paths": 64,
+                   "segments": int(a["seg_offset"][-1]), "loss": loss},
+        "mpix_s": value * 256 * 256 / 1e6,
+        "e2e": {"value": 256 * 1e3 / e2e_ms, "unit": "scenes/s", "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d},
+        "gpu_launches": 12 * args.steps,
+        "clocks": clk.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
 def main():
     args = parse()
     rank, world = dist_setup(args.gpus)
@@ -312,6 +387,9 @@ def main():
         return
     if args.config == 3:
         run_batched(args, rank, world)
+        return
+    if args.config == 4:
+        run_soft(args, rank, world)
         return
     import torch
     import resvg_gb300 as R

@@ -175,18 +175,45 @@ int rgpu_filter_box_blur_noalloc(uint8_t *device_img, uint32_t width, uint32_t h
                                  double sigma_y, void *stream);
 
 /* ---- differentiable soft-coverage form ---------------------------------- */
-/* Scene parameters for the analytic-area soft rasteriser (no counterpart in
- * the reference).  See resvg_gb300/csrc/kernels/soft.cu. */
-typedef struct rgpu_soft_scene {
-    uint32_t width, height;     /* canvas */
-    uint32_t path_count;        /* closed cubic paths */
-    const uint32_t *seg_offset; /* path i owns cubic segments [seg_offset[i], seg_offset[i+1]) */
-    float *points;              /* 3 control points (x,y) per segment + implicit start: see soft.cu */
-    float *colors;              /* RGBA per path (straight alpha) */
-    float *stops;               /* 4 stops x (offset, r, g, b, a) per path, linear gradient */
-    float *grad_line;           /* (x1,y1,x2,y2) per path */
-    float *sigma;               /* blur sigma (1 per scene) */
-} rgpu_soft_scene;
+/* A batch of scenes for the FP32 analytic-area soft rasteriser and its
+ * hand-written adjoint (no counterpart in the reference: resvg's coverage is
+ * not differentiable).  All pointers are DEVICE pointers; every scene has the
+ * same canvas (width <= 1024) and `paths_per_scene` closed cubic paths drawn
+ * in order.  Path j = scene * paths_per_scene + p owns n = seg_offset[j+1] -
+ * seg_offset[j] cubics and the 3n points (x, y) starting at
+ * points[2 * 3 * seg_offset[j]]: its start point, then (control 1, control 2,
+ * end) per cubic except the last, which has (control 1, control 2) and ends
+ * at the start point (closed by construction).  See
+ * resvg_gb300/csrc/kernels/soft.cu for the coverage, paint, composite and blur
+ * definitions. */
+typedef struct rgpu_soft_batch {
+    uint32_t scenes, width, height, paths_per_scene;
+    uint32_t total_segments;     /* seg_offset[scenes * paths_per_scene] */
+    const uint32_t *seg_offset;  /* scenes * paths_per_scene + 1 */
+    const float *points;         /* (x, y) pairs as above */
+    const uint32_t *paint_kind;  /* per path: 0 solid colour, 1 linear gradient */
+    const float *colors;         /* per path: straight RGBA (solid) */
+    const float *stop_offsets;   /* per path: 4 ascending offsets (gradient) */
+    const float *stop_colors;    /* per path: 4 straight RGBA stop colours */
+    const float *grad_line;      /* per path: x1, y1, x2, y2 of the gradient (pad spread) */
+    const float *sigma;          /* per scene: Gaussian blur sigma */
+} rgpu_soft_batch;
+/* Gradients, same layouts as the parameters (device; overwritten). */
+typedef struct rgpu_soft_grads {
+    float *points, *colors, *stop_offsets, *stop_colors, *sigma;
+} rgpu_soft_grads;
+/* image = composite (premultiplied RGBA, scenes x height x width x 4 floats),
+ * blurred = its Gaussian blur.  Synchronous. */
+int rgpu_soft_forward(const rgpu_soft_batch *batch, float *image, float *blurred, void *stream);
+/* Vector-Jacobian product: given dL/d(blurred) (same layout), writes dL/d of
+ * every parameter.  `image` is the forward's composite.  Coverage is
+ * recomputed row by row; scratch is bounded by the number of SMs. */
+int rgpu_soft_backward(const rgpu_soft_batch *batch, const float *image, const float *grad_blurred,
+                       rgpu_soft_grads *grads, void *stream);
+/* Mean squared error over `count` floats: loss (1 float) and, if non-null,
+ * dloss/d(blurred). */
+int rgpu_soft_mse(const float *blurred, const float *target, size_t count, float *loss, float *grad_blurred,
+                  void *stream);
 
 #ifdef __cplusplus
 }

@@ -4,7 +4,9 @@ A C++ restatement of resvg 0.48.1's render path (crates/resvg/src/{render,path,
 clip,mask,geom}.rs, crates/resvg/src/filter/*.rs) over a restatement of the
 tiny-skia 0.12.0 raster pipeline (not vendored in the reference; Skia's
 published algorithms).  Parity with resvg is pinned against resvg's own golden
-PNGs (crates/resvg/tests/tests/**, see tests/test_golden.py).
+PNGs (crates/resvg/tests/tests/**; tests/golden/pin_oracle.py and
+tests/test_oracle_golden.py).  soft.cpp is the FP64 reference of the
+differentiable soft-coverage renderer (forward + forward-mode gradients).
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may load
 this module.  The product (resvg_gb300) never imports it.
@@ -98,3 +100,50 @@ def to_linear(img):
 
 def to_srgb(img):
     return _img_op("oracle_to_srgb", img)
+
+
+def _soft_struct(arrays):
+    """rgpu_soft_batch over host numpy arrays (kept alive by the caller)."""
+    from resvg_gb300 import _abi
+    b = _abi.SoftBatch()
+    b.scenes, b.width, b.height, b.paths_per_scene = (int(arrays[k]) for k in ("scenes", "width", "height", "paths"))
+    b.total_segments = int(arrays["seg_offset"][-1])
+    for f, k in (("seg_offset", "seg_offset"), ("points", "points"), ("paint_kind", "paint_kind"),
+                 ("colors", "colors"), ("stop_offsets", "stop_offsets"), ("stop_colors", "stop_colors"),
+                 ("grad_line", "grad_line"), ("sigma", "sigma")):
+        setattr(b, f, arrays[k].ctypes.data)
+    return b
+
+
+def soft_forward(arrays):
+    """FP64 forward: (image, blurred) as (S, H, W, 4) float64 arrays."""
+    L = lib()
+    L.oracle_soft_forward.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+    b = _soft_struct(arrays)
+    shape = (int(arrays["scenes"]), int(arrays["height"]), int(arrays["width"]), 4)
+    im = np.zeros(shape, np.float64)
+    bl = np.zeros(shape, np.float64)
+    L.oracle_soft_forward(C.byref(b), im.ctypes.data, bl.ctypes.data)
+    return im, bl
+
+
+def soft_dloss(arrays, target, direction):
+    """(loss, dloss/dv) in FP64 for a parameter direction v (dict of float64
+    arrays keyed like the parameters; missing keys are zero)."""
+    L = lib()
+    L.oracle_soft_dloss.argtypes = [C.c_void_p, C.c_void_p] + [C.c_void_p] * 5 + [C.c_void_p, C.c_void_p]
+    b = _soft_struct(arrays)
+    t = np.ascontiguousarray(target, dtype=np.float32)
+    keep = []
+
+    def ptr(k):
+        if k not in direction:
+            return None
+        a = np.ascontiguousarray(direction[k], dtype=np.float64)
+        keep.append(a)
+        return a.ctypes.data
+    loss = C.c_double()
+    dl = C.c_double()
+    L.oracle_soft_dloss(C.byref(b), t.ctypes.data, ptr("points"), ptr("colors"), ptr("stop_offsets"),
+                        ptr("stop_colors"), ptr("sigma"), C.byref(loss), C.byref(dl))
+    return loss.value, dl.value

@@ -104,6 +104,20 @@ class Stats(C.Structure):
                 ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64), ("raster_ms", f32)]
 
 
+class SoftBatch(C.Structure):
+    """rgpu_soft_batch (resvg_gpu.h): pointers are device pointers for the
+    product and host pointers for the FP64 reference."""
+    _fields_ = [("scenes", u32), ("width", u32), ("height", u32), ("paths_per_scene", u32),
+                ("total_segments", u32), ("seg_offset", C.c_void_p), ("points", C.c_void_p),
+                ("paint_kind", C.c_void_p), ("colors", C.c_void_p), ("stop_offsets", C.c_void_p),
+                ("stop_colors", C.c_void_p), ("grad_line", C.c_void_p), ("sigma", C.c_void_p)]
+
+
+class SoftGrads(C.Structure):
+    _fields_ = [("points", C.c_void_p), ("colors", C.c_void_p), ("stop_offsets", C.c_void_p),
+                ("stop_colors", C.c_void_p), ("sigma", C.c_void_p)]
+
+
 # enums (rgpu_tree.h)
 MOVE, LINE, QUAD, CUBIC, CLOSE = range(5)
 NONZERO, EVENODD = 0, 1
