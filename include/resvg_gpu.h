@@ -75,8 +75,10 @@ resvg_render_tree *rgpu_tree_generate(int config, uint64_t seed, uint64_t index,
 /* resvg_render: crates/c-api/resvg.h:485, lib.rs:875-893. */
 void resvg_render(const resvg_render_tree *tree, resvg_transform transform, uint32_t width, uint32_t height,
                   char *pixmap);
-/* resvg_render_node: crates/c-api/resvg.h:505, lib.rs:908-942.  `id` is the
- * index of a root child given as a decimal string (the tree keeps no SVG ids). */
+/* resvg_render_node: crates/c-api/resvg.h:505, lib.rs:908-942 (resvg::render_node,
+ * crates/resvg/src/lib.rs:55-70).  The tree keeps no SVG ids: `id` is "<n>" for
+ * group n or "p<n>" for path n.  The node's absolute layer bounding box is moved
+ * to the pixmap origin; returns false for an unknown id or an empty box. */
 bool resvg_render_node(const resvg_render_tree *tree, const char *id, resvg_transform transform, uint32_t width,
                        uint32_t height, char *pixmap);
 

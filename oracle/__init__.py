@@ -62,6 +62,20 @@ def render(tree_view_ptr, transform, width: int, height: int, pixmap: np.ndarray
     return pixmap
 
 
+def render_node(tree_view_ptr, node_id: str, transform, width: int, height: int,
+                pixmap: np.ndarray | None = None):
+    """resvg_render_node restated (lib.rs:55-70); None when the node has no box."""
+    L = lib()
+    L.oracle_render_node.argtypes = [C.c_void_p, C.c_char_p, C.POINTER(C.c_float), C.c_uint32, C.c_uint32,
+                                     C.c_void_p]
+    if pixmap is None:
+        pixmap = np.zeros((height, width, 4), dtype=np.uint8)
+    ts = (C.c_float * 6)(*[float(v) for v in transform])
+    r = L.oracle_render_node(C.cast(tree_view_ptr, C.c_void_p), node_id.encode(), ts, width, height,
+                             pixmap.ctypes.data)
+    return pixmap if r == 0 else None
+
+
 def render_parallel(tree_view_ptr, transform, width: int, height: int, threads: int,
                     pixmap: np.ndarray | None = None) -> np.ndarray:
     """All-core timing variant of render(): strips of the canvas on `threads` threads."""

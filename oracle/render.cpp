@@ -11,7 +11,9 @@
 // (resvg_gb300/csrc/host/geom.cpp), the same input preparation the GPU path uses.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
+#include <vector>
 #include "raster.h"
 #include "../resvg_gb300/csrc/host/tree.h"
 
@@ -270,10 +272,66 @@ void render_tree(const rgpu_tree_view &t, const Transform &ts, Pixmap &pm) {
     render_nodes(c, 0, ts, pm);
 }
 
+// lib.rs:55-70 (resvg::render_node) behind the C API's id lookup
+// (crates/c-api/lib.rs:908-942).  Ids: "<n>" is group n, "p<n>" is path n.
+bool render_node_id(const rgpu_tree_view &t, const char *id, const Transform &ts_in, Pixmap &pm) {
+    if (!id || !*id) return false;
+    const bool is_path = id[0] == 'p';
+    char *end = nullptr;
+    const unsigned long idx = std::strtoul(id + (is_path ? 1 : 0), &end, 10);
+    if (!end || *end || end == id + (is_path ? 1 : 0)) return false;
+    if (idx >= (is_path ? (unsigned long)t.path_count : (unsigned long)t.group_count)) return false;
+    std::vector<int32_t> gp(t.group_count, -1), pp(t.path_count, -1);
+    for (uint32_t g = 0; g < t.group_count; g++)
+        for (uint32_t k = 0; k < t.groups[g].child_count; k++) {
+            const rgpu_node &n = t.children[t.groups[g].child_offset + k];
+            (n.kind == RGPU_NODE_GROUP ? gp : pp)[n.index] = (int32_t)g;
+        }
+    auto tf = [](const rgpu_transform &x) { return Transform::from_row(x.sx, x.ky, x.kx, x.sy, x.tx, x.ty); };
+    Transform abs = is_path ? Transform() : tf(t.groups[idx].transform);
+    for (int32_t g = is_path ? pp[idx] : gp[idx]; g >= 0; g = gp[g]) abs = tf(t.groups[g].transform).pre_concat(abs);
+    Rect r;
+    if (is_path) {
+        const rgpu_path &p = t.paths[idx];
+        r = Rect{p.bbox_x, p.bbox_y, p.bbox_x + p.bbox_w, p.bbox_y + p.bbox_h};
+    } else {
+        const rgpu_group &g = t.groups[idx];
+        if (!g.has_layer_bbox) return false;
+        r = Rect{g.layer_x, g.layer_y, g.layer_x + g.layer_w, g.layer_y + g.layer_h};
+    }
+    if (!(r.r > r.l && r.b > r.t)) return false;
+    // NonZeroRect::transform: bounds of the mapped corners
+    Point c[4] = {{r.l, r.t}, {r.r, r.t}, {r.r, r.b}, {r.l, r.b}};
+    abs.map_points(c, 4);
+    float l = c[0].x, tp = c[0].y, rr = c[0].x, b = c[0].y;
+    for (int i = 1; i < 4; i++) {
+        l = std::min(l, c[i].x); rr = std::max(rr, c[i].x);
+        tp = std::min(tp, c[i].y); b = std::max(b, c[i].y);
+    }
+    if (!(rr > l && b > tp)) return false;
+    Transform ts = ts_in.pre_concat(Transform::translate(-l, -tp));
+    Ctx cx{t, max_filter_bbox(pm.width, pm.height)};
+    if (is_path) render_path(cx, (uint32_t)idx, ts, pm);
+    else render_group(cx, (uint32_t)idx, ts, pm);
+    return true;
+}
+
 }  // namespace ora
 
 // ---------------------------------------------------------------- C entry points (tests / bench only)
 extern "C" {
+
+// resvg_render_node with the same id convention as the product's.
+int oracle_render_node(const rgpu_tree_view *tree, const char *id, const float ts6[6], uint32_t w, uint32_t h,
+                       uint8_t *pixmap) {
+    if (!tree || !pixmap || w == 0 || h == 0) return -1;
+    ora::Pixmap pm(w, h);
+    std::memcpy(pm.data.data(), pixmap, (size_t)w * h * 4);
+    ora::Transform ts = ora::Transform::from_row(ts6[0], ts6[1], ts6[2], ts6[3], ts6[4], ts6[5]);
+    if (!ora::render_node_id(*tree, id, ts, pm)) return 1;
+    std::memcpy(pixmap, pm.data.data(), (size_t)w * h * 4);
+    return 0;
+}
 
 // Renders `tree` onto the premultiplied RGBA8 `pixmap` (w*h*4 bytes), drawing
 // onto its existing content, as resvg_render does.

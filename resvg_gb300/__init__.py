@@ -172,6 +172,70 @@ def render(tree: Tree, transform=(1, 0, 0, 1, 0, 0), width: int | None = None, h
     return pixmap
 
 
+def node_abs_bbox(tree: Tree, node_id: str):
+    """Absolute layer bounding box (x, y, w, h) of a node, the box resvg's
+    render_node places at the pixmap origin; None for a zero-sized box.
+    Ids: "<n>" is group n, "p<n>" is path n."""
+    v = tree.view().contents
+    is_path = node_id.startswith("p")
+    idx = int(node_id[1:] if is_path else node_id)
+    gp = [-1] * v.group_count
+    pp = [-1] * v.path_count
+    for g in range(v.group_count):
+        gr = v.groups[g]
+        for k in range(gr.child_count):
+            n = v.children[gr.child_offset + k]
+            (gp if n.kind == _abi.NODE_GROUP else pp)[n.index] = g
+    f32 = np.float32
+
+    def concat(a, b):  # tiny-skia Transform::concat (f64 products for skewed matrices)
+        if a == (1, 0, 0, 1, 0, 0):
+            return b
+        if b == (1, 0, 0, 1, 0, 0):
+            return a
+        if a[1] == 0 and a[2] == 0 and b[1] == 0 and b[2] == 0:
+            return (f32(a[0] * b[0]), 0.0, 0.0, f32(a[3] * b[3]), f32(f32(a[0] * b[4]) + a[4]), f32(f32(a[3] * b[5]) + a[5]))
+        m = lambda p, q, r, s_: float(f32(float(p) * float(q) + float(r) * float(s_)))  # noqa: E731
+        return (m(a[0], b[0], a[2], b[1]), m(a[1], b[0], a[3], b[1]), m(a[0], b[2], a[2], b[3]),
+                m(a[1], b[2], a[3], b[3]), float(f32(m(a[0], b[4], a[2], b[5]) + a[4])),
+                float(f32(m(a[1], b[4], a[3], b[5]) + a[5])))
+    tup = lambda t: tuple(float(x) for x in t.tuple())  # noqa: E731
+    ab = (1.0, 0.0, 0.0, 1.0, 0.0, 0.0) if is_path else tup(v.groups[idx].transform)
+    g = pp[idx] if is_path else gp[idx]
+    while g >= 0:
+        ab = concat(tup(v.groups[g].transform), ab)
+        g = gp[g]
+    if is_path:
+        p = v.paths[idx]
+        r = (p.bbox_x, p.bbox_y, p.bbox_x + p.bbox_w, p.bbox_y + p.bbox_h)
+    else:
+        gr = v.groups[idx]
+        if not gr.has_layer_bbox:
+            return None
+        r = (gr.layer_x, gr.layer_y, gr.layer_x + gr.layer_w, gr.layer_y + gr.layer_h)
+    if not (r[2] > r[0] and r[3] > r[1]):
+        return None
+    xs, ys = [], []
+    for x, y in ((r[0], r[1]), (r[2], r[1]), (r[2], r[3]), (r[0], r[3])):
+        x, y = f32(x), f32(y)
+        xs.append(float(f32(f32(f32(x * f32(ab[0])) + f32(y * f32(ab[2]))) + f32(ab[4]))))
+        ys.append(float(f32(f32(f32(x * f32(ab[1])) + f32(y * f32(ab[3]))) + f32(ab[5]))))
+    l, t, rr, b = min(xs), min(ys), max(xs), max(ys)
+    return (l, t, rr - l, b - t) if rr > l and b > t else None
+
+
+def render_node(tree: Tree, node_id: str, transform, width: int, height: int,
+                pixmap: np.ndarray | None = None) -> np.ndarray | None:
+    """resvg_render_node through the C ABI; None when the id is unknown or the
+    node's bounding box is empty."""
+    if pixmap is None:
+        pixmap = np.zeros((int(height), int(width), 4), dtype=np.uint8)
+    tree.view()
+    ok = lib().resvg_render_node(tree.handle, node_id.encode(), _rt(transform), pixmap.shape[1], pixmap.shape[0],
+                                 pixmap.ctypes.data)
+    return pixmap if ok else None
+
+
 def render_device(tree: Tree, transform, width: int, height: int, device_ptr: int, stride: int,
                   stream: int = 0) -> None:
     """Renders onto a device pixmap (e.g. a torch.uint8 CUDA tensor's data_ptr())."""

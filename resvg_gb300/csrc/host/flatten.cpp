@@ -509,6 +509,11 @@ uint32_t SceneBuild::append_stream(StreamBuild &b) {
 }
 
 int SceneBuild::add_tree(Tree &tree, const Xf &ts, int32_t w, int32_t h, uint64_t out_ptr, uint32_t stride) {
+    return add_node(tree, RGPU_NODE_GROUP, UINT32_MAX, ts, w, h, out_ptr, stride);
+}
+
+int SceneBuild::add_node(Tree &tree, uint32_t node_kind, uint32_t node_index, const Xf &ts, int32_t w, int32_t h,
+                         uint64_t out_ptr, uint32_t stride) {
     const rgpu_tree_view &t = *tree.get_view();
     Flattener f{*this, tree, t, (uint32_t)verbs.size(), (uint32_t)(pts.size() / 2)};
     verbs.insert(verbs.end(), t.verbs, t.verbs + t.verb_count);
@@ -520,7 +525,13 @@ int SceneBuild::add_tree(Tree &tree, const Xf &ts, int32_t w, int32_t h, uint64_
     root.stride = stride;
     root.out_ptr = out_ptr;
     f.cur = &root;
-    if (t.group_count) f.render_nodes(0, ts, Target{w, h, 0, 0});
+    if (node_index == UINT32_MAX) {
+        if (t.group_count) f.render_nodes(0, ts, Target{w, h, 0, 0});  // resvg::render: the root's children
+    } else if (node_kind == RGPU_NODE_GROUP && node_index < t.group_count) {
+        f.render_group(node_index, ts, Target{w, h, 0, 0});
+    } else if (node_kind == RGPU_NODE_PATH && node_index < t.path_count) {
+        f.render_path(node_index, ts, Target{w, h, 0, 0});
+    }
     if (f.unsupported) {
         error = "a filter region of more than 2^28 pixels";
         return -1;

@@ -61,6 +61,11 @@ struct SceneBuild {
     // Appends one tree rendered onto a device surface (`out_ptr`, `stride`,
     // size w x h); returns the index of its output stream or -1.
     int add_tree(Tree &tree, const Xf &ts, int32_t w, int32_t h, uint64_t out_ptr, uint32_t stride);
+    // Appends one node of a tree (render::render_node, crates/resvg/src/render.rs:31-46:
+    // a group through render_group, a path through path::render) with `ts` as
+    // its parent transform; node_kind is RGPU_NODE_GROUP or RGPU_NODE_PATH.
+    int add_node(Tree &tree, uint32_t node_kind, uint32_t node_index, const Xf &ts, int32_t w, int32_t h,
+                 uint64_t out_ptr, uint32_t stride);
     // internal: concatenates a finished stream
     uint32_t append_stream(StreamBuild &sbd);
 };

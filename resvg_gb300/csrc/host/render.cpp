@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -388,7 +389,8 @@ int check_err(Buffers &b, cudaStream_t s, cudaEvent_t ev0, cudaEvent_t ev1) {
     return RGPU_OK;
 }
 
-int render_host(const rgpu_tree *tree, const resvg_transform &ts, uint32_t w, uint32_t h, char *pixmap) {
+int render_host(const rgpu_tree *tree, const resvg_transform &ts, uint32_t w, uint32_t h, char *pixmap,
+                int node_kind = -1, uint32_t node_index = 0) {
     g_last_error.clear();
     std::memset(&g_stats, 0, sizeof(g_stats));
     if (!tree || !pixmap || w == 0 || h == 0 || w > 32767 || h > 32767) {
@@ -405,8 +407,11 @@ int render_host(const rgpu_tree *tree, const resvg_transform &ts, uint32_t w, ui
     Plan p;
     rgpu_tree *tr = const_cast<rgpu_tree *>(tree);
     if (!tr->finalized) tr->finalize();
-    if (p.sb.add_tree(*tr, Xf::row(ts.a, ts.b, ts.c, ts.d, ts.e, ts.f), (int32_t)w, (int32_t)h,
-                      (uint64_t)(uintptr_t)c.surface.p, w * 4) < 0) {
+    const Xf xts = Xf::row(ts.a, ts.b, ts.c, ts.d, ts.e, ts.f);
+    const int added = node_kind < 0 ? p.sb.add_tree(*tr, xts, (int32_t)w, (int32_t)h, (uint64_t)(uintptr_t)c.surface.p, w * 4)
+                                    : p.sb.add_node(*tr, (uint32_t)node_kind, node_index, xts, (int32_t)w, (int32_t)h,
+                                                    (uint64_t)(uintptr_t)c.surface.p, w * 4);
+    if (added < 0) {
         set_error("%s", p.sb.error.c_str());
         return RGPU_ERR_UNSUPPORTED;
     }
@@ -459,9 +464,57 @@ void resvg_render(const resvg_render_tree *tree, resvg_transform transform, uint
 
 bool resvg_render_node(const resvg_render_tree *tree, const char *id, resvg_transform transform, uint32_t width,
                        uint32_t height, char *pixmap) {
-    (void)tree; (void)id; (void)transform; (void)width; (void)height; (void)pixmap;
-    set_error("resvg_render_node: not implemented");
-    return false;
+    // resvg::render_node (crates/resvg/src/lib.rs:55-70) behind the C API's
+    // id lookup (crates/c-api/lib.rs:908-942): the node's absolute layer
+    // bounding box moves to the pixmap origin (transform.pre_translate(-x, -y))
+    // and the node renders with only its own transform on top of that.
+    g_last_error.clear();
+    if (!tree || !pixmap || !width || !height) { set_error("invalid arguments"); return false; }
+    if (!id || !*id) { set_error("resvg_render_node: empty id"); return false; }
+    rgpu_tree *tr = const_cast<rgpu_tree *>(tree);
+    if (!tr->finalized) tr->finalize();
+    const rgpu_tree_view &t = *tr->get_view();
+    // ids: "<n>" is group n, "p<n>" is path n (the tree keeps no SVG ids)
+    const bool is_path = id[0] == 'p';
+    char *end = nullptr;
+    const unsigned long idx = std::strtoul(id + (is_path ? 1 : 0), &end, 10);
+    if (!end || *end || end == id + (is_path ? 1 : 0) ||
+        idx >= (is_path ? (unsigned long)t.path_count : (unsigned long)t.group_count)) {
+        set_error("resvg_render_node: no node with id '%s'", id);
+        return false;
+    }
+    // parents, then the absolute transform (parent_abs.pre_concat(own))
+    std::vector<int32_t> group_parent(t.group_count, -1), path_parent(t.path_count, -1);
+    for (uint32_t g = 0; g < t.group_count; g++)
+        for (uint32_t k = 0; k < t.groups[g].child_count; k++) {
+            const rgpu_node &n = t.children[t.groups[g].child_offset + k];
+            if (n.kind == RGPU_NODE_GROUP) group_parent[n.index] = (int32_t)g;
+            else path_parent[n.index] = (int32_t)g;
+        }
+    Xf abs = is_path ? Xf() : Xf::of(t.groups[idx].transform);
+    for (int32_t g = is_path ? path_parent[idx] : group_parent[idx]; g >= 0; g = group_parent[g])
+        abs = concat(Xf::of(t.groups[g].transform), abs);
+    float r[4];
+    if (is_path) {
+        const rgpu_path &p = t.paths[idx];
+        r[0] = p.bbox_x; r[1] = p.bbox_y; r[2] = p.bbox_x + p.bbox_w; r[3] = p.bbox_y + p.bbox_h;
+    } else {
+        const rgpu_group &g = t.groups[idx];
+        if (!g.has_layer_bbox) { set_error("resvg_render_node: the node has no bounding box"); return false; }
+        r[0] = g.layer_x; r[1] = g.layer_y; r[2] = g.layer_x + g.layer_w; r[3] = g.layer_y + g.layer_h;
+    }
+    float bb[4];
+    if (!(r[2] > r[0] && r[3] > r[1]) || !map_rect(abs, r[0], r[1], r[2], r[3], bb)) {
+        set_error("resvg_render_node: the node has a zero-sized bounding box");
+        return false;
+    }
+    const Xf ts = concat(Xf::row(transform.a, transform.b, transform.c, transform.d, transform.e, transform.f),
+                         Xf::translate(-bb[0], -bb[1]));
+    const resvg_transform rt{ts.sx, ts.ky, ts.kx, ts.sy, ts.tx, ts.ty};
+    const int rr = render_host(tree, rt, width, height, pixmap, is_path ? RGPU_NODE_PATH : RGPU_NODE_GROUP,
+                               (uint32_t)idx);
+    if (rr != RGPU_OK) fprintf(stderr, "resvg_render_node: %s\n", g_last_error.c_str());
+    return rr == RGPU_OK;
 }
 
 }  // extern "C"

@@ -84,7 +84,11 @@ def read_png(path: str) -> np.ndarray:
             vals = (vals << 1) | bits[:, :, i]
         vals = vals[:, :w].astype(np.uint8)
         if ctype == 0:
-            vals = (vals.astype(np.int32) * 255 // ((1 << depth) - 1)).astype(np.uint8)
+            out = _expand((vals.astype(np.int32) * 255 // ((1 << depth) - 1)).astype(np.uint8)[..., None], ctype,
+                          plte, None, w, h)
+            if trns is not None and len(trns) >= 2:  # tRNS gray key, in the sample's own bit depth
+                out[..., 3][vals == struct.unpack(">H", trns[:2])[0]] = 0
+            return out
         return _expand(vals[..., None], ctype, plte, trns, w, h)
     stride = w * chans
     px = _unfilter(raw, h, stride, chans).reshape(h, w, chans)
@@ -105,6 +109,8 @@ def _expand(px, ctype, plte, trns, w, h):
     elif ctype == 0:
         out[..., 0] = out[..., 1] = out[..., 2] = px[..., 0]
         out[..., 3] = 255
+        if trns is not None and len(trns) >= 2:
+            out[..., 3][px[..., 0] == struct.unpack(">H", trns[:2])[0]] = 0
     elif ctype == 4:
         out[..., 0] = out[..., 1] = out[..., 2] = px[..., 0]
         out[..., 3] = px[..., 1]

@@ -532,6 +532,7 @@ class Loader:
             if e.get("class") is not None or e.get("systemLanguage") is not None:
                 raise Unsupported("class/systemLanguage")
         self.clip_cache, self.mask_cache, self.filter_cache = {}, {}, {}
+        self.ids_out = {}  # SVG id -> render_node id ("<group>" or "p<path>")
 
     # ---- attributes with style and inheritance
     def attrs(self, e):
@@ -632,6 +633,7 @@ class Builder(Loader):
         for c in svg:
             self.node(c, root)
         self.tree.finalize()
+        self.tree.ids = self.ids_out
         return self.tree
 
     def visible(self, e):
@@ -688,8 +690,10 @@ class Builder(Loader):
         isolate = a.get("isolation", "auto").strip() == "isolate"
         if clip == "missing" or mask == "missing":
             return None  # references to missing elements: the element is not rendered
+        eid = e.get("id")
+        keep_id = eid is not None and _tag(e) in ("g", "use")
         needs = ts != IDENT or opacity != 1.0 or clip is not None or mask is not None or filt or \
-            blend != "source-over" or isolate
+            blend != "source-over" or isolate or keep_id
         if not needs:
             return parent
         bbox = None
@@ -722,6 +726,8 @@ class Builder(Loader):
         gi = self.tree.add_group(parent, g)
         if fids:
             self.tree.set_group_filters(gi, fids)
+        if eid is not None:
+            self.ids_out.setdefault(eid, str(gi))
         return gi
 
     # ---- bounding boxes (object bounding box of an element, its user space)
@@ -1036,7 +1042,9 @@ class Builder(Loader):
             return
         if path.stroke_paint < 0:
             path.stroke_width = 1.0
-        self.tree.add_path(parent, path, verbs, pts, dashes)
+        pi = self.tree.add_path(parent, path, verbs, pts, dashes)
+        if e.get("id") is not None:
+            self.ids_out.setdefault(e.get("id"), "p%d" % pi)
 
     # ---- clip paths
     def clip(self, ce, bbox):

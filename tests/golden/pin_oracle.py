@@ -85,6 +85,42 @@ def collect(root):
     return out
 
 
+def collect_extra(root):
+    """crates/resvg/tests/integration/extra.rs: (name, path, mode, arg) with
+    mode "scale" (render_extra_with_scale) or "node" (render_node by id)."""
+    d = os.path.join(root, "crates", "resvg", "tests", "extra")
+    src = os.path.join(root, "crates", "resvg", "tests", "integration", "extra.rs")
+    out = []
+    if not os.path.exists(src):
+        return out
+    import re
+    text = open(src).read()
+    for m in re.finditer(r'render_extra\("extra/([^"]+)"\)', text):
+        out.append((m.group(1), os.path.join(d, m.group(1) + ".svg"), "scale", 1.0))
+    for m in re.finditer(r'render_extra_with_scale\(\s*"extra/([^"]+)",\s*([0-9.]+)\)', text):
+        out.append((m.group(1), os.path.join(d, m.group(1) + ".svg"), "scale", float(m.group(2))))
+    for m in re.finditer(r'render_node\("extra/([^"]+)",\s*"([^"]+)"\)', text):
+        out.append((m.group(1), os.path.join(d, m.group(1) + ".svg"), "node", m.group(2)))
+    return out
+
+
+def render_extra(tree, mode, arg):
+    """The pixmap size, transform (or node id) of main.rs:96-108 for extra tests."""
+    tw, th = tree.size
+    if mode == "scale":
+        iw = max(1, int(round_half_away(tw)))
+        ih = max(1, int(round_half_away(th)))
+        w = int(math.ceil(np.float32(iw) * np.float32(arg)))
+        h = int(math.ceil(np.float32(ih) * np.float32(arg)))
+        return w, h, (float(arg), 0.0, 0.0, float(arg), 0.0, 0.0), None
+    from resvg_gb300 import node_abs_bbox
+    nid = tree.ids.get(arg)
+    b = node_abs_bbox(tree, nid) if nid else None
+    if b is None:
+        return None
+    return max(1, int(round_half_away(b[2]))), max(1, int(round_half_away(b[3]))), (1, 0, 0, 1, 0, 0), nid
+
+
 def run(root, verbose=False, only=None):
     oracle.build()
     results, fixtures = {}, {}
@@ -111,6 +147,31 @@ def run(root, verbose=False, only=None):
         results[key] = {"status": "pass" if n == 0 else "fail", "pixels": n}
         if n == 0:
             fixtures[key] = (text, expected)
+        if verbose:
+            print("%-60s %s" % (key, results[key]))
+    for name, path, mode, arg in collect_extra(root):
+        key = "extra/" + name
+        if only and only not in key:
+            continue
+        if not os.path.exists(path[:-4] + ".png"):
+            continue
+        try:
+            tree = svg.load_svg(open(path, encoding="utf-8").read())
+        except svg.Unsupported as e:
+            results[key] = {"status": "unsupported", "why": str(e)[:80]}
+            continue
+        except Exception as e:
+            results[key] = {"status": "unsupported", "why": type(e).__name__}
+            continue
+        spec = render_extra(tree, mode, arg)
+        if spec is None:
+            results[key] = {"status": "fail", "pixels": -1}
+            continue
+        w, h, ts, nid = spec
+        pm = oracle.render(tree.view(), ts, w, h) if nid is None else oracle.render_node(tree.view(), nid, ts, w, h)
+        expected = png.read_png(path[:-4] + ".png")
+        n = pixel_diff(expected, png.demultiply(pm)) if pm is not None else -1
+        results[key] = {"status": "pass" if n == 0 else "fail", "pixels": n, "mode": mode}
         if verbose:
             print("%-60s %s" % (key, results[key]))
     return results, fixtures
