@@ -9,6 +9,7 @@ g++ -std=c++17 -O2 -fPIC -shared -ffp-contract=off -fno-fast-math -fwrapv -fno-s
     -I"$HERE/../include" \
     "$HERE/raster.cpp" "$HERE/render.cpp" "$HERE/filter.cpp" "$HERE/soft.cpp" \
     "$HERE/../resvg_gb300/csrc/host/geom.cpp" "$HERE/../resvg_gb300/csrc/host/stroke.cpp" \
+    "$HERE/../resvg_gb300/csrc/host/hairline.cpp" \
     "$HERE/../resvg_gb300/csrc/host/tree.cpp" \
     -o "$HERE/_build/liboracle.so.tmp" -lpthread
 mv "$HERE/_build/liboracle.so.tmp" "$HERE/_build/liboracle.so"

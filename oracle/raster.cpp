@@ -14,6 +14,7 @@
 #include "raster.h"
 #include <algorithm>
 #include <cfloat>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <type_traits>
@@ -1671,6 +1672,189 @@ void fill_path(Pixmap &pm, const Path &path_in, const Paint &paint_in, uint32_t 
     if (!bl.setup(pm, paint)) return;
     IntRect clip{0, 0, (int32_t)pm.width, (int32_t)pm.height};
     scan_path(path, rule, paint.anti_alias, clip, [&](int32_t x, int32_t y, uint8_t c) { bl.pixel(x, y, c); });
+}
+
+// ---------------------------------------------------------------- anti-aliased hairlines
+// scan/hairline_aa.rs: do_anti_hairline (Skia's SkScan_Antihair.cpp) with the
+// HLine / Horish / VLine / Vertish anti-hair blitters, drawing through the
+// pipeline blitter; a clip rect (the RectClipBlitter) drops pixels outside it.
+namespace {
+struct HairClip {
+    bool on;
+    int32_t l, t, r, b;
+};
+inline uint8_t hair_small_scale(uint32_t v, int32_t dot6) { return (uint8_t)((v * (uint32_t)dot6) >> 6); }
+inline int32_t contribution_64(int32_t o) { return ((o - 1) & 63) + 1; }
+inline int32_t fdot16_fast_div(int32_t a, int32_t b) {
+    if (a >= -32768 && a <= 32767) return (int32_t)((uint32_t)a << 16) / b;
+    int64_t v = ((int64_t)a << 16) / b;
+    return (int32_t)std::min<int64_t>(std::max<int64_t>(v, INT32_MIN), INT32_MAX);
+}
+inline int32_t fdot16_ceil(int32_t x) { return (int32_t)(((int64_t)x + 0xFFFF) >> 16); }
+
+struct HairBlit {
+    PipelineBlitter &bl;
+    HairClip clip;
+    int32_t w, h;
+    void px(int64_t x, int64_t y, uint8_t a) {
+        if (a == 0) return;
+        if (clip.on && (x < clip.l || x >= clip.r || y < clip.t || y >= clip.b)) return;
+        if (x < 0 || y < 0 || x >= w || y >= h) return;
+        bl.pixel((int32_t)x, (int32_t)y, a);
+    }
+};
+
+enum HairKind { HK_HLINE, HK_HORISH, HK_VLINE, HK_VERTISH };
+
+// draw_cap / draw_line of the four blitters for one step of the major axis
+void hair_step(HairKind k, HairBlit &b, int32_t major, int32_t &f, int32_t slope, int32_t mod64) {
+    const int32_t half = 1 << 15;
+    int32_t fy = f + half;
+    if (fy < 0) fy = 0;
+    const int32_t hi = fy >> 16;
+    const uint8_t a = (uint8_t)((fy >> 8) & 0xFF);
+    switch (k) {
+    case HK_HLINE: {
+        uint8_t m = hair_small_scale(a, mod64);
+        if (m) b.px(major, hi, m);
+        m = hair_small_scale(255 - a, mod64);
+        if (m && hi >= 1) b.px(major, hi - 1, m);
+        f = fy - half;
+        break;
+    }
+    case HK_HORISH: {
+        const int32_t y0 = std::max(hi, 1) - 1;
+        b.px(major, y0, hair_small_scale(255 - a, mod64));
+        b.px(major, y0 + 1, hair_small_scale(a, mod64));
+        f = fy + slope - half;
+        break;
+    }
+    case HK_VLINE: {
+        uint8_t m = hair_small_scale(a, mod64);
+        if (m) b.px(hi, major, m);
+        m = hair_small_scale(255 - a, mod64);
+        if (m) b.px(std::max(hi, 1) - 1, major, m);
+        f = fy - half;
+        break;
+    }
+    case HK_VERTISH: {
+        const int32_t x0 = std::max(hi, 1) - 1;
+        b.px(x0, major, hair_small_scale(255 - a, mod64));
+        b.px(x0 + 1, major, hair_small_scale(a, mod64));
+        f = fy + slope - half;
+        break;
+    }
+    }
+}
+
+void do_anti_hairline(int32_t x0, int32_t y0, int32_t x1, int32_t y1, HairClip clip, HairBlit &b) {
+    auto bad = [](int32_t v) { return v == INT32_MIN; };
+    if (bad(x0) || bad(y0) || bad(x1) || bad(y1)) return;
+    if (std::abs(x1 - x0) > 511 * 64 || std::abs(y1 - y0) > 511 * 64) {
+        const int32_t hx = (x0 >> 1) + (x1 >> 1), hy = (y0 >> 1) + (y1 >> 1);
+        do_anti_hairline(x0, y0, hx, hy, clip, b);
+        do_anti_hairline(hx, hy, x1, y1, clip, b);
+        return;
+    }
+    int32_t scale_start, scale_stop, istart, istop, fstart, slope;
+    HairKind kind;
+    if (std::abs(x1 - x0) > std::abs(y1 - y0)) {
+        if (x0 > x1) { std::swap(x0, x1); std::swap(y0, y1); }
+        istart = x0 >> 6;
+        istop = (x1 + 63) >> 6;
+        fstart = (int32_t)((uint32_t)y0 << 10);
+        if (y0 == y1) {
+            slope = 0;
+            kind = HK_HLINE;
+        } else {
+            slope = fdot16_fast_div(y1 - y0, x1 - x0);
+            fstart += (slope * (32 - (x0 & 63)) + 32) >> 6;
+            kind = HK_HORISH;
+        }
+        if (istop - istart == 1) { scale_start = x1 - x0; scale_stop = 0; }
+        else { scale_start = 64 - (x0 & 63); scale_stop = x1 & 63; }
+        if (clip.on) {
+            if (istart >= clip.r || istop <= clip.l) return;
+            if (istart < clip.l) {
+                fstart += slope * (clip.l - istart);
+                istart = clip.l;
+                scale_start = 64;
+                if (istop - istart == 1) { scale_start = contribution_64(x1); scale_stop = 0; }
+            }
+            if (istop > clip.r) { istop = clip.r; scale_stop = 0; }
+            if (istart == istop) return;
+            int32_t top, bottom;
+            if (slope >= 0) {
+                top = (fstart - (1 << 15)) >> 16;
+                bottom = fdot16_ceil(fstart + (istop - istart - 1) * slope + (1 << 15));
+            } else {
+                bottom = fdot16_ceil(fstart + (1 << 15));
+                top = (fstart + (istop - istart - 1) * slope - (1 << 15)) >> 16;
+            }
+            top -= 1;
+            bottom += 1;
+            if (top >= clip.b || bottom <= clip.t) return;
+            if (clip.t <= top && clip.b >= bottom) clip.on = false;
+        }
+    } else {
+        if (y0 > y1) { std::swap(x0, x1); std::swap(y0, y1); }
+        istart = y0 >> 6;
+        istop = (y1 + 63) >> 6;
+        fstart = (int32_t)((uint32_t)x0 << 10);
+        if (x0 == x1) {
+            if (y0 == y1) return;
+            slope = 0;
+            kind = HK_VLINE;
+        } else {
+            slope = fdot16_fast_div(x1 - x0, y1 - y0);
+            fstart += (slope * (32 - (y0 & 63)) + 32) >> 6;
+            kind = HK_VERTISH;
+        }
+        if (istop - istart == 1) { scale_start = y1 - y0; scale_stop = 0; }
+        else { scale_start = 64 - (y0 & 63); scale_stop = y1 & 63; }
+        if (clip.on) {
+            if (istart >= clip.b || istop <= clip.t) return;
+            if (istart < clip.t) {
+                fstart += slope * (clip.t - istart);
+                istart = clip.t;
+                scale_start = 64;
+                if (istop - istart == 1) { scale_start = contribution_64(y1); scale_stop = 0; }
+            }
+            if (istop > clip.b) { istop = clip.b; scale_stop = 0; }
+            if (istart == istop) return;
+            int32_t left, right;
+            if (slope >= 0) {
+                left = (fstart - (1 << 15)) >> 16;
+                right = fdot16_ceil(fstart + (istop - istart - 1) * slope + (1 << 15));
+            } else {
+                right = fdot16_ceil(fstart + (1 << 15));
+                left = (fstart + (istop - istart - 1) * slope - (1 << 15)) >> 16;
+            }
+            left -= 1;
+            right += 1;
+            if (left >= clip.r || right <= clip.l) return;
+            if (clip.l <= left && clip.r >= right) clip.on = false;
+        }
+    }
+    HairBlit bb{b.bl, clip, b.w, b.h};
+    int32_t f = fstart;
+    hair_step(kind, bb, istart, f, slope, scale_start);
+    istart += 1;
+    const int32_t full = istop - istart - (scale_stop > 0 ? 1 : 0);
+    for (int32_t i = 0; i < full; i++) hair_step(kind, bb, istart + i, f, slope, 64);
+    if (scale_stop > 0) hair_step(kind, bb, istop - 1, f, slope, scale_stop);
+}
+}  // namespace
+
+void anti_hairlines(Pixmap &pm, const Paint &paint, const int32_t *calls, size_t ncalls) {
+    PipelineBlitter bl;
+    if (!bl.setup(pm, paint)) return;
+    HairBlit b{bl, HairClip{false, 0, 0, 0, 0}, (int32_t)pm.width, (int32_t)pm.height};
+    for (size_t i = 0; i < ncalls; i++) {
+        const int32_t *c = calls + 9 * i;
+        HairClip clip{c[8] != 0, c[4], c[5], c[6], c[7]};
+        do_anti_hairline(c[0], c[1], c[2], c[3], clip, b);
+    }
 }
 
 void pixmap_fill(Pixmap &pm, ColorF c) {

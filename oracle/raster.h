@@ -118,6 +118,11 @@ struct Paint {
 
 // tiny-skia Pixmap::fill_path (painter.rs).
 void fill_path(Pixmap &pm, const Path &path, const Paint &paint, uint32_t rule, const Transform &ts);
+// tiny-skia's anti-aliased hairline (scan/hairline_aa.rs do_anti_hairline and
+// its four blitters) for a list of fixed-point line calls, drawn with `paint`
+// (already opacity-scaled; its shader in device space).  call = {x0, y0, x1,
+// y1 (FDot6), clip l, t, r, b, has_clip}.
+void anti_hairlines(Pixmap &pm, const Paint &paint, const int32_t *calls, size_t ncalls);
 // tiny-skia Pixmap::fill_rect for an integer-aligned rect, no AA (painter.rs).
 void fill_rect(Pixmap &pm, const Rect &r, const Paint &paint);
 // tiny-skia Pixmap::draw_pixmap (painter.rs): pattern + fill_rect, highp.

@@ -15,6 +15,7 @@
 #include <cstring>
 #include <vector>
 #include "raster.h"
+#include "../resvg_gb300/csrc/host/hairline.h"
 #include "../resvg_gb300/csrc/host/tree.h"
 
 namespace ora {
@@ -109,6 +110,13 @@ void fill_path_node(Ctx &c, const rgpu_path &p, uint32_t blend, const Transform 
     fill_path(pm, path, paint, p.fill_rule, ts);
 }
 
+// BlendMode::should_pre_scale_coverage (tiny-skia blend_mode.rs)
+bool pre_scale_blend(uint32_t b) {
+    return b == RGPU_BLEND_DESTINATION || b == RGPU_BLEND_DESTINATION_OVER || b == RGPU_BLEND_PLUS ||
+           b == RGPU_BLEND_DESTINATION_OUT || b == RGPU_BLEND_SOURCE_ATOP || b == RGPU_BLEND_SOURCE_OVER ||
+           b == RGPU_BLEND_XOR;
+}
+
 void stroke_path_node(Ctx &c, uint32_t pi, uint32_t blend, const Transform &ts, Pixmap &pm) {
     const rgpu_path &p = c.t.paths[pi];
     if (p.stroke_paint < 0) return;
@@ -117,6 +125,26 @@ void stroke_path_node(Ctx &c, uint32_t pi, uint32_t blend, const Transform &ts, 
     paint.anti_alias = p.anti_alias != 0;
     paint.blend = blend;
     float rs = rgpu::resolution_scale(ts.sx, ts.ky, ts.kx, ts.sy);
+    // tiny-skia stroke_path: a stroke at most one device pixel wide is an
+    // anti-aliased hairline of the (dashed) path, its paint scaled by coverage
+    const rgpu::Xf xts = rgpu::Xf::row(ts.sx, ts.ky, ts.kx, ts.sy, ts.tx, ts.ty);
+    float coverage = 1.0f;
+    if (rgpu::treat_as_hairline(paint.anti_alias, p.stroke_width, xts, &coverage)) {
+        rgpu::PathData src;
+        if (!rgpu::hairline_source_view(c.t, pi, rs, src)) return;
+        if (coverage != 1.0f && pre_scale_blend(blend)) {
+            const float op = rgpu::hairline_opacity(coverage);
+            auto scale = [op](ColorF &col) { col.a = std::min(std::max(col.a * std::min(std::max(op, 0.0f), 1.0f), 0.0f), 1.0f); };
+            if (paint.shader.kind == SHADER_SOLID) scale(paint.shader.color);
+            for (auto &st : paint.shader.stops) scale(st.color);
+        }
+        std::vector<rgpu::HairCall> calls;
+        rgpu::hairline_calls(src, xts, p.line_cap, (int32_t)pm.width, (int32_t)pm.height, calls);
+        if (!ts.is_identity() && paint.shader.kind != SHADER_SOLID)
+            paint.shader.transform = paint.shader.transform.post_concat(ts);
+        anti_hairlines(pm, paint, reinterpret_cast<const int32_t *>(calls.data()), calls.size());
+        return;
+    }
     rgpu::PathData out;
     if (!rgpu::stroke_outline_view(c.t, pi, rs, out)) return;
     Path sp;

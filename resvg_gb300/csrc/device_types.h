@@ -94,7 +94,8 @@ enum CmdOp : uint32_t {
     CMD_POP_MASK = 4,     // a = popped layer, b = 0 luminance / 1 alpha
     CMD_APPLY_REGION = 5, // a = draw: top *= coverage(draw)
     CMD_CLEAR = 6,        // top = transparent
-    CMD_END = 7
+    CMD_END = 7,
+    CMD_HAIR = 8          // a = hairline draw (HairRec): anti-aliased hairline stroke
 };
 
 struct Cmd {
@@ -123,5 +124,33 @@ struct StreamRec {
     int32_t surface;               // internal surface rendered into (filter content), or -1
     uint32_t level;                // dependency level: content streams render before their parents
 };
+
+
+// An anti-aliased hairline stroke (tiny-skia scan/hairline_aa.rs): its line
+// spans after do_anti_hairline's setup, drawn with `paint` into the current
+// layer (layer origin ox, oy in the stream's output space); [x0, x1) x
+// [y0, y1) bounds the layer pixels of all its spans.
+struct HairRec {
+    uint32_t span_off, span_cnt, paint;
+    int32_t ox, oy, x0, y0, x1, y1;
+    uint32_t _pad[3];
+};
+
+// One set-up do_anti_hairline line: n steps along the major axis from
+// `istart`; the minor coordinate of step k is (FDot16, clamped at 0 as the
+// blitters clamp it) c_k = max(f0 + k*slope, 0) for slope < 0, else
+// max(f0, 0) + k*slope, with f0 = fstart + 1/2.  Only pixels inside the rect
+// [x0, x1) x [y0, y1) (the clip, the layer and the line's own bounds
+// intersected) are touched.  `pack` holds the blitter kind (bits 0-1: 0 hline,
+// 1 horish, 2 vline, 3 vertish), the end-cap scales of the first (bits 2-8)
+// and last (bits 9-15, 0 = none) step, n (bits 16-25, at most 512) and
+// HAIR_SECOND: a vline whose two blit columns coincide is emitted twice, the
+// first span drawing only the first blit, the second only the second.
+struct HairSpan {
+    int32_t istart, f0, slope;
+    uint32_t pack;
+    int32_t x0, y0, x1, y1;
+};
+enum : uint32_t { HAIR_SECOND = 1u << 26 };
 
 }  // namespace rgpu

@@ -6,6 +6,7 @@
 // RasterPipelineBlitter::new strength reduction of SourceOver to Source for
 // opaque paints and the memset fast path).
 #include "flatten.h"
+#include "hairline.h"
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -282,12 +283,62 @@ struct Flattener {
                   ts, tg, p.fill_rule, p.anti_alias != 0, add_paint(pr));
     }
     // path.rs:77-116 (outline from the host stroker, filled non-zero)
+    // tiny-skia stroke_path: a stroke at most one device pixel wide is drawn as
+    // an anti-aliased hairline of the (dashed) path; for blend modes that
+    // pre-scale coverage its paint is scaled by the stroke's coverage.
+    bool hairline(uint32_t pi, Shader sh, uint32_t blend, const Xf &ts, const Target &tg, float rs) {
+        const rgpu_path &p = t.paths[pi];
+        float coverage = 1.0f;
+        if (!treat_as_hairline(p.anti_alias != 0, p.stroke_width, ts, &coverage)) return false;
+        PathData src;
+        if (!hairline_source_view(t, pi, rs, src)) return true;
+        const bool pre_scale = blend == RGPU_BLEND_DESTINATION || blend == RGPU_BLEND_DESTINATION_OVER ||
+                               blend == RGPU_BLEND_PLUS || blend == RGPU_BLEND_DESTINATION_OUT ||
+                               blend == RGPU_BLEND_SOURCE_ATOP || blend == RGPU_BLEND_SOURCE_OVER ||
+                               blend == RGPU_BLEND_XOR;
+        if (coverage != 1.0f && pre_scale) {
+            const float op = std::min(std::max(hairline_opacity(coverage), 0.0f), 1.0f);
+            auto scale = [op](ColorF &c) { c.a = std::min(std::max(c.a * op, 0.0f), 1.0f); };
+            if (sh.kind == SH_SOLID) scale(sh.color);
+            for (auto &st : sh.stops) scale(st.c);
+        }
+        PaintRec pr;
+        if (!paint_rec(sh, blend, true, ts, pr)) return true;
+        std::vector<HairCall> calls;
+        hairline_calls(src, ts, p.line_cap, tg.w, tg.h, calls);
+        HairRec hr;
+        std::memset(&hr, 0, sizeof(hr));
+        hr.span_off = (uint32_t)sb.hair_spans.size();
+        for (const HairCall &c : calls) hairline_spans(c, sb.hair_spans);
+        // the blitters never write outside the layer: fold it into each span's rect
+        size_t keep = hr.span_off;
+        hr.x0 = hr.y0 = INT32_MAX;
+        hr.x1 = hr.y1 = INT32_MIN;
+        for (size_t k = hr.span_off; k < sb.hair_spans.size(); k++) {
+            HairSpan s = sb.hair_spans[k];
+            s.x0 = std::max(s.x0, 0); s.y0 = std::max(s.y0, 0);
+            s.x1 = std::min(s.x1, tg.w); s.y1 = std::min(s.y1, tg.h);
+            if (s.x0 >= s.x1 || s.y0 >= s.y1) continue;
+            hr.x0 = std::min(hr.x0, s.x0); hr.y0 = std::min(hr.y0, s.y0);
+            hr.x1 = std::max(hr.x1, s.x1); hr.y1 = std::max(hr.y1, s.y1);
+            sb.hair_spans[keep++] = s;
+        }
+        sb.hair_spans.resize(keep);
+        hr.span_cnt = (uint32_t)sb.hair_spans.size() - hr.span_off;
+        if (!hr.span_cnt) return true;
+        hr.paint = add_paint(pr);
+        hr.ox = tg.ox; hr.oy = tg.oy;
+        sb.hairs.push_back(hr);
+        cur->cmds.push_back(Cmd{CMD_HAIR, (uint32_t)sb.hairs.size() - 1, 0, 0.0f});
+        return true;
+    }
     void stroke_path(uint32_t pi, uint32_t blend, const Xf &ts, const Target &tg) {
         const rgpu_path &p = t.paths[pi];
         if (p.stroke_paint < 0) return;
         Shader sh;
         if (!make_shader(t, p.stroke_paint, p.stroke_opacity, sh)) return;
         float rs = resolution_scale(ts.sx, ts.ky, ts.kx, ts.sy);
+        if (hairline(pi, sh, blend, ts, tg, rs)) return;
         auto outline = tree.stroke_outline(pi, rs);
         if (!outline || outline->verbs.empty()) return;
         PaintRec pr;

@@ -52,6 +52,8 @@ struct SceneBuild {
     std::vector<StreamRec> streams;
     std::vector<SurfaceReq> surfaces;
     std::vector<FilterJob> jobs;
+    std::vector<HairRec> hairs;       // anti-aliased hairline strokes
+    std::vector<HairSpan> hair_spans;
     std::vector<uint8_t> verbs;
     std::vector<float> pts;
     uint64_t nsegs = 0, ntpts = 0;

@@ -80,12 +80,13 @@ struct Buffers {
     DevBuf tpts, segs, seg_counts, seg_offsets, scan_scratch, totals;
     DevBuf edges, edge_draw, bin_counts, bin_offsets, bins;
     DevBuf stack, span_ovf, err, counter;
+    DevBuf hairs, hair_spans;
     std::vector<DevBuf> surf, img;   // internal surfaces (filter content/results) and filter images
     DevBuf plane;                    // f64 plane of the IIR blur
     void release() {
         DevBuf *all[] = {&verbs, &pts, &draws, &paints, &grads, &layers, &cmds, &streams, &items, &tpts, &segs,
                          &seg_counts, &seg_offsets, &scan_scratch, &totals, &edges, &edge_draw, &bin_counts,
-                         &bin_offsets, &bins, &stack, &span_ovf, &err, &counter, &plane};
+                         &bin_offsets, &bins, &stack, &span_ovf, &err, &counter, &plane, &hairs, &hair_spans};
         for (DevBuf *b : all) {
             if (b->p) cudaFree(b->p);
             b->p = nullptr;
@@ -263,7 +264,8 @@ int upload_plan(Context &c, Buffers &b, Plan &p, cudaStream_t s) {
     size_t stage = rup(sb.verbs.size()) + rup(sb.pts.size() * 4) + rup(sb.draws.size() * sizeof(DrawRec)) +
                    rup(sb.paints.size() * sizeof(PaintRec)) + rup(sb.grads.size() * sizeof(GradRec)) +
                    rup(sb.layers.size() * sizeof(LayerRec)) + rup(sb.cmds.size() * sizeof(Cmd)) +
-                   rup(sb.streams.size() * sizeof(StreamRec)) + rup(p.items.size() * sizeof(WorkItem)) + 4096;
+                   rup(sb.streams.size() * sizeof(StreamRec)) + rup(p.items.size() * sizeof(WorkItem)) +
+                   rup(sb.hairs.size() * sizeof(HairRec)) + rup(sb.hair_spans.size() * sizeof(HairSpan)) + 4096;
     CK(c.staging.ensure(stage));
     size_t off = 0;
     int r;
@@ -276,6 +278,8 @@ int upload_plan(Context &c, Buffers &b, Plan &p, cudaStream_t s) {
     if ((r = upload(c, b.cmds, sb.cmds, off, s))) return r;
     if ((r = upload(c, b.streams, sb.streams, off, s))) return r;
     if ((r = upload(c, b.items, p.items, off, s))) return r;
+    if ((r = upload(c, b.hairs, sb.hairs, off, s))) return r;
+    if ((r = upload(c, b.hair_spans, sb.hair_spans, off, s))) return r;
     // fixed-size work buffers
     uint64_t nsegs = sb.nsegs;
     CK(b.tpts.ensure(std::max<uint64_t>(sb.ntpts, 1) * 8));
@@ -356,7 +360,7 @@ int enqueue_plan(Context &c, Buffers &b, Plan &p, cudaStream_t s, cudaEvent_t ev
                              b.cmds.as<Cmd>(), b.draws.as<DrawRec>(), b.paints.as<PaintRec>(), b.grads.as<GradRec>(),
                              b.layers.as<LayerRec>(), b.bins.as<EdgeRec>(), b.bin_offsets.as<uint32_t>(),
                              b.bin_counts.as<uint32_t>(), b.stack.as<uint32_t>(), b.span_ovf.as<int2>(), ovf_cap,
-                             b.err.as<uint32_t>(), s));
+                             b.hairs.as<HairRec>(), b.hair_spans.as<HairSpan>(), b.err.as<uint32_t>(), s));
         if (ev1 && last) CK(cudaEventRecord(ev1, s));
         for (const auto &job : sb.jobs) {
             if (job.level != lv) continue;

@@ -82,6 +82,24 @@ bool stroke_outline_view(const rgpu_tree_view &t, uint32_t pi, float res_scale, 
     return stroke_path(v, p.verb_count, pts, p.point_count, st, res_scale, out);
 }
 
+bool hairline_source_view(const rgpu_tree_view &t, uint32_t pi, float res_scale, PathData &out) {
+    const rgpu_path &p = t.paths[pi];
+    const uint8_t *v = t.verbs + p.verb_offset;
+    const float *pts = t.points + 2 * (size_t)p.point_offset;
+    if (p.dash_count) {
+        PathData dashed;
+        if (dash_path(v, p.verb_count, pts, p.point_count, t.dashes + p.dash_offset, p.dash_count, p.dash_phase,
+                      res_scale, dashed)) {
+            if (dashed.empty()) return false;
+            out = std::move(dashed);
+            return true;
+        }
+    }
+    out.verbs.assign(v, v + p.verb_count);
+    out.pts.assign(pts, pts + 2 * (size_t)p.point_count);
+    return !out.verbs.empty();
+}
+
 std::shared_ptr<PathData> Tree::stroke_outline(uint32_t pi, float rs) {
     uint32_t bits;
     std::memcpy(&bits, &rs, 4);

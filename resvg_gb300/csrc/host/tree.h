@@ -55,5 +55,8 @@ struct Tree {
 
 // Stroke outline for a path of any tree view (used by the oracle too).
 bool stroke_outline_view(const rgpu_tree_view &t, uint32_t pi, float res_scale, PathData &out);
+// The path a hairline stroke draws: the dashed path when the stroke is dashed
+// (false when dashing leaves nothing), else the path itself.
+bool hairline_source_view(const rgpu_tree_view &t, uint32_t pi, float res_scale, PathData &out);
 
 }  // namespace rgpu

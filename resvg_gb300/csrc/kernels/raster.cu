@@ -39,11 +39,11 @@ struct VmShared {
     uint16_t span_cnt[kThreads];
     int2 spans[kThreads * kSpanCap];
     int4 rects[kMaxDepth];       // layer-stack rects (x, y, w, h), uniform across the CTA
-    PaintRec paint[kMaxSlots];   // paints of the window's draws
+    PaintRec paint[kMaxSlots + 1];   // paints of the window's draws; the last: the current hairline's
     int4 slot_geo[kMaxSlots];    // (valid | shift << 1, ox, oy, unused) per slot
     int4 slot_sect[kMaxSlots];   // coverage rect (l, t, r, b) per slot
     int32_t grad_slot[kMaxSlots];// index into grad[] or -1
-    GradRec grad[kMaxSlots];     // gradients of the window's draws
+    GradRec grad[kMaxSlots + 1];     // gradients of the window's draws (and the hairline's)
     int32_t item;
     // followed by the top layer: kThreads * px uint32 pixels (dynamic)
 };
@@ -155,11 +155,58 @@ __device__ __forceinline__ uint32_t span_cov(const int2 *L, int n, int &q, int32
     return cov;
 }
 
+// Coverage of layer pixel (px, py) from one hairline span (tiny-skia
+// scan/hairline_aa.rs: the step k on the pixel's major coordinate, the two
+// pixels its blitter touches, alpha scaled by the end-cap fraction); 0 = no
+// blit.  A vline whose two columns coincide (x in [0, 1)) blits each pixel
+// twice: the host emits it as two spans, the second (HAIR_SECOND) carrying
+// only the second blit.
+static_assert(sizeof(HairSpan) == 32, "a hairline span is two int4: setup, then its pixel rect");
+
+// A read-only 16-byte load the compiler keeps in place: hoisting a span's
+// fields out of the per-pixel loop would hold eight more registers across it.
+__device__ __forceinline__ int4 ld_span(const int4 *p) {
+    int4 r;
+    asm volatile("ld.global.nc.v4.s32 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+                 : "l"(p));
+    return r;
+}
+
+__device__ __forceinline__ uint32_t hair_cov(const HairSpan *hsp, int32_t px, int32_t py) {
+    const int4 r = ld_span(reinterpret_cast<const int4 *>(hsp) + 1);
+    if (px < r.x || py < r.y || px >= r.z || py >= r.w) return 0u;
+    const int4 q = ld_span(reinterpret_cast<const int4 *>(hsp));
+    const int32_t istart = q.x, f0 = q.y, slope = q.z;
+    const uint32_t pack = (uint32_t)q.w, kind = pack & 3u;
+    const int32_t n = (int32_t)(pack >> 16);
+    const int32_t k = (kind < 2 ? px : py) - istart, minor = kind < 2 ? py : px;
+    const int32_t cv = slope >= 0 ? max(f0, 0) + k * slope : max(f0 + k * slope, 0);
+    const int32_t hi = cv >> 16;
+    const uint32_t a = (uint32_t)(cv >> 8) & 0xFFu;
+    const uint32_t stop = (pack >> 9) & 127u;
+    const uint32_t mod = k == 0 ? ((pack >> 2) & 127u) : ((k == n - 1 && stop > 0) ? stop : 64u);
+    const uint32_t sa = (a * mod) >> 6, sna = ((255u - a) * mod) >> 6;
+    const int32_t lo = max(hi, 1) - 1;
+    if (kind == 0) {  // hline: row hi, then row hi - 1 (when hi >= 1)
+        if (minor == hi) return sa;
+        return (hi >= 1 && minor == hi - 1) ? sna : 0u;
+    }
+    if (kind == 2) {  // vline: column hi, then column max(hi, 1) - 1
+        if (pack & HAIR_SECOND) return minor == lo ? sna : 0u;
+        if (minor == hi) return sa;
+        return (minor == lo && lo != hi) ? sna : 0u;
+    }
+    // horish / vertish: lo then lo + 1
+    return minor == lo ? sna : (minor == lo + 1 ? sa : 0u);
+}
+
 __global__ void __launch_bounds__(kThreads, 3)
 k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitems, uint32_t *item_counter,
          const Cmd *cmds, const DrawRec *draws, const PaintRec *paints, const GradRec *grads, const LayerRec *layers,
          const EdgeRec *bins, const uint32_t *bin_offsets, const uint32_t *bin_counts, uint32_t *stack_scratch,
-         uint32_t stack_depth, int2 *span_ovf, uint32_t ovf_cap, uint32_t *err) {
+         uint32_t stack_depth, int2 *span_ovf, uint32_t ovf_cap, const HairRec *hairs, const HairSpan *hair_spans,
+         uint32_t *err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     VmShared &sh = *reinterpret_cast<VmShared *>(smem_raw);
     uint32_t *layer = reinterpret_cast<uint32_t *>(smem_raw + ((sizeof(VmShared) + 15) & ~(size_t)15));
@@ -198,8 +245,8 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
 
         for (uint32_t ci = 0; ci < st.cmd_cnt; ci++) {
             const Cmd c = cmds[st.cmd_off + ci];
-            if (c.op == CMD_FILL || c.op == CMD_APPLY_REGION) {
-                if ((int32_t)ci >= sh.win_last) {
+            if (c.op == CMD_FILL || c.op == CMD_APPLY_REGION || c.op == CMD_HAIR) {
+                if ((int32_t)ci >= sh.win_last && c.op != CMD_HAIR) {
                     // ---- prepare a phase-A window over the next K fill commands
                     __syncthreads();
                     if (tid < 32) {
@@ -272,25 +319,59 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
                     }
                     __syncthreads();
                 }
-                // ---- phase B: coverage + shading, one pixel per (thread, i)
-                const int slot = slot_next++;
-                const int4 geo = sh.slot_geo[slot];
-                const bool dvalid = geo.x & 1, aa = geo.x & 2;
-                if (!dvalid && c.op == CMD_FILL) continue;
-                const int4 sect = sh.slot_sect[slot];
-                const int32_t ox = geo.y, oy = geo.z;
-                const int32_t ly = cy - oy;
-                const int32_t lrow0 = (int32_t)wi.band * BH - oy;
-                const bool row_in = dvalid && row_ok && ly >= sect.y && ly < sect.w;
-                if (c.op == CMD_FILL && !row_in) continue;
-                const PaintRec &pr = sh.paint[slot];
-                const GradRec *gr = sh.grad_slot[slot] >= 0 ? &sh.grad[sh.grad_slot[slot]] : &grads[pr.grad];
-                const int nsl = aa ? 4 : 1;
-                const int sj0 = slot * S + (ly - lrow0) * nsl;
+                // ---- phase B: coverage + shading, one pixel per (thread, i).  A hairline
+                // (CMD_HAIR) runs its spans in order through the same loop, each thread
+                // for its own pixels, so blits to one pixel keep their order.
+                const bool hair = c.op == CMD_HAIR;
+                int32_t ox, oy;
+                bool aa = true, row_in;
+                int4 sect = make_int4(0, 0, 0, 0);
+                int slot;
                 const int2 *sp[4];
                 int ns[4], cur[4] = {0, 0, 0, 0};
+                if (hair) {
+                    // stage the hairline's paint in the spare slot (uniform across the CTA)
+                    const HairRec hr = hairs[c.a];
+                    {
+                        const int32_t lx0 = wi.x0 - hr.ox, ly0 = (int32_t)wi.band * BH - hr.oy;
+                        if (hr.x1 <= lx0 || hr.x0 >= wi.x1 - hr.ox || hr.y1 <= ly0 || hr.y0 >= ly0 + BH) continue;
+                    }
+                    __syncthreads();  // the previous hairline's pixels are done with the slot
+                    slot = kMaxSlots;
+                    if (tid == 0) sh.paint[slot] = paints[hr.paint];
+                    const PaintRec &gp = paints[hr.paint];
+                    if (gp.kind == 1)
+                        for (int w = tid; w < (int)(sizeof(GradRec) / 4); w += kThreads)
+                            ((uint32_t *)&sh.grad[slot])[w] = ((const uint32_t *)&grads[gp.grad])[w];
+                    __syncthreads();
+                    if (sh.paint[slot].flags & PAINT_SKIP) continue;
+                    ox = hr.ox; oy = hr.oy;
+                    // the fill span registers carry the hairline's span list: sp[0] the
+                    // spans, ns[0] their count, cur[0] the chunk of 32 being walked and
+                    // cur[1] its spans that meet this work item; sp[1] the span drawn
+                    sp[0] = reinterpret_cast<const int2 *>(hair_spans + hr.span_off);
+                    ns[0] = (int)hr.span_cnt;
+                    cur[0] = -32;
+                    row_in = row_ok;
+                } else {
+                    slot = slot_next++;
+                    const int4 geo = sh.slot_geo[slot];
+                    const bool dvalid = geo.x & 1;
+                    aa = geo.x & 2;
+                    if (!dvalid && c.op == CMD_FILL) continue;
+                    sect = sh.slot_sect[slot];
+                    ox = geo.y; oy = geo.z;
+                    row_in = dvalid && row_ok && cy - oy >= sect.y && cy - oy < sect.w;
+                    if (c.op == CMD_FILL && !row_in) continue;
+                }
+                const PaintRec &pr = sh.paint[slot];
+                const GradRec *gr = &sh.grad[slot];  // read only for gradient paints
+                const int32_t ly = cy - oy;
+                const int32_t lrow0 = (int32_t)wi.band * BH - oy;
+                const int nsl = aa ? 4 : 1;
+                const int sj0 = slot * S + (ly - lrow0) * nsl;
                 int32_t rowL = INT32_MAX, rowR = INT32_MIN;
-                if (row_in) {
+                if (row_in && !hair) {
 #pragma unroll
                     for (int q = 0; q < 4; q++) {
                         ns[q] = 0;
@@ -305,45 +386,71 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
                 if (c.op == CMD_FILL && rowL >= rowR) continue;  // no span on this row
                 const int sub = aa ? 2 : 0;  // sub-column shift
 #pragma unroll 1
-                for (int i = 0; i < PX; i++) {
-                    const int32_t x = wi.x0 + i * tpr + lr;
-                    const int32_t lx = x - ox;
-                    uint32_t cv = 0;
-                    const int32_t wx = wi.x0 + i * tpr + (lr & ~31) - ox;  // warp window start (layer x)
-                    const int32_t w0 = wx << sub, w1 = (wx + 32) << sub;
-                    if (row_in && w1 > rowL && w0 < rowR) {
-                        if (aa) {
-                            const int32_t p0 = lx << 2;
-                            cv = span_cov(sp[0], ns[0], cur[0], w0, w1, p0, 64u) +
-                                 span_cov(sp[1], ns[1], cur[1], w0, w1, p0, 64u) +
-                                 span_cov(sp[2], ns[2], cur[2], w0, w1, p0, 64u) +
-                                 span_cov(sp[3], ns[3], cur[3], w0, w1, p0, 63u);
-                            cv = min(cv, 255u);
+                for (;;) {
+                    if (hair) {
+                        // the next span that meets this work item, in order: each warp
+                        // tests 32 span rects at a time (the same answer in every warp)
+                        while (cur[1] == 0) {
+                            cur[0] += 32;
+                            if (cur[0] >= ns[0]) break;
+                            const int j = cur[0] + (tid & 31);
+                            bool meets = false;
+                            if (j < ns[0]) {
+                                const int4 r = __ldg(reinterpret_cast<const int4 *>(sp[0]) + 2 * j + 1);
+                                meets = !(r.z <= wi.x0 - ox || r.x >= wi.x1 - ox || r.w <= lrow0 || r.y >= lrow0 + BH);
+                            }
+                            cur[1] = (int)__ballot_sync(0xffffffffu, meets);
+                        }
+                        if (cur[1] == 0) break;
+                        sp[1] = sp[0] + 4 * (cur[0] + __ffs(cur[1]) - 1);  // the span to draw
+                        cur[1] &= cur[1] - 1;
+                    }
+#pragma unroll 1
+                    for (int i = 0; i < PX; i++) {
+                        const int32_t x = wi.x0 + i * tpr + lr;
+                        const int32_t lx = x - ox;
+                        uint32_t cv = 0;
+                        if (hair) {
+                            if (row_in && x < wi.x1) cv = hair_cov(reinterpret_cast<const HairSpan *>(sp[1]), lx, ly);
                         } else {
-                            int q = cur[0];
-                            while (q < ns[0] && sp[0][q].y <= w0) q++;
-                            cur[0] = q;
-                            for (int k2 = q; k2 < ns[0]; k2++) {
-                                const int2 a2 = sp[0][k2];
-                                if (a2.x >= w1) break;
-                                if (lx >= a2.x && lx < a2.y) cv = 255;
+                            const int32_t wx = wi.x0 + i * tpr + (lr & ~31) - ox;  // warp window start (layer x)
+                            const int32_t w0 = wx << sub, w1 = (wx + 32) << sub;
+                            if (row_in && w1 > rowL && w0 < rowR) {
+                                if (aa) {
+                                    const int32_t p0 = lx << 2;
+                                    cv = span_cov(sp[0], ns[0], cur[0], w0, w1, p0, 64u) +
+                                         span_cov(sp[1], ns[1], cur[1], w0, w1, p0, 64u) +
+                                         span_cov(sp[2], ns[2], cur[2], w0, w1, p0, 64u) +
+                                         span_cov(sp[3], ns[3], cur[3], w0, w1, p0, 63u);
+                                    cv = min(cv, 255u);
+                                } else {
+                                    int q = cur[0];
+                                    while (q < ns[0] && sp[0][q].y <= w0) q++;
+                                    cur[0] = q;
+                                    for (int k2 = q; k2 < ns[0]; k2++) {
+                                        const int2 a2 = sp[0][k2];
+                                        if (a2.x >= w1) break;
+                                        if (lx >= a2.x && lx < a2.y) cv = 255;
+                                    }
+                                }
+                                if (lx < sect.x || lx >= sect.z) cv = 0;
                             }
                         }
-                        if (lx < sect.x || lx >= sect.z) cv = 0;
-                    }
-                    uint32_t &px = layer[i * kThreads + tid];
-                    if (c.op == CMD_FILL) {
-                        if (cv && !(pr.flags & PAINT_SKIP)) px = dev::shade_pixel(pr, gr, lx, ly, cv, px);
-                    } else {
-                        // region mask: Mask::fill_path coverage (lerp 0 -> 255), then apply_mask
-                        const bool in_top = row_ok && x < wi.x1 && x >= top_x && x < top_x + top_w && cy >= top_y &&
-                                            cy < top_y + top_h;
-                        if (in_top) {
-                            uint32_t m = cv == 255 ? 255u
-                                                   : (uint32_t)dev::div255((uint32_t)dev::sat_u16(((float)cv * dev::kInv255) * 255.0f + 0.5f) * 255u);
-                            px = dev::mask_pixel(px, m);
+                        uint32_t &px = layer[i * kThreads + tid];
+                        if (c.op != CMD_APPLY_REGION) {
+                            if (cv && !(pr.flags & PAINT_SKIP)) px = dev::shade_pixel(pr, gr, lx, ly, cv, px);
+                        } else {
+                            // region mask: Mask::fill_path coverage (lerp 0 -> 255), then apply_mask
+                            const bool in_top = row_ok && x < wi.x1 && x >= top_x && x < top_x + top_w && cy >= top_y &&
+                                                cy < top_y + top_h;
+                            if (in_top) {
+                                uint32_t m = cv == 255 ? 255u
+                                                       : (uint32_t)dev::div255((uint32_t)dev::sat_u16(((float)cv * dev::kInv255) * 255.0f + 0.5f) * 255u);
+                                px = dev::mask_pixel(px, m);
+                            }
                         }
                     }
+                    if (!hair) break;
                 }
             } else if (c.op == CMD_PUSH) {
                 __syncthreads();
@@ -420,10 +527,11 @@ cudaError_t launch_raster(int px, uint32_t grid, uint32_t stack_depth, const Str
                           uint32_t nitems, uint32_t *item_counter, const Cmd *cmds, const DrawRec *draws,
                           const PaintRec *paints, const GradRec *grads, const LayerRec *layers, const EdgeRec *bins,
                           const uint32_t *bin_offsets, const uint32_t *bin_counts, uint32_t *stack, int2 *span_ovf,
-                          uint32_t ovf_cap, uint32_t *err, cudaStream_t s) {
+                          uint32_t ovf_cap, const HairRec *hairs, const HairSpan *hair_spans, uint32_t *err,
+                          cudaStream_t s) {
     k_raster<<<grid, kThreads, raster_smem_bytes_px(px), s>>>(px, streams, items, nitems, item_counter, cmds, draws, paints,
                                                               grads, layers, bins, bin_offsets, bin_counts, stack,
-                                                              stack_depth, span_ovf, ovf_cap, err);
+                                                              stack_depth, span_ovf, ovf_cap, hairs, hair_spans, err);
     return cudaGetLastError();
 }
 
