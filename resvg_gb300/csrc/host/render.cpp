@@ -79,14 +79,14 @@ struct Buffers {
     DevBuf verbs, pts, draws, paints, grads, layers, cmds, streams, items;
     DevBuf tpts, segs, seg_counts, seg_offsets, scan_scratch, totals;
     DevBuf edges, edge_draw, bin_counts, bin_offsets, bins;
-    DevBuf stack, span_ovf, err, counter;
+    DevBuf stack, span_ovf, run_ovf, err, counter;
     DevBuf hairs, hair_spans;
     std::vector<DevBuf> surf, img;   // internal surfaces (filter content/results) and filter images
     DevBuf plane;                    // f64 plane of the IIR blur
     void release() {
         DevBuf *all[] = {&verbs, &pts, &draws, &paints, &grads, &layers, &cmds, &streams, &items, &tpts, &segs,
                          &seg_counts, &seg_offsets, &scan_scratch, &totals, &edges, &edge_draw, &bin_counts,
-                         &bin_offsets, &bins, &stack, &span_ovf, &err, &counter, &plane, &hairs, &hair_spans};
+                         &bin_offsets, &bins, &stack, &span_ovf, &run_ovf, &err, &counter, &plane, &hairs, &hair_spans};
         for (DevBuf *b : all) {
             if (b->p) cudaFree(b->p);
             b->p = nullptr;
@@ -117,6 +117,8 @@ struct BufScratch : FilterScratch {
 };
 
 // A flattened submission with its work decomposition.
+constexpr uint32_t kSpanOvf = 64;  // spans one sub-scanline of one draw may hold in the raster kernel
+
 struct Plan {
     SceneBuild sb;
     std::vector<WorkItem> items;
@@ -125,6 +127,7 @@ struct Plan {
     uint64_t nbins = 0;
     uint32_t max_depth = 1;
     uint32_t grid = 1;
+    uint32_t run_cap = 0;              // alpha-run overflow entries per (draw, row) pair
     uint32_t nedges = 0, nbinned = 0;  // known after the first (sizing) run
     bool sized = false;
 };
@@ -246,6 +249,11 @@ int plan_scene(Context &c, Plan &p) {
                          [&](const WorkItem &a, const WorkItem &b) { return cost(a) > cost(b); });
     }
     if (p.nbins > 0xF0000000ull) { set_error("too many (band, draw) bins"); return RGPU_ERR_CAPACITY; }
+    // a pair's runs cover at most its work item's width, one entry per pixel
+    // step, or two per aliased span (kSpanOvf spans a scanline at most)
+    uint32_t item_w = 0;
+    for (const auto &st : sb.streams) item_w = std::max(item_w, (256 / st.band_rows) * p.px);
+    p.run_cap = std::max(item_w, 2 * kSpanOvf) + 2;
     uint32_t per_sm = (uint32_t)raster_max_blocks_per_sm((int)p.px);
     p.grid = std::max<uint32_t>(1, std::min<uint32_t>((uint32_t)p.items.size(), (uint32_t)c.sms * per_sm));
     return RGPU_OK;
@@ -290,10 +298,10 @@ int upload_plan(Context &c, Buffers &b, Plan &p, cudaStream_t s) {
     CK(b.scan_scratch.ensure(scan_scratch_words(std::max<uint64_t>(nsegs + 1, p.nbins + 1)) * 4));
     CK(b.bin_counts.ensure((p.nbins + 1) * 4));
     CK(b.bin_offsets.ensure((p.nbins + 1) * 4));
-    const uint32_t ovf_cap = 64;
     size_t stack_words = (size_t)p.max_depth * raster_threads() * p.px;
     CK(b.stack.ensure((size_t)p.grid * stack_words * 4));
-    CK(b.span_ovf.ensure((size_t)p.grid * raster_threads() * ovf_cap * 8));
+    CK(b.span_ovf.ensure((size_t)p.grid * raster_threads() * kSpanOvf * 8));
+    CK(b.run_ovf.ensure((size_t)p.grid * raster_max_pairs() * p.run_cap * 8));
     CK(b.err.ensure(16));
     CK(b.counter.ensure(4 * (sb.max_level + 1)));
     return RGPU_OK;
@@ -349,7 +357,6 @@ int enqueue_plan(Context &c, Buffers &b, Plan &p, cudaStream_t s, cudaEvent_t ev
     CK(cudaMemsetAsync(b.counter.p, 0, 4 * (sb.max_level + 1), s));
     for (const auto &st : sb.streams)
         if (st.surface >= 0) CK(cudaMemsetAsync(b.surf[st.surface].p, 0, (size_t)st.out_w * st.out_h * 4, s));
-    const uint32_t ovf_cap = 64;
     BufScratch scratch(b);
     for (uint32_t lv = 0; lv <= sb.max_level; lv++) {
         bool last = lv == sb.max_level;
@@ -359,8 +366,8 @@ int enqueue_plan(Context &c, Buffers &b, Plan &p, cudaStream_t s, cudaEvent_t ev
                              b.items.as<WorkItem>() + p.level_off[lv], p.level_cnt[lv], b.counter.as<uint32_t>() + lv,
                              b.cmds.as<Cmd>(), b.draws.as<DrawRec>(), b.paints.as<PaintRec>(), b.grads.as<GradRec>(),
                              b.layers.as<LayerRec>(), b.bins.as<EdgeRec>(), b.bin_offsets.as<uint32_t>(),
-                             b.bin_counts.as<uint32_t>(), b.stack.as<uint32_t>(), b.span_ovf.as<int2>(), ovf_cap,
-                             b.hairs.as<HairRec>(), b.hair_spans.as<HairSpan>(), b.err.as<uint32_t>(), s));
+                             b.bin_counts.as<uint32_t>(), b.stack.as<uint32_t>(), b.span_ovf.as<int2>(), kSpanOvf,
+                             b.run_ovf.as<int2>(), p.run_cap, b.hairs.as<HairRec>(), b.hair_spans.as<HairSpan>(), b.err.as<uint32_t>(), s));
         if (ev1 && last) CK(cudaEventRecord(ev1, s));
         for (const auto &job : sb.jobs) {
             if (job.level != lv) continue;

@@ -31,9 +31,10 @@ cudaError_t launch_raster(int px, uint32_t grid, uint32_t stack_depth, const Str
                           uint32_t *item_counter, const Cmd *cmds, const DrawRec *draws, const PaintRec *paints,
                           const GradRec *grads, const LayerRec *layers, const EdgeRec *bins,
                           const uint32_t *bin_offsets, const uint32_t *bin_counts, uint32_t *stack, int2 *span_ovf,
-                          uint32_t ovf_cap, const HairRec *hairs, const HairSpan *hair_spans, uint32_t *err,
+                          uint32_t ovf_cap, int2 *run_ovf, uint32_t run_ovf_cap, const HairRec *hairs, const HairSpan *hair_spans, uint32_t *err,
                           cudaStream_t s);
 int raster_max_blocks_per_sm(int px);
+int raster_max_pairs();  // (draw, row) pairs of one phase-A window
 
 // filters.cu
 cudaError_t filter_color_space(uint32_t *img, size_t n, bool to_linear, cudaStream_t s);

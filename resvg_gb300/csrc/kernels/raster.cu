@@ -30,6 +30,8 @@ constexpr int kSpanCap = 8;      // spans per (slot, sub-scanline) kept in share
 constexpr int kMaxDepth = 48;    // layer stack depth
 
 constexpr int kMaxSlots = 32;   // draws per phase-A window
+constexpr int kMaxPairs = kThreads / 4;  // (slot, row) pairs per window: K x BH <= kThreads / 4
+constexpr int kRunCap = 32;     // alpha runs per (slot, row) kept in shared memory
 
 struct VmShared {
     int32_t win_first;           // first command index of the prepared window
@@ -38,6 +40,8 @@ struct VmShared {
     int32_t slot_cmd[kMaxSlots]; // command index per slot
     uint16_t span_cnt[kThreads];
     int2 spans[kThreads * kSpanCap];
+    uint16_t run_cnt[kMaxPairs];  // alpha runs per (slot, row), including the closing sentinel
+    int2 runs[kMaxPairs * kRunCap];
     int4 rects[kMaxDepth];       // layer-stack rects (x, y, w, h), uniform across the CTA
     PaintRec paint[kMaxSlots + 1];   // paints of the window's draws; the last: the current hairline's
     int4 slot_geo[kMaxSlots];    // (valid | shift << 1, ox, oy, unused) per slot
@@ -155,6 +159,91 @@ __device__ __forceinline__ uint32_t span_cov(const int2 *L, int n, int &q, int32
     return cov;
 }
 
+// Alpha runs of one (slot, row): entries (end, alpha), alpha covering the
+// layer pixels [previous end, end), the list closed by (INT32_MAX, 0), so a
+// pixel's coverage is the alpha of the first entry whose end exceeds it.  The
+// pixel coverage is SuperBlitter's (scan/path_aa.rs): over the row's 4
+// sub-scanlines, 16 per covered sub-column, or 64 (63 on the 4th) for a fully
+// covered pixel, capped at 255; aliased spans are whole pixels at 255.  Only
+// [lo, hi) (the draw's coverage rect, the work item) can be non-zero.
+struct RunWriter {
+    int2 *sm, *gl;
+    uint32_t gcap;
+    int n;
+    int32_t alpha;  // alpha from the last stored end onwards
+    __device__ void put(int32_t end, int32_t a, uint32_t *err) {
+        if (n < kRunCap) sm[n] = make_int2(end, a);
+        else {
+            if (n == kRunCap)
+                for (int k = 0; k < kRunCap; k++) gl[k] = sm[k];
+            // the last entry that fits stays a sentinel, so readers always stop
+            if ((uint32_t)n + 1 < gcap) gl[n] = make_int2(end, a);
+            else { gl[gcap - 1] = make_int2(INT32_MAX, 0); if (end != INT32_MAX) atomicOr(err, 2u); }
+        }
+        n++;
+    }
+    // coverage changes to `a` at pixel x
+    __device__ __forceinline__ void set(int32_t x, int32_t a, uint32_t *err) {
+        if (a != alpha) { put(x, alpha, err); alpha = a; }
+    }
+};
+
+__device__ void merge_runs(VmShared &sh, const int2 *ovf, uint32_t ovf_cap, int2 *rovf, uint32_t rovf_cap, int pair,
+                           int sj, bool aa, int32_t lo, int32_t hi, uint32_t *err) {
+    RunWriter w{&sh.runs[pair * kRunCap], rovf + (size_t)pair * rovf_cap, rovf_cap, 0, 0};
+    if (aa) {
+        const int2 *L[4];
+        int n[4], q[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            n[j] = sh.span_cnt[sj + j];
+            L[j] = span_base(sh, ovf, ovf_cap, sj + j, n[j]);
+            q[j] = 0;
+        }
+        int32_t x = lo;
+        while (x < hi) {
+            int32_t nxt = hi;
+            uint32_t sum = 0;
+            const int32_t p0 = x << 2;
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                while (q[j] < n[j] && L[j][q[j]].y <= p0) q[j]++;
+                for (int k = q[j]; k < n[j]; k++) {
+                    const int2 a = L[j][k];
+                    if (a.x >= p0 + 4) { nxt = min(nxt, a.x >> 2); break; }
+                    const int32_t ov = min(a.y, p0 + 4) - max(a.x, p0);
+                    if (ov == 4) {  // full from here up to the pixel holding the span's end
+                        sum += j == 3 ? 63u : 64u;
+                        nxt = min(nxt, a.y >> 2);
+                    } else {
+                        sum += (uint32_t)ov * 16u;
+                        nxt = min(nxt, x + 1);
+                    }
+                }
+            }
+            w.set(x, (int32_t)min(sum, 255u), err);
+            x = nxt;
+        }
+    } else {
+        const int n0 = sh.span_cnt[sj];
+        const int2 *L0 = span_base(sh, ovf, ovf_cap, sj, n0);
+        for (int k = 0; k < n0; k++) {
+            const int2 a = L0[k];
+            const int32_t x0 = max(a.x, lo), x1 = min(a.y, hi);
+            if (x0 >= x1) continue;
+            w.set(x0, 255, err);
+            w.set(x1, 0, err);
+        }
+    }
+    w.set(hi, 0, err);
+    w.put(INT32_MAX, 0, err);
+    sh.run_cnt[pair] = (uint16_t)min(w.n, (int)rovf_cap);
+}
+
+__device__ __forceinline__ const int2 *run_base(const VmShared &sh, const int2 *rovf, uint32_t rovf_cap, int pair) {
+    return sh.run_cnt[pair] <= kRunCap ? &sh.runs[pair * kRunCap] : rovf + (size_t)pair * rovf_cap;
+}
+
 // Coverage of layer pixel (px, py) from one hairline span (tiny-skia
 // scan/hairline_aa.rs: the step k on the pixel's major coordinate, the two
 // pixels its blitter touches, alpha scaled by the end-cap fraction); 0 = no
@@ -205,14 +294,15 @@ __global__ void __launch_bounds__(kThreads, 3)
 k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitems, uint32_t *item_counter,
          const Cmd *cmds, const DrawRec *draws, const PaintRec *paints, const GradRec *grads, const LayerRec *layers,
          const EdgeRec *bins, const uint32_t *bin_offsets, const uint32_t *bin_counts, uint32_t *stack_scratch,
-         uint32_t stack_depth, int2 *span_ovf, uint32_t ovf_cap, const HairRec *hairs, const HairSpan *hair_spans,
-         uint32_t *err) {
+         uint32_t stack_depth, int2 *span_ovf, uint32_t ovf_cap, int2 *run_ovf, uint32_t rovf_cap, const HairRec *hairs,
+         const HairSpan *hair_spans, uint32_t *err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     VmShared &sh = *reinterpret_cast<VmShared *>(smem_raw);
     uint32_t *layer = reinterpret_cast<uint32_t *>(smem_raw + ((sizeof(VmShared) + 15) & ~(size_t)15));
     const int tid = threadIdx.x;
     uint32_t *stack = stack_scratch + (size_t)blockIdx.x * stack_depth * kThreads * PX;
     int2 *ovf = span_ovf + (size_t)blockIdx.x * kThreads * ovf_cap;
+    int2 *rovf = run_ovf + (size_t)blockIdx.x * kMaxPairs * rovf_cap;
 
     for (;;) {
         if (tid == 0) sh.item = (int32_t)atomicAdd(item_counter, 1u);
@@ -318,17 +408,33 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
                         else sh.span_cnt[tid] = 0;
                     }
                     __syncthreads();
+                    // ---- merge each (slot, row)'s sub-scanline spans into alpha runs
+                    if (tid < sh.nslots * BH) {
+                        const int k2 = tid / BH, r2 = tid % BH;
+                        const int4 geo = sh.slot_geo[k2];
+                        const int4 sect = sh.slot_sect[k2];
+                        const int32_t ly = (int32_t)wi.band * BH + r2 - geo.z;
+                        int32_t lo = max(sect.x, wi.x0 - geo.y), hi = min(sect.z, wi.x1 - geo.y);
+                        if (!(geo.x & 1) || ly < sect.y || ly >= sect.w || (int32_t)wi.band * BH + r2 >= st.out_h) hi = lo;
+                        const bool aa2 = geo.x & 2;
+                        merge_runs(sh, ovf, ovf_cap, rovf, rovf_cap, tid, k2 * S + r2 * (aa2 ? 4 : 1), aa2, lo, hi, err);
+                    }
+                    __syncthreads();
                 }
                 // ---- phase B: coverage + shading, one pixel per (thread, i).  A hairline
                 // (CMD_HAIR) runs its spans in order through the same loop, each thread
                 // for its own pixels, so blits to one pixel keep their order.
                 const bool hair = c.op == CMD_HAIR;
                 int32_t ox, oy;
-                bool aa = true, row_in;
-                int4 sect = make_int4(0, 0, 0, 0);
                 int slot;
-                const int2 *sp[4];
-                int ns[4], cur[4] = {0, 0, 0, 0};
+                // coverage source: alpha runs of a fill (rp, cursor q), or for a
+                // hairline its span list (hs, hn), the chunk of 32 being walked (hq)
+                // and the chunk's spans that meet this work item (hm)
+                const int2 *rp = nullptr;
+                int q = 0;
+                const HairSpan *hs = nullptr;
+                int hn = 0, hq = -32;
+                uint32_t hm = 0;
                 if (hair) {
                     // stage the hairline's paint in the spare slot (uniform across the CTA)
                     const HairRec hr = hairs[c.a];
@@ -346,64 +452,41 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
                     __syncthreads();
                     if (sh.paint[slot].flags & PAINT_SKIP) continue;
                     ox = hr.ox; oy = hr.oy;
-                    // the fill span registers carry the hairline's span list: sp[0] the
-                    // spans, ns[0] their count, cur[0] the chunk of 32 being walked and
-                    // cur[1] its spans that meet this work item; sp[1] the span drawn
-                    sp[0] = reinterpret_cast<const int2 *>(hair_spans + hr.span_off);
-                    ns[0] = (int)hr.span_cnt;
-                    cur[0] = -32;
-                    row_in = row_ok;
+                    hs = hair_spans + hr.span_off;
+                    hn = (int)hr.span_cnt;
                 } else {
                     slot = slot_next++;
+                    const int pair = slot * BH + row;
+                    // one entry: the closing sentinel alone, nothing covered on this row
+                    if (c.op == CMD_FILL && sh.run_cnt[pair] <= 1) continue;
                     const int4 geo = sh.slot_geo[slot];
-                    const bool dvalid = geo.x & 1;
-                    aa = geo.x & 2;
-                    if (!dvalid && c.op == CMD_FILL) continue;
-                    sect = sh.slot_sect[slot];
                     ox = geo.y; oy = geo.z;
-                    row_in = dvalid && row_ok && cy - oy >= sect.y && cy - oy < sect.w;
-                    if (c.op == CMD_FILL && !row_in) continue;
+                    rp = run_base(sh, rovf, rovf_cap, pair);
                 }
                 const PaintRec &pr = sh.paint[slot];
                 const GradRec *gr = &sh.grad[slot];  // read only for gradient paints
                 const int32_t ly = cy - oy;
                 const int32_t lrow0 = (int32_t)wi.band * BH - oy;
-                const int nsl = aa ? 4 : 1;
-                const int sj0 = slot * S + (ly - lrow0) * nsl;
-                int32_t rowL = INT32_MAX, rowR = INT32_MIN;
-                if (row_in && !hair) {
-#pragma unroll
-                    for (int q = 0; q < 4; q++) {
-                        ns[q] = 0;
-                        sp[q] = nullptr;
-                        if (q < nsl) {
-                            ns[q] = sh.span_cnt[sj0 + q];
-                            sp[q] = span_base(sh, ovf, ovf_cap, sj0 + q, ns[q]);
-                            if (ns[q]) { rowL = min(rowL, sp[q][0].x); rowR = max(rowR, sp[q][ns[q] - 1].y); }
-                        }
-                    }
-                }
-                if (c.op == CMD_FILL && rowL >= rowR) continue;  // no span on this row
-                const int sub = aa ? 2 : 0;  // sub-column shift
 #pragma unroll 1
                 for (;;) {
+                    const HairSpan *hcur = nullptr;
                     if (hair) {
                         // the next span that meets this work item, in order: each warp
                         // tests 32 span rects at a time (the same answer in every warp)
-                        while (cur[1] == 0) {
-                            cur[0] += 32;
-                            if (cur[0] >= ns[0]) break;
-                            const int j = cur[0] + (tid & 31);
+                        while (hm == 0) {
+                            hq += 32;
+                            if (hq >= hn) break;
+                            const int j = hq + (tid & 31);
                             bool meets = false;
-                            if (j < ns[0]) {
-                                const int4 r = __ldg(reinterpret_cast<const int4 *>(sp[0]) + 2 * j + 1);
+                            if (j < hn) {
+                                const int4 r = __ldg(reinterpret_cast<const int4 *>(hs + j) + 1);
                                 meets = !(r.z <= wi.x0 - ox || r.x >= wi.x1 - ox || r.w <= lrow0 || r.y >= lrow0 + BH);
                             }
-                            cur[1] = (int)__ballot_sync(0xffffffffu, meets);
+                            hm = __ballot_sync(0xffffffffu, meets);
                         }
-                        if (cur[1] == 0) break;
-                        sp[1] = sp[0] + 4 * (cur[0] + __ffs(cur[1]) - 1);  // the span to draw
-                        cur[1] &= cur[1] - 1;
+                        if (hm == 0) break;
+                        hcur = hs + hq + __ffs(hm) - 1;  // the span to draw
+                        hm &= hm - 1;
                     }
 #pragma unroll 1
                     for (int i = 0; i < PX; i++) {
@@ -411,30 +494,10 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
                         const int32_t lx = x - ox;
                         uint32_t cv = 0;
                         if (hair) {
-                            if (row_in && x < wi.x1) cv = hair_cov(reinterpret_cast<const HairSpan *>(sp[1]), lx, ly);
+                            if (row_ok && x < wi.x1) cv = hair_cov(hcur, lx, ly);
                         } else {
-                            const int32_t wx = wi.x0 + i * tpr + (lr & ~31) - ox;  // warp window start (layer x)
-                            const int32_t w0 = wx << sub, w1 = (wx + 32) << sub;
-                            if (row_in && w1 > rowL && w0 < rowR) {
-                                if (aa) {
-                                    const int32_t p0 = lx << 2;
-                                    cv = span_cov(sp[0], ns[0], cur[0], w0, w1, p0, 64u) +
-                                         span_cov(sp[1], ns[1], cur[1], w0, w1, p0, 64u) +
-                                         span_cov(sp[2], ns[2], cur[2], w0, w1, p0, 64u) +
-                                         span_cov(sp[3], ns[3], cur[3], w0, w1, p0, 63u);
-                                    cv = min(cv, 255u);
-                                } else {
-                                    int q = cur[0];
-                                    while (q < ns[0] && sp[0][q].y <= w0) q++;
-                                    cur[0] = q;
-                                    for (int k2 = q; k2 < ns[0]; k2++) {
-                                        const int2 a2 = sp[0][k2];
-                                        if (a2.x >= w1) break;
-                                        if (lx >= a2.x && lx < a2.y) cv = 255;
-                                    }
-                                }
-                                if (lx < sect.x || lx >= sect.z) cv = 0;
-                            }
+                            while (rp[q].x <= lx) q++;
+                            cv = (uint32_t)rp[q].y;
                         }
                         uint32_t &px = layer[i * kThreads + tid];
                         if (c.op != CMD_APPLY_REGION) {
@@ -518,6 +581,7 @@ size_t raster_smem_bytes_px(int px) { return ((sizeof(VmShared) + 15) & ~(size_t
 size_t raster_smem_bytes() { return raster_smem_bytes_px(16); }
 size_t raster_stack_words_per_cta(int px) { return (size_t)kMaxDepth * kThreads * px; }
 int raster_threads() { return kThreads; }
+int raster_max_pairs() { return kMaxPairs; }
 
 cudaError_t raster_init() {
     return cudaFuncSetAttribute(k_raster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)raster_smem_bytes_px(16));
@@ -527,11 +591,12 @@ cudaError_t launch_raster(int px, uint32_t grid, uint32_t stack_depth, const Str
                           uint32_t nitems, uint32_t *item_counter, const Cmd *cmds, const DrawRec *draws,
                           const PaintRec *paints, const GradRec *grads, const LayerRec *layers, const EdgeRec *bins,
                           const uint32_t *bin_offsets, const uint32_t *bin_counts, uint32_t *stack, int2 *span_ovf,
-                          uint32_t ovf_cap, const HairRec *hairs, const HairSpan *hair_spans, uint32_t *err,
+                          uint32_t ovf_cap, int2 *run_ovf, uint32_t run_ovf_cap, const HairRec *hairs, const HairSpan *hair_spans, uint32_t *err,
                           cudaStream_t s) {
     k_raster<<<grid, kThreads, raster_smem_bytes_px(px), s>>>(px, streams, items, nitems, item_counter, cmds, draws, paints,
                                                               grads, layers, bins, bin_offsets, bin_counts, stack,
-                                                              stack_depth, span_ovf, ovf_cap, hairs, hair_spans, err);
+                                                              stack_depth, span_ovf, ovf_cap, run_ovf, run_ovf_cap, hairs,
+                                                              hair_spans, err);
     return cudaGetLastError();
 }
 
