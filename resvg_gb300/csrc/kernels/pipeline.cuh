@@ -266,17 +266,36 @@ __device__ __forceinline__ void gradient_eval_lowp(const GradRec &g, int32_t px,
     }
 }
 
+// Two u16 lanes per register (r | b << 16, g | a << 16): every lane value of
+// the lowp source-over path stays <= 255 * 255 + 255, so lanes never carry into
+// each other and div255 = (v + 255) >> 8 runs on both at once.
+__device__ __forceinline__ uint32_t div255_2(uint32_t v) { return ((v + 0x00FF00FFu) >> 8) & 0x00FF00FFu; }
+
+// lowp gradient colour as two lane pairs (same arithmetic as gradient_eval_lowp).
+__device__ __forceinline__ void gradient_eval_lowp2(const GradRec &g, int32_t px, int32_t py, uint32_t &rb,
+                                                    uint32_t &ga) {
+    float c[4];
+    gradient_eval(g, px, py, c, false);
+    uint32_t s[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) s[k] = (uint32_t)(fminf(fmaxf(c[k], 0.0f), 1.0f) * 255.0f + 0.5f);
+    rb = s[0] | s[2] << 16;
+    ga = s[1] | s[3] << 16;
+    if (g.flags & GRAD_PREMUL) {
+        rb = div255_2(rb * s[3]);
+        ga = (div255_2(ga * s[3]) & 0xFFFFu) | s[3] << 16;
+    }
+}
+
 __device__ __forceinline__ float4 unpack_f(uint32_t p) {
     return make_float4((float)ch(p, 0) * kInv255, (float)ch(p, 1) * kInv255, (float)ch(p, 2) * kInv255,
                        (float)ch(p, 3) * kInv255);
 }
 __device__ __forceinline__ uint32_t pack_f(float4 o) { return pack(unnorm(o.x), unnorm(o.y), unnorm(o.z), unnorm(o.w)); }
 
-// Blits one pixel of a fill with coverage `cov` (1..255) onto `dst`.
-__device__ __forceinline__ uint32_t shade_pixel(const PaintRec &pr, const GradRec *grad, int32_t lx, int32_t ly,
-                                                uint32_t cov, uint32_t dst) {
-    if (cov == 255 && (pr.flags & PAINT_MEMSET))
-        return pack(pr.memset_rgba[0], pr.memset_rgba[1], pr.memset_rgba[2], pr.memset_rgba[3]);
+// shade_pixel for the paints and blend modes off the inline fast path.
+__device__ __forceinline__ uint32_t shade_pixel_slow(const PaintRec &pr, const GradRec *grad, int32_t lx,
+                                                         int32_t ly, uint32_t cov, uint32_t dst) {
     const uint32_t blend = pr.blend;
     if (pr.flags & PAINT_LOWP) {
         uint16_t s[4] = {pr.rgba16[0], pr.rgba16[1], pr.rgba16[2], pr.rgba16[3]};
@@ -326,6 +345,36 @@ __device__ __forceinline__ uint32_t shade_pixel(const PaintRec &pr, const GradRe
         }
     }
     return pack_f(o);
+}
+
+// Blits one pixel of a fill with coverage `cov` (1..255) onto `dst`: the
+// common lowp source-over case inline, every other paint and blend mode out of
+// line (rare in practice, and kept out of the caller's registers).
+__device__ __forceinline__ uint32_t shade_pixel(const PaintRec &pr, const GradRec *grad, int32_t lx, int32_t ly,
+                                                uint32_t cov, uint32_t dst) {
+    if (cov == 255 && (pr.flags & PAINT_MEMSET))
+        return pack(pr.memset_rgba[0], pr.memset_rgba[1], pr.memset_rgba[2], pr.memset_rgba[3]);
+    const uint32_t blend = pr.blend;
+    if ((pr.flags & PAINT_LOWP) && blend == RGPU_BLEND_SOURCE_OVER) {
+        // lowp source-over (pre-scaled by coverage), two lanes per register
+        uint32_t rb, ga;
+        if (pr.kind != 0) gradient_eval_lowp2(*grad, lx, ly, rb, ga);
+        else {
+            const uint32_t w0 = *reinterpret_cast<const uint32_t *>(&pr.rgba16[0]);
+            const uint32_t w1 = *reinterpret_cast<const uint32_t *>(&pr.rgba16[2]);
+            rb = __byte_perm(w0, w1, 0x5410);
+            ga = __byte_perm(w0, w1, 0x7632);
+        }
+        if (cov != 255) {
+            rb = div255_2(rb * cov);
+            ga = div255_2(ga * cov);
+        }
+        const uint32_t inv = 255u - (ga >> 16);
+        rb += div255_2((dst & 0x00FF00FFu) * inv);
+        ga += div255_2(((dst >> 8) & 0x00FF00FFu) * inv);
+        return (rb & 0x00FF00FFu) | ((ga & 0x00FF00FFu) << 8);
+    }
+    return shade_pixel_slow(pr, grad, lx, ly, cov, dst);
 }
 
 // draw_pixmap of one pixel: highp pattern (already at the right pixel),

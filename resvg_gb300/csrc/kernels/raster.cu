@@ -42,7 +42,9 @@ struct VmShared {
     int2 spans[kThreads * kSpanCap];
     uint16_t run_cnt[kMaxPairs];  // alpha runs per (slot, row), including the closing sentinel
     int2 runs[kMaxPairs * kRunCap];
-    int4 rects[kMaxDepth];       // layer-stack rects (x, y, w, h), uniform across the CTA
+    int4 rects[kMaxDepth];       // layer-stack rects (x, y, w, h) by depth, the top one at [depth]
+    WorkItem wi;                 // the work item being rendered, and its stream
+    StreamRec st;
     PaintRec paint[kMaxSlots + 1];   // paints of the window's draws; the last: the current hairline's
     int4 slot_geo[kMaxSlots];    // (valid | shift << 1, ox, oy, unused) per slot
     int4 slot_sect[kMaxSlots];   // coverage rect (l, t, r, b) per slot
@@ -305,13 +307,22 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
     int2 *rovf = run_ovf + (size_t)blockIdx.x * kMaxPairs * rovf_cap;
 
     for (;;) {
-        if (tid == 0) sh.item = (int32_t)atomicAdd(item_counter, 1u);
+        if (tid == 0) {
+            const int32_t idx = (int32_t)atomicAdd(item_counter, 1u);
+            sh.item = idx;
+            if (idx < (int32_t)nitems) {
+                sh.wi = items[idx];
+                sh.st = streams[sh.wi.stream];
+                sh.rects[0] = make_int4(0, 0, sh.st.out_w, sh.st.out_h);
+            }
+        }
         __syncthreads();
         const int32_t item_idx = sh.item;
         __syncthreads();
         if (item_idx >= (int32_t)nitems) break;
-        const WorkItem wi = items[item_idx];
-        const StreamRec st = streams[wi.stream];
+        // uniform across the CTA: read from shared memory where used
+        const WorkItem &wi = sh.wi;
+        const StreamRec &st = sh.st;
         const int BH = (int)st.band_rows;
         const int S = 4 * BH;                 // scanline slots per draw (sub-scanlines for AA)
         const int K = min(kThreads / S, kMaxSlots);
@@ -328,7 +339,6 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
                 (row_ok && x < wi.x1) ? *(const uint32_t *)(out + (size_t)cy * st.out_stride + 4 * (size_t)x) : 0u;
         }
         int32_t depth = 0;
-        int32_t top_x = 0, top_y = 0, top_w = st.out_w, top_h = st.out_h;
         if (tid == 0) { sh.win_first = 0; sh.win_last = 0; sh.nslots = 0; }
         __syncthreads();
         int32_t slot_next = 0;
@@ -432,8 +442,7 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
                 // and the chunk's spans that meet this work item (hm)
                 const int2 *rp = nullptr;
                 int q = 0;
-                const HairSpan *hs = nullptr;
-                int hn = 0, hq = -32;
+                int hs = 0, hn = 0, hq = -32;
                 uint32_t hm = 0;
                 if (hair) {
                     // stage the hairline's paint in the spare slot (uniform across the CTA)
@@ -452,7 +461,7 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
                     __syncthreads();
                     if (sh.paint[slot].flags & PAINT_SKIP) continue;
                     ox = hr.ox; oy = hr.oy;
-                    hs = hair_spans + hr.span_off;
+                    hs = (int)hr.span_off;
                     hn = (int)hr.span_cnt;
                 } else {
                     slot = slot_next++;
@@ -469,7 +478,7 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
                 const int32_t lrow0 = (int32_t)wi.band * BH - oy;
 #pragma unroll 1
                 for (;;) {
-                    const HairSpan *hcur = nullptr;
+                    int hcur = 0;
                     if (hair) {
                         // the next span that meets this work item, in order: each warp
                         // tests 32 span rects at a time (the same answer in every warp)
@@ -479,7 +488,7 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
                             const int j = hq + (tid & 31);
                             bool meets = false;
                             if (j < hn) {
-                                const int4 r = __ldg(reinterpret_cast<const int4 *>(hs + j) + 1);
+                                const int4 r = __ldg(reinterpret_cast<const int4 *>(hair_spans + hs + j) + 1);
                                 meets = !(r.z <= wi.x0 - ox || r.x >= wi.x1 - ox || r.w <= lrow0 || r.y >= lrow0 + BH);
                             }
                             hm = __ballot_sync(0xffffffffu, meets);
@@ -494,7 +503,7 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
                         const int32_t lx = x - ox;
                         uint32_t cv = 0;
                         if (hair) {
-                            if (row_ok && x < wi.x1) cv = hair_cov(hcur, lx, ly);
+                            if (row_ok && x < wi.x1) cv = hair_cov(hair_spans + hcur, lx, ly);
                         } else {
                             while (rp[q].x <= lx) q++;
                             cv = (uint32_t)rp[q].y;
@@ -504,8 +513,9 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
                             if (cv && !(pr.flags & PAINT_SKIP)) px = dev::shade_pixel(pr, gr, lx, ly, cv, px);
                         } else {
                             // region mask: Mask::fill_path coverage (lerp 0 -> 255), then apply_mask
-                            const bool in_top = row_ok && x < wi.x1 && x >= top_x && x < top_x + top_w && cy >= top_y &&
-                                                cy < top_y + top_h;
+                            const int4 t = sh.rects[depth];
+                            const bool in_top = row_ok && x < wi.x1 && x >= t.x && x < t.x + t.z && cy >= t.y &&
+                                                cy < t.y + t.w;
                             if (in_top) {
                                 uint32_t m = cv == 255 ? 255u
                                                        : (uint32_t)dev::div255((uint32_t)dev::sat_u16(((float)cv * dev::kInv255) * 255.0f + 0.5f) * 255u);
@@ -520,33 +530,33 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
                 if (depth + 1 >= kMaxDepth || (uint32_t)depth >= stack_depth) { atomicOr(err, 4u); break; }
                 uint32_t *lvl = stack + (size_t)depth * kThreads * PX;
                 for (int i = 0; i < PX; i++) lvl[i * kThreads + tid] = layer[i * kThreads + tid];
-                if (tid == 0) sh.rects[depth] = make_int4(top_x, top_y, top_w, top_h);
                 depth++;
                 const LayerRec L = layers[st.layer_off + c.a];
-                top_x = L.x; top_y = L.y; top_w = L.w; top_h = L.h;
                 const uint32_t init = c.b == 1 ? 0xFF000000u : 0u;
-                const bool row_in = cy >= top_y && cy < top_y + top_h;
+                const bool row_in = cy >= L.y && cy < L.y + L.h;
                 const uint32_t *src = (c.b == 2 && L.buf) ? (const uint32_t *)(uintptr_t)L.buf : nullptr;
                 for (int i = 0; i < PX; i++) {
                     const int32_t x = wi.x0 + i * tpr + lr;
                     uint32_t v = 0u;
-                    if (row_in && x >= top_x && x < top_x + top_w)
-                        v = src ? src[(size_t)(cy - top_y) * top_w + (x - top_x)] : init;
+                    if (row_in && x >= L.x && x < L.x + L.w)
+                        v = src ? src[(size_t)(cy - L.y) * L.w + (x - L.x)] : init;
                     layer[i * kThreads + tid] = v;
                 }
+                if (tid == 0) sh.rects[depth] = make_int4(L.x, L.y, L.w, L.h);
+                __syncthreads();
             } else if (c.op == CMD_POP_COMPOSITE || c.op == CMD_POP_CLIP || c.op == CMD_POP_MASK) {
                 if (depth == 0) { atomicOr(err, 4u); break; }
                 __syncthreads();
                 depth--;
                 const uint32_t *lvl = stack + (size_t)depth * kThreads * PX;
-                const int4 p4 = sh.rects[depth];
-                const bool in_child_row = cy >= top_y && cy < top_y + top_h;
+                const int4 p4 = sh.rects[depth], t = sh.rects[depth + 1];
+                const bool in_child_row = cy >= t.y && cy < t.y + t.w;
                 const bool in_parent_row = cy >= p4.y && cy < p4.y + p4.w;
                 for (int i = 0; i < PX; i++) {
                     const int32_t x = wi.x0 + i * tpr + lr;
                     uint32_t parent = lvl[i * kThreads + tid];
                     const uint32_t child = layer[i * kThreads + tid];
-                    const bool in_child = in_child_row && x >= top_x && x < top_x + top_w;
+                    const bool in_child = in_child_row && x >= t.x && x < t.x + t.z;
                     const bool in_parent = in_parent_row && x >= p4.x && x < p4.x + p4.z;
                     if (in_child && in_parent) {
                         if (c.op == CMD_POP_COMPOSITE) parent = dev::composite_pixel(child, parent, c.f, c.b);
@@ -555,12 +565,12 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
                     }
                     layer[i * kThreads + tid] = parent;
                 }
-                top_x = p4.x; top_y = p4.y; top_w = p4.z; top_h = p4.w;
             } else if (c.op == CMD_CLEAR) {
-                const bool row_in = cy >= top_y && cy < top_y + top_h;
+                const int4 t = sh.rects[depth];
+                const bool row_in = cy >= t.y && cy < t.y + t.w;
                 for (int i = 0; i < PX; i++) {
                     const int32_t x = wi.x0 + i * tpr + lr;
-                    if (row_in && x >= top_x && x < top_x + top_w) layer[i * kThreads + tid] = 0u;
+                    if (row_in && x >= t.x && x < t.x + t.z) layer[i * kThreads + tid] = 0u;
                 }
             } else if (c.op == CMD_END) {
                 break;
