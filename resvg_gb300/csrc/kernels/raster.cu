@@ -41,6 +41,7 @@ struct VmShared {
     uint16_t span_cnt[kThreads];
     int2 spans[kThreads * kSpanCap];
     uint16_t run_cnt[kMaxPairs];  // alpha runs per (slot, row), including the closing sentinel
+    int2 run_ext[kMaxPairs];      // [first, last) layer x with non-zero coverage per (slot, row)
     int2 runs[kMaxPairs * kRunCap];
     int4 rects[kMaxDepth];       // layer-stack rects (x, y, w, h) by depth, the top one at [depth]
     WorkItem wi;                 // the work item being rendered, and its stream
@@ -172,7 +173,8 @@ struct RunWriter {
     int2 *sm, *gl;
     uint32_t gcap;
     int n;
-    int32_t alpha;  // alpha from the last stored end onwards
+    int32_t alpha;        // alpha from the last stored end onwards
+    int32_t first, last;  // extent of the non-zero coverage
     __device__ void put(int32_t end, int32_t a, uint32_t *err) {
         if (n < kRunCap) sm[n] = make_int2(end, a);
         else {
@@ -186,13 +188,18 @@ struct RunWriter {
     }
     // coverage changes to `a` at pixel x
     __device__ __forceinline__ void set(int32_t x, int32_t a, uint32_t *err) {
-        if (a != alpha) { put(x, alpha, err); alpha = a; }
+        if (a != alpha) {
+            if (alpha == 0) first = min(first, x);
+            else if (a == 0) last = x;
+            put(x, alpha, err);
+            alpha = a;
+        }
     }
 };
 
 __device__ void merge_runs(VmShared &sh, const int2 *ovf, uint32_t ovf_cap, int2 *rovf, uint32_t rovf_cap, int pair,
                            int sj, bool aa, int32_t lo, int32_t hi, uint32_t *err) {
-    RunWriter w{&sh.runs[pair * kRunCap], rovf + (size_t)pair * rovf_cap, rovf_cap, 0, 0};
+    RunWriter w{&sh.runs[pair * kRunCap], rovf + (size_t)pair * rovf_cap, rovf_cap, 0, 0, INT32_MAX, INT32_MIN};
     if (aa) {
         const int2 *L[4];
         int n[4], q[4];
@@ -240,6 +247,7 @@ __device__ void merge_runs(VmShared &sh, const int2 *ovf, uint32_t ovf_cap, int2
     w.set(hi, 0, err);
     w.put(INT32_MAX, 0, err);
     sh.run_cnt[pair] = (uint16_t)min(w.n, (int)rovf_cap);
+    sh.run_ext[pair] = make_int2(w.first, w.last);
 }
 
 __device__ __forceinline__ const int2 *run_base(const VmShared &sh, const int2 *rovf, uint32_t rovf_cap, int pair) {
@@ -442,6 +450,7 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
                 // and the chunk's spans that meet this work item (hm)
                 const int2 *rp = nullptr;
                 int q = 0;
+                int i_lo = 0, i_hi = PX;  // this thread's pixels that can be covered
                 int hs = 0, hn = 0, hq = -32;
                 uint32_t hm = 0;
                 if (hair) {
@@ -471,6 +480,14 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
                     const int4 geo = sh.slot_geo[slot];
                     ox = geo.y; oy = geo.z;
                     rp = run_base(sh, rovf, rovf_cap, pair);
+                    if (c.op == CMD_FILL) {
+                        // pixel i sits at layer x = x0 - ox + lr + i * tpr
+                        const int2 e = sh.run_ext[pair];
+                        const int32_t b0 = wi.x0 - ox + lr;
+                        const int32_t n0 = e.x - b0, n1 = e.y - b0;
+                        i_lo = n0 <= 0 ? 0 : (n0 + tpr - 1) / tpr;
+                        i_hi = n1 <= 0 ? 0 : min(PX, (n1 + tpr - 1) / tpr);
+                    }
                 }
                 const PaintRec &pr = sh.paint[slot];
                 const GradRec *gr = &sh.grad[slot];  // read only for gradient paints
@@ -498,7 +515,7 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
                         hm &= hm - 1;
                     }
 #pragma unroll 1
-                    for (int i = 0; i < PX; i++) {
+                    for (int i = i_lo; i < i_hi; i++) {
                         const int32_t x = wi.x0 + i * tpr + lr;
                         const int32_t lx = x - ox;
                         uint32_t cv = 0;
