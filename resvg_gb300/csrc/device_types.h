@@ -123,6 +123,7 @@ struct StreamRec {
     uint32_t max_depth;            // layer-stack depth needed
     int32_t surface;               // internal surface rendered into (filter content), or -1
     uint32_t level;                // dependency level: content streams render before their parents
+    uint32_t fill_off, fill_cnt;   // this stream's fill / region commands (indices into its commands)
 };
 
 

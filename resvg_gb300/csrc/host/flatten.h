@@ -54,6 +54,7 @@ struct SceneBuild {
     std::vector<FilterJob> jobs;
     std::vector<HairRec> hairs;       // anti-aliased hairline strokes
     std::vector<HairSpan> hair_spans;
+    std::vector<uint32_t> fill_cmds;  // per stream: its fill / region command indices (plan_scene)
     std::vector<uint8_t> verbs;
     std::vector<float> pts;
     uint64_t nsegs = 0, ntpts = 0;

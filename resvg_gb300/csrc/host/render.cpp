@@ -79,14 +79,14 @@ struct Buffers {
     DevBuf verbs, pts, draws, paints, grads, layers, cmds, streams, items;
     DevBuf tpts, segs, seg_counts, seg_offsets, scan_scratch, totals;
     DevBuf edges, edge_draw, bin_counts, bin_offsets, bins;
-    DevBuf stack, span_ovf, run_ovf, err, counter;
+    DevBuf stack, span_ovf, run_ovf, err, counter, fill_cmds;
     DevBuf hairs, hair_spans;
     std::vector<DevBuf> surf, img;   // internal surfaces (filter content/results) and filter images
     DevBuf plane;                    // f64 plane of the IIR blur
     void release() {
         DevBuf *all[] = {&verbs, &pts, &draws, &paints, &grads, &layers, &cmds, &streams, &items, &tpts, &segs,
                          &seg_counts, &seg_offsets, &scan_scratch, &totals, &edges, &edge_draw, &bin_counts,
-                         &bin_offsets, &bins, &stack, &span_ovf, &run_ovf, &err, &counter, &plane, &hairs, &hair_spans};
+                         &bin_offsets, &bins, &stack, &span_ovf, &run_ovf, &err, &counter, &fill_cmds, &plane, &hairs, &hair_spans};
         for (DevBuf *b : all) {
             if (b->p) cudaFree(b->p);
             b->p = nullptr;
@@ -216,8 +216,16 @@ int plan_scene(Context &c, Plan &p) {
     p.items.clear();
     p.nbins = 0;
     p.max_depth = 1;
+    sb.fill_cmds.clear();
     for (uint32_t si = 0; si < sb.streams.size(); si++) {
         StreamRec &st = sb.streams[si];
+        // the raster kernel's phase-A windows take the stream's fill commands in order
+        st.fill_off = (uint32_t)sb.fill_cmds.size();
+        for (uint32_t ci = 0; ci < st.cmd_cnt; ci++) {
+            const uint32_t op = sb.cmds[st.cmd_off + ci].op;
+            if (op == CMD_FILL || op == CMD_APPLY_REGION) sb.fill_cmds.push_back(ci);
+        }
+        st.fill_cnt = (uint32_t)sb.fill_cmds.size() - st.fill_off;
         uint32_t bh = pick_bh(st.out_w, p.px, c.tuning);
         st.band_rows = bh;
         st.nbands = (uint32_t)((st.out_h + (int32_t)bh - 1) / (int32_t)bh);
@@ -273,7 +281,8 @@ int upload_plan(Context &c, Buffers &b, Plan &p, cudaStream_t s) {
                    rup(sb.paints.size() * sizeof(PaintRec)) + rup(sb.grads.size() * sizeof(GradRec)) +
                    rup(sb.layers.size() * sizeof(LayerRec)) + rup(sb.cmds.size() * sizeof(Cmd)) +
                    rup(sb.streams.size() * sizeof(StreamRec)) + rup(p.items.size() * sizeof(WorkItem)) +
-                   rup(sb.hairs.size() * sizeof(HairRec)) + rup(sb.hair_spans.size() * sizeof(HairSpan)) + 4096;
+                   rup(sb.hairs.size() * sizeof(HairRec)) + rup(sb.hair_spans.size() * sizeof(HairSpan)) +
+                   rup(sb.fill_cmds.size() * 4) + 4096;
     CK(c.staging.ensure(stage));
     size_t off = 0;
     int r;
@@ -288,6 +297,7 @@ int upload_plan(Context &c, Buffers &b, Plan &p, cudaStream_t s) {
     if ((r = upload(c, b.items, p.items, off, s))) return r;
     if ((r = upload(c, b.hairs, sb.hairs, off, s))) return r;
     if ((r = upload(c, b.hair_spans, sb.hair_spans, off, s))) return r;
+    if ((r = upload(c, b.fill_cmds, sb.fill_cmds, off, s))) return r;
     // fixed-size work buffers
     uint64_t nsegs = sb.nsegs;
     CK(b.tpts.ensure(std::max<uint64_t>(sb.ntpts, 1) * 8));
@@ -364,7 +374,7 @@ int enqueue_plan(Context &c, Buffers &b, Plan &p, cudaStream_t s, cudaEvent_t ev
         if (p.level_cnt[lv])
             CK(launch_raster((int)p.px, p.grid, p.max_depth, b.streams.as<StreamRec>(),
                              b.items.as<WorkItem>() + p.level_off[lv], p.level_cnt[lv], b.counter.as<uint32_t>() + lv,
-                             b.cmds.as<Cmd>(), b.draws.as<DrawRec>(), b.paints.as<PaintRec>(), b.grads.as<GradRec>(),
+                             b.cmds.as<Cmd>(), b.fill_cmds.as<uint32_t>(), b.draws.as<DrawRec>(), b.paints.as<PaintRec>(), b.grads.as<GradRec>(),
                              b.layers.as<LayerRec>(), b.bins.as<EdgeRec>(), b.bin_offsets.as<uint32_t>(),
                              b.bin_counts.as<uint32_t>(), b.stack.as<uint32_t>(), b.span_ovf.as<int2>(), kSpanOvf,
                              b.run_ovf.as<int2>(), p.run_cap, b.hairs.as<HairRec>(), b.hair_spans.as<HairSpan>(), b.err.as<uint32_t>(), s));

@@ -28,7 +28,7 @@ size_t raster_smem_bytes();
 size_t raster_stack_words_per_cta(int px);
 int raster_threads();
 cudaError_t launch_raster(int px, uint32_t grid, uint32_t stack_depth, const StreamRec *streams, const WorkItem *items, uint32_t nitems,
-                          uint32_t *item_counter, const Cmd *cmds, const DrawRec *draws, const PaintRec *paints,
+                          uint32_t *item_counter, const Cmd *cmds, const uint32_t *fill_cmds, const DrawRec *draws, const PaintRec *paints,
                           const GradRec *grads, const LayerRec *layers, const EdgeRec *bins,
                           const uint32_t *bin_offsets, const uint32_t *bin_counts, uint32_t *stack, int2 *span_ovf,
                           uint32_t ovf_cap, int2 *run_ovf, uint32_t run_ovf_cap, const HairRec *hairs, const HairSpan *hair_spans, uint32_t *err,

@@ -34,10 +34,6 @@ constexpr int kMaxPairs = kThreads / 4;  // (slot, row) pairs per window: K x BH
 constexpr int kRunCap = 32;     // alpha runs per (slot, row) kept in shared memory
 
 struct VmShared {
-    int32_t win_first;           // first command index of the prepared window
-    int32_t win_last;            // one past the last command index covered by the window
-    int32_t nslots;
-    int32_t slot_cmd[kMaxSlots]; // command index per slot
     uint16_t span_cnt[kThreads];
     int2 spans[kThreads * kSpanCap];
     uint16_t run_cnt[kMaxPairs];  // alpha runs per (slot, row), including the closing sentinel
@@ -47,9 +43,7 @@ struct VmShared {
     WorkItem wi;                 // the work item being rendered, and its stream
     StreamRec st;
     PaintRec paint[kMaxSlots + 1];   // paints of the window's draws; the last: the current hairline's
-    int4 slot_geo[kMaxSlots];    // (valid | shift << 1, ox, oy, unused) per slot
-    int4 slot_sect[kMaxSlots];   // coverage rect (l, t, r, b) per slot
-    int32_t grad_slot[kMaxSlots];// index into grad[] or -1
+    int4 slot_geo[kMaxSlots];    // (unused, ox, oy, unused) per slot
     GradRec grad[kMaxSlots + 1];     // gradients of the window's draws (and the hairline's)
     int32_t item;
     // followed by the top layer: kThreads * px uint32 pixels (dynamic)
@@ -302,7 +296,7 @@ __device__ __forceinline__ uint32_t hair_cov(const HairSpan *hsp, int32_t px, in
 
 __global__ void __launch_bounds__(kThreads, 3)
 k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitems, uint32_t *item_counter,
-         const Cmd *cmds, const DrawRec *draws, const PaintRec *paints, const GradRec *grads, const LayerRec *layers,
+         const Cmd *cmds, const uint32_t *fill_cmds, const DrawRec *draws, const PaintRec *paints, const GradRec *grads, const LayerRec *layers,
          const EdgeRec *bins, const uint32_t *bin_offsets, const uint32_t *bin_counts, uint32_t *stack_scratch,
          uint32_t stack_depth, int2 *span_ovf, uint32_t ovf_cap, int2 *run_ovf, uint32_t rovf_cap, const HairRec *hairs,
          const HairSpan *hair_spans, uint32_t *err) {
@@ -347,75 +341,43 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
                 (row_ok && x < wi.x1) ? *(const uint32_t *)(out + (size_t)cy * st.out_stride + 4 * (size_t)x) : 0u;
         }
         int32_t depth = 0;
-        if (tid == 0) { sh.win_first = 0; sh.win_last = 0; sh.nslots = 0; }
-        __syncthreads();
-        int32_t slot_next = 0;
+        int32_t slot_next = 0, win_last = 0;
+        uint32_t fill_seen = 0;  // fill commands of the stream before the current one
 
         for (uint32_t ci = 0; ci < st.cmd_cnt; ci++) {
             const Cmd c = cmds[st.cmd_off + ci];
             if (c.op == CMD_FILL || c.op == CMD_APPLY_REGION || c.op == CMD_HAIR) {
-                if ((int32_t)ci >= sh.win_last && c.op != CMD_HAIR) {
-                    // ---- prepare a phase-A window over the next K fill commands
-                    __syncthreads();
-                    if (tid < 32) {
-                        // warp 0 finds the next K fill commands with a ballot scan
-                        int ns = 0;
-                        uint32_t cj = ci;
-                        uint32_t end = st.cmd_cnt;
-                        while (cj < st.cmd_cnt && ns < K) {
-                            uint32_t idx = cj + (uint32_t)tid;
-                            bool isfill = false;
-                            if (idx < st.cmd_cnt) {
-                                uint32_t op = cmds[st.cmd_off + idx].op;
-                                isfill = op == CMD_FILL || op == CMD_APPLY_REGION;
-                            }
-                            uint32_t m = __ballot_sync(0xffffffffu, isfill);
-                            int slot = ns + __popc(m & ((1u << tid) - 1u));
-                            if (isfill && slot < K) sh.slot_cmd[slot] = (int32_t)idx;
-                            int tot = __popc(m);
-                            if (ns + tot >= K) {
-                                // the window ends after the K-th fill command
-                                uint32_t mk = __ballot_sync(0xffffffffu, isfill && slot == K - 1);
-                                uint32_t last = __shfl_sync(0xffffffffu, idx, __ffs(mk) - 1);
-                                end = last + 1;
-                                ns = K;
-                                break;
-                            }
-                            ns += tot;
-                            cj += 32;
-                        }
-                        if (tid == 0) {
-                            sh.win_first = (int32_t)ci;
-                            sh.win_last = (int32_t)min(end, st.cmd_cnt);
-                            sh.nslots = ns;
-                        }
-                    }
-                    __syncthreads();
-                    if (tid < sh.nslots) {
-                        const DrawRec &d = draws[cmds[st.cmd_off + sh.slot_cmd[tid]].a];
-                        const PaintRec &pr = paints[d.paint];
-                        sh.paint[tid] = pr;
-                        sh.grad_slot[tid] = pr.kind == 1 ? tid : -1;
-                        sh.slot_geo[tid] = make_int4((d.valid ? 1 : 0) | (d.shift ? 2 : 0), d.ox, d.oy, 0);
-                        sh.slot_sect[tid] = make_int4(d.sect_l, d.sect_t, d.sect_r, d.sect_b);
-                    }
-                    __syncthreads();
-                    // stage the window's gradients cooperatively
-                    {
-                        const int words = (int)(sizeof(GradRec) / 4);
-                        const int total = sh.nslots * words;
-                        for (int w = tid; w < total; w += kThreads) {
-                            const int k = w / words, o = w - k * words;
-                            if (sh.grad_slot[k] >= 0)
-                                ((uint32_t *)&sh.grad[k])[o] = ((const uint32_t *)&grads[sh.paint[k].grad])[o];
+                if (c.op != CMD_HAIR && (int32_t)ci >= win_last) {
+                    // ---- a phase-A window over the next K fill commands of the stream's
+                    // fill list (fill_seen of them come before this one)
+                    const uint32_t nsl = min((uint32_t)K, st.fill_cnt - fill_seen);
+                    const uint32_t *flist = fill_cmds + st.fill_off + fill_seen;
+                    win_last = (int32_t)flist[nsl - 1] + 1;
+                    __syncthreads();  // the previous window's readers are done
+                    // stage paints, draw geometry and gradients: warp w takes the slots
+                    // w, w + 8, ...
+                    const int warp = tid >> 5, lane = tid & 31;
+                    for (uint32_t k = (uint32_t)warp; k < nsl; k += kThreads / 32) {
+                        const uint32_t di = cmds[st.cmd_off + flist[k]].a;
+                        const uint32_t pi = draws[di].paint;
+                        if (lane < (int)(sizeof(PaintRec) / 4))
+                            ((uint32_t *)&sh.paint[k])[lane] = ((const uint32_t *)&paints[pi])[lane];
+                        if (lane == 0) sh.slot_geo[k] = make_int4(0, draws[di].ox, draws[di].oy, 0);
+                        if (paints[pi].kind == 1) {
+                            const uint32_t *src = (const uint32_t *)&grads[paints[pi].grad];
+                            for (int w = lane; w < (int)(sizeof(GradRec) / 4); w += 32) ((uint32_t *)&sh.grad[k])[w] = src[w];
                         }
                     }
                     slot_next = 0;
+                    // phase A: thread (k, j) walks sub-scanline j of slot k; then lane
+                    // 4r of each slot merges row r (its 4 sub-scanlines sit in the same
+                    // warp: S divides 32)
                     const int k = tid / S, j = tid % S;
-                    if (k < sh.nslots) {
-                        const Cmd fc = cmds[st.cmd_off + sh.slot_cmd[k]];
-                        const DrawRec dr = draws[fc.a];
-                        const uint32_t ld = fc.a - st.draw_off;
+                    DrawRec dr;
+                    if (k < (int)nsl) {
+                        const uint32_t di = cmds[st.cmd_off + flist[k]].a;
+                        dr = draws[di];
+                        const uint32_t ld = di - st.draw_off;
                         const uint32_t slot = st.bin_off + wi.band * st.draw_cnt + ld;
                         const int32_t lrow0 = (int32_t)wi.band * BH - dr.oy;
                         int32_t y;
@@ -425,17 +387,15 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
                         if (ok && dr.valid) phase_a(sh, tid, dr, y, bins + bin_offsets[slot], bin_counts[slot], ovf, ovf_cap, err);
                         else sh.span_cnt[tid] = 0;
                     }
-                    __syncthreads();
-                    // ---- merge each (slot, row)'s sub-scanline spans into alpha runs
-                    if (tid < sh.nslots * BH) {
-                        const int k2 = tid / BH, r2 = tid % BH;
-                        const int4 geo = sh.slot_geo[k2];
-                        const int4 sect = sh.slot_sect[k2];
-                        const int32_t ly = (int32_t)wi.band * BH + r2 - geo.z;
-                        int32_t lo = max(sect.x, wi.x0 - geo.y), hi = min(sect.z, wi.x1 - geo.y);
-                        if (!(geo.x & 1) || ly < sect.y || ly >= sect.w || (int32_t)wi.band * BH + r2 >= st.out_h) hi = lo;
-                        const bool aa2 = geo.x & 2;
-                        merge_runs(sh, ovf, ovf_cap, rovf, rovf_cap, tid, k2 * S + r2 * (aa2 ? 4 : 1), aa2, lo, hi, err);
+                    __syncwarp();
+                    if (k < (int)nsl && (j & 3) == 0) {
+                        const int r2 = j >> 2;
+                        const int32_t ly = (int32_t)wi.band * BH + r2 - dr.oy;
+                        int32_t lo = max(dr.sect_l, wi.x0 - dr.ox), hi = min(dr.sect_r, wi.x1 - dr.ox);
+                        if (!dr.valid || ly < dr.sect_t || ly >= dr.sect_b || (int32_t)wi.band * BH + r2 >= st.out_h) hi = lo;
+                        if (r2 < BH)
+                            merge_runs(sh, ovf, ovf_cap, rovf, rovf_cap, k * BH + r2, k * S + (dr.shift ? j : r2),
+                                       dr.shift != 0, lo, hi, err);
                     }
                     __syncthreads();
                 }
@@ -473,6 +433,7 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
                     hs = (int)hr.span_off;
                     hn = (int)hr.span_cnt;
                 } else {
+                    fill_seen++;
                     slot = slot_next++;
                     const int pair = slot * BH + row;
                     // one entry: the closing sentinel alone, nothing covered on this row
@@ -615,12 +576,12 @@ cudaError_t raster_init() {
 }
 
 cudaError_t launch_raster(int px, uint32_t grid, uint32_t stack_depth, const StreamRec *streams, const WorkItem *items,
-                          uint32_t nitems, uint32_t *item_counter, const Cmd *cmds, const DrawRec *draws,
+                          uint32_t nitems, uint32_t *item_counter, const Cmd *cmds, const uint32_t *fill_cmds, const DrawRec *draws,
                           const PaintRec *paints, const GradRec *grads, const LayerRec *layers, const EdgeRec *bins,
                           const uint32_t *bin_offsets, const uint32_t *bin_counts, uint32_t *stack, int2 *span_ovf,
                           uint32_t ovf_cap, int2 *run_ovf, uint32_t run_ovf_cap, const HairRec *hairs, const HairSpan *hair_spans, uint32_t *err,
                           cudaStream_t s) {
-    k_raster<<<grid, kThreads, raster_smem_bytes_px(px), s>>>(px, streams, items, nitems, item_counter, cmds, draws, paints,
+    k_raster<<<grid, kThreads, raster_smem_bytes_px(px), s>>>(px, streams, items, nitems, item_counter, cmds, fill_cmds, draws, paints,
                                                               grads, layers, bins, bin_offsets, bin_counts, stack,
                                                               stack_depth, span_ovf, ovf_cap, run_ovf, run_ovf_cap, hairs,
                                                               hair_spans, err);
