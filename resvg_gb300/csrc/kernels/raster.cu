@@ -27,18 +27,20 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kXCap = 40;        // crossings held per thread before the exact slow path
 constexpr int kSpanCap = 8;      // spans per (slot, sub-scanline) kept in shared memory
+constexpr int kSpanStride = kSpanCap + 1;  // padded: neighbouring lists start in different banks
 constexpr int kMaxDepth = 48;    // layer stack depth
 
 constexpr int kMaxSlots = 32;   // draws per phase-A window
 constexpr int kMaxPairs = kThreads / 4;  // (slot, row) pairs per window: K x BH <= kThreads / 4
 constexpr int kRunCap = 32;     // alpha runs per (slot, row) kept in shared memory
+constexpr int kRunStride = kRunCap + 1;
 
 struct VmShared {
     uint16_t span_cnt[kThreads];
-    int2 spans[kThreads * kSpanCap];
+    int2 spans[kThreads * kSpanStride];
     uint16_t run_cnt[kMaxPairs];  // alpha runs per (slot, row), including the closing sentinel
     int2 run_ext[kMaxPairs];      // [first, last) layer x with non-zero coverage per (slot, row)
-    int2 runs[kMaxPairs * kRunCap];
+    int2 runs[kMaxPairs * kRunStride];
     int4 rects[kMaxDepth];       // layer-stack rects (x, y, w, h) by depth, the top one at [depth]
     WorkItem wi;                 // the work item being rendered, and its stream
     StreamRec st;
@@ -61,17 +63,17 @@ __device__ void store_span(VmShared &sh, int2 *ovf, uint32_t ovf_cap, int slot_j
                            uint32_t *err) {
     int2 *o = ovf + (size_t)slot_j * ovf_cap;
     if (idx < kSpanCap) {
-        sh.spans[slot_j * kSpanCap + idx] = make_int2(L, R);
+        sh.spans[slot_j * kSpanStride + idx] = make_int2(L, R);
         return;
     }
     if (idx == kSpanCap)
-        for (int k = 0; k < kSpanCap; k++) o[k] = sh.spans[slot_j * kSpanCap + k];
+        for (int k = 0; k < kSpanCap; k++) o[k] = sh.spans[slot_j * kSpanStride + k];
     if ((uint32_t)idx < ovf_cap) o[idx] = make_int2(L, R);
     else atomicOr(err, 2u);
 }
 __device__ __forceinline__ const int2 *span_base(const VmShared &sh, const int2 *ovf, uint32_t ovf_cap, int slot_j,
                                                  int n) {
-    return n <= kSpanCap ? &sh.spans[slot_j * kSpanCap] : ovf + (size_t)slot_j * ovf_cap;
+    return n <= kSpanCap ? &sh.spans[slot_j * kSpanStride] : ovf + (size_t)slot_j * ovf_cap;
 }
 
 // Phase A for one (draw, scanline): spans into slot `sj`.  
@@ -84,8 +86,10 @@ __device__ void phase_a(VmShared &sh, int sj, const DrawRec &dr, int32_t y, cons
     Crossing xs[kXCap];
     int n = 0;
     bool overflow = false;
+    EdgeRec en = bl[0];  // the next edge, loaded one iteration ahead
     for (uint32_t i = 0; i < nb; i++) {
-        EdgeRec e = bl[i];
+        const EdgeRec e = en;
+        if (i + 1 < nb) en = bl[i + 1];
         int32_t h = e.hw >> 8;
         if (y < e.first_y || y > e.first_y + h) continue;
         int32_t X = (int32_t)((uint32_t)e.x + (uint32_t)(y - e.first_y) * (uint32_t)e.dx);
@@ -193,7 +197,7 @@ struct RunWriter {
 
 __device__ void merge_runs(VmShared &sh, const int2 *ovf, uint32_t ovf_cap, int2 *rovf, uint32_t rovf_cap, int pair,
                            int sj, bool aa, int32_t lo, int32_t hi, uint32_t *err) {
-    RunWriter w{&sh.runs[pair * kRunCap], rovf + (size_t)pair * rovf_cap, rovf_cap, 0, 0, INT32_MAX, INT32_MIN};
+    RunWriter w{&sh.runs[pair * kRunStride], rovf + (size_t)pair * rovf_cap, rovf_cap, 0, 0, INT32_MAX, INT32_MIN};
     if (aa) {
         const int2 *L[4];
         int n[4], q[4];
@@ -245,7 +249,7 @@ __device__ void merge_runs(VmShared &sh, const int2 *ovf, uint32_t ovf_cap, int2
 }
 
 __device__ __forceinline__ const int2 *run_base(const VmShared &sh, const int2 *rovf, uint32_t rovf_cap, int pair) {
-    return sh.run_cnt[pair] <= kRunCap ? &sh.runs[pair * kRunCap] : rovf + (size_t)pair * rovf_cap;
+    return sh.run_cnt[pair] <= kRunCap ? &sh.runs[pair * kRunStride] : rovf + (size_t)pair * rovf_cap;
 }
 
 // Coverage of layer pixel (px, py) from one hairline span (tiny-skia
