@@ -10,6 +10,7 @@
 //   crates/resvg/src/filter/box_blur.rs       box blur (5 box passes, V then H)
 //   crates/resvg/src/filter/iir_blur.rs       IIR blur (f64)
 //   crates/resvg/src/filter/color_matrix.rs, morphology.rs, composite.rs, convolve_matrix.rs
+//   crates/resvg/src/filter/lighting.rs        diffuse / specular lighting, mod.rs:1020-1098 drivers
 // The two sRGB <-> linearRGB tables are resvg's (mod.rs:161-238): both are
 // the standard transfer functions evaluated and rounded to u8 (a data table
 // has to be identical to give identical output).
@@ -367,6 +368,155 @@ void convolve(const rgpu_primitive &p, Pixmap &src) {
     src.data = buf;
 }
 
+// ---- diffuse / specular lighting (lighting.rs; light source mapping mod.rs:1062-1098)
+struct V3 { float x, y, z; };
+inline float dot3(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline float len3(V3 a) { return std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
+inline V3 normalized_or_self(V3 v) {
+    float l = len3(v);
+    if (approx_zero_ulps(l)) return v;
+    return V3{v.x / l, v.y / l, v.z / l};
+}
+bool approx_eq_ulps_f(float a, float b) {
+    int32_t ia, ib;
+    std::memcpy(&ia, &a, 4);
+    std::memcpy(&ib, &b, 4);
+    if ((ia < 0) != (ib < 0)) return a == b;
+    return std::abs(ia - ib) <= 4;
+}
+inline float deg_to_rad(float d) { return d * (3.14159265358979323846f / 180.0f); }
+
+// Sobel-style surface normal of the alpha channel at (x, y) with the border
+// variants of lighting.rs:296-476: (factor x, factor y, nx, ny).
+void surface_normal(const Pixmap &img, uint32_t x, uint32_t y, float *fx, float *fy, int *nx, int *ny) {
+    const uint32_t w = img.width, h = img.height;
+    auto a = [&](uint32_t xx, uint32_t yy) -> int { return img.px(xx, yy)[3]; };
+    const bool l = x == 0, r = x == w - 1, t = y == 0, b = y == h - 1;
+    if (t && l) {
+        int c = a(0, 0), rt = a(1, 0), bt = a(0, 1), br = a(1, 1);
+        *fx = *fy = 2.0f / 3.0f;
+        *nx = -2 * c + 2 * rt - bt + br; *ny = -2 * c - rt + 2 * bt + br;
+    } else if (t && r) {
+        int lf = a(w - 2, 0), c = a(w - 1, 0), bl = a(w - 2, 1), bt = a(w - 1, 1);
+        *fx = *fy = 2.0f / 3.0f;
+        *nx = -2 * lf + 2 * c - bl + bt; *ny = -lf - 2 * c + bl + 2 * bt;
+    } else if (b && l) {
+        int tp = a(0, h - 2), tr = a(1, h - 2), c = a(0, h - 1), rt = a(1, h - 1);
+        *fx = *fy = 2.0f / 3.0f;
+        *nx = -tp + tr - 2 * c + 2 * rt; *ny = -2 * tp - tr + 2 * c + rt;
+    } else if (b && r) {
+        int tl = a(w - 2, h - 2), tp = a(w - 1, h - 2), lf = a(w - 2, h - 1), c = a(w - 1, h - 1);
+        *fx = *fy = 2.0f / 3.0f;
+        *nx = -tl + tp - 2 * lf + 2 * c; *ny = -tl - 2 * tp + lf + 2 * c;
+    } else if (t) {
+        int lf = a(x - 1, 0), c = a(x, 0), rt = a(x + 1, 0), bl = a(x - 1, 1), bt = a(x, 1), br = a(x + 1, 1);
+        *fx = 1.0f / 3.0f; *fy = 1.0f / 2.0f;
+        *nx = -2 * lf + 2 * rt - bl + br; *ny = -lf - 2 * c - rt + bl + 2 * bt + br;
+    } else if (b) {
+        int tl = a(x - 1, h - 2), tp = a(x, h - 2), tr = a(x + 1, h - 2), lf = a(x - 1, h - 1), c = a(x, h - 1),
+            rt = a(x + 1, h - 1);
+        *fx = 1.0f / 3.0f; *fy = 1.0f / 2.0f;
+        *nx = -tl + tr - 2 * lf + 2 * rt; *ny = -tl - 2 * tp - tr + lf + 2 * c + rt;
+    } else if (l) {
+        int tp = a(0, y - 1), tr = a(1, y - 1), c = a(0, y), rt = a(1, y), bt = a(0, y + 1), br = a(1, y + 1);
+        *fx = 1.0f / 2.0f; *fy = 1.0f / 3.0f;
+        *nx = -tp + tr - 2 * c + 2 * rt - bt + br; *ny = -2 * tp - tr + 2 * bt + br;
+    } else if (r) {
+        int tl = a(w - 2, y - 1), tp = a(w - 1, y - 1), lf = a(w - 2, y), c = a(w - 1, y), bl = a(w - 2, y + 1),
+            bt = a(w - 1, y + 1);
+        *fx = 1.0f / 2.0f; *fy = 1.0f / 3.0f;
+        *nx = -tl + tp - 2 * lf + 2 * c - bl + bt; *ny = -tl - 2 * tp + bl + 2 * bt;
+    } else {
+        int tl = a(x - 1, y - 1), tp = a(x, y - 1), tr = a(x + 1, y - 1), lf = a(x - 1, y), rt = a(x + 1, y),
+            bl = a(x - 1, y + 1), bt = a(x, y + 1), br = a(x + 1, y + 1);
+        *fx = *fy = 1.0f / 4.0f;
+        *nx = -tl + tr - 2 * lf + 2 * rt - bl + br; *ny = -tl - 2 * tp - tr + bl + 2 * bt + br;
+    }
+}
+
+void lighting(bool specular, const rgpu_primitive &p, const Transform &ts, const IntRect &region, const Pixmap &src,
+              Pixmap &dst) {
+    const uint32_t w = src.width, h = src.height;
+    if (w < 3 || h < 3) return;
+    const float ss = p.f[0], kc = p.f[1], sexp = p.f[2];
+    const int kind = p.i[0];
+    const uint8_t lc[3] = {(uint8_t)p.i[1], (uint8_t)p.i[2], (uint8_t)p.i[3]};
+    // the light source in the region's pixel space (transform_light_source)
+    float lx = p.f[4], ly = p.f[5], lz = p.f[6], ax = p.f[7], ay = p.f[8], az = p.f[9];
+    if (kind != RGPU_LIGHT_DISTANT) {
+        const float sz = std::sqrt(ts.sx * ts.sx + ts.sy * ts.sy) / 1.41421356237309504880f;
+        Point q{lx, ly};
+        ts.map_points(&q, 1);
+        lx = q.x - (float)region.x; ly = q.y - (float)region.y; lz = lz * sz;
+        if (kind == RGPU_LIGHT_SPOT) {
+            Point q2{ax, ay};
+            ts.map_points(&q2, 1);
+            ax = q2.x - (float)region.x; ay = q2.y - (float)region.y; az = az * sz;
+        }
+    }
+    V3 lv{1.0f, 1.0f, 1.0f};
+    if (kind == RGPU_LIGHT_DISTANT) {
+        const float azi = deg_to_rad(p.f[4]), ele = deg_to_rad(p.f[5]);
+        lv = V3{std::cos(azi) * std::cos(ele), std::sin(azi) * std::cos(ele), std::sin(ele)};
+    }
+    for (uint32_t y = 0; y < h; y++)
+        for (uint32_t x = 0; x < w; x++) {
+            if (kind != RGPU_LIGHT_DISTANT) {
+                const float nz = (float)src.px(x, y)[3] / 255.0f * ss;
+                lv = normalized_or_self(V3{lx - (float)x, ly - (float)y, lz - nz});
+            }
+            // light colour (light_color)
+            uint8_t col[3] = {lc[0], lc[1], lc[2]};
+            if (kind == RGPU_LIGHT_SPOT) {
+                V3 d = normalized_or_self(V3{ax - lx, ay - ly, az - lz});
+                const float mls = -dot3(lv, d);
+                bool black = mls <= 0.0f;
+                if (!black && !std::isnan(p.f[11]) && mls < std::cos(deg_to_rad(p.f[11]))) black = true;
+                if (black) col[0] = col[1] = col[2] = 0;
+                else {
+                    const float fac = std::pow(mls, p.f[10]);
+                    for (int k = 0; k < 3; k++) col[k] = (uint8_t)(f32_bound(0.0f, (float)lc[k] * fac, 255.0f) + 0.5f);
+                }
+            }
+            float fx, fy;
+            int inx, iny;
+            surface_normal(src, x, y, &fx, &fy, &inx, &iny);
+            const float nxv = (float)(int16_t)(-inx), nyv = (float)(int16_t)(-iny);
+            const bool flat = approx_zero_ulps(nxv) && approx_zero_ulps(nyv);
+            float factor;
+            if (!specular) {
+                float k;
+                if (flat) k = lv.z;
+                else {
+                    const float sc = ss / 255.0f;
+                    V3 n{nxv * sc * fx, nyv * sc * fy, 1.0f};
+                    k = dot3(n, lv) / len3(n);
+                }
+                factor = kc * k;
+            } else {
+                V3 hv{lv.x + 0.0f, lv.y + 0.0f, lv.z + 1.0f};
+                const float hl = len3(hv);
+                if (approx_zero_ulps(hl)) factor = 0.0f;
+                else {
+                    float ndh;
+                    if (flat) ndh = hv.z / hl;
+                    else {
+                        const float sc = ss / 255.0f;
+                        V3 n{nxv * sc * fx, nyv * sc * fy, 1.0f};
+                        ndh = dot3(n, hv) / len3(n) / hl;
+                    }
+                    const float k = approx_eq_ulps_f(sexp, 1.0f) ? ndh : std::pow(ndh, sexp);
+                    factor = kc * k;
+                }
+            }
+            uint8_t o[3];
+            for (int k = 0; k < 3; k++) o[k] = (uint8_t)(f32_bound(0.0f, (float)col[k] * factor, 255.0f) + 0.5f);
+            uint8_t *d = &dst.data[((size_t)y * w + x) * 4];
+            d[0] = o[0]; d[1] = o[1]; d[2] = o[2];
+            d[3] = specular ? std::max(std::max(o[0], o[1]), o[2]) : 255;
+        }
+}
+
 bool int_rect_eq(const IntRect &a, const IntRect &b) { return a.x == b.x && a.y == b.y && a.w == b.w && a.h == b.h; }
 
 struct Result { Image image; };
@@ -461,6 +611,14 @@ bool filter_apply(const rgpu_tree_view &t, const rgpu_filter &f, const Transform
             auto pm = std::make_shared<Pixmap>(*c.image);
             if (p.i[5]) demultiply_alpha(pm->data);
             convolve(p, *pm);
+            res = Image{pm, IntRect{0, 0, (int32_t)pm->width, (int32_t)pm->height}, lin};
+            break;
+        }
+        case RGPU_FE_DIFFUSE:
+        case RGPU_FE_SPECULAR: {
+            Image in = get_input(p.in1);
+            auto pm = std::make_shared<Pixmap>((uint32_t)region.w, (uint32_t)region.h);
+            lighting(p.kind == RGPU_FE_SPECULAR, p, ts, region, *in.image, *pm);
             res = Image{pm, IntRect{0, 0, (int32_t)pm->width, (int32_t)pm->height}, lin};
             break;
         }

@@ -208,6 +208,69 @@ int run_filter_job(const FilterJob &job, uint32_t *content, uint32_t *result, Fi
                 res = Img{o, in.linear};
                 break;
             }
+            case RGPU_FE_CONVOLVE: {
+                // apply_convolve_matrix (mod.rs:919-933)
+                Img in = r.in_space(input(p.in1), lin);
+                ConvolveParams cp{};
+                cp.cols = p.i[0]; cp.rows = p.i[1]; cp.tx = p.i[2]; cp.ty = p.i[3];
+                cp.edge = p.i[4]; cp.preserve_alpha = p.i[5];
+                cp.divisor = p.f[0]; cp.bias = p.f[1];
+                if (cp.cols <= 0 || cp.rows <= 0 || cp.cols * cp.rows > (int)(sizeof(cp.k) / sizeof(float))) {
+                    err = "convolve kernel larger than the primitive record";
+                    return RGPU_ERR_UNSUPPORTED;
+                }
+                for (int k = 0; k < cp.cols * cp.rows; k++) cp.k[k] = p.f[2 + k];
+                uint32_t *o = r.fresh();
+                r.ck(filter_convolve(in.p, o, r.w, r.h, cp, s));
+                res = Img{o, lin};
+                break;
+            }
+            case RGPU_FE_DIFFUSE:
+            case RGPU_FE_SPECULAR: {
+                // apply_diffuse_lighting / apply_specular_lighting + transform_light_source
+                // (mod.rs:1020-1098); the region is the whole layer here
+                Img in = input(p.in1);
+                LightingParams lp{};
+                lp.specular = p.kind == RGPU_FE_SPECULAR;
+                lp.kind = p.i[0];
+                lp.surface_scale = p.f[0];
+                lp.constant = p.f[1];
+                lp.exponent = p.f[2];
+                for (int k = 0; k < 3; k++) lp.color[k] = (uint32_t)(uint8_t)p.i[1 + k];
+                const float d2r = 3.14159265358979323846f / 180.0f;
+                if (lp.kind == RGPU_LIGHT_DISTANT) {
+                    const float az = p.f[4] * d2r, el = p.f[5] * d2r;
+                    lp.lv[0] = std::cos(az) * std::cos(el);
+                    lp.lv[1] = std::sin(az) * std::cos(el);
+                    lp.lv[2] = std::sin(el);
+                } else {
+                    lp.lv[0] = lp.lv[1] = lp.lv[2] = 1.0f;
+                    const float sz = std::sqrt(job.ts.sx * job.ts.sx + job.ts.sy * job.ts.sy) / 1.41421356237309504880f;
+                    float lx = p.f[4], ly = p.f[5];
+                    map_point(job.ts, lx, ly);
+                    lp.pos[0] = lx - (float)region.x;
+                    lp.pos[1] = ly - (float)region.y;
+                    lp.pos[2] = p.f[6] * sz;
+                    if (lp.kind == RGPU_LIGHT_SPOT) {
+                        float ax = p.f[7], ay = p.f[8];
+                        map_point(job.ts, ax, ay);
+                        ax -= (float)region.x;
+                        ay -= (float)region.y;
+                        const float az = p.f[9] * sz;
+                        float dx = ax - lp.pos[0], dy = ay - lp.pos[1], dz = az - lp.pos[2];
+                        const float len = std::sqrt(dx * dx + dy * dy + dz * dz);
+                        if (!approx_zero_ulps(len)) { dx = dx / len; dy = dy / len; dz = dz / len; }
+                        lp.dir[0] = dx; lp.dir[1] = dy; lp.dir[2] = dz;
+                        lp.spot_exponent = p.f[10];
+                        lp.has_cone = !std::isnan(p.f[11]);
+                        lp.cone_cos = lp.has_cone ? std::cos(p.f[11] * d2r) : 0.0f;
+                    }
+                }
+                uint32_t *o = r.fresh();
+                r.ck(filter_lighting(in.p, o, r.w, r.h, lp, s));
+                res = Img{o, lin};
+                break;
+            }
             default:
                 err = "filter primitive not supported on the device";
                 return RGPU_ERR_UNSUPPORTED;

@@ -62,6 +62,15 @@ inline bool invert(const Xf &t, Xf *out) {
     return true;
 }
 
+// One point mapped by t (tiny-skia Transform::map_point).
+inline void map_point(const Xf &t, float &x, float &y) {
+    if (t.identity()) return;
+    if (!t.skew() && !t.has_scale()) { x += t.tx; y += t.ty; return; }
+    if (!t.skew()) { x = x * t.sx + t.tx; y = y * t.sy + t.ty; return; }
+    const float nx = x * t.sx + y * t.kx + t.tx, ny = x * t.ky + y * t.sy + t.ty;
+    x = nx; y = ny;
+}
+
 // Bounds of a rect mapped by t (4 corners, as NonZeroRect::transform).
 inline bool map_rect(const Xf &t, float l, float tp, float r, float b, float out[4]) {
     float xs[4] = {l, r, r, l}, ys[4] = {tp, tp, b, b};

@@ -9,6 +9,9 @@
 //   morphology     filter/morphology.rs (min/max over the window; the window is a
 //                  rectangle, so it is applied as a row pass then a column pass)
 //   arithmetic     filter/composite.rs
+//   convolve       filter/convolve_matrix.rs (f32 sums in kernel order)
+//   lighting       filter/lighting.rs (Sobel normals with the border variants,
+//                  N.L / (N.H)^e per pixel; powf is CUDA's, within 1/255)
 // All memory-bound: each pass streams its input once and writes once; the
 // sliding-window passes re-read a window edge from L1/L2.
 #include <cuda_runtime.h>
@@ -420,4 +423,156 @@ cudaError_t filter_alpha_only(uint32_t *img, size_t n, cudaStream_t s) {
     k_alpha_only<<<nblk(n, 256), 256, 0, s>>>(img, n);
     return cudaGetLastError();
 }
+namespace {
+
+__global__ void k_convolve(const uint32_t *src, uint32_t *dst, int w, int h, ConvolveParams cp) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+    if (x >= w || y >= h) return;
+    const bool pres = cp.preserve_alpha != 0;
+    float nr = 0.0f, ng = 0.0f, nb = 0.0f, na = 0.0f;
+    for (int oy = 0; oy < cp.rows; oy++)
+        for (int ox = 0; ox < cp.cols; ox++) {
+            int tx = x - cp.tx + ox, ty = y - cp.ty + oy;
+            if (cp.edge == RGPU_EDGE_NONE) {
+                if (tx < 0 || tx >= w || ty < 0 || ty >= h) continue;
+            } else if (cp.edge == RGPU_EDGE_DUPLICATE) {
+                tx = min(max(tx, 0), w - 1);
+                ty = min(max(ty, 0), h - 1);
+            } else {
+                tx = ((tx % w) + w) % w;
+                ty = ((ty % h) + h) % h;
+            }
+            const float kv = cp.k[(cp.rows - oy - 1) * cp.cols + (cp.cols - ox - 1)];
+            uint32_t p = src[(size_t)ty * w + tx];
+            if (pres) p = demul(p);
+            nr += __fdiv_rn((float)chn(p, 0), 255.0f) * kv;
+            ng += __fdiv_rn((float)chn(p, 1), 255.0f) * kv;
+            nb += __fdiv_rn((float)chn(p, 2), 255.0f) * kv;
+            if (!pres) na += __fdiv_rn((float)chn(p, 3), 255.0f) * kv;
+        }
+    if (pres) na = __fdiv_rn((float)chn(src[(size_t)y * w + x], 3), 255.0f);
+    else na = __fdiv_rn(na, cp.divisor) + cp.bias;
+    const float bna = f32_bound(0.0f, na, 1.0f);
+    auto calc = [&](float v) {
+        float q = __fdiv_rn(v, cp.divisor) + cp.bias * na;
+        q = pres ? f32_bound(0.0f, q, 1.0f) * bna : f32_bound(0.0f, q, bna);
+        return sat_u8f(q * 255.0f + 0.5f);
+    };
+    dst[(size_t)y * w + x] = pk(calc(nr), calc(ng), calc(nb), sat_u8f(bna * 255.0f + 0.5f));
+}
+
+// ApproxEqUlps(4) of two f32s, as in float-cmp
+__device__ __forceinline__ bool ulps_eq4(float a, float b) {
+    const int32_t ia = __float_as_int(a), ib = __float_as_int(b);
+    if ((ia < 0) != (ib < 0)) return a == b;
+    return abs(ia - ib) <= 4;
+}
+
+__global__ void k_lighting(const uint32_t *src, uint32_t *dst, int w, int h, LightingParams lp) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+    if (x >= w || y >= h) return;
+    auto A = [&](int xx, int yy) -> int { return (int)chn(src[(size_t)yy * w + xx], 3); };
+    // surface normal: interior Sobel, or the edge / corner variant
+    const bool l = x == 0, r = x == w - 1, t = y == 0, b = y == h - 1;
+    float fx, fy;
+    int nx, ny;
+    if ((l || r) && (t || b)) {
+        // corners: the 2x2 neighbourhood towards the inside
+        const int xi = l ? 1 : w - 2, yi = t ? 1 : h - 2;
+        const int sxn = l ? 1 : -1, syn = t ? 1 : -1;  // direction of the inner neighbour
+        const int c = A(x, y), hx = A(xi, y), vy = A(x, yi), d = A(xi, yi);
+        fx = fy = 2.0f / 3.0f;
+        // d/dx ~ (2 (right - left) + (lower-right - lower-left)) in the 2x2 block
+        nx = sxn * (2 * hx - 2 * c + d - vy);
+        ny = syn * (2 * vy - 2 * c + d - hx);
+    } else if (t || b) {
+        const int yi = t ? 1 : h - 2, syn = t ? 1 : -1;
+        const int lf = A(x - 1, y), c = A(x, y), rt = A(x + 1, y);
+        const int il = A(x - 1, yi), ic = A(x, yi), ir = A(x + 1, yi);
+        fx = 1.0f / 3.0f; fy = 1.0f / 2.0f;
+        nx = -2 * lf + 2 * rt - il + ir;
+        ny = syn * (-lf - 2 * c - rt + il + 2 * ic + ir);
+    } else if (l || r) {
+        const int xi = l ? 1 : w - 2, sxn = l ? 1 : -1;
+        const int tp = A(x, y - 1), c = A(x, y), bt = A(x, y + 1);
+        const int it = A(xi, y - 1), ic = A(xi, y), ib = A(xi, y + 1);
+        fx = 1.0f / 2.0f; fy = 1.0f / 3.0f;
+        nx = sxn * (-tp + it - 2 * c + 2 * ic - bt + ib);
+        ny = -2 * tp - it + 2 * bt + ib;
+    } else {
+        const int tl = A(x - 1, y - 1), tp = A(x, y - 1), tr = A(x + 1, y - 1), lf = A(x - 1, y), rt = A(x + 1, y),
+                  bl = A(x - 1, y + 1), bt = A(x, y + 1), br = A(x + 1, y + 1);
+        fx = fy = 1.0f / 4.0f;
+        nx = -tl + tr - 2 * lf + 2 * rt - bl + br;
+        ny = -tl - 2 * tp - tr + bl + 2 * bt + br;
+    }
+    float lx = lp.lv[0], ly = lp.lv[1], lz = lp.lv[2];
+    if (lp.kind != RGPU_LIGHT_DISTANT) {
+        const float nz = __fdiv_rn((float)A(x, y), 255.0f) * lp.surface_scale;
+        const float vx = lp.pos[0] - (float)x, vy = lp.pos[1] - (float)y, vz = lp.pos[2] - nz;
+        const float len = __fsqrt_rn(vx * vx + vy * vy + vz * vz);
+        if (ulps_eq4(len, 0.0f)) { lx = vx; ly = vy; lz = vz; }
+        else { lx = __fdiv_rn(vx, len); ly = __fdiv_rn(vy, len); lz = __fdiv_rn(vz, len); }
+    }
+    uint32_t col[3] = {lp.color[0], lp.color[1], lp.color[2]};
+    if (lp.kind == RGPU_LIGHT_SPOT) {
+        const float mls = -(lx * lp.dir[0] + ly * lp.dir[1] + lz * lp.dir[2]);
+        if (mls <= 0.0f || (lp.has_cone && mls < lp.cone_cos)) {
+            col[0] = col[1] = col[2] = 0;
+        } else {
+            const float fac = powf(mls, lp.spot_exponent);
+#pragma unroll
+            for (int k = 0; k < 3; k++) col[k] = (uint32_t)(uint8_t)(f32_bound(0.0f, (float)lp.color[k] * fac, 255.0f) + 0.5f);
+        }
+    }
+    const float nxv = (float)(int16_t)(-nx), nyv = (float)(int16_t)(-ny);
+    const bool flat = ulps_eq4(nxv, 0.0f) && ulps_eq4(nyv, 0.0f);
+    const float sc = __fdiv_rn(lp.surface_scale, 255.0f);
+    float factor;
+    if (!lp.specular) {
+        float k;
+        if (flat) k = lz;
+        else {
+            const float mx = nxv * sc * fx, my = nyv * sc * fy;
+            k = __fdiv_rn(mx * lx + my * ly + 1.0f * lz, __fsqrt_rn(mx * mx + my * my + 1.0f * 1.0f));
+        }
+        factor = lp.constant * k;
+    } else {
+        const float hx = lx + 0.0f, hy = ly + 0.0f, hz = lz + 1.0f;
+        const float hl = __fsqrt_rn(hx * hx + hy * hy + hz * hz);
+        if (ulps_eq4(hl, 0.0f)) factor = 0.0f;
+        else {
+            float ndh;
+            if (flat) ndh = __fdiv_rn(hz, hl);
+            else {
+                const float mx = nxv * sc * fx, my = nyv * sc * fy;
+                ndh = __fdiv_rn(__fdiv_rn(mx * hx + my * hy + 1.0f * hz, __fsqrt_rn(mx * mx + my * my + 1.0f * 1.0f)), hl);
+            }
+            const float k = ulps_eq4(lp.exponent, 1.0f) ? ndh : powf(ndh, lp.exponent);
+            factor = lp.constant * k;
+        }
+    }
+    uint32_t o[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) o[k] = (uint32_t)(uint8_t)(f32_bound(0.0f, (float)col[k] * factor, 255.0f) + 0.5f);
+    const uint32_t a = lp.specular ? max(max(o[0], o[1]), o[2]) : 255u;
+    dst[(size_t)y * w + x] = pk(o[0], o[1], o[2], a);
+}
+
+}  // namespace
+
+cudaError_t filter_convolve(const uint32_t *src, uint32_t *dst, int w, int h, const ConvolveParams &cp,
+                            cudaStream_t s) {
+    if (w <= 0 || h <= 0) return cudaSuccess;
+    k_convolve<<<dim3((unsigned)((w + 127) / 128), (unsigned)h), 128, 0, s>>>(src, dst, w, h, cp);
+    return cudaGetLastError();
+}
+
+cudaError_t filter_lighting(const uint32_t *src, uint32_t *dst, int w, int h, const LightingParams &lp,
+                            cudaStream_t s) {
+    if (w < 3 || h < 3) return cudaMemsetAsync(dst, 0, (size_t)(w > 0 ? w : 0) * (h > 0 ? h : 0) * 4, s);
+    k_lighting<<<dim3((unsigned)((w + 127) / 128), (unsigned)h), 128, 0, s>>>(src, dst, w, h, lp);
+    return cudaGetLastError();
+}
+
 }  // namespace rgpu

@@ -53,4 +53,31 @@ cudaError_t filter_draw(const uint32_t *src, uint32_t *dst, int w, int h, int dx
 cudaError_t filter_fill(uint32_t *img, size_t n, uint32_t v, cudaStream_t s);
 cudaError_t filter_alpha_only(uint32_t *img, size_t n, cudaStream_t s);
 
+// feConvolveMatrix (convolve_matrix.rs): kernel k[rows * cols] row-major as
+// given, applied flipped; edge = rgpu_edge_mode.
+struct ConvolveParams {
+    int32_t cols, rows, tx, ty, edge, preserve_alpha;
+    float divisor, bias;
+    float k[62];
+};
+cudaError_t filter_convolve(const uint32_t *src, uint32_t *dst, int w, int h, const ConvolveParams &cp,
+                            cudaStream_t s);
+
+// feDiffuseLighting / feSpecularLighting (lighting.rs) with the light source
+// already in the region's pixel space; the distant light vector, the spot
+// direction and the cosine of the cone angle are prepared on the host.
+struct LightingParams {
+    int32_t specular, kind;          // kind: rgpu_light_kind
+    float surface_scale, constant, exponent;
+    uint32_t color[3];               // lighting colour, u8 per channel
+    float lv[3];                     // distant: unit light vector
+    float pos[3];                    // point / spot: position
+    float dir[3];                    // spot: direction (normalised where possible)
+    float spot_exponent;
+    int32_t has_cone;
+    float cone_cos;
+};
+cudaError_t filter_lighting(const uint32_t *src, uint32_t *dst, int w, int h, const LightingParams &lp,
+                            cudaStream_t s);
+
 }  // namespace rgpu

@@ -90,11 +90,56 @@ def parse_color(s: str, current=(0, 0, 0)):
         if len(parts) > 3:
             a = float(parts[3][:-1]) / 100 if parts[3].endswith("%") else float(parts[3])
         return tuple(vals), max(0.0, min(1.0, a))
+    m = re.match(r"hsla?\(([^)]*)\)", low)
+    if m:
+        # CSS Color 3 hsl(): hue in degrees, saturation and lightness in
+        # [0, 1], each channel rounded to u8 (f32 arithmetic)
+        parts = [p.strip() for p in re.split(r"[,\s/]+", m.group(1).strip()) if p.strip()]
+        if len(parts) < 3:
+            raise Unsupported("color " + s)
+
+        def frac(v):
+            return float(v[:-1]) / 100 if v.endswith("%") else float(v)
+        hue = (float(parts[0]) % 360.0 + 360.0) % 360.0
+        sat, lig = F(max(0.0, min(1.0, frac(parts[1])))), F(max(0.0, min(1.0, frac(parts[2]))))
+        h6 = F(F(hue) / F(60.0))
+        t2 = F(lig * F(sat + F(1.0))) if lig <= 0.5 else F(F(lig + sat) - F(lig * sat))
+        t1 = F(F(lig * F(2.0)) - t2)
+
+        def channel(hh):
+            hh = F(hh)
+            if hh < 0:
+                hh = F(hh + F(6.0))
+            if hh >= 6:
+                hh = F(hh - F(6.0))
+            if hh < 1:
+                v = F(F(F(t2 - t1) * hh) + t1)
+            elif hh < 3:
+                v = t2
+            elif hh < 4:
+                v = F(F(F(t2 - t1) * F(F(4.0) - hh)) + t1)
+            else:
+                v = t1
+            x = F(v * F(255.0))
+            return int(np.floor(x + 0.5)) if x >= 0 else -int(np.floor(-x + 0.5))
+        rgb = tuple(max(0, min(255, channel(h6 + d))) for d in (F(2.0), F(0.0), F(-2.0)))
+        a = 1.0
+        if len(parts) > 3:
+            a = frac(parts[3])
+        return rgb, max(0.0, min(1.0, a))
     raise Unsupported("color " + s)
 
 
 # ---------------------------------------------------------------- numbers, lengths, transforms
 NUM = r"[-+]?(?:\d+\.?\d*|\.\d+)(?:[eE][-+]?\d+)?"
+
+
+def _approx_zero_ulps(v):
+    """usvg's approx_zero_ulps(4) for an f32."""
+    a = int(np.array([v], dtype=np.float32).view(np.int32)[0])
+    if a < 0:
+        return float(v) == 0.0
+    return a <= 4
 
 
 def numbers(s):
@@ -497,7 +542,7 @@ NON_INHERITED = {"opacity", "clip-path", "mask", "filter", "mix-blend-mode", "is
                  "stop-color", "stop-opacity", "flood-color", "flood-opacity", "transform"}
 UNSUPPORTED_ELEMS = {"text", "image", "pattern", "marker", "switch", "foreignObject", "tspan", "textPath", "symbol",
                      "feImage", "feTile", "feTurbulence", "feDisplacementMap", "feComponentTransfer",
-                     "feDropShadow", "feDiffuseLighting", "feSpecularLighting", "feConvolveMatrix", "feFuncR",
+                     "feDropShadow", "feFuncR",
                      "style", "animate", "set"}
 BLEND = {"normal": "source-over", "multiply": "multiply", "screen": "screen", "overlay": "overlay",
          "darken": "darken", "lighten": "lighten", "color-dodge": "color-dodge", "color-burn": "color-burn",
@@ -1171,6 +1216,104 @@ class Builder(Loader):
         return self.tree.add_mask(m)
 
     # ---- filters
+    def convolve(self, c, p):
+        """feConvolveMatrix as usvg converts it (parser/filter.rs:648-714);
+        False where usvg substitutes a transparent flood."""
+        ox, oy = 3, 3
+        if c.get("order") is not None:
+            v = numbers(c.get("order"))
+            x = int(v[0]) if v else 3
+            y = int(v[1]) if len(v) > 1 else x
+            if x > 0 and y > 0:
+                ox, oy = x, y
+        m = [F(v) for v in numbers(c.get("kernelMatrix"))] if c.get("kernelMatrix") is not None else []
+        if len(m) != ox * oy:
+            m = []
+        ksum = F(0)
+        for v in m:
+            ksum = F(ksum + v)
+        r = F(ksum * F(1000000.0))
+        r = F(np.sign(r) * np.floor(np.abs(r) + F(0.5))) if np.isfinite(r) else r
+        ksum = F(r / F(1000000.0))
+        if _approx_zero_ulps(ksum):
+            ksum = F(1.0)
+        divisor = F(float(c.get("divisor"))) if c.get("divisor") is not None else ksum
+        if _approx_zero_ulps(divisor):
+            return False
+        bias = F(float(c.get("bias"))) if c.get("bias") is not None else F(0.0)
+
+        def target(name, order):
+            t = c.get(name)
+            t = int(float(t)) if t is not None else int(np.floor(F(order) / F(2.0)))
+            return t if 0 <= t < order else None
+        tx, ty = target("targetX", ox), target("targetY", oy)
+        if tx is None or ty is None or not m:
+            return False
+        if len(m) > len(p.f) - 2:
+            raise Unsupported("convolve kernel larger than the primitive record")
+        p.kind = A.FE_CONVOLVE
+        edge = (c.get("edgeMode") or "duplicate").strip()
+        p.i[0], p.i[1], p.i[2], p.i[3] = ox, oy, tx, ty
+        p.i[4] = {"none": A.EDGE_NONE, "wrap": A.EDGE_WRAP}.get(edge, A.EDGE_DUPLICATE)
+        p.i[5] = 1 if (c.get("preserveAlpha") or "false").strip() == "true" else 0
+        p.f[0], p.f[1] = divisor, bias
+        for k, v in enumerate(m):
+            p.f[2 + k] = v
+        return True
+
+    def lighting(self, c, p, specular):
+        """feDiffuseLighting / feSpecularLighting with their light source
+        (parser/filter.rs:882-981); False where usvg substitutes a transparent flood."""
+        light = None
+        for n in c:
+            if _tag(n) in ("feDistantLight", "fePointLight", "feSpotLight"):
+                light = n
+                break
+        if light is None:
+            return False
+
+        def fa(e, name, default):
+            v = e.get(name)
+            return F(float(v)) if v is not None else F(default)
+        if specular:
+            se = fa(c, "specularExponent", 1.0)
+            if not (1.0 <= se <= 128.0):
+                return False
+            p.kind = A.FE_SPECULAR
+            p.f[0], p.f[1], p.f[2] = fa(c, "surfaceScale", 1.0), fa(c, "specularConstant", 1.0), se
+        else:
+            p.kind = A.FE_DIFFUSE
+            p.f[0], p.f[1] = fa(c, "surfaceScale", 1.0), fa(c, "diffuseConstant", 1.0)
+        lc = self.get(c, "lighting-color", inherited=False)
+        col = (255, 255, 255)
+        if lc is not None:
+            if lc.strip().lower() == "currentcolor":
+                cur = self.get(c, "color")
+                pc = parse_color(cur) if cur is not None else None
+                col = pc[0] if pc else (0, 0, 0)
+            else:
+                try:
+                    pc = parse_color(lc)
+                    col = pc[0] if pc else (255, 255, 255)
+                except Exception:
+                    col = (255, 255, 255)
+        p.i[1], p.i[2], p.i[3] = col
+        lt = _tag(light)
+        if lt == "feDistantLight":
+            p.i[0] = A.LIGHT_DISTANT
+            p.f[4], p.f[5] = fa(light, "azimuth", 0.0), fa(light, "elevation", 0.0)
+        elif lt == "fePointLight":
+            p.i[0] = A.LIGHT_POINT
+            p.f[4], p.f[5], p.f[6] = fa(light, "x", 0.0), fa(light, "y", 0.0), fa(light, "z", 0.0)
+        else:
+            p.i[0] = A.LIGHT_SPOT
+            p.f[4], p.f[5], p.f[6] = fa(light, "x", 0.0), fa(light, "y", 0.0), fa(light, "z", 0.0)
+            p.f[7], p.f[8], p.f[9] = fa(light, "pointsAtX", 0.0), fa(light, "pointsAtY", 0.0), fa(light, "pointsAtZ", 0.0)
+            sx = fa(light, "specularExponent", 1.0)
+            p.f[10] = sx if sx >= 0.0 else F(1.0)
+            p.f[11] = fa(light, "limitingConeAngle", np.nan)
+        return True
+
     def filter(self, fe, bbox):
         if _tag(fe) != "filter":
             return None
@@ -1226,6 +1369,12 @@ class Builder(Loader):
                     raise Unsupported("input " + v)
                 return len(prims) - 1 if prims else A.IN_SOURCE_GRAPHIC
             p.in1 = inp("in")
+
+            def dummy(q):
+                # usvg's stand-in for an invalid primitive: a transparent black flood
+                q.kind = A.FE_FLOOD
+                q.i[0] = q.i[1] = q.i[2] = 0
+                q.f[0] = 0.0
             if tag == "feGaussianBlur":
                 sd = numbers(c.get("stdDeviation", "0"))
                 sdx, sdy = (sd[0], sd[1]) if len(sd) > 1 else ((sd[0], sd[0]) if sd else (0.0, 0.0))
@@ -1299,6 +1448,12 @@ class Builder(Loader):
                 p.kind = A.FE_BLEND
                 p.in2 = inp("in2")
                 p.i[0] = A.BLEND[BLEND.get((c.get("mode") or "normal").strip(), "source-over")]
+            elif tag == "feConvolveMatrix":
+                if not self.convolve(c, p):
+                    dummy(p)
+            elif tag in ("feDiffuseLighting", "feSpecularLighting"):
+                if not self.lighting(c, p, tag == "feSpecularLighting"):
+                    dummy(p)
             else:
                 raise Unsupported("filter primitive " + tag)
             res = c.get("result")

@@ -45,6 +45,8 @@ CATEGORIES = [
     "structure/transform", "structure/style", "structure/svg",
     "filters/feGaussianBlur", "filters/feColorMatrix", "filters/feMorphology", "filters/feComposite",
     "filters/feFlood", "filters/feOffset", "filters/feMerge", "filters/feBlend", "filters/filter",
+    "filters/feConvolveMatrix", "filters/feDiffuseLighting", "filters/feSpecularLighting",
+    "filters/feDistantLight", "filters/fePointLight", "filters/feSpotLight",
     "filters/filter-functions",
 ]
 IMAGE_SIZE = 300
