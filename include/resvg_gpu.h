@@ -151,6 +151,8 @@ typedef struct rgpu_stats {
 int rgpu_get_stats(rgpu_stats *s);
 
 /* ---- filter kernels on device images (filter module primitives) --------- */
+/* With stream == NULL the call runs on the library's stream and returns when
+ * the image is done; with a stream it is enqueued there and returns at once. */
 /* Box blur, 5 passes of (vertical, horizontal) box sums: crates/resvg/src/filter/box_blur.rs:23. */
 int rgpu_filter_box_blur(uint8_t *device_img, uint32_t width, uint32_t height, double sigma_x, double sigma_y,
                          void *stream);

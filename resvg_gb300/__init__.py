@@ -377,26 +377,29 @@ class Scene:
             self._h = None
 
 
-def _dev_filter(name, tensor, *args):
-    """Runs a filter kernel in place on a CUDA uint8 tensor of shape (h, w, 4)."""
+def _dev_filter(name, tensor, *args, stream=None):
+    """Runs a filter kernel in place on a CUDA uint8 tensor of shape (h, w, 4):
+    synchronously on the library's stream, or enqueued on `stream` (a CUDA
+    stream handle) and returning at once."""
     assert tensor.is_cuda and tensor.dtype.itemsize == 1 and tensor.dim() == 3 and tensor.shape[2] == 4
     assert tensor.is_contiguous()
     h, w = tensor.shape[0], tensor.shape[1]
-    check(getattr(lib(), name)(C.c_void_p(tensor.data_ptr()), w, h, *args, None), name)
+    check(getattr(lib(), name)(C.c_void_p(tensor.data_ptr()), w, h, *args, C.c_void_p(stream) if stream else None),
+          name)
     return tensor
 
 
-def box_blur(tensor, sx, sy):
-    return _dev_filter("rgpu_filter_box_blur", tensor, C.c_double(sx), C.c_double(sy))
+def box_blur(tensor, sx, sy, stream=None):
+    return _dev_filter("rgpu_filter_box_blur", tensor, C.c_double(sx), C.c_double(sy), stream=stream)
 
 
-def iir_blur(tensor, sx, sy):
-    return _dev_filter("rgpu_filter_iir_blur", tensor, C.c_double(sx), C.c_double(sy))
+def iir_blur(tensor, sx, sy, stream=None):
+    return _dev_filter("rgpu_filter_iir_blur", tensor, C.c_double(sx), C.c_double(sy), stream=stream)
 
 
-def morphology(tensor, dilate, rx, ry):
-    return _dev_filter("rgpu_filter_morphology", tensor, int(dilate), C.c_float(rx), C.c_float(ry))
+def morphology(tensor, dilate, rx, ry, stream=None):
+    return _dev_filter("rgpu_filter_morphology", tensor, int(dilate), C.c_float(rx), C.c_float(ry), stream=stream)
 
 
-def color_space(tensor, to_linear):
-    return _dev_filter("rgpu_filter_color_space", tensor, int(to_linear))
+def color_space(tensor, to_linear, stream=None):
+    return _dev_filter("rgpu_filter_color_space", tensor, int(to_linear), stream=stream)

@@ -123,7 +123,7 @@ int run_filter_job(const FilterJob &job, uint32_t *content, uint32_t *result, Fi
                 bool box = x >= 2.0f || y >= 2.0f;
                 res = r.private_in(in, lin);
                 if (box) r.ck(filter_box_blur(res.p, r.fresh(), r.w, r.h, x, y, s));
-                else r.ck(filter_iir_blur(res.p, scratch.plane(r.n), r.w, r.h, x, y, s));
+                else r.ck(filter_iir_blur(res.p, scratch.plane(4 * r.n), r.w, r.h, x, y, s));
                 break;
             }
             case RGPU_FE_COLOR_MATRIX: {

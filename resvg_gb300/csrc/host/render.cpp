@@ -843,7 +843,7 @@ int rgpu_filter_box_blur(uint8_t *img, uint32_t w, uint32_t h, double sx, double
     cudaStream_t s = stream ? (cudaStream_t)stream : c.stream;
     CK(g_ftmp.ensure((size_t)w * h * 4));
     CK(filter_box_blur((uint32_t *)img, g_ftmp.as<uint32_t>(), (int)w, (int)h, sx, sy, s));
-    CK(cudaStreamSynchronize(s));
+    if (!stream) CK(cudaStreamSynchronize(s));  // a caller stream: asynchronous
     return RGPU_OK;
 }
 
@@ -855,9 +855,9 @@ int rgpu_filter_iir_blur(uint8_t *img, uint32_t w, uint32_t h, double sx, double
     int r = ensure_device(c);
     if (r) return r;
     cudaStream_t s = stream ? (cudaStream_t)stream : c.stream;
-    CK(g_fplane.ensure((size_t)w * h * 8));
+    CK(g_fplane.ensure((size_t)w * h * 8 * 4));  // four f64 planes
     CK(filter_iir_blur((uint32_t *)img, g_fplane.as<double>(), (int)w, (int)h, sx, sy, s));
-    CK(cudaStreamSynchronize(s));
+    if (!stream) CK(cudaStreamSynchronize(s));  // a caller stream: asynchronous
     return RGPU_OK;
 }
 
@@ -871,7 +871,7 @@ int rgpu_filter_morphology(uint8_t *img, uint32_t w, uint32_t h, int dilate, flo
     cudaStream_t s = stream ? (cudaStream_t)stream : c.stream;
     CK(g_ftmp.ensure((size_t)w * h * 4));
     CK(filter_morphology((uint32_t *)img, g_ftmp.as<uint32_t>(), (int)w, (int)h, dilate != 0, rx, ry, s));
-    CK(cudaStreamSynchronize(s));
+    if (!stream) CK(cudaStreamSynchronize(s));  // a caller stream: asynchronous
     return RGPU_OK;
 }
 
@@ -884,7 +884,7 @@ int rgpu_filter_color_space(uint8_t *img, uint32_t w, uint32_t h, int to_linear,
     if (r) return r;
     cudaStream_t s = stream ? (cudaStream_t)stream : c.stream;
     CK(filter_color_space((uint32_t *)img, (size_t)w * h, to_linear != 0, s));
-    CK(cudaStreamSynchronize(s));
+    if (!stream) CK(cudaStreamSynchronize(s));  // a caller stream: asynchronous
     return RGPU_OK;
 }
 

@@ -21,8 +21,8 @@
 namespace rgpu {
 namespace {
 
-__constant__ uint8_t c_srgb_to_linear[256];
-__constant__ uint8_t c_linear_to_srgb[256];
+__constant__ __align__(16) uint8_t c_srgb_to_linear[256];
+__constant__ __align__(16) uint8_t c_linear_to_srgb[256];
 
 // The two resvg tables (filter/mod.rs:161-238): the sRGB transfer functions
 // evaluated and rounded to u8.
@@ -85,13 +85,39 @@ __device__ __forceinline__ uint32_t mul(uint32_t p) {
               sat_u8f((float)chn(p, 2) * a + 0.5f), chn(p, 3));
 }
 
+// Exact per-(alpha, channel) tables, built once on the host with the same f32
+// operations as demul / mul: demultiply, multiply, and the two colour-space
+// conversions (demultiply -> transfer table -> multiply) in one lookup.
+enum { TAB_DEMUL = 0, TAB_MUL = 1, TAB_TO_LINEAR = 2, TAB_TO_SRGB = 3 };
+__device__ uint8_t g_tab[4][256 * 256];
+__device__ __forceinline__ uint32_t tab(int t, uint32_t a, uint32_t c) { return __ldg(&g_tab[t][(a << 8) | c]); }
+__device__ __forceinline__ uint32_t tab_px(int t, uint32_t p) {
+    const uint32_t a = p >> 24;
+    return tab(t, a, p & 0xFFu) | (tab(t, a, (p >> 8) & 0xFFu) << 8) | (tab(t, a, (p >> 16) & 0xFFu) << 16) | (a << 24);
+}
+
+// Elementwise kernels take four pixels per thread: one 16-byte access when the
+// group is whole and the image 16-byte aligned, else pixel by pixel.
+__device__ __forceinline__ bool vec4(const void *p, size_t i, size_t n) {
+    return i + 4 <= n && (reinterpret_cast<uintptr_t>(p) & 15) == 0;
+}
+#define RGPU_MAP4(img, n, F)                                                         \
+    do {                                                                             \
+        const size_t i_ = 4 * ((size_t)blockIdx.x * blockDim.x + threadIdx.x);      \
+        if (i_ >= (n)) return;                                                       \
+        if (vec4((img), i_, (n))) {                                                  \
+            uint4 v_ = *reinterpret_cast<const uint4 *>((img) + i_);                 \
+            v_.x = F(v_.x); v_.y = F(v_.y); v_.z = F(v_.z); v_.w = F(v_.w);          \
+            *reinterpret_cast<uint4 *>((img) + i_) = v_;                             \
+        } else {                                                                     \
+            for (size_t k_ = i_; k_ < (n) && k_ < i_ + 4; k_++) (img)[k_] = F((img)[k_]); \
+        }                                                                            \
+    } while (0)
+
 __global__ void k_color_space(uint32_t *img, size_t n, int to_linear) {
-    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    uint32_t p = demul(img[i]);
-    const uint8_t *lut = to_linear ? c_srgb_to_linear : c_linear_to_srgb;
-    p = pk(lut[chn(p, 0)], lut[chn(p, 1)], lut[chn(p, 2)], chn(p, 3));
-    img[i] = mul(p);
+    const int t = to_linear ? TAB_TO_LINEAR : TAB_TO_SRGB;
+    auto g = [t](uint32_t p) { return tab_px(t, p); };
+    RGPU_MAP4(img, n, g);
 }
 
 // One box pass along lines: line l, element k at base + l*lstride + k*stride.
@@ -124,50 +150,80 @@ __global__ void k_box_pass(const uint32_t *src, uint32_t *dst, int len, int line
                                    sat_u8f(rintf(__fmul_rn((float)v2, iarr))), sat_u8f(rintf(__fmul_rn((float)v3, iarr))));
     }
 }
-__global__ void k_copy(const uint32_t *src, uint32_t *dst, size_t n) {
-    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) dst[i] = src[i];
-}
 
-// ---- IIR (iir_blur.rs): one channel at a time in an f64 plane
-__global__ void k_iir_load(const uint32_t *img, double *buf, size_t n, int ch) {
-    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) buf[i] = __ddiv_rn((double)chn(img[i], ch), 255.0);
-}
-__global__ void k_iir_rows(double *buf, int w, int h, double dnu, int steps) {
-    int y = blockIdx.x * blockDim.x + threadIdx.x;
-    if (y >= h) return;
-    double *row = buf + (size_t)y * w;
-    for (int s = 0; s < steps; s++) {
-        for (int x = 1; x < w; x++) row[x] = __dadd_rn(row[x], __dmul_rn(dnu, row[x - 1]));
-        for (int x = w - 1; x > 0; x--) row[x - 1] = __dadd_rn(row[x - 1], __dmul_rn(dnu, row[x]));
-    }
-}
-__global__ void k_iir_cols(double *buf, int w, int h, double dnu, int steps) {
-    int x = blockIdx.x * blockDim.x + threadIdx.x;
-    if (x >= w) return;
-    for (int s = 0; s < steps; s++) {
-        for (int y = 1; y < h; y++)
-            buf[(size_t)y * w + x] = __dadd_rn(buf[(size_t)y * w + x], __dmul_rn(dnu, buf[(size_t)(y - 1) * w + x]));
-        for (int y = h - 1; y > 0; y--)
-            buf[(size_t)(y - 1) * w + x] = __dadd_rn(buf[(size_t)(y - 1) * w + x], __dmul_rn(dnu, buf[(size_t)y * w + x]));
-    }
-}
-__global__ void k_iir_store(uint32_t *img, const double *buf, size_t n, int ch, double post) {
-    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+// ---- IIR (iir_blur.rs): four f64 planes (one per channel), each row and each
+// column a first-order recursion run forwards then backwards `steps` times in
+// exactly the reference's operation order.  A thread owns one (line, channel)
+// and moves the line through registers kIirChunk values at a time, so loads
+// and stores stay off the dependency chain.
+constexpr int kIirChunk = 16;
+__global__ void k_iir_load4(const uint32_t *img, double *planes, size_t n) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    uint32_t v = sat_u8d(__dmul_rn(__dmul_rn(buf[i], post), 255.0));
-    uint32_t p = img[i] & ~(0xffu << (8 * ch));
-    img[i] = p | (v << (8 * ch));
+    const uint32_t p = img[i];
+#pragma unroll
+    for (int ch = 0; ch < 4; ch++) planes[(size_t)ch * n + i] = __ddiv_rn((double)chn(p, ch), 255.0);
+}
+// one line of `len` values at base[k * step]; the next chunk is loaded
+// before the current one is computed, so memory latency overlaps the chain
+__device__ __forceinline__ void iir_load_chunk(const double *base, size_t step, int k0, int dir, int m,
+                                               double (&v)[kIirChunk]) {
+#pragma unroll
+    for (int j = 0; j < kIirChunk; j++)
+        if (j < m) v[j] = base[(ptrdiff_t)(k0 + dir * j) * (ptrdiff_t)step];
+}
+__device__ __forceinline__ void iir_line(double *base, size_t step, int len, double dnu, int steps) {
+    for (int s = 0; s < steps; s++) {
+        // forwards over k = 1 .. len-1: v[k] += dnu * v[k - 1]; backwards over
+        // k = len-2 .. 0: v[k] += dnu * v[k + 1]
+        for (int dir = 1; dir >= -1; dir -= 2) {
+            const int first = dir > 0 ? 1 : len - 2, count = len - 1;
+            double carry = base[(ptrdiff_t)(first - dir) * (ptrdiff_t)step];
+            double cur[kIirChunk], nxt[kIirChunk];
+            int m = min(kIirChunk, count);
+            if (m > 0) iir_load_chunk(base, step, first, dir, m, cur);
+            for (int done = 0; done < count; done += kIirChunk) {
+                const int mn = min(kIirChunk, count - done - kIirChunk);
+                if (mn > 0) iir_load_chunk(base, step, first + dir * (done + kIirChunk), dir, mn, nxt);
+#pragma unroll
+                for (int j = 0; j < kIirChunk; j++)
+                    if (j < m) { carry = __dadd_rn(cur[j], __dmul_rn(dnu, carry)); cur[j] = carry; }
+#pragma unroll
+                for (int j = 0; j < kIirChunk; j++)
+                    if (j < m) base[(ptrdiff_t)(first + dir * (done + j)) * (ptrdiff_t)step] = cur[j];
+#pragma unroll
+                for (int j = 0; j < kIirChunk; j++) cur[j] = nxt[j];
+                m = mn;
+            }
+        }
+    }
+}
+__global__ void k_iir_rows4(double *planes, int w, int h, double dnu, int steps) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 4 * h) return;
+    const int ch = t / h, y = t - ch * h;
+    iir_line(planes + (size_t)ch * w * h + (size_t)y * w, 1, w, dnu, steps);
+}
+__global__ void k_iir_cols4(double *planes, int w, int h, double dnu, int steps) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 4 * w) return;
+    const int ch = t / w, x = t - ch * w;  // consecutive threads: consecutive columns
+    iir_line(planes + (size_t)ch * w * h + x, (size_t)w, h, dnu, steps);
+}
+__global__ void k_iir_store4(uint32_t *img, const double *planes, size_t n, double post) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t o = 0;
+#pragma unroll
+    for (int ch = 0; ch < 4; ch++) o |= sat_u8d(__dmul_rn(__dmul_rn(planes[(size_t)ch * n + i], post), 255.0)) << (8 * ch);
+    img[i] = o;
 }
 
 // ---- colour matrix (color_matrix.rs), demultiply and multiply fused
 struct CmParams { int kind; float m[20]; };
 __device__ __forceinline__ uint32_t from_normalized(float c) { return sat_u8f(f32_bound(0.0f, c, 1.0f) * 255.0f); }
-__global__ void k_color_matrix(uint32_t *img, size_t n, CmParams cp) {
-    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    uint32_t p = demul(img[i]);
+__device__ __forceinline__ uint32_t color_matrix_px(uint32_t px, const CmParams &cp) {
+    uint32_t p = tab_px(TAB_DEMUL, px);
     float r = (float)chn(p, 0) / 255.0f, g = (float)chn(p, 1) / 255.0f, b = (float)chn(p, 2) / 255.0f,
           a = (float)chn(p, 3) / 255.0f;
     const float *m = cp.m;
@@ -185,7 +241,11 @@ __global__ void k_color_matrix(uint32_t *img, size_t n, CmParams cp) {
         float na = r * 0.2125f + g * 0.7154f + b * 0.0721f;
         o = pk(0, 0, 0, from_normalized(na));
     }
-    img[i] = mul(o);
+    return tab_px(TAB_MUL, o);
+}
+__global__ void k_color_matrix(uint32_t *img, size_t n, CmParams cp) {
+    auto f = [&cp](uint32_t p) { return color_matrix_px(p, cp); };
+    RGPU_MAP4(img, n, f);
 }
 
 // ---- morphology: window [x - tx, x - tx + cols) x [y - ty, y - ty + rows),
@@ -194,7 +254,11 @@ __global__ void k_morph_pass(const uint32_t *src, uint32_t *dst, int len, int li
                              int taps, int target, int dilate) {
     size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (size_t)len * lines) return;
-    int l = (int)(t % lines), i = (int)(t / lines);
+    // consecutive threads take consecutive pixels in memory: along the line
+    // for a row pass (stride 1), across lines for a column pass
+    int l, i;
+    if (stride == 1) { l = (int)(t / len); i = (int)(t % len); }
+    else { l = (int)(t % lines); i = (int)(t / lines); }
     const uint32_t *s = src + (size_t)l * lstride;
     uint32_t c0 = dilate ? 0 : 255, c1 = c0, c2 = c0, c3 = c0;
     for (int o = 0; o < taps; o++) {
@@ -213,29 +277,62 @@ __device__ __forceinline__ bool approx_zero_ulps4(float v) {
     if (a < 0) return v == 0.0f;
     return a <= 4;
 }
-__global__ void k_arithmetic(const uint32_t *s1, const uint32_t *s2, uint32_t *dst, size_t n, float k1, float k2,
-                             float k3, float k4) {
-    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    uint32_t c1 = s1[i], c2 = s2[i];
+__device__ __forceinline__ uint32_t arithmetic_px(uint32_t c1, uint32_t c2, float k1, float k2, float k3, float k4) {
     auto calc = [&](uint32_t i1, uint32_t i2, float mx) {
         float a = (float)i1 / 255.0f, b = (float)i2 / 255.0f;
         float r = k1 * a * b + k2 * a + k3 * b + k4;
         return f32_bound(0.0f, r, mx);
     };
     float a = calc(chn(c1, 3), chn(c2, 3), 1.0f);
-    if (approx_zero_ulps4(a)) { dst[i] = 0; return; }  // pixel left as initialised (transparent)
-    dst[i] = pk(sat_u8f(calc(chn(c1, 0), chn(c2, 0), a) * 255.0f), sat_u8f(calc(chn(c1, 1), chn(c2, 1), a) * 255.0f),
-                sat_u8f(calc(chn(c1, 2), chn(c2, 2), a) * 255.0f), sat_u8f(a * 255.0f));
+    if (approx_zero_ulps4(a)) return 0u;  // pixel left as initialised (transparent)
+    return pk(sat_u8f(calc(chn(c1, 0), chn(c2, 0), a) * 255.0f), sat_u8f(calc(chn(c1, 1), chn(c2, 1), a) * 255.0f),
+              sat_u8f(calc(chn(c1, 2), chn(c2, 2), a) * 255.0f), sat_u8f(a * 255.0f));
+}
+__global__ void k_arithmetic(const uint32_t *s1, const uint32_t *s2, uint32_t *dst, size_t n, float k1, float k2,
+                             float k3, float k4) {
+    const size_t i = 4 * ((size_t)blockIdx.x * blockDim.x + threadIdx.x);
+    if (i >= n) return;
+    if (vec4(s1, i, n) && vec4(s2, i, n) && vec4(dst, i, n)) {
+        const uint4 a = *reinterpret_cast<const uint4 *>(s1 + i), b = *reinterpret_cast<const uint4 *>(s2 + i);
+        *reinterpret_cast<uint4 *>(dst + i) =
+            make_uint4(arithmetic_px(a.x, b.x, k1, k2, k3, k4), arithmetic_px(a.y, b.y, k1, k2, k3, k4),
+                       arithmetic_px(a.z, b.z, k1, k2, k3, k4), arithmetic_px(a.w, b.w, k1, k2, k3, k4));
+    } else {
+        for (size_t k = i; k < n && k < i + 4; k++) dst[k] = arithmetic_px(s1[k], s2[k], k1, k2, k3, k4);
+    }
 }
 
 inline uint32_t nblk(size_t n, uint32_t t) { return (uint32_t)((n + t - 1) / t); }
 
+uint32_t host_sat_u8(float v) {
+    if (!(v > 0.0f)) return 0;
+    if (v >= 255.0f) return 255;
+    return (uint32_t)v;
+}
 bool g_luts_ready = false;
 cudaError_t ensure_luts() {
     if (g_luts_ready) return cudaSuccess;
     cudaError_t e = cudaMemcpyToSymbol(c_srgb_to_linear, kSrgbToLinear, 256);
     if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_linear_to_srgb, kLinearToSrgb, 256);
+    // the same f32 operations as demul / mul (host and device division and
+    // multiplication are both IEEE round-to-nearest, without contraction)
+    static uint8_t t[4][256 * 256];
+    for (uint32_t a = 0; a < 256 && e == cudaSuccess; a++) {
+        const float af = (float)a / 255.0f;
+        for (uint32_t c = 0; c < 256; c++) {
+            const uint32_t d = host_sat_u8((float)c / af + 0.5f);
+            t[TAB_DEMUL][(a << 8) | c] = (uint8_t)d;
+            t[TAB_MUL][(a << 8) | c] = (uint8_t)host_sat_u8((float)c * af + 0.5f);
+        }
+    }
+    for (uint32_t a = 0; a < 256 && e == cudaSuccess; a++) {
+        for (uint32_t c = 0; c < 256; c++) {
+            const uint32_t d = t[TAB_DEMUL][(a << 8) | c];
+            t[TAB_TO_LINEAR][(a << 8) | c] = t[TAB_MUL][(a << 8) | kSrgbToLinear[d]];
+            t[TAB_TO_SRGB][(a << 8) | c] = t[TAB_MUL][(a << 8) | kLinearToSrgb[d]];
+        }
+    }
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_tab, t, sizeof(t));
     if (e == cudaSuccess) g_luts_ready = true;
     return e;
 }
@@ -246,7 +343,7 @@ cudaError_t ensure_luts() {
 cudaError_t filter_color_space(uint32_t *img, size_t n, bool to_linear, cudaStream_t s) {
     cudaError_t e = ensure_luts();
     if (e != cudaSuccess || n == 0) return e;
-    k_color_space<<<nblk(n, 256), 256, 0, s>>>(img, n, to_linear ? 1 : 0);
+    k_color_space<<<nblk((n + 3) / 4, 256), 256, 0, s>>>(img, n, to_linear ? 1 : 0);
     return cudaGetLastError();
 }
 
@@ -268,6 +365,208 @@ void box_sizes(float sigma, int sizes[5]) {
     }
 }
 
+// Shared-memory tiled box passes (same sums and rounding as k_box_pass, which
+// stays for radii beyond the tile halo).  Loads and stores are coalesced; each
+// thread slides the zero-padded window over 32 outputs inside the tile.
+constexpr int kBoxT = 128;     // outputs along the pass per tile
+constexpr int kBoxMaxR = 96;   // largest radius the tiles take
+// Window sums as two 16-bit lanes per register (r | b << 16, g | a << 16): a
+// lane holds at most (2 * kBoxMaxR + 2) * 255 < 65536 at any step, so lanes
+// never carry or borrow into each other.  round(sum * iarr) is the f32
+// product rounded half to even (box_blur.rs round); it never exceeds 255.
+__device__ __forceinline__ uint32_t box_round2(uint32_t rb, uint32_t ga, float iarr) {
+    const uint32_t r = (uint32_t)__float2int_rn(__fmul_rn((float)(rb & 0xFFFFu), iarr));
+    const uint32_t b = (uint32_t)__float2int_rn(__fmul_rn((float)(rb >> 16), iarr));
+    const uint32_t g = (uint32_t)__float2int_rn(__fmul_rn((float)(ga & 0xFFFFu), iarr));
+    const uint32_t a = (uint32_t)__float2int_rn(__fmul_rn((float)(ga >> 16), iarr));
+    return r | (g << 8) | (b << 16) | (a << 24);
+}
+#define BOX_ADD(p) do { rb += (p) & 0x00FF00FFu; ga += ((p) >> 8) & 0x00FF00FFu; } while (0)
+#define BOX_SLIDE(pa, ps)                                                         \
+    do {                                                                          \
+        rb = rb + ((pa) & 0x00FF00FFu) - ((ps) & 0x00FF00FFu);                    \
+        ga = ga + (((pa) >> 8) & 0x00FF00FFu) - (((ps) >> 8) & 0x00FF00FFu);      \
+    } while (0)
+
+// vertical: tile of 32 columns x kBoxT rows; thread (lane = column, warp = 32-row group)
+__global__ void __launch_bounds__(256) k_box_v(const uint32_t *src, uint32_t *dst, int w, int h, int r, float iarr) {
+    extern __shared__ uint32_t tile[];  // (kBoxT + 2r) rows x 32
+    const int x0 = blockIdx.x * 32, y0 = blockIdx.y * kBoxT;
+    const int rows = kBoxT + 2 * r;
+    if ((w & 3) == 0 && x0 + 32 <= w) {
+        // 16-byte loads: 8 threads per tile row, several rows in flight per thread
+        const int q = threadIdx.x & 7;
+#pragma unroll 4
+        for (int ry = threadIdx.x >> 3; ry < rows; ry += 32) {
+            const int y = y0 - r + ry;
+            const uint4 v = (y >= 0 && y < h) ? __ldg(reinterpret_cast<const uint4 *>(src + (size_t)y * w + x0) + q)
+                                              : make_uint4(0u, 0u, 0u, 0u);
+            reinterpret_cast<uint4 *>(tile + ry * 32)[q] = v;
+        }
+    } else {
+#pragma unroll 4
+        for (int i = threadIdx.x; i < rows * 32; i += 256) {
+            const int ry = i >> 5, x = x0 + (i & 31), y = y0 - r + ry;
+            tile[i] = (x < w && y >= 0 && y < h) ? src[(size_t)y * w + x] : 0u;
+        }
+    }
+    __syncthreads();
+    const int c = threadIdx.x & 31, g = threadIdx.x >> 5;
+    const int x = x0 + c;
+    constexpr int kPer = kBoxT / 8;  // outputs per thread
+    const int oy0 = g * kPer;        // first output row of this thread, tile-relative
+    uint32_t rb = 0, ga = 0;
+    // window of output oy0: tile rows oy0 .. oy0 + 2r
+    for (int k = oy0; k <= oy0 + 2 * r; k++) {
+        const uint32_t p = tile[k * 32 + c];
+        BOX_ADD(p);
+    }
+#pragma unroll 4
+    for (int i = 0; i < kPer; i++) {
+        const int oy = oy0 + i, y = y0 + oy;
+        if (i > 0) {
+            const uint32_t pa = tile[(oy + 2 * r) * 32 + c], ps = tile[(oy - 1) * 32 + c];
+            BOX_SLIDE(pa, ps);
+        }
+        if (x < w && y < h) dst[(size_t)y * w + x] = box_round2(rb, ga, iarr);
+    }
+}
+
+// horizontal: tile of 32 rows x kBoxT columns; thread (lane = row, warp = 32-column
+// group); the outputs go through shared memory so the stores are row-coalesced
+__global__ void __launch_bounds__(256) k_box_h(const uint32_t *src, uint32_t *dst, int w, int h, int r, float iarr) {
+    extern __shared__ uint32_t tile[];
+    const int cols = kBoxT + 2 * r, stride = cols | 1;  // odd row stride: lanes hit distinct banks
+    uint32_t *out = tile + 32 * stride;                  // 32 rows x (kBoxT + 1)
+    const int ostride = kBoxT + 1;
+    const int x0 = blockIdx.x * kBoxT, y0 = blockIdx.y * 32;
+    // each warp copies rows: lane-consecutive columns, several loads in flight
+    const int wp = threadIdx.x >> 5, ln = threadIdx.x & 31;
+    for (int ry = wp; ry < 32; ry += 8) {
+        const int y = y0 + ry;
+        const uint32_t *srow = src + (size_t)y * w;
+#pragma unroll 4
+        for (int cx = ln; cx < cols; cx += 32) {
+            const int x = x0 - r + cx;
+            tile[ry * stride + cx] = (y < h && x >= 0 && x < w) ? __ldg(srow + x) : 0u;
+        }
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, g = threadIdx.x >> 5;
+    const uint32_t *row = tile + lane * stride;
+    constexpr int kPer = kBoxT / 8;
+    const int ox0 = g * kPer;
+    uint32_t rb = 0, ga = 0;
+    for (int k = ox0; k <= ox0 + 2 * r; k++) {
+        const uint32_t p = row[k];
+        BOX_ADD(p);
+    }
+#pragma unroll 4
+    for (int i = 0; i < kPer; i++) {
+        const int ox = ox0 + i;
+        if (i > 0) {
+            const uint32_t pa = row[ox + 2 * r], ps = row[ox - 1];
+            BOX_SLIDE(pa, ps);
+        }
+        out[lane * ostride + ox] = box_round2(rb, ga, iarr);
+    }
+    __syncthreads();
+    for (int ry = wp; ry < 32; ry += 8) {
+        const int y = y0 + ry;
+        if (y >= h) break;
+#pragma unroll 4
+        for (int cx = ln; cx < kBoxT; cx += 32) {
+            const int x = x0 + cx;
+            if (x < w) dst[(size_t)y * w + x] = out[ry * ostride + cx];
+        }
+    }
+}
+
+// Morphology passes on the same tiles: window [i - target, i - target + taps)
+// along the pass, taps outside the image skipped (= the identity of min / max
+// as padding), per-byte min or max of the premultiplied pixels.
+__device__ __forceinline__ uint32_t morph_op(uint32_t a, uint32_t b, bool dilate) {
+    return dilate ? __vmaxu4(a, b) : __vminu4(a, b);
+}
+__global__ void __launch_bounds__(256) k_morph_v(const uint32_t *src, uint32_t *dst, int w, int h, int taps,
+                                                 int target, int dilate) {
+    extern __shared__ uint32_t tile[];
+    const uint32_t pad = dilate ? 0u : 0xFFFFFFFFu;
+    const int x0 = blockIdx.x * 32, y0 = blockIdx.y * kBoxT;
+    const int rows = kBoxT + taps - 1;
+    for (int i = threadIdx.x; i < rows * 32; i += 256) {
+        const int ry = i >> 5, x = x0 + (i & 31), y = y0 - target + ry;
+        tile[i] = (x < w && y >= 0 && y < h) ? __ldg(src + (size_t)y * w + x) : pad;
+    }
+    __syncthreads();
+    const int c = threadIdx.x & 31, g = threadIdx.x >> 5, x = x0 + c;
+    constexpr int kPer = kBoxT / 8;
+    for (int i = 0; i < kPer; i++) {
+        const int oy = g * kPer + i, y = y0 + oy;
+        uint32_t v = pad;
+        for (int k = 0; k < taps; k++) v = morph_op(v, tile[(oy + k) * 32 + c], dilate != 0);
+        if (x < w && y < h) dst[(size_t)y * w + x] = v;
+    }
+}
+__global__ void __launch_bounds__(256) k_morph_h(const uint32_t *src, uint32_t *dst, int w, int h, int taps,
+                                                 int target, int dilate) {
+    extern __shared__ uint32_t tile[];
+    const uint32_t pad = dilate ? 0u : 0xFFFFFFFFu;
+    const int cols = kBoxT + taps - 1, stride = cols | 1;
+    uint32_t *out = tile + 32 * stride;
+    const int ostride = kBoxT + 1;
+    const int x0 = blockIdx.x * kBoxT, y0 = blockIdx.y * 32;
+    const int wp = threadIdx.x >> 5, ln = threadIdx.x & 31;
+    for (int ry = wp; ry < 32; ry += 8) {
+        const int y = y0 + ry;
+        const uint32_t *srow = src + (size_t)y * w;
+        for (int cx = ln; cx < cols; cx += 32) {
+            const int x = x0 - target + cx;
+            tile[ry * stride + cx] = (y < h && x >= 0 && x < w) ? __ldg(srow + x) : pad;
+        }
+    }
+    __syncthreads();
+    const uint32_t *row = tile + ln * stride;
+    constexpr int kPer = kBoxT / 8;
+    for (int i = 0; i < kPer; i++) {
+        const int ox = wp * kPer + i;
+        uint32_t v = pad;
+        for (int k = 0; k < taps; k++) v = morph_op(v, row[ox + k], dilate != 0);
+        out[ln * ostride + ox] = v;
+    }
+    __syncthreads();
+    for (int ry = wp; ry < 32; ry += 8) {
+        const int y = y0 + ry;
+        if (y >= h) break;
+        for (int cx = ln; cx < kBoxT; cx += 32) {
+            const int x = x0 + cx;
+            if (x < w) dst[(size_t)y * w + x] = out[ry * ostride + cx];
+        }
+    }
+}
+size_t morph_v_smem(int taps) { return (size_t)(kBoxT + taps - 1) * 32 * 4; }
+size_t morph_h_smem(int taps) { return ((size_t)32 * ((kBoxT + taps - 1) | 1) + (size_t)32 * (kBoxT + 1)) * 4; }
+constexpr int kMorphMaxTaps = 192;
+
+size_t box_v_smem(int r) { return (size_t)(kBoxT + 2 * r) * 32 * 4; }
+size_t box_h_smem(int r) { return ((size_t)32 * ((kBoxT + 2 * r) | 1) + (size_t)32 * (kBoxT + 1)) * 4; }
+
+cudaError_t box_attrs() {
+    static bool done = false;
+    if (done) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(k_box_v, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)box_v_smem(kBoxMaxR));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_box_h, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)box_h_smem(kBoxMaxR));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_morph_v, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)morph_v_smem(kMorphMaxTaps));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_morph_h, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)morph_h_smem(kMorphMaxTaps));
+    if (e == cudaSuccess) done = true;
+    return e;
+}
+
 // 5 x (vertical pass img -> tmp, horizontal pass tmp -> img)
 cudaError_t filter_box_blur(uint32_t *img, uint32_t *tmp, int w, int h, double sx, double sy, cudaStream_t s) {
     int bh[5], bv[5];
@@ -275,15 +574,29 @@ cudaError_t filter_box_blur(uint32_t *img, uint32_t *tmp, int w, int h, double s
     box_sizes((float)sy, bv);
     const int seg = 32;
     size_t n = (size_t)w * h;
+    cudaError_t ae = box_attrs();
+    if (ae != cudaSuccess) return ae;
     for (int i = 0; i < 5; i++) {
         int rh = (bh[i] - 1) / 2, rv = (bv[i] - 1) / 2;
-        if (rv == 0) k_copy<<<nblk(n, 256), 256, 0, s>>>(img, tmp, n);
-        else {
+        if (rv == 0) {
+            cudaError_t ce = cudaMemcpyAsync(tmp, img, n * 4, cudaMemcpyDeviceToDevice, s);
+            if (ce != cudaSuccess) return ce;
+        }
+        else if (rv <= kBoxMaxR) {
+            dim3 g((unsigned)((w + 31) / 32), (unsigned)((h + kBoxT - 1) / kBoxT));
+            k_box_v<<<g, 256, box_v_smem(rv), s>>>(img, tmp, w, h, rv, 1.0f / (float)(rv + rv + 1));
+        } else {
             size_t th = (size_t)w * ((h + seg - 1) / seg);
             k_box_pass<<<nblk(th, 256), 256, 0, s>>>(img, tmp, h, w, (size_t)w, 1, rv, seg, 1.0f / (float)(rv + rv + 1));
         }
-        if (rh == 0) k_copy<<<nblk(n, 256), 256, 0, s>>>(tmp, img, n);
-        else {
+        if (rh == 0) {
+            cudaError_t ce = cudaMemcpyAsync(img, tmp, n * 4, cudaMemcpyDeviceToDevice, s);
+            if (ce != cudaSuccess) return ce;
+        }
+        else if (rh <= kBoxMaxR) {
+            dim3 g((unsigned)((w + kBoxT - 1) / kBoxT), (unsigned)((h + 31) / 32));
+            k_box_h<<<g, 256, box_h_smem(rh), s>>>(tmp, img, w, h, rh, 1.0f / (float)(rh + rh + 1));
+        } else {
             size_t th = (size_t)h * ((w + seg - 1) / seg);
             k_box_pass<<<nblk(th, 256), 256, 0, s>>>(tmp, img, w, h, 1, (size_t)w, rh, seg, 1.0f / (float)(rh + rh + 1));
         }
@@ -298,12 +611,12 @@ cudaError_t filter_iir_blur(uint32_t *img, double *buf, int w, int h, double sx,
     if (sy > 0.0) { ly = (sy * sy) / (2.0 * steps); dy = (1.0 + 2.0 * ly - sqrt(1.0 + 4.0 * ly)) / (2.0 * ly); }
     double post = pow(sqrt(dx * dy) / sqrt(lx * ly), 2 * steps);
     size_t n = (size_t)w * h;
-    for (int ch = 0; ch < 4; ch++) {
-        k_iir_load<<<nblk(n, 256), 256, 0, s>>>(img, buf, n, ch);
-        if (sx > 0.0) k_iir_rows<<<nblk(h, 64), 64, 0, s>>>(buf, w, h, dx, steps);
-        if (sy > 0.0) k_iir_cols<<<nblk(w, 64), 64, 0, s>>>(buf, w, h, dy, steps);
-        k_iir_store<<<nblk(n, 256), 256, 0, s>>>(img, buf, n, ch, post);
-    }
+    if (n == 0) return cudaSuccess;
+    // buf holds four planes of n doubles
+    k_iir_load4<<<nblk(n, 256), 256, 0, s>>>(img, buf, n);
+    if (sx > 0.0) k_iir_rows4<<<nblk((size_t)4 * h, 64), 64, 0, s>>>(buf, w, h, dx, steps);
+    if (sy > 0.0) k_iir_cols4<<<nblk((size_t)4 * w, 64), 64, 0, s>>>(buf, w, h, dy, steps);
+    k_iir_store4<<<nblk(n, 256), 256, 0, s>>>(img, buf, n, post);
     return cudaGetLastError();
 }
 
@@ -336,7 +649,9 @@ cudaError_t filter_color_matrix(uint32_t *img, size_t n, int kind, const float *
         cp.kind = 2;
     }
     if (n == 0) return cudaSuccess;
-    k_color_matrix<<<nblk(n, 256), 256, 0, s>>>(img, n, cp);
+    cudaError_t te = ensure_luts();
+    if (te != cudaSuccess) return te;
+    k_color_matrix<<<nblk((n + 3) / 4, 256), 256, 0, s>>>(img, n, cp);
     return cudaGetLastError();
 }
 
@@ -347,22 +662,33 @@ cudaError_t filter_morphology(uint32_t *img, uint32_t *tmp, int w, int h, bool d
     int txc = (int)floorf((float)cols / 2.0f), tyr = (int)floorf((float)rows / 2.0f);
     size_t n = (size_t)w * h;
     if (n == 0) return cudaSuccess;
-    k_morph_pass<<<nblk(n, 256), 256, 0, s>>>(img, tmp, w, h, 1, (size_t)w, cols, txc, dilate ? 1 : 0);
-    k_morph_pass<<<nblk(n, 256), 256, 0, s>>>(tmp, img, h, w, (size_t)w, 1, rows, tyr, dilate ? 1 : 0);
+    cudaError_t ae = box_attrs();
+    if (ae != cudaSuccess) return ae;
+    if (cols <= kMorphMaxTaps) {
+        dim3 g((unsigned)((w + kBoxT - 1) / kBoxT), (unsigned)((h + 31) / 32));
+        k_morph_h<<<g, 256, morph_h_smem(cols), s>>>(img, tmp, w, h, cols, txc, dilate ? 1 : 0);
+    } else {
+        k_morph_pass<<<nblk(n, 256), 256, 0, s>>>(img, tmp, w, h, 1, (size_t)w, cols, txc, dilate ? 1 : 0);
+    }
+    if (rows <= kMorphMaxTaps) {
+        dim3 g((unsigned)((w + 31) / 32), (unsigned)((h + kBoxT - 1) / kBoxT));
+        k_morph_v<<<g, 256, morph_v_smem(rows), s>>>(tmp, img, w, h, rows, tyr, dilate ? 1 : 0);
+    } else {
+        k_morph_pass<<<nblk(n, 256), 256, 0, s>>>(tmp, img, h, w, (size_t)w, 1, rows, tyr, dilate ? 1 : 0);
+    }
     return cudaGetLastError();
 }
 
 cudaError_t filter_arithmetic(const uint32_t *a, const uint32_t *b, uint32_t *dst, size_t n, const float k[4],
                               cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    k_arithmetic<<<nblk(n, 256), 256, 0, s>>>(a, b, dst, n, k[0], k[1], k[2], k[3]);
+    k_arithmetic<<<nblk((n + 3) / 4, 256), 256, 0, s>>>(a, b, dst, n, k[0], k[1], k[2], k[3]);
     return cudaGetLastError();
 }
 
 cudaError_t filter_copy(const uint32_t *src, uint32_t *dst, size_t n, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    k_copy<<<nblk(n, 256), 256, 0, s>>>(src, dst, n);
-    return cudaGetLastError();
+    return cudaMemcpyAsync(dst, src, n * 4, cudaMemcpyDeviceToDevice, s);
 }
 
 }  // namespace rgpu
@@ -387,8 +713,8 @@ __global__ void k_draw(const uint32_t *src, uint32_t *dst, int w, int h, int dx,
     dst[i] = dev::composite_pixel(src[(size_t)sy * w + sx], dst[i], 1.0f, blend);
 }
 __global__ void k_fill(uint32_t *img, size_t n, uint32_t v) {
-    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) img[i] = v;
+    auto f = [v](uint32_t) { return v; };
+    RGPU_MAP4(img, n, f);
 }
 }  // namespace
 
@@ -406,7 +732,8 @@ cudaError_t filter_draw(const uint32_t *src, uint32_t *dst, int w, int h, int dx
 }
 cudaError_t filter_fill(uint32_t *img, size_t n, uint32_t v, cudaStream_t s) {
     if (!n) return cudaSuccess;
-    k_fill<<<nblk(n, 256), 256, 0, s>>>(img, n, v);
+    if ((v & 0xFFu) * 0x01010101u == v) return cudaMemsetAsync(img, (int)(v & 0xFFu), n * 4, s);
+    k_fill<<<nblk((n + 3) / 4, 256), 256, 0, s>>>(img, n, v);
     return cudaGetLastError();
 }
 }  // namespace rgpu
@@ -414,13 +741,13 @@ cudaError_t filter_fill(uint32_t *img, size_t n, uint32_t v, cudaStream_t s) {
 namespace rgpu {
 namespace {
 __global__ void k_alpha_only(uint32_t *img, size_t n) {
-    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) img[i] &= 0xFF000000u;
+    auto f = [](uint32_t p) { return p & 0xFF000000u; };
+    RGPU_MAP4(img, n, f);
 }
 }  // namespace
 cudaError_t filter_alpha_only(uint32_t *img, size_t n, cudaStream_t s) {
     if (!n) return cudaSuccess;
-    k_alpha_only<<<nblk(n, 256), 256, 0, s>>>(img, n);
+    k_alpha_only<<<nblk((n + 3) / 4, 256), 256, 0, s>>>(img, n);
     return cudaGetLastError();
 }
 namespace {

@@ -40,6 +40,7 @@ int raster_max_pairs();  // (draw, row) pairs of one phase-A window
 cudaError_t filter_color_space(uint32_t *img, size_t n, bool to_linear, cudaStream_t s);
 void box_sizes(float sigma, int sizes[5]);
 cudaError_t filter_box_blur(uint32_t *img, uint32_t *tmp, int w, int h, double sx, double sy, cudaStream_t s);
+// buf: scratch for four f64 planes of w * h values
 cudaError_t filter_iir_blur(uint32_t *img, double *buf, int w, int h, double sx, double sy, cudaStream_t s);
 cudaError_t filter_color_matrix(uint32_t *img, size_t n, int kind, const float *values, cudaStream_t s);
 cudaError_t filter_morphology(uint32_t *img, uint32_t *tmp, int w, int h, bool dilate, float rx, float ry,
