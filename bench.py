@@ -166,6 +166,9 @@ def run_reference(args, rank, world):
     import oracle
     import resvg_gb300 as R
     oracle.lib()
+    if args.config in (3, 4):
+        run_reference_batched(args)
+        return
     tree = R.Tree.generate(args.config, seed=SEED, index=0, scale=1.0)
     w, h = (int(v) for v in tree.size)
     threads = os.cpu_count() or 1
@@ -188,6 +191,42 @@ def run_reference(args, rank, world):
             "cpu_baseline": {"value": value, "unit": "scenes/s", "cores": threads, "kind": "port",
                              "sample": "one full scene per step, canvas split into %d row strips rendered on %d "
                                        "threads by the C++ restatement of resvg+tiny-skia" % (threads, threads)},
+            "e2e": {"value": value, "unit": "scenes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_reference_batched(args):
+    """Reference arm of the batched (config 3) and differentiable (config 4)
+    forms: the CPU restatement on a bounded sample per step, all host cores
+    for config 3, one core for the FP64 soft reference of config 4."""
+    import resvg_gb300 as R
+    steps = []
+    if args.config == 3:
+        trees = [R.Tree.generate(3, seed=SEED, index=i, scale=args.scale) for i in range(args.scenes)]
+        sizes = [tuple(int(v) for v in t.size) for t in trees]
+        for i in range(args.warmup + args.steps):
+            cb = cpu_baseline_batch(trees, sizes, budget_s=5.0)
+            if i >= args.warmup:
+                steps.append(cb)
+        metric = "scenes/s (batched render, config 3)"
+    else:
+        from resvg_gb300 import soft
+        a = soft.make_scenes(seed=SEED, scenes=256, size=256, paths=64)
+        t = soft.perturb(a, seed=SEED + 1000)
+        for i in range(args.warmup + args.steps):
+            cb = cpu_baseline_soft(a, t, scenes=2)
+            if i >= args.warmup:
+                steps.append(cb)
+        metric = "grads/s (scenes x (forward + adjoint) per second, config 4)"
+    value = sum(c["value"] for c in steps) / len(steps)
+    cb = dict(steps[-1])
+    cb["value"] = value
+    line = {"metric": metric, "value": value, "unit": "scenes/s", "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / value, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u8" if args.config == 3 else "f64",
+            "data": "synthetic (seeded generator)",
+            "config": {"workload": "config%d: %s" % (args.config, CONFIG_DESC.get(args.config, ""))},
+            "cpu_baseline": cb,
             "e2e": {"value": value, "unit": "scenes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -281,6 +320,19 @@ def run_batched(args, rank, world):
         e2e_t.append(time.perf_counter() - t0)
     e2e_ms = 1e3 * sum(e2e_t) / len(e2e_t)
     st = R.stats()
+    # raster-kernel device time for the roofline (un-captured renders, events
+    # around the raster launches of every level)
+    scene.set_timing(True)
+    raster_ms = []
+    for _ in range(2):
+        step()
+        raster_ms.append(scene.check())
+    scene.set_timing(False)
+    rms = sum(raster_ms) / len(raster_ms)
+    alg_bytes = info["output_pixels"] * 8 + info["binned_edges"] * 16 + info["record_bytes"] + \
+        info["layer_pixels"] * 8
+    peak, peak_kind = peaks()
+    achieved = alg_bytes / (rms * 1e-3) / 1e9
     line = {
         "metric": "scenes/s (batched render, config 3)", "value": value, "unit": "scenes/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
@@ -295,15 +347,74 @@ def run_batched(args, rank, world):
         "plain": {"value": plain_value, "unit": "scenes/s", "sample_scenes": len(psamp),
                   "how": "rgpu_render_device per scene (host flatten + upload + kernels), synchronised"},
         "batched_vs_plain": value / plain_value,
+        "raster_ms": rms,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind, "traffic": None, "kernel": "k_raster (band VM)",
+                     "algorithmic_bytes": alg_bytes},
         "e2e": {"value": n * 1e3 / e2e_ms, "unit": "scenes/s", "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": int(st["h2d_bytes"]), "d2h_bytes_per_step": int(total)},
         "gpu_launches": int(info["kernel_launches"]) * args.steps,
         "clocks": clk.summary(),
     }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_batch(trees, sizes, budget_s=10.0)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def cpu_baseline_batch(trees, sizes, budget_s=10.0, threads=None):
+    """The C++ restatement over a stratified sample of the batch (every k-th
+    scene, until about `budget_s` of CPU time), each scene split into row
+    strips over `threads` host threads: scenes/s of the sample."""
+    import oracle
+    threads = threads or os.cpu_count() or 1
+    n = len(trees)
+    order = [i for k in range(16) for i in range(k, n, 16)]
+    done, pixels, t_all = 0, 0, 0.0
+    for i in order:
+        w, h = sizes[i]
+        t0 = time.perf_counter()
+        oracle.render_parallel(trees[i].view(), (1, 0, 0, 1, 0, 0), w, h, threads)
+        t_all += time.perf_counter() - t0
+        done += 1
+        pixels += w * h
+        if t_all >= budget_s:
+            break
+    return {"value": done / t_all, "unit": "scenes/s", "cores": threads, "kind": "port",
+            "sample": "%d of %d scenes (every 16th first, %.1f Mpx), each in row strips on %d threads, by the C++ "
+                      "restatement of resvg+tiny-skia (%.1f s)" % (done, n, pixels / 1e6, threads, t_all)}
+
+
+def _soft_slice(arr, scenes):
+    """The first `scenes` scenes of a soft-renderer batch (host arrays)."""
+    P = int(arr["paths"])
+    segs_end = int(arr["seg_offset"][scenes * P])
+    out = dict(arr)
+    out["scenes"] = scenes
+    out["seg_offset"] = np.ascontiguousarray(arr["seg_offset"][:scenes * P + 1])
+    out["points"] = np.ascontiguousarray(arr["points"][:3 * segs_end])
+    for k in ("paint_kind", "colors", "stop_offsets", "stop_colors", "grad_line"):
+        out[k] = np.ascontiguousarray(arr[k][:scenes * P])
+    out["sigma"] = np.ascontiguousarray(arr["sigma"][:scenes])
+    return out
+
+
+def cpu_baseline_soft(a, t_arrays, scenes=4):
+    """The FP64 C++ reference of the soft renderer on `scenes` scenes, one core:
+    forward, loss and one directional derivative per scene (a full gradient by
+    forward mode would take one such pass per parameter)."""
+    import oracle
+    sub = _soft_slice(a, scenes)
+    _, target = oracle.soft_forward(_soft_slice(t_arrays, scenes))
+    direction = {"colors": np.ones_like(sub["colors"], dtype=np.float64)}
+    t0 = time.perf_counter()
+    oracle.soft_dloss(sub, target.astype(np.float32), direction)
+    dt = time.perf_counter() - t0
+    return {"value": scenes / dt, "unit": "scenes/s", "cores": 1, "kind": "port",
+            "sample": "%d scenes: FP64 forward + loss + one directional derivative (C++ reference, %.1f s)" %
+                      (scenes, dt)}
 
 
 def run_soft(args, rank, world):
@@ -373,6 +484,15 @@ def run_soft(args, rank, world):
         "gpu_launches": 12 * args.steps,
         "clocks": clk.summary(),
     }
+    # the soft renderer is FP32-ALU bound; the HBM line is reported for
+    # completeness: parameters + target + image + blurred image + gradients
+    peak, peak_kind = peaks()
+    alg_bytes = 2 * h2d + 3 * 256 * 256 * 256 * 16
+    line["roofline"] = {"bound": "hbm", "achieved": alg_bytes / (ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                        "frac": alg_bytes / (ms * 1e-3) / 1e9 / peak, "peak_kind": peak_kind, "traffic": None,
+                        "kernel": "soft forward + adjoint (one step)", "algorithmic_bytes": alg_bytes}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_soft(a, t)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -132,12 +132,37 @@ struct Plan {
     bool sized = false;
 };
 
+// CUDA events around the raster launch of each dependency level (created on
+// first use); the raster time of a render is the sum over its levels.
+struct RasterTimer {
+    static constexpr int kPairs = 16;
+    cudaEvent_t start[kPairs] = {}, stop[kPairs] = {};
+    int used = 0;
+    bool made = false;
+    cudaError_t ensure() {
+        if (made) return cudaSuccess;
+        for (int k = 0; k < kPairs; k++) {
+            cudaError_t e = cudaEventCreate(&start[k]);
+            if (e == cudaSuccess) e = cudaEventCreate(&stop[k]);
+            if (e != cudaSuccess) return e;
+        }
+        made = true;
+        return cudaSuccess;
+    }
+    ~RasterTimer() {
+        for (int k = 0; k < kPairs; k++) {
+            if (start[k]) cudaEventDestroy(start[k]);
+            if (stop[k]) cudaEventDestroy(stop[k]);
+        }
+    }
+};
+
 struct Context {
     std::mutex mu;
     int device = -1;
     int sms = 0;
     cudaStream_t stream = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    RasterTimer timer;
     Buffers buf;
     DevBuf surface;
     HostBuf staging;
@@ -177,8 +202,6 @@ int ensure_device(Context &c) {
     }
     c.sms = prop.multiProcessorCount;
     CK(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
-    CK(cudaEventCreate(&c.ev0));
-    CK(cudaEventCreate(&c.ev1));
     CK(raster_init());
     c.device = dev;
     return RGPU_OK;
@@ -320,7 +343,7 @@ int upload_plan(Context &c, Buffers &b, Plan &p, cudaStream_t s) {
 // Enqueues the device pipeline.  Without known sizes it synchronises twice to
 // read the edge and bin totals; with known sizes (a prepared scene rendered
 // before) it is fully asynchronous and capturable into a CUDA graph.
-int enqueue_plan(Context &c, Buffers &b, Plan &p, cudaStream_t s, cudaEvent_t ev0, cudaEvent_t ev1) {
+int enqueue_plan(Context &c, Buffers &b, Plan &p, cudaStream_t s, RasterTimer *tm) {
     SceneBuild &sb = p.sb;
     uint32_t ndraws = (uint32_t)sb.draws.size();
     uint64_t nsegs = sb.nsegs;
@@ -368,9 +391,13 @@ int enqueue_plan(Context &c, Buffers &b, Plan &p, cudaStream_t s, cudaEvent_t ev
     for (const auto &st : sb.streams)
         if (st.surface >= 0) CK(cudaMemsetAsync(b.surf[st.surface].p, 0, (size_t)st.out_w * st.out_h * 4, s));
     BufScratch scratch(b);
+    if (tm) {
+        CK(tm->ensure());
+        tm->used = 0;
+    }
     for (uint32_t lv = 0; lv <= sb.max_level; lv++) {
-        bool last = lv == sb.max_level;
-        if (ev0 && last) CK(cudaEventRecord(ev0, s));
+        const bool timed = tm && p.level_cnt[lv] && tm->used < RasterTimer::kPairs;
+        if (timed) CK(cudaEventRecord(tm->start[tm->used], s));
         if (p.level_cnt[lv])
             CK(launch_raster((int)p.px, p.grid, p.max_depth, b.streams.as<StreamRec>(),
                              b.items.as<WorkItem>() + p.level_off[lv], p.level_cnt[lv], b.counter.as<uint32_t>() + lv,
@@ -378,7 +405,7 @@ int enqueue_plan(Context &c, Buffers &b, Plan &p, cudaStream_t s, cudaEvent_t ev
                              b.layers.as<LayerRec>(), b.bins.as<EdgeRec>(), b.bin_offsets.as<uint32_t>(),
                              b.bin_counts.as<uint32_t>(), b.stack.as<uint32_t>(), b.span_ovf.as<int2>(), kSpanOvf,
                              b.run_ovf.as<int2>(), p.run_cap, b.hairs.as<HairRec>(), b.hair_spans.as<HairSpan>(), b.err.as<uint32_t>(), s));
-        if (ev1 && last) CK(cudaEventRecord(ev1, s));
+        if (timed) CK(cudaEventRecord(tm->stop[tm->used++], s));
         for (const auto &job : sb.jobs) {
             if (job.level != lv) continue;
             std::string ferr;
@@ -394,13 +421,18 @@ int enqueue_plan(Context &c, Buffers &b, Plan &p, cudaStream_t s, cudaEvent_t ev
     return RGPU_OK;
 }
 
-int check_err(Buffers &b, cudaStream_t s, cudaEvent_t ev0, cudaEvent_t ev1) {
+int check_err(Buffers &b, cudaStream_t s, RasterTimer *tm) {
     uint32_t e = 0;
     CK(cudaMemcpyAsync(&e, b.err.p, 4, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
-    float ms = 0;
-    if (ev0) {
-        if (cudaEventElapsedTime(&ms, ev0, ev1) == cudaSuccess) g_stats.raster_ms = ms;
+    if (tm && tm->used) {
+        // the raster launches of every dependency level, summed
+        float total = 0.0f;
+        for (int k = 0; k < tm->used; k++) {
+            float ms = 0.0f;
+            if (cudaEventElapsedTime(&ms, tm->start[k], tm->stop[k]) == cudaSuccess) total += ms;
+        }
+        g_stats.raster_ms = total;
         cudaGetLastError();  // never leave a pending error behind for the caller
     }
     if (e) {
@@ -443,8 +475,8 @@ int render_host(const rgpu_tree *tree, const resvg_transform &ts, uint32_t w, ui
     g_stats.h2d_bytes += bytes;
     if ((r = plan_scene(c, p))) return r;
     if ((r = upload_plan(c, c.buf, p, s))) return r;
-    if ((r = enqueue_plan(c, c.buf, p, s, c.ev0, c.ev1))) return r;
-    if ((r = check_err(c.buf, s, c.ev0, c.ev1))) return r;
+    if ((r = enqueue_plan(c, c.buf, p, s, &c.timer))) return r;
+    if ((r = check_err(c.buf, s, &c.timer))) return r;
     CK(c.staging.ensure(bytes));
     CK(cudaMemcpyAsync(c.staging.p, c.surface.p, bytes, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
@@ -551,11 +583,9 @@ struct rgpu_scene {
     cudaStream_t last_stream = nullptr;
     bool timing = false;        // un-captured renders with events around the raster kernel
     bool timed_valid = false;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    RasterTimer timer;
     ~rgpu_scene() {
         if (graph) cudaGraphExecDestroy(graph);
-        if (ev0) cudaEventDestroy(ev0);
-        if (ev1) cudaEventDestroy(ev1);
         buf.release();
     }
 };
@@ -601,8 +631,8 @@ int rgpu_render_device(const resvg_render_tree *tree, resvg_transform ts, uint32
     if ((r = build_batch(p, &tree, &ts, 1, &w, &h, &device_pixmap, &stride))) return r;
     if ((r = plan_scene(c, p))) return r;
     if ((r = upload_plan(c, c.buf, p, s))) return r;
-    if ((r = enqueue_plan(c, c.buf, p, s, c.ev0, c.ev1))) return r;
-    return check_err(c.buf, s, c.ev0, c.ev1);
+    if ((r = enqueue_plan(c, c.buf, p, s, &c.timer))) return r;
+    return check_err(c.buf, s, &c.timer);
 }
 
 int rgpu_render_batch(const resvg_render_tree *const *trees, const resvg_transform *transforms, uint32_t count,
@@ -622,8 +652,8 @@ int rgpu_render_batch(const resvg_render_tree *const *trees, const resvg_transfo
     if ((r = build_batch(p, trees, transforms, count, widths, heights, device_pixmaps, nullptr))) return r;
     if ((r = plan_scene(c, p))) return r;
     if ((r = upload_plan(c, c.buf, p, s))) return r;
-    if ((r = enqueue_plan(c, c.buf, p, s, c.ev0, c.ev1))) return r;
-    return check_err(c.buf, s, c.ev0, c.ev1);
+    if ((r = enqueue_plan(c, c.buf, p, s, &c.timer))) return r;
+    return check_err(c.buf, s, &c.timer);
 }
 
 int rgpu_scene_prepare(const resvg_render_tree *const *trees, const resvg_transform *transforms, uint32_t count,
@@ -647,8 +677,6 @@ int rgpu_scene_prepare(const resvg_render_tree *const *trees, const resvg_transf
         return r;
     }
     cudaError_t e = cudaStreamSynchronize(c.stream);
-    if (e == cudaSuccess) e = cudaEventCreate(&sc->ev0);
-    if (e == cudaSuccess) e = cudaEventCreate(&sc->ev1);
     if (e != cudaSuccess) {
         set_error("rgpu_scene_prepare: %s", cudaGetErrorString(e));
         delete sc;
@@ -669,7 +697,7 @@ int rgpu_scene_render(rgpu_scene *sc, void *stream) {
     if (!sc->plan.sized || sc->timing) {
         // the first render sizes the edge and bin buffers (two synchronisations);
         // timing renders run un-captured with events around the raster kernel
-        r = enqueue_plan(c, sc->buf, sc->plan, s, sc->timing ? sc->ev0 : nullptr, sc->timing ? sc->ev1 : nullptr);
+        r = enqueue_plan(c, sc->buf, sc->plan, s, sc->timing ? &sc->timer : nullptr);
         sc->timed_valid = sc->timing && r == RGPU_OK;
         return r;
     }
@@ -678,7 +706,7 @@ int rgpu_scene_render(rgpu_scene *sc, void *stream) {
         if (sc->graph) { cudaGraphExecDestroy(sc->graph); sc->graph = nullptr; }
         cudaGraph_t g;
         CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-        r = enqueue_plan(c, sc->buf, sc->plan, s, nullptr, nullptr);
+        r = enqueue_plan(c, sc->buf, sc->plan, s, nullptr);
         cudaError_t e = cudaStreamEndCapture(s, &g);
         if (r) return r;
         CK(e);
@@ -702,7 +730,7 @@ int rgpu_scene_check(rgpu_scene *sc, float *raster_ms) {
     Context &c = ctx();
     std::lock_guard<std::mutex> lock(c.mu);
     cudaStream_t s = sc->last_stream ? sc->last_stream : c.stream;
-    int r = check_err(sc->buf, s, sc->timed_valid ? sc->ev0 : nullptr, sc->timed_valid ? sc->ev1 : nullptr);
+    int r = check_err(sc->buf, s, sc->timed_valid ? &sc->timer : nullptr);
     if (raster_ms) *raster_ms = sc->timed_valid ? g_stats.raster_ms : -1.0f;
     return r;
 }
