@@ -65,15 +65,33 @@ def parse():
     return ap.parse_args()
 
 
-def dist_setup(n):
+def dist_setup(n, backend="nccl"):
+    """(rank, world) from the torchrun environment; joins the process group
+    when world > 1 (one rank per GPU over NCCL; `gloo` for CPU-only runs)."""
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if world > 1:
         import torch.distributed as dist
-        import torch
-        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-        dist.init_process_group("nccl")
+        if backend == "nccl":
+            import torch
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group(backend)
     return rank, world
+
+
+def max_over_ranks(ms, world, device):
+    """The slowest rank's step time: every rank reports the job's time."""
+    if world <= 1:
+        return ms
+    import torch
+    t = torch.tensor([ms], device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def shard(rank, n):
+    """Scene indices of a rank in the batched form: disjoint, n per rank."""
+    return [rank * n + i for i in range(n)]
 
 
 def _smi_index():
@@ -243,7 +261,7 @@ def run_batched(args, rank, world):
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
     torch.cuda.set_device(dev)
     n = args.scenes
-    trees = [R.Tree.generate(3, seed=SEED, index=rank * n + i, scale=args.scale) for i in range(n)]
+    trees = [R.Tree.generate(3, seed=SEED, index=i, scale=args.scale) for i in shard(rank, n)]
     sizes = [tuple(int(v) for v in t.size) for t in trees]
     offs, total = [], 0
     for w, h in sizes:
@@ -290,11 +308,7 @@ def run_batched(args, rank, world):
             scene.check()
             step_ms.append(s0.elapsed_time(s1))
         torch.cuda.synchronize()
-    ms = sum(step_ms) / len(step_ms)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(sum(step_ms) / len(step_ms), world, dev)
     value = world * n * 1e3 / ms
     out_px = sum(w * h for w, h in sizes)
     # plain per-scene drop-in (device pixmap, one call per scene, synchronised)
@@ -451,11 +465,7 @@ def run_soft(args, rank, world):
             s1.record()
             torch.cuda.synchronize()
             ms_list.append(s0.elapsed_time(s1))
-    ms = sum(ms_list) / len(ms_list)
-    if world > 1:
-        tt = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        ms = float(tt.item())
+    ms = max_over_ranks(sum(ms_list) / len(ms_list), world, dev)
     value = world * 256 * 1e3 / ms
     # end to end: parameters from pinned host memory, gradients back to the host
     host = {k: torch.from_numpy(np.ascontiguousarray(a[k])).pin_memory() for k in soft.PARAMS}
@@ -563,11 +573,7 @@ def main():
     scene.set_timing(False)
     if world > 1:
         torch.distributed.barrier()
-    ms = sum(step_ms) / len(step_ms)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(sum(step_ms) / len(step_ms), world, dev)
     value = world * 1e3 / ms
     rms = sum(raster_ms) / len(raster_ms)
 
