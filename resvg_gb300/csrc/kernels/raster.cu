@@ -24,7 +24,9 @@
 namespace rgpu {
 namespace {
 
-constexpr int kThreads = 256;
+constexpr int kThreads = 256;    // consumer threads: they own the band's pixels
+constexpr int kProducers = 128;  // producer threads: phase A and the run merge of the next window
+constexpr int kBlock = kThreads + kProducers;
 constexpr int kXCap = 40;        // crossings held per thread before the exact slow path
 constexpr int kSpanCap = 8;      // spans per (slot, sub-scanline) kept in shared memory
 constexpr int kSpanStride = kSpanCap + 1;  // padded: neighbouring lists start in different banks
@@ -35,21 +37,64 @@ constexpr int kMaxPairs = kThreads / 4;  // (slot, row) pairs per window: K x BH
 constexpr int kRunCap = 32;     // alpha runs per (slot, row) kept in shared memory
 constexpr int kRunStride = kRunCap + 1;
 
-struct VmShared {
-    uint16_t span_cnt[kThreads];
-    int2 spans[kThreads * kSpanStride];
+// One phase-A window as the consumers read it: the window's paints, gradients
+// and draw origins, and per (slot, row) the alpha runs.  Two of them alternate:
+// the producers fill one while the consumers shade from the other.
+struct WinBuf {
     uint16_t run_cnt[kMaxPairs];  // alpha runs per (slot, row), including the closing sentinel
     int2 run_ext[kMaxPairs];      // [first, last) layer x with non-zero coverage per (slot, row)
     int2 runs[kMaxPairs * kRunStride];
+    PaintRec paint[kMaxSlots + 1];   // paints of the window's draws; [kMaxSlots] of buffer 0: the hairline's
+    int4 slot_geo[kMaxSlots];    // (unused, ox, oy, unused) per slot
+    GradRec grad[kMaxSlots + 1];     // gradients of the window's draws (and the hairline's)
+};
+struct VmShared {
+    uint16_t span_cnt[kThreads];  // producer-private: spans per (slot, sub-scanline) task
+    int2 spans[kThreads * kSpanStride];
+    WinBuf win[2];
+    unsigned long long mb_ready[2];  // mbarriers: window in buffer b produced (kProducers arrivals)
+    unsigned long long mb_free[2];   // buffer b consumed (kThreads arrivals)
+    int32_t abort;                   // set on an error: the rest of the launch skips work and waits
     int4 rects[kMaxDepth];       // layer-stack rects (x, y, w, h) by depth, the top one at [depth]
     WorkItem wi;                 // the work item being rendered, and its stream
     StreamRec st;
-    PaintRec paint[kMaxSlots + 1];   // paints of the window's draws; the last: the current hairline's
-    int4 slot_geo[kMaxSlots];    // (unused, ox, oy, unused) per slot
-    GradRec grad[kMaxSlots + 1];     // gradients of the window's draws (and the hairline's)
     int32_t item;
     // followed by the top layer: kThreads * px uint32 pixels (dynamic)
 };
+
+// ---- producer / consumer hand-off (mbarriers, every wait bounded)
+constexpr uint32_t kWaitLimit = 1u << 22;  // try_wait rounds before a wait is declared stuck
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mb_init(unsigned long long *mb, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(mb)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mb_arrive(unsigned long long *mb) {
+    asm volatile("{ .reg .b64 st; mbarrier.arrive.shared::cta.b64 st, [%0]; }" ::"r"(smem_addr(mb)) : "memory");
+}
+// Waits for the phase of parity `parity` to complete; false (and error bit 16)
+// when it does not within kWaitLimit rounds, after which the caller proceeds
+// so every thread still reaches every later barrier.
+__device__ __forceinline__ bool mb_wait(unsigned long long *mb, uint32_t parity, uint32_t *err,
+                                        const volatile int32_t *abort) {
+    const uint32_t a = smem_addr(mb);
+    for (uint32_t it = 0; it < kWaitLimit; it++) {
+        if ((it & 255u) == 0u && *abort) return false;
+        uint32_t ok;
+        asm volatile(
+            "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+            : "=r"(ok)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    atomicOr(err, 16u);
+    *const_cast<volatile int32_t *>(abort) = 1;
+    return false;
+}
+// barrier of the consumer threads only (named barrier 1)
+__device__ __forceinline__ void consumer_sync() { asm volatile("bar.sync 1, %0;" ::"n"(kThreads) : "memory"); }
 
 __device__ __forceinline__ int32_t round16(int32_t x) { return (int32_t)((uint32_t)x + 0x8000u) >> 16; }
 
@@ -195,9 +240,9 @@ struct RunWriter {
     }
 };
 
-__device__ void merge_runs(VmShared &sh, const int2 *ovf, uint32_t ovf_cap, int2 *rovf, uint32_t rovf_cap, int pair,
-                           int sj, bool aa, int32_t lo, int32_t hi, uint32_t *err) {
-    RunWriter w{&sh.runs[pair * kRunStride], rovf + (size_t)pair * rovf_cap, rovf_cap, 0, 0, INT32_MAX, INT32_MIN};
+__device__ void merge_runs(VmShared &sh, WinBuf &wb, const int2 *ovf, uint32_t ovf_cap, int2 *rovf, uint32_t rovf_cap,
+                           int pair, int sj, bool aa, int32_t lo, int32_t hi, uint32_t *err) {
+    RunWriter w{&wb.runs[pair * kRunStride], rovf + (size_t)pair * rovf_cap, rovf_cap, 0, 0, INT32_MAX, INT32_MIN};
     if (aa) {
         const int2 *L[4];
         int n[4], q[4];
@@ -244,12 +289,12 @@ __device__ void merge_runs(VmShared &sh, const int2 *ovf, uint32_t ovf_cap, int2
     }
     w.set(hi, 0, err);
     w.put(INT32_MAX, 0, err);
-    sh.run_cnt[pair] = (uint16_t)min(w.n, (int)rovf_cap);
-    sh.run_ext[pair] = make_int2(w.first, w.last);
+    wb.run_cnt[pair] = (uint16_t)min(w.n, (int)rovf_cap);
+    wb.run_ext[pair] = make_int2(w.first, w.last);
 }
 
-__device__ __forceinline__ const int2 *run_base(const VmShared &sh, const int2 *rovf, uint32_t rovf_cap, int pair) {
-    return sh.run_cnt[pair] <= kRunCap ? &sh.runs[pair * kRunStride] : rovf + (size_t)pair * rovf_cap;
+__device__ __forceinline__ const int2 *run_base(const WinBuf &wb, const int2 *rovf, uint32_t rovf_cap, int pair) {
+    return wb.run_cnt[pair] <= kRunCap ? &wb.runs[pair * kRunStride] : rovf + (size_t)pair * rovf_cap;
 }
 
 // Coverage of layer pixel (px, py) from one hairline span (tiny-skia
@@ -298,7 +343,69 @@ __device__ __forceinline__ uint32_t hair_cov(const HairSpan *hsp, int32_t px, in
     return minor == lo ? sna : (minor == lo + 1 ? sa : 0u);
 }
 
-__global__ void __launch_bounds__(kThreads, 3)
+// One phase-A window by the producer threads (pt = 0 .. kProducers-1) into
+// buffer wb: stage the window's paints, gradients and draw origins, run phase
+// A for two (slot, sub-scanline) tasks per thread, then merge each (slot, row)
+// into alpha runs (a row's tasks sit in one warp, so a warp barrier orders
+// them).
+__device__ __forceinline__ void produce_window(VmShared &sh, WinBuf &wb, int pt, uint32_t wfirst, const Cmd *cmds,
+                                               const uint32_t *fill_cmds, const DrawRec *draws,
+                                               const PaintRec *paints, const GradRec *grads, const EdgeRec *bins,
+                                               const uint32_t *bin_offsets, const uint32_t *bin_counts, int2 *ovf,
+                                               uint32_t ovf_cap, int2 *rovf, uint32_t rovf_cap, uint32_t *err) {
+    const WorkItem &wi = sh.wi;
+    const StreamRec &st = sh.st;
+    const int BH = (int)st.band_rows;
+    const int S = 4 * BH;
+    const int K = min(kThreads / S, kMaxSlots);
+    const uint32_t nsl = min((uint32_t)K, st.fill_cnt - wfirst);
+    const uint32_t *flist = fill_cmds + st.fill_off + wfirst;
+    const int pw = pt >> 5, lane = pt & 31;
+    for (uint32_t k = (uint32_t)pw; k < nsl; k += kProducers / 32) {
+        const uint32_t di = cmds[st.cmd_off + flist[k]].a;
+        const uint32_t pi = draws[di].paint;
+        if (lane < (int)(sizeof(PaintRec) / 4))
+            ((uint32_t *)&wb.paint[k])[lane] = ((const uint32_t *)&paints[pi])[lane];
+        if (lane == 0) wb.slot_geo[k] = make_int4(0, draws[di].ox, draws[di].oy, 0);
+        if (paints[pi].kind == 1) {
+            const uint32_t *src = (const uint32_t *)&grads[paints[pi].grad];
+            for (int w = lane; w < (int)(sizeof(GradRec) / 4); w += 32) ((uint32_t *)&wb.grad[k])[w] = src[w];
+        }
+    }
+    // tasks 2 pt and 2 pt + 1: the same slot (S is even)
+    const int u0 = 2 * pt, k = u0 / S, j0 = u0 % S;
+    DrawRec dr;
+    if (k < (int)nsl) {
+        const uint32_t di = cmds[st.cmd_off + flist[k]].a;
+        dr = draws[di];
+        const uint32_t slot = st.bin_off + wi.band * st.draw_cnt + (di - st.draw_off);
+        const EdgeRec *bl = bins + bin_offsets[slot];
+        const uint32_t nb = bin_counts[slot];
+        const int32_t lrow0 = (int32_t)wi.band * BH - dr.oy;
+        for (int h = 0; h < 2; h++) {
+            const int j = j0 + h;
+            int32_t y;
+            bool ok;
+            if (dr.shift) { y = lrow0 * 4 + j; ok = true; }
+            else { y = lrow0 + j; ok = j < BH; }
+            if (ok && dr.valid) phase_a(sh, u0 + h, dr, y, bl, nb, ovf, ovf_cap, err);
+            else sh.span_cnt[u0 + h] = 0;
+        }
+    }
+    __syncwarp();
+    if (k < (int)nsl && (j0 & 3) == 0) {
+        const int r2 = j0 >> 2;
+        const int32_t ly = (int32_t)wi.band * BH + r2 - dr.oy;
+        int32_t lo = max(dr.sect_l, wi.x0 - dr.ox), hi = min(dr.sect_r, wi.x1 - dr.ox);
+        if (!dr.valid || ly < dr.sect_t || ly >= dr.sect_b || (int32_t)wi.band * BH + r2 >= st.out_h) hi = lo;
+        if (r2 < BH)
+            merge_runs(sh, wb, ovf, ovf_cap, rovf, rovf_cap, k * BH + r2, k * S + (dr.shift ? j0 : r2), dr.shift != 0,
+                       lo, hi, err);
+    }
+    __syncwarp();  // the merge has read the spans before the next window's phase A overwrites them
+}
+
+__global__ void __launch_bounds__(kBlock, 2)
 k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitems, uint32_t *item_counter,
          const Cmd *cmds, const uint32_t *fill_cmds, const DrawRec *draws, const PaintRec *paints, const GradRec *grads, const LayerRec *layers,
          const EdgeRec *bins, const uint32_t *bin_offsets, const uint32_t *bin_counts, uint32_t *stack_scratch,
@@ -310,7 +417,17 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
     const int tid = threadIdx.x;
     uint32_t *stack = stack_scratch + (size_t)blockIdx.x * stack_depth * kThreads * PX;
     int2 *ovf = span_ovf + (size_t)blockIdx.x * kThreads * ovf_cap;
-    int2 *rovf = run_ovf + (size_t)blockIdx.x * kMaxPairs * rovf_cap;
+    // two run-overflow areas per CTA, one per window buffer
+    int2 *rovf = run_ovf + (size_t)blockIdx.x * 2 * kMaxPairs * rovf_cap;
+    if (tid == 0) {
+        mb_init(&sh.mb_ready[0], kProducers);
+        mb_init(&sh.mb_ready[1], kProducers);
+        mb_init(&sh.mb_free[0], kThreads);
+        mb_init(&sh.mb_free[1], kThreads);
+        sh.abort = 0;
+    }
+    __syncthreads();
+    uint32_t win_base = 0;  // windows produced and consumed by this CTA so far
 
     for (;;) {
         if (tid == 0) {
@@ -332,6 +449,24 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
         const int BH = (int)st.band_rows;
         const int S = 4 * BH;                 // scanline slots per draw (sub-scanlines for AA)
         const int K = min(kThreads / S, kMaxSlots);
+        const uint32_t nwin = (st.fill_cnt + (uint32_t)K - 1) / (uint32_t)K;
+        if (tid >= kThreads) {
+            // ---- producers: the item's windows in order, two buffers ahead at most
+            const int pt = tid - kThreads;
+            for (uint32_t w = 0; w < nwin; w++) {
+                const uint32_t gw = win_base + w, b = gw & 1u;
+                if (gw >= 2) mb_wait(&sh.mb_free[b], ((gw >> 1) - 1u) & 1u, err, &sh.abort);
+                if (!*(volatile int32_t *)&sh.abort)
+                    produce_window(sh, sh.win[b], pt, w * (uint32_t)K, cmds, fill_cmds, draws, paints, grads, bins,
+                                   bin_offsets, bin_counts, ovf, ovf_cap, rovf + (size_t)b * kMaxPairs * rovf_cap,
+                                   rovf_cap, err);
+                mb_arrive(&sh.mb_ready[b]);
+            }
+            win_base += nwin;
+            __syncthreads();
+            continue;
+        }
+        // ---- consumers
         const int tpr = kThreads / BH;        // threads per pixel row
         const int row = tid / tpr;
         const int lr = tid % tpr;             // lane within the row: pixel x = x0 + i*tpr + lr
@@ -345,63 +480,20 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
                 (row_ok && x < wi.x1) ? *(const uint32_t *)(out + (size_t)cy * st.out_stride + 4 * (size_t)x) : 0u;
         }
         int32_t depth = 0;
-        int32_t slot_next = 0, win_last = 0;
+        int32_t slot_next = 0;
+        uint32_t cur_b = 0;      // window buffer of the current fills
         uint32_t fill_seen = 0;  // fill commands of the stream before the current one
 
         for (uint32_t ci = 0; ci < st.cmd_cnt; ci++) {
             const Cmd c = cmds[st.cmd_off + ci];
             if (c.op == CMD_FILL || c.op == CMD_APPLY_REGION || c.op == CMD_HAIR) {
-                if (c.op != CMD_HAIR && (int32_t)ci >= win_last) {
-                    // ---- a phase-A window over the next K fill commands of the stream's
-                    // fill list (fill_seen of them come before this one)
-                    const uint32_t nsl = min((uint32_t)K, st.fill_cnt - fill_seen);
-                    const uint32_t *flist = fill_cmds + st.fill_off + fill_seen;
-                    win_last = (int32_t)flist[nsl - 1] + 1;
-                    __syncthreads();  // the previous window's readers are done
-                    // stage paints, draw geometry and gradients: warp w takes the slots
-                    // w, w + 8, ...
-                    const int warp = tid >> 5, lane = tid & 31;
-                    for (uint32_t k = (uint32_t)warp; k < nsl; k += kThreads / 32) {
-                        const uint32_t di = cmds[st.cmd_off + flist[k]].a;
-                        const uint32_t pi = draws[di].paint;
-                        if (lane < (int)(sizeof(PaintRec) / 4))
-                            ((uint32_t *)&sh.paint[k])[lane] = ((const uint32_t *)&paints[pi])[lane];
-                        if (lane == 0) sh.slot_geo[k] = make_int4(0, draws[di].ox, draws[di].oy, 0);
-                        if (paints[pi].kind == 1) {
-                            const uint32_t *src = (const uint32_t *)&grads[paints[pi].grad];
-                            for (int w = lane; w < (int)(sizeof(GradRec) / 4); w += 32) ((uint32_t *)&sh.grad[k])[w] = src[w];
-                        }
-                    }
+                if (c.op != CMD_HAIR && fill_seen % (uint32_t)K == 0) {
+                    // ---- the next window: release the previous buffer, wait for this one
+                    const uint32_t gw = win_base + fill_seen / (uint32_t)K;
+                    if (fill_seen) mb_arrive(&sh.mb_free[(gw - 1u) & 1u]);
+                    mb_wait(&sh.mb_ready[gw & 1u], (gw >> 1) & 1u, err, &sh.abort);
+                    cur_b = gw & 1u;
                     slot_next = 0;
-                    // phase A: thread (k, j) walks sub-scanline j of slot k; then lane
-                    // 4r of each slot merges row r (its 4 sub-scanlines sit in the same
-                    // warp: S divides 32)
-                    const int k = tid / S, j = tid % S;
-                    DrawRec dr;
-                    if (k < (int)nsl) {
-                        const uint32_t di = cmds[st.cmd_off + flist[k]].a;
-                        dr = draws[di];
-                        const uint32_t ld = di - st.draw_off;
-                        const uint32_t slot = st.bin_off + wi.band * st.draw_cnt + ld;
-                        const int32_t lrow0 = (int32_t)wi.band * BH - dr.oy;
-                        int32_t y;
-                        bool ok;
-                        if (dr.shift) { y = lrow0 * 4 + j; ok = true; }
-                        else { y = lrow0 + j; ok = j < BH; }
-                        if (ok && dr.valid) phase_a(sh, tid, dr, y, bins + bin_offsets[slot], bin_counts[slot], ovf, ovf_cap, err);
-                        else sh.span_cnt[tid] = 0;
-                    }
-                    __syncwarp();
-                    if (k < (int)nsl && (j & 3) == 0) {
-                        const int r2 = j >> 2;
-                        const int32_t ly = (int32_t)wi.band * BH + r2 - dr.oy;
-                        int32_t lo = max(dr.sect_l, wi.x0 - dr.ox), hi = min(dr.sect_r, wi.x1 - dr.ox);
-                        if (!dr.valid || ly < dr.sect_t || ly >= dr.sect_b || (int32_t)wi.band * BH + r2 >= st.out_h) hi = lo;
-                        if (r2 < BH)
-                            merge_runs(sh, ovf, ovf_cap, rovf, rovf_cap, k * BH + r2, k * S + (dr.shift ? j : r2),
-                                       dr.shift != 0, lo, hi, err);
-                    }
-                    __syncthreads();
                 }
                 // ---- phase B: coverage + shading, one pixel per (thread, i).  A hairline
                 // (CMD_HAIR) runs its spans in order through the same loop, each thread
@@ -424,15 +516,15 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
                         const int32_t lx0 = wi.x0 - hr.ox, ly0 = (int32_t)wi.band * BH - hr.oy;
                         if (hr.x1 <= lx0 || hr.x0 >= wi.x1 - hr.ox || hr.y1 <= ly0 || hr.y0 >= ly0 + BH) continue;
                     }
-                    __syncthreads();  // the previous hairline's pixels are done with the slot
-                    slot = kMaxSlots;
-                    if (tid == 0) sh.paint[slot] = paints[hr.paint];
+                    consumer_sync();  // the previous hairline's pixels are done with the slot
+                    slot = kMaxSlots;  // the spare slot of buffer 0 (producers never write it)
+                    if (tid == 0) sh.win[0].paint[slot] = paints[hr.paint];
                     const PaintRec &gp = paints[hr.paint];
                     if (gp.kind == 1)
                         for (int w = tid; w < (int)(sizeof(GradRec) / 4); w += kThreads)
-                            ((uint32_t *)&sh.grad[slot])[w] = ((const uint32_t *)&grads[gp.grad])[w];
-                    __syncthreads();
-                    if (sh.paint[slot].flags & PAINT_SKIP) continue;
+                            ((uint32_t *)&sh.win[0].grad[slot])[w] = ((const uint32_t *)&grads[gp.grad])[w];
+                    consumer_sync();
+                    if (sh.win[0].paint[slot].flags & PAINT_SKIP) continue;
                     ox = hr.ox; oy = hr.oy;
                     hs = (int)hr.span_off;
                     hn = (int)hr.span_cnt;
@@ -441,21 +533,23 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
                     slot = slot_next++;
                     const int pair = slot * BH + row;
                     // one entry: the closing sentinel alone, nothing covered on this row
-                    if (c.op == CMD_FILL && sh.run_cnt[pair] <= 1) continue;
-                    const int4 geo = sh.slot_geo[slot];
+                    const WinBuf &wb = sh.win[cur_b];
+                    if (c.op == CMD_FILL && wb.run_cnt[pair] <= 1) continue;
+                    const int4 geo = wb.slot_geo[slot];
                     ox = geo.y; oy = geo.z;
-                    rp = run_base(sh, rovf, rovf_cap, pair);
+                    rp = run_base(wb, rovf + (size_t)cur_b * kMaxPairs * rovf_cap, rovf_cap, pair);
                     if (c.op == CMD_FILL) {
                         // pixel i sits at layer x = x0 - ox + lr + i * tpr
-                        const int2 e = sh.run_ext[pair];
+                        const int2 e = wb.run_ext[pair];
                         const int32_t b0 = wi.x0 - ox + lr;
                         const int32_t n0 = e.x - b0, n1 = e.y - b0;
                         i_lo = n0 <= 0 ? 0 : (n0 + tpr - 1) / tpr;
                         i_hi = n1 <= 0 ? 0 : min(PX, (n1 + tpr - 1) / tpr);
                     }
                 }
-                const PaintRec &pr = sh.paint[slot];
-                const GradRec *gr = &sh.grad[slot];  // read only for gradient paints
+                const WinBuf &pb = sh.win[hair ? 0u : cur_b];
+                const PaintRec &pr = pb.paint[slot];
+                const GradRec *gr = &pb.grad[slot];  // read only for gradient paints
                 const int32_t ly = cy - oy;
                 const int32_t lrow0 = (int32_t)wi.band * BH - oy;
 #pragma unroll 1
@@ -508,8 +602,12 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
                     if (!hair) break;
                 }
             } else if (c.op == CMD_PUSH) {
-                __syncthreads();
-                if (depth + 1 >= kMaxDepth || (uint32_t)depth >= stack_depth) { atomicOr(err, 4u); break; }
+                consumer_sync();
+                if (depth + 1 >= kMaxDepth || (uint32_t)depth >= stack_depth) {
+                    atomicOr(err, 4u);
+                    sh.abort = 1;
+                    break;
+                }
                 uint32_t *lvl = stack + (size_t)depth * kThreads * PX;
                 for (int i = 0; i < PX; i++) lvl[i * kThreads + tid] = layer[i * kThreads + tid];
                 depth++;
@@ -525,10 +623,14 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
                     layer[i * kThreads + tid] = v;
                 }
                 if (tid == 0) sh.rects[depth] = make_int4(L.x, L.y, L.w, L.h);
-                __syncthreads();
+                consumer_sync();
             } else if (c.op == CMD_POP_COMPOSITE || c.op == CMD_POP_CLIP || c.op == CMD_POP_MASK) {
-                if (depth == 0) { atomicOr(err, 4u); break; }
-                __syncthreads();
+                if (depth == 0) {
+                    atomicOr(err, 4u);
+                    sh.abort = 1;
+                    break;
+                }
+                consumer_sync();
                 depth--;
                 const uint32_t *lvl = stack + (size_t)depth * kThreads * PX;
                 const int4 p4 = sh.rects[depth], t = sh.rects[depth + 1];
@@ -558,6 +660,8 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
                 break;
             }
         }
+        if (nwin) mb_arrive(&sh.mb_free[(win_base + nwin - 1u) & 1u]);
+        win_base += nwin;
         if (depth != 0) atomicOr(err, 8u);
         for (int i = 0; i < PX; i++) {
             const int32_t x = wi.x0 + i * tpr + lr;
@@ -585,7 +689,7 @@ cudaError_t launch_raster(int px, uint32_t grid, uint32_t stack_depth, const Str
                           const uint32_t *bin_offsets, const uint32_t *bin_counts, uint32_t *stack, int2 *span_ovf,
                           uint32_t ovf_cap, int2 *run_ovf, uint32_t run_ovf_cap, const HairRec *hairs, const HairSpan *hair_spans, uint32_t *err,
                           cudaStream_t s) {
-    k_raster<<<grid, kThreads, raster_smem_bytes_px(px), s>>>(px, streams, items, nitems, item_counter, cmds, fill_cmds, draws, paints,
+    k_raster<<<grid, kBlock, raster_smem_bytes_px(px), s>>>(px, streams, items, nitems, item_counter, cmds, fill_cmds, draws, paints,
                                                               grads, layers, bins, bin_offsets, bin_counts, stack,
                                                               stack_depth, span_ovf, ovf_cap, run_ovf, run_ovf_cap, hairs,
                                                               hair_spans, err);
@@ -594,7 +698,7 @@ cudaError_t launch_raster(int px, uint32_t grid, uint32_t stack_depth, const Str
 
 int raster_max_blocks_per_sm(int px) {
     int n = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_raster, kThreads, raster_smem_bytes_px(px));
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_raster, kBlock, raster_smem_bytes_px(px));
     if (e != cudaSuccess || n < 1) { cudaGetLastError(); n = 1; }
     return n;
 }
