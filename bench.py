@@ -44,7 +44,8 @@ CONFIG_DESC = {
     4: "differentiable: 256 scenes of 256x256, 64 closed cubic paths (4-16 segments), solid/4-stop linear "
        "gradient paints, one Gaussian blur (learnable sigma), L2 loss against a perturbed target",
 }
-TUNING_CANDIDATES = [(1, 4), (2, 4), (4, 4), (8, 4), (2, 8), (4, 8), (8, 8), (4, 16), (8, 16)]
+# (band rows, pixels per thread); band rows 0 = chosen per stream from its width
+TUNING_CANDIDATES = [(0, 8), (0, 16), (1, 4), (2, 4), (4, 4), (2, 8), (4, 8), (8, 8), (4, 16), (8, 16)]
 SEED = 2026
 
 
@@ -317,9 +318,11 @@ def run_batched(args, rank, world):
         R.render_device(trees[i], ident[i], ws[i], hs[i], ptrs[i], ws[i] * 4, sh)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
+    plain_raster_ms = 0.0
     for i in psamp:
         R.render_device(trees[i], ident[i], ws[i], hs[i], ptrs[i], ws[i] * 4, sh)
         stream.synchronize()
+        plain_raster_ms += R.stats()["raster_ms"]
     plain_s = time.perf_counter() - t0
     plain_value = len(psamp) / plain_s
     # end to end through the public batch call: flatten + upload + render + read back every output
@@ -359,6 +362,7 @@ def run_batched(args, rank, world):
                    "prepare_s": prep_s, "l2": "outputs %.1f GB > L2" % (total / 1e9), "graph_replay": True},
         "mpix_s": value * out_px / n / 1e6 if n else 0.0,
         "plain": {"value": plain_value, "unit": "scenes/s", "sample_scenes": len(psamp),
+                  "raster_kernel_share": plain_raster_ms * 1e-3 / plain_s,
                   "how": "rgpu_render_device per scene (host flatten + upload + kernels), synchronised"},
         "batched_vs_plain": value / plain_value,
         "raster_ms": rms,

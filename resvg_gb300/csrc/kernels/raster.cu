@@ -37,6 +37,15 @@ constexpr int kMaxPairs = kThreads / 4;  // (slot, row) pairs per window: K x BH
 constexpr int kRunCap = 32;     // alpha runs per (slot, row) kept in shared memory
 constexpr int kRunStride = kRunCap + 1;
 
+// A work item taken from the queue, with its stream (idx >= the item count:
+// the queue is empty and both roles stop).
+struct ItemInfo {
+    int32_t idx;
+    int32_t _pad[3];
+    WorkItem wi;
+    StreamRec st;
+};
+
 // One phase-A window as the consumers read it: the window's paints, gradients
 // and draw origins, and per (slot, row) the alpha runs.  Two of them alternate:
 // the producers fill one while the consumers shade from the other.
@@ -55,10 +64,11 @@ struct VmShared {
     unsigned long long mb_ready[2];  // mbarriers: window in buffer b produced (kProducers arrivals)
     unsigned long long mb_free[2];   // buffer b consumed (kThreads arrivals)
     int32_t abort;                   // set on an error: the rest of the launch skips work and waits
+    unsigned long long mb_item_ready[2];  // item ring entry filled (1 arrival: producer 0)
+    unsigned long long mb_item_free[2];   // item ring entry done with (kThreads arrivals)
     int4 rects[kMaxDepth];       // layer-stack rects (x, y, w, h) by depth, the top one at [depth]
-    WorkItem wi;                 // the work item being rendered, and its stream
-    StreamRec st;
-    int32_t item;
+    ItemInfo items[2];           // ring of work items: producers fetch ahead of the consumers
+    ItemInfo cur;                // the consumers' current item (a copy: the ring entry is released early)
     // followed by the top layer: kThreads * px uint32 pixels (dynamic)
 };
 
@@ -93,8 +103,10 @@ __device__ __forceinline__ bool mb_wait(unsigned long long *mb, uint32_t parity,
     *const_cast<volatile int32_t *>(abort) = 1;
     return false;
 }
-// barrier of the consumer threads only (named barrier 1)
+// barriers of the consumer threads only (named barrier 1) and of the producer
+// threads only (named barrier 2)
 __device__ __forceinline__ void consumer_sync() { asm volatile("bar.sync 1, %0;" ::"n"(kThreads) : "memory"); }
+__device__ __forceinline__ void producer_sync() { asm volatile("bar.sync 2, %0;" ::"n"(kProducers) : "memory"); }
 
 __device__ __forceinline__ int32_t round16(int32_t x) { return (int32_t)((uint32_t)x + 0x8000u) >> 16; }
 
@@ -348,13 +360,14 @@ __device__ __forceinline__ uint32_t hair_cov(const HairSpan *hsp, int32_t px, in
 // A for two (slot, sub-scanline) tasks per thread, then merge each (slot, row)
 // into alpha runs (a row's tasks sit in one warp, so a warp barrier orders
 // them).
-__device__ __forceinline__ void produce_window(VmShared &sh, WinBuf &wb, int pt, uint32_t wfirst, const Cmd *cmds,
+__device__ __forceinline__ void produce_window(VmShared &sh, const ItemInfo &itm, WinBuf &wb, int pt, uint32_t wfirst,
+                                               const Cmd *cmds,
                                                const uint32_t *fill_cmds, const DrawRec *draws,
                                                const PaintRec *paints, const GradRec *grads, const EdgeRec *bins,
                                                const uint32_t *bin_offsets, const uint32_t *bin_counts, int2 *ovf,
                                                uint32_t ovf_cap, int2 *rovf, uint32_t rovf_cap, uint32_t *err) {
-    const WorkItem &wi = sh.wi;
-    const StreamRec &st = sh.st;
+    const WorkItem &wi = itm.wi;
+    const StreamRec &st = itm.st;
     const int BH = (int)st.band_rows;
     const int S = 4 * BH;
     const int K = min(kThreads / S, kMaxSlots);
@@ -424,48 +437,68 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
         mb_init(&sh.mb_ready[1], kProducers);
         mb_init(&sh.mb_free[0], kThreads);
         mb_init(&sh.mb_free[1], kThreads);
+        mb_init(&sh.mb_item_ready[0], 1);
+        mb_init(&sh.mb_item_ready[1], 1);
+        mb_init(&sh.mb_item_free[0], kThreads);
+        mb_init(&sh.mb_item_free[1], kThreads);
         sh.abort = 0;
     }
     __syncthreads();
     uint32_t win_base = 0;  // windows produced and consumed by this CTA so far
 
-    for (;;) {
-        if (tid == 0) {
-            const int32_t idx = (int32_t)atomicAdd(item_counter, 1u);
-            sh.item = idx;
-            if (idx < (int32_t)nitems) {
-                sh.wi = items[idx];
-                sh.st = streams[sh.wi.stream];
-                sh.rects[0] = make_int4(0, 0, sh.st.out_w, sh.st.out_h);
+    if (tid >= kThreads) {
+        // ---- producers: take items from the queue (up to two ahead of the
+        // consumers) and build each item's windows in order (two buffers ahead)
+        const int pt = tid - kThreads;
+        for (uint32_t seq = 0;; seq++) {
+            const uint32_t is = seq & 1u;
+            if (pt == 0) {
+                if (seq >= 2) mb_wait(&sh.mb_item_free[is], ((seq >> 1) - 1u) & 1u, err, &sh.abort);
+                ItemInfo &w = sh.items[is];
+                const int32_t idx = (int32_t)atomicAdd(item_counter, 1u);
+                w.idx = idx;
+                if (idx < (int32_t)nitems) {
+                    w.wi = items[idx];
+                    w.st = streams[w.wi.stream];
+                }
             }
-        }
-        __syncthreads();
-        const int32_t item_idx = sh.item;
-        __syncthreads();
-        if (item_idx >= (int32_t)nitems) break;
-        // uniform across the CTA: read from shared memory where used
-        const WorkItem &wi = sh.wi;
-        const StreamRec &st = sh.st;
-        const int BH = (int)st.band_rows;
-        const int S = 4 * BH;                 // scanline slots per draw (sub-scanlines for AA)
-        const int K = min(kThreads / S, kMaxSlots);
-        const uint32_t nwin = (st.fill_cnt + (uint32_t)K - 1) / (uint32_t)K;
-        if (tid >= kThreads) {
-            // ---- producers: the item's windows in order, two buffers ahead at most
-            const int pt = tid - kThreads;
+            producer_sync();
+            if (pt == 0) mb_arrive(&sh.mb_item_ready[is]);
+            const ItemInfo &itm = sh.items[is];
+            if (itm.idx >= (int32_t)nitems) break;
+            const int S = 4 * (int)itm.st.band_rows;
+            const int K = min(kThreads / S, kMaxSlots);
+            const uint32_t nwin = (itm.st.fill_cnt + (uint32_t)K - 1) / (uint32_t)K;
             for (uint32_t w = 0; w < nwin; w++) {
                 const uint32_t gw = win_base + w, b = gw & 1u;
                 if (gw >= 2) mb_wait(&sh.mb_free[b], ((gw >> 1) - 1u) & 1u, err, &sh.abort);
                 if (!*(volatile int32_t *)&sh.abort)
-                    produce_window(sh, sh.win[b], pt, w * (uint32_t)K, cmds, fill_cmds, draws, paints, grads, bins,
-                                   bin_offsets, bin_counts, ovf, ovf_cap, rovf + (size_t)b * kMaxPairs * rovf_cap,
-                                   rovf_cap, err);
+                    produce_window(sh, itm, sh.win[b], pt, w * (uint32_t)K, cmds, fill_cmds, draws, paints, grads,
+                                   bins, bin_offsets, bin_counts, ovf, ovf_cap,
+                                   rovf + (size_t)b * kMaxPairs * rovf_cap, rovf_cap, err);
                 mb_arrive(&sh.mb_ready[b]);
             }
             win_base += nwin;
-            __syncthreads();
-            continue;
         }
+        return;
+    }
+
+    for (uint32_t seq = 0;; seq++) {
+        const uint32_t is = seq & 1u;
+        mb_wait(&sh.mb_item_ready[is], (seq >> 1) & 1u, err, &sh.abort);
+        if (tid == 0) {
+            sh.cur = sh.items[is];
+            sh.rects[0] = make_int4(0, 0, sh.cur.st.out_w, sh.cur.st.out_h);
+        }
+        consumer_sync();
+        mb_arrive(&sh.mb_item_free[is]);  // the entry is copied: the producers may refill it
+        if (sh.cur.idx >= (int32_t)nitems) break;
+        const WorkItem &wi = sh.cur.wi;
+        const StreamRec &st = sh.cur.st;
+        const int BH = (int)st.band_rows;
+        const int S = 4 * BH;                 // scanline slots per draw (sub-scanlines for AA)
+        const int K = min(kThreads / S, kMaxSlots);
+        const uint32_t nwin = (st.fill_cnt + (uint32_t)K - 1) / (uint32_t)K;
         // ---- consumers
         const int tpr = kThreads / BH;        // threads per pixel row
         const int row = tid / tpr;
@@ -667,7 +700,7 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
             const int32_t x = wi.x0 + i * tpr + lr;
             if (row_ok && x < wi.x1) *(uint32_t *)(out + (size_t)cy * st.out_stride + 4 * (size_t)x) = layer[i * kThreads + tid];
         }
-        __syncthreads();
+        consumer_sync();  // every consumer is done with the item copy and the layer stack
     }
 }
 
