@@ -17,15 +17,15 @@ namespace rgpu {
 
 constexpr int kMaxGradStops = 12;   // intervals incl. the two constant ends (<= 10 stops after padding)
 
-struct GradRec {
+struct alignas(16) GradRec {
+    float f[kMaxGradStops][4];   // per stop interval: colour = t * f + b (16-byte rows: one vector load)
+    float b[kMaxGradStops][4];
     float ts[6];         // device pixel -> unit gradient space (sx, ky, kx, sy, tx, ty)
     uint32_t flags;      // see GRAD_* below
     uint32_t spread;     // rgpu_spread
     uint32_t n;          // number of t_values / factors / biases
     float fr0, fr1, cdx, cdy;  // two-point conical parameters (unit space)
     float t[kMaxGradStops];
-    float f[kMaxGradStops][4];
-    float b[kMaxGradStops][4];
 };
 enum : uint32_t {
     GRAD_TWO_STOP = 1, GRAD_PAD_CLAMP = 2, GRAD_PREMUL = 4, GRAD_RADIAL_SIMPLE = 8, GRAD_RADIAL_CONICAL = 16

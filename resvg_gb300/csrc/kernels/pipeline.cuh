@@ -246,8 +246,12 @@ __device__ __forceinline__ bool gradient_eval(const GradRec &g, int32_t px, int3
         for (uint32_t i = 1; i < g.n; i++)
             if (t >= g.t[i]) idx++;
     }
-#pragma unroll
-    for (int k = 0; k < 4; k++) c[k] = t * g.f[idx][k] + g.b[idx][k];
+    const float4 fv = reinterpret_cast<const float4 *>(g.f)[idx];
+    const float4 bv = reinterpret_cast<const float4 *>(g.b)[idx];
+    c[0] = t * fv.x + bv.x;
+    c[1] = t * fv.y + bv.y;
+    c[2] = t * fv.z + bv.z;
+    c[3] = t * fv.w + bv.w;
     if ((g.flags & GRAD_PREMUL) && premul_stage) { c[0] *= c[3]; c[1] *= c[3]; c[2] *= c[3]; }
     return true;
 }
