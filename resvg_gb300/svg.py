@@ -53,8 +53,13 @@ NAMED = {
 }
 
 
+class InvalidColor(Unsupported):
+    """A colour value svgtypes would reject."""
+
+
 def parse_color(s: str, current=(0, 0, 0)):
-    """Returns ((r, g, b), alpha) or None for 'none'."""
+    """Returns ((r, g, b), alpha) or None for 'none'; InvalidColor for text
+    svgtypes rejects (including a trailing icc-color(...))."""
     s = s.strip()
     low = s.lower()
     if low == "none":
@@ -75,10 +80,14 @@ def parse_color(s: str, current=(0, 0, 0)):
             return (int(h[0:2], 16), int(h[2:4], 16), int(h[4:6], 16)), 1.0
         if len(h) == 8:
             return (int(h[0:2], 16), int(h[2:4], 16), int(h[4:6], 16)), int(h[6:8], 16) / 255.0
-        raise Unsupported("color " + s)
-    m = re.match(r"rgba?\(([^)]*)\)", low)
+        raise InvalidColor("color " + s)
+    m = re.match(r"rgba?\(([^)]*)\)$", low)
     if m:
         parts = [p.strip() for p in re.split(r"[,\s/]+", m.group(1).strip()) if p.strip()]
+        # svgtypes: the three channels all numbers or all percentages, alpha a number
+        if len(parts) < 3 or len({q.endswith("%") for q in parts[:3]}) != 1 or \
+                (len(parts) > 3 and parts[3].endswith("%")):
+            raise InvalidColor("color " + s)
         vals = []
         for p in parts[:3]:
             if p.endswith("%"):
@@ -127,7 +136,7 @@ def parse_color(s: str, current=(0, 0, 0)):
         if len(parts) > 3:
             a = frac(parts[3])
         return rgb, max(0.0, min(1.0, a))
-    raise Unsupported("color " + s)
+    raise InvalidColor("color " + s)
 
 
 # ---------------------------------------------------------------- numbers, lengths, transforms
@@ -351,7 +360,11 @@ def svg_arc_to_cubics(p0, p1, rx, ry, rot_deg, large, sweep, tol=0.1):
 def parse_path_data(d: str) -> PathB:
     """svgtypes SimplifyingPathParser semantics: absolute coordinates, H/V as
     lines, S/T as reflected curves, arcs as cubics."""
-    toks = re.findall(r"[MmLlHhVvCcSsQqTtAaZz]|" + NUM, d or "")
+    # tokens up to the first character that is neither a command, a number,
+    # whitespace nor a comma: svgtypes stops parsing there
+    d = d or ""
+    stop = re.search(r"[^MmLlHhVvCcSsQqTtAaZz0-9eE+\-.,\s]", d)
+    toks = re.findall(r"[MmLlHhVvCcSsQqTtAaZz]|" + NUM, d[:stop.start()] if stop else d)
     b = PathB()
     i, cmd = 0, None
     cx = cy = sx = sy = 0.0
@@ -596,7 +609,9 @@ class Loader:
             return a[name]
         if inherited or (name in a and a[name].strip() == "inherit"):
             p = self.parent.get(e)
-            while p is not None:
+            hops = 0
+            while p is not None and hops < 10000:
+                hops += 1
                 pa = self.attrs(p)
                 if name in pa and pa[name].strip() != "inherit":
                     return pa[name]
@@ -605,11 +620,31 @@ class Loader:
                 p = self.parent.get(p)
         return None
 
+    def font_size(self, e):
+        """The element's font size in user units: `font-size` resolved down its
+        ancestors (em and % relative to the parent's size), 12 at the root."""
+        chain = []
+        n = e
+        while n is not None and len(chain) < 10000:
+            chain.append(n)
+            n = self.parent.get(n)
+        fs = 12.0
+        for n in reversed(chain):
+            v = self.attrs(n).get("font-size")
+            if v is None or v.strip() == "inherit":
+                continue
+            v = v.strip()
+            try:
+                fs = fs * float(v[:-1]) / 100.0 if v.endswith("%") else parse_length(v, fs, fs)
+            except (Unsupported, ValueError):
+                pass  # named sizes and invalid values keep the inherited size
+        return fs
+
     def num(self, e, name, default, ref=0.0):
         v = self.attrs(e).get(name)
         if v is None:
             return default
-        return parse_length(v, ref)
+        return parse_length(v, ref, self.font_size(e))
 
     def href(self, e):
         h = e.get(XLINK) or e.get("href")
@@ -714,7 +749,22 @@ class Builder(Loader):
             for c in e:
                 self.node(c, g)
         elif tag == "use":
-            self.node(ref, g)
+            # the instanced element inherits from the <use>, not from where it
+            # is defined
+            n = e
+            while n is not None:  # a <use> inside what it references: not rendered
+                if n is ref:
+                    return
+                n = self.parent.get(n)
+            saved = self.parent.get(ref)
+            self.parent[ref] = e
+            try:
+                self.node(ref, g)
+            finally:
+                if saved is None:
+                    self.parent.pop(ref, None)
+                else:
+                    self.parent[ref] = saved
         elif tag == "svg":
             raise Unsupported("nested svg")
         else:
@@ -729,10 +779,17 @@ class Builder(Loader):
         clip = self.ref(a.get("clip-path"))
         mask = self.ref(a.get("mask"))
         filt = a.get("filter")
-        blend = BLEND.get(a.get("mix-blend-mode", "normal").strip(), None)
+        # mix-blend-mode and isolation count only as CSS properties (style), not as
+        # presentation attributes
+        css = {}
+        for part in (e.get("style") or "").split(";"):
+            if ":" in part:
+                k, v = part.split(":", 1)
+                css[k.strip()] = v.strip()
+        blend = BLEND.get(css.get("mix-blend-mode", "normal").strip(), None)
         if blend is None:
             raise Unsupported("blend mode")
-        isolate = a.get("isolation", "auto").strip() == "isolate"
+        isolate = css.get("isolation", "auto").strip() == "isolate"
         if clip == "missing" or mask == "missing":
             return None  # references to missing elements: the element is not rendered
         eid = e.get("id")
@@ -810,7 +867,8 @@ class Builder(Loader):
     def geometry(self, e):
         tag = _tag(e)
         a = self.attrs(e)
-        L = lambda n, d, ref: parse_length(a[n], ref) if n in a else d  # noqa: E731
+        fsz = self.font_size(e) if any(("em" in v or "ex" in v) for v in a.values()) else 12.0
+        L = lambda n, d, ref: parse_length(a[n], ref, fsz) if n in a else d  # noqa: E731
         b = PathB()
         if tag == "path":
             b = parse_path_data(a.get("d", ""))
@@ -903,23 +961,44 @@ class Builder(Loader):
             op = op.strip()
             opacity = float(op[:-1]) / 100 if op.endswith("%") else float(op)
         opacity = max(0.0, min(1.0, opacity))
+        # style.rs convert_paint: an unparseable fill is black, an unparseable
+        # stroke is none; a paint server that yields nothing uses the fallback
+        def fallback_paint(fb):
+            if not fb:
+                return None
+            try:
+                c = parse_color(fb, cur)
+            except InvalidColor:
+                return None
+            if c is None:
+                return None
+            return self.solid(c), opacity * c[1]
+        invalid = (self.solid(((0, 0, 0), 1.0)), opacity) if which == "fill" else None
+        if v in ("context-fill", "context-stroke"):
+            raise Unsupported("paint " + v)
         if v.startswith("url("):
             m = re.match(r"url\(\s*['\"]?#([^'\")]+)['\"]?\s*\)\s*(.*)$", v)
             if not m:
-                raise Unsupported("paint " + v)
+                return invalid
             ref = self.ids.get(m.group(1))
             fallback = m.group(2).strip()
-            if ref is None or _tag(ref) not in ("linearGradient", "radialGradient"):
-                if ref is not None and _tag(ref) == "pattern":
-                    raise Unsupported("pattern")
-                if fallback:
-                    c = parse_color(fallback, cur)
-                    if c is None:
-                        return None
-                    return self.solid(c), opacity * c[1]
+            if fallback:
+                try:
+                    parse_color(fallback, cur)
+                except InvalidColor:
+                    return invalid  # the whole paint value fails to parse
+            if ref is None:
+                return fallback_paint(fallback)
+            if _tag(ref) == "pattern":
+                raise Unsupported("pattern")
+            if _tag(ref) not in ("linearGradient", "radialGradient"):
                 return None
-            return self.gradient(ref, bbox, opacity)
-        c = parse_color(v, cur)
+            g = self.gradient(ref, bbox, opacity)
+            return g if g is not None else fallback_paint(fallback)
+        try:
+            c = parse_color(v, cur)
+        except InvalidColor:
+            return invalid
         if c is None:
             return None
         return self.solid(c), opacity * c[1]
@@ -963,7 +1042,10 @@ class Builder(Loader):
             prev = o
             o = max(0.0, min(1.0, o))
             col = sa.get("stop-color", "black")
-            c = parse_color(col, (0, 0, 0)) or ((0, 0, 0), 0.0)
+            # currentColor: the `color` the stop inherits through its ancestors
+            cur_s = self.get(s, "color")
+            cur_c = parse_color(cur_s) if cur_s is not None else None
+            c = parse_color(col, cur_c[0] if cur_c else (0, 0, 0)) or ((0, 0, 0), 0.0)
             sop = sa.get("stop-opacity", "1").strip()
             sop = float(sop[:-1]) / 100 if sop.endswith("%") else float(sop)
             stops.append([float(np.float32(o)), c[0], c[1] * max(0.0, min(1.0, sop))])
@@ -993,9 +1075,11 @@ class Builder(Loader):
         units = self.grad_attr(ref, "gradientUnits", chain) or "objectBoundingBox"
         spread = {"pad": 0, "reflect": 1, "repeat": 2}.get((self.grad_attr(ref, "spreadMethod", chain) or "pad").strip(), 0)
         gts = parse_transform(self.grad_attr(ref, "gradientTransform", chain) or "")
+        if abs(gts[0] * gts[3] - gts[1] * gts[2]) <= 0.0 or not all(math.isfinite(v) for v in gts):
+            gts = (1.0, 0.0, 0.0, 1.0, 0.0, 0.0)  # a non-invertible gradientTransform reads as none
         p = A.Paint()
         p.spread = spread
-        obb = units.strip() == "objectBoundingBox"
+        obb = units.strip() != "userSpaceOnUse"  # anything else is the default, objectBoundingBox
         if obb:
             if bbox is None or bbox[2] - bbox[0] <= 0 or bbox[3] - bbox[1] <= 0:
                 return None
@@ -1024,9 +1108,11 @@ class Builder(Loader):
             p.r_ = ln("r", 0.5 if obb else diag / 2, diag)
             p.fx = ln("fx", p.cx, self.vbw)
             p.fy = ln("fy", p.cy, self.vbh)
-            p.fr = ln("fr", 0.0, diag)
-            if not p.r_ > 0:
-                return None
+            p.fr = max(ln("fr", 0.0, diag), 0.0)
+            if not p.r_ > 0 and len(stops) >= 2:
+                # paint_server.rs convert_radial: a non-positive r paints the last stop
+                c = stops[-1]
+                return self.solid((c[1], 1.0)), opacity * c[2]
         p.transform = _tf(gts)
         if len(stops) == 1:
             c = stops[0]
@@ -1060,7 +1146,8 @@ class Builder(Loader):
             path.fill_paint, path.fill_opacity = fill[0], float(np.float32(fill[1]))
         path.fill_rule = A.EVENODD if (self.get(e, "fill-rule") or "nonzero").strip() == "evenodd" else A.NONZERO
         sw = self.get(e, "stroke-width")
-        width = parse_length(sw, math.hypot(self.vbw, self.vbh) / math.sqrt(2)) if sw else 1.0
+        fsz = self.font_size(e)
+        width = parse_length(sw, math.hypot(self.vbw, self.vbh) / math.sqrt(2), fsz) if sw else 1.0
         dashes = []
         if width > 0:
             stroke = self.paint(e, "stroke", bbox, "stroke-opacity")
@@ -1068,21 +1155,19 @@ class Builder(Loader):
                 path.stroke_paint, path.stroke_opacity = stroke[0], float(np.float32(stroke[1]))
                 path.stroke_width = float(np.float32(width))
                 ml = self.get(e, "stroke-miterlimit")
-                path.miter_limit = float(ml) if ml else 4.0
-                if path.miter_limit < 1:
-                    path.stroke_paint = -1
+                path.miter_limit = max(float(ml), 1.0) if ml else 4.0  # style.rs: below 1 reads as 1
                 path.line_cap = {"butt": 0, "round": 1, "square": 2}.get((self.get(e, "stroke-linecap") or "butt").strip(), 0)
                 path.line_join = {"miter": 0, "miter-clip": 1, "round": 2, "bevel": 3, "arcs": 0}.get(
                     (self.get(e, "stroke-linejoin") or "miter").strip(), 0)
                 da = self.get(e, "stroke-dasharray")
                 if da and da.strip() != "none":
-                    dashes = [parse_length(x, self.vbw) for x in re.split(r"[\s,]+", da.strip()) if x]
+                    dashes = [parse_length(x, self.vbw, fsz) for x in re.split(r"[\s,]+", da.strip()) if x]
                     if any(d < 0 for d in dashes) or sum(dashes) <= 0:
                         dashes = []
                     elif len(dashes) % 2:
                         dashes = dashes * 2
                     do = self.get(e, "stroke-dashoffset")
-                    path.dash_phase = float(parse_length(do, self.vbw)) if do else 0.0
+                    path.dash_phase = float(parse_length(do, self.vbw, fsz)) if do else 0.0
         if path.fill_paint < 0 and path.stroke_paint < 0:
             return
         if path.stroke_paint < 0:
@@ -1376,22 +1461,30 @@ class Builder(Loader):
                 q.i[0] = q.i[1] = q.i[2] = 0
                 q.f[0] = 0.0
             if tag == "feGaussianBlur":
+                # parser/filter.rs convert_std_dev_attr: one or two numbers, else
+                # 0 0; a negative component becomes 0
                 sd = numbers(c.get("stdDeviation", "0"))
-                sdx, sdy = (sd[0], sd[1]) if len(sd) > 1 else ((sd[0], sd[0]) if sd else (0.0, 0.0))
-                if sdx < 0 or sdy < 0:
-                    sdx = sdy = 0.0
+                sdx, sdy = (sd[0], sd[1]) if len(sd) == 2 else ((sd[0], sd[0]) if len(sd) == 1 else (0.0, 0.0))
                 p.kind = A.FE_BLUR
-                p.f[0], p.f[1] = sdx, sdy
+                p.f[0], p.f[1] = max(sdx, 0.0), max(sdy, 0.0)
             elif tag == "feColorMatrix":
                 p.kind = A.FE_COLOR_MATRIX
                 t = (c.get("type") or "matrix").strip()
                 vals = numbers(c.get("values", ""))
-                if t == "saturate":
+                has_vals = c.get("values") is not None
+                identity = [1, 0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 1, 0]
+                # parser/filter.rs convert_color_matrix_kind: saturate and hueRotate
+                # without `values` fall back to the identity matrix
+                if t == "saturate" and has_vals:
                     p.i[0] = A.CM_SATURATE
-                    p.f[0] = vals[0] if vals else 1.0
-                elif t == "hueRotate":
+                    p.f[0] = min(max(vals[0], 0.0), 1.0) if vals else 1.0
+                elif t == "hueRotate" and has_vals:
                     p.i[0] = A.CM_HUE_ROTATE
                     p.f[0] = vals[0] if vals else 0.0
+                elif t in ("saturate", "hueRotate"):
+                    p.i[0] = A.CM_MATRIX
+                    for k in range(20):
+                        p.f[k] = identity[k]
                 elif t == "luminanceToAlpha":
                     p.i[0] = A.CM_LUM_TO_ALPHA
                 else:
@@ -1403,10 +1496,21 @@ class Builder(Loader):
             elif tag == "feMorphology":
                 p.kind = A.FE_MORPHOLOGY
                 p.i[0] = 1 if (c.get("operator") or "erode").strip() == "dilate" else 0
-                r = numbers(c.get("radius", "0"))
-                rx, ry = (r[0], r[1]) if len(r) > 1 else ((r[0], r[0]) if r else (0.0, 0.0))
-                if rx < 0 or ry < 0 or (rx == 0 and ry == 0):
-                    rx = ry = 0.0
+                # parser/filter.rs convert_morphology: default 1 1; one or two
+                # numbers (else 0 0); a zero component becomes 1; a negative one
+                # keeps the default
+                rx = ry = 1.0
+                if c.get("radius") is not None:
+                    r = numbers(c.get("radius"))
+                    a, b = (r[0], r[1]) if len(r) == 2 else ((r[0], r[0]) if len(r) == 1 else (0.0, 0.0))
+                    if a == 0 and b == 0:
+                        a = b = 1.0
+                    if a == 0:
+                        a = 1.0
+                    if b == 0:
+                        b = 1.0
+                    if math.copysign(1.0, a) > 0 and math.copysign(1.0, b) > 0:
+                        rx, ry = a, b
                 p.f[0], p.f[1] = rx, ry
             elif tag == "feComposite":
                 p.kind = A.FE_COMPOSITE
