@@ -131,7 +131,7 @@ typedef struct rgpu_mask {
 enum rgpu_prim_kind {
     RGPU_FE_BLUR = 0, RGPU_FE_COLOR_MATRIX, RGPU_FE_MORPHOLOGY, RGPU_FE_COMPOSITE,
     RGPU_FE_CONVOLVE, RGPU_FE_DIFFUSE, RGPU_FE_SPECULAR, RGPU_FE_FLOOD, RGPU_FE_OFFSET,
-    RGPU_FE_MERGE, RGPU_FE_BLEND
+    RGPU_FE_MERGE, RGPU_FE_BLEND, RGPU_FE_COMPONENT_TRANSFER, RGPU_FE_DROP_SHADOW
 };
 
 /* inputs */
@@ -142,6 +142,8 @@ enum rgpu_cm_kind { RGPU_CM_MATRIX = 0, RGPU_CM_SATURATE, RGPU_CM_HUE_ROTATE, RG
 enum rgpu_composite_op { RGPU_OP_OVER = 0, RGPU_OP_IN, RGPU_OP_OUT, RGPU_OP_ATOP, RGPU_OP_XOR, RGPU_OP_ARITHMETIC };
 enum rgpu_edge_mode { RGPU_EDGE_NONE = 0, RGPU_EDGE_DUPLICATE, RGPU_EDGE_WRAP };
 enum rgpu_light_kind { RGPU_LIGHT_DISTANT = 0, RGPU_LIGHT_POINT, RGPU_LIGHT_SPOT };
+enum rgpu_transfer_kind { RGPU_TF_IDENTITY = 0, RGPU_TF_TABLE, RGPU_TF_DISCRETE, RGPU_TF_LINEAR, RGPU_TF_GAMMA };
+#define RGPU_TF_MAX_VALUES 16
 
 /* One filter primitive.  Which fields are meaningful depends on `kind`:
  *   BLUR:         f[0]=stdDeviationX f[1]=stdDeviationY
@@ -161,6 +163,12 @@ enum rgpu_light_kind { RGPU_LIGHT_DISTANT = 0, RGPU_LIGHT_POINT, RGPU_LIGHT_SPOT
  *   OFFSET:       f[0]=dx f[1]=dy
  *   MERGE:        inputs in merge_inputs[i[0] .. i[0]+i[1])
  *   BLEND:        i[0]=rgpu_blend
+ *   COMPONENT_TRANSFER: channel c = 0..3 (R, G, B, A): i[c]=rgpu_transfer_kind,
+ *                 i[4+c]=number of table values (table, discrete; at most
+ *                 RGPU_TF_MAX_VALUES); parameters at f[16*c ..]: the table values,
+ *                 or slope, intercept (linear), or amplitude, exponent, offset (gamma)
+ *   DROP_SHADOW:  i[0..2]=flood rgb; f[0]=stdDeviationX f[1]=stdDeviationY
+ *                 f[2]=dx f[3]=dy f[4]=opacity (flood-opacity times the colour's alpha)
  */
 #define RGPU_PRIM_F 64
 typedef struct rgpu_primitive {

@@ -11,6 +11,8 @@
 //   crates/resvg/src/filter/iir_blur.rs       IIR blur (f64)
 //   crates/resvg/src/filter/color_matrix.rs, morphology.rs, composite.rs, convolve_matrix.rs
 //   crates/resvg/src/filter/lighting.rs        diffuse / specular lighting, mod.rs:1020-1098 drivers
+//   crates/resvg/src/filter/component_transfer.rs  transfer functions, mod.rs:891-903 driver
+//   crates/resvg/src/filter/mod.rs:581-649   apply_drop_shadow
 // The two sRGB <-> linearRGB tables are resvg's (mod.rs:161-238): both are
 // the standard transfer functions evaluated and rounded to u8 (a data table
 // has to be identical to give identical output).
@@ -524,6 +526,75 @@ struct Result { Image image; };
 }  // namespace
 
 // mod.rs:335-521 apply/apply_inner + mod.rs:1100-1114 apply_to_canvas
+// ---- component transfer (component_transfer.rs:10-78), on demultiplied pixels
+bool transfer_is_dummy(const rgpu_primitive &p, int ch) {
+    switch (p.i[ch]) {
+    case RGPU_TF_TABLE:
+    case RGPU_TF_DISCRETE: return p.i[4 + ch] <= 0;
+    case RGPU_TF_LINEAR:
+    case RGPU_TF_GAMMA: return false;
+    default: return true;
+    }
+}
+uint8_t transfer(const rgpu_primitive &p, int ch, uint8_t c8) {
+    const float *v = p.f + 16 * ch;
+    float c = c8 / 255.0f;
+    switch (p.i[ch]) {
+    case RGPU_TF_TABLE: {
+        const int n = p.i[4 + ch] - 1;
+        float fk = std::floor(c * (float)n);
+        int k = fk >= (float)n ? n : (int)fk;
+        if (k == n) {
+            c = v[k];
+        } else {
+            const float vk = v[k], vk1 = v[k + 1];
+            const float kf = (float)k, nf = (float)n;
+            c = vk + (c - kf / nf) * nf * (vk1 - vk);
+        }
+        break;
+    }
+    case RGPU_TF_DISCRETE: {
+        const int n = p.i[4 + ch];
+        float fk = std::floor(c * (float)n);
+        int k = fk >= (float)(n - 1) ? n - 1 : (int)fk;
+        c = v[k];
+        break;
+    }
+    case RGPU_TF_LINEAR: c = v[0] * c + v[1]; break;
+    case RGPU_TF_GAMMA: c = v[0] * std::pow(c, v[1]) + v[2]; break;
+    default: break;
+    }
+    return sat_u8f(f32_bound(0.0f, c, 1.0f) * 255.0f);
+}
+// mod.rs:891-903: colour space, demultiply, transfer R, B, G, A, multiply
+void component_transfer(const rgpu_primitive &p, Pixmap &pm) {
+    demultiply_alpha(pm.data);
+    static const int order[4] = {0, 2, 1, 3};
+    for (int oi = 0; oi < 4; oi++) {
+        const int ch = order[oi];
+        if (transfer_is_dummy(p, ch)) continue;
+        for (size_t i = 0; i < pm.data.size(); i += 4) pm.data[i + ch] = transfer(p, ch, pm.data[i + ch]);
+    }
+    multiply_alpha(pm.data);
+}
+
+// ---- drop shadow (mod.rs:581-649)
+// The flood step: Color::from_rgba8(r, g, b, opacity.to_u8()), apply_opacity(alpha / 255),
+// premultiply, to_color_u8.
+void drop_shadow_flood(const rgpu_primitive &p, Pixmap &sh) {
+    const ColorF col = color_from_rgba8((uint8_t)p.i[0], (uint8_t)p.i[1], (uint8_t)p.i[2], to_u8_norm(p.f[4]));
+    auto clamp01 = [](float v) { return std::min(std::max(v, 0.0f), 1.0f); };
+    for (size_t i = 0; i < sh.data.size(); i += 4) {
+        ColorF c = col;
+        c.a = clamp01(c.a * clamp01(sh.data[i + 3] / 255.0f));
+        if (c.a != 1.0f) { c.r = clamp01(c.r * c.a); c.g = clamp01(c.g * c.a); c.b = clamp01(c.b * c.a); }
+        sh.data[i + 0] = sat_u8f(c.r * 255.0f + 0.5f);
+        sh.data[i + 1] = sat_u8f(c.g * 255.0f + 0.5f);
+        sh.data[i + 2] = sat_u8f(c.b * 255.0f + 0.5f);
+        sh.data[i + 3] = sat_u8f(c.a * 255.0f + 0.5f);
+    }
+}
+
 bool filter_apply(const rgpu_tree_view &t, const rgpu_filter &f, const Transform &ts, Pixmap &source) {
     auto fail = [&]() { pixmap_fill(source, ColorF{0, 0, 0, 0}); return false; };
     bool ok;
@@ -552,6 +623,8 @@ bool filter_apply(const rgpu_tree_view &t, const rgpu_filter &f, const Transform
         if (!ok) return fail();
         IntRect subregion;
         if (!rect_to_int_rect(pr, &subregion)) return fail();
+        // mod.rs:384-391: feOffset inherits its subregion from a referenced input
+        if (p.kind == RGPU_FE_OFFSET && p.in1 >= 0 && (size_t)p.in1 < results.size()) subregion = results[p.in1].region;
         bool lin = p.linear_rgb != 0;
         Image res;
         switch (p.kind) {
@@ -619,6 +692,32 @@ bool filter_apply(const rgpu_tree_view &t, const rgpu_filter &f, const Transform
             Image in = get_input(p.in1);
             auto pm = std::make_shared<Pixmap>((uint32_t)region.w, (uint32_t)region.h);
             lighting(p.kind == RGPU_FE_SPECULAR, p, ts, region, *in.image, *pm);
+            res = Image{pm, IntRect{0, 0, (int32_t)pm->width, (int32_t)pm->height}, lin};
+            break;
+        }
+        case RGPU_FE_COMPONENT_TRANSFER: {
+            Image c = into_cs(get_input(p.in1), lin);
+            auto pm = std::make_shared<Pixmap>(*c.image);
+            component_transfer(p, *pm);
+            res = Image{pm, IntRect{0, 0, (int32_t)pm->width, (int32_t)pm->height}, lin};
+            break;
+        }
+        case RGPU_FE_DROP_SHADOW: {
+            Image c = into_cs(get_input(p.in1), lin);
+            float sx, sy;
+            ts.get_scale(&sx, &sy);
+            const float dx = p.f[2] * sx, dy = p.f[3] * sy;
+            Pixmap sh(*c.image);
+            double bx, by;
+            bool box;
+            if (resolve_std_dev(p.f[0], p.f[1], ts, &bx, &by, &box)) {
+                if (box) box_blur(bx, by, sh); else iir_blur(bx, by, sh);
+            }
+            drop_shadow_flood(p, sh);
+            if (lin) into_linear(sh); else into_srgb(sh);
+            auto pm = std::make_shared<Pixmap>(c.image->width, c.image->height);
+            draw_pixmap(*pm, sat_i32(dx), sat_i32(dy), sh, 1.0f, RGPU_BLEND_SOURCE_OVER);
+            draw_pixmap(*pm, 0, 0, *c.image, 1.0f, RGPU_BLEND_SOURCE_OVER);
             res = Image{pm, IntRect{0, 0, (int32_t)pm->width, (int32_t)pm->height}, lin};
             break;
         }

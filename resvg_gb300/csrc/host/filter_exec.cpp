@@ -44,9 +44,91 @@ bool approx_zero_ulps(float v) {
     return a <= 4;
 }
 
+// resolve_std_dev (mod.rs:1119-1142): the sigmas scaled by the transform;
+// false when both are zero; sigmas under 0.05 become 0; a box blur when either
+// is at least 2, else IIR.
+bool resolve_std_dev(const Xf &ts, float sdx, float sdy, float *ox, float *oy, bool *box) {
+    const float sx = std::sqrt(ts.sx * ts.sx + ts.kx * ts.kx);
+    const float sy = std::sqrt(ts.ky * ts.ky + ts.sy * ts.sy);
+    float x = sdx * sx, y = sdy * sy;
+    if (approx_zero_ulps(x) && approx_zero_ulps(y)) return false;
+    if (x < 0.05f) x = 0.0f;
+    if (y < 0.05f) y = 0.0f;
+    *ox = x; *oy = y;
+    *box = x >= 2.0f || y >= 2.0f;
+    return true;
+}
+
+inline uint32_t sat_u8(float v) {
+    if (!(v > 0.0f)) return 0;
+    if (v >= 255.0f) return 255;
+    return (uint32_t)v;
+}
+
+// One channel of feComponentTransfer (component_transfer.rs:41-78) at value c8;
+// the same f32 operations in the same order, NaN saturating to 0.
+uint32_t transfer_value(const rgpu_primitive &p, int ch, uint32_t c8) {
+    const float *v = p.f + 16 * ch;
+    float c = (float)c8 / 255.0f;
+    switch (p.i[ch]) {
+    case RGPU_TF_TABLE: {
+        const int n = p.i[4 + ch] - 1;
+        const float fk = std::floor(c * (float)n);
+        const int k = fk >= (float)n ? n : (int)fk;
+        if (k == n) {
+            c = v[k];
+        } else {
+            const float vk = v[k], vk1 = v[k + 1], kf = (float)k, nf = (float)n;
+            c = vk + (c - kf / nf) * nf * (vk1 - vk);
+        }
+        break;
+    }
+    case RGPU_TF_DISCRETE: {
+        const int n = p.i[4 + ch];
+        const float fk = std::floor(c * (float)n);
+        c = v[fk >= (float)(n - 1) ? n - 1 : (int)fk];
+        break;
+    }
+    case RGPU_TF_LINEAR: c = v[0] * c + v[1]; break;
+    case RGPU_TF_GAMMA: c = v[0] * std::pow(c, v[1]) + v[2]; break;
+    default: break;
+    }
+    const float b = c > 1.0f ? 1.0f : (c >= 0.0f ? c : 0.0f);
+    return sat_u8(b * 255.0f);
+}
+
+// The four channels as one table of packed results; a channel whose function
+// is the identity or an empty table keeps its value (is_dummy).
+bool transfer_lut(const rgpu_primitive &p, uint32_t lut[256], std::string &err) {
+    for (int ch = 0; ch < 4; ch++) {
+        const int kind = p.i[ch];
+        const bool tab = kind == RGPU_TF_TABLE || kind == RGPU_TF_DISCRETE;
+        if (tab && (p.i[4 + ch] < 0 || p.i[4 + ch] > RGPU_TF_MAX_VALUES)) {
+            err = "component transfer table longer than the primitive record";
+            return false;
+        }
+    }
+    for (uint32_t c = 0; c < 256; c++) {
+        uint32_t o = 0;
+        for (int ch = 0; ch < 4; ch++) {
+            const int kind = p.i[ch];
+            const bool dummy = (kind == RGPU_TF_TABLE || kind == RGPU_TF_DISCRETE) ? p.i[4 + ch] == 0
+                               : !(kind == RGPU_TF_LINEAR || kind == RGPU_TF_GAMMA);
+            o |= (dummy ? c : transfer_value(p, ch, c)) << (8 * ch);
+        }
+        lut[c] = o;
+    }
+    return true;
+}
+
+// A filter image: a layer-sized device buffer, its colour space, and the
+// region the reference's Image carries (only feOffset reads it): the filter
+// region for SourceGraphic / SourceAlpha, the primitive subregion after a
+// crop, else the whole image (w < 0 here).
 struct Img {
     uint32_t *p;
     bool linear;
+    IRect reg{0, 0, -1, -1};
 };
 
 struct Runner {
@@ -88,8 +170,21 @@ int run_filter_job(const FilterJob &job, uint32_t *content, uint32_t *result, Fi
             region = IRect{l, tp, rr - l, b - tp};
         }
         if (ok && (region.x != 0 || region.y != 0 || region.w != job.w || region.h != job.h)) {
-            err = "filter region smaller than its layer";
-            return RGPU_ERR_UNSUPPORTED;
+            // A filter region inside a larger layer (several filters on one
+            // element, whose layer is the union of their regions): primitives
+            // whose result has the input's size work on the whole layer as in
+            // the reference; those that make a region-sized image (flood,
+            // composite, merge, blend, lighting) are not expressed here.
+            for (uint32_t pi = 0; pi < f.prim_count; pi++) {
+                switch (t.prims[f.prim_offset + pi].kind) {
+                case RGPU_FE_BLUR: case RGPU_FE_COLOR_MATRIX: case RGPU_FE_MORPHOLOGY: case RGPU_FE_CONVOLVE:
+                case RGPU_FE_OFFSET: case RGPU_FE_COMPONENT_TRANSFER: case RGPU_FE_DROP_SHADOW:
+                    break;
+                default:
+                    err = "filter region smaller than its layer with a region-sized primitive";
+                    return RGPU_ERR_UNSUPPORTED;
+                }
+            }
         }
         std::vector<Img> results;
         bool failed = !ok;
@@ -97,6 +192,11 @@ int run_filter_job(const FilterJob &job, uint32_t *content, uint32_t *result, Fi
             const rgpu_primitive &p = t.prims[f.prim_offset + pi];
             IRect sub;
             if (!map_int_rect(job.ts, p.x, p.y, p.w, p.h, &sub)) { failed = true; break; }
+            // feOffset inherits its subregion from a referenced input (mod.rs:384-391)
+            if (p.kind == RGPU_FE_OFFSET && p.in1 >= 0 && (size_t)p.in1 < results.size()) {
+                sub = results[p.in1].reg;
+                if (sub.w < 0) sub = IRect{0, 0, job.w, job.h};
+            }
             const bool lin = p.linear_rgb != 0;
             auto input = [&](int32_t in) -> Img {
                 if (in >= 0 && (size_t)in < results.size()) return results[in];
@@ -105,22 +205,17 @@ int run_filter_job(const FilterJob &job, uint32_t *content, uint32_t *result, Fi
                     uint32_t *o = r.fresh();
                     r.ck(filter_copy(source, o, r.n, s));
                     r.ck(filter_alpha_only(o, r.n, s));
-                    return Img{o, false};
+                    return Img{o, false, region};
                 }
-                return Img{source, false};
+                return Img{source, false, region};
             };
             Img res{nullptr, lin};
             switch (p.kind) {
             case RGPU_FE_BLUR: {
                 Img in = input(p.in1);
-                float sx, sy;
-                sx = std::sqrt(job.ts.sx * job.ts.sx + job.ts.kx * job.ts.kx);
-                sy = std::sqrt(job.ts.ky * job.ts.ky + job.ts.sy * job.ts.sy);
-                float x = p.f[0] * sx, y = p.f[1] * sy;
-                if (approx_zero_ulps(x) && approx_zero_ulps(y)) { res = in; break; }
-                if (x < 0.05f) x = 0.0f;
-                if (y < 0.05f) y = 0.0f;
-                bool box = x >= 2.0f || y >= 2.0f;
+                float x, y;
+                bool box;
+                if (!resolve_std_dev(job.ts, p.f[0], p.f[1], &x, &y, &box)) { res = in; break; }
                 res = r.private_in(in, lin);
                 if (box) r.ck(filter_box_blur(res.p, r.fresh(), r.w, r.h, x, y, s));
                 else r.ck(filter_iir_blur(res.p, scratch.plane(4 * r.n), r.w, r.h, x, y, s));
@@ -271,6 +366,35 @@ int run_filter_job(const FilterJob &job, uint32_t *content, uint32_t *result, Fi
                 res = Img{o, lin};
                 break;
             }
+            case RGPU_FE_COMPONENT_TRANSFER: {
+                // apply_component_transfer (mod.rs:891-903)
+                uint32_t lut[256];
+                if (!transfer_lut(p, lut, err)) return RGPU_ERR_UNSUPPORTED;
+                res = r.private_in(input(p.in1), lin);
+                r.ck(filter_component_transfer(res.p, r.n, lut, s));
+                break;
+            }
+            case RGPU_FE_DROP_SHADOW: {
+                // apply_drop_shadow (mod.rs:581-649)
+                Img in = r.in_space(input(p.in1), lin);
+                const float sx = std::sqrt(job.ts.sx * job.ts.sx + job.ts.kx * job.ts.kx);
+                const float sy = std::sqrt(job.ts.ky * job.ts.ky + job.ts.sy * job.ts.sy);
+                const float dx = p.f[2] * sx, dy = p.f[3] * sy;
+                Img sh = r.private_in(in, lin);
+                float x, y;
+                bool box;
+                if (resolve_std_dev(job.ts, p.f[0], p.f[1], &x, &y, &box)) {
+                    if (box) r.ck(filter_box_blur(sh.p, r.fresh(), r.w, r.h, x, y, s));
+                    else r.ck(filter_iir_blur(sh.p, scratch.plane(4 * r.n), r.w, r.h, x, y, s));
+                }
+                const uint32_t op8 = sat_u8(p.f[4] * 255.0f + 0.5f);
+                const uint32_t flood = (uint32_t)(uint8_t)p.i[0] | ((uint32_t)(uint8_t)p.i[1] << 8) |
+                                       ((uint32_t)(uint8_t)p.i[2] << 16) | (op8 << 24);
+                uint32_t *o = r.fresh();
+                r.ck(filter_drop_shadow(in.p, sh.p, o, r.w, r.h, sat_i32(dx), sat_i32(dy), flood, lin, s));
+                res = Img{o, lin};
+                break;
+            }
             default:
                 err = "filter primitive not supported on the device";
                 return RGPU_ERR_UNSUPPORTED;
@@ -279,12 +403,13 @@ int run_filter_job(const FilterJob &job, uint32_t *content, uint32_t *result, Fi
                 uint32_t *o = r.fresh();
                 r.ck(filter_copy(res.p, o, r.n, s));
                 if (p.kind == RGPU_FE_OFFSET) {
-                    // feOffset is not cropped
+                    // feOffset is cropped to the region's size at the origin
+                    r.ck(filter_crop(o, r.w, r.h, 0, 0, region.w, region.h, s));
                 } else {
                     int32_t l = sub.x - region.x, tp = sub.y - region.y;
                     r.ck(filter_crop(o, r.w, r.h, l, tp, l + sub.w, tp + sub.h, s));
                 }
-                res = Img{o, res.linear};
+                res = Img{o, res.linear, sub};
             }
             results.push_back(res);
         }

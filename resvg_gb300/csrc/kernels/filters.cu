@@ -310,13 +310,15 @@ uint32_t host_sat_u8(float v) {
     return (uint32_t)v;
 }
 bool g_luts_ready = false;
+// host copy of g_tab, for tables derived from it on the host
+uint8_t g_host_tab[4][256 * 256];
 cudaError_t ensure_luts() {
     if (g_luts_ready) return cudaSuccess;
     cudaError_t e = cudaMemcpyToSymbol(c_srgb_to_linear, kSrgbToLinear, 256);
     if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_linear_to_srgb, kLinearToSrgb, 256);
     // the same f32 operations as demul / mul (host and device division and
     // multiplication are both IEEE round-to-nearest, without contraction)
-    static uint8_t t[4][256 * 256];
+    uint8_t (*t)[256 * 256] = g_host_tab;
     for (uint32_t a = 0; a < 256 && e == cudaSuccess; a++) {
         const float af = (float)a / 255.0f;
         for (uint32_t c = 0; c < 256; c++) {
@@ -332,7 +334,7 @@ cudaError_t ensure_luts() {
             t[TAB_TO_SRGB][(a << 8) | c] = t[TAB_MUL][(a << 8) | kLinearToSrgb[d]];
         }
     }
-    if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_tab, t, sizeof(t));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_tab, g_host_tab, sizeof(g_host_tab));
     if (e == cudaSuccess) g_luts_ready = true;
     return e;
 }
@@ -902,4 +904,84 @@ cudaError_t filter_lighting(const uint32_t *src, uint32_t *dst, int w, int h, co
     return cudaGetLastError();
 }
 
+}  // namespace rgpu
+
+namespace rgpu {
+namespace {
+
+// ---- component transfer (component_transfer.rs): demultiply, the four
+// channel functions as one 256-entry table of packed (r, g, b, a) results,
+// multiply.  The table sits in shared memory; each thread maps four pixels.
+struct Lut256 { uint32_t v[256]; };
+__global__ void k_component_transfer(uint32_t *img, size_t n, Lut256 lut) {
+    __shared__ uint32_t s_lut[256];
+    for (int k = threadIdx.x; k < 256; k += blockDim.x) s_lut[k] = lut.v[k];
+    __syncthreads();
+    auto f = [](uint32_t px) {
+        const uint32_t p = tab_px(TAB_DEMUL, px);
+        const uint32_t o = (s_lut[chn(p, 0)] & 0xFFu) | (s_lut[chn(p, 1)] & 0xFF00u) |
+                           (s_lut[chn(p, 2)] & 0xFF0000u) | (s_lut[chn(p, 3)] & 0xFF000000u);
+        return tab_px(TAB_MUL, o);
+    };
+    RGPU_MAP4(img, n, f);
+}
+
+// ---- drop shadow (mod.rs:581-649), after the shadow copy is blurred: the
+// flooded, colour-space converted shadow is a function of the blurred alpha
+// alone (a 256-entry table); it is drawn at (dx, dy) onto a transparent
+// image, then the input is drawn over it, both source-over.
+__global__ void k_drop_shadow(const uint32_t *in, const uint32_t *shadow, uint32_t *out, int w, int h, int dx,
+                              int dy, Lut256 lut) {
+    __shared__ uint32_t s_lut[256];
+    for (int k = threadIdx.x; k < 256; k += blockDim.x) s_lut[k] = lut.v[k];
+    __syncthreads();
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (size_t)w * h) return;
+    const int x = (int)(i % w), y = (int)(i / w);
+    const int64_t sx = (int64_t)x - dx, sy = (int64_t)y - dy;
+    uint32_t d = 0;
+    if (sx >= 0 && sy >= 0 && sx < w && sy < h)
+        d = dev::composite_pixel(s_lut[shadow[(size_t)sy * w + (size_t)sx] >> 24], 0u, 1.0f, RGPU_BLEND_SOURCE_OVER);
+    out[i] = dev::composite_pixel(in[i], d, 1.0f, RGPU_BLEND_SOURCE_OVER);
+}
+
+}  // namespace
+
+cudaError_t filter_component_transfer(uint32_t *img, size_t n, const uint32_t lut[256], cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    cudaError_t e = ensure_luts();
+    if (e != cudaSuccess) return e;
+    Lut256 l;
+    for (int k = 0; k < 256; k++) l.v[k] = lut[k];
+    k_component_transfer<<<nblk((n + 3) / 4, 256), 256, 0, s>>>(img, n, l);
+    return cudaGetLastError();
+}
+
+cudaError_t filter_drop_shadow(const uint32_t *in, const uint32_t *shadow, uint32_t *out, int w, int h, int dx,
+                               int dy, uint32_t flood, bool linear, cudaStream_t s) {
+    const size_t n = (size_t)w * h;
+    if (n == 0) return cudaSuccess;
+    cudaError_t e = ensure_luts();
+    if (e != cudaSuccess) return e;
+    // Color::from_rgba8(r, g, b, opacity.to_u8()); apply_opacity(alpha / 255) clamps
+    // the product; premultiply (skipped when opaque) clamps each channel;
+    // to_color_u8 rounds v * 255 + 0.5 down.  Then into_srgb / into_linear_rgb.
+    auto clamp01 = [](float v) { return v < 0.0f ? 0.0f : (v > 1.0f ? 1.0f : v); };
+    const float cr = (float)(flood & 0xFFu) / 255.0f, cg = (float)((flood >> 8) & 0xFFu) / 255.0f,
+                cb = (float)((flood >> 16) & 0xFFu) / 255.0f, ca = (float)(flood >> 24) / 255.0f;
+    const int t = linear ? TAB_TO_LINEAR : TAB_TO_SRGB;
+    Lut256 l;
+    for (uint32_t sa = 0; sa < 256; sa++) {
+        const float a = clamp01(ca * clamp01((float)sa / 255.0f));
+        float r = cr, g = cg, b = cb;
+        if (a != 1.0f) { r = clamp01(r * a); g = clamp01(g * a); b = clamp01(b * a); }
+        const uint32_t pa = host_sat_u8(a * 255.0f + 0.5f);
+        const uint32_t pr = host_sat_u8(r * 255.0f + 0.5f), pg = host_sat_u8(g * 255.0f + 0.5f),
+                       pb = host_sat_u8(b * 255.0f + 0.5f);
+        l.v[sa] = (uint32_t)g_host_tab[t][(pa << 8) | pr] | ((uint32_t)g_host_tab[t][(pa << 8) | pg] << 8) |
+                  ((uint32_t)g_host_tab[t][(pa << 8) | pb] << 16) | (pa << 24);
+    }
+    k_drop_shadow<<<nblk(n, 256), 256, 0, s>>>(in, shadow, out, w, h, dx, dy, l);
+    return cudaGetLastError();
+}
 }  // namespace rgpu

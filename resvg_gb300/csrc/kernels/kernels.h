@@ -53,6 +53,12 @@ cudaError_t filter_draw(const uint32_t *src, uint32_t *dst, int w, int h, int dx
                         cudaStream_t s);
 cudaError_t filter_fill(uint32_t *img, size_t n, uint32_t v, cudaStream_t s);
 cudaError_t filter_alpha_only(uint32_t *img, size_t n, cudaStream_t s);
+// feComponentTransfer on a premultiplied image: demultiply, lut[c] holds the
+// four channels' results for value c (r in the low byte), multiply.
+cudaError_t filter_component_transfer(uint32_t *img, size_t n, const uint32_t lut[256], cudaStream_t s);
+// feDropShadow after the shadow copy is blurred; flood = r | g << 8 | b << 16 | opacity_u8 << 24.
+cudaError_t filter_drop_shadow(const uint32_t *in, const uint32_t *shadow, uint32_t *out, int w, int h, int dx,
+                               int dy, uint32_t flood, bool linear, cudaStream_t s);
 
 // feConvolveMatrix (convolve_matrix.rs): kernel k[rows * cols] row-major as
 // given, applied flipped; edge = rgpu_edge_mode.

@@ -155,6 +155,179 @@ def numbers(s):
     return [float(x) for x in re.findall(NUM, s or "")]
 
 
+def number_strict(s):
+    """svgtypes Number::from_str: one number with optional surrounding spaces,
+    else None (usvg then uses the attribute's default)."""
+    if s is None:
+        return None
+    m = re.fullmatch(r"\s*(" + NUM + r")\s*", s)
+    return float(m.group(1)) if m else None
+
+
+_WS = re.compile(r"[ \t\n\r]*")
+_SEP = re.compile(r"[ \t\n\r]*,?")
+_NUM_RE = re.compile(NUM)
+
+
+def number_list_items(s):
+    """svgtypes NumberListParser: numbers separated by spaces and at most one
+    comma; an item that does not parse yields None and ends the list."""
+    out, pos, n = [], 0, len(s or "")
+    while True:
+        pos = _WS.match(s, pos).end()
+        if pos >= n:
+            return out
+        m = _NUM_RE.match(s, pos)
+        if not m:
+            out.append(None)
+            return out
+        out.append(float(m.group(0)))
+        pos = _SEP.match(s, m.end()).end()
+
+
+def number_list_strict(s):
+    """usvg's Vec<f32> attribute: the whole list, or None when any item fails."""
+    items = number_list_items(s)
+    return None if None in items else items
+
+
+def std_dev_attr(text):
+    """parser/filter.rs convert_std_dev_attr: one or two numbers (a third one,
+    or none, gives 0 0); each negative component becomes 0."""
+    n1, n2, n3 = (number_list_items(text) + [None, None, None])[:3]
+    if n1 is not None and n2 is not None and n3 is None:
+        x, y = n1, n2
+    elif n1 is not None and n2 is None:
+        x, y = n1, n1
+    else:
+        x, y = 0.0, 0.0
+    x, y = F(x), F(y)
+    return (float(x) if x >= 0 else 0.0), (float(y) if y >= 0 else 0.0)
+
+
+def opacity_value(s, default=1.0):
+    """usvg's Opacity attribute: a number or a percentage, clamped to [0, 1]."""
+    if s is None:
+        return default
+    m = re.fullmatch(r"\s*(" + NUM + r")\s*(%?)\s*", s)
+    if not m:
+        return default
+    v = float(m.group(1)) / (100.0 if m.group(2) else 1.0)
+    return float(min(max(F(v), F(0.0)), F(1.0)))
+
+
+_LEN_UNITS = ("px", "em", "ex", "in", "cm", "mm", "pt", "pc", "%")
+
+
+def _split_top(s):
+    """Splits at whitespace outside parentheses."""
+    out, depth, cur = [], 0, ""
+    for ch in s:
+        if ch == "(":
+            depth += 1
+        elif ch == ")":
+            depth -= 1
+        if ch in " \t\n\r" and depth == 0:
+            if cur:
+                out.append(cur)
+            cur = ""
+        else:
+            cur += ch
+    if cur:
+        out.append(cur)
+    return out
+
+
+def _css_length(tok):
+    m = re.fullmatch("(" + NUM + r")(px|em|ex|in|cm|mm|pt|pc|%)?", tok)
+    return (float(m.group(1)), m.group(2) or "") if m else None
+
+
+def parse_filter_list(value):
+    """The `filter` property's value as a list of ("url", id) and filter
+    functions (Filter Effects 1, section 12: blur, brightness, contrast,
+    drop-shadow, grayscale, hue-rotate, invert, opacity, saturate, sepia),
+    following svgtypes' FilterValueListParser as usvg consumes it
+    (parser/filter.rs:86-148).  None when any item does not parse: usvg then
+    drops the whole list.  Arguments: a length (number, unit; no percentage)
+    for blur; an amount (a number or a percentage, not negative) for the colour
+    functions; degrees for hue-rotate (a unit is required unless the angle is
+    0); (colour or None, dx, dy, std) for drop-shadow, two or three lengths
+    without percentages and the colour first or last."""
+    out, pos, n = [], 0, len(value)
+    while True:
+        pos = _WS.match(value, pos).end()
+        if pos >= n:
+            return out
+        m = re.compile(r"([A-Za-z-]+)\(").match(value, pos)
+        if not m:
+            return None
+        depth, k = 1, m.end()
+        while k < n and depth:
+            depth += {"(": 1, ")": -1}.get(value[k], 0)
+            k += 1
+        if depth:
+            return None
+        name, arg = m.group(1), value[m.end():k - 1].strip()
+        pos = k
+        if name == "url":
+            out.append(("url", arg.strip("'\"").lstrip("#")))
+        elif name == "blur":
+            if not arg:
+                out.append(("blur", (0.0, "")))
+                continue
+            ln = _css_length(arg)
+            if ln is None or ln[1] == "%" or ln[0] < 0:
+                return None
+            out.append(("blur", ln))
+        elif name in ("brightness", "contrast", "grayscale", "invert", "opacity", "saturate", "sepia"):
+            if not arg:
+                out.append((name, 1.0))
+                continue
+            mm = re.fullmatch("(" + NUM + r")(%?)", arg)
+            if not mm or float(mm.group(1)) < 0:
+                return None
+            out.append((name, float(mm.group(1)) / (100.0 if mm.group(2) else 1.0)))
+        elif name == "hue-rotate":
+            if not arg:
+                out.append((name, 0.0))
+                continue
+            mm = re.fullmatch("(" + NUM + r")(deg|grad|rad|turn)?", arg)
+            if not mm or (mm.group(2) is None and float(mm.group(1)) != 0.0):
+                return None  # an angle needs its unit; only zero may go without
+            v, u = float(mm.group(1)), mm.group(2) or "deg"
+            deg = {"deg": v, "grad": v * 180.0 / 200.0, "rad": math.degrees(v), "turn": v * 360.0}[u]
+            out.append((name, deg))
+        elif name == "drop-shadow":
+            toks = _split_top(arg)
+            color, lens = None, []
+            for i, t in enumerate(toks):
+                ln = _css_length(t)
+                if ln is not None:
+                    if ln[1] == "%":
+                        return None  # lengths only, no percentages
+                    lens.append(ln)
+                    continue
+                if color is not None or (i != 0 and i != len(toks) - 1):
+                    return None
+                if t.lower() == "currentcolor":
+                    color = "current"
+                    continue
+                try:
+                    c = parse_color(t)
+                except (InvalidColor, Unsupported):
+                    return None
+                if c is None:
+                    return None
+                color = c
+            if len(lens) not in (2, 3):
+                return None
+            out.append((name, (None if color == "current" else color, lens[0], lens[1],
+                               lens[2] if len(lens) == 3 else (0.0, ""))))
+        else:
+            return None
+
+
 def parse_length(s, ref=0.0, font_size=12.0):
     s = s.strip()
     m = re.match(r"(" + NUM + r")\s*([a-z%]*)$", s)
@@ -554,8 +727,7 @@ INHERITED = {"fill", "fill-opacity", "fill-rule", "stroke", "stroke-width", "str
 NON_INHERITED = {"opacity", "clip-path", "mask", "filter", "mix-blend-mode", "isolation", "display",
                  "stop-color", "stop-opacity", "flood-color", "flood-opacity", "transform"}
 UNSUPPORTED_ELEMS = {"text", "image", "pattern", "marker", "switch", "foreignObject", "tspan", "textPath", "symbol",
-                     "feImage", "feTile", "feTurbulence", "feDisplacementMap", "feComponentTransfer",
-                     "feDropShadow", "feFuncR",
+                     "feImage", "feTile", "feTurbulence", "feDisplacementMap",
                      "style", "animate", "set"}
 BLEND = {"normal": "source-over", "multiply": "multiply", "screen": "screen", "overlay": "overlay",
          "darken": "darken", "lighten": "lighten", "color-dodge": "color-dodge", "color-burn": "color-burn",
@@ -813,16 +985,24 @@ class Builder(Loader):
                 return None
         fids = []
         if has_filter:
-            for fref in re.findall(r"url\([^)]*\)", filt):
-                fe = self.ref(fref)
-                if fe == "missing" or fe is None:
-                    return None
-                fi = self.filter(fe, bbox)
-                if fi is None:
-                    return None
-                fids.append(fi)
-            if not fids:
-                raise Unsupported("filter functions")
+            # parser/filter.rs convert: a list that does not parse is dropped
+            # whole; urls that resolve to no filter only matter when nothing
+            # else in the list made one (then the element is not rendered)
+            invalid_url = False
+            for fn in parse_filter_list(filt) or []:
+                if fn[0] == "url":
+                    fe = self.ids.get(fn[1])
+                    fi = self.filter(fe, bbox) if fe is not None else None
+                    if fi is None:
+                        invalid_url = True
+                    else:
+                        fids.append(fi)
+                else:
+                    fi = self.filter_function(e, fn, bbox)
+                    if fi is not None:
+                        fids.append(fi)
+            if not fids and invalid_url:
+                return None
         g = _group(transform=_tf(ts), opacity=float(np.float32(opacity)), blend=A.BLEND[blend],
                    isolate=1 if isolate else 0, clip_path=ci, mask=mi)
         gi = self.tree.add_group(parent, g)
@@ -1399,6 +1579,160 @@ class Builder(Loader):
             p.f[11] = fa(light, "limitingConeAngle", np.nan)
         return True
 
+    def attr_color(self, e, name):
+        """An element's own colour attribute as svgtypes parses it and usvg splits
+        it: ((r, g, b), alpha) with the alpha stored as u8; black when absent or
+        invalid."""
+        v = self.attrs(e).get(name)
+        try:
+            c = parse_color(v) if v is not None and v.strip().lower() != "currentcolor" else None
+        except (InvalidColor, Unsupported):
+            c = None
+        if c is None:
+            return (0, 0, 0), 1.0
+        return c[0], float(F(round(c[1] * 255.0)) / F(255.0))
+
+    def component_transfer(self, c, p):
+        """feComponentTransfer as usvg converts it (parser/filter.rs:570-622): per
+        channel the last feFunc child with a known type; `tableValues` that do
+        not parse give an empty table, which leaves the channel unchanged."""
+        p.kind = A.FE_COMPONENT_TRANSFER
+        chans = {"feFuncR": 0, "feFuncG": 1, "feFuncB": 2, "feFuncA": 3}
+        for n in c:
+            ch = chans.get(_tag(n))
+            if ch is None:
+                continue
+            t = n.get("type")
+            t = t.strip() if t is not None else None
+            vals = []
+            if t == "identity":
+                kind = A.TF_IDENTITY
+            elif t in ("table", "discrete"):
+                kind = A.TF_TABLE if t == "table" else A.TF_DISCRETE
+                vals = number_list_strict(n.get("tableValues")) if n.get("tableValues") is not None else []
+                vals = vals or []
+                if len(vals) > A.TF_MAX_VALUES:
+                    raise Unsupported("component transfer table longer than the primitive record")
+            elif t == "linear":
+                kind = A.TF_LINEAR
+                sl, ic = number_strict(n.get("slope")), number_strict(n.get("intercept"))
+                vals = [sl if sl is not None else 1.0, ic if ic is not None else 0.0]
+            elif t == "gamma":
+                kind = A.TF_GAMMA
+                am, ex, of = (number_strict(n.get(k)) for k in ("amplitude", "exponent", "offset"))
+                vals = [am if am is not None else 1.0, ex if ex is not None else 1.0, of if of is not None else 0.0]
+            else:
+                continue
+            p.i[ch] = kind
+            p.i[4 + ch] = len(vals) if kind in (A.TF_TABLE, A.TF_DISCRETE) else 0
+            for k in range(16):
+                p.f[16 * ch + k] = vals[k] if k < len(vals) else 0.0
+
+    def filter_function(self, e, fn, bbox):
+        """One CSS filter function as usvg lowers it (parser/filter.rs:36-84 and
+        :1088-1290): a filter of one sRGB primitive on SourceGraphic whose
+        region is the element's bounding box grown to (-50%, -50%, 200%, 200%)
+        for blur and drop-shadow, (-10%, -10%, 120%, 120%) for the others.
+        None for an element without a bounding box."""
+        if bbox is None or not (bbox[2] > bbox[0] and bbox[3] > bbox[1]):
+            return None
+        name, arg = fn
+        p = A.Primitive()
+        p.linear_rgb = 0
+        p.in1, p.in2 = A.IN_SOURCE_GRAPHIC, A.IN_SOURCE_GRAPHIC
+        one = F(1.0)
+
+        def length(ln, horizontal):
+            # units.rs convert_user_length with AId::Dx / AId::Dy
+            v, u = F(ln[0]), ln[1]
+            if u in ("", "px"):
+                return v
+            if u == "%":
+                return F(F(F(self.vbw if horizontal else self.vbh) * v) / F(100.0))
+            if u in ("em", "ex"):
+                r = F(v * F(self.font_size(e)))
+                return F(r / F(2.0)) if u == "ex" else r
+            return F(F(v * F(96.0)) / F({"in": 1.0, "cm": 2.54, "mm": 25.4, "pt": 72.0, "pc": 6.0}[u]))
+
+        def table(ch, vals):
+            p.i[ch], p.i[4 + ch] = A.TF_TABLE, len(vals)
+            for k, v in enumerate(vals):
+                p.f[16 * ch + k] = float(v)
+
+        def matrix(rows):
+            p.kind = A.FE_COLOR_MATRIX
+            p.i[0] = A.CM_MATRIX
+            for k, v in enumerate(rows):
+                p.f[k] = float(v)
+        if name == "blur":
+            p.kind = A.FE_BLUR
+            sd = length(arg, True)
+            p.f[0] = p.f[1] = float(sd) if sd >= 0 else 0.0
+        elif name == "drop-shadow":
+            p.kind = A.FE_DROP_SHADOW
+            col, dx, dy, sd = arg
+            if col is None:
+                try:
+                    col = parse_color(self.get(e, "color") or "black")
+                except (InvalidColor, Unsupported):
+                    col = None
+                col = col or ((0, 0, 0), 1.0)
+            p.i[0], p.i[1], p.i[2] = col[0]
+            sd = length(sd, True)
+            p.f[0] = p.f[1] = float(sd) if sd >= 0 else 0.0
+            p.f[2], p.f[3] = float(length(dx, True)), float(length(dy, False))
+            p.f[4] = float(F(round(col[1] * 255.0)) / F(255.0))
+        elif name in ("brightness", "contrast"):
+            p.kind = A.FE_COMPONENT_TRANSFER
+            a = F(arg)
+            icpt = F(0.0) if name == "brightness" else F(F(-F(F(0.5) * a)) + F(0.5))
+            for ch in range(3):
+                p.i[ch] = A.TF_LINEAR
+                p.f[16 * ch], p.f[16 * ch + 1] = float(a), float(icpt)
+        elif name == "invert":
+            p.kind = A.FE_COMPONENT_TRANSFER
+            a = F(min(arg, 1.0))
+            for ch in range(3):
+                table(ch, [a, F(one - a)])
+        elif name == "opacity":
+            p.kind = A.FE_COMPONENT_TRANSFER
+            table(3, [F(0.0), F(min(arg, 1.0))])
+        elif name in ("grayscale", "sepia"):
+            a = F(min(arg, 1.0))
+            r = F(one - a)
+            if name == "grayscale":
+                base = [(0.2126, 0.7874), (0.7152, -0.7152), (0.0722, -0.0722),
+                        (0.2126, -0.2126), (0.7152, 0.2848), (0.0722, -0.0722),
+                        (0.2126, -0.2126), (0.7152, -0.7152), (0.0722, 0.9278)]
+            else:
+                base = [(0.393, 0.607), (0.769, -0.769), (0.189, -0.189),
+                        (0.349, -0.349), (0.686, 0.314), (0.168, -0.168),
+                        (0.272, -0.272), (0.534, -0.534), (0.131, 0.869)]
+            m = []
+            for k, (b0, b1) in enumerate(base):
+                t = F(F(abs(b1)) * r)
+                m.append(F(F(b0) + t) if b1 > 0 else F(F(b0) - t))
+                if k % 3 == 2:
+                    m += [F(0.0), F(0.0)]
+            matrix(m + [0.0, 0.0, 0.0, 1.0, 0.0])
+        elif name == "saturate":
+            p.kind = A.FE_COLOR_MATRIX
+            p.i[0] = A.CM_SATURATE
+            p.f[0] = float(max(F(arg), F(0.0)))
+        elif name == "hue-rotate":
+            p.kind = A.FE_COLOR_MATRIX
+            p.i[0] = A.CM_HUE_ROTATE
+            p.f[0] = float(F(arg))
+        big = name in ("blur", "drop-shadow")
+        rx, rw = (F(-0.5), F(2.0)) if big else (F(-0.1), F(1.2))
+        bx, by = F(bbox[0]), F(bbox[1])
+        bw, bh = F(F(bbox[2]) - bx), F(F(bbox[3]) - by)
+        f = A.Filter()
+        f.x, f.y = float(F(F(rx * bw) + bx)), float(F(F(rx * bh) + by))
+        f.w, f.h = float(F(rw * bw)), float(F(rw * bh))
+        p.x, p.y, p.w, p.h = f.x, f.y, f.w, f.h
+        return self.tree.add_filter(f, [p], [])
+
     def filter(self, fe, bbox):
         if _tag(fe) != "filter":
             return None
@@ -1439,8 +1773,8 @@ class Builder(Loader):
             cif = (self.get(c, "color-interpolation-filters") or "linearRGB").strip()
             p.linear_rgb = 0 if cif == "sRGB" else 1
 
-            def inp(name):
-                v = c.get(name)
+            def inp(name, node=c):
+                v = node.get(name)
                 if v is None:
                     return len(prims) - 1 if prims else A.IN_SOURCE_GRAPHIC
                 v = v.strip()
@@ -1451,7 +1785,7 @@ class Builder(Loader):
                 if v in names:
                     return names[v]
                 if v in ("BackgroundImage", "BackgroundAlpha", "FillPaint", "StrokePaint"):
-                    raise Unsupported("input " + v)
+                    return A.IN_SOURCE_GRAPHIC  # parser/filter.rs parse_in: not supported, SourceGraphic
                 return len(prims) - 1 if prims else A.IN_SOURCE_GRAPHIC
             p.in1 = inp("in")
 
@@ -1463,10 +1797,8 @@ class Builder(Loader):
             if tag == "feGaussianBlur":
                 # parser/filter.rs convert_std_dev_attr: one or two numbers, else
                 # 0 0; a negative component becomes 0
-                sd = numbers(c.get("stdDeviation", "0"))
-                sdx, sdy = (sd[0], sd[1]) if len(sd) == 2 else ((sd[0], sd[0]) if len(sd) == 1 else (0.0, 0.0))
                 p.kind = A.FE_BLUR
-                p.f[0], p.f[1] = max(sdx, 0.0), max(sdy, 0.0)
+                p.f[0], p.f[1] = std_dev_attr(c.get("stdDeviation", "0 0"))
             elif tag == "feColorMatrix":
                 p.kind = A.FE_COLOR_MATRIX
                 t = (c.get("type") or "matrix").strip()
@@ -1529,23 +1861,26 @@ class Builder(Loader):
                 p.f[0] = max(0.0, min(1.0, fo)) * col[1]
             elif tag == "feOffset":
                 p.kind = A.FE_OFFSET
-                p.f[0], p.f[1] = float(c.get("dx", "0")), float(c.get("dy", "0"))
+                dx, dy = number_strict(c.get("dx")), number_strict(c.get("dy"))
+                p.f[0], p.f[1] = dx if dx is not None else 0.0, dy if dy is not None else 0.0
+            elif tag == "feComponentTransfer":
+                self.component_transfer(c, p)
+            elif tag == "feDropShadow":
+                # parser/filter.rs convert_drop_shadow: stdDeviation "2 2", dx and dy
+                # numbers (default 2), flood colour and opacity as feFlood
+                p.kind = A.FE_DROP_SHADOW
+                p.f[0], p.f[1] = std_dev_attr(c.get("stdDeviation", "2 2"))
+                dx, dy = number_strict(c.get("dx")), number_strict(c.get("dy"))
+                p.f[2], p.f[3] = dx if dx is not None else 2.0, dy if dy is not None else 2.0
+                rgb, alpha = self.attr_color(c, "flood-color")
+                p.i[0], p.i[1], p.i[2] = rgb
+                p.f[4] = float(F(alpha) * F(opacity_value(self.attrs(c).get("flood-opacity"))))
             elif tag == "feMerge":
                 p.kind = A.FE_MERGE
                 ins = []
                 for n in c:
                     if _tag(n) == "feMergeNode":
-                        v = n.get("in")
-                        if v is None:
-                            ins.append(len(prims) - 1 if prims else A.IN_SOURCE_GRAPHIC)
-                        elif v == "SourceGraphic":
-                            ins.append(A.IN_SOURCE_GRAPHIC)
-                        elif v == "SourceAlpha":
-                            ins.append(A.IN_SOURCE_ALPHA)
-                        elif v in names:
-                            ins.append(names[v])
-                        else:
-                            raise Unsupported("merge input")
+                        ins.append(inp("in", n))
                 p.i[0], p.i[1] = len(merge), len(ins)
                 merge += ins
             elif tag == "feBlend":

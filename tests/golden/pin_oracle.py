@@ -47,7 +47,7 @@ CATEGORIES = [
     "filters/feFlood", "filters/feOffset", "filters/feMerge", "filters/feBlend", "filters/filter",
     "filters/feConvolveMatrix", "filters/feDiffuseLighting", "filters/feSpecularLighting",
     "filters/feDistantLight", "filters/fePointLight", "filters/feSpotLight",
-    "filters/filter-functions",
+    "filters/filter-functions", "filters/feComponentTransfer", "filters/feDropShadow",
 ]
 IMAGE_SIZE = 300
 FIXTURES_PER_DIR = 4

@@ -62,3 +62,47 @@ def test_rect_corners_in_f32(native):
     pts = np.ctypeslib.as_array(v.points, shape=(v.point_count * 2,))[2 * p.point_offset:2 * (p.point_offset + 2)]
     f = np.float32
     assert pts[0] == f(0.2) + f(0.1) and pts[2] == (f(0.2) + f(0.6)) - f(0.1)
+
+
+def test_number_lists_as_usvg_reads_them():
+    assert svg.number_list_strict("1 0,0.5 -1e1") == [1.0, 0.0, 0.5, -10.0]
+    assert svg.number_list_strict("100-100") == [100.0, -100.0]
+    assert svg.number_list_strict("1px") is None
+    assert svg.number_list_strict("") == []
+    assert svg.number_strict(" 0.5 ") == 0.5
+    assert svg.number_strict("0.5px") is None and svg.number_strict("50%") is None
+    # stdDeviation: one or two numbers, else 0 0; negative components become 0
+    assert svg.std_dev_attr("3") == (3.0, 3.0)
+    assert svg.std_dev_attr("3 -1") == (3.0, 0.0)
+    assert svg.std_dev_attr("1 2 3") == (0.0, 0.0)
+    assert svg.std_dev_attr("4 x") == (4.0, 4.0)
+    assert svg.opacity_value("50%") == 0.5 and svg.opacity_value("2") == 1.0
+
+
+def test_filter_function_list():
+    fl = svg.parse_filter_list("grayscale() url(#a) hue-rotate(0.25turn) blur(1mm) opacity(50%)")
+    assert fl[0] == ("grayscale", 1.0) and fl[1] == ("url", "a")
+    assert fl[2] == ("hue-rotate", 90.0) and fl[3] == ("blur", (1.0, "mm")) and fl[4] == ("opacity", 0.5)
+    ds = svg.parse_filter_list("drop-shadow(4 5 6 blue)")[0]
+    assert ds[0] == "drop-shadow" and ds[1][0] == ((0, 0, 255), 1.0) and ds[1][3] == (6.0, "")
+    assert svg.parse_filter_list("drop-shadow(currentColor 1 2)")[0][1][0] is None
+    # any item that does not parse drops the whole list
+    for bad in ("blur(4 2)", "blur(50%)", "blur(-5)", "drop-shadow(red, 10, 15)", "drop-shadow(4)",
+                "drop-shadow(blue 4 5 6 7)", "drop-shadow(blue 3% 4% 5%)", "hue-rotate(45)",
+                "grayscale() hue-rotate(random) opacity(0.5)", "contrast(-1)", "bogus(1)"):
+        assert svg.parse_filter_list(bad) is None, bad
+    assert svg.parse_filter_list("hue-rotate(0)") == [("hue-rotate", 0.0)]
+
+
+def test_component_transfer_record():
+    text = ('<svg viewBox="0 0 10 10" xmlns="http://www.w3.org/2000/svg"><filter id="f">'
+            '<feComponentTransfer><feFuncB type="table" tableValues="0 0 1 1"/>'
+            '<feFuncB type="table" tableValues="1 1 0 0"/><feFuncR type="random"/>'
+            '<feFuncA type="gamma" amplitude="2px" offset="0.5"/></feComponentTransfer></filter>'
+            '<rect width="5" height="5" filter="url(#f)"/></svg>')
+    tree = svg.load_svg(text)
+    p = tree.view().contents.prims[0]
+    assert p.kind == A.FE_COMPONENT_TRANSFER
+    assert p.i[0] == A.TF_IDENTITY and p.i[2] == A.TF_TABLE and p.i[6] == 4
+    assert list(p.f[32:36]) == [1.0, 1.0, 0.0, 0.0]       # the later feFuncB wins
+    assert p.i[3] == A.TF_GAMMA and list(p.f[48:51]) == [1.0, 1.0, 0.5]   # invalid amplitude: default
