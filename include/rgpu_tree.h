@@ -131,7 +131,8 @@ typedef struct rgpu_mask {
 enum rgpu_prim_kind {
     RGPU_FE_BLUR = 0, RGPU_FE_COLOR_MATRIX, RGPU_FE_MORPHOLOGY, RGPU_FE_COMPOSITE,
     RGPU_FE_CONVOLVE, RGPU_FE_DIFFUSE, RGPU_FE_SPECULAR, RGPU_FE_FLOOD, RGPU_FE_OFFSET,
-    RGPU_FE_MERGE, RGPU_FE_BLEND, RGPU_FE_COMPONENT_TRANSFER, RGPU_FE_DROP_SHADOW
+    RGPU_FE_MERGE, RGPU_FE_BLEND, RGPU_FE_COMPONENT_TRANSFER, RGPU_FE_DROP_SHADOW,
+    RGPU_FE_TURBULENCE, RGPU_FE_TILE, RGPU_FE_DISPLACEMENT_MAP
 };
 
 /* inputs */
@@ -169,7 +170,14 @@ enum rgpu_transfer_kind { RGPU_TF_IDENTITY = 0, RGPU_TF_TABLE, RGPU_TF_DISCRETE,
  *                 or slope, intercept (linear), or amplitude, exponent, offset (gamma)
  *   DROP_SHADOW:  i[0..2]=flood rgb; f[0]=stdDeviationX f[1]=stdDeviationY
  *                 f[2]=dx f[3]=dy f[4]=opacity (flood-opacity times the colour's alpha)
+ *   TURBULENCE:   f[0]=baseFrequencyX f[1]=baseFrequencyY (both >= 0); i[0]=numOctaves
+ *                 (at most RGPU_TURB_MAX_OCTAVES on the device) i[1]=seed
+ *                 i[2]=stitchTiles i[3]=1 fractalNoise, 0 turbulence
+ *   TILE:         in1 only
+ *   DISPLACEMENT_MAP: i[0]=xChannelSelector i[1]=yChannelSelector (0..3 = R, G, B, A);
+ *                 f[0]=scale; in1 = the image displaced, in2 = the map
  */
+#define RGPU_TURB_MAX_OCTAVES 1024
 #define RGPU_PRIM_F 64
 typedef struct rgpu_primitive {
     uint32_t kind;

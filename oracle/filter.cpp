@@ -13,6 +13,8 @@
 //   crates/resvg/src/filter/lighting.rs        diffuse / specular lighting, mod.rs:1020-1098 drivers
 //   crates/resvg/src/filter/component_transfer.rs  transfer functions, mod.rs:891-903 driver
 //   crates/resvg/src/filter/mod.rs:581-649   apply_drop_shadow
+//   crates/resvg/src/filter/turbulence.rs, mod.rs:988-1018 apply_turbulence
+//   crates/resvg/src/filter/mod.rs:835-859 apply_tile, displacement_map.rs + mod.rs:958-986
 // The two sRGB <-> linearRGB tables are resvg's (mod.rs:161-238): both are
 // the standard transfer functions evaluated and rounded to u8 (a data table
 // has to be identical to give identical output).
@@ -526,6 +528,197 @@ struct Result { Image image; };
 }  // namespace
 
 // mod.rs:335-521 apply/apply_inner + mod.rs:1100-1114 apply_to_canvas
+// ---- turbulence (turbulence.rs:33-304): the Perlin noise of the SVG 1.1
+// specification, f64 throughout, lattice and gradients from a Park-Miller
+// generator seeded by `seed`.
+namespace turb {
+const int32_t kRandM = 2147483647, kRandA = 16807, kRandQ = 127773, kRandR = 2836;
+const int kB = 0x100, kBLen = 0x100 + 0x100 + 2, kBM = 0xff, kPerlinN = 0x1000;
+struct Tables { int32_t sel[kBLen]; double grad[4][kBLen][2]; };
+int32_t random(int32_t seed) {
+    int32_t r = kRandA * (seed % kRandQ) - kRandR * (seed / kRandQ);
+    if (r <= 0) r += kRandM;
+    return r;
+}
+void init(int32_t seed, Tables &t) {
+    if (seed <= 0) seed = (int32_t)(0u - (uint32_t)seed) % (kRandM - 1) + 1;  // -seed wraps, as in Rust
+    if (seed > kRandM - 1) seed = kRandM - 1;
+    for (int k = 0; k < 4; k++) {
+        for (int i = 0; i < kB; i++) {
+            t.sel[i] = i;
+            for (int j = 0; j < 2; j++) {
+                seed = random(seed);
+                t.grad[k][i][j] = (double)((seed % (kB + kB)) - kB) / (double)kB;
+            }
+            const double s = std::sqrt(t.grad[k][i][0] * t.grad[k][i][0] + t.grad[k][i][1] * t.grad[k][i][1]);
+            t.grad[k][i][0] /= s;
+            t.grad[k][i][1] /= s;
+        }
+    }
+    for (int i = kB - 1; i >= 1; i--) {
+        const int32_t k = t.sel[i];
+        seed = random(seed);
+        const int32_t j = seed % kB;
+        t.sel[i] = t.sel[j];
+        t.sel[j] = k;
+    }
+    for (int i = 0; i < kB + 2; i++) {
+        t.sel[kB + i] = t.sel[i];
+        for (int g = 0; g < 4; g++)
+            for (int j = 0; j < 2; j++) t.grad[g][kB + i][j] = t.grad[g][i][j];
+    }
+}
+// Rust's saturating float -> integer casts
+int32_t to_i32(double v) {
+    if (std::isnan(v)) return 0;
+    if (v >= 2147483647.0) return INT32_MAX;
+    if (v <= -2147483648.0) return INT32_MIN;
+    return (int32_t)v;
+}
+int64_t to_i64(double v) {
+    if (std::isnan(v)) return 0;
+    if (v >= 9223372036854775807.0) return INT64_MAX;
+    if (v <= -9223372036854775808.0) return INT64_MIN;
+    return (int64_t)v;
+}
+struct Stitch { int32_t width, height, wrap_x, wrap_y; };
+inline double s_curve(double t) { return t * t * (3.0 - 2.0 * t); }
+inline double lerp(double t, double a, double b) { return a + t * (b - a); }
+double noise2(int ch, double x, double y, const Tables &t, const Stitch *st) {
+    double tt = x + (double)kPerlinN;
+    int32_t bx0 = to_i32(tt), bx1 = (int32_t)((uint32_t)bx0 + 1u);
+    const double rx0 = tt - (double)to_i64(tt), rx1 = rx0 - 1.0;
+    tt = y + (double)kPerlinN;
+    int32_t by0 = to_i32(tt), by1 = (int32_t)((uint32_t)by0 + 1u);
+    const double ry0 = tt - (double)to_i64(tt), ry1 = ry0 - 1.0;
+    if (st) {
+        if (bx0 >= st->wrap_x) bx0 = (int32_t)((uint32_t)bx0 - (uint32_t)st->width);
+        if (bx1 >= st->wrap_x) bx1 = (int32_t)((uint32_t)bx1 - (uint32_t)st->width);
+        if (by0 >= st->wrap_y) by0 = (int32_t)((uint32_t)by0 - (uint32_t)st->height);
+        if (by1 >= st->wrap_y) by1 = (int32_t)((uint32_t)by1 - (uint32_t)st->height);
+    }
+    bx0 &= kBM; bx1 &= kBM; by0 &= kBM; by1 &= kBM;
+    const int32_t i = t.sel[bx0], j = t.sel[bx1];
+    const int32_t b00 = t.sel[i + by0], b10 = t.sel[j + by0], b01 = t.sel[i + by1], b11 = t.sel[j + by1];
+    const double sx = s_curve(rx0), sy = s_curve(ry0);
+    const double *q = t.grad[ch][b00];
+    double u = rx0 * q[0] + ry0 * q[1];
+    q = t.grad[ch][b10];
+    double v = rx1 * q[0] + ry0 * q[1];
+    const double a = lerp(sx, u, v);
+    q = t.grad[ch][b01];
+    u = rx0 * q[0] + ry1 * q[1];
+    q = t.grad[ch][b11];
+    v = rx1 * q[0] + ry1 * q[1];
+    const double b = lerp(sx, u, v);
+    return lerp(sy, a, b);
+}
+bool approx_zero_ulps_d(double v) {  // f64 approx_zero_ulps(4)
+    int64_t a;
+    std::memcpy(&a, &v, 8);
+    if (a < 0) return v == 0.0;
+    return a <= 4;
+}
+double turbulence(int ch, double x, double y, double tile_x, double tile_y, double tile_w, double tile_h,
+                  double bfx, double bfy, uint32_t octaves, bool fractal, bool stitching, const Tables &t) {
+    Stitch st{0, 0, 0, 0};
+    if (stitching) {
+        if (!approx_zero_ulps_d(bfx)) {
+            const double lo = std::floor(tile_w * bfx) / tile_w, hi = std::ceil(tile_w * bfx) / tile_w;
+            bfx = (bfx / lo < hi / bfx) ? lo : hi;
+        }
+        if (!approx_zero_ulps_d(bfy)) {
+            const double lo = std::floor(tile_h * bfy) / tile_h, hi = std::ceil(tile_h * bfy) / tile_h;
+            bfy = (bfy / lo < hi / bfy) ? lo : hi;
+        }
+        st.width = to_i32(tile_w * bfx + 0.5);
+        st.height = to_i32(tile_h * bfy + 0.5);
+        st.wrap_x = to_i32(tile_x * bfx + (double)kPerlinN + (double)st.width);
+        st.wrap_y = to_i32(tile_y * bfy + (double)kPerlinN + (double)st.height);
+    }
+    double sum = 0.0, ratio = 1.0;
+    x *= bfx;
+    y *= bfy;
+    for (uint32_t o = 0; o < octaves; o++) {
+        const double n = noise2(ch, x, y, t, stitching ? &st : nullptr);
+        sum += (fractal ? n : std::fabs(n)) / ratio;
+        x *= 2.0;
+        y *= 2.0;
+        ratio *= 2.0;
+        if (stitching) {  // wrapping i32 arithmetic, as Rust's release build
+            st.width = (int32_t)((uint32_t)st.width * 2u);
+            st.wrap_x = (int32_t)((uint32_t)st.wrap_x * 2u - (uint32_t)kPerlinN);
+            st.height = (int32_t)((uint32_t)st.height * 2u);
+            st.wrap_y = (int32_t)((uint32_t)st.wrap_y * 2u - (uint32_t)kPerlinN);
+        }
+    }
+    return sum;
+}
+}  // namespace turb
+
+// apply_turbulence (mod.rs:988-1018): a region-sized image, unpremultiplied
+// noise then multiply_alpha.
+void turbulence(const rgpu_primitive &p, const Transform &ts, const IntRect &region, Pixmap &pm) {
+    float fsx, fsy;
+    ts.get_scale(&fsx, &fsy);
+    if (approx_zero_ulps(fsx) || approx_zero_ulps(fsy)) return;
+    turb::Tables t;
+    turb::init(p.i[1], t);
+    const double ox = (double)region.x - (double)ts.tx, oy = (double)region.y - (double)ts.ty;
+    const double sx = fsx, sy = fsy, bfx = p.f[0], bfy = p.f[1];
+    const bool fractal = p.i[3] != 0, stitch = p.i[2] != 0;
+    const uint32_t oct = (uint32_t)p.i[0];
+    for (uint32_t y = 0; y < pm.height; y++)
+        for (uint32_t x = 0; x < pm.width; x++)
+            for (int ch = 0; ch < 4; ch++) {
+                const double tx = ((double)x + ox) / sx, ty = ((double)y + oy) / sy;
+                double n = turb::turbulence(ch, tx, ty, (double)x, (double)y, (double)pm.width, (double)pm.height,
+                                            bfx, bfy, oct, fractal, stitch, t);
+                n = fractal ? (n * 255.0 + 255.0) / 2.0 : n * 255.0;
+                pm.data[((size_t)y * pm.width + x) * 4 + ch] = sat_u8f(f32_bound(0.0f, (float)n, 255.0f) + 0.5f);
+            }
+    multiply_alpha(pm.data);
+}
+
+// ---- tile (mod.rs:835-859): the input's region, cut from its image (the
+// part inside the image), repeats from the region's origin over a
+// region-sized image.  The pattern's transform is an integer translation, so
+// its sampling is nearest and the repeat is an integer modulus.
+bool tile(const Image &in, const IntRect &region, Pixmap &out) {
+    const IntRect sub{in.region.x - region.x, in.region.y - region.y, in.region.w, in.region.h};
+    const int32_t l = std::max(sub.x, 0), t = std::max(sub.y, 0);
+    const int32_t r = std::min(sub.right(), (int32_t)in.image->width), b = std::min(sub.bottom(), (int32_t)in.image->height);
+    if (r <= l || b <= t) return false;
+    const int32_t tw = r - l, th = b - t;
+    for (uint32_t y = 0; y < out.height; y++)
+        for (uint32_t x = 0; x < out.width; x++) {
+            int32_t u = ((int32_t)x - sub.x) % tw, v = ((int32_t)y - sub.y) % th;
+            if (u < 0) u += tw;
+            if (v < 0) v += th;
+            std::memcpy(&out.data[((size_t)y * out.width + x) * 4],
+                        &in.image->data[((size_t)(t + v) * in.image->width + (size_t)(l + u)) * 4], 4);
+        }
+    return true;
+}
+
+// ---- displacement map (displacement_map.rs:15-62, mod.rs:958-986); the map
+// is read as stored (premultiplied), as the driver passes it.
+void displacement_map(const rgpu_primitive &p, float sx, float sy, const Pixmap &src, const Pixmap &map,
+                      Pixmap &dst) {
+    const int32_t w = (int32_t)src.width, h = (int32_t)src.height;
+    const float scale = p.f[0];
+    for (uint32_t y = 0; y < map.height; y++)
+        for (uint32_t x = 0; x < map.width; x++) {
+            const uint8_t *m = &map.data[((size_t)y * map.width + x) * 4];
+            const float dx = m[p.i[0] & 3] / 255.0f - 0.5f, dy = m[p.i[1] & 3] / 255.0f - 0.5f;
+            const float fx = (float)x + dx * sx * scale, fy = (float)y + dy * sy * scale;
+            const int32_t ox = sat_i32(std::round(fx)), oy = sat_i32(std::round(fy));
+            if ((int32_t)x < w && (int32_t)y < h && ox >= 0 && ox < w && oy >= 0 && oy < h &&
+                x < dst.width && y < dst.height)
+                std::memcpy(&dst.data[((size_t)y * dst.width + x) * 4], &src.data[((size_t)oy * w + ox) * 4], 4);
+        }
+}
+
 // ---- component transfer (component_transfer.rs:10-78), on demultiplied pixels
 bool transfer_is_dummy(const rgpu_primitive &p, int ch) {
     switch (p.i[ch]) {
@@ -692,6 +885,28 @@ bool filter_apply(const rgpu_tree_view &t, const rgpu_filter &f, const Transform
             Image in = get_input(p.in1);
             auto pm = std::make_shared<Pixmap>((uint32_t)region.w, (uint32_t)region.h);
             lighting(p.kind == RGPU_FE_SPECULAR, p, ts, region, *in.image, *pm);
+            res = Image{pm, IntRect{0, 0, (int32_t)pm->width, (int32_t)pm->height}, lin};
+            break;
+        }
+        case RGPU_FE_TILE: {
+            Image in = get_input(p.in1);
+            auto pm = std::make_shared<Pixmap>((uint32_t)region.w, (uint32_t)region.h);
+            if (!tile(in, region, *pm)) return fail();
+            res = Image{pm, IntRect{0, 0, (int32_t)pm->width, (int32_t)pm->height}, false};
+            break;
+        }
+        case RGPU_FE_DISPLACEMENT_MAP: {
+            Image i1 = into_cs(get_input(p.in1), lin), i2 = into_cs(get_input(p.in2), lin);
+            auto pm = std::make_shared<Pixmap>((uint32_t)region.w, (uint32_t)region.h);
+            float sx, sy;
+            ts.get_scale(&sx, &sy);
+            displacement_map(p, p.f[0] * sx, p.f[0] * sy, *i1.image, *i2.image, *pm);
+            res = Image{pm, IntRect{0, 0, (int32_t)pm->width, (int32_t)pm->height}, lin};
+            break;
+        }
+        case RGPU_FE_TURBULENCE: {
+            auto pm = std::make_shared<Pixmap>((uint32_t)region.w, (uint32_t)region.h);
+            turbulence(p, ts, region, *pm);
             res = Image{pm, IntRect{0, 0, (int32_t)pm->width, (int32_t)pm->height}, lin};
             break;
         }

@@ -133,7 +133,8 @@ BLEND = {n: i for i, n in enumerate([
     "overlay", "darken", "lighten", "color-dodge", "color-burn", "hard-light", "soft-light", "difference",
     "exclusion", "multiply", "hue", "saturation", "color", "luminosity"])}
 FE_BLUR, FE_COLOR_MATRIX, FE_MORPHOLOGY, FE_COMPOSITE, FE_CONVOLVE, FE_DIFFUSE, FE_SPECULAR, FE_FLOOD, \
-    FE_OFFSET, FE_MERGE, FE_BLEND, FE_COMPONENT_TRANSFER, FE_DROP_SHADOW = range(13)
+    FE_OFFSET, FE_MERGE, FE_BLEND, FE_COMPONENT_TRANSFER, FE_DROP_SHADOW, FE_TURBULENCE, FE_TILE, \
+    FE_DISPLACEMENT_MAP = range(16)
 IN_SOURCE_GRAPHIC, IN_SOURCE_ALPHA = -1, -2
 CM_MATRIX, CM_SATURATE, CM_HUE_ROTATE, CM_LUM_TO_ALPHA = range(4)
 OP_OVER, OP_IN, OP_OUT, OP_ATOP, OP_XOR, OP_ARITHMETIC = range(6)
@@ -141,6 +142,7 @@ EDGE_NONE, EDGE_DUPLICATE, EDGE_WRAP = range(3)
 LIGHT_DISTANT, LIGHT_POINT, LIGHT_SPOT = range(3)
 TF_IDENTITY, TF_TABLE, TF_DISCRETE, TF_LINEAR, TF_GAMMA = range(5)
 TF_MAX_VALUES = 16
+TURB_MAX_OCTAVES = 1024
 
 
 def declare(lib: C.CDLL) -> C.CDLL:

@@ -366,6 +366,59 @@ int run_filter_job(const FilterJob &job, uint32_t *content, uint32_t *result, Fi
                 res = Img{o, lin};
                 break;
             }
+            case RGPU_FE_TILE: {
+                // apply_tile (mod.rs:835-859)
+                Img in = input(p.in1);
+                IRect ir = in.reg.w < 0 ? IRect{0, 0, job.w, job.h} : in.reg;
+                const int32_t sx0 = ir.x - region.x, sy0 = ir.y - region.y;
+                const int32_t l = std::max(sx0, 0), tp = std::max(sy0, 0);
+                const int32_t rr = std::min(sx0 + ir.w, r.w), bb = std::min(sy0 + ir.h, r.h);
+                if (rr <= l || bb <= tp) { failed = true; break; }
+                uint32_t *o = r.fresh();
+                r.ck(filter_tile(in.p, o, r.w, r.h, sx0, sy0, l, tp, rr - l, bb - tp, s));
+                res = Img{o, false};
+                break;
+            }
+            case RGPU_FE_DISPLACEMENT_MAP: {
+                // apply_displacement_map (mod.rs:958-986)
+                Img a = r.in_space(input(p.in1), lin), b = r.in_space(input(p.in2), lin);
+                const float sx = std::sqrt(job.ts.sx * job.ts.sx + job.ts.kx * job.ts.kx);
+                const float sy = std::sqrt(job.ts.ky * job.ts.ky + job.ts.sy * job.ts.sy);
+                uint32_t *o = r.fresh();
+                r.ck(filter_displacement_map(a.p, b.p, o, r.w, r.h, p.f[0] * sx, p.f[0] * sy, p.f[0], p.i[0], p.i[1],
+                                             s));
+                res = Img{o, lin};
+                break;
+            }
+            case RGPU_FE_TURBULENCE: {
+                // apply_turbulence (mod.rs:988-1018)
+                if (p.i[0] > RGPU_TURB_MAX_OCTAVES) {
+                    err = "feTurbulence numOctaves above the device limit";
+                    return RGPU_ERR_UNSUPPORTED;
+                }
+                uint32_t *o = r.fresh();
+                r.ck(filter_fill(o, r.n, 0u, s));
+                const float sx = std::sqrt(job.ts.sx * job.ts.sx + job.ts.kx * job.ts.kx);
+                const float sy = std::sqrt(job.ts.ky * job.ts.ky + job.ts.sy * job.ts.sy);
+                if (!approx_zero_ulps(sx) && !approx_zero_ulps(sy)) {
+                    // turbulence.rs init: the seed clamped into the generator's range;
+                    // -seed wraps as in Rust, and -1 (from INT32_MIN) is M - 1 mod M
+                    const int32_t m = 2147483647;
+                    int32_t seed = p.i[1];
+                    if (seed <= 0) seed = (int32_t)(0u - (uint32_t)seed) % (m - 1) + 1;
+                    if (seed > m - 1) seed = m - 1;
+                    TurbParams tp{};
+                    tp.ox = (double)region.x - (double)job.ts.tx;
+                    tp.oy = (double)region.y - (double)job.ts.ty;
+                    tp.sx = sx; tp.sy = sy;
+                    tp.bfx = p.f[0]; tp.bfy = p.f[1];
+                    tp.octaves = p.i[0]; tp.stitch = p.i[2] != 0; tp.fractal = p.i[3] != 0;
+                    tp.seed0 = (uint32_t)(((int64_t)seed % m + m) % m);
+                    r.ck(filter_turbulence(o, r.w, r.h, tp, s));
+                }
+                res = Img{o, lin};
+                break;
+            }
             case RGPU_FE_COMPONENT_TRANSFER: {
                 // apply_component_transfer (mod.rs:891-903)
                 uint32_t lut[256];
@@ -399,6 +452,7 @@ int run_filter_job(const FilterJob &job, uint32_t *content, uint32_t *result, Fi
                 err = "filter primitive not supported on the device";
                 return RGPU_ERR_UNSUPPORTED;
             }
+            if (failed) break;
             if (sub.x != region.x || sub.y != region.y || sub.w != region.w || sub.h != region.h) {
                 uint32_t *o = r.fresh();
                 r.ck(filter_copy(res.p, o, r.n, s));

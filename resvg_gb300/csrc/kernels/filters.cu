@@ -16,6 +16,7 @@
 // sliding-window passes re-read a window edge from L1/L2.
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <algorithm>
 #include "kernels.h"
 
 namespace rgpu {
@@ -982,6 +983,225 @@ cudaError_t filter_drop_shadow(const uint32_t *in, const uint32_t *shadow, uint3
                   ((uint32_t)g_host_tab[t][(pa << 8) | pb] << 16) | (pa << 24);
     }
     k_drop_shadow<<<nblk(n, 256), 256, 0, s>>>(in, shadow, out, w, h, dx, dy, l);
+    return cudaGetLastError();
+}
+}  // namespace rgpu
+
+namespace rgpu {
+namespace {
+
+// ---- turbulence (turbulence.rs): the SVG 1.1 Perlin noise in f64.  Each CTA
+// rebuilds the lattice and gradient tables in shared memory: the generator is
+// Park-Miller, seed_n = 16807^n * seed_0 mod (2^31 - 1), so every draw is
+// computed independently; only the 255 swaps of the lattice shuffle are
+// sequential (one thread, shared memory).
+constexpr uint32_t kTurbM = 2147483647u, kTurbA = 16807u;
+constexpr int kTurbB = 256, kTurbBLen = 514, kTurbPerlinN = 4096;
+
+__device__ __forceinline__ uint32_t mulmod_m(uint32_t a, uint32_t b) {
+    const uint64_t p = (uint64_t)a * b;
+    uint64_t r = (p & kTurbM) + (p >> 31);
+    if (r >= kTurbM) r -= kTurbM;
+    return (uint32_t)r;
+}
+__device__ uint32_t powmod_a(uint32_t e) {
+    uint32_t r = 1u, b = kTurbA;
+    while (e) {
+        if (e & 1u) r = mulmod_m(r, b);
+        b = mulmod_m(b, b);
+        e >>= 1;
+    }
+    return r;
+}
+__device__ __forceinline__ int32_t sat_i32_d(double v) { return __double2int_rz(v); }
+__device__ __forceinline__ int64_t sat_i64_d(double v) { return __double2ll_rz(v); }
+
+struct TurbStitch { int32_t width, height, wrap_x, wrap_y; };
+
+__device__ __forceinline__ double turb_noise2(int ch, double x, double y, const int32_t *sel, const double2 *grad,
+                                              bool stitch, const TurbStitch &st) {
+    double t = __dadd_rn(x, (double)kTurbPerlinN);
+    int32_t bx0 = sat_i32_d(t), bx1 = (int32_t)((uint32_t)bx0 + 1u);
+    const double rx0 = __dsub_rn(t, (double)sat_i64_d(t)), rx1 = __dsub_rn(rx0, 1.0);
+    t = __dadd_rn(y, (double)kTurbPerlinN);
+    int32_t by0 = sat_i32_d(t), by1 = (int32_t)((uint32_t)by0 + 1u);
+    const double ry0 = __dsub_rn(t, (double)sat_i64_d(t)), ry1 = __dsub_rn(ry0, 1.0);
+    if (stitch) {
+        if (bx0 >= st.wrap_x) bx0 = (int32_t)((uint32_t)bx0 - (uint32_t)st.width);
+        if (bx1 >= st.wrap_x) bx1 = (int32_t)((uint32_t)bx1 - (uint32_t)st.width);
+        if (by0 >= st.wrap_y) by0 = (int32_t)((uint32_t)by0 - (uint32_t)st.height);
+        if (by1 >= st.wrap_y) by1 = (int32_t)((uint32_t)by1 - (uint32_t)st.height);
+    }
+    bx0 &= 0xff; bx1 &= 0xff; by0 &= 0xff; by1 &= 0xff;
+    const int32_t i = sel[bx0], j = sel[bx1];
+    const double2 *g = grad + ch * kTurbBLen;
+    const double sx = __dmul_rn(__dmul_rn(rx0, rx0), __dsub_rn(3.0, __dmul_rn(2.0, rx0)));
+    const double sy = __dmul_rn(__dmul_rn(ry0, ry0), __dsub_rn(3.0, __dmul_rn(2.0, ry0)));
+    double2 q = g[sel[i + by0]];
+    double u = __dadd_rn(__dmul_rn(rx0, q.x), __dmul_rn(ry0, q.y));
+    q = g[sel[j + by0]];
+    double v = __dadd_rn(__dmul_rn(rx1, q.x), __dmul_rn(ry0, q.y));
+    const double a = __dadd_rn(u, __dmul_rn(sx, __dsub_rn(v, u)));
+    q = g[sel[i + by1]];
+    u = __dadd_rn(__dmul_rn(rx0, q.x), __dmul_rn(ry1, q.y));
+    q = g[sel[j + by1]];
+    v = __dadd_rn(__dmul_rn(rx1, q.x), __dmul_rn(ry1, q.y));
+    const double b = __dadd_rn(u, __dmul_rn(sx, __dsub_rn(v, u)));
+    return __dadd_rn(a, __dmul_rn(sy, __dsub_rn(b, a)));
+}
+
+__device__ __forceinline__ bool approx_zero_ulps_d(double v) {
+    const long long a = __double_as_longlong(v);
+    if (a < 0) return v == 0.0;
+    return a <= 4;
+}
+
+__global__ void __launch_bounds__(256) k_turbulence(uint32_t *out, int w, int h, TurbParams tp) {
+    __shared__ int32_t sel[kTurbBLen];
+    __shared__ double2 grad[4 * kTurbBLen];
+    __shared__ int32_t swap_j[kTurbB];
+    const int t = threadIdx.x;
+    // tables (turbulence.rs init): draw n (1-based) is seed_0 * A^n mod M
+    {
+        const uint32_t base = mulmod_m(tp.seed0, powmod_a(2u * (uint32_t)t + 1u));
+        for (int k = 0; k < 4; k++) {
+            const uint32_t s0 = k == 0 ? base : mulmod_m(base, powmod_a(512u * (uint32_t)k));
+            const uint32_t s1 = mulmod_m(s0, kTurbA);
+            double g0 = (double)((int32_t)(s0 % 512u) - kTurbB) / (double)kTurbB;
+            double g1 = (double)((int32_t)(s1 % 512u) - kTurbB) / (double)kTurbB;
+            const double s = __dsqrt_rn(__dadd_rn(__dmul_rn(g0, g0), __dmul_rn(g1, g1)));
+            grad[k * kTurbBLen + t] = make_double2(__ddiv_rn(g0, s), __ddiv_rn(g1, s));
+        }
+        sel[t] = t;
+        // the shuffle step for lattice index i = 255 .. 1 uses draw 2048 + (256 - i)
+        if (t >= 1) swap_j[t] = (int32_t)(mulmod_m(tp.seed0, powmod_a(2048u + 256u - (uint32_t)t)) % 256u);
+    }
+    __syncthreads();
+    if (t == 0) {
+        for (int i = kTurbB - 1; i >= 1; i--) {
+            const int32_t k = sel[i], j = swap_j[i];
+            sel[i] = sel[j];
+            sel[j] = k;
+        }
+    }
+    __syncthreads();
+    for (int i = t; i < kTurbB + 2; i += blockDim.x) {
+        sel[kTurbB + i] = sel[i % kTurbB];
+        for (int k = 0; k < 4; k++) grad[k * kTurbBLen + kTurbB + i] = grad[k * kTurbBLen + (i % kTurbB)];
+    }
+    __syncthreads();
+
+    const size_t n = (size_t)w * h;
+    for (size_t idx = (size_t)blockIdx.x * blockDim.x + t; idx < n; idx += (size_t)gridDim.x * blockDim.x) {
+        const int x = (int)(idx % w), y = (int)(idx / w);
+        uint32_t px = 0;
+        for (int ch = 0; ch < 4; ch++) {
+            double bfx = tp.bfx, bfy = tp.bfy;
+            TurbStitch st{0, 0, 0, 0};
+            const double tile_w = (double)w, tile_h = (double)h;
+            if (tp.stitch) {
+                if (!approx_zero_ulps_d(bfx)) {
+                    const double lo = __ddiv_rn(floor(__dmul_rn(tile_w, bfx)), tile_w);
+                    const double hi = __ddiv_rn(ceil(__dmul_rn(tile_w, bfx)), tile_w);
+                    bfx = __ddiv_rn(bfx, lo) < __ddiv_rn(hi, bfx) ? lo : hi;
+                }
+                if (!approx_zero_ulps_d(bfy)) {
+                    const double lo = __ddiv_rn(floor(__dmul_rn(tile_h, bfy)), tile_h);
+                    const double hi = __ddiv_rn(ceil(__dmul_rn(tile_h, bfy)), tile_h);
+                    bfy = __ddiv_rn(bfy, lo) < __ddiv_rn(hi, bfy) ? lo : hi;
+                }
+                st.width = sat_i32_d(__dadd_rn(__dmul_rn(tile_w, bfx), 0.5));
+                st.height = sat_i32_d(__dadd_rn(__dmul_rn(tile_h, bfy), 0.5));
+                st.wrap_x = sat_i32_d(__dadd_rn(__dadd_rn(__dmul_rn((double)x, bfx), (double)kTurbPerlinN),
+                                                (double)st.width));
+                st.wrap_y = sat_i32_d(__dadd_rn(__dadd_rn(__dmul_rn((double)y, bfy), (double)kTurbPerlinN),
+                                                (double)st.height));
+            }
+            double vx = __dmul_rn(__ddiv_rn(__dadd_rn((double)x, tp.ox), tp.sx), bfx);
+            double vy = __dmul_rn(__ddiv_rn(__dadd_rn((double)y, tp.oy), tp.sy), bfy);
+            double sum = 0.0, ratio = 1.0;
+            for (int o = 0; o < tp.octaves; o++) {
+                const double nz = turb_noise2(ch, vx, vy, sel, grad, tp.stitch != 0, st);
+                sum = __dadd_rn(sum, __ddiv_rn(tp.fractal ? nz : fabs(nz), ratio));
+                vx = __dmul_rn(vx, 2.0);
+                vy = __dmul_rn(vy, 2.0);
+                ratio = __dmul_rn(ratio, 2.0);
+                if (tp.stitch) {
+                    st.width = (int32_t)((uint32_t)st.width * 2u);
+                    st.wrap_x = (int32_t)((uint32_t)st.wrap_x * 2u - (uint32_t)kTurbPerlinN);
+                    st.height = (int32_t)((uint32_t)st.height * 2u);
+                    st.wrap_y = (int32_t)((uint32_t)st.wrap_y * 2u - (uint32_t)kTurbPerlinN);
+                }
+            }
+            const double v = tp.fractal ? __ddiv_rn(__dadd_rn(__dmul_rn(sum, 255.0), 255.0), 2.0) : __dmul_rn(sum, 255.0);
+            px |= sat_u8f(f32_bound(0.0f, __double2float_rn(v), 255.0f) + 0.5f) << (8 * ch);
+        }
+        out[idx] = tab_px(TAB_MUL, px);
+    }
+}
+
+}  // namespace
+
+cudaError_t filter_turbulence(uint32_t *out, int w, int h, const TurbParams &tp, cudaStream_t s) {
+    const size_t n = (size_t)w * h;
+    if (n == 0) return cudaSuccess;
+    cudaError_t e = ensure_luts();
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const size_t want = (n + 255) / 256;
+    const uint32_t grid = (uint32_t)std::min<size_t>(want, (size_t)std::max(sms, 1) * 4);
+    k_turbulence<<<grid, 256, 0, s>>>(out, w, h, tp);
+    return cudaGetLastError();
+}
+}  // namespace rgpu
+
+namespace rgpu {
+namespace {
+// feTile: out(x, y) = src(l + (x - ox) mod tw, t + (y - oy) mod th), the tile
+// being the input's region cut at (l, t, tw, th) and repeated from (ox, oy).
+__global__ void k_tile(const uint32_t *src, uint32_t *dst, int w, int h, int ox, int oy, int l, int t, int tw,
+                       int th) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (size_t)w * h) return;
+    const int x = (int)(i % w), y = (int)(i / w);
+    int u = (int)(((int64_t)x - ox) % tw), v = (int)(((int64_t)y - oy) % th);
+    if (u < 0) u += tw;
+    if (v < 0) v += th;
+    dst[i] = src[(size_t)(t + v) * w + (size_t)(l + u)];
+}
+// feDisplacementMap (displacement_map.rs): each pixel takes the source pixel
+// at its position moved by (map channel / 255 - 0.5) * scale * s, rounded half
+// away from zero; 0 outside.
+__global__ void k_displace(const uint32_t *src, const uint32_t *map, uint32_t *dst, int w, int h, float sx, float sy,
+                           float scale, int xch, int ych) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (size_t)w * h) return;
+    const int x = (int)(i % w), y = (int)(i / w);
+    const uint32_t m = map[i];
+    const float dx = __fsub_rn(__fdiv_rn((float)chn(m, xch), 255.0f), 0.5f);
+    const float dy = __fsub_rn(__fdiv_rn((float)chn(m, ych), 255.0f), 0.5f);
+    const float fx = __fadd_rn((float)x, __fmul_rn(__fmul_rn(dx, sx), scale));
+    const float fy = __fadd_rn((float)y, __fmul_rn(__fmul_rn(dy, sy), scale));
+    const int ox = __float2int_rz(roundf(fx)), oy = __float2int_rz(roundf(fy));
+    dst[i] = (ox >= 0 && ox < w && oy >= 0 && oy < h) ? src[(size_t)oy * w + ox] : 0u;
+}
+}  // namespace
+
+cudaError_t filter_tile(const uint32_t *src, uint32_t *dst, int w, int h, int ox, int oy, int l, int t, int tw,
+                        int th, cudaStream_t s) {
+    const size_t n = (size_t)w * h;
+    if (n == 0) return cudaSuccess;
+    if (tw <= 0 || th <= 0 || l < 0 || t < 0 || l + tw > w || t + th > h) return cudaErrorInvalidValue;
+    k_tile<<<nblk(n, 256), 256, 0, s>>>(src, dst, w, h, ox, oy, l, t, tw, th);
+    return cudaGetLastError();
+}
+cudaError_t filter_displacement_map(const uint32_t *src, const uint32_t *map, uint32_t *dst, int w, int h, float sx,
+                                    float sy, float scale, int xch, int ych, cudaStream_t s) {
+    const size_t n = (size_t)w * h;
+    if (n == 0) return cudaSuccess;
+    k_displace<<<nblk(n, 256), 256, 0, s>>>(src, map, dst, w, h, sx, sy, scale, xch & 3, ych & 3);
     return cudaGetLastError();
 }
 }  // namespace rgpu

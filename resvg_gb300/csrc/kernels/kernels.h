@@ -56,6 +56,21 @@ cudaError_t filter_alpha_only(uint32_t *img, size_t n, cudaStream_t s);
 // feComponentTransfer on a premultiplied image: demultiply, lut[c] holds the
 // four channels' results for value c (r in the low byte), multiply.
 cudaError_t filter_component_transfer(uint32_t *img, size_t n, const uint32_t lut[256], cudaStream_t s);
+// feTurbulence (turbulence.rs) into a w x h image, premultiplied.  seed0 is the
+// generator state after the seed clamp, in [1, 2^31 - 2]; octaves are bounded by
+// the caller.
+struct TurbParams {
+    double ox, oy, sx, sy, bfx, bfy;
+    int octaves, stitch, fractal;
+    uint32_t seed0;
+};
+cudaError_t filter_turbulence(uint32_t *out, int w, int h, const TurbParams &tp, cudaStream_t s);
+// feTile: the tile (l, t, tw, th) of src, inside the image, repeated from (ox, oy).
+cudaError_t filter_tile(const uint32_t *src, uint32_t *dst, int w, int h, int ox, int oy, int l, int t, int tw,
+                        int th, cudaStream_t s);
+// feDisplacementMap with the scaled factors sx, sy and the primitive's scale.
+cudaError_t filter_displacement_map(const uint32_t *src, const uint32_t *map, uint32_t *dst, int w, int h, float sx,
+                                    float sy, float scale, int xch, int ych, cudaStream_t s);
 // feDropShadow after the shadow copy is blurred; flood = r | g << 8 | b << 16 | opacity_u8 << 24.
 cudaError_t filter_drop_shadow(const uint32_t *in, const uint32_t *shadow, uint32_t *out, int w, int h, int dx,
                                int dy, uint32_t flood, bool linear, cudaStream_t s);

@@ -727,7 +727,7 @@ INHERITED = {"fill", "fill-opacity", "fill-rule", "stroke", "stroke-width", "str
 NON_INHERITED = {"opacity", "clip-path", "mask", "filter", "mix-blend-mode", "isolation", "display",
                  "stop-color", "stop-opacity", "flood-color", "flood-opacity", "transform"}
 UNSUPPORTED_ELEMS = {"text", "image", "pattern", "marker", "switch", "foreignObject", "tspan", "textPath", "symbol",
-                     "feImage", "feTile", "feTurbulence", "feDisplacementMap",
+                     "feImage",
                      "style", "animate", "set"}
 BLEND = {"normal": "source-over", "multiply": "multiply", "screen": "screen", "overlay": "overlay",
          "darken": "darken", "lighten": "lighten", "color-dodge": "color-dodge", "color-burn": "color-burn",
@@ -1865,6 +1865,40 @@ class Builder(Loader):
                 p.f[0], p.f[1] = dx if dx is not None else 0.0, dy if dy is not None else 0.0
             elif tag == "feComponentTransfer":
                 self.component_transfer(c, p)
+            elif tag == "feTile":
+                p.kind = A.FE_TILE
+            elif tag == "feDisplacementMap":
+                # parser/filter.rs convert_displacement_map
+                p.kind = A.FE_DISPLACEMENT_MAP
+                p.in2 = inp("in2")
+                ch = {"R": 0, "G": 1, "B": 2}
+                p.i[0] = ch.get(c.get("xChannelSelector"), 3)
+                p.i[1] = ch.get(c.get("yChannelSelector"), 3)
+                sc = number_strict(c.get("scale"))
+                p.f[0] = sc if sc is not None else 0.0
+            elif tag == "feTurbulence":
+                # parser/filter.rs convert_turbulence
+                p.kind = A.FE_TURBULENCE
+                bf = number_list_strict(c.get("baseFrequency")) if c.get("baseFrequency") is not None else None
+                fx = fy = 0.0
+                if bf is not None and len(bf) in (1, 2):
+                    bx, by = F(bf[0]), F(bf[-1])
+                    if math.copysign(1.0, bx) > 0 and math.copysign(1.0, by) > 0:
+                        fx, fy = float(bx), float(by)
+                p.f[0], p.f[1] = fx, fy
+                no = number_strict(c.get("numOctaves"))
+                no = F(no) if no is not None else F(1.0)
+                if math.copysign(1.0, no) < 0:
+                    no = F(0.0)
+                no = math.floor(no + 0.5)  # f32::round (half away from zero), non-negative here
+                if no > A.TURB_MAX_OCTAVES:
+                    raise Unsupported("numOctaves above the device limit")
+                p.i[0] = int(no)
+                sd = number_strict(c.get("seed"))
+                sd = math.trunc(float(F(sd))) if sd is not None and math.isfinite(F(sd)) else 0
+                p.i[1] = max(-2 ** 31, min(2 ** 31 - 1, sd))
+                p.i[2] = 1 if c.get("stitchTiles") == "stitch" else 0
+                p.i[3] = 1 if c.get("type") == "fractalNoise" else 0
             elif tag == "feDropShadow":
                 # parser/filter.rs convert_drop_shadow: stdDeviation "2 2", dx and dy
                 # numbers (default 2), flood colour and opacity as feFlood

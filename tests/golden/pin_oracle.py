@@ -48,6 +48,7 @@ CATEGORIES = [
     "filters/feConvolveMatrix", "filters/feDiffuseLighting", "filters/feSpecularLighting",
     "filters/feDistantLight", "filters/fePointLight", "filters/feSpotLight",
     "filters/filter-functions", "filters/feComponentTransfer", "filters/feDropShadow",
+    "filters/feTurbulence", "filters/feTile", "filters/feDisplacementMap",
 ]
 IMAGE_SIZE = 300
 FIXTURES_PER_DIR = 4

@@ -1,11 +1,12 @@
-"""feComponentTransfer, feDropShadow and the CSS filter functions on the GPU
-vs the CPU oracle.
+"""feComponentTransfer, feDropShadow, feTurbulence, feTile,
+feDisplacementMap and the CSS filter functions on the GPU vs the CPU oracle.
 
 The transfer functions are evaluated on the host into one 256-entry table per
 channel with the same f32 operations as the oracle (powf included), so the
 device result is bit-exact.  The drop shadow runs the blur kernels (box or
 IIR, both exact), a per-alpha flood table and two source-over draws: also
-bit-exact.
+bit-exact.  Turbulence is f64 arithmetic in the reference's order, without
+contraction, with the generator's tables rebuilt on the device: bit-exact.
 """
 import pytest
 
@@ -51,6 +52,27 @@ SHADOW = [
     '<feDropShadow in="SourceAlpha" stdDeviation="3 9" dx="0" dy="12" flood-color="seagreen"/>',
 ]
 
+TURBULENCE = [
+    '<feTurbulence baseFrequency="0.05"/>',
+    '<feTurbulence baseFrequency="0.02 0.07" numOctaves="4" seed="7" type="fractalNoise"/>',
+    '<feTurbulence baseFrequency="0.03" numOctaves="3" seed="-20" stitchTiles="stitch"/>',
+    '<feTurbulence baseFrequency="0.011 0.013" numOctaves="2" seed="1e10" stitchTiles="stitch" '
+    'type="fractalNoise"/>',
+    '<feTurbulence baseFrequency="0.1" numOctaves="0" type="fractalNoise" seed="-1e10"/>',
+    '<feTurbulence baseFrequency="0.04" numOctaves="6" seed="2.9"/>'
+    '<feComposite in2="SourceGraphic" operator="in"/>',
+]
+
+TILE_DISPLACE = [
+    '<feFlood flood-color="seagreen" flood-opacity="0.7" x="28" y="28" width="10" height="13"/>'
+    '<feOffset dx="5" dy="5"/><feTile/>',
+    '<feOffset dx="-7" dy="3" x="30" y="40" width="23" height="17"/><feTile x="20" y="30" width="150" height="120"/>',
+    '<feFlood flood-color="red" x="0" y="0" width="10" height="10"/><feOffset dx="5" dy="5"/><feTile/>',
+    '<feTurbulence baseFrequency="0.03" numOctaves="2" result="t"/>'
+    '<feDisplacementMap in="SourceGraphic" in2="t" scale="12" xChannelSelector="R" yChannelSelector="G"/>',
+    '<feDisplacementMap in2="SourceAlpha" scale="-3" xChannelSelector="A" yChannelSelector="B"/>',
+]
+
 FUNCTIONS = [
     'blur(3)',
     'drop-shadow(blue 4 5 6) grayscale(0.3)',
@@ -84,6 +106,23 @@ def test_component_transfer_exact(gpu, oracle_mod, k, cif, ts):
 def test_drop_shadow_exact(gpu, oracle_mod, k, cif, ts):
     g, o = _render_both(oracle_mod, _scene(SHADOW[k], cif), ts)
     assert o[..., 3].any()
+    assert diff_stats(g, o) == (0, 0)
+
+
+@pytest.mark.parametrize("ts", TRANSFORMS)
+@pytest.mark.parametrize("cif", ["sRGB", "linearRGB"])
+@pytest.mark.parametrize("k", range(len(TURBULENCE)))
+def test_turbulence_exact(gpu, oracle_mod, k, cif, ts):
+    g, o = _render_both(oracle_mod, _scene(TURBULENCE[k], cif), ts)
+    assert o[..., 3].any()
+    assert diff_stats(g, o) == (0, 0)
+
+
+@pytest.mark.parametrize("ts", TRANSFORMS)
+@pytest.mark.parametrize("cif", ["sRGB", "linearRGB"])
+@pytest.mark.parametrize("k", range(len(TILE_DISPLACE)))
+def test_tile_displacement_exact(gpu, oracle_mod, k, cif, ts):
+    g, o = _render_both(oracle_mod, _scene(TILE_DISPLACE[k], cif), ts)
     assert diff_stats(g, o) == (0, 0)
 
 
