@@ -374,15 +374,23 @@ void box_sizes(float sigma, int sizes[5]) {
 constexpr int kBoxT = 128;     // outputs along the pass per tile
 constexpr int kBoxMaxR = 96;   // largest radius the tiles take
 // Window sums as two 16-bit lanes per register (r | b << 16, g | a << 16): a
-// lane holds at most (2 * kBoxMaxR + 2) * 255 < 65536 at any step, so lanes
-// never carry or borrow into each other.  round(sum * iarr) is the f32
-// product rounded half to even (box_blur.rs round); it never exceeds 255.
-__device__ __forceinline__ uint32_t box_round2(uint32_t rb, uint32_t ga, float iarr) {
-    const uint32_t r = (uint32_t)__float2int_rn(__fmul_rn((float)(rb & 0xFFFFu), iarr));
-    const uint32_t b = (uint32_t)__float2int_rn(__fmul_rn((float)(rb >> 16), iarr));
-    const uint32_t g = (uint32_t)__float2int_rn(__fmul_rn((float)(ga & 0xFFFFu), iarr));
-    const uint32_t a = (uint32_t)__float2int_rn(__fmul_rn((float)(ga >> 16), iarr));
-    return r | (g << 8) | (b << 16) | (a << 24);
+// lane holds at most (2 * kBoxMaxR + 1) * 255 + kBoxMaxR < 65536 at any step,
+// so lanes never carry or borrow into each other.  The reference rounds the
+// f32 product sum * (1 / (2r + 1)) half to even; the quotient is never within
+// 1 / (2 (2r + 1)) of a half while the f32 error stays below 2^-15, so that
+// equals the integer (sum + r) / (2r + 1), here a multiply-high by
+// m = ceil(2^32 / (2r + 1)) (exact for sums below 2^16; both identities are
+// checked exhaustively in the tests).  No int <-> float conversions.
+__device__ __forceinline__ uint32_t box_round2(uint32_t rb, uint32_t ga, uint32_t r, uint32_t m) {
+    if (m == 0u) return rb | (ga << 8);  // r = 0: the window is the pixel itself
+    rb += r * 0x10001u;
+    ga += r * 0x10001u;
+    const uint32_t cr = __umulhi(rb & 0xFFFFu, m), cb = __umulhi(rb >> 16, m);
+    const uint32_t cg = __umulhi(ga & 0xFFFFu, m), ca = __umulhi(ga >> 16, m);
+    return cr | (cg << 8) | (cb << 16) | (ca << 24);
+}
+inline uint32_t box_magic(int r) {
+    return r == 0 ? 0u : (uint32_t)((0x100000000ull + (uint64_t)(2 * r)) / (uint64_t)(2 * r + 1));
 }
 #define BOX_ADD(p) do { rb += (p) & 0x00FF00FFu; ga += ((p) >> 8) & 0x00FF00FFu; } while (0)
 #define BOX_SLIDE(pa, ps)                                                         \
@@ -392,7 +400,7 @@ __device__ __forceinline__ uint32_t box_round2(uint32_t rb, uint32_t ga, float i
     } while (0)
 
 // vertical: tile of 32 columns x kBoxT rows; thread (lane = column, warp = 32-row group)
-__global__ void __launch_bounds__(256) k_box_v(const uint32_t *src, uint32_t *dst, int w, int h, int r, float iarr) {
+__global__ void __launch_bounds__(256) k_box_v(const uint32_t *src, uint32_t *dst, int w, int h, int r, uint32_t m) {
     extern __shared__ uint32_t tile[];  // (kBoxT + 2r) rows x 32
     const int x0 = blockIdx.x * 32, y0 = blockIdx.y * kBoxT;
     const int rows = kBoxT + 2 * r;
@@ -431,13 +439,13 @@ __global__ void __launch_bounds__(256) k_box_v(const uint32_t *src, uint32_t *ds
             const uint32_t pa = tile[(oy + 2 * r) * 32 + c], ps = tile[(oy - 1) * 32 + c];
             BOX_SLIDE(pa, ps);
         }
-        if (x < w && y < h) dst[(size_t)y * w + x] = box_round2(rb, ga, iarr);
+        if (x < w && y < h) dst[(size_t)y * w + x] = box_round2(rb, ga, (uint32_t)r, m);
     }
 }
 
 // horizontal: tile of 32 rows x kBoxT columns; thread (lane = row, warp = 32-column
 // group); the outputs go through shared memory so the stores are row-coalesced
-__global__ void __launch_bounds__(256) k_box_h(const uint32_t *src, uint32_t *dst, int w, int h, int r, float iarr) {
+__global__ void __launch_bounds__(256) k_box_h(const uint32_t *src, uint32_t *dst, int w, int h, int r, uint32_t m) {
     extern __shared__ uint32_t tile[];
     const int cols = kBoxT + 2 * r, stride = cols | 1;  // odd row stride: lanes hit distinct banks
     uint32_t *out = tile + 32 * stride;                  // 32 rows x (kBoxT + 1)
@@ -471,7 +479,7 @@ __global__ void __launch_bounds__(256) k_box_h(const uint32_t *src, uint32_t *ds
             const uint32_t pa = row[ox + 2 * r], ps = row[ox - 1];
             BOX_SLIDE(pa, ps);
         }
-        out[lane * ostride + ox] = box_round2(rb, ga, iarr);
+        out[lane * ostride + ox] = box_round2(rb, ga, (uint32_t)r, m);
     }
     __syncthreads();
     for (int ry = wp; ry < 32; ry += 8) {
@@ -484,6 +492,12 @@ __global__ void __launch_bounds__(256) k_box_h(const uint32_t *src, uint32_t *ds
         }
     }
 }
+
+// Tiles of the fused morphology kernel.
+constexpr int kPairTX = 64, kPairTY = 32, kPairSeg = 16;
+// (b0, b2) and (b1, b3) of a pixel as two 16-bit lanes
+__device__ __forceinline__ uint32_t lanes02(uint32_t p) { return __byte_perm(p, 0u, 0x4240); }
+__device__ __forceinline__ uint32_t lanes13(uint32_t p) { return __byte_perm(p, 0u, 0x4341); }
 
 // Morphology passes on the same tiles: window [i - target, i - target + taps)
 // along the pass, taps outside the image skipped (= the identity of min / max
@@ -547,6 +561,82 @@ __global__ void __launch_bounds__(256) k_morph_h(const uint32_t *src, uint32_t *
         }
     }
 }
+// Both morphology passes fused on a TX x TY tile: the tile and its window
+// halo are loaded once, columns then rows are reduced in shared memory (the
+// rectangle's min / max is separable and exact, so this is the reference's
+// 2-D window), and the tile leaves in coalesced rows.  Pixels are split into
+// (r, b) and (g, a) 16-bit lanes so one 16x2 min / max handles two channels.
+constexpr int kMorphPairMaxTaps = 64;
+size_t morph_pair_smem(int tx, int ty) {
+    const size_t st = (size_t)((kPairTX + tx - 1) | 1);
+    return ((size_t)(kPairTY + ty - 1) * st + (size_t)kPairTY * st) * 4;
+}
+__device__ __forceinline__ uint32_t mm2(uint32_t a, uint32_t b, bool dilate) {
+    return dilate ? __vmaxu2(a, b) : __vminu2(a, b);
+}
+__global__ void __launch_bounds__(256) k_morph_vh(const uint32_t *src, uint32_t *dst, int w, int h, int tx, int ty,
+                                                  int ox, int oy, int dilate) {
+    extern __shared__ uint32_t smem[];
+    constexpr int TX = kPairTX, TY = kPairTY, SEG = kPairSeg;
+    const bool dil = dilate != 0;
+    const uint32_t pad = dil ? 0u : 0xFFFFFFFFu, pad2 = dil ? 0u : 0x00FF00FFu;
+    const int cols = TX + tx - 1, rows = TY + ty - 1, st = cols | 1, cst = TX + 1;
+    uint32_t *A = smem, *B = smem + rows * st, *C = smem;
+    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
+    const int wp = threadIdx.x >> 5, ln = threadIdx.x & 31;
+    for (int ry = wp; ry < rows; ry += 8) {
+        const int y = y0 - oy + ry;
+        const bool yin = y >= 0 && y < h;
+        const uint32_t *srow = src + (size_t)(yin ? y : 0) * w;
+#pragma unroll 4
+        for (int cx = ln; cx < cols; cx += 32) {
+            const int x = x0 - ox + cx;
+            A[ry * st + cx] = (yin && x >= 0 && x < w) ? __ldg(srow + x) : pad;
+        }
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < cols * (TY / SEG); t += 256) {
+        const int c = t % cols, o0 = (t / cols) * SEG;
+#pragma unroll 2
+        for (int i = 0; i < SEG; i++) {
+            const int o = o0 + i;
+            uint32_t vr = pad2, vg = pad2;
+            for (int k = 0; k < ty; k++) {
+                const uint32_t p = A[(o + k) * st + c];
+                vr = mm2(vr, lanes02(p), dil);
+                vg = mm2(vg, lanes13(p), dil);
+            }
+            B[o * st + c] = vr | (vg << 8);
+        }
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < TY * (TX / SEG); t += 256) {
+        const int r = t % TY, o0 = (t / TY) * SEG;
+        const uint32_t *row = B + r * st;
+#pragma unroll 2
+        for (int i = 0; i < SEG; i++) {
+            const int o = o0 + i;
+            uint32_t vr = pad2, vg = pad2;
+            for (int k = 0; k < tx; k++) {
+                const uint32_t p = row[o + k];
+                vr = mm2(vr, lanes02(p), dil);
+                vg = mm2(vg, lanes13(p), dil);
+            }
+            C[r * cst + o] = vr | (vg << 8);
+        }
+    }
+    __syncthreads();
+    for (int ry = wp; ry < TY; ry += 8) {
+        const int y = y0 + ry;
+        if (y >= h) break;
+        uint32_t *drow = dst + (size_t)y * w;
+#pragma unroll 4
+        for (int cx = ln; cx < TX; cx += 32) {
+            const int x = x0 + cx;
+            if (x < w) drow[x] = C[ry * cst + cx];
+        }
+    }
+}
 size_t morph_v_smem(int taps) { return (size_t)(kBoxT + taps - 1) * 32 * 4; }
 size_t morph_h_smem(int taps) { return ((size_t)32 * ((kBoxT + taps - 1) | 1) + (size_t)32 * (kBoxT + 1)) * 4; }
 constexpr int kMorphMaxTaps = 192;
@@ -566,6 +656,9 @@ cudaError_t box_attrs() {
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_morph_h, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)morph_h_smem(kMorphMaxTaps));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_morph_vh, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)morph_pair_smem(kMorphPairMaxTaps, kMorphPairMaxTaps));
     if (e == cudaSuccess) done = true;
     return e;
 }
@@ -587,7 +680,7 @@ cudaError_t filter_box_blur(uint32_t *img, uint32_t *tmp, int w, int h, double s
         }
         else if (rv <= kBoxMaxR) {
             dim3 g((unsigned)((w + 31) / 32), (unsigned)((h + kBoxT - 1) / kBoxT));
-            k_box_v<<<g, 256, box_v_smem(rv), s>>>(img, tmp, w, h, rv, 1.0f / (float)(rv + rv + 1));
+            k_box_v<<<g, 256, box_v_smem(rv), s>>>(img, tmp, w, h, rv, box_magic(rv));
         } else {
             size_t th = (size_t)w * ((h + seg - 1) / seg);
             k_box_pass<<<nblk(th, 256), 256, 0, s>>>(img, tmp, h, w, (size_t)w, 1, rv, seg, 1.0f / (float)(rv + rv + 1));
@@ -598,7 +691,7 @@ cudaError_t filter_box_blur(uint32_t *img, uint32_t *tmp, int w, int h, double s
         }
         else if (rh <= kBoxMaxR) {
             dim3 g((unsigned)((w + kBoxT - 1) / kBoxT), (unsigned)((h + 31) / 32));
-            k_box_h<<<g, 256, box_h_smem(rh), s>>>(tmp, img, w, h, rh, 1.0f / (float)(rh + rh + 1));
+            k_box_h<<<g, 256, box_h_smem(rh), s>>>(tmp, img, w, h, rh, box_magic(rh));
         } else {
             size_t th = (size_t)h * ((w + seg - 1) / seg);
             k_box_pass<<<nblk(th, 256), 256, 0, s>>>(tmp, img, w, h, 1, (size_t)w, rh, seg, 1.0f / (float)(rh + rh + 1));
@@ -667,6 +760,14 @@ cudaError_t filter_morphology(uint32_t *img, uint32_t *tmp, int w, int h, bool d
     if (n == 0) return cudaSuccess;
     cudaError_t ae = box_attrs();
     if (ae != cudaSuccess) return ae;
+    if (cols <= kMorphPairMaxTaps && rows <= kMorphPairMaxTaps) {
+        // one fused launch into tmp, then back
+        dim3 g((unsigned)((w + kPairTX - 1) / kPairTX), (unsigned)((h + kPairTY - 1) / kPairTY));
+        k_morph_vh<<<g, 256, morph_pair_smem(cols, rows), s>>>(img, tmp, w, h, cols, rows, txc, tyr, dilate ? 1 : 0);
+        cudaError_t ce = cudaMemcpyAsync(img, tmp, n * 4, cudaMemcpyDeviceToDevice, s);
+        if (ce != cudaSuccess) return ce;
+        return cudaGetLastError();
+    }
     if (cols <= kMorphMaxTaps) {
         dim3 g((unsigned)((w + kBoxT - 1) / kBoxT), (unsigned)((h + 31) / 32));
         k_morph_h<<<g, 256, morph_h_smem(cols), s>>>(img, tmp, w, h, cols, txc, dilate ? 1 : 0);
