@@ -164,6 +164,15 @@ int rgpu_filter_morphology(uint8_t *device_img, uint32_t width, uint32_t height,
                            void *stream);
 /* sRGB <-> linearRGB on premultiplied pixels: crates/resvg/src/filter/mod.rs:115-125. */
 int rgpu_filter_color_space(uint8_t *device_img, uint32_t width, uint32_t height, int to_linear, void *stream);
+/* A whole filter (region + primitive chain, as rgpu_tree_add_filter takes it)
+ * applied in place to a device pixmap that is the filtered layer, under the
+ * layer transform `ts`: crates/resvg/src/filter/mod.rs:335-354 (filter::apply).
+ * SourceGraphic is the pixmap; the filter region must cover the whole pixmap
+ * when a primitive makes a region-sized image (RGPU_ERR_UNSUPPORTED otherwise);
+ * an invalid region clears the pixmap, as in the reference. */
+int rgpu_filter_apply(const rgpu_filter *filter, const rgpu_primitive *prims, uint32_t prim_count,
+                      const int32_t *merge_inputs, uint32_t merge_count, resvg_transform ts, uint8_t *device_pixmap,
+                      uint32_t width, uint32_t height, void *stream);
 
 /* Allocation-free box blur (no counterpart in the reference): the same result
  * as rgpu_filter_box_blur, with the intermediate image in a fixed device array

@@ -45,6 +45,8 @@ def lib() -> C.CDLL:
         L.oracle_morphology.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_int, C.c_float, C.c_float]
         L.oracle_to_linear.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32]
         L.oracle_to_srgb.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32]
+        L.oracle_filter_apply.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32,
+                                          C.POINTER(C.c_float), C.c_void_p, C.c_uint32, C.c_uint32]
         _lib = L
     return _lib
 
@@ -114,6 +116,19 @@ def to_linear(img):
 
 def to_srgb(img):
     return _img_op("oracle_to_srgb", img)
+
+
+def filter_apply(img, filt, prims, merge_inputs=(), transform=(1, 0, 0, 1, 0, 0)):
+    """filter::apply on a copy of `img` (premultiplied RGBA8, (h, w, 4)); `filt`
+    and `prims` are the ctypes records the product's Tree.add_filter takes."""
+    assert img.dtype == np.uint8 and img.ndim == 3 and img.shape[2] == 4
+    out = np.ascontiguousarray(img).copy()
+    arr = (type(prims[0]) * len(prims))(*prims) if prims else None
+    m = (C.c_int32 * max(1, len(merge_inputs)))(*merge_inputs)
+    ts = (C.c_float * 6)(*[float(v) for v in transform])
+    lib().oracle_filter_apply(C.byref(filt), arr, len(prims), m, len(merge_inputs), ts, out.ctypes.data,
+                              out.shape[1], out.shape[0])
+    return out
 
 
 def _soft_struct(arrays):

@@ -1000,6 +1000,25 @@ bool filter_apply(const rgpu_tree_view &t, const rgpu_filter &f, const Transform
 }  // namespace ora
 
 extern "C" {
+// filter::apply (mod.rs:335-354) on a premultiplied RGBA8 image, in place: one
+// filter with its primitives, under the layer transform ts[6] (tests only).
+void oracle_filter_apply(const rgpu_filter *f, const rgpu_primitive *prims, uint32_t n, const int32_t *merge,
+                         uint32_t nm, const float *ts, uint8_t *img, uint32_t w, uint32_t h) {
+    rgpu_filter ff = *f;
+    ff.prim_offset = 0;
+    ff.prim_count = n;
+    const uint32_t ref = 0;
+    rgpu_tree_view view;
+    std::memset(&view, 0, sizeof(view));
+    view.filters = &ff; view.filter_count = 1;
+    view.filter_refs = &ref; view.filter_ref_count = 1;
+    view.prims = prims; view.prim_count = n;
+    view.merge_inputs = merge; view.merge_input_count = nm;
+    ora::Pixmap p(w, h);
+    std::memcpy(p.data.data(), img, (size_t)w * h * 4);
+    ora::filter_apply(view, ff, ora::Transform::from_row(ts[0], ts[1], ts[2], ts[3], ts[4], ts[5]), p);
+    std::memcpy(img, p.data.data(), (size_t)w * h * 4);
+}
 // Direct filter-kernel oracles (tests only): operate on a premultiplied RGBA8
 // image in place.
 void oracle_box_blur(uint8_t *img, uint32_t w, uint32_t h, double sx, double sy) {

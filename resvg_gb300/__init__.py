@@ -68,6 +68,11 @@ def _declare_render(L):
     if hasattr(L, "rgpu_filter_color_space"):
         L.rgpu_filter_color_space.restype = C.c_int
         L.rgpu_filter_color_space.argtypes = [P, C.c_uint32, C.c_uint32, C.c_int, P]
+    if hasattr(L, "rgpu_filter_apply"):
+        L.rgpu_filter_apply.restype = C.c_int
+        L.rgpu_filter_apply.argtypes = [C.POINTER(_abi.Filter), C.POINTER(_abi.Primitive), C.c_uint32,
+                                        C.POINTER(C.c_int32), C.c_uint32, _abi.ResvgTransform, P, C.c_uint32,
+                                        C.c_uint32, P]
 
 
 def check(status: int, what: str = "") -> None:
@@ -403,3 +408,18 @@ def morphology(tensor, dilate, rx, ry, stream=None):
 
 def color_space(tensor, to_linear, stream=None):
     return _dev_filter("rgpu_filter_color_space", tensor, int(to_linear), stream=stream)
+
+
+def filter_apply(tensor, filt: Filter, prims, merge_inputs=(), transform=(1, 0, 0, 1, 0, 0), stream=None):
+    """Applies a whole filter (region and primitive chain, as Tree.add_filter
+    takes them) in place to a CUDA uint8 tensor (h, w, 4) holding the filtered
+    layer, under the layer transform (crates/resvg/src/filter/mod.rs:335)."""
+    assert tensor.is_cuda and tensor.dtype.itemsize == 1 and tensor.dim() == 3 and tensor.shape[2] == 4
+    assert tensor.is_contiguous()
+    h, w = tensor.shape[0], tensor.shape[1]
+    arr = (Primitive * max(1, len(prims)))(*prims)
+    m = (C.c_int32 * max(1, len(merge_inputs)))(*merge_inputs)
+    check(lib().rgpu_filter_apply(C.byref(filt), arr, len(prims), m, len(merge_inputs), _rt(transform),
+                                  C.c_void_p(tensor.data_ptr()), w, h, C.c_void_p(stream) if stream else None),
+          "rgpu_filter_apply")
+    return tensor

@@ -916,4 +916,55 @@ int rgpu_filter_color_space(uint8_t *img, uint32_t w, uint32_t h, int to_linear,
     return RGPU_OK;
 }
 
+static Buffers g_fjob;
+static DevBuf g_fresult;
+int rgpu_filter_apply(const rgpu_filter *filter, const rgpu_primitive *prims, uint32_t prim_count,
+                      const int32_t *merge_inputs, uint32_t merge_count, resvg_transform ts, uint8_t *img,
+                      uint32_t w, uint32_t h, void *stream) {
+    g_last_error.clear();
+    if (!filter || (!prims && prim_count) || (!merge_inputs && merge_count) || !img || !w || !h ||
+        (uint64_t)w * h > ((uint64_t)1 << 28)) {
+        set_error("invalid arguments");
+        return RGPU_ERR_INVALID_ARG;
+    }
+    for (uint32_t i = 0; i < prim_count; i++) {
+        const rgpu_primitive &p = prims[i];
+        if (p.kind == RGPU_FE_MERGE &&
+            (p.i[0] < 0 || p.i[1] < 0 || (uint64_t)(uint32_t)p.i[0] + (uint32_t)p.i[1] > merge_count)) {
+            set_error("merge inputs out of range");
+            return RGPU_ERR_INVALID_ARG;
+        }
+    }
+    Context &c = ctx();
+    std::lock_guard<std::mutex> lock(c.mu);
+    int r = ensure_device(c);
+    if (r) return r;
+    cudaStream_t s = stream ? (cudaStream_t)stream : c.stream;
+    rgpu_filter f = *filter;
+    f.prim_offset = 0;
+    f.prim_count = prim_count;
+    const uint32_t ref = 0;
+    rgpu_tree_view view;
+    std::memset(&view, 0, sizeof(view));
+    view.filters = &f; view.filter_count = 1;
+    view.filter_refs = &ref; view.filter_ref_count = 1;
+    view.prims = prims; view.prim_count = prim_count;
+    view.merge_inputs = merge_inputs; view.merge_input_count = merge_count;
+    FilterJob job;
+    std::memset(&job, 0, sizeof(job));
+    job.w = (int32_t)w; job.h = (int32_t)h;
+    job.ts = Xf::row(ts.a, ts.b, ts.c, ts.d, ts.e, ts.f);
+    job.tree = &view;
+    job.filter_ref_offset = 0; job.filter_count = 1;
+    CK(g_fresult.ensure((size_t)w * h * 4));
+    BufScratch scratch(g_fjob);
+    std::string ferr;
+    r = run_filter_job(job, (uint32_t *)img, g_fresult.as<uint32_t>(), scratch, s, ferr);
+    if (scratch.e != cudaSuccess) CK(scratch.e);
+    if (r) { set_error("filter: %s", ferr.c_str()); return r; }
+    CK(cudaMemcpyAsync(img, g_fresult.p, (size_t)w * h * 4, cudaMemcpyDeviceToDevice, s));
+    if (!stream) CK(cudaStreamSynchronize(s));
+    return RGPU_OK;
+}
+
 }  // extern "C"

@@ -79,3 +79,44 @@ def test_config2_filter_chain(gpu, oracle_mod, seed):
     o = oracle_mod.render(t.view(), (1, 0, 0, 1, 0, 0), w, h)
     n, mx = diff_stats(g, o)
     assert mx <= 1, "%d px differ, max %d" % (n, mx)
+
+
+def _all_pairs():
+    """256 x 256 pixels: row = alpha, column = channel value (premultiplied or
+    not), so every (alpha, value) pair meets the demultiply / multiply code."""
+    c = np.arange(256, dtype=np.uint8)
+    img = np.zeros((256, 256, 4), dtype=np.uint8)
+    img[..., 0] = c[None, :]
+    img[..., 1] = 255 - c[None, :]
+    img[..., 2] = (c[None, :].astype(np.uint16) * 7 % 256).astype(np.uint8)
+    img[..., 3] = c[:, None]
+    return img
+
+
+@pytest.mark.parametrize("to_linear", [True, False])
+def test_color_space_every_alpha_value_pair(gpu, oracle_mod, to_linear):
+    img = _all_pairs()
+    g = _on_gpu(R.color_space, img, to_linear)
+    o = oracle_mod.to_linear(img) if to_linear else oracle_mod.to_srgb(img)
+    assert diff_stats(g, o) == (0, 0)
+
+
+@pytest.mark.parametrize("kind", ["saturate", "transfer"])
+def test_demultiply_multiply_every_pair(gpu, oracle_mod, kind):
+    # colour matrix and component transfer both demultiply, map and multiply
+    from resvg_gb300 import _abi as A
+    img = _all_pairs()
+    p = A.Primitive()
+    p.x, p.y, p.w, p.h = 0.0, 0.0, 256.0, 256.0
+    p.in1 = p.in2 = A.IN_SOURCE_GRAPHIC
+    if kind == "saturate":
+        p.kind, p.i[0], p.f[0] = A.FE_COLOR_MATRIX, A.CM_SATURATE, 0.7
+    else:
+        p.kind = A.FE_COMPONENT_TRANSFER
+        p.i[0], p.i[4], p.f[0], p.f[1] = A.TF_TABLE, 2, 0.1, 0.9
+        p.i[3], p.f[48], p.f[49] = A.TF_LINEAR, 1.0, 0.0
+    f = A.Filter()
+    f.x, f.y, f.w, f.h = 0.0, 0.0, 256.0, 256.0
+    o = oracle_mod.filter_apply(img, f, [p])
+    g = _on_gpu(lambda t: R.filter_apply(t, f, [p]), img)
+    assert diff_stats(g, o) == (0, 0)
