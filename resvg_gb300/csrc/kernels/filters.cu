@@ -278,9 +278,16 @@ __device__ __forceinline__ bool approx_zero_ulps4(float v) {
     if (a < 0) return v == 0.0f;
     return a <= 4;
 }
-__device__ __forceinline__ uint32_t arithmetic_px(uint32_t c1, uint32_t c2, float k1, float k2, float k3, float k4) {
+// c / 255 in f32 for every u8 c, the IEEE quotient (host division is IEEE
+// too): kernels read it from shared memory instead of dividing per channel.
+__device__ float g_unit[256];
+__device__ __forceinline__ void load_unit(float *u) {
+    for (int k = threadIdx.x; k < 256; k += blockDim.x) u[k] = g_unit[k];
+}
+__device__ __forceinline__ uint32_t arithmetic_px(uint32_t c1, uint32_t c2, float k1, float k2, float k3, float k4,
+                                                  const float *u) {
     auto calc = [&](uint32_t i1, uint32_t i2, float mx) {
-        float a = (float)i1 / 255.0f, b = (float)i2 / 255.0f;
+        float a = u[i1], b = u[i2];
         float r = k1 * a * b + k2 * a + k3 * b + k4;
         return f32_bound(0.0f, r, mx);
     };
@@ -291,19 +298,32 @@ __device__ __forceinline__ uint32_t arithmetic_px(uint32_t c1, uint32_t c2, floa
 }
 __global__ void k_arithmetic(const uint32_t *s1, const uint32_t *s2, uint32_t *dst, size_t n, float k1, float k2,
                              float k3, float k4) {
-    const size_t i = 4 * ((size_t)blockIdx.x * blockDim.x + threadIdx.x);
-    if (i >= n) return;
-    if (vec4(s1, i, n) && vec4(s2, i, n) && vec4(dst, i, n)) {
-        const uint4 a = *reinterpret_cast<const uint4 *>(s1 + i), b = *reinterpret_cast<const uint4 *>(s2 + i);
-        *reinterpret_cast<uint4 *>(dst + i) =
-            make_uint4(arithmetic_px(a.x, b.x, k1, k2, k3, k4), arithmetic_px(a.y, b.y, k1, k2, k3, k4),
-                       arithmetic_px(a.z, b.z, k1, k2, k3, k4), arithmetic_px(a.w, b.w, k1, k2, k3, k4));
-    } else {
-        for (size_t k = i; k < n && k < i + 4; k++) dst[k] = arithmetic_px(s1[k], s2[k], k1, k2, k3, k4);
+    __shared__ float u[256];
+    load_unit(u);
+    __syncthreads();
+    for (size_t i = 4 * ((size_t)blockIdx.x * blockDim.x + threadIdx.x); i < n; i += 4 * (size_t)gridDim.x * blockDim.x) {
+        if (vec4(s1, i, n) && vec4(s2, i, n) && vec4(dst, i, n)) {
+            const uint4 a = *reinterpret_cast<const uint4 *>(s1 + i), b = *reinterpret_cast<const uint4 *>(s2 + i);
+            *reinterpret_cast<uint4 *>(dst + i) =
+                make_uint4(arithmetic_px(a.x, b.x, k1, k2, k3, k4, u), arithmetic_px(a.y, b.y, k1, k2, k3, k4, u),
+                           arithmetic_px(a.z, b.z, k1, k2, k3, k4, u), arithmetic_px(a.w, b.w, k1, k2, k3, k4, u));
+        } else {
+            for (size_t k = i; k < n && k < i + 4; k++) dst[k] = arithmetic_px(s1[k], s2[k], k1, k2, k3, k4, u);
+        }
     }
 }
 
 inline uint32_t nblk(size_t n, uint32_t t) { return (uint32_t)((n + t - 1) / t); }
+// at most 8 CTAs per SM, for grid-stride kernels that set up shared tables
+uint32_t nblk_capped(size_t n, uint32_t t) {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 1;
+    }
+    return std::max<uint32_t>(1u, std::min<uint32_t>(nblk(n, t), (uint32_t)sms * 8u));
+}
 
 uint32_t host_sat_u8(float v) {
     if (!(v > 0.0f)) return 0;
@@ -317,6 +337,9 @@ cudaError_t ensure_luts() {
     if (g_luts_ready) return cudaSuccess;
     cudaError_t e = cudaMemcpyToSymbol(c_srgb_to_linear, kSrgbToLinear, 256);
     if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_linear_to_srgb, kLinearToSrgb, 256);
+    float unit[256];
+    for (int k = 0; k < 256; k++) unit[k] = (float)k / 255.0f;
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_unit, unit, sizeof(unit));
     // the same f32 operations as demul / mul (host and device division and
     // multiplication are both IEEE round-to-nearest, without contraction)
     uint8_t (*t)[256 * 256] = g_host_tab;
@@ -786,7 +809,9 @@ cudaError_t filter_morphology(uint32_t *img, uint32_t *tmp, int w, int h, bool d
 cudaError_t filter_arithmetic(const uint32_t *a, const uint32_t *b, uint32_t *dst, size_t n, const float k[4],
                               cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    k_arithmetic<<<nblk((n + 3) / 4, 256), 256, 0, s>>>(a, b, dst, n, k[0], k[1], k[2], k[3]);
+    cudaError_t e = ensure_luts();
+    if (e != cudaSuccess) return e;
+    k_arithmetic<<<nblk_capped((n + 3) / 4, 256), 256, 0, s>>>(a, b, dst, n, k[0], k[1], k[2], k[3]);
     return cudaGetLastError();
 }
 
@@ -856,10 +881,17 @@ cudaError_t filter_alpha_only(uint32_t *img, size_t n, cudaStream_t s) {
 }
 namespace {
 
+constexpr int kConvRows = 8;  // output rows per thread
 __global__ void k_convolve(const uint32_t *src, uint32_t *dst, int w, int h, ConvolveParams cp) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
-    if (x >= w || y >= h) return;
+    __shared__ float u[256];
+    __shared__ float kf[sizeof(cp.k) / sizeof(float)];  // the kernel, flipped: kf[oy * cols + ox]
+    load_unit(u);
+    for (int k = threadIdx.x; k < cp.rows * cp.cols; k += blockDim.x) kf[k] = cp.k[cp.rows * cp.cols - 1 - k];
+    __syncthreads();
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= w) return;
     const bool pres = cp.preserve_alpha != 0;
+    for (int y = blockIdx.y * kConvRows; y < min(h, (int)(blockIdx.y + 1) * kConvRows); y++) {
     float nr = 0.0f, ng = 0.0f, nb = 0.0f, na = 0.0f;
     for (int oy = 0; oy < cp.rows; oy++)
         for (int ox = 0; ox < cp.cols; ox++) {
@@ -873,15 +905,15 @@ __global__ void k_convolve(const uint32_t *src, uint32_t *dst, int w, int h, Con
                 tx = ((tx % w) + w) % w;
                 ty = ((ty % h) + h) % h;
             }
-            const float kv = cp.k[(cp.rows - oy - 1) * cp.cols + (cp.cols - ox - 1)];
+            const float kv = kf[oy * cp.cols + ox];
             uint32_t p = src[(size_t)ty * w + tx];
             if (pres) p = demul(p);
-            nr += __fdiv_rn((float)chn(p, 0), 255.0f) * kv;
-            ng += __fdiv_rn((float)chn(p, 1), 255.0f) * kv;
-            nb += __fdiv_rn((float)chn(p, 2), 255.0f) * kv;
-            if (!pres) na += __fdiv_rn((float)chn(p, 3), 255.0f) * kv;
+            nr += u[chn(p, 0)] * kv;
+            ng += u[chn(p, 1)] * kv;
+            nb += u[chn(p, 2)] * kv;
+            if (!pres) na += u[chn(p, 3)] * kv;
         }
-    if (pres) na = __fdiv_rn((float)chn(src[(size_t)y * w + x], 3), 255.0f);
+    if (pres) na = u[chn(src[(size_t)y * w + x], 3)];
     else na = __fdiv_rn(na, cp.divisor) + cp.bias;
     const float bna = f32_bound(0.0f, na, 1.0f);
     auto calc = [&](float v) {
@@ -890,6 +922,7 @@ __global__ void k_convolve(const uint32_t *src, uint32_t *dst, int w, int h, Con
         return sat_u8f(q * 255.0f + 0.5f);
     };
     dst[(size_t)y * w + x] = pk(calc(nr), calc(ng), calc(nb), sat_u8f(bna * 255.0f + 0.5f));
+    }
 }
 
 // ApproxEqUlps(4) of two f32s, as in float-cmp
@@ -995,7 +1028,10 @@ __global__ void k_lighting(const uint32_t *src, uint32_t *dst, int w, int h, Lig
 cudaError_t filter_convolve(const uint32_t *src, uint32_t *dst, int w, int h, const ConvolveParams &cp,
                             cudaStream_t s) {
     if (w <= 0 || h <= 0) return cudaSuccess;
-    k_convolve<<<dim3((unsigned)((w + 127) / 128), (unsigned)h), 128, 0, s>>>(src, dst, w, h, cp);
+    cudaError_t e = ensure_luts();
+    if (e != cudaSuccess) return e;
+    k_convolve<<<dim3((unsigned)((w + 127) / 128), (unsigned)((h + kConvRows - 1) / kConvRows)), 128, 0, s>>>(
+        src, dst, w, h, cp);
     return cudaGetLastError();
 }
 
