@@ -132,7 +132,7 @@ enum rgpu_prim_kind {
     RGPU_FE_BLUR = 0, RGPU_FE_COLOR_MATRIX, RGPU_FE_MORPHOLOGY, RGPU_FE_COMPOSITE,
     RGPU_FE_CONVOLVE, RGPU_FE_DIFFUSE, RGPU_FE_SPECULAR, RGPU_FE_FLOOD, RGPU_FE_OFFSET,
     RGPU_FE_MERGE, RGPU_FE_BLEND, RGPU_FE_COMPONENT_TRANSFER, RGPU_FE_DROP_SHADOW,
-    RGPU_FE_TURBULENCE, RGPU_FE_TILE, RGPU_FE_DISPLACEMENT_MAP
+    RGPU_FE_TURBULENCE, RGPU_FE_TILE, RGPU_FE_DISPLACEMENT_MAP, RGPU_FE_IMAGE
 };
 
 /* inputs */
@@ -176,6 +176,8 @@ enum rgpu_transfer_kind { RGPU_TF_IDENTITY = 0, RGPU_TF_TABLE, RGPU_TF_DISCRETE,
  *   TILE:         in1 only
  *   DISPLACEMENT_MAP: i[0]=xChannelSelector i[1]=yChannelSelector (0..3 = R, G, B, A);
  *                 f[0]=scale; in1 = the image displaced, in2 = the map
+ *   IMAGE:        i[0]=a detached group whose children are rendered (feImage of an
+ *                 element), or -1 for nothing (transparent)
  */
 #define RGPU_TURB_MAX_OCTAVES 1024
 #define RGPU_PRIM_F 64

@@ -27,6 +27,7 @@
 #include "raster.h"
 
 namespace ora {
+void render_group_children(const rgpu_tree_view &t, uint32_t gi, const Transform &ts, Pixmap &pm);
 
 namespace {
 
@@ -886,6 +887,18 @@ bool filter_apply(const rgpu_tree_view &t, const rgpu_filter &f, const Transform
             auto pm = std::make_shared<Pixmap>((uint32_t)region.w, (uint32_t)region.h);
             lighting(p.kind == RGPU_FE_SPECULAR, p, ts, region, *in.image, *pm);
             res = Image{pm, IntRect{0, 0, (int32_t)pm->width, (int32_t)pm->height}, lin};
+            break;
+        }
+        case RGPU_FE_IMAGE: {
+            // apply_image (mod.rs:861-889): the element at the layer's scale, moved
+            // to the subregion, in a region-sized sRGB image
+            auto pm = std::make_shared<Pixmap>((uint32_t)region.w, (uint32_t)region.h);
+            float sx, sy;
+            ts.get_scale(&sx, &sy);
+            if (p.i[0] >= 0 && (uint32_t)p.i[0] < t.group_count)
+                render_group_children(t, (uint32_t)p.i[0],
+                                      Transform::from_row(sx, 0, 0, sy, (float)subregion.x, (float)subregion.y), *pm);
+            res = Image{pm, IntRect{0, 0, (int32_t)pm->width, (int32_t)pm->height}, false};
             break;
         }
         case RGPU_FE_TILE: {

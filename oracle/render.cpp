@@ -293,6 +293,13 @@ IntRect max_filter_bbox(uint32_t w, uint32_t h) {
 
 }  // namespace
 
+// filter/mod.rs:861-889 (apply_image): a group's children rendered into a
+// pixmap whose own bounds are the layer limit
+void render_group_children(const rgpu_tree_view &t, uint32_t gi, const Transform &ts, Pixmap &pm) {
+    Ctx c{t, IntRect{0, 0, (int32_t)pm.width, (int32_t)pm.height}};
+    render_nodes(c, gi, ts, pm);
+}
+
 // lib.rs:34-43
 void render_tree(const rgpu_tree_view &t, const Transform &ts, Pixmap &pm) {
     Ctx c{t, max_filter_bbox(pm.width, pm.height)};

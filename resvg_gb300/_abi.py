@@ -134,7 +134,7 @@ BLEND = {n: i for i, n in enumerate([
     "exclusion", "multiply", "hue", "saturation", "color", "luminosity"])}
 FE_BLUR, FE_COLOR_MATRIX, FE_MORPHOLOGY, FE_COMPOSITE, FE_CONVOLVE, FE_DIFFUSE, FE_SPECULAR, FE_FLOOD, \
     FE_OFFSET, FE_MERGE, FE_BLEND, FE_COMPONENT_TRANSFER, FE_DROP_SHADOW, FE_TURBULENCE, FE_TILE, \
-    FE_DISPLACEMENT_MAP = range(16)
+    FE_DISPLACEMENT_MAP, FE_IMAGE = range(17)
 IN_SOURCE_GRAPHIC, IN_SOURCE_ALPHA = -1, -2
 CM_MATRIX, CM_SATURATE, CM_HUE_ROTATE, CM_LUM_TO_ALPHA = range(4)
 OP_OVER, OP_IN, OP_OUT, OP_ATOP, OP_XOR, OP_ARITHMETIC = range(6)

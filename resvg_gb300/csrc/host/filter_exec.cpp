@@ -154,7 +154,7 @@ struct Runner {
 }  // namespace
 
 int run_filter_job(const FilterJob &job, uint32_t *content, uint32_t *result, FilterScratch &scratch, cudaStream_t s,
-                   std::string &err) {
+                   std::string &err, const std::vector<FeImageSurface> *images) {
     const rgpu_tree_view &t = *job.tree;
     Runner r{scratch, s, job.w, job.h, (size_t)job.w * job.h};
     // the layer the filters act on, in place, one filter after another
@@ -364,6 +364,22 @@ int run_filter_job(const FilterJob &job, uint32_t *content, uint32_t *result, Fi
                 uint32_t *o = r.fresh();
                 r.ck(filter_lighting(in.p, o, r.w, r.h, lp, s));
                 res = Img{o, lin};
+                break;
+            }
+            case RGPU_FE_IMAGE: {
+                // apply_image (mod.rs:861-889): the element was rendered into a
+                // surface of its own before the job; an sRGB image
+                const uint32_t *src = nullptr;
+                if (images)
+                    for (const auto &im : *images)
+                        if (im.prim == f.prim_offset + pi) src = im.p;
+                if (!src) {
+                    err = "feImage without its rendered element";
+                    return RGPU_ERR_UNSUPPORTED;
+                }
+                uint32_t *o = r.fresh();
+                r.ck(filter_copy(src, o, r.n, s));
+                res = Img{o, false};
                 break;
             }
             case RGPU_FE_TILE: {

@@ -3,6 +3,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <string>
+#include <vector>
 #include "flatten.h"
 
 namespace rgpu {
@@ -18,7 +19,10 @@ struct FilterScratch {
 
 // Applies the job's filters to `content` (w x h, premultiplied sRGB) and
 // writes the filtered layer to `result`.  Returns 0 or an rgpu_status.
+// `images` holds, for each feImage primitive (global index), the surface its
+// element was rendered into; NULL when there are none.
+struct FeImageSurface { uint32_t prim; const uint32_t *p; };
 int run_filter_job(const FilterJob &job, uint32_t *content, uint32_t *result, FilterScratch &scratch, cudaStream_t s,
-                   std::string &err);
+                   std::string &err, const std::vector<FeImageSurface> *images = nullptr);
 
 }  // namespace rgpu

@@ -460,7 +460,47 @@ struct Flattener {
         depth = saved_depth;
         child_level = std::max(saved_child, sub.level + 1);
         sb.append_stream(sub);
+        // feImage of an element (filter/mod.rs:861-889): the element's group,
+        // scaled by the layer's scale and moved to the primitive subregion,
+        // rendered into a layer-sized surface of its own
+        uint32_t image_first = (uint32_t)sb.fe_images.size(), level = sub.level;
+        for (uint32_t fi = 0; fi < g.filter_count; fi++) {
+            const rgpu_filter &f = t.filters[t.filter_refs[g.filter_offset + fi]];
+            for (uint32_t pi = 0; pi < f.prim_count; pi++) {
+                const rgpu_primitive &p = t.prims[f.prim_offset + pi];
+                if (p.kind != RGPU_FE_IMAGE) continue;
+                uint32_t surf = (uint32_t)sb.surfaces.size();
+                sb.surfaces.push_back(SurfaceReq{w, h});
+                float b[4];
+                float sx = std::sqrt(lts.sx * lts.sx + lts.kx * lts.kx), sy = std::sqrt(lts.ky * lts.ky + lts.sy * lts.sy);
+                float ox = 0.0f, oy = 0.0f;
+                if (map_rect(lts, p.x, p.y, p.x + p.w, p.y + p.h, b)) {
+                    ox = (float)sat_i32(std::floor(b[0]));
+                    oy = (float)sat_i32(std::floor(b[1]));
+                }
+                StreamBuild im;
+                im.out_w = w; im.out_h = h;
+                im.stride = (uint32_t)w * 4;
+                im.surface = (int32_t)surf;
+                StreamBuild *sv = cur;
+                uint32_t sd = depth, sc = child_level;
+                cur = &im;
+                depth = 0;
+                child_level = 0;
+                if (p.i[0] >= 0 && (uint32_t)p.i[0] < t.group_count)
+                    render_nodes((uint32_t)p.i[0], Xf::row(sx, 0, 0, sy, ox, oy), Target{w, h, 0, 0});
+                im.level = child_level;
+                cur = sv;
+                depth = sd;
+                child_level = std::max(sc, im.level + 1);
+                sb.append_stream(im);
+                level = std::max(level, im.level);
+                sb.fe_images.push_back(FeImageReq{f.prim_offset + pi, surf});
+            }
+        }
         FilterJob job;
+        job.image_first = image_first;
+        job.image_count = (uint32_t)sb.fe_images.size() - image_first;
         job.content = content;
         job.result = result;
         job.w = w; job.h = h;
@@ -468,7 +508,7 @@ struct Flattener {
         job.tree = &t;
         job.filter_ref_offset = g.filter_offset;
         job.filter_count = g.filter_count;
-        job.level = sub.level;
+        job.level = level;
         sb.jobs.push_back(job);
         return (int32_t)result;
     }

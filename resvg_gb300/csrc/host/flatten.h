@@ -29,6 +29,13 @@ struct FilterJob {
     const rgpu_tree_view *tree;
     uint32_t filter_ref_offset, filter_count;
     uint32_t level;                 // runs after the raster pass of this level
+    uint32_t image_first, image_count;  // its feImage renders in SceneBuild::fe_images
+};
+
+// A feImage primitive's element, rendered into its own surface before the job.
+struct FeImageReq {
+    uint32_t prim;     // global primitive index
+    uint32_t surface;
 };
 
 struct StreamBuild {
@@ -52,6 +59,7 @@ struct SceneBuild {
     std::vector<StreamRec> streams;
     std::vector<SurfaceReq> surfaces;
     std::vector<FilterJob> jobs;
+    std::vector<FeImageReq> fe_images;
     std::vector<HairRec> hairs;       // anti-aliased hairline strokes
     std::vector<HairSpan> hair_spans;
     std::vector<uint32_t> fill_cmds;  // per stream: its fill / region command indices (plan_scene)

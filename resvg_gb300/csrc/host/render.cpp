@@ -409,8 +409,13 @@ int enqueue_plan(Context &c, Buffers &b, Plan &p, cudaStream_t s, RasterTimer *t
         for (const auto &job : sb.jobs) {
             if (job.level != lv) continue;
             std::string ferr;
+            std::vector<FeImageSurface> ims;
+            for (uint32_t k = 0; k < job.image_count; k++) {
+                const FeImageReq &q = sb.fe_images[job.image_first + k];
+                ims.push_back(FeImageSurface{q.prim, b.surf[q.surface].as<uint32_t>()});
+            }
             int r = run_filter_job(job, b.surf[job.content].as<uint32_t>(), b.surf[job.result].as<uint32_t>(), scratch,
-                                   s, ferr);
+                                   s, ferr, &ims);
             if (scratch.e != cudaSuccess) CK(scratch.e);
             if (r) { set_error("filter: %s", ferr.c_str()); return r; }
         }

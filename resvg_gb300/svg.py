@@ -727,7 +727,6 @@ INHERITED = {"fill", "fill-opacity", "fill-rule", "stroke", "stroke-width", "str
 NON_INHERITED = {"opacity", "clip-path", "mask", "filter", "mix-blend-mode", "isolation", "display",
                  "stop-color", "stop-opacity", "flood-color", "flood-opacity", "transform"}
 UNSUPPORTED_ELEMS = {"text", "image", "pattern", "marker", "switch", "foreignObject", "tspan", "textPath", "symbol",
-                     "feImage",
                      "style", "animate", "set"}
 BLEND = {"normal": "source-over", "multiply": "multiply", "screen": "screen", "overlay": "overlay",
          "darken": "darken", "lighten": "lighten", "color-dodge": "color-dodge", "color-burn": "color-burn",
@@ -756,6 +755,26 @@ class Loader:
                 self.ids[i] = e
         self.parent = {c: p for p in self.root.iter() for c in p}
         self.tree_cls = tree_cls
+        # usvg's recursive-link fix for feImage: an element that a filter's
+        # feImage links to drops its `filter` attribute when it, or an element
+        # inside it, uses that same filter
+        self.no_filter = set()
+        for f in self.root.iter():
+            if _tag(f) != "filter" or not f.get("id"):
+                continue
+            for c in f:
+                if _tag(c) != "feImage":
+                    continue
+                href = (c.get(XLINK) or c.get("href") or "").strip()
+                target = self.ids.get(href[1:]) if href.startswith("#") else None
+                if target is None:
+                    continue
+                for n in target.iter():
+                    if not isinstance(n.tag, str):
+                        continue
+                    fv = self.attrs(n).get("filter") or ""
+                    if re.search(r"url\(\s*['\"]?#" + re.escape(f.get("id")) + r"['\"]?\s*\)", fv):
+                        self.no_filter.add(n)
         for e in self.root.iter():
             if _tag(e) in UNSUPPORTED_ELEMS:
                 raise Unsupported("element " + _tag(e))
@@ -950,7 +969,7 @@ class Builder(Loader):
         opacity = max(0.0, min(1.0, opacity))
         clip = self.ref(a.get("clip-path"))
         mask = self.ref(a.get("mask"))
-        filt = a.get("filter")
+        filt = a.get("filter") if e not in self.no_filter else None
         # mix-blend-mode and isolation count only as CSS properties (style), not as
         # presentation attributes
         css = {}
@@ -1628,6 +1647,27 @@ class Builder(Loader):
             for k in range(16):
                 p.f[16 * ch + k] = vals[k] if k < len(vals) else 0.0
 
+    def fe_image(self, c, p, fe, dummy):
+        """feImage of an element (parser/filter.rs:821-852): the element converted
+        under a detached group whose children the primitive renders.  No href
+        or a missing element gives usvg's transparent stand-in; an image file
+        or data URL is not supported.  Recursive links are cut when the
+        document is read (no_filter)."""
+        href = (c.get(XLINK) or c.get("href") or "").strip()
+        if not href:
+            dummy(p)
+            return
+        if not href.startswith("#"):
+            raise Unsupported("feImage of an image")
+        ref = self.ids.get(href[1:])
+        if ref is None:
+            dummy(p)
+            return
+        root = self.tree.add_group(-1, _group())
+        self.node(ref, root)
+        p.kind = A.FE_IMAGE
+        p.i[0] = root
+
     def filter_function(self, e, fn, bbox):
         """One CSS filter function as usvg lowers it (parser/filter.rs:36-84 and
         :1088-1290): a filter of one sRGB primitive on SourceGraphic whose
@@ -1865,6 +1905,8 @@ class Builder(Loader):
                 p.f[0], p.f[1] = dx if dx is not None else 0.0, dy if dy is not None else 0.0
             elif tag == "feComponentTransfer":
                 self.component_transfer(c, p)
+            elif tag == "feImage":
+                self.fe_image(c, p, fe, dummy)
             elif tag == "feTile":
                 p.kind = A.FE_TILE
             elif tag == "feDisplacementMap":

@@ -48,7 +48,7 @@ CATEGORIES = [
     "filters/feConvolveMatrix", "filters/feDiffuseLighting", "filters/feSpecularLighting",
     "filters/feDistantLight", "filters/fePointLight", "filters/feSpotLight",
     "filters/filter-functions", "filters/feComponentTransfer", "filters/feDropShadow",
-    "filters/feTurbulence", "filters/feTile", "filters/feDisplacementMap",
+    "filters/feTurbulence", "filters/feTile", "filters/feDisplacementMap", "filters/feImage",
 ]
 IMAGE_SIZE = 300
 FIXTURES_PER_DIR = 4

@@ -1,5 +1,6 @@
 """feComponentTransfer, feDropShadow, feTurbulence, feTile,
-feDisplacementMap and the CSS filter functions on the GPU vs the CPU oracle.
+feDisplacementMap, feImage and the CSS filter functions on the GPU vs the CPU
+oracle.
 
 The transfer functions are evaluated on the host into one 256-entry table per
 channel with the same f32 operations as the oracle (powf included), so the
@@ -73,6 +74,20 @@ TILE_DISPLACE = [
     '<feDisplacementMap in2="SourceAlpha" scale="-3" xChannelSelector="A" yChannelSelector="B"/>',
 ]
 
+# feImage of an element: each scene defines #img (the scene content's own
+# gradient is reused) before the filter
+FE_IMAGE_DEFS = ('<defs><g id="img" opacity="0.8"><rect x="10" y="30" width="90" height="60" fill="#3a7" '
+                 'transform="rotate(15 50 60)"/><circle cx="120" cy="100" r="40" fill="url(#rg)"/></g>'
+                 '<filter id="inner" x="0" y="0" width="200" height="200" filterUnits="userSpaceOnUse">'
+                 '<feGaussianBlur stdDeviation="2"/></filter>'
+                 '<rect id="blurred" x="30" y="30" width="100" height="80" fill="#e52" filter="url(#inner)"/></defs>')
+FE_IMAGE = [
+    '<feImage href="#img"/>',
+    '<feImage href="#img" x="20" y="10" width="150" height="120"/><feComposite in2="SourceGraphic" operator="over"/>',
+    '<feImage href="#blurred"/><feBlend in2="SourceGraphic" mode="multiply"/>',
+    '<feImage href="#missing"/><feMerge><feMergeNode/><feMergeNode in="SourceGraphic"/></feMerge>',
+]
+
 FUNCTIONS = [
     'blur(3)',
     'drop-shadow(blue 4 5 6) grayscale(0.3)',
@@ -123,6 +138,15 @@ def test_turbulence_exact(gpu, oracle_mod, k, cif, ts):
 @pytest.mark.parametrize("k", range(len(TILE_DISPLACE)))
 def test_tile_displacement_exact(gpu, oracle_mod, k, cif, ts):
     g, o = _render_both(oracle_mod, _scene(TILE_DISPLACE[k], cif), ts)
+    assert diff_stats(g, o) == (0, 0)
+
+
+@pytest.mark.parametrize("ts", TRANSFORMS)
+@pytest.mark.parametrize("k", range(len(FE_IMAGE)))
+def test_fe_image_exact(gpu, oracle_mod, k, ts):
+    text = _scene(FE_IMAGE[k]).replace("<filter id=\"f\"", FE_IMAGE_DEFS + "<filter id=\"f\"", 1)
+    g, o = _render_both(oracle_mod, text, ts)
+    assert o[..., 3].any()
     assert diff_stats(g, o) == (0, 0)
 
 
