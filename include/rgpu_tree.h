@@ -47,7 +47,11 @@ enum rgpu_blend {
     RGPU_BLEND_LUMINOSITY
 };
 
-enum rgpu_paint_kind { RGPU_PAINT_SOLID = 0, RGPU_PAINT_LINEAR = 1, RGPU_PAINT_RADIAL = 2 };
+enum rgpu_paint_kind { RGPU_PAINT_SOLID = 0, RGPU_PAINT_LINEAR = 1, RGPU_PAINT_RADIAL = 2, RGPU_PAINT_PATTERN = 3 };
+/* A pattern (usvg::Pattern, resolved to user space): x1, y1, x2, y2 = the tile
+ * rect x, y, width, height; transform = patternTransform; stop_offset = a
+ * detached group whose children are the tile content (viewBox and content
+ * units already applied); stop_count = 0. */
 enum rgpu_spread { RGPU_SPREAD_PAD = 0, RGPU_SPREAD_REFLECT = 1, RGPU_SPREAD_REPEAT = 2 };
 enum rgpu_cap { RGPU_CAP_BUTT = 0, RGPU_CAP_ROUND = 1, RGPU_CAP_SQUARE = 2 };
 enum rgpu_join { RGPU_JOIN_MITER = 0, RGPU_JOIN_MITER_CLIP = 1, RGPU_JOIN_ROUND = 2, RGPU_JOIN_BEVEL = 3 };

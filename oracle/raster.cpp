@@ -1529,6 +1529,62 @@ static void blend_sep(uint32_t mode, const float s[4], const float d[4], float o
 }
 
 // The blitter restated: RasterPipelineBlitter::new + blit_h / blit_anti_h.
+// tiny-skia's Pattern shader (shaders/pattern.rs) in the highp pipeline:
+// seed_shader (pixel centre), the inverse transform, then either nearest
+// (repeat, gather) or bicubic (4x4 taps, each tiled with repeat and gathered,
+// weights 1/18 * (1 + 9t + 27t^2 - 21t^3) and t^2 (7t - 6) / 18), clamp_0,
+// clamp_a, and the opacity scale.
+static inline float ulp_below(float v) {
+    uint32_t b;
+    std::memcpy(&b, &v, 4);
+    b -= 1;
+    std::memcpy(&v, &b, 4);
+    return v;
+}
+static void pattern_gather(const Pixmap &pm, float x, float y, float c[4]) {
+    const float w = (float)pm.width, h = (float)pm.height;
+    x = x - std::floor(x * (1.0f / w)) * w;
+    y = y - std::floor(y * (1.0f / h)) * h;
+    x = std::min(std::max(x, 0.0f), ulp_below(w));
+    y = std::min(std::max(y, 0.0f), ulp_below(h));
+    const uint8_t *p = pm.px((uint32_t)x, (uint32_t)y);
+    for (int i = 0; i < 4; i++) c[i] = (float)p[i] * (1.0f / 255.0f);
+}
+static inline float bicubic_near(float t) {
+    return t * (t * ((-21.0f / 18.0f) * t + 27.0f / 18.0f) + 9.0f / 18.0f) + 1.0f / 18.0f;
+}
+static inline float bicubic_far(float t) { return (t * t) * ((7.0f / 18.0f) * t + (-6.0f / 18.0f)); }
+static void pattern_eval(const Shader &sh, const Transform &inv, bool nearest, int32_t x, int32_t y, float out[4]) {
+    const float px = (float)x + 0.5f, py = (float)y + 0.5f;
+    const float u = px * inv.sx + (py * inv.kx + inv.tx);
+    const float v = px * inv.ky + (py * inv.sy + inv.ty);
+    if (nearest) {
+        pattern_gather(*sh.pattern, u, v, out);
+    } else {
+        const float fx = (u + 0.5f) - std::floor(u + 0.5f), fy = (v + 0.5f) - std::floor(v + 0.5f);
+        const float wx[4] = {bicubic_far(1.0f - fx), bicubic_near(1.0f - fx), bicubic_near(fx), bicubic_far(fx)};
+        const float wy[4] = {bicubic_far(1.0f - fy), bicubic_near(1.0f - fy), bicubic_near(fy), bicubic_far(fy)};
+        float acc[4] = {0, 0, 0, 0};
+        float sy = v - 1.5f;
+        for (int j = 0; j < 4; j++) {
+            float sx = u - 1.5f;
+            for (int i = 0; i < 4; i++) {
+                float c[4];
+                pattern_gather(*sh.pattern, sx, sy, c);
+                const float wgt = wx[i] * wy[j];
+                for (int k = 0; k < 4; k++) acc[k] = wgt * c[k] + acc[k];
+                sx += 1.0f;
+            }
+            sy += 1.0f;
+        }
+        for (int k = 0; k < 4; k++) acc[k] = std::max(acc[k], 0.0f);
+        for (int k = 0; k < 3; k++) acc[k] = std::min(acc[k], acc[3]);
+        for (int k = 0; k < 4; k++) out[k] = acc[k];
+    }
+    if (sh.opacity != 1.0f)
+        for (int k = 0; k < 4; k++) out[k] = out[k] * sh.opacity;
+}
+
 struct PipelineBlitter {
     Pixmap *pm = nullptr;
     uint32_t blend;
@@ -1539,6 +1595,8 @@ struct PipelineBlitter {
     float colorf[4];             // highp uniform colour (premultiplied)
     const Shader *shader = nullptr;
     GradientCtx grad;
+    Transform pinv;
+    bool pnearest = false;
     bool skip = false;
 
     bool setup(Pixmap &p, const Paint &paint) {
@@ -1560,6 +1618,9 @@ struct PipelineBlitter {
             if (blend == RGPU_BLEND_SOURCE) memset_ok = true;
         } else if (paint.shader.kind == SHADER_LINEAR || paint.shader.kind == SHADER_RADIAL) {
             if (!gradient_setup(paint.shader, grad)) { skip = true; return false; }
+        } else if (paint.shader.kind == SHADER_PATTERN) {
+            if (!paint.shader.pattern || !paint.shader.transform.invert(&pinv)) { skip = true; return false; }
+            pnearest = pinv.sx == 1.0f && pinv.sy == 1.0f && pinv.kx == 0.0f && pinv.ky == 0.0f;
         }
         if (blend == RGPU_BLEND_CLEAR && !paint.anti_alias) {
             blend = RGPU_BLEND_SOURCE;
@@ -1626,6 +1687,8 @@ struct PipelineBlitter {
         float s[4];
         if (shader->kind == SHADER_SOLID) {
             for (int i = 0; i < 4; i++) s[i] = colorf[i];
+        } else if (shader->kind == SHADER_PATTERN) {
+            pattern_eval(*shader, pinv, pnearest, x, y, s);
         } else {
             ColorF c;
             if (!gradient_eval(grad, shader->spread, x, y, &c)) c = ColorF{0, 0, 0, 0};
@@ -1661,7 +1724,8 @@ void fill_path(Pixmap &pm, const Path &path_in, const Paint &paint_in, uint32_t 
     Paint paint = paint_in;
     if (!ts.is_identity()) {
         if (!path.transform(ts)) return;
-        if (paint.shader.kind == SHADER_LINEAR || paint.shader.kind == SHADER_RADIAL)
+        if (paint.shader.kind == SHADER_LINEAR || paint.shader.kind == SHADER_RADIAL ||
+            paint.shader.kind == SHADER_PATTERN)
             paint.shader.transform = paint.shader.transform.post_concat(ts);
     } else {
         path.compute_bounds();

@@ -17,6 +17,7 @@
 #pragma once
 #include <cstdint>
 #include <cmath>
+#include <memory>
 #include <vector>
 #include "rgpu_tree.h"
 
@@ -104,8 +105,11 @@ struct Shader {
     Transform transform;          // gradient -> user space (gradientTransform, then paint transform)
     Point p0{0, 0}, p1{0, 0};     // linear start/end; radial: start(focal), end(centre)
     float r0 = 0, r1 = 0;         // radial radii (focal radius, radius)
-    // pattern
+    // pattern: the tile pixmap (kept alive by pattern_owner), sampled through
+    // `transform` (tile -> user space, then the paint transform) with Repeat
+    // tiling, bicubic unless the transform is a pure translation
     const Pixmap *pattern = nullptr;
+    std::shared_ptr<Pixmap> pattern_owner;
     float opacity = 1;
     bool is_opaque() const;
 };

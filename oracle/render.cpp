@@ -48,8 +48,37 @@ Path tree_path(const rgpu_tree_view &t, const rgpu_path &p) {
 }
 
 // path.rs:118-177 (convert_linear/radial/base_gradient) + tiny-skia shader constructors.
+void render_nodes(Ctx &c, uint32_t group, const Transform &ts, Pixmap &pm);
+
+// path.rs:179-205 render_pattern_pixmap + the Pattern shader it makes: the
+// tile is the pattern content at the fill's device scale, sampled back through
+// patternTransform * translate(rect) * scale(1 / scale).
+bool make_pattern(Ctx &c, const rgpu_paint &pp, float opacity, const Transform &ts, Shader &sh) {
+    const Transform pts = Transform::from(pp.transform);
+    float sx, sy;
+    ts.pre_concat(pts).get_scale(&sx, &sy);
+    auto to_u32 = [](float v) -> uint32_t {
+        v = std::round(v);
+        if (!(v > 0.0f)) return 0;
+        if (v >= 4294967296.0f) return 0xFFFFFFFFu;
+        return (uint32_t)v;
+    };
+    const uint32_t iw = to_u32(pp.x2 * sx), ih = to_u32(pp.y2 * sy);
+    if (!iw || !ih || (uint64_t)iw * ih > ((uint64_t)1 << 26)) return false;
+    if (pp.stop_offset >= c.t.group_count) return false;
+    auto tile = std::make_shared<Pixmap>(iw, ih);
+    render_nodes(c, pp.stop_offset, Transform::scale(sx, sy), *tile);
+    sh.kind = SHADER_PATTERN;
+    sh.pattern = tile.get();
+    sh.pattern_owner = tile;
+    sh.opacity = opacity;
+    sh.transform = pts.pre_concat(Transform::translate(pp.x1, pp.y1)).pre_concat(Transform::scale(1.0f / sx, 1.0f / sy));
+    return true;
+}
+
 bool make_shader(const rgpu_tree_view &t, int32_t paint_idx, float opacity, Shader &sh) {
     const rgpu_paint &pp = t.paints[paint_idx];
+    if (pp.kind == RGPU_PAINT_PATTERN) return false;  // make_pattern: needs the path transform
     uint8_t a8 = to_u8_norm(opacity);
     if (pp.kind == RGPU_PAINT_SOLID) {
         sh.kind = SHADER_SOLID;
@@ -104,7 +133,11 @@ void fill_path_node(Ctx &c, const rgpu_path &p, uint32_t blend, const Transform 
     Path path = tree_path(c.t, p);
     if (path.bounds.w() == 0.0f || path.bounds.h() == 0.0f) return;
     Paint paint;
-    if (!make_shader(c.t, p.fill_paint, p.fill_opacity, paint.shader)) return;
+    if (c.t.paints[p.fill_paint].kind == RGPU_PAINT_PATTERN) {
+        if (!make_pattern(c, c.t.paints[p.fill_paint], p.fill_opacity, ts, paint.shader)) return;
+    } else if (!make_shader(c.t, p.fill_paint, p.fill_opacity, paint.shader)) {
+        return;
+    }
     paint.anti_alias = p.anti_alias != 0;
     paint.blend = blend;
     fill_path(pm, path, paint, p.fill_rule, ts);
@@ -121,7 +154,11 @@ void stroke_path_node(Ctx &c, uint32_t pi, uint32_t blend, const Transform &ts, 
     const rgpu_path &p = c.t.paths[pi];
     if (p.stroke_paint < 0) return;
     Paint paint;
-    if (!make_shader(c.t, p.stroke_paint, p.stroke_opacity, paint.shader)) return;
+    if (c.t.paints[p.stroke_paint].kind == RGPU_PAINT_PATTERN) {
+        if (!make_pattern(c, c.t.paints[p.stroke_paint], p.stroke_opacity, ts, paint.shader)) return;
+    } else if (!make_shader(c.t, p.stroke_paint, p.stroke_opacity, paint.shader)) {
+        return;
+    }
     paint.anti_alias = p.anti_alias != 0;
     paint.blend = blend;
     float rs = rgpu::resolution_scale(ts.sx, ts.ky, ts.kx, ts.sy);
@@ -137,6 +174,8 @@ void stroke_path_node(Ctx &c, uint32_t pi, uint32_t blend, const Transform &ts, 
             auto scale = [op](ColorF &col) { col.a = std::min(std::max(col.a * std::min(std::max(op, 0.0f), 1.0f), 0.0f), 1.0f); };
             if (paint.shader.kind == SHADER_SOLID) scale(paint.shader.color);
             for (auto &st : paint.shader.stops) scale(st.color);
+            if (paint.shader.kind == SHADER_PATTERN)
+                paint.shader.opacity = std::min(std::max(paint.shader.opacity * std::min(std::max(op, 0.0f), 1.0f), 0.0f), 1.0f);
         }
         std::vector<rgpu::HairCall> calls;
         rgpu::hairline_calls(src, xts, p.line_cap, (int32_t)pm.width, (int32_t)pm.height, calls);

@@ -121,7 +121,7 @@ class SoftGrads(C.Structure):
 # enums (rgpu_tree.h)
 MOVE, LINE, QUAD, CUBIC, CLOSE = range(5)
 NONZERO, EVENODD = 0, 1
-PAINT_SOLID, PAINT_LINEAR, PAINT_RADIAL = 0, 1, 2
+PAINT_SOLID, PAINT_LINEAR, PAINT_RADIAL, PAINT_PATTERN = 0, 1, 2, 3
 SPREAD_PAD, SPREAD_REFLECT, SPREAD_REPEAT = 0, 1, 2
 CAP_BUTT, CAP_ROUND, CAP_SQUARE = 0, 1, 2
 JOIN_MITER, JOIN_MITER_CLIP, JOIN_ROUND, JOIN_BEVEL = 0, 1, 2, 3

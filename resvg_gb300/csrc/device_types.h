@@ -31,11 +31,20 @@ enum : uint32_t {
     GRAD_TWO_STOP = 1, GRAD_PAD_CLAMP = 2, GRAD_PREMUL = 4, GRAD_RADIAL_SIMPLE = 8, GRAD_RADIAL_CONICAL = 16
 };
 
+// A precomputed source image (a pattern shader evaluated per pixel, highp
+// premultiplied float4, bw x bh from layer pixel (bx, by)); stored in a
+// GradRec slot, the device address filled in when the scene's buffers exist.
+struct ImageRec {
+    uint64_t ptr;
+    int32_t bx, by, bw, bh;
+};
+static_assert(sizeof(ImageRec) <= sizeof(GradRec), "ImageRec fits a GradRec slot");
+
 struct PaintRec {
-    uint32_t kind;       // 0 solid, 1 gradient
+    uint32_t kind;       // 0 solid, 1 gradient, 2 image (ImageRec in the GradRec slot)
     uint32_t blend;      // rgpu_blend after tiny-skia's strength reduction
     uint32_t flags;      // PAINT_* below
-    uint32_t grad;       // index into GradRec when kind == 1
+    uint32_t grad;       // index into GradRec when kind != 0
     uint16_t rgba16[4];  // lowp uniform colour
     float colorf[4];     // highp uniform colour (premultiplied)
     uint8_t memset_rgba[4];

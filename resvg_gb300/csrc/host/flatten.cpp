@@ -271,14 +271,74 @@ struct Flattener {
         return r - l == 0.0f || b - tp == 0.0f;
     }
 
+    // path.rs:179-205 render_pattern_pixmap and the Pattern shader: the tile is
+    // the pattern content at the fill's device scale, rendered by its own
+    // stream; its shader (patternTransform * translate(rect) * scale(1 / s),
+    // then the fill transform) is evaluated per layer pixel by a job after
+    // that stream's pass, and the fill reads the result as an image paint.
+    bool pattern_paint(const rgpu_paint &pp, float opacity, uint32_t blend, const Xf &ts, const Target &tg,
+                       PaintRec &pr) {
+        const Xf pts = Xf::of(pp.transform);
+        const Xf t2 = pre_concat(ts, pts);
+        const float sx = std::sqrt(t2.sx * t2.sx + t2.kx * t2.kx), sy = std::sqrt(t2.ky * t2.ky + t2.sy * t2.sy);
+        auto to_u32 = [](float v) -> uint32_t {  // (v).round() as u32
+            v = std::round(v);
+            if (!(v > 0.0f)) return 0;
+            if (v >= 4294967296.0f) return 0xFFFFFFFFu;
+            return (uint32_t)v;
+        };
+        const uint32_t iw = to_u32(pp.x2 * sx), ih = to_u32(pp.y2 * sy);
+        if (!iw || !ih || (uint64_t)iw * ih > ((uint64_t)1 << 26) || pp.stop_offset >= t.group_count) return false;
+        if ((uint64_t)tg.w * tg.h > ((uint64_t)1 << 26)) { unsupported = true; return false; }
+        const Xf st = pre_concat(pre_concat(pts, Xf::translate(pp.x1, pp.y1)), Xf::row(1.0f / sx, 0, 0, 1.0f / sy, 0, 0));
+        Xf inv;
+        if (!invert(pre_concat(ts, st), &inv)) return false;
+        const uint32_t tile = (uint32_t)sb.surfaces.size();
+        sb.surfaces.push_back(SurfaceReq{(int32_t)iw, (int32_t)ih});
+        StreamBuild ps;
+        ps.out_w = (int32_t)iw; ps.out_h = (int32_t)ih;
+        ps.stride = iw * 4;
+        ps.surface = (int32_t)tile;
+        StreamBuild *sv = cur;
+        uint32_t sd = depth, sc = child_level;
+        cur = &ps;
+        depth = 0;
+        child_level = 0;
+        render_nodes(pp.stop_offset, Xf::row(sx, 0, 0, sy, 0, 0), Target{(int32_t)iw, (int32_t)ih, 0, 0});
+        ps.level = child_level;
+        cur = sv;
+        depth = sd;
+        child_level = std::max(sc, ps.level + 1);
+        sb.append_stream(ps);
+        const uint32_t shade = (uint32_t)sb.surfaces.size();
+        sb.surfaces.push_back(SurfaceReq{tg.w * 4, tg.h});
+        GradRec g;
+        std::memset(&g, 0, sizeof(g));
+        const uint32_t gi = (uint32_t)sb.grads.size();
+        sb.grads.push_back(g);
+        const bool nearest = inv.sx == 1.0f && inv.sy == 1.0f && inv.kx == 0.0f && inv.ky == 0.0f;
+        sb.patterns.push_back(PatternReq{gi, tile, (int32_t)iw, (int32_t)ih, shade, 0, 0, tg.w, tg.h, inv,
+                                         nearest ? 1 : 0, opacity, ps.level});
+        std::memset(&pr, 0, sizeof(pr));
+        pr.kind = 2;
+        pr.blend = blend;
+        pr.grad = gi;
+        if (blend == RGPU_BLEND_DESTINATION) pr.flags = PAINT_SKIP;
+        return true;
+    }
+
     // path.rs:26-75
     void fill_path(const rgpu_path &p, uint32_t blend, const Xf &ts, const Target &tg) {
         if (p.fill_paint < 0) return;
         if (path_bounds_empty(p)) return;
         Shader sh;
-        if (!make_shader(t, p.fill_paint, p.fill_opacity, sh)) return;
         PaintRec pr;
-        if (!paint_rec(sh, blend, p.anti_alias != 0, ts, pr)) return;
+        if (t.paints[p.fill_paint].kind == RGPU_PAINT_PATTERN) {
+            if (!pattern_paint(t.paints[p.fill_paint], p.fill_opacity, blend, ts, tg, pr)) return;
+        } else {
+            if (!make_shader(t, p.fill_paint, p.fill_opacity, sh)) return;
+            if (!paint_rec(sh, blend, p.anti_alias != 0, ts, pr)) return;
+        }
         emit_draw(CMD_FILL, tree_verb_base + p.verb_offset, p.verb_count, tree_pt_base + p.point_offset, p.point_count,
                   ts, tg, p.fill_rule, p.anti_alias != 0, add_paint(pr));
     }
@@ -286,6 +346,11 @@ struct Flattener {
     // tiny-skia stroke_path: a stroke at most one device pixel wide is drawn as
     // an anti-aliased hairline of the (dashed) path; for blend modes that
     // pre-scale coverage its paint is scaled by the stroke's coverage.
+    static bool pre_scale_blend(uint32_t blend) {
+        return blend == RGPU_BLEND_DESTINATION || blend == RGPU_BLEND_DESTINATION_OVER || blend == RGPU_BLEND_PLUS ||
+               blend == RGPU_BLEND_DESTINATION_OUT || blend == RGPU_BLEND_SOURCE_ATOP ||
+               blend == RGPU_BLEND_SOURCE_OVER || blend == RGPU_BLEND_XOR;
+    }
     bool hairline(uint32_t pi, Shader sh, uint32_t blend, const Xf &ts, const Target &tg, float rs) {
         const rgpu_path &p = t.paths[pi];
         float coverage = 1.0f;
@@ -304,6 +369,11 @@ struct Flattener {
         }
         PaintRec pr;
         if (!paint_rec(sh, blend, true, ts, pr)) return true;
+        emit_hairline(pi, pr, src, ts, tg);
+        return true;
+    }
+    void emit_hairline(uint32_t pi, PaintRec &pr, const PathData &src, const Xf &ts, const Target &tg) {
+        const rgpu_path &p = t.paths[pi];
         std::vector<HairCall> calls;
         hairline_calls(src, ts, p.line_cap, tg.w, tg.h, calls);
         HairRec hr;
@@ -325,24 +395,38 @@ struct Flattener {
         }
         sb.hair_spans.resize(keep);
         hr.span_cnt = (uint32_t)sb.hair_spans.size() - hr.span_off;
-        if (!hr.span_cnt) return true;
+        if (!hr.span_cnt) return;
         hr.paint = add_paint(pr);
         hr.ox = tg.ox; hr.oy = tg.oy;
         sb.hairs.push_back(hr);
         cur->cmds.push_back(Cmd{CMD_HAIR, (uint32_t)sb.hairs.size() - 1, 0, 0.0f});
-        return true;
     }
     void stroke_path(uint32_t pi, uint32_t blend, const Xf &ts, const Target &tg) {
         const rgpu_path &p = t.paths[pi];
         if (p.stroke_paint < 0) return;
         Shader sh;
-        if (!make_shader(t, p.stroke_paint, p.stroke_opacity, sh)) return;
         float rs = resolution_scale(ts.sx, ts.ky, ts.kx, ts.sy);
-        if (hairline(pi, sh, blend, ts, tg, rs)) return;
+        PaintRec pr;
+        if (t.paints[p.stroke_paint].kind == RGPU_PAINT_PATTERN) {
+            float coverage = 1.0f;
+            if (treat_as_hairline(p.anti_alias != 0, p.stroke_width, ts, &coverage)) {
+                PathData src;
+                if (!hairline_source_view(t, pi, rs, src)) return;
+                float op = p.stroke_opacity;
+                if (coverage != 1.0f && pre_scale_blend(blend))
+                    op = std::min(std::max(op * std::min(std::max(hairline_opacity(coverage), 0.0f), 1.0f), 0.0f), 1.0f);
+                if (!pattern_paint(t.paints[p.stroke_paint], op, blend, ts, tg, pr)) return;
+                emit_hairline(pi, pr, src, ts, tg);
+                return;
+            }
+            if (!pattern_paint(t.paints[p.stroke_paint], p.stroke_opacity, blend, ts, tg, pr)) return;
+        } else {
+            if (!make_shader(t, p.stroke_paint, p.stroke_opacity, sh)) return;
+            if (hairline(pi, sh, blend, ts, tg, rs)) return;
+            if (!paint_rec(sh, blend, p.anti_alias != 0, ts, pr)) return;
+        }
         auto outline = tree.stroke_outline(pi, rs);
         if (!outline || outline->verbs.empty()) return;
-        PaintRec pr;
-        if (!paint_rec(sh, blend, p.anti_alias != 0, ts, pr)) return;
         uint32_t vo = (uint32_t)sb.verbs.size(), po = (uint32_t)(sb.pts.size() / 2);
         sb.verbs.insert(sb.verbs.end(), outline->verbs.begin(), outline->verbs.end());
         sb.pts.insert(sb.pts.end(), outline->pts.begin(), outline->pts.end());
@@ -624,7 +708,7 @@ int SceneBuild::add_node(Tree &tree, uint32_t node_kind, uint32_t node_index, co
         f.render_path(node_index, ts, Target{w, h, 0, 0});
     }
     if (f.unsupported) {
-        error = "a filter region of more than 2^28 pixels";
+        error = "not supported on the device: a pattern paint, or a filter region of more than 2^28 pixels";
         return -1;
     }
     root.level = f.child_level;

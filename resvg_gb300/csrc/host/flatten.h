@@ -32,6 +32,22 @@ struct FilterJob {
     uint32_t image_first, image_count;  // its feImage renders in SceneBuild::fe_images
 };
 
+// A pattern fill: its tile is rendered by a stream into `tile` (tw x th); after
+// that stream's raster pass, the shader (inverse transform `inv`, nearest or
+// bicubic, opacity) is evaluated per layer pixel of (bx, by, bw, bh) into the
+// float4 surface `shade`, which the draw's ImageRec (GradRec slot `grad`)
+// points to.
+struct PatternReq {
+    uint32_t grad, tile;
+    int32_t tw, th;
+    uint32_t shade;
+    int32_t bx, by, bw, bh;
+    Xf inv;
+    int32_t nearest;
+    float opacity;
+    uint32_t level;
+};
+
 // A feImage primitive's element, rendered into its own surface before the job.
 struct FeImageReq {
     uint32_t prim;     // global primitive index
@@ -60,6 +76,7 @@ struct SceneBuild {
     std::vector<SurfaceReq> surfaces;
     std::vector<FilterJob> jobs;
     std::vector<FeImageReq> fe_images;
+    std::vector<PatternReq> patterns;
     std::vector<HairRec> hairs;       // anti-aliased hairline strokes
     std::vector<HairSpan> hair_spans;
     std::vector<uint32_t> fill_cmds;  // per stream: its fill / region command indices (plan_scene)

@@ -299,6 +299,10 @@ int upload_plan(Context &c, Buffers &b, Plan &p, cudaStream_t s) {
         if (st.surface >= 0) st.out_ptr = (uint64_t)(uintptr_t)b.surf[st.surface].p;
     for (auto &L : sb.layers)
         if (L.surf >= 0) L.buf = (uint64_t)(uintptr_t)b.surf[L.surf].p;
+    for (const auto &q : sb.patterns) {
+        ImageRec im{(uint64_t)(uintptr_t)b.surf[q.shade].p, q.bx, q.by, q.bw, q.bh};
+        std::memcpy(&sb.grads[q.grad], &im, sizeof(im));
+    }
     auto rup = [](size_t n) { return (n + 255) & ~(size_t)255; };
     size_t stage = rup(sb.verbs.size()) + rup(sb.pts.size() * 4) + rup(sb.draws.size() * sizeof(DrawRec)) +
                    rup(sb.paints.size() * sizeof(PaintRec)) + rup(sb.grads.size() * sizeof(GradRec)) +
@@ -406,6 +410,12 @@ int enqueue_plan(Context &c, Buffers &b, Plan &p, cudaStream_t s, RasterTimer *t
                              b.bin_counts.as<uint32_t>(), b.stack.as<uint32_t>(), b.span_ovf.as<int2>(), kSpanOvf,
                              b.run_ovf.as<int2>(), p.run_cap, b.hairs.as<HairRec>(), b.hair_spans.as<HairSpan>(), b.err.as<uint32_t>(), s));
         if (timed) CK(cudaEventRecord(tm->stop[tm->used++], s));
+        for (const auto &q : sb.patterns) {
+            if (q.level != lv) continue;
+            const float inv[6] = {q.inv.sx, q.inv.ky, q.inv.kx, q.inv.sy, q.inv.tx, q.inv.ty};
+            CK(filter_pattern_shade(b.surf[q.tile].as<uint32_t>(), q.tw, q.th, (float *)b.surf[q.shade].p, q.bx, q.by,
+                                    q.bw, q.bh, inv, q.nearest != 0, q.opacity, s));
+        }
         for (const auto &job : sb.jobs) {
             if (job.level != lv) continue;
             std::string ferr;

@@ -37,6 +37,11 @@ int32_t Tree::add_path(int32_t parent, const rgpu_path &p0, const uint8_t *v, ui
 
 int32_t Tree::add_paint(const rgpu_paint &p0, const rgpu_stop *s, uint32_t ns) {
     rgpu_paint p = p0;
+    if (p.kind == RGPU_PAINT_PATTERN) {  // stop_offset names the tile content group
+        p.stop_count = 0;
+        paints.push_back(p);
+        return (int32_t)paints.size() - 1;
+    }
     p.stop_offset = (uint32_t)stops.size();
     p.stop_count = ns;
     if (ns) stops.insert(stops.end(), s, s + ns);

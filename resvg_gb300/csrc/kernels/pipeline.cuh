@@ -329,6 +329,11 @@ __device__ __forceinline__ uint32_t shade_pixel_slow(const PaintRec &pr, const G
     float4 s;
     if (pr.kind == 0) {
         s = make_float4(pr.colorf[0], pr.colorf[1], pr.colorf[2], pr.colorf[3]);
+    } else if (pr.kind == 2) {
+        // an image paint: the precomputed shader over the whole layer target
+        // (bx = by = 0, bw = its width), which holds every covered pixel
+        const ImageRec &im = *reinterpret_cast<const ImageRec *>(grad);
+        s = __ldg(reinterpret_cast<const float4 *>(im.ptr) + (uint32_t)(ly * im.bw + lx));
     } else {
         float c[4];
         if (gradient_eval(*grad, lx, ly, c)) s = make_float4(c[0], c[1], c[2], c[3]);

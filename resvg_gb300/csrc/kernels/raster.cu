@@ -380,7 +380,7 @@ __device__ __forceinline__ void produce_window(VmShared &sh, const ItemInfo &itm
         if (lane < (int)(sizeof(PaintRec) / 4))
             ((uint32_t *)&wb.paint[k])[lane] = ((const uint32_t *)&paints[pi])[lane];
         if (lane == 0) wb.slot_geo[k] = make_int4(0, draws[di].ox, draws[di].oy, 0);
-        if (paints[pi].kind == 1) {
+        if (paints[pi].kind != 0) {
             const uint32_t *src = (const uint32_t *)&grads[paints[pi].grad];
             for (int w = lane; w < (int)(sizeof(GradRec) / 4); w += 32) ((uint32_t *)&wb.grad[k])[w] = src[w];
         }
@@ -553,7 +553,7 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
                     slot = kMaxSlots;  // the spare slot of buffer 0 (producers never write it)
                     if (tid == 0) sh.win[0].paint[slot] = paints[hr.paint];
                     const PaintRec &gp = paints[hr.paint];
-                    if (gp.kind == 1)
+                    if (gp.kind != 0)
                         for (int w = tid; w < (int)(sizeof(GradRec) / 4); w += kThreads)
                             ((uint32_t *)&sh.win[0].grad[slot])[w] = ((const uint32_t *)&grads[gp.grad])[w];
                     consumer_sync();

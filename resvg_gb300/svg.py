@@ -355,6 +355,34 @@ def parse_length(s, ref=0.0, font_size=12.0):
     raise Unsupported("unit " + u)
 
 
+def view_box_transform(vb, par, w, h):
+    """usvg ViewBox::to_transform (utils.rs view_box_to_transform): the viewBox
+    (x, y, w, h) fitted into a w x h viewport by preserveAspectRatio."""
+    F = np.float32
+    sx, sy = F(w) / F(vb[2]), F(h) / F(vb[3])
+    parts = par.split()
+    if parts and parts[0] == "defer":
+        parts = parts[1:]
+    align = parts[0] if parts else "xMidYMid"
+    slice_ = len(parts) > 1 and parts[1] == "slice"
+    if align == "none":
+        return (float(sx), 0.0, 0.0, float(sy), float(-F(vb[0]) * sx), float(-F(vb[1]) * sy))
+    sc = max(sx, sy) if slice_ else min(sx, sy)
+    x, y = -F(vb[0]) * sc, -F(vb[1]) * sc
+    nw, nh = F(vb[2]) * sc, F(vb[3]) * sc
+    ax = align[1:4] if len(align) >= 8 else "Mid"
+    ay = align[5:8] if len(align) >= 8 else "Mid"
+    if ax == "Mid":
+        x = x + (F(w) - nw) / F(2)
+    elif ax == "Max":
+        x = x + (F(w) - nw)
+    if ay == "Mid":
+        y = y + (F(h) - nh) / F(2)
+    elif ay == "Max":
+        y = y + (F(h) - nh)
+    return (float(sc), 0.0, 0.0, float(sc), float(x), float(y))
+
+
 def mat_mul(a, b):
     """a * b for (sx, ky, kx, sy, tx, ty) row-form transforms (f64)."""
     return (a[0] * b[0] + a[2] * b[1], a[1] * b[0] + a[3] * b[1],
@@ -726,7 +754,7 @@ INHERITED = {"fill", "fill-opacity", "fill-rule", "stroke", "stroke-width", "str
              "shape-rendering", "clip-rule", "color", "color-interpolation-filters", "paint-order", "font-size"}
 NON_INHERITED = {"opacity", "clip-path", "mask", "filter", "mix-blend-mode", "isolation", "display",
                  "stop-color", "stop-opacity", "flood-color", "flood-opacity", "transform"}
-UNSUPPORTED_ELEMS = {"text", "image", "pattern", "marker", "switch", "foreignObject", "tspan", "textPath", "symbol",
+UNSUPPORTED_ELEMS = {"text", "image", "marker", "switch", "foreignObject", "tspan", "textPath", "symbol",
                      "style", "animate", "set"}
 BLEND = {"normal": "source-over", "multiply": "multiply", "screen": "screen", "overlay": "overlay",
          "darken": "darken", "lighten": "lighten", "color-dodge": "color-dodge", "color-burn": "color-burn",
@@ -758,6 +786,38 @@ class Loader:
         # usvg's recursive-link fix for feImage: an element that a filter's
         # feImage links to drops its `filter` attribute when it, or an element
         # inside it, uses that same filter
+        self.pattern_active = set()
+        # usvg's recursive-pattern fix, in document order: inside pattern P, a
+        # fill or stroke linking to P reads as none; one linking to pattern Q
+        # stays, and the paints inside Q that link back to P read as none
+        self.no_paint = set()
+
+        def paint_link(n, which):
+            if (n, which) in self.no_paint:
+                return None
+            v = self.attrs(n).get(which)
+            m = re.match(r"\s*url\(\s*['\"]?#([^'\")]+)['\"]?\s*\)", v or "")
+            t = self.ids.get(m.group(1)) if m else None
+            return t if t is not None and _tag(t) == "pattern" else None
+        for pat in self.root.iter():
+            if not isinstance(pat.tag, str) or _tag(pat) != "pattern":
+                continue
+            for n in pat.iter():
+                if n is pat or not isinstance(n.tag, str):
+                    continue
+                for which in ("fill", "stroke"):
+                    link = paint_link(n, which)
+                    if link is None:
+                        continue
+                    if link is pat:
+                        self.no_paint.add((n, which))
+                        continue
+                    for n2 in link.iter():
+                        if not isinstance(n2.tag, str):
+                            continue
+                        for w2 in ("fill", "stroke"):
+                            if paint_link(n2, w2) is pat:
+                                self.no_paint.add((n2, w2))
         self.no_filter = set()
         for f in self.root.iter():
             if _tag(f) != "filter" or not f.get("id"):
@@ -915,7 +975,7 @@ class Builder(Loader):
     def node(self, e, parent, transform_extra=IDENT):
         tag = _tag(e)
         if tag in ("defs", "linearGradient", "radialGradient", "clipPath", "mask", "filter", "title", "desc",
-                   "metadata", "stop"):
+                   "metadata", "stop", "pattern"):
             return
         if not self.visible(e):
             return
@@ -1148,6 +1208,8 @@ class Builder(Loader):
         return b.finish()
 
     def paint(self, e, which, bbox, opacity_attr):
+        if (e, which) in self.no_paint:
+            return None
         v = self.get(e, which)
         if v is None:
             v = "black" if which == "fill" else "none"
@@ -1189,7 +1251,10 @@ class Builder(Loader):
             if ref is None:
                 return fallback_paint(fallback)
             if _tag(ref) == "pattern":
-                raise Unsupported("pattern")
+                g = self.pattern(ref, bbox, opacity)
+                if g == "drop":
+                    return None  # usvg process_paint: obb units on a zero-sized shape drop the paint
+                return g if g is not None else fallback_paint(fallback)
             if _tag(ref) not in ("linearGradient", "radialGradient"):
                 return None
             g = self.gradient(ref, bbox, opacity)
@@ -1201,6 +1266,84 @@ class Builder(Loader):
         if c is None:
             return None
         return self.solid(c), opacity * c[1]
+
+    def pattern(self, ref, bbox, opacity):
+        """A <pattern> as usvg converts it (parser/paint_server.rs:150-223) and
+        resolves it to user space (:1007-1061): attributes through the href
+        chain, content from the first pattern in it with children, the tile
+        rect in patternUnits, the content under a group carrying the viewBox
+        transform, or the bounding-box scale for objectBoundingBox content.
+        None when the pattern yields nothing (the fallback applies), "drop"
+        when bounding-box units meet a zero-sized shape."""
+        chain, g, seen = [], ref, set()
+        while g is not None and id(g) not in seen:
+            if _tag(g) != "pattern":
+                return None
+            seen.add(id(g))
+            chain.append(g)
+            g = self.href(g)
+        if id(ref) in self.pattern_active:
+            return None  # a pattern drawn inside its own content
+        content_src = next((c for c in chain if any(isinstance(k.tag, str) for k in c)), None)
+        if content_src is None:
+            return None
+
+        def attr(name):
+            for n in chain:
+                v = n.get(name)
+                if v is not None:
+                    return v
+            return None
+        units = (attr("patternUnits") or "objectBoundingBox").strip()
+        cunits = (attr("patternContentUnits") or "userSpaceOnUse").strip()
+        obb = units != "userSpaceOnUse"
+        cobb = cunits == "objectBoundingBox"
+        pts = parse_transform(attr("patternTransform") or "")
+        if abs(pts[0] * pts[3] - pts[1] * pts[2]) <= 0.0 or not all(math.isfinite(v) for v in pts):
+            pts = (1.0, 0.0, 0.0, 1.0, 0.0, 0.0)  # a non-invertible patternTransform reads as none
+
+        def num(name, ref_len):
+            v = attr(name)
+            if v is None:
+                return 0.0
+            v = v.strip()
+            if obb:
+                return float(v[:-1]) / 100 if v.endswith("%") else float(v)
+            return parse_length(v, ref_len, self.font_size(ref))
+        x, y = num("x", self.vbw), num("y", self.vbh)
+        w, h = num("width", self.vbw), num("height", self.vbh)
+        if not (w > 0 and h > 0):
+            return None
+        vb = numbers(attr("viewBox")) if attr("viewBox") is not None else None
+        if vb is not None and (len(vb) != 4 or not (vb[2] > 0 and vb[3] > 0)):
+            vb = None
+        if obb or cobb:
+            if bbox is None or not (bbox[2] > bbox[0] and bbox[3] > bbox[1]):
+                return "drop"
+        F32 = np.float32
+        if obb:
+            bw, bh = F32(bbox[2]) - F32(bbox[0]), F32(bbox[3]) - F32(bbox[1])
+            x, y = float(F32(x) * bw + F32(bbox[0])), float(F32(y) * bh + F32(bbox[1]))
+            w, h = float(F32(w) * bw), float(F32(h) * bh)
+        wrap = None
+        if vb is not None:
+            wrap = view_box_transform(vb, attr("preserveAspectRatio") or "", w, h)
+        elif cobb:
+            wrap = (float(F32(bbox[2]) - F32(bbox[0])), 0.0, 0.0, float(F32(bbox[3]) - F32(bbox[1])), 0.0, 0.0)
+        root = self.tree.add_group(-1, _group())
+        content = self.tree.add_group(root, _group(transform=_tf(wrap))) if wrap is not None else root
+        self.pattern_active.add(id(ref))
+        try:
+            for c in content_src:
+                self.node(c, content)
+        finally:
+            self.pattern_active.discard(id(ref))
+        p = A.Paint()
+        p.kind = A.PAINT_PATTERN
+        p.x1, p.y1, p.x2, p.y2 = x, y, w, h
+        p.transform = _tf(pts)
+        p.stop_offset = root
+        return self.tree.add_paint(p, []), opacity
 
     def solid(self, c):
         p = A.Paint()
