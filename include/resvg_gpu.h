@@ -62,6 +62,9 @@ int32_t rgpu_tree_add_clip(resvg_render_tree *tree, const rgpu_clip *clip);
 int32_t rgpu_tree_add_mask(resvg_render_tree *tree, const rgpu_mask *mask);
 int32_t rgpu_tree_add_filter(resvg_render_tree *tree, const rgpu_filter *filter, const rgpu_primitive *prims,
                              uint32_t prim_count, const int32_t *merge_inputs, uint32_t merge_count);
+/* Adds a decoded raster image (premultiplied RGBA8, width * height * 4 bytes,
+ * copied); returns its index for an RGPU_PAINT_IMAGE paint, or -1. */
+int32_t rgpu_tree_add_image(resvg_render_tree *tree, uint32_t width, uint32_t height, const uint8_t *rgba);
 /* Attaches filters (indices from rgpu_tree_add_filter) to a group. */
 int rgpu_tree_set_group_filters(resvg_render_tree *tree, int32_t group, const uint32_t *filters, uint32_t count);
 /* Computes path and layer bounding boxes; call once after building. */

@@ -47,7 +47,17 @@ enum rgpu_blend {
     RGPU_BLEND_LUMINOSITY
 };
 
-enum rgpu_paint_kind { RGPU_PAINT_SOLID = 0, RGPU_PAINT_LINEAR = 1, RGPU_PAINT_RADIAL = 2, RGPU_PAINT_PATTERN = 3 };
+enum rgpu_paint_kind { RGPU_PAINT_SOLID = 0, RGPU_PAINT_LINEAR = 1, RGPU_PAINT_RADIAL = 2, RGPU_PAINT_PATTERN = 3,
+                       RGPU_PAINT_IMAGE = 4 };
+/* A raster image (resvg image.rs render_raster): stop_offset = an image of the
+ * tree (rgpu_tree_add_image), spread = rgpu_image_quality; the pattern is
+ * padded (not repeated) and sampled in the path's user space, where the image
+ * spans (0, 0, width, height).  The path is that rect. */
+enum rgpu_image_quality { RGPU_IMAGE_NEAREST = 0, RGPU_IMAGE_BILINEAR = 1, RGPU_IMAGE_BICUBIC = 2 };
+typedef struct rgpu_image {
+    uint32_t width, height;
+    uint64_t pixel_offset;    /* into image_pixels: premultiplied RGBA8, row-major */
+} rgpu_image;
 /* A pattern (usvg::Pattern, resolved to user space): x1, y1, x2, y2 = the tile
  * rect x, y, width, height; transform = patternTransform; stop_offset = a
  * detached group whose children are the tile content (viewBox and content
@@ -216,6 +226,8 @@ typedef struct rgpu_tree_view {
     const rgpu_filter *filters; uint32_t filter_count;
     const rgpu_primitive *prims; uint32_t prim_count;
     const int32_t *merge_inputs; uint32_t merge_input_count;
+    const rgpu_image *images; uint32_t image_count;
+    const uint8_t *image_pixels; uint64_t image_pixel_bytes;
 } rgpu_tree_view;
 
 #ifdef __cplusplus

@@ -1541,10 +1541,12 @@ static inline float ulp_below(float v) {
     std::memcpy(&v, &b, 4);
     return v;
 }
-static void pattern_gather(const Pixmap &pm, float x, float y, float c[4]) {
+static void pattern_gather(const Pixmap &pm, bool repeat, float x, float y, float c[4]) {
     const float w = (float)pm.width, h = (float)pm.height;
-    x = x - std::floor(x * (1.0f / w)) * w;
-    y = y - std::floor(y * (1.0f / h)) * h;
+    if (repeat) {
+        x = x - std::floor(x * (1.0f / w)) * w;
+        y = y - std::floor(y * (1.0f / h)) * h;
+    }
     x = std::min(std::max(x, 0.0f), ulp_below(w));
     y = std::min(std::max(y, 0.0f), ulp_below(h));
     const uint8_t *p = pm.px((uint32_t)x, (uint32_t)y);
@@ -1554,12 +1556,31 @@ static inline float bicubic_near(float t) {
     return t * (t * ((-21.0f / 18.0f) * t + 27.0f / 18.0f) + 9.0f / 18.0f) + 1.0f / 18.0f;
 }
 static inline float bicubic_far(float t) { return (t * t) * ((7.0f / 18.0f) * t + (-6.0f / 18.0f)); }
-static void pattern_eval(const Shader &sh, const Transform &inv, bool nearest, int32_t x, int32_t y, float out[4]) {
+static void pattern_eval(const Shader &sh, const Transform &inv, int quality, int32_t x, int32_t y, float out[4]) {
+    const bool rep = sh.spread == RGPU_SPREAD_REPEAT;
     const float px = (float)x + 0.5f, py = (float)y + 0.5f;
     const float u = px * inv.sx + (py * inv.kx + inv.tx);
     const float v = px * inv.ky + (py * inv.sy + inv.ty);
-    if (nearest) {
-        pattern_gather(*sh.pattern, u, v, out);
+    if (quality == 0) {
+        pattern_gather(*sh.pattern, rep, u, v, out);
+    } else if (quality == 1) {
+        // bilinear: 2x2 taps at -0.5 / +0.5, weights 1 - f and f
+        const float fx = (u + 0.5f) - std::floor(u + 0.5f), fy = (v + 0.5f) - std::floor(v + 0.5f);
+        const float wx[2] = {1.0f - fx, fx}, wy[2] = {1.0f - fy, fy};
+        float acc[4] = {0, 0, 0, 0};
+        float sy = v - 0.5f;
+        for (int j = 0; j < 2; j++) {
+            float sx = u - 0.5f;
+            for (int i = 0; i < 2; i++) {
+                float c[4];
+                pattern_gather(*sh.pattern, rep, sx, sy, c);
+                const float wgt = wx[i] * wy[j];
+                for (int k = 0; k < 4; k++) acc[k] = wgt * c[k] + acc[k];
+                sx += 1.0f;
+            }
+            sy += 1.0f;
+        }
+        for (int k = 0; k < 4; k++) out[k] = acc[k];
     } else {
         const float fx = (u + 0.5f) - std::floor(u + 0.5f), fy = (v + 0.5f) - std::floor(v + 0.5f);
         const float wx[4] = {bicubic_far(1.0f - fx), bicubic_near(1.0f - fx), bicubic_near(fx), bicubic_far(fx)};
@@ -1570,7 +1591,7 @@ static void pattern_eval(const Shader &sh, const Transform &inv, bool nearest, i
             float sx = u - 1.5f;
             for (int i = 0; i < 4; i++) {
                 float c[4];
-                pattern_gather(*sh.pattern, sx, sy, c);
+                pattern_gather(*sh.pattern, rep, sx, sy, c);
                 const float wgt = wx[i] * wy[j];
                 for (int k = 0; k < 4; k++) acc[k] = wgt * c[k] + acc[k];
                 sx += 1.0f;
@@ -1596,7 +1617,7 @@ struct PipelineBlitter {
     const Shader *shader = nullptr;
     GradientCtx grad;
     Transform pinv;
-    bool pnearest = false;
+    int pquality = 2;
     bool skip = false;
 
     bool setup(Pixmap &p, const Paint &paint) {
@@ -1620,7 +1641,9 @@ struct PipelineBlitter {
             if (!gradient_setup(paint.shader, grad)) { skip = true; return false; }
         } else if (paint.shader.kind == SHADER_PATTERN) {
             if (!paint.shader.pattern || !paint.shader.transform.invert(&pinv)) { skip = true; return false; }
-            pnearest = pinv.sx == 1.0f && pinv.sy == 1.0f && pinv.kx == 0.0f && pinv.ky == 0.0f;
+            // a translation-only transform samples nearest (tiny-skia's quality downgrade)
+            const bool translate = pinv.sx == 1.0f && pinv.sy == 1.0f && pinv.kx == 0.0f && pinv.ky == 0.0f;
+            pquality = translate ? 0 : paint.shader.quality;
         }
         if (blend == RGPU_BLEND_CLEAR && !paint.anti_alias) {
             blend = RGPU_BLEND_SOURCE;
@@ -1688,7 +1711,7 @@ struct PipelineBlitter {
         if (shader->kind == SHADER_SOLID) {
             for (int i = 0; i < 4; i++) s[i] = colorf[i];
         } else if (shader->kind == SHADER_PATTERN) {
-            pattern_eval(*shader, pinv, pnearest, x, y, s);
+            pattern_eval(*shader, pinv, pquality, x, y, s);
         } else {
             ColorF c;
             if (!gradient_eval(grad, shader->spread, x, y, &c)) c = ColorF{0, 0, 0, 0};

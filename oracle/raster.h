@@ -110,6 +110,7 @@ struct Shader {
     // tiling, bicubic unless the transform is a pure translation
     const Pixmap *pattern = nullptr;
     std::shared_ptr<Pixmap> pattern_owner;
+    int quality = 2;              // 0 nearest, 1 bilinear, 2 bicubic; `spread` repeat or pad
     float opacity = 1;
     bool is_opaque() const;
 };

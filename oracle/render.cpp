@@ -71,6 +71,8 @@ bool make_pattern(Ctx &c, const rgpu_paint &pp, float opacity, const Transform &
     sh.kind = SHADER_PATTERN;
     sh.pattern = tile.get();
     sh.pattern_owner = tile;
+    sh.spread = RGPU_SPREAD_REPEAT;
+    sh.quality = 2;
     sh.opacity = opacity;
     sh.transform = pts.pre_concat(Transform::translate(pp.x1, pp.y1)).pre_concat(Transform::scale(1.0f / sx, 1.0f / sy));
     return true;
@@ -79,6 +81,21 @@ bool make_pattern(Ctx &c, const rgpu_paint &pp, float opacity, const Transform &
 bool make_shader(const rgpu_tree_view &t, int32_t paint_idx, float opacity, Shader &sh) {
     const rgpu_paint &pp = t.paints[paint_idx];
     if (pp.kind == RGPU_PAINT_PATTERN) return false;  // make_pattern: needs the path transform
+    if (pp.kind == RGPU_PAINT_IMAGE) {
+        // image.rs render_raster: Pattern(raster, Pad, quality, opacity 1, identity)
+        if (pp.stop_offset >= t.image_count) return false;
+        const rgpu_image &im = t.images[pp.stop_offset];
+        auto tile = std::make_shared<Pixmap>(im.width, im.height);
+        std::memcpy(tile->data.data(), t.image_pixels + im.pixel_offset, (size_t)im.width * im.height * 4);
+        sh.kind = SHADER_PATTERN;
+        sh.pattern = tile.get();
+        sh.pattern_owner = tile;
+        sh.spread = RGPU_SPREAD_PAD;
+        sh.quality = (int)std::min<uint32_t>(pp.spread, 2u);
+        sh.opacity = 1.0f;
+        sh.transform = Transform();
+        return true;
+    }
     uint8_t a8 = to_u8_norm(opacity);
     if (pp.kind == RGPU_PAINT_SOLID) {
         sh.kind = SHADER_SOLID;

@@ -134,6 +134,12 @@ class Tree:
         m = (C.c_int32 * max(1, len(merge_inputs)))(*merge_inputs)
         return lib().rgpu_tree_add_filter(self._h, C.byref(filt), arr, len(prims), m, len(merge_inputs))
 
+    def add_image(self, rgba) -> int:
+        """A decoded raster image: a (h, w, 4) uint8 array, premultiplied."""
+        a = np.ascontiguousarray(rgba, dtype=np.uint8)
+        assert a.ndim == 3 and a.shape[2] == 4
+        return lib().rgpu_tree_add_image(self._h, a.shape[1], a.shape[0], a.ctypes.data)
+
     def set_group_filters(self, group: int, filters) -> None:
         arr = (C.c_uint32 * max(1, len(filters)))(*filters)
         check(lib().rgpu_tree_set_group_filters(self._h, group, arr, len(filters)), "set_group_filters")

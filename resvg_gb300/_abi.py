@@ -87,7 +87,9 @@ class TreeView(C.Structure):
                 ("filter_refs", C.POINTER(u32)), ("filter_ref_count", u32),
                 ("filters", C.POINTER(Filter)), ("filter_count", u32),
                 ("prims", C.POINTER(Primitive)), ("prim_count", u32),
-                ("merge_inputs", C.POINTER(i32)), ("merge_input_count", u32)]
+                ("merge_inputs", C.POINTER(i32)), ("merge_input_count", u32),
+                ("images", C.c_void_p), ("image_count", u32),
+                ("image_pixels", C.c_void_p), ("image_pixel_bytes", C.c_uint64)]
 
 
 class ResvgTransform(C.Structure):
@@ -121,7 +123,8 @@ class SoftGrads(C.Structure):
 # enums (rgpu_tree.h)
 MOVE, LINE, QUAD, CUBIC, CLOSE = range(5)
 NONZERO, EVENODD = 0, 1
-PAINT_SOLID, PAINT_LINEAR, PAINT_RADIAL, PAINT_PATTERN = 0, 1, 2, 3
+PAINT_SOLID, PAINT_LINEAR, PAINT_RADIAL, PAINT_PATTERN, PAINT_IMAGE = 0, 1, 2, 3, 4
+IMAGE_NEAREST, IMAGE_BILINEAR, IMAGE_BICUBIC = 0, 1, 2
 SPREAD_PAD, SPREAD_REFLECT, SPREAD_REPEAT = 0, 1, 2
 CAP_BUTT, CAP_ROUND, CAP_SQUARE = 0, 1, 2
 JOIN_MITER, JOIN_MITER_CLIP, JOIN_ROUND, JOIN_BEVEL = 0, 1, 2, 3
@@ -162,6 +165,8 @@ def declare(lib: C.CDLL) -> C.CDLL:
     lib.rgpu_tree_add_clip.argtypes = [P, C.POINTER(Clip)]
     lib.rgpu_tree_add_mask.restype = i32
     lib.rgpu_tree_add_mask.argtypes = [P, C.POINTER(Mask)]
+    lib.rgpu_tree_add_image.restype = i32
+    lib.rgpu_tree_add_image.argtypes = [P, u32, u32, C.c_void_p]
     lib.rgpu_tree_add_filter.restype = i32
     lib.rgpu_tree_add_filter.argtypes = [P, C.POINTER(Filter), C.POINTER(Primitive), u32, C.POINTER(i32), u32]
     lib.rgpu_tree_set_group_filters.restype = C.c_int

@@ -55,6 +55,11 @@ int32_t rgpu_tree_add_filter(resvg_render_tree *t, const rgpu_filter *f, const r
     return t->add_filter(*f, prims, n, merge, nm);
 }
 
+int32_t rgpu_tree_add_image(resvg_render_tree *t, uint32_t w, uint32_t h, const uint8_t *rgba) {
+    if (!t) return -1;
+    return t->add_image(w, h, rgba);
+}
+
 int rgpu_tree_set_group_filters(resvg_render_tree *t, int32_t group, const uint32_t *filters, uint32_t count) {
     if (!t || group < 0 || group >= (int32_t)t->groups.size()) return RGPU_ERR_INVALID_ARG;
     t->groups[group].filter_offset = (uint32_t)t->filter_refs.size();
@@ -88,6 +93,7 @@ resvg_render_tree *rgpu_tree_generate(int config, uint64_t seed, uint64_t index,
     t->clips = std::move(g->clips); t->masks = std::move(g->masks);
     t->filter_refs = std::move(g->filter_refs); t->filters = std::move(g->filters);
     t->prims = std::move(g->prims); t->merge_inputs = std::move(g->merge_inputs);
+    t->images = std::move(g->images); t->image_pixels = std::move(g->image_pixels);
     t->finalized = g->finalized;
     delete g;
     t->get_view();

@@ -318,7 +318,37 @@ struct Flattener {
         sb.grads.push_back(g);
         const bool nearest = inv.sx == 1.0f && inv.sy == 1.0f && inv.kx == 0.0f && inv.ky == 0.0f;
         sb.patterns.push_back(PatternReq{gi, tile, (int32_t)iw, (int32_t)ih, shade, 0, 0, tg.w, tg.h, inv,
-                                         nearest ? 1 : 0, opacity, ps.level});
+                                         nearest ? 0 : 2, 1, opacity, ps.level});
+        std::memset(&pr, 0, sizeof(pr));
+        pr.kind = 2;
+        pr.blend = blend;
+        pr.grad = gi;
+        if (blend == RGPU_BLEND_DESTINATION) pr.flags = PAINT_SKIP;
+        return true;
+    }
+
+    // image.rs:167-201 render_raster: the decoded image as a padded pattern in
+    // the path's user space, evaluated per layer pixel before the first raster
+    // pass (the stream drawing it is pushed to level 1 or later).
+    bool image_paint(const rgpu_paint &pp, uint32_t blend, const Xf &ts, const Target &tg, PaintRec &pr) {
+        if (pp.stop_offset >= t.image_count) return false;
+        if ((uint64_t)tg.w * tg.h > ((uint64_t)1 << 26)) { unsupported = true; return false; }
+        const rgpu_image &im = t.images[pp.stop_offset];
+        Xf inv;
+        if (!invert(ts, &inv)) return false;
+        const uint32_t tile = (uint32_t)sb.surfaces.size();
+        sb.surfaces.push_back(SurfaceReq{(int32_t)im.width, (int32_t)im.height, t.image_pixels + im.pixel_offset});
+        const uint32_t shade = (uint32_t)sb.surfaces.size();
+        sb.surfaces.push_back(SurfaceReq{tg.w * 4, tg.h});
+        GradRec g;
+        std::memset(&g, 0, sizeof(g));
+        const uint32_t gi = (uint32_t)sb.grads.size();
+        sb.grads.push_back(g);
+        const bool translate = inv.sx == 1.0f && inv.sy == 1.0f && inv.kx == 0.0f && inv.ky == 0.0f;
+        sb.patterns.push_back(PatternReq{gi, tile, (int32_t)im.width, (int32_t)im.height, shade, 0, 0, tg.w, tg.h,
+                                         inv, translate ? 0 : (int32_t)std::min<uint32_t>(pp.spread, 2u), 0, 1.0f,
+                                         0});
+        child_level = std::max<uint32_t>(child_level, 1);
         std::memset(&pr, 0, sizeof(pr));
         pr.kind = 2;
         pr.blend = blend;
@@ -335,6 +365,8 @@ struct Flattener {
         PaintRec pr;
         if (t.paints[p.fill_paint].kind == RGPU_PAINT_PATTERN) {
             if (!pattern_paint(t.paints[p.fill_paint], p.fill_opacity, blend, ts, tg, pr)) return;
+        } else if (t.paints[p.fill_paint].kind == RGPU_PAINT_IMAGE) {
+            if (!image_paint(t.paints[p.fill_paint], blend, ts, tg, pr)) return;
         } else {
             if (!make_shader(t, p.fill_paint, p.fill_opacity, sh)) return;
             if (!paint_rec(sh, blend, p.anti_alias != 0, ts, pr)) return;
@@ -407,6 +439,7 @@ struct Flattener {
         Shader sh;
         float rs = resolution_scale(ts.sx, ts.ky, ts.kx, ts.sy);
         PaintRec pr;
+        if (t.paints[p.stroke_paint].kind == RGPU_PAINT_IMAGE) return;  // images are fills only
         if (t.paints[p.stroke_paint].kind == RGPU_PAINT_PATTERN) {
             float coverage = 1.0f;
             if (treat_as_hairline(p.anti_alias != 0, p.stroke_width, ts, &coverage)) {

@@ -19,6 +19,7 @@ namespace rgpu {
 
 struct SurfaceReq {
     int32_t w, h;
+    const uint8_t *init = nullptr;  // host pixels copied in at upload (raster images)
 };
 
 struct FilterJob {
@@ -32,8 +33,8 @@ struct FilterJob {
     uint32_t image_first, image_count;  // its feImage renders in SceneBuild::fe_images
 };
 
-// A pattern fill: its tile is rendered by a stream into `tile` (tw x th); after
-// that stream's raster pass, the shader (inverse transform `inv`, nearest or
+// A pattern or raster-image fill: its tile is rendered by a stream into `tile`
+// (tw x th), or holds the image's pixels; after that stream's raster pass, the shader (inverse transform `inv`, nearest or
 // bicubic, opacity) is evaluated per layer pixel of (bx, by, bw, bh) into the
 // float4 surface `shade`, which the draw's ImageRec (GradRec slot `grad`)
 // points to.
@@ -43,7 +44,8 @@ struct PatternReq {
     uint32_t shade;
     int32_t bx, by, bw, bh;
     Xf inv;
-    int32_t nearest;
+    int32_t quality;   // 0 nearest, 1 bilinear, 2 bicubic
+    int32_t repeat;    // 1 repeat (patterns), 0 pad (raster images)
     float opacity;
     uint32_t level;
 };

@@ -293,8 +293,12 @@ int plan_scene(Context &c, Plan &p) {
 int upload_plan(Context &c, Buffers &b, Plan &p, cudaStream_t s) {
     SceneBuild &sb = p.sb;
     if (b.surf.size() < sb.surfaces.size()) b.surf.resize(sb.surfaces.size());
-    for (size_t i = 0; i < sb.surfaces.size(); i++)
+    for (size_t i = 0; i < sb.surfaces.size(); i++) {
         CK(b.surf[i].ensure((size_t)sb.surfaces[i].w * sb.surfaces[i].h * 4));
+        if (sb.surfaces[i].init)
+            CK(cudaMemcpyAsync(b.surf[i].p, sb.surfaces[i].init, (size_t)sb.surfaces[i].w * sb.surfaces[i].h * 4,
+                               cudaMemcpyHostToDevice, s));
+    }
     for (auto &st : sb.streams)
         if (st.surface >= 0) st.out_ptr = (uint64_t)(uintptr_t)b.surf[st.surface].p;
     for (auto &L : sb.layers)
@@ -414,7 +418,7 @@ int enqueue_plan(Context &c, Buffers &b, Plan &p, cudaStream_t s, RasterTimer *t
             if (q.level != lv) continue;
             const float inv[6] = {q.inv.sx, q.inv.ky, q.inv.kx, q.inv.sy, q.inv.tx, q.inv.ty};
             CK(filter_pattern_shade(b.surf[q.tile].as<uint32_t>(), q.tw, q.th, (float *)b.surf[q.shade].p, q.bx, q.by,
-                                    q.bw, q.bh, inv, q.nearest != 0, q.opacity, s));
+                                    q.bw, q.bh, inv, q.quality, q.repeat != 0, q.opacity, s));
         }
         for (const auto &job : sb.jobs) {
             if (job.level != lv) continue;

@@ -37,7 +37,7 @@ int32_t Tree::add_path(int32_t parent, const rgpu_path &p0, const uint8_t *v, ui
 
 int32_t Tree::add_paint(const rgpu_paint &p0, const rgpu_stop *s, uint32_t ns) {
     rgpu_paint p = p0;
-    if (p.kind == RGPU_PAINT_PATTERN) {  // stop_offset names the tile content group
+    if (p.kind == RGPU_PAINT_PATTERN || p.kind == RGPU_PAINT_IMAGE) {  // stop_offset names the group / image
         p.stop_count = 0;
         paints.push_back(p);
         return (int32_t)paints.size() - 1;
@@ -47,6 +47,14 @@ int32_t Tree::add_paint(const rgpu_paint &p0, const rgpu_stop *s, uint32_t ns) {
     if (ns) stops.insert(stops.end(), s, s + ns);
     paints.push_back(p);
     return (int32_t)paints.size() - 1;
+}
+
+int32_t Tree::add_image(uint32_t w, uint32_t h, const uint8_t *rgba) {
+    if (!w || !h || !rgba || (uint64_t)w * h > ((uint64_t)1 << 28)) return -1;
+    rgpu_image im{w, h, (uint64_t)image_pixels.size()};
+    image_pixels.insert(image_pixels.end(), rgba, rgba + (size_t)w * h * 4);
+    images.push_back(im);
+    return (int32_t)images.size() - 1;
 }
 
 int32_t Tree::add_filter(const rgpu_filter &f0, const rgpu_primitive *pr, uint32_t n, const int32_t *merge,
@@ -224,6 +232,8 @@ const rgpu_tree_view *Tree::get_view() {
     view.filters = filters.data(); view.filter_count = (uint32_t)filters.size();
     view.prims = prims.data(); view.prim_count = (uint32_t)prims.size();
     view.merge_inputs = merge_inputs.data(); view.merge_input_count = (uint32_t)merge_inputs.size();
+    view.images = images.data(); view.image_count = (uint32_t)images.size();
+    view.image_pixels = image_pixels.data(); view.image_pixel_bytes = (uint64_t)image_pixels.size();
     return &view;
 }
 

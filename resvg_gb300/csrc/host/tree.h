@@ -33,6 +33,8 @@ struct Tree {
     std::vector<rgpu_filter> filters;
     std::vector<rgpu_primitive> prims;
     std::vector<int32_t> merge_inputs;
+    std::vector<rgpu_image> images;
+    std::vector<uint8_t> image_pixels;
     rgpu_tree_view view{};
     bool finalized = false;
 
@@ -44,6 +46,7 @@ struct Tree {
     int32_t add_path(int32_t parent, const rgpu_path &p, const uint8_t *v, uint32_t nv, const float *pts,
                      uint32_t npts, const float *dash, uint32_t nd);
     int32_t add_paint(const rgpu_paint &p, const rgpu_stop *s, uint32_t ns);
+    int32_t add_image(uint32_t w, uint32_t h, const uint8_t *rgba);
     int32_t add_filter(const rgpu_filter &f, const rgpu_primitive *pr, uint32_t n, const int32_t *merge, uint32_t nm);
     bool finalize();
     const rgpu_tree_view *get_view();

@@ -1345,18 +1345,21 @@ cudaError_t filter_displacement_map(const uint32_t *src, const uint32_t *map, ui
 
 namespace rgpu {
 namespace {
-// ---- the Pattern shader (tiny-skia shaders/pattern.rs, highp stages): the
+// ---- the Pattern shader (tiny-skia shaders/pattern.rs, highp stages; raster
+// images use it padded, image.rs:167-201): the
 // same f32 operations in the same order as the CPU restatement, no contraction.
 struct PatternParams {
     float sx, ky, kx, sy, tx, ty;
-    int tw, th, bx, by, bw, bh, nearest;
+    int tw, th, bx, by, bw, bh, quality, repeat;
     float opacity;
 };
 __device__ __forceinline__ float ulp_below_f(float v) { return __int_as_float(__float_as_int(v) - 1); }
 __device__ __forceinline__ float4 pattern_gather(const uint32_t *tile, const PatternParams &pp, float x, float y) {
     const float w = (float)pp.tw, h = (float)pp.th;
-    x = __fsub_rn(x, __fmul_rn(floorf(__fmul_rn(x, __fdiv_rn(1.0f, w))), w));
-    y = __fsub_rn(y, __fmul_rn(floorf(__fmul_rn(y, __fdiv_rn(1.0f, h))), h));
+    if (pp.repeat) {
+        x = __fsub_rn(x, __fmul_rn(floorf(__fmul_rn(x, __fdiv_rn(1.0f, w))), w));
+        y = __fsub_rn(y, __fmul_rn(floorf(__fmul_rn(y, __fdiv_rn(1.0f, h))), h));
+    }
     x = fminf(fmaxf(x, 0.0f), ulp_below_f(w));
     y = fminf(fmaxf(y, 0.0f), ulp_below_f(h));
     const uint32_t p = __ldg(tile + (size_t)(uint32_t)y * (uint32_t)pp.tw + (uint32_t)x);
@@ -1380,8 +1383,30 @@ __global__ void k_pattern_shade(const uint32_t *tile, float4 *out, PatternParams
         const float u = __fadd_rn(__fmul_rn(px, pp.sx), __fadd_rn(__fmul_rn(py, pp.kx), pp.tx));
         const float v = __fadd_rn(__fmul_rn(px, pp.ky), __fadd_rn(__fmul_rn(py, pp.sy), pp.ty));
         float4 o;
-        if (pp.nearest) {
+        if (pp.quality == 0) {
             o = pattern_gather(tile, pp, u, v);
+        } else if (pp.quality == 1) {
+            const float fx = __fsub_rn(__fadd_rn(u, 0.5f), floorf(__fadd_rn(u, 0.5f)));
+            const float fy = __fsub_rn(__fadd_rn(v, 0.5f), floorf(__fadd_rn(v, 0.5f)));
+            const float wx[2] = {__fsub_rn(1.0f, fx), fx}, wy[2] = {__fsub_rn(1.0f, fy), fy};
+            float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+            float sy = __fsub_rn(v, 0.5f);
+#pragma unroll
+            for (int j = 0; j < 2; j++) {
+                float sx = __fsub_rn(u, 0.5f);
+#pragma unroll
+                for (int k = 0; k < 2; k++) {
+                    const float4 c = pattern_gather(tile, pp, sx, sy);
+                    const float wgt = __fmul_rn(wx[k], wy[j]);
+                    acc.x = __fadd_rn(__fmul_rn(wgt, c.x), acc.x);
+                    acc.y = __fadd_rn(__fmul_rn(wgt, c.y), acc.y);
+                    acc.z = __fadd_rn(__fmul_rn(wgt, c.z), acc.z);
+                    acc.w = __fadd_rn(__fmul_rn(wgt, c.w), acc.w);
+                    sx = __fadd_rn(sx, 1.0f);
+                }
+                sy = __fadd_rn(sy, 1.0f);
+            }
+            o = acc;
         } else {
             const float fx = __fsub_rn(__fadd_rn(u, 0.5f), floorf(__fadd_rn(u, 0.5f)));
             const float fy = __fsub_rn(__fadd_rn(v, 0.5f), floorf(__fadd_rn(v, 0.5f)));
@@ -1419,10 +1444,11 @@ __global__ void k_pattern_shade(const uint32_t *tile, float4 *out, PatternParams
 }  // namespace
 
 cudaError_t filter_pattern_shade(const uint32_t *tile, int tw, int th, float *out, int bx, int by, int bw, int bh,
-                                 const float inv[6], bool nearest, float opacity, cudaStream_t s) {
+                                 const float inv[6], int quality, bool repeat, float opacity, cudaStream_t s) {
     const size_t n = (size_t)bw * bh;
     if (n == 0 || tw <= 0 || th <= 0) return cudaSuccess;
-    PatternParams pp{inv[0], inv[1], inv[2], inv[3], inv[4], inv[5], tw, th, bx, by, bw, bh, nearest ? 1 : 0, opacity};
+    PatternParams pp{inv[0], inv[1], inv[2], inv[3], inv[4], inv[5], tw, th, bx, by, bw, bh, quality,
+                     repeat ? 1 : 0, opacity};
     k_pattern_shade<<<nblk_capped(n, 256), 256, 0, s>>>(tile, reinterpret_cast<float4 *>(out), pp);
     return cudaGetLastError();
 }

@@ -73,10 +73,11 @@ cudaError_t filter_displacement_map(const uint32_t *src, const uint32_t *map, ui
                                     float sy, float scale, int xch, int ych, cudaStream_t s);
 // The Pattern shader of a fill (tiny-skia's pattern pipeline, highp): for each
 // layer pixel of (bx, by, bw, bh), the pixel centre through `inv` (sx, ky, kx,
-// sy, tx, ty) into the tw x th tile, repeat tiling, nearest or bicubic
-// sampling, clamp, opacity; premultiplied float4 per pixel into `out`.
+// sy, tx, ty) into the tw x th tile, repeat or pad tiling, nearest (0),
+// bilinear (1) or bicubic (2, then clamped) sampling, opacity; premultiplied
+// float4 per pixel into `out`.
 cudaError_t filter_pattern_shade(const uint32_t *tile, int tw, int th, float *out, int bx, int by, int bw, int bh,
-                                 const float inv[6], bool nearest, float opacity, cudaStream_t s);
+                                 const float inv[6], int quality, bool repeat, float opacity, cudaStream_t s);
 // feDropShadow after the shadow copy is blurred; flood = r | g << 8 | b << 16 | opacity_u8 << 24.
 cudaError_t filter_drop_shadow(const uint32_t *in, const uint32_t *shadow, uint32_t *out, int w, int h, int dx,
                                int dy, uint32_t flood, bool linear, cudaStream_t s);

@@ -43,8 +43,15 @@ def _unfilter(raw: bytes, h: int, stride: int, bpp: int) -> np.ndarray:
 
 def read_png(path: str) -> np.ndarray:
     """Returns an (h, w, 4) uint8 RGBA (straight alpha) array."""
-    data = open(path, "rb").read()
-    assert data[:8] == b"\x89PNG\r\n\x1a\n", path
+    with open(path, "rb") as fh:
+        return decode_png(fh.read())
+
+
+def decode_png(data: bytes) -> np.ndarray:
+    """An (h, w, 4) uint8 RGBA (straight alpha) array from PNG bytes; 16-bit
+    samples keep their high byte."""
+    if data[:8] != b"\x89PNG\r\n\x1a\n":
+        raise ValueError("not a PNG")
     pos = 8
     idat = b""
     plte = None
@@ -124,19 +131,22 @@ def _expand(px, ctype, plte, trns, w, h):
     return out
 
 
-def write_png(path: str, rgba: np.ndarray) -> None:
-    """Writes an (h, w, 4) uint8 straight-alpha RGBA array."""
+def encode_png(rgba: np.ndarray) -> bytes:
+    """PNG bytes of an (h, w, 4) uint8 straight-alpha RGBA array."""
     h, w, _ = rgba.shape
     raw = b"".join(b"\x00" + rgba[y].tobytes() for y in range(h))
 
     def chunk(tp, body):
         return struct.pack(">I", len(body)) + tp + body + struct.pack(">I", zlib.crc32(tp + body) & 0xFFFFFFFF)
 
+    return (b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 6, 0, 0, 0)) +
+            chunk(b"IDAT", zlib.compress(raw, 6)) + chunk(b"IEND", b""))
+
+
+def write_png(path: str, rgba: np.ndarray) -> None:
+    """Writes an (h, w, 4) uint8 straight-alpha RGBA array."""
     with open(path, "wb") as fh:
-        fh.write(b"\x89PNG\r\n\x1a\n")
-        fh.write(chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 6, 0, 0, 0)))
-        fh.write(chunk(b"IDAT", zlib.compress(raw, 6)))
-        fh.write(chunk(b"IEND", b""))
+        fh.write(encode_png(rgba))
 
 
 def demultiply(premul: np.ndarray) -> np.ndarray:

@@ -355,6 +355,16 @@ def parse_length(s, ref=0.0, font_size=12.0):
     raise Unsupported("unit " + u)
 
 
+def struct_error():
+    import struct
+    return struct.error
+
+
+def zlib_error():
+    import zlib
+    return zlib.error
+
+
 def view_box_transform(vb, par, w, h):
     """usvg ViewBox::to_transform (utils.rs view_box_to_transform): the viewBox
     (x, y, w, h) fitted into a w x h viewport by preserveAspectRatio."""
@@ -754,7 +764,7 @@ INHERITED = {"fill", "fill-opacity", "fill-rule", "stroke", "stroke-width", "str
              "shape-rendering", "clip-rule", "color", "color-interpolation-filters", "paint-order", "font-size"}
 NON_INHERITED = {"opacity", "clip-path", "mask", "filter", "mix-blend-mode", "isolation", "display",
                  "stop-color", "stop-opacity", "flood-color", "flood-opacity", "transform"}
-UNSUPPORTED_ELEMS = {"text", "image", "marker", "switch", "foreignObject", "tspan", "textPath", "symbol",
+UNSUPPORTED_ELEMS = {"text", "marker", "switch", "foreignObject", "tspan", "textPath", "symbol",
                      "style", "animate", "set"}
 BLEND = {"normal": "source-over", "multiply": "multiply", "screen": "screen", "overlay": "overlay",
          "darken": "darken", "lighten": "lighten", "color-dodge": "color-dodge", "color-burn": "color-burn",
@@ -979,11 +989,15 @@ class Builder(Loader):
             return
         if not self.visible(e):
             return
-        if tag not in ("g", "path", "rect", "circle", "ellipse", "line", "polyline", "polygon", "use", "svg", "a"):
+        if tag not in ("g", "path", "rect", "circle", "ellipse", "line", "polyline", "polygon", "use", "svg", "a",
+                       "image"):
             raise Unsupported("element " + tag)
         ts = parse_transform(self.attrs(e).get("transform", ""))
         if transform_extra != IDENT:
             ts = mat_mul(transform_extra, ts)
+        if tag == "image":
+            self.image(e, parent, ts)
+            return
         if tag == "use":
             ref = self.href(e)
             if ref is None:
@@ -1517,6 +1531,103 @@ class Builder(Loader):
         pi = self.tree.add_path(parent, path, verbs, pts, dashes)
         if e.get("id") is not None:
             self.ids_out.setdefault(e.get("id"), "p%d" % pi)
+
+    # ---- raster images
+    def image(self, e, parent, ts):
+        """<image> of a PNG data URL, as usvg converts it (parser/image.rs:110-264)
+        and resvg draws it (image.rs:167-201): the decoded pixels, premultiplied
+        like tiny-skia's decoder, fill the rect (0, 0, width, height) of a group
+        whose transform fits that rect into the element's viewport by
+        preserveAspectRatio (a clip to the viewport for `slice`); padded, and
+        sampled nearest, bilinear or bicubic by image-rendering.  JPEG, GIF,
+        WebP, SVG images and file references are not supported."""
+        import base64
+        from . import png
+        href = (e.get(XLINK) or e.get("href") or "").strip()
+        if not href.startswith("data:"):
+            raise Unsupported("image file reference")
+        head, _, payload = href.partition(",")
+        if ";base64" not in head:
+            raise Unsupported("image data URL encoding")
+        try:
+            data = base64.b64decode("".join(payload.split()))
+        except ValueError:
+            return
+        mime = head[5:].split(";")[0].strip().lower()
+        if mime in ("image/jpg", "image/jpeg", "image/gif", "image/webp", "image/svg+xml"):
+            raise Unsupported("image " + mime)
+        if mime != "image/png" and data[:8] != b"\x89PNG\r\n\x1a\n":
+            raise Unsupported("image of an unknown type")
+        try:
+            rgba = png.decode_png(data)
+        except (ValueError, KeyError, IndexError, struct_error(), zlib_error()):
+            return
+        if (self.get(e, "visibility") or "visible").strip() != "visible":
+            return
+        a = rgba[..., 3:4].astype(np.uint32)
+        prod = rgba[..., :3].astype(np.uint32) * a + 128  # tiny-skia premultiply_u8
+        rgba = np.concatenate([((prod + (prod >> 8)) >> 8).astype(np.uint8), rgba[..., 3:4]], axis=2)
+        F = np.float32
+        ah, aw = F(rgba.shape[0]), F(rgba.shape[1])
+        x, y = F(self.num(e, "x", 0.0, self.vbw)), F(self.num(e, "y", 0.0, self.vbh))
+        w, h = F(self.num(e, "width", float(aw), self.vbw)), F(self.num(e, "height", float(ah), self.vbh))
+        has_w, has_h = e.get("width") is not None, e.get("height") is not None
+        if has_w and not has_h:
+            h = F(ah * F(w / aw))
+        elif has_h and not has_w:
+            w = F(aw * F(h / ah))
+        if not (w > 0 and h > 0):
+            return
+        parts = (e.get("preserveAspectRatio") or "").split()
+        if parts and parts[0] == "defer":
+            parts = parts[1:]
+        align = parts[0] if parts else "xMidYMid"
+        slice_ = len(parts) > 1 and parts[1] == "slice"
+        if align == "none":
+            sw, sh = w, h
+        else:
+            # tiny-skia-path Size::scale_to / expand_to
+            rw = F(F(h * aw) / ah)
+            with_h = (rw <= w) if slice_ else (rw >= w)
+            sw, sh = (rw, h) if not with_h else (w, F(F(w * ah) / aw))
+        ox, oy = x, y
+        if align != "none":
+            ax, ay = align[1:4], align[5:8]
+            dx, dy = F(w - sw), F(h - sh)
+            ox = x + (F(dx / F(2)) if ax == "Mid" else (dx if ax == "Max" else F(0)))
+            oy = y + (F(dy / F(2)) if ay == "Mid" else (dy if ay == "Max" else F(0)))
+        image_ts = (float(F(sw / aw)), 0.0, 0.0, float(F(sh / ah)), float(F(ox)), float(F(oy)))
+        mode = (self.get(e, "image-rendering") or "optimizeQuality").strip()
+        quality = {"optimizeSpeed": A.IMAGE_NEAREST, "crisp-edges": A.IMAGE_NEAREST, "pixelated": A.IMAGE_NEAREST,
+                   "smooth": A.IMAGE_BILINEAR}.get(mode, A.IMAGE_BICUBIC)
+        g = self.group_for(e, parent, ts)
+        if g is None:
+            return
+        if slice_ and align != "none":
+            root = self.tree.add_group(-1, _group())
+            self.rect_path(root, (float(x), float(y), float(w), float(h)), self.solid(((0, 0, 0), 1.0)))
+            c = A.Clip()
+            c.transform = _tf(IDENT)
+            c.clip_path = -1
+            c.root = root
+            g = self.tree.add_group(g, _group(clip_path=self.tree.add_clip(c)))
+        gi = self.tree.add_group(g, _group(transform=_tf(image_ts)))
+        p = A.Paint()
+        p.kind = A.PAINT_IMAGE
+        p.stop_offset = self.tree.add_image(rgba)
+        p.spread = quality
+        p.transform = A.Transform.identity()
+        self.rect_path(gi, (0.0, 0.0, float(aw), float(ah)), self.tree.add_paint(p, []))
+
+    def rect_path(self, parent, r, paint):
+        """A filled rect path (PathBuilder::from_rect) under `parent`."""
+        x, y, w, h = r
+        path = A.Path()
+        path.fill_paint, path.fill_opacity, path.fill_rule = paint, 1.0, A.NONZERO
+        path.stroke_paint, path.stroke_width = -1, 1.0
+        path.visible, path.anti_alias = 1, 1
+        self.tree.add_path(parent, path, [A.MOVE, A.LINE, A.LINE, A.LINE, A.CLOSE],
+                           [(x, y), (x + w, y), (x + w, y + h), (x, y + h)])
 
     # ---- clip paths
     def clip(self, ce, bbox):

@@ -49,7 +49,7 @@ CATEGORIES = [
     "filters/feDistantLight", "filters/fePointLight", "filters/feSpotLight",
     "filters/filter-functions", "filters/feComponentTransfer", "filters/feDropShadow",
     "filters/feTurbulence", "filters/feTile", "filters/feDisplacementMap", "filters/feImage",
-    "paint-servers/pattern",
+    "paint-servers/pattern", "structure/image",
 ]
 IMAGE_SIZE = 300
 FIXTURES_PER_DIR = 4

@@ -1,4 +1,4 @@
-"""Pattern fills and strokes on the GPU vs the CPU oracle.
+"""Pattern fills and strokes, and raster images, on the GPU vs the CPU oracle.
 
 The tile is rendered by its own command stream, the Pattern shader (repeat
 tiling, bicubic or nearest sampling, clamp, opacity) is evaluated per layer
@@ -50,6 +50,38 @@ TRANSFORMS = [(1.5, 0, 0, 1.5, 0, 0), (1, 0, 0, 1, 0, 0), (0.8660254, 0.5, -0.5,
 def test_pattern_exact(gpu, oracle_mod, k, ts):
     text = ('<svg viewBox="0 0 200 200" xmlns="http://www.w3.org/2000/svg"><defs>%s</defs>%s</svg>'
             % (DEFS, SCENES[k]))
+    tree = svg.load_svg(text)
+    g = R.render(tree, ts, 300, 300)
+    o = oracle_mod.render(tree.view(), ts, 300, 300)
+    assert o[..., 3].any()
+    assert diff_stats(g, o) == (0, 0)
+
+
+def _png_data_url(seed, w, h):
+    import base64
+    import numpy as np
+    from resvg_gb300 import png
+    rng = np.random.default_rng(seed)
+    img = rng.integers(0, 256, (h, w, 4), dtype=np.uint8)
+    img[rng.random((h, w)) < 0.4, 3] = 255
+    return "data:image/png;base64," + base64.b64encode(png.encode_png(img)).decode()
+
+
+IMAGES = [
+    '<image x="20" y="30" width="160" height="100" href="%s"/>',
+    '<image x="20" y="30" width="160" height="100" preserveAspectRatio="xMaxYMid slice" '
+    'image-rendering="optimizeSpeed" href="%s"/>',
+    '<image x="10" y="10" width="170" href="%s" style="image-rendering:smooth" opacity="0.6" '
+    'transform="rotate(12 100 100)"/>',
+    '<g transform="translate(7 5)"><image width="40" height="30" href="%s" preserveAspectRatio="none"/></g>',
+]
+
+
+@pytest.mark.parametrize("ts", TRANSFORMS)
+@pytest.mark.parametrize("k", range(len(IMAGES)))
+def test_raster_image_exact(gpu, oracle_mod, k, ts):
+    text = ('<svg viewBox="0 0 200 200" xmlns="http://www.w3.org/2000/svg">%s</svg>'
+            % (IMAGES[k] % _png_data_url(k, 23 + k, 17)))
     tree = svg.load_svg(text)
     g = R.render(tree, ts, 300, 300)
     o = oracle_mod.render(tree.view(), ts, 300, 300)
