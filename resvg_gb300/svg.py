@@ -72,6 +72,8 @@ def parse_color(s: str, current=(0, 0, 0)):
         return NAMED[low], 1.0
     if s.startswith("#"):
         h = s[1:]
+        if not re.fullmatch(r"[0-9a-fA-F]*", h):
+            raise InvalidColor("color " + s)
         if len(h) == 3:
             return tuple(int(c * 2, 16) for c in h), 1.0
         if len(h) == 4:
@@ -797,6 +799,43 @@ class Loader:
         # feImage links to drops its `filter` attribute when it, or an element
         # inside it, uses that same filter
         self.pattern_active = set()
+        # usvg's fix_recursive_links (svgtree/parse.rs:776-810) for clip paths and
+        # masks: inside element P (P included), a clip-path / mask linking to P,
+        # or to an element with a link back to P inside it, reads as none;
+        # repeated, in document order, until none is left
+        self.no_link = set()
+
+        def link_of(n, name):
+            if (n, name) in self.no_link:
+                return None
+            v = self.attrs(n).get(name)
+            m = re.match(r"\s*url\(\s*['\"]?#([^'\")]+)['\"]?\s*\)", v or "")
+            return self.ids.get(m.group(1)) if m else None
+        for tag, name in (("clipPath", "clip-path"), ("mask", "mask")):
+            nodes = [n for n in self.root.iter() if isinstance(n.tag, str) and _tag(n) == tag]
+            for _ in range(10000):
+                found = None
+                for node in nodes:
+                    for child in node.iter():
+                        if not isinstance(child.tag, str):
+                            continue
+                        link = link_of(child, name)
+                        if link is None:
+                            continue
+                        if link is node:
+                            found = (child, name)
+                        else:
+                            for n2 in link.iter():
+                                if isinstance(n2.tag, str) and link_of(n2, name) is node:
+                                    found = (n2, name)
+                                    break
+                        if found:
+                            break
+                    if found:
+                        break
+                if not found:
+                    break
+                self.no_link.add(found)
         # usvg's recursive-pattern fix, in document order: inside pattern P, a
         # fill or stroke linking to P reads as none; one linking to pattern Q
         # stays, and the paints inside Q that link back to P read as none
@@ -908,9 +947,9 @@ class Loader:
         return parse_length(v, ref, self.font_size(e))
 
     def href(self, e):
-        h = e.get(XLINK) or e.get("href")
-        if h and h.startswith("#"):
-            return self.ids.get(h[1:])
+        h = e.get("href") or e.get(XLINK)  # SVG 2: href takes precedence
+        if h and h.strip().startswith("#"):
+            return self.ids.get(h.strip()[1:])
         return None
 
     def ref(self, value):
@@ -971,8 +1010,13 @@ class Builder(Loader):
         root = self.tree.add_group(-1, _group())
         if root_ts != IDENT:
             root = self.tree.add_group(root, _group(transform=_tf(root_ts)))
-        for c in svg:
-            self.node(c, root)
+        # the root <svg> is a group of its own (opacity, clip-path, mask, filter,
+        # display) inside the viewBox transform, as usvg converts it
+        if self.attrs(svg).get("display", "").strip() != "none":
+            g = self.group_for(svg, root, IDENT)
+            if g is not None:
+                for c in svg:
+                    self.node(c, g)
         self.tree.finalize()
         self.tree.ids = self.ids_out
         return self.tree
@@ -1039,10 +1083,10 @@ class Builder(Loader):
         """Creates the group an element needs (transform, opacity, clip, mask,
         filter, blend); returns the parent to add children to."""
         a = self.attrs(e)
-        opacity = float(a.get("opacity", "1").strip()) if "opacity" in a else 1.0
+        opacity = opacity_value(a.get("opacity"))
         opacity = max(0.0, min(1.0, opacity))
-        clip = self.ref(a.get("clip-path"))
-        mask = self.ref(a.get("mask"))
+        clip = self.ref(a.get("clip-path") if (e, "clip-path") not in self.no_link else None)
+        mask = self.ref(a.get("mask") if (e, "mask") not in self.no_link else None)
         filt = a.get("filter") if e not in self.no_filter else None
         # mix-blend-mode and isolation count only as CSS properties (style), not as
         # presentation attributes
@@ -1055,8 +1099,9 @@ class Builder(Loader):
         if blend is None:
             raise Unsupported("blend mode")
         isolate = css.get("isolation", "auto").strip() == "isolate"
-        if clip == "missing" or mask == "missing":
-            return None  # references to missing elements: the element is not rendered
+        # svgtree drops a clip-path / mask attribute whose link has no element
+        clip = None if clip == "missing" else clip
+        mask = None if mask == "missing" else mask
         eid = e.get("id")
         keep_id = eid is not None and _tag(e) in ("g", "use")
         needs = ts != IDENT or opacity != 1.0 or clip is not None or mask is not None or filt or \
@@ -1108,7 +1153,7 @@ class Builder(Loader):
     # ---- bounding boxes (object bounding box of an element, its user space)
     def element_bbox(self, e):
         tag = _tag(e)
-        if tag in ("g", "a"):
+        if tag in ("g", "a", "svg"):
             boxes = []
             for c in e:
                 if _tag(c) in ("defs", "title", "desc") or not self.visible(c):
@@ -1367,7 +1412,12 @@ class Builder(Loader):
         return self.tree.add_paint(p)
 
     def grad_attr(self, e, name, chain):
+        """usvg resolve_attr: the gradient attributes through the href chain;
+        vector / circle attributes only from gradients of the same kind."""
+        own = {"x1", "y1", "x2", "y2"} if _tag(e) == "linearGradient" else {"cx", "cy", "r", "fx", "fy", "fr"}
         for g in chain:
+            if name in own and _tag(g) != _tag(e):
+                continue
             v = g.get(name)
             if v is not None:
                 return v
@@ -1376,7 +1426,7 @@ class Builder(Loader):
     def gradient(self, ref, bbox, opacity):
         chain, g = [], ref
         seen = set()
-        while g is not None and id(g) not in seen:
+        while g is not None and id(g) not in seen and _tag(g) in ("linearGradient", "radialGradient"):
             seen.add(id(g))
             chain.append(g)
             g = self.href(g)
@@ -1394,7 +1444,8 @@ class Builder(Loader):
                 o = prev
             else:
                 off = off.strip()
-                o = float(off[:-1]) / 100 if off.endswith("%") else float(off)
+                ov = number_strict(off[:-1] if off.endswith("%") else off)
+                o = (ov / 100 if off.endswith("%") else ov) if ov is not None else 0.0
             prev = o
             o = max(0.0, min(1.0, o))
             col = sa.get("stop-color", "black")
@@ -1511,7 +1562,8 @@ class Builder(Loader):
                 path.stroke_paint, path.stroke_opacity = stroke[0], float(np.float32(stroke[1]))
                 path.stroke_width = float(np.float32(width))
                 ml = self.get(e, "stroke-miterlimit")
-                path.miter_limit = max(float(ml), 1.0) if ml else 4.0  # style.rs: below 1 reads as 1
+                mlv = number_strict(ml) if ml else None
+                path.miter_limit = max(mlv, 1.0) if mlv is not None else 4.0  # style.rs: below 1 reads as 1
                 path.line_cap = {"butt": 0, "round": 1, "square": 2}.get((self.get(e, "stroke-linecap") or "butt").strip(), 0)
                 path.line_join = {"miter": 0, "miter-clip": 1, "round": 2, "bevel": 3, "arcs": 0}.get(
                     (self.get(e, "stroke-linejoin") or "miter").strip(), 0)
@@ -1653,7 +1705,7 @@ class Builder(Loader):
         c.transform = _tf(ts)
         c.clip_path = -1
         c.root = root
-        nested = self.ref(self.attrs(ce).get("clip-path"))
+        nested = self.ref(self.attrs(ce).get("clip-path") if (ce, "clip-path") not in self.no_link else None)
         if nested == "missing":
             return None
         if nested is not None:
@@ -1676,7 +1728,7 @@ class Builder(Loader):
                 raise Unsupported("clip use")
             ts = mat_mul(ts, (1, 0, 0, 1, self.num(e, "x", 0.0, self.vbw), self.num(e, "y", 0.0, self.vbh)))
         parent = root
-        cp = self.ref(a.get("clip-path"))
+        cp = self.ref(a.get("clip-path") if (e, "clip-path") not in self.no_link else None)
         ci = -1
         if cp is not None:
             if cp == "missing":
@@ -1743,7 +1795,7 @@ class Builder(Loader):
         m.kind = A.MASK_ALPHA if mt == "alpha" else A.MASK_LUMINANCE
         m.mask = -1
         m.root = root
-        nested = self.ref(self.attrs(me).get("mask"))
+        nested = self.ref(self.attrs(me).get("mask") if (me, "mask") not in self.no_link else None)
         if nested == "missing":
             return None
         if nested is not None:
@@ -2030,10 +2082,40 @@ class Builder(Loader):
     def filter(self, fe, bbox):
         if _tag(fe) != "filter":
             return None
+        # parser/filter.rs convert_url: region attributes and units through the
+        # xlink:href chain, primitives from the first filter in it with children
+        chain, g, seen = [], fe, set()
+        while g is not None and id(g) not in seen and _tag(g) == "filter":  # links to other elements end it
+            seen.add(id(g))
+            chain.append(g)
+            g = self.href(g)
+        if len(chain) > 1:
+            merged = ET.Element(fe.tag, dict(fe.attrib))
+            for name in ("x", "y", "width", "height", "filterUnits", "primitiveUnits"):
+                if merged.get(name) is None:
+                    v = next((n.get(name) for n in chain[1:] if n.get(name) is not None), None)
+                    if v is not None:
+                        merged.set(name, v)
+            src = next((n for n in chain if any(isinstance(k.tag, str) for k in n)), None)
+            if src is None:
+                return None
+            merged.extend(list(src))
+            fe = merged
         units = (fe.get("filterUnits") or "objectBoundingBox").strip()
         punits = (fe.get("primitiveUnits") or "userSpaceOnUse").strip()
-        if punits != "userSpaceOnUse":
-            raise Unsupported("primitiveUnits")
+        pobb = punits == "objectBoundingBox"
+        F32 = np.float32
+        if pobb and (bbox is None or not (bbox[2] > bbox[0] and bbox[3] > bbox[1])):
+            return None  # parser/filter.rs: primitive units on a zero-sized shape
+        # parser/filter.rs:307-320: objectBoundingBox primitive units scale
+        # lengths (std deviations, offsets, radii, displacement) by the bbox size
+        sw, sh = (F32(F32(bbox[2]) - F32(bbox[0])), F32(F32(bbox[3]) - F32(bbox[1]))) if pobb else (F32(1), F32(1))
+
+        def frac(v, default):
+            if v is None:
+                return F32(default)
+            v = v.strip()
+            return F32(float(v[:-1]) / 100) if v.endswith("%") else F32(float(v))
 
         def fr(e, name, default):
             v = e.get(name)
@@ -2060,10 +2142,25 @@ class Builder(Loader):
             if tag in ("title", "desc"):
                 continue
             p = A.Primitive()
-            p.x = self.num(c, "x", x, self.vbw) if c.get("x") is not None else x
-            p.y = self.num(c, "y", y, self.vbh) if c.get("y") is not None else y
-            p.w = self.num(c, "width", w, self.vbw) if c.get("width") is not None else w
-            p.h = self.num(c, "height", h, self.vbh) if c.get("height") is not None else h
+            if pobb:
+                # parser/filter.rs resolve_primitive_region: flood / image
+                # subregions are fractions of the element's bbox; the others map
+                # the filter region through the fractions (as usvg does)
+                fx, fy = frac(c.get("x"), 0.0), frac(c.get("y"), 0.0)
+                fw, fh = frac(c.get("width"), 1.0), frac(c.get("height"), 1.0)
+                if not (fw > 0 and fh > 0):
+                    break
+                if tag in ("feFlood", "feImage"):
+                    p.x, p.y = float(F32(fx * sw) + F32(bbox[0])), float(F32(fy * sh) + F32(bbox[1]))
+                    p.w, p.h = float(F32(fw * sw)), float(F32(fh * sh))
+                else:
+                    p.x, p.y = float(F32(F32(x) * fw) + fx), float(F32(F32(y) * fh) + fy)
+                    p.w, p.h = float(F32(F32(w) * fw)), float(F32(F32(h) * fh))
+            else:
+                p.x = self.num(c, "x", x, self.vbw) if c.get("x") is not None else x
+                p.y = self.num(c, "y", y, self.vbh) if c.get("y") is not None else y
+                p.w = self.num(c, "width", w, self.vbw) if c.get("width") is not None else w
+                p.h = self.num(c, "height", h, self.vbh) if c.get("height") is not None else h
             cif = (self.get(c, "color-interpolation-filters") or "linearRGB").strip()
             p.linear_rgb = 0 if cif == "sRGB" else 1
 
@@ -2092,7 +2189,8 @@ class Builder(Loader):
                 # parser/filter.rs convert_std_dev_attr: one or two numbers, else
                 # 0 0; a negative component becomes 0
                 p.kind = A.FE_BLUR
-                p.f[0], p.f[1] = std_dev_attr(c.get("stdDeviation", "0 0"))
+                sdx, sdy = std_dev_attr(c.get("stdDeviation", "0 0"))
+                p.f[0], p.f[1] = float(F32(sdx) * sw), float(F32(sdy) * sh)
             elif tag == "feColorMatrix":
                 p.kind = A.FE_COLOR_MATRIX
                 t = (c.get("type") or "matrix").strip()
@@ -2125,7 +2223,7 @@ class Builder(Loader):
                 # parser/filter.rs convert_morphology: default 1 1; one or two
                 # numbers (else 0 0); a zero component becomes 1; a negative one
                 # keeps the default
-                rx = ry = 1.0
+                rx, ry = 1.0, 1.0
                 if c.get("radius") is not None:
                     r = numbers(c.get("radius"))
                     a, b = (r[0], r[1]) if len(r) == 2 else ((r[0], r[0]) if len(r) == 1 else (0.0, 0.0))
@@ -2137,7 +2235,7 @@ class Builder(Loader):
                         b = 1.0
                     if math.copysign(1.0, a) > 0 and math.copysign(1.0, b) > 0:
                         rx, ry = a, b
-                p.f[0], p.f[1] = rx, ry
+                p.f[0], p.f[1] = float(F32(rx) * sw), float(F32(ry) * sh)
             elif tag == "feComposite":
                 p.kind = A.FE_COMPOSITE
                 p.in2 = inp("in2")
@@ -2156,7 +2254,8 @@ class Builder(Loader):
             elif tag == "feOffset":
                 p.kind = A.FE_OFFSET
                 dx, dy = number_strict(c.get("dx")), number_strict(c.get("dy"))
-                p.f[0], p.f[1] = dx if dx is not None else 0.0, dy if dy is not None else 0.0
+                p.f[0] = float(F32(dx if dx is not None else 0.0) * sw)
+                p.f[1] = float(F32(dy if dy is not None else 0.0) * sh)
             elif tag == "feComponentTransfer":
                 self.component_transfer(c, p)
             elif tag == "feImage":
@@ -2171,7 +2270,7 @@ class Builder(Loader):
                 p.i[0] = ch.get(c.get("xChannelSelector"), 3)
                 p.i[1] = ch.get(c.get("yChannelSelector"), 3)
                 sc = number_strict(c.get("scale"))
-                p.f[0] = sc if sc is not None else 0.0
+                p.f[0] = float(F32(sc if sc is not None else 0.0) * F32(F32(sw + sh) / F32(2)))
             elif tag == "feTurbulence":
                 # parser/filter.rs convert_turbulence
                 p.kind = A.FE_TURBULENCE
@@ -2199,9 +2298,11 @@ class Builder(Loader):
                 # parser/filter.rs convert_drop_shadow: stdDeviation "2 2", dx and dy
                 # numbers (default 2), flood colour and opacity as feFlood
                 p.kind = A.FE_DROP_SHADOW
-                p.f[0], p.f[1] = std_dev_attr(c.get("stdDeviation", "2 2"))
+                sdx, sdy = std_dev_attr(c.get("stdDeviation", "2 2"))
+                p.f[0], p.f[1] = float(F32(sdx) * sw), float(F32(sdy) * sh)
                 dx, dy = number_strict(c.get("dx")), number_strict(c.get("dy"))
-                p.f[2], p.f[3] = dx if dx is not None else 2.0, dy if dy is not None else 2.0
+                p.f[2] = float(F32(dx if dx is not None else 2.0) * sw)
+                p.f[3] = float(F32(dy if dy is not None else 2.0) * sh)
                 rgb, alpha = self.attr_color(c, "flood-color")
                 p.i[0], p.i[1], p.i[2] = rgb
                 p.f[4] = float(F(alpha) * F(opacity_value(self.attrs(c).get("flood-opacity"))))
