@@ -996,10 +996,11 @@ class Builder(Loader):
             W = parse_length(w, vb[2]) if (w and not w.strip().endswith("%")) else vb[2]
             H = parse_length(h, vb[3]) if (h and not h.strip().endswith("%")) else vb[3]
             par = svg.get("preserveAspectRatio")
-            if par not in (None, "xMidYMid", "xMidYMid meet"):
-                raise Unsupported("preserveAspectRatio")
-            s = min(W / vb[2], H / vb[3])
-            root_ts = (s, 0, 0, s, -vb[0] * s + (W - vb[2] * s) / 2, -vb[1] * s + (H - vb[3] * s) / 2)
+            if par in (None, "xMidYMid", "xMidYMid meet"):
+                s = min(W / vb[2], H / vb[3])
+                root_ts = (s, 0, 0, s, -vb[0] * s + (W - vb[2] * s) / 2, -vb[1] * s + (H - vb[3] * s) / 2)
+            else:
+                root_ts = view_box_transform(vb, par, W, H)
         else:
             W = parse_length(w, 100) if w else 100.0
             H = parse_length(h, 100) if h else 100.0
@@ -1075,9 +1076,43 @@ class Builder(Loader):
                 else:
                     self.parent[ref] = saved
         elif tag == "svg":
-            raise Unsupported("nested svg")
+            self.nested_svg(e, g)
         else:
             self.shape(e, g)
+
+    def nested_svg(self, e, g):
+        """A nested <svg> as usvg converts it (use_node.rs:163-211, 295-371): its
+        content under translate(x, y) and the viewBox transform, in a new
+        viewport for percentages, clipped to (x, y, width, height) unless
+        overflow is visible / auto or width and height are not both given."""
+        x, y = self.num(e, "x", 0.0, self.vbw), self.num(e, "y", 0.0, self.vbh)
+        w, h = self.num(e, "width", self.vbw, self.vbw), self.num(e, "height", self.vbh, self.vbh)
+        vb = numbers(e.get("viewBox")) if e.get("viewBox") is not None else None
+        if vb is not None and (len(vb) != 4 or not (vb[2] > 0 and vb[3] > 0)):
+            vb = None
+        new_ts = (1.0, 0.0, 0.0, 1.0, x, y)
+        if vb is not None and w > 0 and h > 0:
+            new_ts = mat_mul(new_ts, view_box_transform(vb, e.get("preserveAspectRatio") or "", w, h))
+        new_vb = (vb[2], vb[3]) if vb is not None else ((w, h) if w > 0 and h > 0 else (self.vbw, self.vbh))
+        ov = (self.attrs(e).get("overflow") or "").strip()
+        parent = g
+        if ov not in ("visible", "auto") and e.get("width") is not None and e.get("height") is not None \
+                and w > 0 and h > 0:
+            root = self.tree.add_group(-1, _group())
+            self.rect_path(root, (x, y, w, h), self.solid(((0, 0, 0), 1.0)))
+            c = A.Clip()
+            c.transform = _tf(IDENT)
+            c.clip_path = -1
+            c.root = root
+            parent = self.tree.add_group(g, _group(clip_path=self.tree.add_clip(c)))
+        inner = self.tree.add_group(parent, _group(transform=_tf(new_ts)))
+        saved = (self.vbw, self.vbh)
+        self.vbw, self.vbh = new_vb
+        try:
+            for c in e:
+                self.node(c, inner)
+        finally:
+            self.vbw, self.vbh = saved
 
     def group_for(self, e, parent, ts):
         """Creates the group an element needs (transform, opacity, clip, mask,
