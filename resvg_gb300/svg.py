@@ -357,6 +357,133 @@ def parse_length(s, ref=0.0, font_size=12.0):
     raise Unsupported("unit " + u)
 
 
+_CSS_NOT_PRESENTATION = {"x", "y", "width", "height", "rx", "ry", "cx", "cy", "r", "d", "points", "x1", "y1",
+                         "x2", "y2", "href", "id", "class", "viewBox", "preserveAspectRatio", "offset"}
+_CSS_SIMPLE = re.compile(r"\*|[A-Za-z][\w-]*|#[\w-]+|\.[\w-]+|:first-child|"
+                         r"\[\s*([\w-]+)\s*(?:([~|^$*]?=)\s*[\"']?([^\"'\]]*)[\"']?\s*)?\]")
+
+
+def _css_compound(text):
+    """A compound selector as a list of (kind, value) tests, None if unsupported."""
+    out, pos = [], 0
+    while pos < len(text):
+        m = _CSS_SIMPLE.match(text, pos)
+        if not m:
+            return None
+        t = m.group(0)
+        if t.startswith("["):
+            out.append(("attr", (m.group(1), m.group(2), m.group(3))))
+        elif t == ":first-child":
+            out.append(("first", None))
+        elif t[0] in "#.":
+            out.append(("id" if t[0] == "#" else "class", t[1:]))
+        elif t != "*":
+            out.append(("type", t))
+        pos = m.end()
+    return out
+
+
+def _css_selector(text):
+    """(parts, specificity): parts right to left as (compound, combinator to the left)."""
+    toks = re.findall(r">|[^\s>]+", text.strip())
+    parts, comb = [], " "
+    seq = []
+    for t in toks:
+        if t == ">":
+            comb = ">"
+            continue
+        c = _css_compound(t)
+        if c is None:
+            return None
+        seq.append((c, comb))
+        comb = " "
+    if not seq:
+        return None
+    spec = [0, 0, 0]
+    for c, _ in seq:
+        for kind, _v in c:
+            spec[0 if kind == "id" else (2 if kind == "type" else 1)] += 1
+    for i, (c, cb) in enumerate(seq):
+        parts.append((c, seq[i][1]))
+    return list(reversed(parts)), tuple(spec)
+
+
+def stylesheet_rules(root):
+    """{element: [(name, value, important)]} from the document's <style> sheets
+    (type text/css or none), in cascade order (specificity, then source order)."""
+    rules = []
+    for st in root.iter():
+        if not isinstance(st.tag, str) or _tag(st) != "style":
+            continue
+        if (st.get("type") or "text/css").strip() not in ("text/css", ""):
+            continue
+        text = re.sub(r"/\*.*?\*/", "", "".join(st.itertext()), flags=re.S)
+        for sel, body in re.findall(r"([^{}@]+)\{([^}]*)\}", text):
+            decls = []
+            for d in body.split(";"):
+                if ":" not in d:
+                    continue
+                k, v = d.split(":", 1)
+                v = v.strip()
+                imp = v.endswith("!important")
+                if imp:
+                    v = v[:-len("!important")].strip()
+                if k.strip() in _CSS_NOT_PRESENTATION:
+                    continue  # only presentation attributes come from style sheets
+                decls.append((k.strip(), v, imp))
+            for one in sel.split(","):
+                parsed = _css_selector(one)
+                if parsed is not None:
+                    rules.append((parsed[1], len(rules), parsed[0], decls))
+    if not rules:
+        return {}
+    parent = {c: p for p in root.iter() for c in p}
+
+    def test(e, comp):
+        for kind, v in comp:
+            if kind == "type" and _tag(e) != v:
+                return False
+            if kind == "id" and e.get("id") != v:
+                return False
+            if kind == "class" and v not in (e.get("class") or "").split():
+                return False
+            if kind == "first":
+                p = parent.get(e)
+                if p is None or [c for c in p if isinstance(c.tag, str)][0] is not e:
+                    return False
+            if kind == "attr":
+                name, op, val = v
+                got = e.get(name)
+                if got is None or (op == "=" and got != val) or (op == "~=" and val not in got.split()) or \
+                        (op == "^=" and not got.startswith(val)) or (op == "$=" and not got.endswith(val)) or \
+                        (op == "*=" and val not in got):
+                    return False
+        return True
+
+    def match(e, parts):
+        comp, comb = parts[0]
+        if not test(e, comp):
+            return False
+        if len(parts) == 1:
+            return True
+        p = parent.get(e)
+        if comb == ">":
+            return p is not None and match(p, parts[1:])
+        while p is not None:
+            if match(p, parts[1:]):
+                return True
+            p = parent.get(p)
+        return False
+    out = {}
+    for e in root.iter():
+        if not isinstance(e.tag, str):
+            continue
+        hits = sorted((spec, order, decls) for spec, order, parts, decls in rules if match(e, parts))
+        if hits:
+            out[e] = [d for _, _, decls in hits for d in decls]
+    return out
+
+
 def struct_error():
     import struct
     return struct.error
@@ -767,7 +894,7 @@ INHERITED = {"fill", "fill-opacity", "fill-rule", "stroke", "stroke-width", "str
 NON_INHERITED = {"opacity", "clip-path", "mask", "filter", "mix-blend-mode", "isolation", "display",
                  "stop-color", "stop-opacity", "flood-color", "flood-opacity", "transform"}
 UNSUPPORTED_ELEMS = {"text", "marker", "switch", "foreignObject", "tspan", "textPath", "symbol",
-                     "style", "animate", "set"}
+                     "animate", "set"}
 BLEND = {"normal": "source-over", "multiply": "multiply", "screen": "screen", "overlay": "overlay",
          "darken": "darken", "lighten": "lighten", "color-dodge": "color-dodge", "color-burn": "color-burn",
          "hard-light": "hard-light", "soft-light": "soft-light", "difference": "difference",
@@ -786,6 +913,7 @@ def _tag(e):
 class Loader:
     def __init__(self, text: str, tree_cls):
         self.root = ET.fromstring(text)
+        self.css = stylesheet_rules(self.root)
         if _tag(self.root) != "svg":
             raise Unsupported("root is not svg")
         self.ids = {}
@@ -887,20 +1015,30 @@ class Loader:
         for e in self.root.iter():
             if _tag(e) in UNSUPPORTED_ELEMS:
                 raise Unsupported("element " + _tag(e))
-            if e.get("class") is not None or e.get("systemLanguage") is not None:
-                raise Unsupported("class/systemLanguage")
+            if e.get("systemLanguage") is not None:
+                raise Unsupported("systemLanguage")
         self.clip_cache, self.mask_cache, self.filter_cache = {}, {}, {}
         self.ids_out = {}  # SVG id -> render_node id ("<group>" or "p<path>")
 
     # ---- attributes with style and inheritance
     def attrs(self, e):
+        """Attributes with CSS applied, as usvg's svgtree does: presentation
+        attributes, then matching <style> rules by specificity and order, then
+        the style attribute, then `!important` rules."""
         a = dict(e.attrib)
         st = a.pop("style", None)
+        important = {}
+        for k, v, imp in self.css.get(e, ()):
+            if imp:
+                important[k] = v
+            else:
+                a[k] = v
         if st:
             for part in st.split(";"):
                 if ":" in part:
                     k, v = part.split(":", 1)
                     a[k.strip()] = v.strip()
+        a.update(important)
         return a
 
     def get(self, e, name, inherited=True):
@@ -1030,7 +1168,7 @@ class Builder(Loader):
     def node(self, e, parent, transform_extra=IDENT):
         tag = _tag(e)
         if tag in ("defs", "linearGradient", "radialGradient", "clipPath", "mask", "filter", "title", "desc",
-                   "metadata", "stop", "pattern"):
+                   "metadata", "stop", "pattern", "style"):
             return
         if not self.visible(e):
             return
