@@ -91,6 +91,69 @@ def render_parallel(tree_view_ptr, transform, width: int, height: int, threads: 
     return pixmap
 
 
+class GeneratedTree:
+    """A seeded synthetic tree built inside the oracle library (the product's
+    generator source compiled in), so that no product library is loaded."""
+
+    def __init__(self, config: int, seed: int, index: int, scale: float = 1.0):
+        L = lib()
+        L.oracle_tree_generate.restype = C.c_void_p
+        L.oracle_tree_generate.argtypes = [C.c_int, C.c_uint64, C.c_uint64, C.c_float]
+        L.oracle_tree_view.restype = C.c_void_p
+        L.oracle_tree_view.argtypes = [C.c_void_p]
+        L.oracle_tree_free.restype = None
+        L.oracle_tree_free.argtypes = [C.c_void_p]
+        self._h = L.oracle_tree_generate(int(config), int(seed), int(index), float(scale))
+        if not self._h:
+            raise ValueError("unknown config %r" % config)
+        self._view = L.oracle_tree_view(self._h)
+        w, h = C.cast(self._view, C.POINTER(C.c_float * 2)).contents
+        self.size = (float(w), float(h))
+        self.path_count = _view_path_count(self._view)
+
+    def view(self):
+        return self._view
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            _lib.oracle_tree_free(h)
+            self._h = None
+
+
+def _view_path_count(view_ptr) -> int:
+    # rgpu_tree_view: width, height, groups*, group_count, children*, child_count, paths*, path_count
+    class _Head(C.Structure):
+        _fields_ = [("width", C.c_float), ("height", C.c_float), ("groups", C.c_void_p), ("group_count", C.c_uint32),
+                    ("children", C.c_void_p), ("child_count", C.c_uint32), ("paths", C.c_void_p),
+                    ("path_count", C.c_uint32)]
+    return int(C.cast(view_ptr, C.POINTER(_Head)).contents.path_count)
+
+
+def render_many(views, transforms, sizes, threads: int, pixmaps=None):
+    """Renders whole trees in parallel, one tree per host thread at a time, in
+    the order given; each result is identical to render() of that tree.
+    `views` are rgpu_tree_view pointers, `sizes` (w, h) pairs.  Returns the
+    pixmaps (fresh transparent ones when None)."""
+    n = len(views)
+    if pixmaps is None:
+        pixmaps = [np.zeros((int(h), int(w), 4), dtype=np.uint8) for w, h in sizes]
+    L = lib()
+    L.oracle_render_many.restype = C.c_int
+    L.oracle_render_many.argtypes = [C.POINTER(C.c_void_p), C.POINTER(C.c_float), C.POINTER(C.c_uint32),
+                                     C.POINTER(C.c_uint32), C.POINTER(C.c_void_p), C.c_uint32, C.c_uint32]
+    vs = (C.c_void_p * max(1, n))(*[C.cast(v, C.c_void_p).value for v in views])
+    ts = (C.c_float * max(6, 6 * n))(*[float(x) for t in transforms for x in t])
+    ws = (C.c_uint32 * max(1, n))(*[int(w) for w, _ in sizes])
+    hs = (C.c_uint32 * max(1, n))(*[int(h) for _, h in sizes])
+    for p, (w, h) in zip(pixmaps, sizes):
+        assert p.dtype == np.uint8 and p.shape == (int(h), int(w), 4) and p.flags.c_contiguous
+    ps = (C.c_void_p * max(1, n))(*[p.ctypes.data for p in pixmaps])
+    if L.oracle_render_many(vs, ts, ws, hs, ps, n, max(1, int(threads))) != 0:
+        raise RuntimeError("oracle_render_many failed")
+    return pixmaps
+
+
 def _img_op(name, img, *args):
     assert img.dtype == np.uint8 and img.ndim == 3 and img.shape[2] == 4
     out = np.ascontiguousarray(img).copy()

@@ -1,9 +1,9 @@
 """GPU render vs the CPU oracle on the same trees (parity gate).
 
-The integer (lowp) path must be bit-exact.  Gradients and layer composites run
-the highp f32 pipeline; the GPU evaluates the same IEEE operations in the same
-order, and the tolerance written here is the spec one: at most 1/255 per
-channel, with the differing-pixel count reported.
+Every case here runs tiny-skia's lowp pipeline (solid colours, linear and
+simple radial gradients, group opacity, the separable blend modes, integer
+clip and mask passes) or resvg's integer / f64 filter code, so the tolerance
+is 0: bit-exact, with the differing-pixel count in the failure message.
 """
 import numpy as np
 import pytest
@@ -42,7 +42,7 @@ def test_config1_small(gpu, oracle_mod):
     t = R.Tree.generate(1, seed=3, index=0, scale=0.04)
     g, o = _both(t, 1024, 1024)
     n, mx = diff_stats(g, o)
-    assert mx <= 1, "config1: %d px differ, max %d" % (n, mx)
+    assert n == 0, "config1: %d px differ, max %d" % (n, mx)
 
 
 def test_transform_and_clipping(gpu, oracle_mod):
@@ -89,7 +89,7 @@ def test_shapes_exact(gpu, oracle_mod):
     t = _scene_shapes()
     g, o = _both(t, 300, 300, (1.5, 0, 0, 1.5, 0, 0))
     n, mx = diff_stats(g, o)
-    assert mx <= 1, "%d px differ (max %d)" % (n, mx)
+    assert n == 0, "%d px differ (max %d)" % (n, mx)
 
 
 def test_clip_and_mask(gpu, oracle_mod):
@@ -124,17 +124,16 @@ def test_clip_and_mask(gpu, oracle_mod):
     t.finalize()
     g, o = _both(t, 300, 300, (1.5, 0, 0, 1.5, 0, 0))
     n, mx = diff_stats(g, o)
-    assert mx <= 1, "%d px differ (max %d)" % (n, mx)
+    assert n == 0, "%d px differ (max %d)" % (n, mx)
 
 
 @pytest.mark.parametrize("index", [0, 1, 2, 3, 5, 8, 13, 21])
 def test_config3_scenes(gpu, oracle_mod, index):
     """Scenes of the batched workload (sizes 64..1024, 10..2000 paths, 10% with
-    clip + blur) rendered one at a time through resvg_render."""
+    clip + blur) rendered one at a time through resvg_render, the largest
+    included."""
     t = R.Tree.generate(3, seed=2026, index=index)
     w, h = (int(v) for v in t.size)
-    if w * h * t.view().contents.path_count > 3e8:
-        pytest.skip("scene too large for a quick oracle render")
     g, o = _both(t, w, h)
     n, mx = diff_stats(g, o)
-    assert mx <= 1, "%d px differ (max %d)" % (n, mx)
+    assert n == 0, "%d px differ (max %d)" % (n, mx)
