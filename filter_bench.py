@@ -1,6 +1,6 @@
 """Device time of each filter primitive on one image, through rgpu_filter_apply.
 
-    python -m resvg_gb300.filter_bench [--size 2048] [--reps 20]
+    python filter_bench.py [--size 2048] [--reps 20]
 
 Every case is one filter whose region is the whole image (identity layer
 transform, sRGB interpolation so no colour-space passes are added) applied to
@@ -17,8 +17,13 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import sys
 
-from . import _abi as A
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+from resvg_gb300 import _abi as A  # noqa: E402
 
 _IN = A.IN_SOURCE_GRAPHIC
 
@@ -70,9 +75,8 @@ def primitive_cases(w, h):
 
 def measured_hbm():
     """(GB/s, label): the measured copy bandwidth when the peaks file is there."""
-    here = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
     try:
-        with open(os.path.join(here, "MEASURED_PEAKS.json")) as fh:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
             d = json.load(fh)
         for k in ("hbm_gbs", "hbm_GBps", "hbm"):
             if k in d and isinstance(d[k], (int, float)):

@@ -65,6 +65,15 @@ int32_t rgpu_tree_add_filter(resvg_render_tree *tree, const rgpu_filter *filter,
 /* Adds a decoded raster image (premultiplied RGBA8, width * height * 4 bytes,
  * copied); returns its index for an RGPU_PAINT_IMAGE paint, or -1. */
 int32_t rgpu_tree_add_image(resvg_render_tree *tree, uint32_t width, uint32_t height, const uint8_t *rgba);
+/* Gives a group (node_kind RGPU_NODE_GROUP) or a path (RGPU_NODE_PATH) its SVG
+ * id, the `id` that usvg keeps on every node (crates/usvg/src/tree/mod.rs,
+ * Node::id) and resvg_render_node looks up.  The string is copied. */
+int rgpu_tree_set_node_id(resvg_render_tree *tree, uint32_t node_kind, uint32_t index, const char *id);
+/* usvg's Tree::node_by_id (crates/usvg/src/tree/mod.rs:1629-1635,1718-1732):
+ * the first node with this id in depth-first pre-order below the root group.
+ * RGPU_OK and (kind, index) when found; RGPU_ERR_INVALID_ARG otherwise (an
+ * empty id never matches). */
+int rgpu_tree_find_node(const resvg_render_tree *tree, const char *id, uint32_t *node_kind, uint32_t *index);
 /* Attaches filters (indices from rgpu_tree_add_filter) to a group. */
 int rgpu_tree_set_group_filters(resvg_render_tree *tree, int32_t group, const uint32_t *filters, uint32_t count);
 /* Computes path and layer bounding boxes; call once after building. */
@@ -79,9 +88,10 @@ resvg_render_tree *rgpu_tree_generate(int config, uint64_t seed, uint64_t index,
 void resvg_render(const resvg_render_tree *tree, resvg_transform transform, uint32_t width, uint32_t height,
                   char *pixmap);
 /* resvg_render_node: crates/c-api/resvg.h:505, lib.rs:908-942 (resvg::render_node,
- * crates/resvg/src/lib.rs:55-70).  The tree keeps no SVG ids: `id` is "<n>" for
- * group n or "p<n>" for path n.  The node's absolute layer bounding box is moved
- * to the pixmap origin; returns false for an unknown id or an empty box. */
+ * crates/resvg/src/lib.rs:55-70).  `id` is an SVG id given with
+ * rgpu_tree_set_node_id, resolved as usvg's node_by_id does
+ * (rgpu_tree_find_node).  The node's absolute layer bounding box is moved to
+ * the pixmap origin; returns false for an empty or unknown id or an empty box. */
 bool resvg_render_node(const resvg_render_tree *tree, const char *id, resvg_transform transform, uint32_t width,
                        uint32_t height, char *pixmap);
 
@@ -90,6 +100,11 @@ bool resvg_render_node(const resvg_render_tree *tree, const char *id, resvg_tran
 int rgpu_init(int device);
 /* Last error message of the calling thread ("" when none). */
 const char *rgpu_last_error(void);
+/* Warnings of the calling thread's last render or filter call ("" when none):
+ * what the reference skips or clears with a log message while rendering goes
+ * on, e.g. a filter that fails clears its layer (crates/resvg/src/filter/
+ * mod.rs:343-354).  A warning is not an error: the call returned RGPU_OK. */
+const char *rgpu_last_warning(void);
 /* Render into a DEVICE pixmap on `stream` (cudaStream_t; 0 = default).  The
  * pixmap is premultiplied RGBA8, `stride` bytes per row; rendering draws onto
  * its content.  Asynchronous: returns after enqueueing.  Counterpart of
@@ -145,6 +160,27 @@ int rgpu_autotune(const resvg_render_tree *const *trees, const resvg_transform *
                   const uint32_t *strides, const rgpu_tuning *candidates, uint32_t candidate_count, uint32_t reps,
                   rgpu_tuning *best, float *best_ms);
 
+/* Failure detection (no counterpart in the reference, whose only limits are
+ * defensive skips: crates/resvg/src/render.rs:108-109, filter/mod.rs:343-354).
+ * The raster kernel's producer/consumer hand-offs wait at most `rounds`
+ * try_wait rounds (0 = the default, 4,194,304, about a second); a wait that
+ * runs out makes the render return RGPU_ERR_DEVICE_FAULT with the pixmap
+ * partly rendered, and the next render starts clean.  Applies to launches made
+ * afterwards (a prepared scene's captured graph keeps the value it was
+ * captured with). */
+int rgpu_set_wait_limit(uint32_t rounds);
+/* Test hooks of the failure paths, for the library's own tests:
+ * rgpu_test_withhold_window(1) makes the first raster CTA withhold its first
+ * window, so that hand-off's bounded wait must run out (no GPU fault is made);
+ * rgpu_test_fail_allocations(n) makes the library's next n device or pinned
+ * host allocations fail as if memory were exhausted (RGPU_ERR_OUT_OF_MEMORY,
+ * the pixmap untouched). */
+int rgpu_test_withhold_window(int enabled);
+int rgpu_test_fail_allocations(uint32_t count);
+/* Frees the library's cached device buffers and pinned staging (they grow to
+ * the largest render seen and are otherwise kept for reuse). */
+int rgpu_trim(void);
+
 /* Per-call statistics of the last render on this thread (for benchmarking). */
 typedef struct rgpu_stats {
     uint64_t draws, edges, crossings_capacity, work_items, kernel_launches;
@@ -156,7 +192,8 @@ int rgpu_get_stats(rgpu_stats *s);
 /* ---- filter kernels on device images (filter module primitives) --------- */
 /* With stream == NULL the call runs on the library's stream and returns when
  * the image is done; with a stream it is enqueued there and returns at once. */
-/* Box blur, 5 passes of (vertical, horizontal) box sums: crates/resvg/src/filter/box_blur.rs:23. */
+/* Box blur, 5 passes of (vertical, horizontal) box sums: crates/resvg/src/filter/box_blur.rs:23.
+ * Standard deviations must be finite, >= 0 and <= 1e8 (RGPU_ERR_INVALID_ARG otherwise). */
 int rgpu_filter_box_blur(uint8_t *device_img, uint32_t width, uint32_t height, double sigma_x, double sigma_y,
                          void *stream);
 /* IIR (recursive Gaussian) blur in f64: crates/resvg/src/filter/iir_blur.rs:47. */
@@ -170,9 +207,12 @@ int rgpu_filter_color_space(uint8_t *device_img, uint32_t width, uint32_t height
 /* A whole filter (region + primitive chain, as rgpu_tree_add_filter takes it)
  * applied in place to a device pixmap that is the filtered layer, under the
  * layer transform `ts`: crates/resvg/src/filter/mod.rs:335-354 (filter::apply).
- * SourceGraphic is the pixmap; the filter region must cover the whole pixmap
- * when a primitive makes a region-sized image (RGPU_ERR_UNSUPPORTED otherwise);
- * an invalid region clears the pixmap, as in the reference. */
+ * SourceGraphic is the pixmap; primitives that make region-sized images
+ * (flood, composite, merge, blend, tile, turbulence, lighting, displacement
+ * map) make them at the pixmap origin, as the reference does.  A filter that
+ * fails (an invalid region, sizes the reference cannot combine) clears the
+ * pixmap and the call still returns RGPU_OK with a warning
+ * (rgpu_last_warning), as filter::apply clears on error. */
 int rgpu_filter_apply(const rgpu_filter *filter, const rgpu_primitive *prims, uint32_t prim_count,
                       const int32_t *merge_inputs, uint32_t merge_count, resvg_transform ts, uint8_t *device_pixmap,
                       uint32_t width, uint32_t height, void *stream);
@@ -186,7 +226,9 @@ int rgpu_filter_apply(const rgpu_filter *filter, const rgpu_primitive *prims, ui
  * images return RGPU_ERR_INVALID_ARG.  The first call on a device does the
  * set-up (looks up the array's address) and should come before any stream
  * capture.  The scratch is shared by all calls on a device: overlapping calls
- * race.  NULL stream = the default stream; returns after the blur finished. */
+ * race.  With a NULL stream the blur runs on the default stream and the call
+ * returns after it finished; with a stream it is enqueued there and the call
+ * returns at once.  Standard deviations must be finite, >= 0 and <= 1e8. */
 int rgpu_filter_box_blur_noalloc(uint8_t *device_img, uint32_t width, uint32_t height, double sigma_x,
                                  double sigma_y, void *stream);
 

@@ -884,6 +884,10 @@ bool filter_apply(const rgpu_tree_view &t, const rgpu_filter &f, const Transform
         case RGPU_FE_DIFFUSE:
         case RGPU_FE_SPECULAR: {
             Image in = get_input(p.in1);
+            // lighting.rs indexes the region-sized result with the input's size
+            // (debug-asserted equal): with a layer-sized input under a smaller
+            // region the reference indexes out of range, so the filter fails
+            if ((int32_t)in.image->width != region.w || (int32_t)in.image->height != region.h) return fail();
             auto pm = std::make_shared<Pixmap>((uint32_t)region.w, (uint32_t)region.h);
             lighting(p.kind == RGPU_FE_SPECULAR, p, ts, region, *in.image, *pm);
             res = Image{pm, IntRect{0, 0, (int32_t)pm->width, (int32_t)pm->height}, lin};
@@ -910,6 +914,12 @@ bool filter_apply(const rgpu_tree_view &t, const rgpu_filter &f, const Transform
         }
         case RGPU_FE_DISPLACEMENT_MAP: {
             Image i1 = into_cs(get_input(p.in1), lin), i2 = into_cs(get_input(p.in2), lin);
+            // displacement_map.rs walks the map with the source's width and
+            // writes the region-sized result at the same index (sizes
+            // debug-asserted equal): any mismatch fails the filter
+            if ((int32_t)i1.image->width != region.w || (int32_t)i1.image->height != region.h ||
+                (int32_t)i2.image->width != region.w || (int32_t)i2.image->height != region.h)
+                return fail();
             auto pm = std::make_shared<Pixmap>((uint32_t)region.w, (uint32_t)region.h);
             float sx, sy;
             ts.get_scale(&sx, &sy);

@@ -47,6 +47,7 @@ def _declare_render(L):
     L.rgpu_init.restype = C.c_int
     L.rgpu_init.argtypes = [C.c_int]
     L.rgpu_last_error.restype = C.c_char_p
+    L.rgpu_last_warning.restype = C.c_char_p
     L.rgpu_render_device.restype = C.c_int
     L.rgpu_render_device.argtypes = [P, _abi.ResvgTransform, C.c_uint32, C.c_uint32, P, C.c_uint32, P]
     L.rgpu_render_batch.restype = C.c_int
@@ -140,6 +141,18 @@ class Tree:
         assert a.ndim == 3 and a.shape[2] == 4
         return lib().rgpu_tree_add_image(self._h, a.shape[1], a.shape[0], a.ctypes.data)
 
+    def set_node_id(self, kind: int, index: int, node_id: str) -> None:
+        """Gives group (kind NODE_GROUP) or path (NODE_PATH) `index` its SVG id."""
+        check(lib().rgpu_tree_set_node_id(self._h, int(kind), int(index), node_id.encode()), "set_node_id")
+
+    def find_node(self, node_id: str):
+        """(kind, index) of the node resvg_render_node renders for this SVG id
+        (usvg's node_by_id: first match in depth-first pre-order), or None."""
+        k, i = C.c_uint32(), C.c_uint32()
+        if lib().rgpu_tree_find_node(self._h, node_id.encode(), C.byref(k), C.byref(i)) != 0:
+            return None
+        return k.value, i.value
+
     def set_group_filters(self, group: int, filters) -> None:
         arr = (C.c_uint32 * max(1, len(filters)))(*filters)
         check(lib().rgpu_tree_set_group_filters(self._h, group, arr, len(filters)), "set_group_filters")
@@ -155,6 +168,13 @@ class Tree:
     def size(self):
         v = self.view().contents
         return v.width, v.height
+
+
+def last_warning() -> str:
+    """Warnings of this thread's last render or filter call: parts the
+    reference skips or clears with a log message (a failing filter clears its
+    layer) while the call itself succeeded."""
+    return lib().rgpu_last_warning().decode(errors="replace")
 
 
 def _rt(transform) -> _abi.ResvgTransform:
@@ -184,12 +204,17 @@ def render(tree: Tree, transform=(1, 0, 0, 1, 0, 0), width: int | None = None, h
 
 
 def node_abs_bbox(tree: Tree, node_id: str):
-    """Absolute layer bounding box (x, y, w, h) of a node, the box resvg's
-    render_node places at the pixmap origin; None for a zero-sized box.
-    Ids: "<n>" is group n, "p<n>" is path n."""
+    """Absolute layer bounding box (x, y, w, h) of the node with this SVG id,
+    the box resvg's render_node places at the pixmap origin; None for an
+    unknown id or a zero-sized box."""
+    node = tree.find_node(node_id)
+    return None if node is None else node_abs_bbox_at(tree, *node)
+
+
+def node_abs_bbox_at(tree: Tree, kind: int, idx: int):
+    """node_abs_bbox for node (kind, index): NODE_GROUP or NODE_PATH."""
     v = tree.view().contents
-    is_path = node_id.startswith("p")
-    idx = int(node_id[1:] if is_path else node_id)
+    is_path = kind == _abi.NODE_PATH
     gp = [-1] * v.group_count
     pp = [-1] * v.path_count
     for g in range(v.group_count):
@@ -237,8 +262,9 @@ def node_abs_bbox(tree: Tree, node_id: str):
 
 def render_node(tree: Tree, node_id: str, transform, width: int, height: int,
                 pixmap: np.ndarray | None = None) -> np.ndarray | None:
-    """resvg_render_node through the C ABI; None when the id is unknown or the
-    node's bounding box is empty."""
+    """resvg_render_node through the C ABI: `node_id` is an SVG id given with
+    Tree.set_node_id; None when the id is unknown or the node's bounding box
+    is empty."""
     if pixmap is None:
         pixmap = np.zeros((int(height), int(width), 4), dtype=np.uint8)
     tree.view()

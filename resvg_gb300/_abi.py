@@ -169,6 +169,10 @@ def declare(lib: C.CDLL) -> C.CDLL:
     lib.rgpu_tree_add_image.argtypes = [P, u32, u32, C.c_void_p]
     lib.rgpu_tree_add_filter.restype = i32
     lib.rgpu_tree_add_filter.argtypes = [P, C.POINTER(Filter), C.POINTER(Primitive), u32, C.POINTER(i32), u32]
+    lib.rgpu_tree_set_node_id.restype = C.c_int
+    lib.rgpu_tree_set_node_id.argtypes = [P, u32, u32, C.c_char_p]
+    lib.rgpu_tree_find_node.restype = C.c_int
+    lib.rgpu_tree_find_node.argtypes = [P, C.c_char_p, C.POINTER(u32), C.POINTER(u32)]
     lib.rgpu_tree_set_group_filters.restype = C.c_int
     lib.rgpu_tree_set_group_filters.argtypes = [P, i32, C.POINTER(u32), u32]
     lib.rgpu_tree_finalize.restype = C.c_int

@@ -60,6 +60,16 @@ int32_t rgpu_tree_add_image(resvg_render_tree *t, uint32_t w, uint32_t h, const 
     return t->add_image(w, h, rgba);
 }
 
+int rgpu_tree_set_node_id(resvg_render_tree *t, uint32_t node_kind, uint32_t index, const char *id) {
+    if (!t || !id) return RGPU_ERR_INVALID_ARG;
+    return t->set_node_id(node_kind, index, id) ? RGPU_OK : RGPU_ERR_INVALID_ARG;
+}
+
+int rgpu_tree_find_node(const resvg_render_tree *t, const char *id, uint32_t *node_kind, uint32_t *index) {
+    if (!t || !id || !node_kind || !index) return RGPU_ERR_INVALID_ARG;
+    return t->node_by_id(id, node_kind, index) ? RGPU_OK : RGPU_ERR_INVALID_ARG;
+}
+
 int rgpu_tree_set_group_filters(resvg_render_tree *t, int32_t group, const uint32_t *filters, uint32_t count) {
     if (!t || group < 0 || group >= (int32_t)t->groups.size()) return RGPU_ERR_INVALID_ARG;
     t->groups[group].filter_offset = (uint32_t)t->filter_refs.size();
@@ -94,6 +104,7 @@ resvg_render_tree *rgpu_tree_generate(int config, uint64_t seed, uint64_t index,
     t->filter_refs = std::move(g->filter_refs); t->filters = std::move(g->filters);
     t->prims = std::move(g->prims); t->merge_inputs = std::move(g->merge_inputs);
     t->images = std::move(g->images); t->image_pixels = std::move(g->image_pixels);
+    t->group_ids = std::move(g->group_ids); t->path_ids = std::move(g->path_ids);
     t->finalized = g->finalized;
     delete g;
     t->get_view();

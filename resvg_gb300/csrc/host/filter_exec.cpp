@@ -121,14 +121,20 @@ bool transfer_lut(const rgpu_primitive &p, uint32_t lut[256], std::string &err) 
     return true;
 }
 
-// A filter image: a layer-sized device buffer, its colour space, and the
-// region the reference's Image carries (only feOffset reads it): the filter
-// region for SourceGraphic / SourceAlpha, the primitive subregion after a
-// crop, else the whole image (w < 0 here).
+// A filter image: a device buffer holding a w x h image (stride w), its colour
+// space, and the region the reference's Image carries (feOffset and feTile read
+// it): the filter region for SourceGraphic / SourceAlpha, the primitive
+// subregion after a crop, else the whole image (reg.w < 0 here).  Images are
+// layer-sized (the inputs and what input-sized primitives make) or
+// region-sized (what flood, composite, merge, blend, tile, turbulence,
+// lighting, displacement map and feImage make), as tiny-skia pixmaps are in
+// the reference; a region-sized image sits at the layer origin.
 struct Img {
     uint32_t *p;
     bool linear;
+    int32_t w, h;
     IRect reg{0, 0, -1, -1};
+    size_t n() const { return (size_t)w * h; }
 };
 
 struct Runner {
@@ -139,16 +145,23 @@ struct Runner {
     uint32_t next = 0;
     cudaError_t e = cudaSuccess;
 
+    // scratch buffers are layer-sized: any image of this job fits
     uint32_t *fresh() { return sc.image(next++, n); }
     void ck(cudaError_t x) { if (e == cudaSuccess) e = x; }
     // a private copy of `in` in colour space `lin`
     Img private_in(Img in, bool lin) {
         uint32_t *o = fresh();
-        ck(filter_copy(in.p, o, n, s));
-        if (in.linear != lin) ck(filter_color_space(o, n, lin, s));
-        return Img{o, lin};
+        ck(filter_copy(in.p, o, in.n(), s));
+        if (in.linear != lin) ck(filter_color_space(o, in.n(), lin, s));
+        return Img{o, lin, in.w, in.h};
     }
     Img in_space(Img in, bool lin) { return in.linear == lin ? in : private_in(in, lin); }
+    // a cleared image of the given size
+    Img blank(int32_t iw, int32_t ih, bool lin) {
+        uint32_t *o = fresh();
+        ck(filter_fill(o, (size_t)iw * ih, 0u, s));
+        return Img{o, lin, iw, ih};
+    }
 };
 
 }  // namespace
@@ -161,6 +174,8 @@ int run_filter_job(const FilterJob &job, uint32_t *content, uint32_t *result, Fi
     uint32_t *source = content;
     for (uint32_t fi = 0; fi < job.filter_count; fi++) {
         const rgpu_filter &f = t.filters[t.filter_refs[job.filter_ref_offset + fi]];
+        // the filter region: filter.rect.transform(ts).to_int_rect() fitted to
+        // the layer (mod.rs:362-373)
         IRect region;
         bool ok = map_int_rect(job.ts, f.x, f.y, f.w, f.h, &region);
         if (ok) {
@@ -169,47 +184,35 @@ int run_filter_job(const FilterJob &job, uint32_t *content, uint32_t *result, Fi
             ok = rr > l && b > tp;
             region = IRect{l, tp, rr - l, b - tp};
         }
-        if (ok && (region.x != 0 || region.y != 0 || region.w != job.w || region.h != job.h)) {
-            // A filter region inside a larger layer (several filters on one
-            // element, whose layer is the union of their regions): primitives
-            // whose result has the input's size work on the whole layer as in
-            // the reference; those that make a region-sized image (flood,
-            // composite, merge, blend, lighting) are not expressed here.
-            for (uint32_t pi = 0; pi < f.prim_count; pi++) {
-                switch (t.prims[f.prim_offset + pi].kind) {
-                case RGPU_FE_BLUR: case RGPU_FE_COLOR_MATRIX: case RGPU_FE_MORPHOLOGY: case RGPU_FE_CONVOLVE:
-                case RGPU_FE_OFFSET: case RGPU_FE_COMPONENT_TRANSFER: case RGPU_FE_DROP_SHADOW:
-                    break;
-                default:
-                    err = "filter region smaller than its layer with a region-sized primitive";
-                    return RGPU_ERR_UNSUPPORTED;
-                }
-            }
-        }
+        // A failure inside the filter (an invalid region or subregion, a tile
+        // outside its input, sizes the reference cannot combine, a primitive
+        // this device build does not run) clears the layer and rendering goes
+        // on, as apply() does (mod.rs:343-354); the reason becomes a warning.
+        std::string why = ok ? "" : "filter has an invalid region";
         std::vector<Img> results;
-        bool failed = !ok;
-        for (uint32_t pi = 0; pi < f.prim_count && !failed; pi++) {
+        auto input = [&](int32_t in) -> Img {
+            if (in >= 0 && (size_t)in < results.size()) return results[in];
+            if (in == RGPU_IN_SOURCE_ALPHA) {
+                // SourceAlpha: RGB set to zero, alpha kept
+                uint32_t *o = r.fresh();
+                r.ck(filter_copy(source, o, r.n, s));
+                r.ck(filter_alpha_only(o, r.n, s));
+                return Img{o, false, job.w, job.h, region};
+            }
+            return Img{source, false, job.w, job.h, region};
+        };
+        for (uint32_t pi = 0; pi < f.prim_count && why.empty(); pi++) {
             const rgpu_primitive &p = t.prims[f.prim_offset + pi];
             IRect sub;
-            if (!map_int_rect(job.ts, p.x, p.y, p.w, p.h, &sub)) { failed = true; break; }
+            if (!map_int_rect(job.ts, p.x, p.y, p.w, p.h, &sub)) { why = "primitive has an invalid subregion"; break; }
             // feOffset inherits its subregion from a referenced input (mod.rs:384-391)
             if (p.kind == RGPU_FE_OFFSET && p.in1 >= 0 && (size_t)p.in1 < results.size()) {
                 sub = results[p.in1].reg;
-                if (sub.w < 0) sub = IRect{0, 0, job.w, job.h};
+                if (sub.w < 0) sub = IRect{0, 0, results[p.in1].w, results[p.in1].h};
             }
             const bool lin = p.linear_rgb != 0;
-            auto input = [&](int32_t in) -> Img {
-                if (in >= 0 && (size_t)in < results.size()) return results[in];
-                if (in == RGPU_IN_SOURCE_ALPHA) {
-                    // SourceAlpha: RGB set to zero, alpha kept
-                    uint32_t *o = r.fresh();
-                    r.ck(filter_copy(source, o, r.n, s));
-                    r.ck(filter_alpha_only(o, r.n, s));
-                    return Img{o, false, region};
-                }
-                return Img{source, false, region};
-            };
-            Img res{nullptr, lin};
+            const int32_t rw = region.w, rh = region.h;
+            Img res{nullptr, lin, 0, 0};
             switch (p.kind) {
             case RGPU_FE_BLUR: {
                 Img in = input(p.in1);
@@ -217,13 +220,13 @@ int run_filter_job(const FilterJob &job, uint32_t *content, uint32_t *result, Fi
                 bool box;
                 if (!resolve_std_dev(job.ts, p.f[0], p.f[1], &x, &y, &box)) { res = in; break; }
                 res = r.private_in(in, lin);
-                if (box) r.ck(filter_box_blur(res.p, r.fresh(), r.w, r.h, x, y, s));
-                else r.ck(filter_iir_blur(res.p, scratch.plane(4 * r.n), r.w, r.h, x, y, s));
+                if (box) r.ck(filter_box_blur(res.p, r.fresh(), res.w, res.h, x, y, s));
+                else r.ck(filter_iir_blur(res.p, scratch.plane(4 * r.n), res.w, res.h, x, y, s));
                 break;
             }
             case RGPU_FE_COLOR_MATRIX: {
                 res = r.private_in(input(p.in1), lin);
-                r.ck(filter_color_matrix(res.p, r.n, p.i[0], p.f, s));
+                r.ck(filter_color_matrix(res.p, res.n(), p.i[0], p.f, s));
                 break;
             }
             case RGPU_FE_MORPHOLOGY: {
@@ -231,16 +234,20 @@ int run_filter_job(const FilterJob &job, uint32_t *content, uint32_t *result, Fi
                 float sx = std::sqrt(job.ts.sx * job.ts.sx + job.ts.kx * job.ts.kx);
                 float sy = std::sqrt(job.ts.ky * job.ts.ky + job.ts.sy * job.ts.sy);
                 float rx = p.f[0] * sx, ry = p.f[1] * sy;
-                if (!(rx > 0.0f && ry > 0.0f)) r.ck(filter_fill(res.p, r.n, 0u, s));
-                else r.ck(filter_morphology(res.p, r.fresh(), r.w, r.h, p.i[0] == 1, rx, ry, s));
+                if (!(rx > 0.0f && ry > 0.0f)) r.ck(filter_fill(res.p, res.n(), 0u, s));
+                else r.ck(filter_morphology(res.p, r.fresh(), res.w, res.h, p.i[0] == 1, rx, ry, s));
                 break;
             }
             case RGPU_FE_COMPOSITE: {
+                // apply_composite (mod.rs:731-793): a region-sized image; the
+                // arithmetic form pairs pixels by index, the others draw both
+                // inputs at the origin
                 Img a = r.in_space(input(p.in1), lin), b = r.in_space(input(p.in2), lin);
-                uint32_t *o = r.fresh();
+                res = r.blank(rw, rh, lin);
                 if (p.i[0] == RGPU_OP_ARITHMETIC) {
                     const float k[4] = {p.f[0], p.f[1], p.f[2], p.f[3]};
-                    r.ck(filter_arithmetic(a.p, b.p, o, r.n, k, s));
+                    if (a.n() < res.n() || b.n() < res.n()) { why = "arithmetic composite of images smaller than the region"; break; }
+                    r.ck(filter_arithmetic(a.p, b.p, res.p, res.n(), k, s));
                 } else {
                     uint32_t bm = RGPU_BLEND_SOURCE_OVER;
                     switch (p.i[0]) {
@@ -250,34 +257,27 @@ int run_filter_job(const FilterJob &job, uint32_t *content, uint32_t *result, Fi
                     case RGPU_OP_XOR: bm = RGPU_BLEND_XOR; break;
                     default: break;
                     }
-                    r.ck(filter_fill(o, r.n, 0u, s));
-                    r.ck(filter_draw(b.p, o, r.w, r.h, 0, 0, RGPU_BLEND_SOURCE_OVER, s));
-                    r.ck(filter_draw(a.p, o, r.w, r.h, 0, 0, bm, s));
+                    r.ck(filter_draw(b.p, b.w, b.h, res.p, rw, rh, 0, 0, RGPU_BLEND_SOURCE_OVER, s));
+                    r.ck(filter_draw(a.p, a.w, a.h, res.p, rw, rh, 0, 0, bm, s));
                 }
-                res = Img{o, lin};
                 break;
             }
             case RGPU_FE_BLEND: {
                 Img a = r.in_space(input(p.in1), lin), b = r.in_space(input(p.in2), lin);
-                uint32_t *o = r.fresh();
-                r.ck(filter_fill(o, r.n, 0u, s));
-                r.ck(filter_draw(b.p, o, r.w, r.h, 0, 0, RGPU_BLEND_SOURCE_OVER, s));
-                r.ck(filter_draw(a.p, o, r.w, r.h, 0, 0, (uint32_t)p.i[0], s));
-                res = Img{o, lin};
+                res = r.blank(rw, rh, lin);
+                r.ck(filter_draw(b.p, b.w, b.h, res.p, rw, rh, 0, 0, RGPU_BLEND_SOURCE_OVER, s));
+                r.ck(filter_draw(a.p, a.w, a.h, res.p, rw, rh, 0, 0, (uint32_t)p.i[0], s));
                 break;
             }
             case RGPU_FE_MERGE: {
-                uint32_t *o = r.fresh();
-                r.ck(filter_fill(o, r.n, 0u, s));
+                res = r.blank(rw, rh, lin);
                 for (int32_t k = 0; k < p.i[1]; k++) {
                     Img in = r.in_space(input(t.merge_inputs[p.i[0] + k]), lin);
-                    r.ck(filter_draw(in.p, o, r.w, r.h, 0, 0, RGPU_BLEND_SOURCE_OVER, s));
+                    r.ck(filter_draw(in.p, in.w, in.h, res.p, rw, rh, 0, 0, RGPU_BLEND_SOURCE_OVER, s));
                 }
-                res = Img{o, lin};
                 break;
             }
             case RGPU_FE_FLOOD: {
-                uint32_t *o = r.fresh();
                 // Pixmap::fill(Color::from_rgba8(r, g, b, opacity.to_u8())): premultiplied
                 float a = (float)(uint8_t)std::min(255.0f, std::max(0.0f, p.f[0] * 255.0f + 0.5f)) / 255.0f;
                 auto pm = [&](int c) {
@@ -287,8 +287,8 @@ int run_filter_job(const FilterJob &job, uint32_t *content, uint32_t *result, Fi
                 };
                 uint32_t a8 = (uint32_t)(uint8_t)std::min(255.0f, a * 255.0f + 0.5f);
                 uint32_t v = pm(p.i[0]) | (pm(p.i[1]) << 8) | (pm(p.i[2]) << 16) | (a8 << 24);
-                r.ck(filter_fill(o, r.n, v, s));
-                res = Img{o, false};
+                res = Img{r.fresh(), false, rw, rh};
+                r.ck(filter_fill(res.p, res.n(), v, s));
                 break;
             }
             case RGPU_FE_OFFSET: {
@@ -297,10 +297,9 @@ int run_filter_job(const FilterJob &job, uint32_t *content, uint32_t *result, Fi
                 float sy = std::sqrt(job.ts.ky * job.ts.ky + job.ts.sy * job.ts.sy);
                 float dx = p.f[0] * sx, dy = p.f[1] * sy;
                 if (approx_zero_ulps(dx) && approx_zero_ulps(dy)) { res = in; break; }
-                uint32_t *o = r.fresh();
-                r.ck(filter_fill(o, r.n, 0u, s));
-                r.ck(filter_draw(in.p, o, r.w, r.h, sat_i32(dx), sat_i32(dy), RGPU_BLEND_SOURCE_OVER, s));
-                res = Img{o, in.linear};
+                res = r.blank(in.w, in.h, in.linear);
+                r.ck(filter_draw(in.p, in.w, in.h, res.p, in.w, in.h, sat_i32(dx), sat_i32(dy), RGPU_BLEND_SOURCE_OVER,
+                                 s));
                 break;
             }
             case RGPU_FE_CONVOLVE: {
@@ -311,20 +310,22 @@ int run_filter_job(const FilterJob &job, uint32_t *content, uint32_t *result, Fi
                 cp.edge = p.i[4]; cp.preserve_alpha = p.i[5];
                 cp.divisor = p.f[0]; cp.bias = p.f[1];
                 if (cp.cols <= 0 || cp.rows <= 0 || cp.cols * cp.rows > (int)(sizeof(cp.k) / sizeof(float))) {
-                    err = "convolve kernel larger than the primitive record";
-                    return RGPU_ERR_UNSUPPORTED;
+                    why = "convolve kernel larger than the primitive record";
+                    break;
                 }
                 for (int k = 0; k < cp.cols * cp.rows; k++) cp.k[k] = p.f[2 + k];
-                uint32_t *o = r.fresh();
-                r.ck(filter_convolve(in.p, o, r.w, r.h, cp, s));
-                res = Img{o, lin};
+                res = Img{r.fresh(), lin, in.w, in.h};
+                r.ck(filter_convolve(in.p, res.p, in.w, in.h, cp, s));
                 break;
             }
             case RGPU_FE_DIFFUSE:
             case RGPU_FE_SPECULAR: {
                 // apply_diffuse_lighting / apply_specular_lighting + transform_light_source
-                // (mod.rs:1020-1098); the region is the whole layer here
+                // (mod.rs:1020-1098): a region-sized result computed over the
+                // input's pixels; lighting.rs indexes both with the input's
+                // size, which only holds when the input is region-sized too
                 Img in = input(p.in1);
+                if (in.w != rw || in.h != rh) { why = "lighting input and filter region differ in size"; break; }
                 LightingParams lp{};
                 lp.specular = p.kind == RGPU_FE_SPECULAR;
                 lp.kind = p.i[0];
@@ -361,59 +362,58 @@ int run_filter_job(const FilterJob &job, uint32_t *content, uint32_t *result, Fi
                         lp.cone_cos = lp.has_cone ? std::cos(p.f[11] * d2r) : 0.0f;
                     }
                 }
-                uint32_t *o = r.fresh();
-                r.ck(filter_lighting(in.p, o, r.w, r.h, lp, s));
-                res = Img{o, lin};
+                res = r.blank(rw, rh, lin);
+                r.ck(filter_lighting(in.p, res.p, rw, rh, lp, s));
                 break;
             }
             case RGPU_FE_IMAGE: {
                 // apply_image (mod.rs:861-889): the element was rendered into a
-                // surface of its own before the job; an sRGB image
+                // layer-sized surface of its own before the job; the result is
+                // its region-sized corner, in sRGB
                 const uint32_t *src = nullptr;
                 if (images)
                     for (const auto &im : *images)
                         if (im.prim == f.prim_offset + pi) src = im.p;
-                if (!src) {
-                    err = "feImage without its rendered element";
-                    return RGPU_ERR_UNSUPPORTED;
-                }
-                uint32_t *o = r.fresh();
-                r.ck(filter_copy(src, o, r.n, s));
-                res = Img{o, false};
+                if (!src) { why = "feImage without its rendered element"; break; }
+                res = r.blank(rw, rh, false);
+                if (rw == job.w && rh == job.h) r.ck(filter_copy(src, res.p, res.n(), s));
+                else r.ck(filter_draw(src, job.w, job.h, res.p, rw, rh, 0, 0, RGPU_BLEND_SOURCE, s));
                 break;
             }
             case RGPU_FE_TILE: {
-                // apply_tile (mod.rs:835-859)
+                // apply_tile (mod.rs:835-859): the input's region, cut from its
+                // image, repeated over a region-sized image
                 Img in = input(p.in1);
-                IRect ir = in.reg.w < 0 ? IRect{0, 0, job.w, job.h} : in.reg;
+                IRect ir = in.reg.w < 0 ? IRect{0, 0, in.w, in.h} : in.reg;
                 const int32_t sx0 = ir.x - region.x, sy0 = ir.y - region.y;
                 const int32_t l = std::max(sx0, 0), tp = std::max(sy0, 0);
-                const int32_t rr = std::min(sx0 + ir.w, r.w), bb = std::min(sy0 + ir.h, r.h);
-                if (rr <= l || bb <= tp) { failed = true; break; }
-                uint32_t *o = r.fresh();
-                r.ck(filter_tile(in.p, o, r.w, r.h, sx0, sy0, l, tp, rr - l, bb - tp, s));
-                res = Img{o, false};
+                const int32_t rr = std::min(sx0 + ir.w, in.w), bb = std::min(sy0 + ir.h, in.h);
+                if (rr <= l || bb <= tp) { why = "feTile input region outside its image"; break; }
+                res = Img{r.fresh(), false, rw, rh};
+                r.ck(filter_tile(in.p, in.w, in.h, res.p, rw, rh, sx0, sy0, l, tp, rr - l, bb - tp, s));
                 break;
             }
             case RGPU_FE_DISPLACEMENT_MAP: {
-                // apply_displacement_map (mod.rs:958-986)
+                // apply_displacement_map (mod.rs:958-986): displacement_map.rs
+                // walks the map with the source's width and writes the
+                // region-sized result at the same index, which only holds when
+                // all three are the same size
                 Img a = r.in_space(input(p.in1), lin), b = r.in_space(input(p.in2), lin);
+                if (a.w != rw || a.h != rh || b.w != rw || b.h != rh) {
+                    why = "displacement map inputs and filter region differ in size";
+                    break;
+                }
                 const float sx = std::sqrt(job.ts.sx * job.ts.sx + job.ts.kx * job.ts.kx);
                 const float sy = std::sqrt(job.ts.ky * job.ts.ky + job.ts.sy * job.ts.sy);
-                uint32_t *o = r.fresh();
-                r.ck(filter_displacement_map(a.p, b.p, o, r.w, r.h, p.f[0] * sx, p.f[0] * sy, p.f[0], p.i[0], p.i[1],
+                res = Img{r.fresh(), lin, rw, rh};
+                r.ck(filter_displacement_map(a.p, b.p, res.p, rw, rh, p.f[0] * sx, p.f[0] * sy, p.f[0], p.i[0], p.i[1],
                                              s));
-                res = Img{o, lin};
                 break;
             }
             case RGPU_FE_TURBULENCE: {
-                // apply_turbulence (mod.rs:988-1018)
-                if (p.i[0] > RGPU_TURB_MAX_OCTAVES) {
-                    err = "feTurbulence numOctaves above the device limit";
-                    return RGPU_ERR_UNSUPPORTED;
-                }
-                uint32_t *o = r.fresh();
-                r.ck(filter_fill(o, r.n, 0u, s));
+                // apply_turbulence (mod.rs:988-1018): a region-sized image
+                if (p.i[0] > RGPU_TURB_MAX_OCTAVES) { why = "feTurbulence numOctaves above the device limit"; break; }
+                res = r.blank(rw, rh, lin);
                 const float sx = std::sqrt(job.ts.sx * job.ts.sx + job.ts.kx * job.ts.kx);
                 const float sy = std::sqrt(job.ts.ky * job.ts.ky + job.ts.sy * job.ts.sy);
                 if (!approx_zero_ulps(sx) && !approx_zero_ulps(sy)) {
@@ -430,21 +430,20 @@ int run_filter_job(const FilterJob &job, uint32_t *content, uint32_t *result, Fi
                     tp.bfx = p.f[0]; tp.bfy = p.f[1];
                     tp.octaves = p.i[0]; tp.stitch = p.i[2] != 0; tp.fractal = p.i[3] != 0;
                     tp.seed0 = (uint32_t)(((int64_t)seed % m + m) % m);
-                    r.ck(filter_turbulence(o, r.w, r.h, tp, s));
+                    r.ck(filter_turbulence(res.p, rw, rh, tp, s));
                 }
-                res = Img{o, lin};
                 break;
             }
             case RGPU_FE_COMPONENT_TRANSFER: {
                 // apply_component_transfer (mod.rs:891-903)
                 uint32_t lut[256];
-                if (!transfer_lut(p, lut, err)) return RGPU_ERR_UNSUPPORTED;
+                if (!transfer_lut(p, lut, why)) break;
                 res = r.private_in(input(p.in1), lin);
-                r.ck(filter_component_transfer(res.p, r.n, lut, s));
+                r.ck(filter_component_transfer(res.p, res.n(), lut, s));
                 break;
             }
             case RGPU_FE_DROP_SHADOW: {
-                // apply_drop_shadow (mod.rs:581-649)
+                // apply_drop_shadow (mod.rs:581-649): an input-sized image
                 Img in = r.in_space(input(p.in1), lin);
                 const float sx = std::sqrt(job.ts.sx * job.ts.sx + job.ts.kx * job.ts.kx);
                 const float sy = std::sqrt(job.ts.ky * job.ts.ky + job.ts.sy * job.ts.sy);
@@ -453,44 +452,57 @@ int run_filter_job(const FilterJob &job, uint32_t *content, uint32_t *result, Fi
                 float x, y;
                 bool box;
                 if (resolve_std_dev(job.ts, p.f[0], p.f[1], &x, &y, &box)) {
-                    if (box) r.ck(filter_box_blur(sh.p, r.fresh(), r.w, r.h, x, y, s));
-                    else r.ck(filter_iir_blur(sh.p, scratch.plane(4 * r.n), r.w, r.h, x, y, s));
+                    if (box) r.ck(filter_box_blur(sh.p, r.fresh(), sh.w, sh.h, x, y, s));
+                    else r.ck(filter_iir_blur(sh.p, scratch.plane(4 * r.n), sh.w, sh.h, x, y, s));
                 }
                 const uint32_t op8 = sat_u8(p.f[4] * 255.0f + 0.5f);
                 const uint32_t flood = (uint32_t)(uint8_t)p.i[0] | ((uint32_t)(uint8_t)p.i[1] << 8) |
                                        ((uint32_t)(uint8_t)p.i[2] << 16) | (op8 << 24);
-                uint32_t *o = r.fresh();
-                r.ck(filter_drop_shadow(in.p, sh.p, o, r.w, r.h, sat_i32(dx), sat_i32(dy), flood, lin, s));
-                res = Img{o, lin};
+                res = Img{r.fresh(), lin, in.w, in.h};
+                r.ck(filter_drop_shadow(in.p, sh.p, res.p, in.w, in.h, sat_i32(dx), sat_i32(dy), flood, lin, s));
                 break;
             }
             default:
-                err = "filter primitive not supported on the device";
-                return RGPU_ERR_UNSUPPORTED;
+                why = "filter primitive not supported on the device";
+                break;
             }
-            if (failed) break;
+            if (!why.empty()) break;
             if (sub.x != region.x || sub.y != region.y || sub.w != region.w || sub.h != region.h) {
-                uint32_t *o = r.fresh();
-                r.ck(filter_copy(res.p, o, r.n, s));
+                // clip the result by clearing outside the subregion, in the
+                // result's own pixel space (mod.rs:457-508)
+                Img o{r.fresh(), res.linear, res.w, res.h, sub};
+                r.ck(filter_copy(res.p, o.p, res.n(), s));
                 if (p.kind == RGPU_FE_OFFSET) {
                     // feOffset is cropped to the region's size at the origin
-                    r.ck(filter_crop(o, r.w, r.h, 0, 0, region.w, region.h, s));
+                    r.ck(filter_crop(o.p, o.w, o.h, 0, 0, region.w, region.h, s));
                 } else {
                     int32_t l = sub.x - region.x, tp = sub.y - region.y;
-                    r.ck(filter_crop(o, r.w, r.h, l, tp, l + sub.w, tp + sub.h, s));
+                    r.ck(filter_crop(o.p, o.w, o.h, l, tp, l + sub.w, tp + sub.h, s));
                 }
-                res = Img{o, res.linear, sub};
+                res = o;
             }
             results.push_back(res);
         }
-        if (results.empty()) failed = true;
+        if (why.empty() && results.empty()) why = "filter has no primitives";  // Error::NoResults
         uint32_t *dst = (fi + 1 == job.filter_count) ? result : r.fresh();
-        if (failed) {
+        if (!why.empty()) {
+            if (why != "filter has no primitives") {
+                if (!err.empty()) err += "; ";
+                err += why;
+            }
             r.ck(filter_fill(dst, r.n, 0u, s));
         } else {
+            // apply_to_canvas (mod.rs:1100-1114): back to sRGB, the layer
+            // cleared, the result drawn at the origin
             Img last = results.back();
-            r.ck(filter_copy(last.p, dst, r.n, s));
-            if (last.linear) r.ck(filter_color_space(dst, r.n, false, s));
+            if (last.w == job.w && last.h == job.h) {
+                r.ck(filter_copy(last.p, dst, r.n, s));
+                if (last.linear) r.ck(filter_color_space(dst, r.n, false, s));
+            } else {
+                Img srgb = last.linear ? r.private_in(last, false) : last;
+                r.ck(filter_fill(dst, r.n, 0u, s));
+                r.ck(filter_draw(srgb.p, srgb.w, srgb.h, dst, job.w, job.h, 0, 0, RGPU_BLEND_SOURCE_OVER, s));
+            }
         }
         source = dst;
     }

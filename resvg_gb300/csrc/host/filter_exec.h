@@ -18,7 +18,11 @@ struct FilterScratch {
 };
 
 // Applies the job's filters to `content` (w x h, premultiplied sRGB) and
-// writes the filtered layer to `result`.  Returns 0 or an rgpu_status.
+// writes the filtered layer to `result`.  Returns 0 or an rgpu_status (a CUDA
+// error).  A filter that fails for reasons of its own (an invalid region, sizes
+// the reference cannot combine, a primitive the device does not run) leaves a
+// cleared layer, as resvg's filter::apply does, and rendering goes on: the job
+// still returns 0 and the reasons are appended to `err` as warnings.
 // `images` holds, for each feImage primitive (global index), the surface its
 // element was rendered into; NULL when there are none.
 struct FeImageSurface { uint32_t prim; const uint32_t *p; };

@@ -8,8 +8,10 @@
 #include "flatten.h"
 #include "hairline.h"
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
+#include <thread>
 
 namespace rgpu {
 namespace {
@@ -716,13 +718,131 @@ uint32_t SceneBuild::append_stream(StreamBuild &b) {
     return si;
 }
 
+void SceneBuild::merge(std::vector<SceneBuild> &parts, unsigned threads) {
+    // Every index a part's records hold into another array moves by where
+    // that array's part starts; the result equals flattening the parts' trees
+    // one after another into one build.  Arrays are sized first, then each part
+    // is copied into its ranges with the index fix-ups, parts in parallel.
+    struct Off {
+        size_t verbs, pts, draws, paints, grads, layers, cmds, streams, surfaces, jobs, fe, patterns, hairs, hspans;
+        uint64_t nsegs, ntpts;
+    };
+    const size_t n = parts.size();
+    std::vector<Off> off(n + 1);
+    Off cur{verbs.size(), pts.size(), draws.size(), paints.size(), grads.size(), layers.size(), cmds.size(),
+            streams.size(), surfaces.size(), jobs.size(), fe_images.size(), patterns.size(), hairs.size(),
+            hair_spans.size(), nsegs, ntpts};
+    for (size_t k = 0; k < n; k++) {
+        const SceneBuild &o = parts[k];
+        off[k] = cur;
+        cur.verbs += o.verbs.size(); cur.pts += o.pts.size(); cur.draws += o.draws.size();
+        cur.paints += o.paints.size(); cur.grads += o.grads.size(); cur.layers += o.layers.size();
+        cur.cmds += o.cmds.size(); cur.streams += o.streams.size(); cur.surfaces += o.surfaces.size();
+        cur.jobs += o.jobs.size(); cur.fe += o.fe_images.size(); cur.patterns += o.patterns.size();
+        cur.hairs += o.hairs.size(); cur.hspans += o.hair_spans.size();
+        cur.nsegs += o.nsegs; cur.ntpts += o.ntpts;
+        max_level = std::max(max_level, o.max_level);
+    }
+    off[n] = cur;
+    verbs.resize(cur.verbs); pts.resize(cur.pts); draws.resize(cur.draws); paints.resize(cur.paints);
+    grads.resize(cur.grads); layers.resize(cur.layers); cmds.resize(cur.cmds); streams.resize(cur.streams);
+    surfaces.resize(cur.surfaces); jobs.resize(cur.jobs); fe_images.resize(cur.fe); patterns.resize(cur.patterns);
+    hairs.resize(cur.hairs); hair_spans.resize(cur.hspans);
+    nsegs = cur.nsegs;
+    ntpts = cur.ntpts;
+    auto copy_part = [&](size_t k) {
+        const SceneBuild &o = parts[k];
+        const Off &b = off[k];
+        const uint32_t V = (uint32_t)b.verbs, P = (uint32_t)(b.pts / 2), D = (uint32_t)b.draws;
+        const uint32_t PA = (uint32_t)b.paints, G = (uint32_t)b.grads, L = (uint32_t)b.layers, C = (uint32_t)b.cmds;
+        const uint32_t S = (uint32_t)b.streams, SU = (uint32_t)b.surfaces, FE = (uint32_t)b.fe;
+        const uint32_t H = (uint32_t)b.hairs, HS = (uint32_t)b.hspans;
+        std::copy(o.verbs.begin(), o.verbs.end(), verbs.begin() + b.verbs);
+        std::copy(o.pts.begin(), o.pts.end(), pts.begin() + b.pts);
+        for (size_t i = 0; i < o.draws.size(); i++) {
+            DrawRec d = o.draws[i];
+            d.verb_off += V;
+            d.pt_off += P;
+            d.paint += PA;
+            d.seg_base += (uint32_t)b.nsegs;
+            d.tpt_base += (uint32_t)b.ntpts;
+            d.stream += S;
+            draws[b.draws + i] = d;
+        }
+        for (size_t i = 0; i < o.paints.size(); i++) {
+            PaintRec q = o.paints[i];
+            if (q.kind != 0) q.grad += G;
+            paints[b.paints + i] = q;
+        }
+        std::copy(o.grads.begin(), o.grads.end(), grads.begin() + b.grads);
+        for (size_t i = 0; i < o.layers.size(); i++) {
+            LayerRec l = o.layers[i];
+            if (l.surf >= 0) l.surf += (int32_t)SU;
+            layers[b.layers + i] = l;
+        }
+        for (size_t i = 0; i < o.cmds.size(); i++) {
+            Cmd c = o.cmds[i];
+            if (c.op == CMD_FILL || c.op == CMD_APPLY_REGION) c.a += D;
+            else if (c.op == CMD_HAIR) c.a += H;
+            cmds[b.cmds + i] = c;
+        }
+        for (size_t i = 0; i < o.streams.size(); i++) {
+            StreamRec st = o.streams[i];
+            st.cmd_off += C;
+            st.draw_off += D;
+            st.layer_off += L;
+            if (st.surface >= 0) st.surface += (int32_t)SU;
+            streams[b.streams + i] = st;
+        }
+        std::copy(o.surfaces.begin(), o.surfaces.end(), surfaces.begin() + b.surfaces);
+        for (size_t i = 0; i < o.jobs.size(); i++) {
+            FilterJob j = o.jobs[i];
+            j.content += SU;
+            j.result += SU;
+            j.image_first += FE;
+            jobs[b.jobs + i] = j;
+        }
+        for (size_t i = 0; i < o.fe_images.size(); i++) {
+            FeImageReq f = o.fe_images[i];
+            f.surface += SU;
+            fe_images[b.fe + i] = f;
+        }
+        for (size_t i = 0; i < o.patterns.size(); i++) {
+            PatternReq q = o.patterns[i];
+            q.grad += G;
+            q.tile += SU;
+            q.shade += SU;
+            patterns[b.patterns + i] = q;
+        }
+        for (size_t i = 0; i < o.hairs.size(); i++) {
+            HairRec h = o.hairs[i];
+            h.span_off += HS;
+            h.paint += PA;
+            hairs[b.hairs + i] = h;
+        }
+        std::copy(o.hair_spans.begin(), o.hair_spans.end(), hair_spans.begin() + b.hspans);
+    };
+    std::atomic<size_t> next{0};
+    auto work = [&]() {
+        for (;;) {
+            const size_t k = next.fetch_add(1);
+            if (k >= n) return;
+            copy_part(k);
+        }
+    };
+    std::vector<std::thread> pool;
+    for (unsigned t = 1; t < std::max(1u, threads) && t < n; t++) pool.emplace_back(work);
+    work();
+    for (auto &t : pool) t.join();
+}
+
 int SceneBuild::add_tree(Tree &tree, const Xf &ts, int32_t w, int32_t h, uint64_t out_ptr, uint32_t stride) {
     return add_node(tree, RGPU_NODE_GROUP, UINT32_MAX, ts, w, h, out_ptr, stride);
 }
 
 int SceneBuild::add_node(Tree &tree, uint32_t node_kind, uint32_t node_index, const Xf &ts, int32_t w, int32_t h,
                          uint64_t out_ptr, uint32_t stride) {
-    const rgpu_tree_view &t = *tree.get_view();
+    const rgpu_tree_view &t = tree.finalized ? tree.view : *tree.get_view();
     Flattener f{*this, tree, t, (uint32_t)verbs.size(), (uint32_t)(pts.size() / 2)};
     verbs.insert(verbs.end(), t.verbs, t.verbs + t.verb_count);
     pts.insert(pts.end(), t.points, t.points + 2 * (size_t)t.point_count);

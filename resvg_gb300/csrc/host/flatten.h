@@ -98,6 +98,10 @@ struct SceneBuild {
                  uint64_t out_ptr, uint32_t stride);
     // internal: concatenates a finished stream
     uint32_t append_stream(StreamBuild &sbd);
+    // Appends other builds in order (their trees after this one's), moving
+    // every index their records hold, on up to `threads` host threads; lets
+    // trees be flattened on separate threads.
+    void merge(std::vector<SceneBuild> &parts, unsigned threads);
 };
 
 }  // namespace rgpu

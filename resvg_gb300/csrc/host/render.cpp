@@ -8,12 +8,14 @@
 // usable device the call fails with RGPU_ERR_NO_DEVICE.
 #include <cuda_runtime.h>
 #include <algorithm>
+#include <atomic>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 #include "../kernels/kernels.h"
 #include "filter_exec.h"
@@ -27,7 +29,17 @@ namespace rgpu {
 namespace {
 
 thread_local std::string g_last_error;
+thread_local std::string g_last_warning;
 thread_local rgpu_stats g_stats{};
+
+// Warnings of the current call: parts of the tree that the reference skips or
+// clears with a log message (a failing filter clears its layer,
+// crates/resvg/src/filter/mod.rs:343-354) while the render goes on.
+void add_warning(const std::string &w) {
+    if (w.empty()) return;
+    if (!g_last_warning.empty()) g_last_warning += "; ";
+    g_last_warning += w;
+}
 
 void set_error(const char *fmt, ...) {
     char buf[512];
@@ -36,6 +48,15 @@ void set_error(const char *fmt, ...) {
     vsnprintf(buf, sizeof(buf), fmt, ap);
     va_end(ap);
     g_last_error = buf;
+}
+
+// Failure-detection test hook: the next this-many device or pinned host
+// allocations of the library fail as if memory were exhausted.
+std::atomic<uint32_t> g_fail_allocs{0};
+bool forced_alloc_failure() {
+    uint32_t n = g_fail_allocs.load();
+    while (n && !g_fail_allocs.compare_exchange_weak(n, n - 1)) {}
+    return n != 0;
 }
 
 struct DevBuf {
@@ -48,11 +69,17 @@ struct DevBuf {
         cap = 0;
         size_t want = std::max(bytes, (size_t)4096);
         want = want + want / 4;
+        if (forced_alloc_failure()) return cudaErrorMemoryAllocation;
         cudaError_t e = cudaMalloc(&p, want);
         if (e == cudaSuccess) cap = want;
         return e;
     }
     template <class T> T *as() const { return (T *)p; }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
 };
 
 struct HostBuf {
@@ -64,9 +91,15 @@ struct HostBuf {
         p = nullptr;
         cap = 0;
         size_t want = std::max(bytes, (size_t)4096) * 5 / 4;
+        if (forced_alloc_failure()) return cudaErrorMemoryAllocation;
         cudaError_t e = cudaMallocHost(&p, want);
         if (e == cudaSuccess) cap = want;
         return e;
+    }
+    void release() {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        cap = 0;
     }
 };
 
@@ -87,13 +120,9 @@ struct Buffers {
         DevBuf *all[] = {&verbs, &pts, &draws, &paints, &grads, &layers, &cmds, &streams, &items, &tpts, &segs,
                          &seg_counts, &seg_offsets, &scan_scratch, &totals, &edges, &edge_draw, &bin_counts,
                          &bin_offsets, &bins, &stack, &span_ovf, &run_ovf, &err, &counter, &fill_cmds, &plane, &hairs, &hair_spans};
-        for (DevBuf *b : all) {
-            if (b->p) cudaFree(b->p);
-            b->p = nullptr;
-            b->cap = 0;
-        }
-        for (auto &b : surf) if (b.p) cudaFree(b.p);
-        for (auto &b : img) if (b.p) cudaFree(b.p);
+        for (DevBuf *b : all) b->release();
+        for (auto &b : surf) b.release();
+        for (auto &b : img) b.release();
         surf.clear();
         img.clear();
     }
@@ -432,6 +461,7 @@ int enqueue_plan(Context &c, Buffers &b, Plan &p, cudaStream_t s, RasterTimer *t
                                    s, ferr, &ims);
             if (scratch.e != cudaSuccess) CK(scratch.e);
             if (r) { set_error("filter: %s", ferr.c_str()); return r; }
+            if (!ferr.empty()) add_warning("filter: " + ferr + " (layer cleared)");
         }
     }
     g_stats.draws += ndraws;
@@ -464,6 +494,7 @@ int check_err(Buffers &b, cudaStream_t s, RasterTimer *tm) {
 int render_host(const rgpu_tree *tree, const resvg_transform &ts, uint32_t w, uint32_t h, char *pixmap,
                 int node_kind = -1, uint32_t node_index = 0) {
     g_last_error.clear();
+    g_last_warning.clear();
     std::memset(&g_stats, 0, sizeof(g_stats));
     if (!tree || !pixmap || w == 0 || h == 0 || w > 32767 || h > 32767) {
         set_error("invalid arguments");
@@ -527,6 +558,7 @@ int rgpu_init(int device) {
 }
 
 const char *rgpu_last_error(void) { return g_last_error.c_str(); }
+const char *rgpu_last_warning(void) { return g_last_warning.c_str(); }
 
 void resvg_render(const resvg_render_tree *tree, resvg_transform transform, uint32_t width, uint32_t height,
                   char *pixmap) {
@@ -546,15 +578,13 @@ bool resvg_render_node(const resvg_render_tree *tree, const char *id, resvg_tran
     rgpu_tree *tr = const_cast<rgpu_tree *>(tree);
     if (!tr->finalized) tr->finalize();
     const rgpu_tree_view &t = *tr->get_view();
-    // ids: "<n>" is group n, "p<n>" is path n (the tree keeps no SVG ids)
-    const bool is_path = id[0] == 'p';
-    char *end = nullptr;
-    const unsigned long idx = std::strtoul(id + (is_path ? 1 : 0), &end, 10);
-    if (!end || *end || end == id + (is_path ? 1 : 0) ||
-        idx >= (is_path ? (unsigned long)t.path_count : (unsigned long)t.group_count)) {
+    // tree.node_by_id(id) (crates/c-api/lib.rs:931)
+    uint32_t kind = 0, idx = 0;
+    if (!tr->node_by_id(id, &kind, &idx)) {
         set_error("resvg_render_node: no node with id '%s'", id);
         return false;
     }
+    const bool is_path = kind == RGPU_NODE_PATH;
     // parents, then the absolute transform (parent_abs.pre_concat(own))
     std::vector<int32_t> group_parent(t.group_count, -1), path_parent(t.path_count, -1);
     for (uint32_t g = 0; g < t.group_count; g++)
@@ -609,6 +639,9 @@ struct rgpu_scene {
     }
 };
 
+// Flattens a batch of trees into one SceneBuild.  Trees are flattened (and
+// their strokes outlined) on host threads, in contiguous chunks that are then
+// appended in order, so the records equal a one-thread flatten of the batch.
 static int build_batch(Plan &p, const resvg_render_tree *const *trees, const resvg_transform *transforms,
                        uint32_t count, const uint32_t *widths, const uint32_t *heights, uint8_t *const *ptrs,
                        const uint32_t *strides) {
@@ -620,14 +653,55 @@ static int build_batch(Plan &p, const resvg_render_tree *const *trees, const res
         }
         uint32_t stride = strides ? strides[i] : widths[i] * 4;
         if (stride < widths[i] * 4) { set_error("invalid stride for entry %u", i); return RGPU_ERR_INVALID_ARG; }
+        // finalised here, on one thread: the flatten threads only read trees
         if (!tr->finalized) tr->finalize();
-        const resvg_transform &ts = transforms[i];
-        if (p.sb.add_tree(*tr, Xf::row(ts.a, ts.b, ts.c, ts.d, ts.e, ts.f), (int32_t)widths[i], (int32_t)heights[i],
-                          (uint64_t)(uintptr_t)ptrs[i], stride) < 0) {
-            set_error("entry %u: %s", i, p.sb.error.c_str());
+    }
+    auto flatten_range = [&](SceneBuild &sb, uint32_t a, uint32_t b, uint32_t *failed) {
+        for (uint32_t i = a; i < b; i++) {
+            rgpu_tree *tr = const_cast<rgpu_tree *>(trees[i]);
+            const resvg_transform &ts = transforms[i];
+            const uint32_t stride = strides ? strides[i] : widths[i] * 4;
+            if (sb.add_tree(*tr, Xf::row(ts.a, ts.b, ts.c, ts.d, ts.e, ts.f), (int32_t)widths[i], (int32_t)heights[i],
+                            (uint64_t)(uintptr_t)ptrs[i], stride) < 0) {
+                *failed = i;
+                return false;
+            }
+        }
+        return true;
+    };
+    const uint32_t hw = std::max(1u, std::thread::hardware_concurrency());
+    const uint32_t nthreads = std::min<uint32_t>(hw, 64);
+    if (count < 16 || nthreads == 1) {
+        uint32_t failed = 0;
+        if (!flatten_range(p.sb, 0, count, &failed)) {
+            set_error("entry %u: %s", failed, p.sb.error.c_str());
             return RGPU_ERR_UNSUPPORTED;
         }
+        return RGPU_OK;
     }
+    const uint32_t nchunks = std::min<uint32_t>(count, 8 * nthreads);
+    std::vector<SceneBuild> parts(nchunks);
+    std::vector<uint32_t> fail_at(nchunks, UINT32_MAX);
+    std::atomic<uint32_t> next{0};
+    auto work = [&]() {
+        for (;;) {
+            const uint32_t c = next.fetch_add(1);
+            if (c >= nchunks) return;
+            const uint32_t a = (uint32_t)((uint64_t)count * c / nchunks), b = (uint32_t)((uint64_t)count * (c + 1) / nchunks);
+            uint32_t failed = 0;
+            if (!flatten_range(parts[c], a, b, &failed)) fail_at[c] = failed;
+        }
+    };
+    std::vector<std::thread> pool;
+    for (uint32_t k = 1; k < std::min(nthreads, nchunks); k++) pool.emplace_back(work);
+    work();
+    for (auto &t : pool) t.join();
+    for (uint32_t c = 0; c < nchunks; c++)
+        if (fail_at[c] != UINT32_MAX) {
+            set_error("entry %u: %s", fail_at[c], parts[c].error.c_str());
+            return RGPU_ERR_UNSUPPORTED;
+        }
+    p.sb.merge(parts, nthreads);
     return RGPU_OK;
 }
 
@@ -636,6 +710,7 @@ extern "C" {
 int rgpu_render_device(const resvg_render_tree *tree, resvg_transform ts, uint32_t w, uint32_t h,
                        uint8_t *device_pixmap, uint32_t stride, void *stream) {
     g_last_error.clear();
+    g_last_warning.clear();
     std::memset(&g_stats, 0, sizeof(g_stats));
     if (!tree || !device_pixmap || w == 0 || h == 0 || stride < w * 4) {
         set_error("invalid arguments");
@@ -657,6 +732,7 @@ int rgpu_render_device(const resvg_render_tree *tree, resvg_transform ts, uint32
 int rgpu_render_batch(const resvg_render_tree *const *trees, const resvg_transform *transforms, uint32_t count,
                       const uint32_t *widths, const uint32_t *heights, uint8_t *const *device_pixmaps, void *stream) {
     g_last_error.clear();
+    g_last_warning.clear();
     std::memset(&g_stats, 0, sizeof(g_stats));
     if (!trees || !transforms || !widths || !heights || !device_pixmaps) {
         set_error("invalid arguments");
@@ -707,6 +783,7 @@ int rgpu_scene_prepare(const resvg_render_tree *const *trees, const resvg_transf
 
 int rgpu_scene_render(rgpu_scene *sc, void *stream) {
     g_last_error.clear();
+    g_last_warning.clear();
     if (!sc) { set_error("invalid arguments"); return RGPU_ERR_INVALID_ARG; }
     Context &c = ctx();
     std::lock_guard<std::mutex> lock(c.mu);
@@ -866,6 +943,36 @@ int rgpu_autotune(const resvg_render_tree *const *trees, const resvg_transform *
     return RGPU_OK;
 }
 
+int rgpu_set_wait_limit(uint32_t rounds) {
+    Context &c = ctx();
+    std::lock_guard<std::mutex> lock(c.mu);
+    raster_set_wait_limit(rounds);
+    return RGPU_OK;
+}
+
+int rgpu_test_withhold_window(int enabled) {
+    Context &c = ctx();
+    std::lock_guard<std::mutex> lock(c.mu);
+    raster_set_withhold(enabled != 0);
+    return RGPU_OK;
+}
+
+int rgpu_test_fail_allocations(uint32_t count) {
+    g_fail_allocs.store(count);
+    return RGPU_OK;
+}
+
+int rgpu_trim(void) {
+    Context &c = ctx();
+    std::lock_guard<std::mutex> lock(c.mu);
+    if (c.device < 0) return RGPU_OK;
+    if (c.stream) cudaStreamSynchronize(c.stream);
+    c.buf.release();
+    c.surface.release();
+    c.staging.release();
+    return RGPU_OK;
+}
+
 int rgpu_get_stats(rgpu_stats *s) {
     if (!s) return RGPU_ERR_INVALID_ARG;
     *s = g_stats;
@@ -883,6 +990,10 @@ extern "C" {
 int rgpu_filter_box_blur(uint8_t *img, uint32_t w, uint32_t h, double sx, double sy, void *stream) {
     g_last_error.clear();
     if (!img || !w || !h) { set_error("invalid arguments"); return RGPU_ERR_INVALID_ARG; }
+    if (!(sx >= 0.0 && sx <= kBoxSigmaMax) || !(sy >= 0.0 && sy <= kBoxSigmaMax)) {
+        set_error("standard deviation must be finite, >= 0 and <= 1e8");
+        return RGPU_ERR_INVALID_ARG;
+    }
     Context &c = ctx();
     std::lock_guard<std::mutex> lock(c.mu);
     int r = ensure_device(c);
@@ -897,6 +1008,10 @@ int rgpu_filter_box_blur(uint8_t *img, uint32_t w, uint32_t h, double sx, double
 int rgpu_filter_iir_blur(uint8_t *img, uint32_t w, uint32_t h, double sx, double sy, void *stream) {
     g_last_error.clear();
     if (!img || !w || !h) { set_error("invalid arguments"); return RGPU_ERR_INVALID_ARG; }
+    if (!(sx >= 0.0 && sx < 1.0e8) || !(sy >= 0.0 && sy < 1.0e8)) {
+        set_error("standard deviation must be finite, >= 0 and < 1e8");
+        return RGPU_ERR_INVALID_ARG;
+    }
     Context &c = ctx();
     std::lock_guard<std::mutex> lock(c.mu);
     int r = ensure_device(c);
@@ -978,9 +1093,11 @@ int rgpu_filter_apply(const rgpu_filter *filter, const rgpu_primitive *prims, ui
     CK(g_fresult.ensure((size_t)w * h * 4));
     BufScratch scratch(g_fjob);
     std::string ferr;
+    g_last_warning.clear();
     r = run_filter_job(job, (uint32_t *)img, g_fresult.as<uint32_t>(), scratch, s, ferr);
     if (scratch.e != cudaSuccess) CK(scratch.e);
     if (r) { set_error("filter: %s", ferr.c_str()); return r; }
+    if (!ferr.empty()) add_warning("filter: " + ferr + " (layer cleared)");
     CK(cudaMemcpyAsync(img, g_fresult.p, (size_t)w * h * 4, cudaMemcpyDeviceToDevice, s));
     if (!stream) CK(cudaStreamSynchronize(s));
     return RGPU_OK;

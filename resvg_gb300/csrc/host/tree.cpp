@@ -73,6 +73,39 @@ int32_t Tree::add_filter(const rgpu_filter &f0, const rgpu_primitive *pr, uint32
     return (int32_t)filters.size() - 1;
 }
 
+bool Tree::set_node_id(uint32_t kind, uint32_t index, const char *id) {
+    std::vector<std::string> *ids = kind == RGPU_NODE_GROUP ? &group_ids : kind == RGPU_NODE_PATH ? &path_ids : nullptr;
+    const size_t count = kind == RGPU_NODE_GROUP ? groups.size() : paths.size();
+    if (!ids || index >= count || !id) return false;
+    if (ids->size() < count) ids->resize(count);
+    (*ids)[index] = id;
+    return true;
+}
+
+bool Tree::node_by_id(const char *id, uint32_t *kind, uint32_t *index) const {
+    if (!id || !*id || groups.empty()) return false;
+    auto id_of = [&](const rgpu_node &n) -> const std::string * {
+        const std::vector<std::string> &ids = n.kind == RGPU_NODE_GROUP ? group_ids : path_ids;
+        return n.index < ids.size() ? &ids[n.index] : nullptr;
+    };
+    // explicit stack of (group, next child) for the pre-order walk
+    std::vector<std::pair<uint32_t, size_t>> stack{{0u, (size_t)0}};
+    while (!stack.empty()) {
+        auto &top = stack.back();
+        const std::vector<rgpu_node> &ch = group_children[top.first];
+        if (top.second >= ch.size()) { stack.pop_back(); continue; }
+        const rgpu_node n = ch[top.second++];
+        const std::string *nid = id_of(n);
+        if (nid && *nid == id) {
+            *kind = n.kind;
+            *index = n.index;
+            return true;
+        }
+        if (n.kind == RGPU_NODE_GROUP && n.index < group_children.size()) stack.push_back({n.index, (size_t)0});
+    }
+    return false;
+}
+
 bool stroke_outline_view(const rgpu_tree_view &t, uint32_t pi, float res_scale, PathData &out) {
     const rgpu_path &p = t.paths[pi];
     if (p.stroke_paint < 0 || !(p.stroke_width > 0)) return false;
@@ -123,7 +156,8 @@ std::shared_ptr<PathData> Tree::stroke_outline(uint32_t pi, float rs) {
         if (it != stroke_cache.end()) return it->second;
     }
     auto out = std::make_shared<PathData>();
-    const rgpu_tree_view *tv = get_view();
+    // a finalised tree's view is read-only: trees are flattened concurrently
+    const rgpu_tree_view *tv = finalized ? &view : get_view();
     if (!stroke_outline_view(*tv, pi, rs, *out)) out.reset();
     std::lock_guard<std::mutex> g(cache_mu);
     stroke_cache[key] = out;

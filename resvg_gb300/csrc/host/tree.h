@@ -10,6 +10,7 @@
 #include <map>
 #include <mutex>
 #include <memory>
+#include <string>
 #include <vector>
 #include "rgpu_tree.h"
 #include "geom.h"
@@ -37,6 +38,8 @@ struct Tree {
     std::vector<uint8_t> image_pixels;
     rgpu_tree_view view{};
     bool finalized = false;
+    // SVG ids of groups and paths ("" = none), for resvg_render_node's lookup
+    std::vector<std::string> group_ids, path_ids;
 
     // stroke outline cache: (path index, res_scale bits) -> outline
     std::mutex cache_mu;
@@ -50,6 +53,12 @@ struct Tree {
     int32_t add_filter(const rgpu_filter &f, const rgpu_primitive *pr, uint32_t n, const int32_t *merge, uint32_t nm);
     bool finalize();
     const rgpu_tree_view *get_view();
+    // Gives node (kind, index) an SVG id; false for an unknown node.
+    bool set_node_id(uint32_t kind, uint32_t index, const char *id);
+    // usvg's Tree::node_by_id (crates/usvg/src/tree/mod.rs:1629-1635,1718-1732):
+    // the first node, in depth-first pre-order over the root group's
+    // descendants, whose id equals `id`; an empty id matches nothing.
+    bool node_by_id(const char *id, uint32_t *kind, uint32_t *index) const;
 
     // Stroke outline of path `pi` (dashing applied) at resolution scale `rs`;
     // null when the stroke produces nothing.

@@ -15,6 +15,7 @@
 // All memory-bound: each pass streams its input once and writes once; the
 // sliding-window passes re-read a window edge from L1/L2.
 #include <cuda_runtime.h>
+#include <mutex>
 #include <stdint.h>
 #include <algorithm>
 #include "kernels.h"
@@ -667,10 +668,19 @@ constexpr int kMorphMaxTaps = 192;
 size_t box_v_smem(int r) { return (size_t)(kBoxT + 2 * r) * 32 * 4; }
 size_t box_h_smem(int r) { return ((size_t)32 * ((kBoxT + 2 * r) | 1) + (size_t)32 * (kBoxT + 1)) * 4; }
 
+// The shared-memory opt-ins are per device: a flag per device index, set
+// under a lock once the attributes are in place on that device.
 cudaError_t box_attrs() {
-    static bool done = false;
-    if (done) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(k_box_v, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)box_v_smem(kBoxMaxR));
+    constexpr int kMaxDevices = 64;
+    static std::mutex mu;
+    static bool done[kMaxDevices] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(mu);
+    if (done[dev]) return cudaSuccess;
+    e = cudaFuncSetAttribute(k_box_v, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)box_v_smem(kBoxMaxR));
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_box_h, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)box_h_smem(kBoxMaxR));
     if (e == cudaSuccess)
@@ -682,12 +692,18 @@ cudaError_t box_attrs() {
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_morph_vh, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)morph_pair_smem(kMorphPairMaxTaps, kMorphPairMaxTaps));
-    if (e == cudaSuccess) done = true;
+    if (e == cudaSuccess) done[dev] = true;
     return e;
 }
 
 // 5 x (vertical pass img -> tmp, horizontal pass tmp -> img)
 cudaError_t filter_box_blur(uint32_t *img, uint32_t *tmp, int w, int h, double sx, double sy, cudaStream_t s) {
+    // Beyond kBoxSigmaMax every box radius exceeds 256 x the longest line a
+    // layer can have, so each pass already rounds every sum to zero; the clamp
+    // keeps the box sizes inside int range without changing the result.
+    // Non-finite or negative deviations mean no blur along that axis.
+    sx = (sx >= 0.0 && sx <= kBoxSigmaMax) ? sx : (sx > kBoxSigmaMax ? kBoxSigmaMax : 0.0);
+    sy = (sy >= 0.0 && sy <= kBoxSigmaMax) ? sy : (sy > kBoxSigmaMax ? kBoxSigmaMax : 0.0);
     int bh[5], bv[5];
     box_sizes((float)sx, bh);
     box_sizes((float)sy, bv);
@@ -832,14 +848,16 @@ __global__ void k_crop(uint32_t *img, int w, int h, int l, int t, int r, int b) 
     int x = (int)(i % w), y = (int)(i / w);
     if (x < l || x >= r || y < t || y >= b) img[i] = 0;
 }
-// draw_pixmap(dx, dy, src) onto dst with a blend mode (highp, Nearest, opacity 1)
-__global__ void k_draw(const uint32_t *src, uint32_t *dst, int w, int h, int dx, int dy, uint32_t blend) {
+// draw_pixmap(dx, dy, src) onto dst with a blend mode (highp, Nearest, opacity
+// 1): src is sw x sh, dst dw x dh; only the overlap is drawn
+__global__ void k_draw(const uint32_t *src, int sw, int sh, uint32_t *dst, int dw, int dh, int dx, int dy,
+                       uint32_t blend) {
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= (size_t)w * h) return;
-    int x = (int)(i % w), y = (int)(i / w);
-    int sx = x - dx, sy = y - dy;
-    if (sx < 0 || sy < 0 || sx >= w || sy >= h) return;
-    dst[i] = dev::composite_pixel(src[(size_t)sy * w + sx], dst[i], 1.0f, blend);
+    if (i >= (size_t)dw * dh) return;
+    int x = (int)(i % dw), y = (int)(i / dw);
+    int64_t sx = (int64_t)x - dx, sy = (int64_t)y - dy;
+    if (sx < 0 || sy < 0 || sx >= sw || sy >= sh) return;
+    dst[i] = dev::composite_pixel(src[(size_t)sy * sw + (size_t)sx], dst[i], 1.0f, blend);
 }
 __global__ void k_fill(uint32_t *img, size_t n, uint32_t v) {
     auto f = [v](uint32_t) { return v; };
@@ -853,10 +871,11 @@ cudaError_t filter_crop(uint32_t *img, int w, int h, int l, int t, int r, int b,
     k_crop<<<nblk(n, 256), 256, 0, s>>>(img, w, h, l, t, r, b);
     return cudaGetLastError();
 }
-cudaError_t filter_draw(const uint32_t *src, uint32_t *dst, int w, int h, int dx, int dy, uint32_t blend, cudaStream_t s) {
-    size_t n = (size_t)w * h;
-    if (!n) return cudaSuccess;
-    k_draw<<<nblk(n, 256), 256, 0, s>>>(src, dst, w, h, dx, dy, blend);
+cudaError_t filter_draw(const uint32_t *src, int sw, int sh, uint32_t *dst, int dw, int dh, int dx, int dy,
+                        uint32_t blend, cudaStream_t s) {
+    size_t n = (size_t)dw * dh;
+    if (!n || sw <= 0 || sh <= 0) return cudaSuccess;
+    k_draw<<<nblk(n, 256), 256, 0, s>>>(src, sw, sh, dst, dw, dh, dx, dy, blend);
     return cudaGetLastError();
 }
 cudaError_t filter_fill(uint32_t *img, size_t n, uint32_t v, cudaStream_t s) {
@@ -1297,8 +1316,9 @@ cudaError_t filter_turbulence(uint32_t *out, int w, int h, const TurbParams &tp,
 namespace rgpu {
 namespace {
 // feTile: out(x, y) = src(l + (x - ox) mod tw, t + (y - oy) mod th), the tile
-// being the input's region cut at (l, t, tw, th) and repeated from (ox, oy).
-__global__ void k_tile(const uint32_t *src, uint32_t *dst, int w, int h, int ox, int oy, int l, int t, int tw,
+// being the input's region cut at (l, t, tw, th) of the sw-wide source and
+// repeated from (ox, oy) over the w x h output.
+__global__ void k_tile(const uint32_t *src, int sw, uint32_t *dst, int w, int h, int ox, int oy, int l, int t, int tw,
                        int th) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (size_t)w * h) return;
@@ -1306,7 +1326,7 @@ __global__ void k_tile(const uint32_t *src, uint32_t *dst, int w, int h, int ox,
     int u = (int)(((int64_t)x - ox) % tw), v = (int)(((int64_t)y - oy) % th);
     if (u < 0) u += tw;
     if (v < 0) v += th;
-    dst[i] = src[(size_t)(t + v) * w + (size_t)(l + u)];
+    dst[i] = src[(size_t)(t + v) * sw + (size_t)(l + u)];
 }
 // feDisplacementMap (displacement_map.rs): each pixel takes the source pixel
 // at its position moved by (map channel / 255 - 0.5) * scale * s, rounded half
@@ -1326,12 +1346,12 @@ __global__ void k_displace(const uint32_t *src, const uint32_t *map, uint32_t *d
 }
 }  // namespace
 
-cudaError_t filter_tile(const uint32_t *src, uint32_t *dst, int w, int h, int ox, int oy, int l, int t, int tw,
-                        int th, cudaStream_t s) {
+cudaError_t filter_tile(const uint32_t *src, int sw, int sh, uint32_t *dst, int w, int h, int ox, int oy, int l,
+                        int t, int tw, int th, cudaStream_t s) {
     const size_t n = (size_t)w * h;
     if (n == 0) return cudaSuccess;
-    if (tw <= 0 || th <= 0 || l < 0 || t < 0 || l + tw > w || t + th > h) return cudaErrorInvalidValue;
-    k_tile<<<nblk(n, 256), 256, 0, s>>>(src, dst, w, h, ox, oy, l, t, tw, th);
+    if (tw <= 0 || th <= 0 || l < 0 || t < 0 || l + tw > sw || t + th > sh) return cudaErrorInvalidValue;
+    k_tile<<<nblk(n, 256), 256, 0, s>>>(src, sw, dst, w, h, ox, oy, l, t, tw, th);
     return cudaGetLastError();
 }
 cudaError_t filter_displacement_map(const uint32_t *src, const uint32_t *map, uint32_t *dst, int w, int h, float sx,

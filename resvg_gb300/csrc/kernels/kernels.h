@@ -34,11 +34,21 @@ cudaError_t launch_raster(int px, uint32_t grid, uint32_t stack_depth, const Str
                           uint32_t ovf_cap, int2 *run_ovf, uint32_t run_ovf_cap, const HairRec *hairs, const HairSpan *hair_spans, uint32_t *err,
                           cudaStream_t s);
 int raster_max_blocks_per_sm(int px);
+// Failure-detection controls of the raster kernel: the try_wait rounds after
+// which a producer/consumer hand-off is declared stuck (0 = the default), and
+// a test hook that withholds the first window of CTA 0 so that wait must run
+// out.  Both apply to launches made afterwards.
+void raster_set_wait_limit(uint32_t rounds);
+uint32_t raster_wait_limit();
+void raster_set_withhold(bool on);
 int raster_max_pairs();  // (draw, row) pairs of one phase-A window
 
 // filters.cu
 cudaError_t filter_color_space(uint32_t *img, size_t n, bool to_linear, cudaStream_t s);
 void box_sizes(float sigma, int sizes[5]);
+// Largest standard deviation the box blur computes with; larger ones give the
+// same (fully transparent) result and are clamped to it.
+constexpr double kBoxSigmaMax = 1.0e8;
 cudaError_t filter_box_blur(uint32_t *img, uint32_t *tmp, int w, int h, double sx, double sy, cudaStream_t s);
 // buf: scratch for four f64 planes of w * h values
 cudaError_t filter_iir_blur(uint32_t *img, double *buf, int w, int h, double sx, double sy, cudaStream_t s);
@@ -49,8 +59,9 @@ cudaError_t filter_arithmetic(const uint32_t *a, const uint32_t *b, uint32_t *ds
                               cudaStream_t s);
 cudaError_t filter_copy(const uint32_t *src, uint32_t *dst, size_t n, cudaStream_t s);
 cudaError_t filter_crop(uint32_t *img, int w, int h, int l, int t, int r, int b, cudaStream_t s);
-cudaError_t filter_draw(const uint32_t *src, uint32_t *dst, int w, int h, int dx, int dy, uint32_t blend,
-                        cudaStream_t s);
+// draw_pixmap of the sw x sh image src at (dx, dy) onto the dw x dh image dst
+cudaError_t filter_draw(const uint32_t *src, int sw, int sh, uint32_t *dst, int dw, int dh, int dx, int dy,
+                        uint32_t blend, cudaStream_t s);
 cudaError_t filter_fill(uint32_t *img, size_t n, uint32_t v, cudaStream_t s);
 cudaError_t filter_alpha_only(uint32_t *img, size_t n, cudaStream_t s);
 // feComponentTransfer on a premultiplied image: demultiply, lut[c] holds the
@@ -65,9 +76,10 @@ struct TurbParams {
     uint32_t seed0;
 };
 cudaError_t filter_turbulence(uint32_t *out, int w, int h, const TurbParams &tp, cudaStream_t s);
-// feTile: the tile (l, t, tw, th) of src, inside the image, repeated from (ox, oy).
-cudaError_t filter_tile(const uint32_t *src, uint32_t *dst, int w, int h, int ox, int oy, int l, int t, int tw,
-                        int th, cudaStream_t s);
+// feTile: the tile (l, t, tw, th) of the sw x sh image src, inside it, repeated
+// from (ox, oy) over the w x h image dst.
+cudaError_t filter_tile(const uint32_t *src, int sw, int sh, uint32_t *dst, int w, int h, int ox, int oy, int l,
+                        int t, int tw, int th, cudaStream_t s);
 // feDisplacementMap with the scaled factors sx, sy and the primitive's scale.
 cudaError_t filter_displacement_map(const uint32_t *src, const uint32_t *map, uint32_t *dst, int w, int h, float sx,
                                     float sy, float scale, int xch, int ych, cudaStream_t s);

@@ -21,7 +21,11 @@
 //    overlap in time (from several host threads or on several streams without
 //    ordering between them) race on it and corrupt each other's results;
 //  * nothing in the scratch needs to start at zero: every blur pass writes the
-//    whole intermediate image before the next pass reads it.
+//    whole intermediate image before the next pass reads it;
+//  * with a NULL stream the blur runs on the default stream and the call
+//    returns when it has finished; with a caller stream it is only enqueued
+//    there and the call returns at once, like the other rgpu_filter_* calls
+//    (the scratch is then in use until that stream reaches the end of it).
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <mutex>
@@ -78,6 +82,10 @@ extern "C" int rgpu_filter_box_blur_noalloc(uint8_t *device_img, uint32_t width,
         set_last_error_message("invalid arguments");
         return RGPU_ERR_INVALID_ARG;
     }
+    if (!(sigma_x >= 0.0 && sigma_x <= kBoxSigmaMax) || !(sigma_y >= 0.0 && sigma_y <= kBoxSigmaMax)) {
+        set_last_error_message("standard deviation must be finite, >= 0 and <= 1e8");
+        return RGPU_ERR_INVALID_ARG;
+    }
     const size_t n = (size_t)width * height;
     if (n > kNoAllocMaxPixels) {
         set_last_error_message("image larger than the allocation-free box blur's scratch (1048576 pixels)");
@@ -88,7 +96,7 @@ extern "C" int rgpu_filter_box_blur_noalloc(uint8_t *device_img, uint32_t width,
     if (r != RGPU_OK) return r;
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e = filter_box_blur((uint32_t *)device_img, scratch, (int)width, (int)height, sigma_x, sigma_y, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess && !stream) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) {
         set_last_error_message(cudaGetErrorString(e));
         return RGPU_ERR_CUDA;

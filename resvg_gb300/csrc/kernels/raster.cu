@@ -73,7 +73,8 @@ struct VmShared {
 };
 
 // ---- producer / consumer hand-off (mbarriers, every wait bounded)
-constexpr uint32_t kWaitLimit = 1u << 22;  // try_wait rounds before a wait is declared stuck
+// try_wait rounds before a wait is declared stuck (the launch's wait_limit
+// argument; rgpu_set_wait_limit changes it)
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {
     return (uint32_t)__cvta_generic_to_shared(p);
 }
@@ -84,12 +85,13 @@ __device__ __forceinline__ void mb_arrive(unsigned long long *mb) {
     asm volatile("{ .reg .b64 st; mbarrier.arrive.shared::cta.b64 st, [%0]; }" ::"r"(smem_addr(mb)) : "memory");
 }
 // Waits for the phase of parity `parity` to complete; false (and error bit 16)
-// when it does not within kWaitLimit rounds, after which the caller proceeds
-// so every thread still reaches every later barrier.
+// when it does not within `limit` rounds, or at once when the CTA has aborted.
+// The caller proceeds either way, so every thread still reaches every later
+// barrier; after an abort no window is read and no pixel is written.
 __device__ __forceinline__ bool mb_wait(unsigned long long *mb, uint32_t parity, uint32_t *err,
-                                        const volatile int32_t *abort) {
+                                        const volatile int32_t *abort, uint32_t limit) {
     const uint32_t a = smem_addr(mb);
-    for (uint32_t it = 0; it < kWaitLimit; it++) {
+    for (uint32_t it = 0; it < limit; it++) {
         if ((it & 255u) == 0u && *abort) return false;
         uint32_t ok;
         asm volatile(
@@ -106,6 +108,15 @@ __device__ __forceinline__ bool mb_wait(unsigned long long *mb, uint32_t parity,
 // barriers of the consumer threads only (named barrier 1) and of the producer
 // threads only (named barrier 2)
 __device__ __forceinline__ void consumer_sync() { asm volatile("bar.sync 1, %0;" ::"n"(kThreads) : "memory"); }
+// consumer barrier that also ORs a predicate over the consumer threads
+__device__ __forceinline__ bool consumer_sync_or(bool v) {
+    uint32_t r;
+    asm volatile("{ .reg .pred pi, po; setp.ne.u32 pi, %1, 0; bar.red.or.pred po, 1, %2, pi; selp.u32 %0, 1, 0, po; }"
+                 : "=r"(r)
+                 : "r"((uint32_t)v), "n"(kThreads)
+                 : "memory");
+    return r != 0;
+}
 __device__ __forceinline__ void producer_sync() { asm volatile("bar.sync 2, %0;" ::"n"(kProducers) : "memory"); }
 
 __device__ __forceinline__ int32_t round16(int32_t x) { return (int32_t)((uint32_t)x + 0x8000u) >> 16; }
@@ -423,7 +434,7 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
          const Cmd *cmds, const uint32_t *fill_cmds, const DrawRec *draws, const PaintRec *paints, const GradRec *grads, const LayerRec *layers,
          const EdgeRec *bins, const uint32_t *bin_offsets, const uint32_t *bin_counts, uint32_t *stack_scratch,
          uint32_t stack_depth, int2 *span_ovf, uint32_t ovf_cap, int2 *run_ovf, uint32_t rovf_cap, const HairRec *hairs,
-         const HairSpan *hair_spans, uint32_t *err) {
+         const HairSpan *hair_spans, uint32_t *err, uint32_t wait_limit, uint32_t withhold) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     VmShared &sh = *reinterpret_cast<VmShared *>(smem_raw);
     uint32_t *layer = reinterpret_cast<uint32_t *>(smem_raw + ((sizeof(VmShared) + 15) & ~(size_t)15));
@@ -453,7 +464,7 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
         for (uint32_t seq = 0;; seq++) {
             const uint32_t is = seq & 1u;
             if (pt == 0) {
-                if (seq >= 2) mb_wait(&sh.mb_item_free[is], ((seq >> 1) - 1u) & 1u, err, &sh.abort);
+                if (seq >= 2) mb_wait(&sh.mb_item_free[is], ((seq >> 1) - 1u) & 1u, err, &sh.abort, wait_limit);
                 ItemInfo &w = sh.items[is];
                 const int32_t idx = (int32_t)atomicAdd(item_counter, 1u);
                 w.idx = idx;
@@ -471,28 +482,44 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
             const uint32_t nwin = (itm.st.fill_cnt + (uint32_t)K - 1) / (uint32_t)K;
             for (uint32_t w = 0; w < nwin; w++) {
                 const uint32_t gw = win_base + w, b = gw & 1u;
-                if (gw >= 2) mb_wait(&sh.mb_free[b], ((gw >> 1) - 1u) & 1u, err, &sh.abort);
-                if (!*(volatile int32_t *)&sh.abort)
+                if (gw >= 2) mb_wait(&sh.mb_free[b], ((gw >> 1) - 1u) & 1u, err, &sh.abort, wait_limit);
+                // one decision per warp: produce_window synchronises its warps
+                const bool skip = __any_sync(0xffffffffu, *(volatile int32_t *)&sh.abort != 0);
+                if (!skip)
                     produce_window(sh, itm, sh.win[b], pt, w * (uint32_t)K, cmds, fill_cmds, draws, paints, grads,
                                    bins, bin_offsets, bin_counts, ovf, ovf_cap,
                                    rovf + (size_t)b * kMaxPairs * rovf_cap, rovf_cap, err);
-                mb_arrive(&sh.mb_ready[b]);
+                // failure-detection test hook: CTA 0 never completes its first
+                // window, so its consumers' bounded wait must run out
+                if (!(withhold && blockIdx.x == 0 && gw == 0)) mb_arrive(&sh.mb_ready[b]);
             }
             win_base += nwin;
         }
         return;
     }
 
+    // set (per thread, for good) once a wait failed or the CTA aborted: the
+    // thread then reads no window and writes no pixel, and only drains the
+    // item queue.  Control flow stays the same in every consumer thread, so
+    // the consumer barriers still match.
+    bool dead = false;
     for (uint32_t seq = 0;; seq++) {
         const uint32_t is = seq & 1u;
-        mb_wait(&sh.mb_item_ready[is], (seq >> 1) & 1u, err, &sh.abort);
+        dead |= !mb_wait(&sh.mb_item_ready[is], (seq >> 1) & 1u, err, &sh.abort, wait_limit);
         if (tid == 0) {
             sh.cur = sh.items[is];
             sh.rects[0] = make_int4(0, 0, sh.cur.st.out_w, sh.cur.st.out_h);
         }
-        consumer_sync();
+        // After an abort the producers no longer wait for the ring entry to be
+        // released, so the copy may mix two items: every consumer then skips
+        // the item (one decision for all of them, taken at this barrier).
+        const bool skip_item = consumer_sync_or(dead || *(volatile int32_t *)&sh.abort != 0);
         mb_arrive(&sh.mb_item_free[is]);  // the entry is copied: the producers may refill it
         if (sh.cur.idx >= (int32_t)nitems) break;
+        if (skip_item) {
+            dead = true;
+            continue;
+        }
         const WorkItem &wi = sh.cur.wi;
         const StreamRec &st = sh.cur.st;
         const int BH = (int)st.band_rows;
@@ -524,7 +551,9 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
                     // ---- the next window: release the previous buffer, wait for this one
                     const uint32_t gw = win_base + fill_seen / (uint32_t)K;
                     if (fill_seen) mb_arrive(&sh.mb_free[(gw - 1u) & 1u]);
-                    mb_wait(&sh.mb_ready[gw & 1u], (gw >> 1) & 1u, err, &sh.abort);
+                    dead |= !mb_wait(&sh.mb_ready[gw & 1u], (gw >> 1) & 1u, err, &sh.abort, wait_limit);
+                    // producers skip windows after an abort but still arrive
+                    dead |= *(volatile int32_t *)&sh.abort != 0;
                     cur_b = gw & 1u;
                     slot_next = 0;
                 }
@@ -564,6 +593,7 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
                 } else {
                     fill_seen++;
                     slot = slot_next++;
+                    if (dead) continue;  // the window may not have been produced
                     const int pair = slot * BH + row;
                     // one entry: the closing sentinel alone, nothing covered on this row
                     const WinBuf &wb = sh.win[cur_b];
@@ -696,13 +726,20 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
         if (nwin) mb_arrive(&sh.mb_free[(win_base + nwin - 1u) & 1u]);
         win_base += nwin;
         if (depth != 0) atomicOr(err, 8u);
-        for (int i = 0; i < PX; i++) {
-            const int32_t x = wi.x0 + i * tpr + lr;
-            if (row_ok && x < wi.x1) *(uint32_t *)(out + (size_t)cy * st.out_stride + 4 * (size_t)x) = layer[i * kThreads + tid];
-        }
+        if (!dead)
+            for (int i = 0; i < PX; i++) {
+                const int32_t x = wi.x0 + i * tpr + lr;
+                if (row_ok && x < wi.x1) *(uint32_t *)(out + (size_t)cy * st.out_stride + 4 * (size_t)x) = layer[i * kThreads + tid];
+            }
         consumer_sync();  // every consumer is done with the item copy and the layer stack
     }
 }
+
+// launch arguments of the failure-detection controls (read at launch time; a
+// captured graph keeps the values it was captured with)
+constexpr uint32_t kDefaultWaitLimit = 1u << 22;
+uint32_t g_wait_limit = kDefaultWaitLimit;
+uint32_t g_withhold = 0;
 
 }  // namespace
 
@@ -725,9 +762,13 @@ cudaError_t launch_raster(int px, uint32_t grid, uint32_t stack_depth, const Str
     k_raster<<<grid, kBlock, raster_smem_bytes_px(px), s>>>(px, streams, items, nitems, item_counter, cmds, fill_cmds, draws, paints,
                                                               grads, layers, bins, bin_offsets, bin_counts, stack,
                                                               stack_depth, span_ovf, ovf_cap, run_ovf, run_ovf_cap, hairs,
-                                                              hair_spans, err);
+                                                              hair_spans, err, g_wait_limit, g_withhold);
     return cudaGetLastError();
 }
+
+void raster_set_wait_limit(uint32_t rounds) { g_wait_limit = rounds ? rounds : kDefaultWaitLimit; }
+uint32_t raster_wait_limit() { return g_wait_limit; }
+void raster_set_withhold(bool on) { g_withhold = on ? 1u : 0u; }
 
 int raster_max_blocks_per_sm(int px) {
     int n = 0;

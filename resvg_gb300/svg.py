@@ -1018,7 +1018,7 @@ class Loader:
             if e.get("systemLanguage") is not None:
                 raise Unsupported("systemLanguage")
         self.clip_cache, self.mask_cache, self.filter_cache = {}, {}, {}
-        self.ids_out = {}  # SVG id -> render_node id ("<group>" or "p<path>")
+        self.ids_out = {}  # SVG id -> the oracle's node id ("<group>" or "p<path>")
 
     # ---- attributes with style and inheritance
     def attrs(self, e):
@@ -1319,8 +1319,9 @@ class Builder(Loader):
         gi = self.tree.add_group(parent, g)
         if fids:
             self.tree.set_group_filters(gi, fids)
-        if eid is not None:
+        if eid:
             self.ids_out.setdefault(eid, str(gi))
+            self.tree.set_node_id(A.NODE_GROUP, gi, eid)
         return gi
 
     # ---- bounding boxes (object bounding box of an element, its user space)
@@ -1754,8 +1755,9 @@ class Builder(Loader):
         if path.stroke_paint < 0:
             path.stroke_width = 1.0
         pi = self.tree.add_path(parent, path, verbs, pts, dashes)
-        if e.get("id") is not None:
+        if e.get("id"):
             self.ids_out.setdefault(e.get("id"), "p%d" % pi)
+            self.tree.set_node_id(A.NODE_PATH, pi, e.get("id"))
 
     # ---- raster images
     def image(self, e, parent, ts):

@@ -16,6 +16,10 @@ Usage:  python tests/golden/pin_oracle.py <resvg checkout> [--write] [--verbose]
            per test directory, the SVG text and the golden image (demultiplied
            RGBA8), both zlib-compressed.  tests/test_oracle_golden.py replays
            them on the oracle (CPU) and tests/test_gpu_golden.py on the GPU.
+  --extra-nodes  writes tests/golden/extra_nodes.npz: the render_node cases of
+           crates/resvg/tests/integration/extra.rs (an SVG, the SVG id rendered,
+           the golden image), replayed by id through the C ABI in
+           tests/test_gpu_render_node.py.
 """
 from __future__ import annotations
 
@@ -119,7 +123,7 @@ def render_extra(tree, mode, arg):
         return w, h, (float(arg), 0.0, 0.0, float(arg), 0.0, 0.0), None
     from resvg_gb300 import node_abs_bbox
     nid = tree.ids.get(arg)
-    b = node_abs_bbox(tree, nid) if nid else None
+    b = node_abs_bbox(tree, arg) if nid else None
     if b is None:
         return None
     return max(1, int(round_half_away(b[2]))), max(1, int(round_half_away(b[3]))), (1, 0, 0, 1, 0, 0), nid
@@ -181,12 +185,34 @@ def run(root, verbose=False, only=None):
     return results, fixtures
 
 
+def write_extra_node_fixtures(root):
+    """The render_node cases of extra.rs: name, SVG text, node id, golden image."""
+    names, blob = [], {}
+    for name, path, mode, arg in collect_extra(root):
+        if mode != "node" or not os.path.exists(path[:-4] + ".png"):
+            continue
+        i = len(names)
+        text = open(path, encoding="utf-8").read()
+        img = png.read_png(path[:-4] + ".png")
+        blob["svg_%d" % i] = np.frombuffer(zlib.compress(text.encode(), 9), dtype=np.uint8)
+        blob["png_%d" % i] = np.frombuffer(zlib.compress(np.ascontiguousarray(img).tobytes(), 9), dtype=np.uint8)
+        blob["shape_%d" % i] = np.array(img.shape, dtype=np.int32)
+        blob["id_%d" % i] = np.array(arg)
+        names.append("extra/" + name)
+    blob["names"] = np.array(names)
+    np.savez(os.path.join(HERE, "extra_nodes.npz"), **blob)
+    return names
+
+
 def main():
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
     root = args[0] if args else None
     if root is None or not os.path.isdir(root):
         print(__doc__)
         return 2
+    if "--extra-nodes" in sys.argv:
+        print(write_extra_node_fixtures(root))
+        return 0
     only = None
     for a in sys.argv[1:]:
         if a.startswith("--only="):

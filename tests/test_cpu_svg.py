@@ -106,3 +106,47 @@ def test_component_transfer_record():
     assert p.i[0] == A.TF_IDENTITY and p.i[2] == A.TF_TABLE and p.i[6] == 4
     assert list(p.f[32:36]) == [1.0, 1.0, 0.0, 0.0]       # the later feFuncB wins
     assert p.i[3] == A.TF_GAMMA and list(p.f[48:51]) == [1.0, 1.0, 0.5]   # invalid amplitude: default
+
+
+def test_node_by_id_follows_usvg_order():
+    """rgpu_tree_find_node restates usvg's node_by_id (crates/usvg/src/tree/
+    mod.rs:1718-1732): depth-first pre-order below the root, first match wins,
+    the root group and detached groups are not searched, "" never matches."""
+    import resvg_gb300 as R
+    from resvg_gb300 import _abi as A
+    from tests.helpers import base_path, plain_group, rect_path
+    t = R.Tree(100, 100)
+    root = t.add_group(-1, plain_group())
+    g1 = t.add_group(root, plain_group())
+    v, p = rect_path(0, 0, 10, 10)
+    p0 = t.add_path(g1, base_path(), v, p)
+    g2 = t.add_group(root, plain_group())
+    p1 = t.add_path(g2, base_path(), v, p)
+    detached = t.add_group(-1, plain_group())
+    p2 = t.add_path(detached, base_path(), v, p)
+    t.set_node_id(A.NODE_GROUP, root, "root")
+    t.set_node_id(A.NODE_PATH, p0, "dup")     # inside g1: visited before g2
+    t.set_node_id(A.NODE_GROUP, g2, "dup")
+    t.set_node_id(A.NODE_PATH, p1, "leaf")
+    t.set_node_id(A.NODE_PATH, p2, "hidden")
+    t.set_node_id(A.NODE_GROUP, detached, "clip-content")
+    t.finalize()
+    assert t.find_node("dup") == (A.NODE_PATH, p0)
+    assert t.find_node("leaf") == (A.NODE_PATH, p1)
+    assert t.find_node("root") is None
+    assert t.find_node("hidden") is None and t.find_node("clip-content") is None
+    assert t.find_node("") is None and t.find_node("missing") is None
+    import pytest
+    with pytest.raises(R.RenderError):
+        t.set_node_id(A.NODE_PATH, 99, "x")
+
+
+def test_front_end_keeps_svg_ids():
+    from resvg_gb300 import svg
+    tree = svg.load_svg('<svg xmlns="http://www.w3.org/2000/svg" width="50" height="50">'
+                        '<g id="outer"><rect id="box" x="5" y="5" width="20" height="20" fill="red"/></g>'
+                        '<circle id="dot" cx="30" cy="30" r="5"/></svg>')
+    from resvg_gb300 import _abi as A
+    assert tree.find_node("box")[0] == A.NODE_PATH
+    assert tree.find_node("dot")[0] == A.NODE_PATH
+    assert tree.find_node("nope") is None

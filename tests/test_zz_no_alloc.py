@@ -36,8 +36,11 @@ def _premul_image(h, w, seed):
     return img
 
 
+# sigma 150 gives box radii above the shared-memory tiles' limit, so those
+# passes run the generic line kernel through the fixed scratch too
 @pytest.mark.parametrize("shape,sigma", [((96, 160), (3.0, 3.0)), ((1024, 1024), (7.5, 2.0)),
-                                         ((33, 1000), (0.0, 12.0))])
+                                         ((33, 1000), (0.0, 12.0)), ((64, 2000), (150.0, 150.0)),
+                                         ((2000, 64), (90.0, 160.0))])
 def test_noalloc_box_blur_matches_allocating_entry(gpu, shape, sigma):
     import torch
     f = _noalloc()
@@ -63,3 +66,33 @@ def test_noalloc_rejects_oversized_image(gpu):
     assert status == 1  # RGPU_ERR_INVALID_ARG
     assert "1048576" in R.lib().rgpu_last_error().decode()
     assert 1025 * 1024 > MAX_PIXELS
+
+
+def test_noalloc_on_a_caller_stream(gpu):
+    """On a caller stream the call is enqueued and returns at once; the result
+    after synchronising that stream matches the allocating entry point."""
+    import torch
+    f = _noalloc()
+    h, w = 300, 700
+    stream = torch.cuda.Stream()
+    for call in range(2):
+        img = _premul_image(h, w, seed=31 + call)
+        ref = torch.from_numpy(img.copy()).cuda()
+        out = torch.from_numpy(img.copy()).cuda()
+        torch.cuda.synchronize()
+        R.box_blur(ref, 4.0, 9.0)
+        status = f(C.c_void_p(out.data_ptr()), w, h, C.c_double(4.0), C.c_double(9.0), C.c_void_p(stream.cuda_stream))
+        assert status == 0, R.lib().rgpu_last_error().decode()
+        stream.synchronize()
+        torch.cuda.synchronize()
+        d = (ref.to(torch.int16) - out.to(torch.int16)).abs().max().item()
+        assert d <= TOLERANCE, "call %d on a caller stream: max channel difference %d" % (call, d)
+
+
+@pytest.mark.parametrize("sigma", [float("nan"), float("inf"), -1.0, 2.0e8])
+def test_noalloc_rejects_bad_sigma(gpu, sigma):
+    f = _noalloc()
+    # rejected before any device work: the pointer is never dereferenced
+    status = f(C.c_void_p(16), 8, 8, C.c_double(sigma), C.c_double(1.0), None)
+    assert status == 1  # RGPU_ERR_INVALID_ARG
+    assert "standard deviation" in R.lib().rgpu_last_error().decode()
