@@ -373,7 +373,7 @@ def run_batched(args, rank, world):
     import torch
     import resvg_gb300 as R
     from resvg_gb300 import build as B
-    from resvg_gb300.batch import TUNING_CANDIDATES
+    from resvg_gb300 import batch as BT
     B.build()
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
     torch.cuda.set_device(dev)
@@ -396,11 +396,12 @@ def run_batched(args, rank, world):
     stream = torch.cuda.Stream(device=dev)
     torch.cuda.set_stream(stream)
     sh = stream.cuda_stream
-    # autotune the raster decomposition on a stratified sample of the scenes
+    # autotune the raster decomposition on a stratified sample of the scenes:
+    # band rows per (canvas-width, draw-count) bucket, then pixels per thread
     samp = list(range(0, n, max(1, n // 256)))
     t0 = time.perf_counter()
-    best, best_ms = R.autotune([trees[i] for i in samp], [ident[i] for i in samp], [ws[i] for i in samp],
-                               [hs[i] for i in samp], [ptrs[i] for i in samp], TUNING_CANDIDATES, reps=2)
+    table, best_px, tune_ms = BT.autotune_table([trees[i] for i in samp], [ws[i] for i in samp],
+                                                [hs[i] for i in samp], [ptrs[i] for i in samp], reps=2)
     tune_s = time.perf_counter() - t0
     t0 = time.perf_counter()
     scene = R.Scene(trees, ident, ws, hs, ptrs)
@@ -498,8 +499,10 @@ def run_batched(args, rank, world):
                    "split": "LPT on side^2 x paths" if world > 1 else "one GPU",
                    "output_mpix": out_px / 1e6, "draws": info["draws"], "edges": info["edges"],
                    "binned_edges": info["binned_edges"], "work_items": info["work_items"],
-                   "tuning": {"band_rows": best[0], "pixels_per_thread": best[1],
-                              "autotune_ms_on_sample": best_ms, "autotune_s": tune_s},
+                   "tuning": {"table": [list(e) for e in table], "pixels_per_thread": best_px,
+                              "autotune_ms_on_sample": min(tune_ms["px"].values()), "autotune_s": tune_s,
+                              "buckets": "width <= %s x draws <= %s" % (list(BT.WIDTH_BUCKETS),
+                                                                        list(BT.DRAW_BUCKETS))},
                    "prepare_s": prep_s, "l2": "outputs %.1f GB > L2 (129 MB)" % (total / 1e9),
                    "graph_replay": True},
         "mpix_s": value * out_px / n / 1e6 if n else 0.0,
@@ -536,7 +539,7 @@ def _soft_slice(arr, scenes):
     out["scenes"] = scenes
     out["seg_offset"] = np.ascontiguousarray(arr["seg_offset"][:scenes * P + 1])
     out["points"] = np.ascontiguousarray(arr["points"][:3 * segs_end])
-    for k in ("paint_kind", "colors", "stop_offsets", "stop_colors", "grad_line"):
+    for k in ("paint_kind", "colors", "stop_offsets", "stop_colors", "grad_line", "opacity"):
         out[k] = np.ascontiguousarray(arr[k][:scenes * P])
     out["sigma"] = np.ascontiguousarray(arr["sigma"][:scenes])
     return out
@@ -556,7 +559,7 @@ def cpu_baseline_soft(a, t_arrays, scenes=4):
     oracle.soft_dloss(sub, target.astype(np.float32), direction)
     dt = time.perf_counter() - t0
     nparams = sum(int(np.asarray(sub[k]).size) for k in ("points", "colors", "stop_offsets", "stop_colors",
-                                                             "sigma")) // scenes
+                                                             "sigma", "opacity")) // scenes
     return {"value": scenes / dt, "unit": "scenes/s (forward + one directional derivative)", "cores": 1,
             "kind": "port", "full_gradient_value": scenes / dt / max(1, nparams),
             "params_per_scene": nparams,

@@ -151,6 +151,17 @@ typedef struct rgpu_tuning {
 } rgpu_tuning;
 int rgpu_set_tuning(const rgpu_tuning *t);
 int rgpu_get_tuning(rgpu_tuning *t);
+/* Tuning table: with band_rows 0 in the tuning, each stream (a scene or an
+ * internal surface) takes the band rows of the first entry whose max_width
+ * and max_draws are at least its width and draw count (band_rows 0 in the
+ * entry: the built-in rule on the width).  The autotuner fills it per
+ * (canvas-size bucket, path-count bucket) (resvg_gb300.batch.autotune_table). */
+typedef struct rgpu_tuning_entry {
+    uint32_t max_width, max_draws, band_rows, reserved;
+} rgpu_tuning_entry;
+int rgpu_set_tuning_table(const rgpu_tuning_entry *entries, uint32_t count);
+/* Copies up to `capacity` entries and stores the table's length in *count. */
+int rgpu_get_tuning_table(rgpu_tuning_entry *entries, uint32_t capacity, uint32_t *count);
 /* Autotuner (no counterpart in the reference): prepares the given scenes once
  * per candidate tuning, times `reps` graph replays of each with CUDA events,
  * keeps the fastest as the current tuning and returns it (and its ms per
@@ -243,7 +254,9 @@ int rgpu_filter_box_blur_noalloc(uint8_t *device_img, uint32_t width, uint32_t h
  * end) per cubic except the last, which has (control 1, control 2) and ends
  * at the start point (closed by construction).  See
  * resvg_gb300/csrc/kernels/soft.cu for the coverage, paint, composite and blur
- * definitions. */
+ * definitions.  Limits: width <= 1024 (4 pixels per thread of a 256-thread
+ * row), blur radius 12 (sigma up to 4), at most 512 flattened lines of one path
+ * crossing one pixel row (RGPU_ERR_CAPACITY beyond). */
 typedef struct rgpu_soft_batch {
     uint32_t scenes, width, height, paths_per_scene;
     uint32_t total_segments;     /* seg_offset[scenes * paths_per_scene] */
@@ -255,10 +268,13 @@ typedef struct rgpu_soft_batch {
     const float *stop_colors;    /* per path: 4 straight RGBA stop colours */
     const float *grad_line;      /* per path: x1, y1, x2, y2 of the gradient (pad spread) */
     const float *sigma;          /* per scene: Gaussian blur sigma */
+    const float *opacity;        /* per path: opacity multiplying the paint's alpha (NULL: 1), as
+                                    resvg's fill opacity (crates/resvg/src/path.rs:49) */
 } rgpu_soft_batch;
-/* Gradients, same layouts as the parameters (device; overwritten). */
+/* Gradients, same layouts as the parameters (device; overwritten).  opacity
+ * may be NULL when the batch has no opacity parameter. */
 typedef struct rgpu_soft_grads {
-    float *points, *colors, *stop_offsets, *stop_colors, *sigma;
+    float *points, *colors, *stop_offsets, *stop_colors, *sigma, *opacity;
 } rgpu_soft_grads;
 /* image = composite (premultiplied RGBA, scenes x height x width x 4 floats),
  * blurred = its Gaussian blur.  Synchronous. */

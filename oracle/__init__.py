@@ -202,8 +202,8 @@ def _soft_struct(arrays):
     b.total_segments = int(arrays["seg_offset"][-1])
     for f, k in (("seg_offset", "seg_offset"), ("points", "points"), ("paint_kind", "paint_kind"),
                  ("colors", "colors"), ("stop_offsets", "stop_offsets"), ("stop_colors", "stop_colors"),
-                 ("grad_line", "grad_line"), ("sigma", "sigma")):
-        setattr(b, f, arrays[k].ctypes.data)
+                 ("grad_line", "grad_line"), ("sigma", "sigma"), ("opacity", "opacity")):
+        setattr(b, f, arrays[k].ctypes.data if k in arrays else None)
     return b
 
 
@@ -223,7 +223,7 @@ def soft_dloss(arrays, target, direction):
     """(loss, dloss/dv) in FP64 for a parameter direction v (dict of float64
     arrays keyed like the parameters; missing keys are zero)."""
     L = lib()
-    L.oracle_soft_dloss.argtypes = [C.c_void_p, C.c_void_p] + [C.c_void_p] * 5 + [C.c_void_p, C.c_void_p]
+    L.oracle_soft_dloss.argtypes = [C.c_void_p, C.c_void_p] + [C.c_void_p] * 6 + [C.c_void_p, C.c_void_p]
     b = _soft_struct(arrays)
     t = np.ascontiguousarray(target, dtype=np.float32)
     keep = []
@@ -237,5 +237,5 @@ def soft_dloss(arrays, target, direction):
     loss = C.c_double()
     dl = C.c_double()
     L.oracle_soft_dloss(C.byref(b), t.ctypes.data, ptr("points"), ptr("colors"), ptr("stop_offsets"),
-                        ptr("stop_colors"), ptr("sigma"), C.byref(loss), C.byref(dl))
+                        ptr("stop_colors"), ptr("sigma"), ptr("opacity"), C.byref(loss), C.byref(dl))
     return loss.value, dl.value

@@ -7,7 +7,8 @@
 // flattening of each cubic into 16 lines at uniform t, the winding-weighted pixel area of every
 // clipped line (sdy * mean of clamp(1 - x, 0, 1) over the line's x range
 // relative to the pixel), soft coverage min(|A|, 1), solid / 4-stop linear
-// gradient paints premultiplied after interpolation, source-over in path
+// gradient paints whose alpha is multiplied by the path's opacity,
+// premultiplied after interpolation, source-over in path
 // order, a separable Gaussian blur of radius 12 with weights normalised over
 // the kernel and zero outside the canvas, and the mean squared error.
 //
@@ -85,7 +86,7 @@ struct Host {
 
 template <class T>
 struct Params {
-    std::vector<T> pts, colors, offsets, stops, sigma;
+    std::vector<T> pts, colors, offsets, stops, sigma, opacity;
 };
 
 template <class T>
@@ -159,6 +160,7 @@ void render(const rgpu_soft_batch &b, const Params<T> &pr, std::vector<T> &image
                             a = sc[4 * i + 3] + w * (sc[4 * i + 7] - sc[4 * i + 3]);
                         }
                     }
+                    a = a * pr.opacity[j];
                     const T ca = c * a, keep = 1.0 - ca;
                     T *cp = &C[4 * (size_t)x];
                     cp[0] = c * (r * a) + keep * cp[0];
@@ -222,6 +224,8 @@ int oracle_soft_forward(const rgpu_soft_batch *b, double *image, double *blurred
     pr.offsets.assign(b->stop_offsets, b->stop_offsets + 4 * np);
     pr.stops.assign(b->stop_colors, b->stop_colors + 16 * np);
     pr.sigma.assign(b->sigma, b->sigma + b->scenes);
+    pr.opacity.assign(np, 1.0);
+    if (b->opacity) pr.opacity.assign(b->opacity, b->opacity + np);
     std::vector<double> im, bl;
     render<double>(*b, pr, im, bl);
     std::memcpy(image, im.data(), im.size() * 8);
@@ -233,8 +237,8 @@ int oracle_soft_forward(const rgpu_soft_batch *b, double *image, double *blurred
 // directional derivative along the parameter direction (same layouts as the
 // parameters), by forward-mode dual numbers in FP64.
 int oracle_soft_dloss(const rgpu_soft_batch *b, const float *target, const double *d_points, const double *d_colors,
-                      const double *d_offsets, const double *d_stops, const double *d_sigma, double *loss,
-                      double *dloss) {
+                      const double *d_offsets, const double *d_stops, const double *d_sigma,
+                      const double *d_opacity, double *loss, double *dloss) {
     const size_t np = (size_t)b->scenes * b->paths_per_scene;
     Params<Dd> pr;
     auto load = [](std::vector<Dd> &v, const float *x, const double *d, size_t n) {
@@ -246,6 +250,11 @@ int oracle_soft_dloss(const rgpu_soft_batch *b, const float *target, const doubl
     load(pr.offsets, b->stop_offsets, d_offsets, 4 * np);
     load(pr.stops, b->stop_colors, d_stops, 16 * np);
     load(pr.sigma, b->sigma, d_sigma, b->scenes);
+    if (b->opacity) {
+        load(pr.opacity, b->opacity, d_opacity, np);
+    } else {
+        pr.opacity.assign(np, D(1.0));
+    }
     std::vector<Dd> im, bl;
     render<Dd>(*b, pr, im, bl);
     Dd L = D(0.0);

@@ -100,6 +100,10 @@ class Tuning(C.Structure):
     _fields_ = [("band_rows", u32), ("pixels_per_thread", u32), ("reserved", u32)]
 
 
+class TuningEntry(C.Structure):
+    _fields_ = [("max_width", u32), ("max_draws", u32), ("band_rows", u32), ("reserved", u32)]
+
+
 class Stats(C.Structure):
     _fields_ = [("draws", C.c_uint64), ("edges", C.c_uint64), ("crossings_capacity", C.c_uint64),
                 ("work_items", C.c_uint64), ("kernel_launches", C.c_uint64),
@@ -112,12 +116,13 @@ class SoftBatch(C.Structure):
     _fields_ = [("scenes", u32), ("width", u32), ("height", u32), ("paths_per_scene", u32),
                 ("total_segments", u32), ("seg_offset", C.c_void_p), ("points", C.c_void_p),
                 ("paint_kind", C.c_void_p), ("colors", C.c_void_p), ("stop_offsets", C.c_void_p),
-                ("stop_colors", C.c_void_p), ("grad_line", C.c_void_p), ("sigma", C.c_void_p)]
+                ("stop_colors", C.c_void_p), ("grad_line", C.c_void_p), ("sigma", C.c_void_p),
+                ("opacity", C.c_void_p)]
 
 
 class SoftGrads(C.Structure):
     _fields_ = [("points", C.c_void_p), ("colors", C.c_void_p), ("stop_offsets", C.c_void_p),
-                ("stop_colors", C.c_void_p), ("sigma", C.c_void_p)]
+                ("stop_colors", C.c_void_p), ("sigma", C.c_void_p), ("opacity", C.c_void_p)]
 
 
 # enums (rgpu_tree.h)

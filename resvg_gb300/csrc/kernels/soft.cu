@@ -16,8 +16,9 @@
 //     with G(a, b) the mean of clamp(1 - x, 0, 1) over x from a to b, written
 //     in closed, well-conditioned form per case;
 //   * paints (at pixel centres): a straight RGBA colour or a linear gradient of
-//     4 stops (pad spread, offsets ascending), premultiplied after
-//     interpolation; paths composite source-over in order from transparent;
+//     4 stops (pad spread, offsets ascending), its alpha multiplied by the
+//     path's opacity, premultiplied after interpolation; paths composite
+//     source-over in order from transparent;
 //   * a Gaussian blur of the composite, separable, radius kRadius, weights
 //     exp(-j^2 / 2 sigma^2) normalised over [-kRadius, kRadius], zero outside
 //     the canvas.
@@ -135,12 +136,24 @@ __device__ __forceinline__ bool clip_row(T x0, T y0, T x1, T y1, float py, T *xl
 
 // ---- paints
 struct PaintOut {
-    float r, g, b, a;  // straight colour at the pixel
+    float r, g, b, a;  // straight colour at the pixel, alpha times the path's opacity
+    float raw_a;       // the paint's alpha before the opacity
+    float op;          // the path's opacity
     int seg;           // gradient: stop interval (-1: below first, 3: at/above last), solid: -2
     float w, t;        // interpolation weight and gradient parameter
 };
 
+__device__ __forceinline__ PaintOut eval_paint_raw(const rgpu_soft_batch &B, uint32_t j, float x, float y);
+
 __device__ __forceinline__ PaintOut eval_paint(const rgpu_soft_batch &B, uint32_t j, float x, float y) {
+    PaintOut o = eval_paint_raw(B, j, x, y);
+    o.op = B.opacity ? B.opacity[j] : 1.0f;
+    o.raw_a = o.a;
+    o.a = o.a * o.op;
+    return o;
+}
+
+__device__ __forceinline__ PaintOut eval_paint_raw(const rgpu_soft_batch &B, uint32_t j, float x, float y) {
     PaintOut o;
     o.w = 0.0f; o.t = 0.0f;
     if (B.paint_kind[j] == 0) {
@@ -394,9 +407,9 @@ __global__ void k_dsigma(const float4 *a, const float4 *b, const float *sigma, u
 }
 
 // ---- adjoint of the rows: persistent CTAs with bounded scratch
-struct ParamAcc {  // per-CTA shared accumulators of one path's paint gradients
-    float v[20];
-};
+// per path: 16 stop colours + 4 stop offsets (gradient) or 4 colour
+// channels (solid), then the opacity at index 20
+constexpr int kAcc = 21;
 
 __device__ __forceinline__ float warp_sum(float v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -408,7 +421,7 @@ __global__ void __launch_bounds__(kThreads) k_backward(rgpu_soft_batch B, rgpu_s
                                                        float4 *scratch_color, float2 *vgrad, uint32_t *row_counter,
                                                        uint32_t *overflow) {
     __shared__ RowShared sh;
-    __shared__ float pacc[20];
+    __shared__ float pacc[kAcc];
     __shared__ int row_sh;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int W = (int)B.width;
@@ -460,9 +473,9 @@ __global__ void __launch_bounds__(kThreads) k_backward(rgpu_soft_batch B, rgpu_s
         }
         for (int p = (int)P - 1; p >= 0; p--) {
             const uint32_t j = s * P + (uint32_t)p;
-            float acc[20];
+            float acc[kAcc];
 #pragma unroll
-            for (int q = 0; q < 20; q++) acc[q] = 0.0f;
+            for (int q = 0; q < kAcc; q++) acc[q] = 0.0f;
             const bool is_grad = B.paint_kind[j] != 0;
 #pragma unroll
             for (int k = 0; k < kMaxPx; k++) {
@@ -481,9 +494,12 @@ __global__ void __launch_bounds__(kThreads) k_backward(rgpu_soft_batch B, rgpu_s
                                      g.w * (Pa - po.a * Cp.w);
                     const float da_keep = -c * (g.x * Cp.x + g.y * Cp.y + g.z * Cp.z + g.w * Cp.w);
                     const float dPr = c * g.x, dPg = c * g.y, dPb = c * g.z, dPa = c * g.w;
-                    // straight colour
+                    // straight colour; `da` is d/d(alpha times opacity): the
+                    // paint's own alpha gets da * opacity, the opacity da * alpha
                     const float dr = dPr * po.a, dg = dPg * po.a, db = dPb * po.a;
-                    const float da = dPr * po.r + dPg * po.g + dPb * po.b + dPa + da_keep;
+                    const float da_eff = dPr * po.r + dPg * po.g + dPb * po.b + dPa + da_keep;
+                    const float da = da_eff * po.op;
+                    acc[20] += da_eff * po.raw_a;
                     if (!is_grad) {
                         acc[0] += dr; acc[1] += dg; acc[2] += db; acc[3] += da;
                     } else if (po.seg < 0 || po.seg == 3) {
@@ -518,16 +534,20 @@ __global__ void __launch_bounds__(kThreads) k_backward(rgpu_soft_batch B, rgpu_s
                 areaS[si] = dA;
             }
             // reduce the paint gradients of this path over the row
-            if (tid < 20) pacc[tid] = 0.0f;
+            if (tid < kAcc) pacc[tid] = 0.0f;
             __syncthreads();
-            const int nq = is_grad ? 20 : 4;
-            for (int q = 0; q < nq; q++) {
-                const float v = warp_sum(acc[q]);
-                if (lane == 0 && v != 0.0f) atomicAdd(&pacc[q], v);
+            const int nq = is_grad ? kAcc : 5;  // solid: colour channels 0..3, then the opacity
+#pragma unroll
+            for (int q = 0; q < kAcc; q++) {
+                if (q >= nq) break;
+                const int qi = (!is_grad && q == 4) ? 20 : q;
+                const float v = warp_sum(acc[qi]);
+                if (lane == 0 && v != 0.0f) atomicAdd(&pacc[qi], v);
             }
             __syncthreads();
-            if (tid < nq && pacc[tid] != 0.0f) {
-                if (!is_grad) atomicAdd(&G.colors[4 * (size_t)j + tid], pacc[tid]);
+            if (tid < kAcc && pacc[tid] != 0.0f) {
+                if (tid == 20) { if (G.opacity) atomicAdd(&G.opacity[j], pacc[20]); }
+                else if (!is_grad) atomicAdd(&G.colors[4 * (size_t)j + tid], pacc[tid]);
                 else if (tid < 16) atomicAdd(&G.stop_colors[16 * (size_t)j + tid], pacc[tid]);
                 else atomicAdd(&G.stop_offsets[4 * (size_t)j + (tid - 16)], pacc[tid]);
             }
@@ -740,6 +760,7 @@ extern "C" int rgpu_soft_backward(const rgpu_soft_batch *b, const float *image, 
     cudaMemsetAsync(g->stop_offsets, 0, (size_t)npaths * 16, s);
     cudaMemsetAsync(g->stop_colors, 0, (size_t)npaths * 64, s);
     cudaMemsetAsync(g->sigma, 0, (size_t)b->scenes * 4, s);
+    if (g->opacity) cudaMemsetAsync(g->opacity, 0, (size_t)npaths * 4, s);
     cudaMemsetAsync(g_vgrad.p, 0, nverts * sizeof(float2), s);
     cudaMemsetAsync(g_flags.p, 0, 16, s);
     const dim3 blk(32, 8), grid((b->width + 31) / 32, (b->height + 7) / 8, b->scenes);

@@ -16,7 +16,7 @@ import numpy as np
 
 from . import _abi, check, lib
 
-PARAMS = ("points", "colors", "stop_offsets", "stop_colors", "sigma")
+PARAMS = ("points", "colors", "stop_offsets", "stop_colors", "sigma", "opacity")
 
 
 def make_scenes(seed=0, scenes=256, size=256, paths=64, min_segs=4, max_segs=16):
@@ -39,9 +39,11 @@ def make_scenes(seed=0, scenes=256, size=256, paths=64, min_segs=4, max_segs=16)
     stop_colors[:, :, 3] = rng.uniform(0.3, 1.0, size=(npaths, 4))
     grad_line = rng.uniform(0.0, float(size), size=(npaths, 4)).astype(np.float32)
     sigma = rng.uniform(0.5, 4.0, size=scenes).astype(np.float32)
+    # drawn last so the other parameters keep the values earlier seeds gave them
+    opacity = rng.uniform(0.3, 1.0, size=npaths).astype(np.float32)
     return {"scenes": scenes, "width": size, "height": size, "paths": paths, "seg_offset": seg_offset,
             "points": points, "paint_kind": paint_kind, "colors": colors, "stop_offsets": stop_offsets,
-            "stop_colors": stop_colors, "grad_line": grad_line, "sigma": sigma}
+            "stop_colors": stop_colors, "grad_line": grad_line, "sigma": sigma, "opacity": opacity}
 
 
 def perturb(arrays, seed=1, point_sd=2.0, color_sd=0.05):
@@ -149,13 +151,13 @@ def _autograd():
     import torch
 
     class SoftRender(torch.autograd.Function):
-        """blurred = render(points, colors, stop_offsets, stop_colors, sigma)."""
+        """blurred = render(points, colors, stop_offsets, stop_colors, sigma, opacity)."""
 
         @staticmethod
-        def forward(ctx, scenes, points, colors, stop_offsets, stop_colors, sigma):
+        def forward(ctx, scenes, points, colors, stop_offsets, stop_colors, sigma, opacity):
             params = {"points": points.contiguous(), "colors": colors.contiguous(),
                       "stop_offsets": stop_offsets.contiguous(), "stop_colors": stop_colors.contiguous(),
-                      "sigma": sigma.contiguous()}
+                      "sigma": sigma.contiguous(), "opacity": opacity.contiguous()}
             image, blurred = forward(scenes, params)
             ctx.scenes = scenes
             ctx.params = params
@@ -166,7 +168,7 @@ def _autograd():
         def backward(ctx, grad_blurred):
             (image,) = ctx.saved_tensors
             g = backward(ctx.scenes, image, grad_blurred, ctx.params)
-            return None, g["points"], g["colors"], g["stop_offsets"], g["stop_colors"], g["sigma"]
+            return None, g["points"], g["colors"], g["stop_offsets"], g["stop_colors"], g["sigma"], g["opacity"]
 
     return SoftRender
 
@@ -174,9 +176,9 @@ def _autograd():
 _SoftRender = None
 
 
-def render(scenes, points, colors, stop_offsets, stop_colors, sigma):
+def render(scenes, points, colors, stop_offsets, stop_colors, sigma, opacity):
     """Differentiable render (torch autograd) of the blurred composite."""
     global _SoftRender
     if _SoftRender is None:
         _SoftRender = _autograd()
-    return _SoftRender.apply(scenes, points, colors, stop_offsets, stop_colors, sigma)
+    return _SoftRender.apply(scenes, points, colors, stop_offsets, stop_colors, sigma, opacity)

@@ -23,7 +23,7 @@ def _loss(oracle_mod, arrays, target):
     return float(np.mean((bl - target.astype(np.float64)) ** 2))
 
 
-@pytest.mark.parametrize("group", ["points", "colors", "stop_offsets", "stop_colors", "sigma"])
+@pytest.mark.parametrize("group", ["points", "colors", "stop_offsets", "stop_colors", "sigma", "opacity"])
 def test_forward_mode_matches_fd(oracle_mod, small, group):
     a, t = small
     target = _target(oracle_mod, t)

@@ -13,7 +13,7 @@ from resvg_gb300 import soft
 
 pytestmark = pytest.mark.gpu
 
-GROUPS = ["points", "colors", "stop_offsets", "stop_colors", "sigma"]
+GROUPS = ["points", "colors", "stop_offsets", "stop_colors", "sigma", "opacity"]
 
 
 @pytest.fixture(scope="module")
@@ -108,7 +108,8 @@ def test_autograd_function_matches_direct_call(case):
     a, sc, target = case
     _, grads = _adjoint(sc, target)
     ps = {k: sc.params[k].clone().requires_grad_(True) for k in GROUPS}
-    out = soft.render(sc, ps["points"], ps["colors"], ps["stop_offsets"], ps["stop_colors"], ps["sigma"])
+    out = soft.render(sc, ps["points"], ps["colors"], ps["stop_offsets"], ps["stop_colors"], ps["sigma"],
+                      ps["opacity"])
     loss = ((out - target) ** 2).mean()
     loss.backward()
     for k in GROUPS:
