@@ -299,6 +299,29 @@ def set_tuning(band_rows: int = 0, pixels_per_thread: int = 0) -> None:
     check(lib().rgpu_set_tuning(C.byref(t)), "rgpu_set_tuning")
 
 
+def set_tuning_table(entries) -> None:
+    """Band rows per (max stream width, max stream draws) bucket, used for
+    streams whose band rows the tuning leaves automatic: entries are
+    (max_width, max_draws, band_rows) tuples, first match wins."""
+    L = lib()
+    L.rgpu_set_tuning_table.restype = C.c_int
+    L.rgpu_set_tuning_table.argtypes = [C.POINTER(_abi.TuningEntry), C.c_uint32]
+    arr = (_abi.TuningEntry * max(1, len(entries)))(*[_abi.TuningEntry(int(w), int(d), int(b), 0)
+                                                       for w, d, b in entries])
+    check(L.rgpu_set_tuning_table(arr, len(entries)), "rgpu_set_tuning_table")
+
+
+def get_tuning_table():
+    L = lib()
+    L.rgpu_get_tuning_table.restype = C.c_int
+    L.rgpu_get_tuning_table.argtypes = [C.POINTER(_abi.TuningEntry), C.c_uint32, C.POINTER(C.c_uint32)]
+    n = C.c_uint32(0)
+    check(L.rgpu_get_tuning_table(None, 0, C.byref(n)), "rgpu_get_tuning_table")
+    arr = (_abi.TuningEntry * max(1, n.value))()
+    check(L.rgpu_get_tuning_table(arr, n.value, C.byref(n)), "rgpu_get_tuning_table")
+    return [(e.max_width, e.max_draws, e.band_rows) for e in arr[:n.value]]
+
+
 def get_tuning():
     t = _abi.Tuning()
     check(lib().rgpu_get_tuning(C.byref(t)), "rgpu_get_tuning")

@@ -17,6 +17,88 @@ import numpy as np
 # per stream from its width.
 TUNING_CANDIDATES = [(0, 8), (0, 16), (1, 4), (2, 4), (4, 4), (2, 8), (4, 8), (8, 8), (4, 16), (8, 16)]
 
+# Buckets of the tuning table: stream width (canvas side) and draws (fills and
+# strokes), upper bounds; the band heights and pixels per thread searched.
+WIDTH_BUCKETS = (128, 256, 512, 1024, 32767)
+DRAW_BUCKETS = (64, 256, 1024, 1 << 30)
+BAND_CANDIDATES = (1, 2, 4, 8)
+PX_CANDIDATES = (4, 8, 16)
+
+
+def scene_draws(tree) -> int:
+    """Draws the flattener makes for a tree: one per fill and one per stroke."""
+    v = tree.view().contents
+    n = 0
+    for i in range(v.path_count):
+        p = v.paths[i]
+        n += (p.fill_paint >= 0) + (p.stroke_paint >= 0)
+    return n
+
+
+def bucket_of(width: float, draws: int):
+    wb = next((b for b in WIDTH_BUCKETS if width <= b), WIDTH_BUCKETS[-1])
+    db = next(b for b in DRAW_BUCKETS if draws <= b)
+    return wb, db
+
+
+def _time_scene(R, torch, trees, widths, heights, ptrs, stream, reps):
+    sc = R.Scene(trees, [(1, 0, 0, 1, 0, 0)] * len(trees), widths, heights, ptrs)
+    for _ in range(2):  # sizing, then graph capture
+        sc.render(stream.cuda_stream)
+    sc.check()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        sc.render(stream.cuda_stream)
+    e1.record(stream)
+    sc.check()
+    return e0.elapsed_time(e1) / reps
+
+
+def autotune_table(trees, widths, heights, device_ptrs, reps: int = 2, per_bucket: int = 24):
+    """The batched form's autotuner.  Scenes are grouped by (canvas-width
+    bucket, draw-count bucket); for every bucket the band height (rows per
+    raster work item, the tile height) is chosen by timing up to `per_bucket`
+    of its scenes under each candidate, then the pixels per thread (the tile
+    width is 256 / band rows x pixels per thread) by timing all of them under
+    the resulting table.  Installs the table and the tuning, and returns
+    (table, pixels per thread, {bucket: {band rows: ms}, "px": {px: ms}})."""
+    import torch
+    import resvg_gb300 as R
+    groups = {}
+    for i, t in enumerate(trees):
+        groups.setdefault(bucket_of(widths[i], scene_draws(t)), []).append(i)
+    stream = torch.cuda.Stream()
+    saved = R.get_tuning()
+    table, timings = [], {}
+    try:
+        for wb in WIDTH_BUCKETS:
+            for db in DRAW_BUCKETS:
+                idx = groups.get((wb, db), [])[:per_bucket]
+                if not idx:
+                    continue
+                sub = ([trees[i] for i in idx], [widths[i] for i in idx], [heights[i] for i in idx],
+                       [device_ptrs[i] for i in idx])
+                res = {}
+                for b in BAND_CANDIDATES:
+                    R.set_tuning(b, 0)
+                    res[b] = _time_scene(R, torch, *sub, stream, reps)
+                timings[(wb, db)] = res
+                table.append((wb, db, min(res, key=res.get)))
+        R.set_tuning(0, 0)
+        R.set_tuning_table(table)
+        px_ms = {}
+        for px in PX_CANDIDATES:
+            R.set_tuning(0, px)
+            px_ms[px] = _time_scene(R, torch, trees, widths, heights, device_ptrs, stream, reps)
+        best_px = min(px_ms, key=px_ms.get)
+        R.set_tuning(0, best_px)
+    except Exception:
+        R.set_tuning(*saved)
+        raise
+    timings["px"] = px_ms
+    return table, best_px, timings
+
 
 def scene_cost(width: float, height: float, paths: int) -> float:
     """Estimated raster cost of a scene: output pixels times path count (each

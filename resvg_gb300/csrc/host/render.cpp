@@ -104,8 +104,9 @@ struct HostBuf {
 };
 
 struct Tuning {
-    uint32_t band_rows = 0;  // 0: automatic
+    uint32_t band_rows = 0;  // 0: automatic (the table, else a rule on the stream width)
     uint32_t px = 0;         // pixels per thread: 0 automatic, else 4/8/16
+    std::vector<rgpu_tuning_entry> table;  // band rows by (stream width, stream draws) bucket
 };
 
 struct Buffers {
@@ -254,8 +255,13 @@ uint32_t pick_px(const SceneBuild &sb, const Tuning &tu) {
     for (auto &s : sb.streams) maxw = std::max(maxw, s.out_w);
     return maxw <= 512 ? 4 : (maxw <= 1024 ? 8 : 16);
 }
-uint32_t pick_bh(int32_t w, uint32_t px, const Tuning &tu) {
+uint32_t pick_bh(int32_t w, uint32_t draws, uint32_t px, const Tuning &tu) {
     if (tu.band_rows) return tu.band_rows;
+    for (const auto &e : tu.table)
+        if ((uint32_t)w <= e.max_width && draws <= e.max_draws) {
+            if (e.band_rows) return e.band_rows;
+            break;
+        }
     uint32_t bh = 1;
     while (bh < 8 && (256 / (bh * 2)) * px >= (uint32_t)w) bh *= 2;
     return bh;
@@ -278,7 +284,7 @@ int plan_scene(Context &c, Plan &p) {
             if (op == CMD_FILL || op == CMD_APPLY_REGION) sb.fill_cmds.push_back(ci);
         }
         st.fill_cnt = (uint32_t)sb.fill_cmds.size() - st.fill_off;
-        uint32_t bh = pick_bh(st.out_w, p.px, c.tuning);
+        uint32_t bh = pick_bh(st.out_w, st.draw_cnt, p.px, c.tuning);
         st.band_rows = bh;
         st.nbands = (uint32_t)((st.out_h + (int32_t)bh - 1) / (int32_t)bh);
         st.bin_off = (uint32_t)p.nbins;
@@ -874,6 +880,27 @@ int rgpu_set_tuning(const rgpu_tuning *t) {
     std::lock_guard<std::mutex> lock(c.mu);
     c.tuning.band_rows = t->band_rows;
     c.tuning.px = t->pixels_per_thread;
+    return RGPU_OK;
+}
+
+int rgpu_set_tuning_table(const rgpu_tuning_entry *entries, uint32_t count) {
+    if (count && !entries) return RGPU_ERR_INVALID_ARG;
+    for (uint32_t i = 0; i < count; i++) {
+        const uint32_t b = entries[i].band_rows;
+        if (b && b != 1 && b != 2 && b != 4 && b != 8) return RGPU_ERR_INVALID_ARG;
+    }
+    Context &c = ctx();
+    std::lock_guard<std::mutex> lock(c.mu);
+    c.tuning.table.assign(entries, entries + count);
+    return RGPU_OK;
+}
+
+int rgpu_get_tuning_table(rgpu_tuning_entry *entries, uint32_t capacity, uint32_t *count) {
+    if (!count || (capacity && !entries)) return RGPU_ERR_INVALID_ARG;
+    Context &c = ctx();
+    std::lock_guard<std::mutex> lock(c.mu);
+    *count = (uint32_t)c.tuning.table.size();
+    for (uint32_t i = 0; i < capacity && i < *count; i++) entries[i] = c.tuning.table[i];
     return RGPU_OK;
 }
 

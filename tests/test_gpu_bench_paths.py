@@ -202,3 +202,29 @@ def test_autotuned_tuning_renders_exactly(tuning_case):
             assert diff_stats(db.image(i), ref) == (0, 0), "autotuned %s: slot %d differs" % (best, i)
     finally:
         R.set_tuning(*saved)
+
+
+def test_tuning_table_autotuner_renders_exactly(tuning_case):
+    """The bench's autotuner: band rows per (width, draws) bucket, then pixels
+    per thread; the batch it tunes renders bit-exactly under the table."""
+    import torch
+    from resvg_gb300 import batch as BT
+    trees, refs = tuning_case
+    saved = R.get_tuning()
+    try:
+        db = _DeviceBatch(trees)
+        table, px, timings = BT.autotune_table(trees, db.ws, db.hs, db.ptrs, reps=1)
+        assert table and px in BT.PX_CANDIDATES
+        assert R.get_tuning_table() == [tuple(e) for e in table]
+        assert all(b in BT.BAND_CANDIDATES for _, _, b in table)
+        scene = R.Scene(trees, [IDENT] * len(trees), db.ws, db.hs, db.ptrs)
+        for _ in range(3):
+            db.buf.zero_()
+            torch.cuda.synchronize()
+            scene.render()
+            scene.check()
+        for i, ref in enumerate(refs):
+            assert diff_stats(db.image(i), ref) == (0, 0), "table %s px %d: slot %d differs" % (table, px, i)
+    finally:
+        R.set_tuning_table([])
+        R.set_tuning(*saved)

@@ -3,9 +3,9 @@
 `test_fixtures_match` replays the committed fixtures (a subset of resvg's
 integration suite, tests/golden/fixtures.npz) through the SVG-subset front
 end and the oracle and requires zero differing pixels under the suite's rule.
-`test_full_suite_summary` reruns the whole comparison when a resvg checkout is
-available (RESVG_REFERENCE, or the default location of the read-only
-checkout) and checks that no test that passed in the committed summary
+`test_full_suite_summary` reruns the whole comparison only when the
+environment variable RESVG_REFERENCE names a resvg checkout (it is skipped
+otherwise) and checks that no test that passed in the committed summary
 (tests/golden/oracle_pin.json) regressed.
 """
 import json
