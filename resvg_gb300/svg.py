@@ -32,24 +32,54 @@ class Unsupported(Exception):
 
 
 # ---------------------------------------------------------------- colours
+# the CSS Color Module keywords (the SVG 1.1 set plus rebeccapurple)
 NAMED = {
-    "black": (0, 0, 0), "white": (255, 255, 255), "red": (255, 0, 0), "green": (0, 128, 0), "blue": (0, 0, 255),
-    "yellow": (255, 255, 0), "cyan": (0, 255, 255), "aqua": (0, 255, 255), "magenta": (255, 0, 255),
-    "fuchsia": (255, 0, 255), "gray": (128, 128, 128), "grey": (128, 128, 128), "silver": (192, 192, 192),
-    "maroon": (128, 0, 0), "olive": (128, 128, 0), "lime": (0, 255, 0), "teal": (0, 128, 128), "navy": (0, 0, 128),
-    "purple": (128, 0, 128), "orange": (255, 165, 0), "pink": (255, 192, 203), "brown": (165, 42, 42),
-    "gold": (255, 215, 0), "seagreen": (46, 139, 87), "darkgreen": (0, 100, 0), "lightblue": (173, 216, 230),
-    "lightgreen": (144, 238, 144), "darkblue": (0, 0, 139), "darkred": (139, 0, 0), "indigo": (75, 0, 130),
-    "violet": (238, 130, 238), "coral": (255, 127, 80), "salmon": (250, 128, 114), "khaki": (240, 230, 140),
-    "crimson": (220, 20, 60), "chocolate": (210, 105, 30), "tomato": (255, 99, 71), "orchid": (218, 112, 214),
-    "skyblue": (135, 206, 235), "steelblue": (70, 130, 180), "springgreen": (0, 255, 127),
-    "mediumseagreen": (60, 179, 113), "forestgreen": (34, 139, 34), "limegreen": (50, 205, 50),
-    "darkgray": (169, 169, 169), "darkgrey": (169, 169, 169), "lightgray": (211, 211, 211),
-    "lightgrey": (211, 211, 211), "whitesmoke": (245, 245, 245), "beige": (245, 245, 220),
-    "turquoise": (64, 224, 208), "royalblue": (65, 105, 225), "slateblue": (106, 90, 205),
-    "darkorange": (255, 140, 0), "goldenrod": (218, 165, 32), "peru": (205, 133, 63), "plum": (221, 160, 221),
-    "tan": (210, 180, 140), "wheat": (245, 222, 179), "ivory": (255, 255, 240), "lavender": (230, 230, 250),
-    "mintcream": (245, 255, 250), "honeydew": (240, 255, 240), "azure": (240, 255, 255),
+    "aliceblue": (240, 248, 255), "antiquewhite": (250, 235, 215), "aqua": (0, 255, 255),
+    "aquamarine": (127, 255, 212), "azure": (240, 255, 255), "beige": (245, 245, 220), "bisque": (255, 228, 196),
+    "black": (0, 0, 0), "blanchedalmond": (255, 235, 205), "blue": (0, 0, 255), "blueviolet": (138, 43, 226),
+    "brown": (165, 42, 42), "burlywood": (222, 184, 135), "cadetblue": (95, 158, 160),
+    "chartreuse": (127, 255, 0), "chocolate": (210, 105, 30), "coral": (255, 127, 80),
+    "cornflowerblue": (100, 149, 237), "cornsilk": (255, 248, 220), "crimson": (220, 20, 60),
+    "cyan": (0, 255, 255), "darkblue": (0, 0, 139), "darkcyan": (0, 139, 139), "darkgoldenrod": (184, 134, 11),
+    "darkgray": (169, 169, 169), "darkgreen": (0, 100, 0), "darkgrey": (169, 169, 169),
+    "darkkhaki": (189, 183, 107), "darkmagenta": (139, 0, 139), "darkolivegreen": (85, 107, 47),
+    "darkorange": (255, 140, 0), "darkorchid": (153, 50, 204), "darkred": (139, 0, 0),
+    "darksalmon": (233, 150, 122), "darkseagreen": (143, 188, 143), "darkslateblue": (72, 61, 139),
+    "darkslategray": (47, 79, 79), "darkslategrey": (47, 79, 79), "darkturquoise": (0, 206, 209),
+    "darkviolet": (148, 0, 211), "deeppink": (255, 20, 147), "deepskyblue": (0, 191, 255),
+    "dimgray": (105, 105, 105), "dimgrey": (105, 105, 105), "dodgerblue": (30, 144, 255),
+    "firebrick": (178, 34, 34), "floralwhite": (255, 250, 240), "forestgreen": (34, 139, 34),
+    "fuchsia": (255, 0, 255), "gainsboro": (220, 220, 220), "ghostwhite": (248, 248, 255),
+    "gold": (255, 215, 0), "goldenrod": (218, 165, 32), "gray": (128, 128, 128), "grey": (128, 128, 128),
+    "green": (0, 128, 0), "greenyellow": (173, 255, 47), "honeydew": (240, 255, 240),
+    "hotpink": (255, 105, 180), "indianred": (205, 92, 92), "indigo": (75, 0, 130), "ivory": (255, 255, 240),
+    "khaki": (240, 230, 140), "lavender": (230, 230, 250), "lavenderblush": (255, 240, 245),
+    "lawngreen": (124, 252, 0), "lemonchiffon": (255, 250, 205), "lightblue": (173, 216, 230),
+    "lightcoral": (240, 128, 128), "lightcyan": (224, 255, 255), "lightgoldenrodyellow": (250, 250, 210),
+    "lightgray": (211, 211, 211), "lightgreen": (144, 238, 144), "lightgrey": (211, 211, 211),
+    "lightpink": (255, 182, 193), "lightsalmon": (255, 160, 122), "lightseagreen": (32, 178, 170),
+    "lightskyblue": (135, 206, 250), "lightslategray": (119, 136, 153), "lightslategrey": (119, 136, 153),
+    "lightsteelblue": (176, 196, 222), "lightyellow": (255, 255, 224), "lime": (0, 255, 0),
+    "limegreen": (50, 205, 50), "linen": (250, 240, 230), "magenta": (255, 0, 255), "maroon": (128, 0, 0),
+    "mediumaquamarine": (102, 205, 170), "mediumblue": (0, 0, 205), "mediumorchid": (186, 85, 211),
+    "mediumpurple": (147, 112, 219), "mediumseagreen": (60, 179, 113), "mediumslateblue": (123, 104, 238),
+    "mediumspringgreen": (0, 250, 154), "mediumturquoise": (72, 209, 204), "mediumvioletred": (199, 21, 133),
+    "midnightblue": (25, 25, 112), "mintcream": (245, 255, 250), "mistyrose": (255, 228, 225),
+    "moccasin": (255, 228, 181), "navajowhite": (255, 222, 173), "navy": (0, 0, 128),
+    "oldlace": (253, 245, 230), "olive": (128, 128, 0), "olivedrab": (107, 142, 35), "orange": (255, 165, 0),
+    "orangered": (255, 69, 0), "orchid": (218, 112, 214), "palegoldenrod": (238, 232, 170),
+    "palegreen": (152, 251, 152), "paleturquoise": (175, 238, 238), "palevioletred": (219, 112, 147),
+    "papayawhip": (255, 239, 213), "peachpuff": (255, 218, 185), "peru": (205, 133, 63), "pink": (255, 192, 203),
+    "plum": (221, 160, 221), "powderblue": (176, 224, 230), "purple": (128, 0, 128),
+    "rebeccapurple": (102, 51, 153), "red": (255, 0, 0), "rosybrown": (188, 143, 143),
+    "royalblue": (65, 105, 225), "saddlebrown": (139, 69, 19), "salmon": (250, 128, 114),
+    "sandybrown": (244, 164, 96), "seagreen": (46, 139, 87), "seashell": (255, 245, 238),
+    "sienna": (160, 82, 45), "silver": (192, 192, 192), "skyblue": (135, 206, 235),
+    "slateblue": (106, 90, 205), "slategray": (112, 128, 144), "slategrey": (112, 128, 144),
+    "snow": (255, 250, 250), "springgreen": (0, 255, 127), "steelblue": (70, 130, 180), "tan": (210, 180, 140),
+    "teal": (0, 128, 128), "thistle": (216, 191, 216), "tomato": (255, 99, 71), "turquoise": (64, 224, 208),
+    "violet": (238, 130, 238), "wheat": (245, 222, 179), "white": (255, 255, 255),
+    "whitesmoke": (245, 245, 245), "yellow": (255, 255, 0), "yellowgreen": (154, 205, 50),
 }
 
 
@@ -532,6 +562,73 @@ def mat_mul(a, b):
 IDENT = (1.0, 0.0, 0.0, 1.0, 0.0, 0.0)
 
 
+def _f32(v):
+    return float(np.float32(v))
+
+
+def sk_concat(a, b):
+    """tiny-skia Transform::concat(a, b) = a * b on f32 components: a scale
+    and translate pair multiplies in f32, otherwise each entry is a sum of two
+    products in f64 rounded once to f32, then the translation added in f32."""
+    if a == IDENT:
+        return b
+    if b == IDENT:
+        return a
+    if a[1] == 0 and a[2] == 0 and b[1] == 0 and b[2] == 0:
+        return (_f32(a[0] * b[0]), 0.0, 0.0, _f32(a[3] * b[3]),
+                _f32(_f32(a[0] * b[4]) + a[4]), _f32(_f32(a[3] * b[5]) + a[5]))
+    return (_f32(a[0] * b[0] + a[2] * b[1]), _f32(a[1] * b[0] + a[3] * b[1]),
+            _f32(a[0] * b[2] + a[2] * b[3]), _f32(a[1] * b[2] + a[3] * b[3]),
+            _f32(_f32(a[0] * b[4] + a[2] * b[5]) + a[4]), _f32(_f32(a[1] * b[4] + a[3] * b[5]) + a[5]))
+
+
+def sk_rotate(deg):
+    """tiny-skia Transform::from_rotate: degrees to radians and cos / sin in f32."""
+    f = np.float32
+    v = f(deg) * (f(math.pi) / f(180.0))
+    c, s = float(np.cos(f(v))), float(np.sin(f(v)))
+    return (c, s, -s, c, 0.0, 0.0)
+
+
+def ulps_eq(a, b, ulps=4):
+    """float-cmp approx_eq_ulps on f32: equal, or of one sign and at most
+    `ulps` representable values apart."""
+    a, b = np.float32(a), np.float32(b)
+    if a == b:
+        return True
+    if np.signbit(a) != np.signbit(b):
+        return False
+    ia, ib = int(a.view(np.int32)), int(b.view(np.int32))
+    return abs(ia - ib) <= ulps
+
+
+def paint_order(v):
+    """svgtypes PaintOrder: up to three of fill / stroke / markers, the missing
+    ones appended in the default order (fill, stroke, markers); `normal`, an
+    unknown word, a repeated word or trailing data give the default order."""
+    default = ["fill", "stroke", "markers"]
+    words = (v or "").split()
+    if not words or len(words) > 3 or any(w not in default for w in words) or len(set(words)) != len(words):
+        return default
+    return words + [w for w in default if w not in words]
+
+
+def parse_angle_deg(s):
+    """svgtypes Angle in degrees: a number with an optional deg, grad, rad or
+    turn unit; None when it does not parse."""
+    m = re.fullmatch(r"\s*([+-]?(?:\d+\.?\d*|\.\d+)(?:[eE][+-]?\d+)?)(deg|grad|rad|turn)?\s*", s or "")
+    if not m:
+        return None
+    v, unit = float(m.group(1)), m.group(2)
+    if unit == "grad":
+        return v * 180.0 / 200.0
+    if unit == "rad":
+        return math.degrees(v)
+    if unit == "turn":
+        return v * 360.0
+    return v
+
+
 def parse_transform(s):
     ts = IDENT
     for name, args in re.findall(r"(\w+)\s*\(([^)]*)\)", s or ""):
@@ -833,6 +930,170 @@ def parse_path_data(d: str) -> PathB:
 
 
 # ---------------------------------------------------------------- tight bounds (usvg compute_tight_bounds)
+# ---------------------------------------------------------------- markers
+def marker_segments(verbs, pts):
+    """The path as usvg's marker code walks it (marker.rs:128-160): moves,
+    lines, cubics (a quad raised to a cubic in f32) and closes; each segment
+    ("M", p), ("L", p), ("C", p1, p2, p) or ("Z",)."""
+    f = np.float32
+    segs, k = [], 0
+    prev = prev_move = (0.0, 0.0)
+    for v in verbs:
+        if v == A.MOVE:
+            p = (pts[k], pts[k + 1])
+            k += 2
+            segs.append(("M", p))
+            prev = prev_move = p
+        elif v == A.LINE:
+            p = (pts[k], pts[k + 1])
+            k += 2
+            segs.append(("L", p))
+            prev = p
+        elif v == A.QUAD:
+            c, p = (pts[k], pts[k + 1]), (pts[k + 2], pts[k + 3])
+            k += 4
+            lift = lambda a, b: float(f(f(f(a) + f(f(b) * f(2.0))) / f(3.0)))  # noqa: E731
+            segs.append(("C", (lift(prev[0], c[0]), lift(prev[1], c[1])), (lift(p[0], c[0]), lift(p[1], c[1])), p))
+            prev = p
+        elif v == A.CUBIC:
+            c1, c2, p = (pts[k], pts[k + 1]), (pts[k + 2], pts[k + 3]), (pts[k + 4], pts[k + 5])
+            k += 6
+            segs.append(("C", c1, c2, p))
+            prev = p
+        else:
+            segs.append(("Z",))
+            prev = prev_move
+    return segs
+
+
+def _subpath_start(segs, idx):
+    for i in range(idx - 1, -1, -1):
+        if segs[i][0] == "M":
+            return segs[i][1]
+    return (0.0, 0.0)
+
+
+def _prev_vertex(segs, idx):
+    s = segs[idx - 1]
+    return _subpath_start(segs, idx) if s[0] == "Z" else s[-1]
+
+
+def _bisector_deg(x1, y1, x2, y2, x3, y3, x4, y4):
+    """Direction halfway between the incoming (1->2) and outgoing (3->4)
+    vectors, in degrees within [0, 360), computed in f32 (marker.rs calc_angle)."""
+    f = np.float32
+    two_pi = f(math.pi) * f(2.0)
+
+    def norm(r):
+        v = np.fmod(f(r), two_pi)
+        return f(v + two_pi) if v < 0 else f(v)
+
+    def vec(vx, vy):
+        r = np.arctan2(f(vy), f(vx))
+        return f(0.0) if np.isnan(r) else norm(r)
+    a_in = vec(f(x2) - f(x1), f(y2) - f(y1))
+    a_out = vec(f(x4) - f(x3), f(y4) - f(y3))
+    d = f(f(a_out - a_in) * f(0.5))
+    ang = f(a_in + d)
+    if f(math.pi / 2) < abs(d):
+        ang = f(ang - f(math.pi))
+    return f(norm(ang) * f(57.29577951308232))
+
+
+def _line_deg(x1, y1, x2, y2):
+    return _bisector_deg(x1, y1, x2, y2, x1, y1, x2, y2)
+
+
+def _curves_deg(px, py, cx1, cy1, x, y, cx2, cy2, nx, ny):
+    if ulps_eq(cx1, x) and ulps_eq(cy1, y):
+        return _bisector_deg(px, py, x, y, x, y, cx2, cy2)
+    if ulps_eq(x, cx2) and ulps_eq(y, cy2):
+        return _bisector_deg(cx1, cy1, x, y, x, y, nx, ny)
+    return _bisector_deg(cx1, cy1, x, y, x, y, cx2, cy2)
+
+
+def marker_vertex_angle(segs, idx):
+    """The orient="auto" angle at vertex `idx` (marker.rs calc_vertex_angle):
+    the first vertex follows the first segment, the last the last segment, a
+    middle one bisects the incoming and outgoing tangents."""
+    f = np.float32
+    n = len(segs)
+    if idx == 0:
+        s1, s2 = segs[0], segs[1]
+        if s1[0] == "M" and s2[0] == "L":
+            return _line_deg(*s1[1], *s2[1])
+        if s1[0] == "M" and s2[0] == "C":
+            pm, p1, p = s1[1], s2[1], s2[3]
+            if ulps_eq(pm[0], p1[0]) and ulps_eq(pm[1], p1[1]):
+                return _line_deg(*pm, *p)
+            return _line_deg(*pm, *p1)
+        return f(0.0)
+    if idx == n - 1:
+        s1, s2 = segs[idx - 1], segs[idx]
+        if s2[0] == "M":
+            return f(0.0)
+        if s2[0] == "L":
+            return _line_deg(*_prev_vertex(segs, idx), *s2[1])
+        if s2[0] == "C":
+            p1, p2, p = s2[1], s2[2], s2[3]
+            if ulps_eq(p2[0], p[0]) and ulps_eq(p2[1], p[1]):
+                return _line_deg(*p1, *p)
+            return _line_deg(*p2, *p)
+        if s1[0] == "L":
+            return _line_deg(*s1[1], *_subpath_start(segs, idx))
+        if s1[0] == "C":
+            nxt = _subpath_start(segs, idx)
+            return _curves_deg(*_prev_vertex(segs, idx), *s1[2], *s1[3], *nxt, *nxt)
+        return f(0.0)
+    s1, s2 = segs[idx], segs[idx + 1]
+    k1, k2 = s1[0], s2[0]
+    if k1 == "M" and k2 == "L":
+        return _line_deg(*s1[1], *s2[1])
+    if k1 == "M" and k2 == "C":
+        return _line_deg(*s1[1], *s2[1])
+    if k1 == "L" and k2 == "L":
+        pv = _prev_vertex(segs, idx)
+        return _bisector_deg(*pv, *s1[1], *s1[1], *s2[1])
+    if k1 == "C" and k2 == "C":
+        return _curves_deg(*_prev_vertex(segs, idx), *s1[2], *s1[3], *s2[1], *s2[3])
+    if k1 == "L" and k2 == "C":
+        pv = _prev_vertex(segs, idx)
+        return _curves_deg(*pv, *pv, *s1[1], *s2[1], *s2[3])
+    if k1 == "C" and k2 == "L":
+        return _curves_deg(*_prev_vertex(segs, idx), *s1[2], *s1[3], *s2[1], *s2[1])
+    if k1 == "L" and k2 == "M":
+        return _line_deg(*_prev_vertex(segs, idx), *s1[1])
+    if k1 == "C" and k2 == "M":
+        p2, p = s1[2], s1[3]
+        if ulps_eq(p[0], p2[0]) and ulps_eq(p[1], p2[1]):
+            return _line_deg(*_prev_vertex(segs, idx), *p)
+        return _line_deg(*p2, *p)
+    if k1 == "L" and k2 == "Z":
+        pv, nx = _prev_vertex(segs, idx), _subpath_start(segs, idx)
+        return _bisector_deg(*pv, *s1[1], *s1[1], *nx)
+    if k2 == "Z" and k1 != "Z":
+        return _line_deg(*_prev_vertex(segs, idx), *_subpath_start(segs, idx))
+    return f(0.0)
+
+
+def marker_vertices(segs, kind):
+    """(point, vertex index) pairs a start / mid / end marker is drawn at
+    (marker.rs draw_markers)."""
+    if not segs:
+        return []
+    if kind == "start":
+        return [(segs[0][1], 0)] if segs[0][0] == "M" else []
+    if kind == "mid":
+        return [(segs[i][-1], i) for i in range(1, len(segs) - 1) if segs[i][0] != "Z"]
+    last = len(segs) - 1
+    s = segs[last]
+    if s[0] in ("L", "C"):
+        return [(s[-1], last)]
+    if s[0] == "Z":
+        return [(_subpath_start(segs, last), last)]
+    return []
+
+
 def tight_bounds(verbs, pts):
     xs, ys = [], []
     P = [(pts[2 * k], pts[2 * k + 1]) for k in range(len(pts) // 2)]
@@ -893,7 +1154,7 @@ INHERITED = {"fill", "fill-opacity", "fill-rule", "stroke", "stroke-width", "str
              "shape-rendering", "clip-rule", "color", "color-interpolation-filters", "paint-order", "font-size"}
 NON_INHERITED = {"opacity", "clip-path", "mask", "filter", "mix-blend-mode", "isolation", "display",
                  "stop-color", "stop-opacity", "flood-color", "flood-opacity", "transform"}
-UNSUPPORTED_ELEMS = {"text", "marker", "switch", "foreignObject", "tspan", "textPath", "symbol",
+UNSUPPORTED_ELEMS = {"text", "switch", "foreignObject", "tspan", "textPath", "symbol",
                      "animate", "set"}
 BLEND = {"normal": "source-over", "multiply": "multiply", "screen": "screen", "overlay": "overlay",
          "darken": "darken", "lighten": "lighten", "color-dodge": "color-dodge", "color-burn": "color-burn",
@@ -1018,6 +1279,13 @@ class Loader:
             if e.get("systemLanguage") is not None:
                 raise Unsupported("systemLanguage")
         self.clip_cache, self.mask_cache, self.filter_cache = {}, {}, {}
+        # markers being converted (a marker inside its own content is skipped;
+        # nodes made for markers carry no id), and the (fill, stroke) that
+        # context-fill / context-stroke resolve to: a solid paint index, None,
+        # or "server" for a gradient or pattern
+        self.marker_stack = []
+        self.ctx = None
+        self.solid_ids = set()
         self.ids_out = {}  # SVG id -> the oracle's node id ("<group>" or "p<path>")
 
     # ---- attributes with style and inheritance
@@ -1028,16 +1296,18 @@ class Loader:
         a = dict(e.attrib)
         st = a.pop("style", None)
         important = {}
+        # the `marker` shorthand sets marker-start, -mid and -end, in CSS only
+        # (svgtree/parse.rs write_declaration); as an XML attribute it is ignored
+        def put(d, k, v):
+            for kk in (("marker-start", "marker-mid", "marker-end") if k == "marker" else (k,)):
+                d[kk] = v
         for k, v, imp in self.css.get(e, ()):
-            if imp:
-                important[k] = v
-            else:
-                a[k] = v
+            put(important if imp else a, k, v)
         if st:
             for part in st.split(";"):
                 if ":" in part:
                     k, v = part.split(":", 1)
-                    a[k.strip()] = v.strip()
+                    put(a, k.strip(), v.strip())
         a.update(important)
         return a
 
@@ -1168,7 +1438,7 @@ class Builder(Loader):
     def node(self, e, parent, transform_extra=IDENT):
         tag = _tag(e)
         if tag in ("defs", "linearGradient", "radialGradient", "clipPath", "mask", "filter", "title", "desc",
-                   "metadata", "stop", "pattern", "style"):
+                   "metadata", "stop", "pattern", "style", "marker"):
             return
         if not self.visible(e):
             return
@@ -1204,11 +1474,16 @@ class Builder(Loader):
                 if n is ref:
                     return
                 n = self.parent.get(n)
-            saved = self.parent.get(ref)
+            # use_node.rs convert: the <use> element's fill and stroke are the
+            # context paints of what it instances
+            ctx = (self.context_paint(e, "fill"), self.context_paint(e, "stroke"))
+            saved, saved_ctx = self.parent.get(ref), self.ctx
             self.parent[ref] = e
+            self.ctx = ctx
             try:
                 self.node(ref, g)
             finally:
+                self.ctx = saved_ctx
                 if saved is None:
                     self.parent.pop(ref, None)
                 else:
@@ -1276,6 +1551,8 @@ class Builder(Loader):
         clip = None if clip == "missing" else clip
         mask = None if mask == "missing" else mask
         eid = e.get("id")
+        if self.marker_stack:
+            eid = None  # nodes made for markers carry no id
         keep_id = eid is not None and _tag(e) in ("g", "use")
         needs = ts != IDENT or opacity != 1.0 or clip is not None or mask is not None or filt or \
             blend != "source-over" or isolate or keep_id
@@ -1469,7 +1746,14 @@ class Builder(Loader):
             return self.solid(c), opacity * c[1]
         invalid = (self.solid(((0, 0, 0), 1.0)), opacity) if which == "fill" else None
         if v in ("context-fill", "context-stroke"):
-            raise Unsupported("paint " + v)
+            # style.rs convert_paint: the context element's paint; its own
+            # opacity is not carried over
+            c = None if self.ctx is None else self.ctx[0 if v == "context-fill" else 1]
+            if c is None:
+                return None
+            if c == "server":
+                raise Unsupported("context paint server")
+            return c, opacity
         if v.startswith("url("):
             m = re.match(r"url\(\s*['\"]?#([^'\")]+)['\"]?\s*\)\s*(.*)$", v)
             if not m:
@@ -1583,7 +1867,32 @@ class Builder(Loader):
         p.kind = A.PAINT_SOLID
         p.r, p.g, p.b = c[0]
         p.transform = A.Transform.identity()
-        return self.tree.add_paint(p)
+        i = self.tree.add_paint(p)
+        self.solid_ids.add(i)
+        return i
+
+    def context_paint(self, e, which, width=None):
+        """What an element hands to context-fill / context-stroke: its solid
+        paint index, None, or "server" for a gradient or pattern (those are
+        resolved against the context element's box, not supported here).  A
+        stroke needs a positive stroke-width (style.rs resolve_stroke)."""
+        if which == "stroke":
+            if width is None:
+                sw = self.get(e, "stroke-width")
+                width = parse_length(sw, math.hypot(self.vbw, self.vbh) / math.sqrt(2), self.font_size(e)) \
+                    if sw else 1.0
+            if not width > 0:
+                return None
+        v = (self.get(e, which) or "").strip()
+        if v.startswith("url("):
+            m = re.match(r"url\(\s*['\"]?#([^'\")]+)['\"]?\s*\)", v)
+            ref = self.ids.get(m.group(1)) if m else None
+            if ref is not None and _tag(ref) in ("linearGradient", "radialGradient", "pattern"):
+                return "server"
+        r = self.paint(e, which, None, which + "-opacity")
+        if r is None:
+            return None
+        return r[0] if r[0] in self.solid_ids else "server"
 
     def grad_attr(self, e, name, chain):
         """usvg resolve_attr: the gradient attributes through the href chain;
@@ -1720,8 +2029,9 @@ class Builder(Loader):
         path.visible = 1 if vis == "visible" else 0
         sr = (self.get(e, "shape-rendering") or "geometricPrecision").strip()
         path.anti_alias = 0 if sr in ("crispEdges", "optimizeSpeed") else 1
-        po = (self.get(e, "paint-order") or "normal").strip().split()
-        path.stroke_first = 1 if po and po[0] == "stroke" else 0
+        order = paint_order(self.get(e, "paint-order"))
+        # converter.rs svg_paint_order_to_usvg
+        path.stroke_first = 1 if order[0] == "stroke" or order[:2] == ["markers", "stroke"] else 0
         fill = self.paint(e, "fill", bbox, "fill-opacity")
         if fill is not None:
             path.fill_paint, path.fill_opacity = fill[0], float(np.float32(fill[1]))
@@ -1750,14 +2060,135 @@ class Builder(Loader):
                         dashes = dashes * 2
                     do = self.get(e, "stroke-dashoffset")
                     path.dash_phase = float(parse_length(do, self.vbw, fsz)) if do else 0.0
-        if path.fill_paint < 0 and path.stroke_paint < 0:
+        links = self.marker_links(e) if vis == "visible" else []
+        if path.fill_paint < 0 and path.stroke_paint < 0 and not links:
             return
         if path.stroke_paint < 0:
             path.stroke_width = 1.0
-        pi = self.tree.add_path(parent, path, verbs, pts, dashes)
-        if e.get("id"):
-            self.ids_out.setdefault(e.get("id"), "p%d" % pi)
-            self.tree.set_node_id(A.NODE_PATH, pi, e.get("id"))
+
+        def add(p, d, with_id):
+            if p.fill_paint < 0 and p.stroke_paint < 0:
+                return
+            pi = self.tree.add_path(parent, p, verbs, pts, d)
+            if with_id and e.get("id") and not self.marker_stack:
+                self.ids_out.setdefault(e.get("id"), "p%d" % pi)
+                self.tree.set_node_id(A.NODE_PATH, pi, e.get("id"))
+        if not links:
+            add(path, dashes, True)
+            return
+
+        def single(which):
+            # converter.rs append_single_paint_path: one paint, no id
+            p = A.Path.from_buffer_copy(path)
+            if which == "fill":
+                p.stroke_paint, p.stroke_width = -1, 1.0
+                add(p, [], False)
+            elif which == "stroke":
+                p.fill_paint = -1
+                add(p, dashes, False)
+
+        def ctx_of(i):
+            return None if i < 0 else (i if i in self.solid_ids else "server")
+        ctx = (ctx_of(path.fill_paint), ctx_of(path.stroke_paint))
+
+        def markers():
+            mg = self.tree.add_group(parent, _group())
+            segs = marker_segments(verbs, pts)
+            for kind, m in links:
+                self.marker(e, segs, m, kind, mg, ctx)
+        # converter.rs convert_path: the marker group before, between or
+        # after the painted path by paint-order
+        if order[0] == "markers":
+            markers()
+            add(path, dashes, True)
+        elif order[1] == "markers":
+            single(order[0])
+            markers()
+            single(order[2])
+        else:
+            add(path, dashes, True)
+            markers()
+
+    def marker_links(self, e):
+        """[(kind, <marker> element)] for marker-start, -mid and -end, skipping
+        links to anything but a marker and markers already being drawn
+        (marker.rs convert)."""
+        out = []
+        for kind in ("start", "mid", "end"):
+            v = self.get(e, "marker-" + kind)
+            if not v or v.strip() == "none":
+                continue
+            m = re.match(r"\s*url\(\s*['\"]?#([^'\")]+)['\"]?\s*\)", v)
+            ref = self.ids.get(m.group(1)) if m else None
+            if ref is None or _tag(ref) != "marker" or any(ref is x for x in self.marker_stack):
+                continue
+            out.append((kind, ref))
+        return out
+
+    def marker(self, e, segs, m, kind, mg, ctx):
+        """One marker-start / -mid / -end of a shape as usvg resolves it
+        (marker.rs resolve): at every vertex of its kind a group under `mg`
+        holding the marker's content, transformed by translate(vertex) .
+        rotate(orient) . scale(the viewBox scale of the marker box, or the
+        stroke scale) . translate(-refX, -refY), and clipped to the viewBox
+        or marker box unless overflow is visible or auto."""
+        f = np.float32
+        a = self.attrs(m)
+        if (m.get("markerUnits") or "").strip() == "userSpaceOnUse":
+            scale = 1.0
+        else:
+            sw = self.get(e, "stroke-width")
+            scale = parse_length(sw, math.hypot(self.vbw, self.vbh) / math.sqrt(2), self.font_size(e)) if sw else 1.0
+        scale = _f32(scale)
+        if not (scale > 0 and math.isfinite(scale)):
+            return
+        rx, ry = _f32(self.num(m, "refX", 0.0, self.vbw)), _f32(self.num(m, "refY", 0.0, self.vbh))
+        mw, mh = _f32(self.num(m, "markerWidth", 3.0, self.vbw)), _f32(self.num(m, "markerHeight", 3.0, self.vbh))
+        if not (mw > 0 and mh > 0 and math.isfinite(mw) and math.isfinite(mh)):
+            return
+        vb = numbers(m.get("viewBox")) if m.get("viewBox") is not None else None
+        if vb is not None and (len(vb) != 4 or not (vb[2] > 0 and vb[3] > 0)):
+            vb = None
+        ov = a.get("overflow")
+        ci = -1
+        if ov is None or ov.strip() in ("hidden", "scroll"):
+            root = self.tree.add_group(-1, _group())
+            rect = tuple(_f32(v) for v in vb) if vb is not None else (0.0, 0.0, mw, mh)
+            self.rect_path(root, rect, self.solid(((0, 0, 0), 1.0)))
+            c = A.Clip()
+            c.transform = _tf(IDENT)
+            c.clip_path = -1
+            c.root = root
+            ci = self.tree.add_clip(c)
+        orient = (m.get("orient") or "").strip()
+        for p, idx in marker_vertices(segs, kind):
+            ts = (1.0, 0.0, 0.0, 1.0, _f32(p[0]), _f32(p[1]))
+            if orient == "auto-start-reverse" and idx == 0:
+                ang = f(np.fmod(f(marker_vertex_angle(segs, idx) + f(180.0)), f(360.0)))
+            elif orient in ("auto", "auto-start-reverse"):
+                ang = marker_vertex_angle(segs, idx)
+            else:
+                d = parse_angle_deg(orient)
+                ang = f(d) if d is not None else f(0.0)
+            if not ulps_eq(ang, 0.0):
+                ts = sk_concat(ts, sk_rotate(ang))
+            if vb is not None:
+                vt = view_box_transform(vb, m.get("preserveAspectRatio") or "", float(f(mw) * f(scale)),
+                                        float(f(mh) * f(scale)))
+                ts = sk_concat(ts, (abs(vt[0]), 0.0, 0.0, abs(vt[3]), 0.0, 0.0))
+            else:
+                ts = sk_concat(ts, (scale, 0.0, 0.0, scale, 0.0, 0.0))
+            ts = sk_concat(ts, (1.0, 0.0, 0.0, 1.0, -rx, -ry))
+            gi = self.tree.add_group(mg, _group(transform=_tf(ts), clip_path=ci))
+            saved = self.ctx
+            self.marker_stack.append(m)
+            self.ctx = ctx
+            try:
+                for c in m:
+                    self.node(c, gi)
+            finally:
+                self.marker_stack.pop()
+                self.ctx = saved
 
     # ---- raster images
     def image(self, e, parent, ts):

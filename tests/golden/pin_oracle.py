@@ -53,7 +53,7 @@ CATEGORIES = [
     "filters/feDistantLight", "filters/fePointLight", "filters/feSpotLight",
     "filters/filter-functions", "filters/feComponentTransfer", "filters/feDropShadow",
     "filters/feTurbulence", "filters/feTile", "filters/feDisplacementMap", "filters/feImage",
-    "paint-servers/pattern", "structure/image",
+    "paint-servers/pattern", "structure/image", "painting/marker", "painting/context",
 ]
 IMAGE_SIZE = 300
 FIXTURES_PER_DIR = 4
