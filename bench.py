@@ -76,6 +76,9 @@ def parse(argv=None):
                     help="seconds of CPU work for the oracle baseline sample")
     ap.add_argument("--scale", type=float, default=1.0,
                     help="path-count scale of configs 0-2 (1.0 = the full workload; smaller only for profiling)")
+    ap.add_argument("--profile", action="store_true",
+                    help="for ncu captures: prepare the workload, render it twice (the sizing render, then the "
+                         "one to capture, k_raster launches 1 + levels onwards) and exit")
     return ap.parse_args(argv)
 
 
@@ -500,7 +503,8 @@ def run_batched(args, rank, world):
                    "output_mpix": out_px / 1e6, "draws": info["draws"], "edges": info["edges"],
                    "binned_edges": info["binned_edges"], "work_items": info["work_items"],
                    "tuning": {"table": [list(e) for e in table], "pixels_per_thread": best_px,
-                              "autotune_ms_on_sample": min(tune_ms["px"].values()), "autotune_s": tune_s,
+                              "autotune_ms_on_sample": min(min(v.values()) for v in tune_ms.values()),
+                              "autotune_s": tune_s,
                               "buckets": "width <= %s x draws <= %s" % (list(BT.WIDTH_BUCKETS),
                                                                         list(BT.DRAW_BUCKETS))},
                    "prepare_s": prep_s, "l2": "outputs %.1f GB > L2 (129 MB)" % (total / 1e9),
@@ -753,9 +757,41 @@ def run_plain(args, rank, world):
         torch.distributed.destroy_process_group()
 
 
+def run_profile(args):
+    """Two renders of the workload through a prepared scene, nothing else:
+    the command ncu captures wrap (`-k regex:k_raster -s <levels> -c 1`)."""
+    import torch
+    import resvg_gb300 as R
+    from resvg_gb300 import build as B
+    B.build()
+    R.init(0)
+    if args.config == 3:
+        trees = [R.Tree.generate(3, seed=SEED, index=i) for i in range(args.scenes)]
+    else:
+        trees = [R.Tree.generate(args.config, seed=SEED, index=0, scale=args.scale)]
+    sizes = [tuple(int(v) for v in t.size) for t in trees]
+    offs, total = [], 0
+    for w, h in sizes:
+        offs.append(total)
+        total += ((w * h * 4 + 255) // 256) * 256
+    buf = torch.zeros(total, dtype=torch.uint8, device="cuda")
+    scene = R.Scene(trees, [IDENT] * len(trees), [w for w, _ in sizes], [h for _, h in sizes],
+                    [buf.data_ptr() + o for o in offs])
+    scene.set_timing(True)  # un-captured renders: every kernel is a launch of its own
+    ms = []
+    for _ in range(2):
+        scene.render()
+        ms.append(scene.check())
+    print(json.dumps({"profile": "config%d" % args.config, "scenes": len(trees), "raster_ms": ms,
+                      "info": scene.info()}), flush=True)
+
+
 def main():
     args = parse()
     rank, world = dist_setup(args.gpus)
+    if args.profile:
+        run_profile(args)
+        return
     if args.impl == "reference":
         run_reference(args, rank, world)
         return

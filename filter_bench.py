@@ -121,6 +121,25 @@ def main():
         us = t0.elapsed_time(t1) * 1e3 / a.reps
         gbs = bpp * w * h / us / 1e3
         print("%-34s %10.1f %10.1f %7.1f%%" % (name, us, gbs, 100.0 * gbs / peak), flush=True)
+    # the IIR blur in its FP32 chunked-scan mode (rgpu_set_iir_precision(1))
+    iir = [c for c in primitive_cases(w, h) if c[0].startswith("blur, IIR")][0]
+    R.set_iir_precision(1)
+    try:
+        img.copy_(base)
+        for _ in range(3):
+            R.filter_apply(img, filt, iir[1], iir[2], stream=stream)
+        torch.cuda.synchronize()
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record()
+        for _ in range(a.reps):
+            R.filter_apply(img, filt, iir[1], iir[2], stream=stream)
+        t1.record()
+        torch.cuda.synchronize()
+    finally:
+        R.set_iir_precision(0)
+    us = t0.elapsed_time(t1) * 1e3 / a.reps
+    gbs = iir[3] * w * h / us / 1e3
+    print("%-34s %10.1f %10.1f %7.1f%%" % (iir[0] + ", FP32 scan", us, gbs, 100.0 * gbs / peak), flush=True)
     print("HBM peak %.0f GB/s (%s); times include the job's input and result copies" % (peak, label))
 
 

@@ -188,6 +188,12 @@ int rgpu_set_wait_limit(uint32_t rounds);
  * the pixmap untouched). */
 int rgpu_test_withhold_window(int enabled);
 int rgpu_test_fail_allocations(uint32_t count);
+/* rgpu_render_batch cuts a batch into chunks of about equal estimated cost
+ * (pixels x paths) and flattens and uploads chunk k + 1 on the host while the
+ * device renders chunk k.  `chunks` = 0: automatic (8 chunks for batches of
+ * 64 scenes or more, else one submission); 1: always one submission; n: n
+ * chunks (at most one per scene).  The pixels do not depend on it. */
+int rgpu_set_batch_chunks(uint32_t chunks);
 /* Frees the library's cached device buffers and pinned staging (they grow to
  * the largest render seen and are otherwise kept for reuse). */
 int rgpu_trim(void);
@@ -210,6 +216,14 @@ int rgpu_filter_box_blur(uint8_t *device_img, uint32_t width, uint32_t height, d
 /* IIR (recursive Gaussian) blur in f64: crates/resvg/src/filter/iir_blur.rs:47. */
 int rgpu_filter_iir_blur(uint8_t *device_img, uint32_t width, uint32_t height, double sigma_x, double sigma_y,
                          void *stream);
+/* Precision of the IIR blur (iir_blur.rs:79-140) everywhere it runs (filter
+ * jobs of a render, rgpu_filter_iir_blur, rgpu_filter_apply): 0 (default) the
+ * reference's f64 recursions in the reference's order, bit-exact; 1 an FP32
+ * chunked parallel scan of the same recursions, within 1 per channel of mode 0
+ * (the 1/255 the IIR blur may differ by), for lines up to 4096 pixels (longer
+ * lines use mode 0).  Read when work is enqueued: a prepared scene's captured
+ * graph keeps the mode it was captured with. */
+int rgpu_set_iir_precision(uint32_t mode);
 /* Morphology erode (0) / dilate (1): crates/resvg/src/filter/morphology.rs:15. */
 int rgpu_filter_morphology(uint8_t *device_img, uint32_t width, uint32_t height, int dilate, float rx, float ry,
                            void *stream);

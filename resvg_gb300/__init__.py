@@ -299,6 +299,15 @@ def set_tuning(band_rows: int = 0, pixels_per_thread: int = 0) -> None:
     check(lib().rgpu_set_tuning(C.byref(t)), "rgpu_set_tuning")
 
 
+def set_batch_chunks(chunks: int) -> None:
+    """Chunks of render_batch's host/device pipeline: 0 automatic (8 for 64
+    scenes or more), 1 one submission, n n chunks."""
+    L = lib()
+    L.rgpu_set_batch_chunks.restype = C.c_int
+    L.rgpu_set_batch_chunks.argtypes = [C.c_uint32]
+    check(L.rgpu_set_batch_chunks(int(chunks)))
+
+
 def set_tuning_table(entries) -> None:
     """Band rows per (max stream width, max stream draws) bucket, used for
     streams whose band rows the tuning leaves automatic: entries are
@@ -455,6 +464,15 @@ def box_blur(tensor, sx, sy, stream=None):
 
 def iir_blur(tensor, sx, sy, stream=None):
     return _dev_filter("rgpu_filter_iir_blur", tensor, C.c_double(sx), C.c_double(sy), stream=stream)
+
+
+def set_iir_precision(mode: int) -> None:
+    """0: the IIR blur in f64 in the reference's order (bit-exact, default);
+    1: an FP32 chunked parallel scan (within 1 per channel)."""
+    L = lib()
+    L.rgpu_set_iir_precision.restype = C.c_int
+    L.rgpu_set_iir_precision.argtypes = [C.c_uint32]
+    check(L.rgpu_set_iir_precision(int(mode)), "rgpu_set_iir_precision")
 
 
 def morphology(tensor, dilate, rx, ry, stream=None):

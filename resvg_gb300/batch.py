@@ -18,11 +18,10 @@ import numpy as np
 TUNING_CANDIDATES = [(0, 8), (0, 16), (1, 4), (2, 4), (4, 4), (2, 8), (4, 8), (8, 8), (4, 16), (8, 16)]
 
 # Buckets of the tuning table: stream width (canvas side) and draws (fills and
-# strokes), upper bounds; the band heights and pixels per thread searched.
+# strokes), upper bounds; the band heights tried per bucket.
 WIDTH_BUCKETS = (128, 256, 512, 1024, 32767)
 DRAW_BUCKETS = (64, 256, 1024, 1 << 30)
 BAND_CANDIDATES = (1, 2, 4, 8)
-PX_CANDIDATES = (4, 8, 16)
 
 
 def scene_draws(tree) -> int:
@@ -55,49 +54,68 @@ def _time_scene(R, torch, trees, widths, heights, ptrs, stream, reps):
     return e0.elapsed_time(e1) / reps
 
 
-def autotune_table(trees, widths, heights, device_ptrs, reps: int = 2, per_bucket: int = 24):
-    """The batched form's autotuner.  Scenes are grouped by (canvas-width
-    bucket, draw-count bucket); for every bucket the band height (rows per
-    raster work item, the tile height) is chosen by timing up to `per_bucket`
-    of its scenes under each candidate, then the pixels per thread (the tile
-    width is 256 / band rows x pixels per thread) by timing all of them under
-    the resulting table.  Installs the table and the tuning, and returns
-    (table, pixels per thread, {bucket: {band rows: ms}, "px": {px: ms}})."""
+def autotune_table(trees, widths, heights, device_ptrs, reps: int = 2, min_share: float = 0.05,
+                   min_gain: float = 0.01):
+    """The batched form's autotuner; every timing renders the whole sample as
+    one prepared batch, so each choice is judged where it runs.
+
+    1. (band rows, pixels per thread) over TUNING_CANDIDATES, one value for
+       every stream: the best pair is the starting point.
+    2. Scenes are grouped by (canvas-width bucket, draw-count bucket); for
+       every bucket holding at least `min_share` of the sample's estimated
+       cost (side^2 x draws), heaviest first, the other band heights are tried
+       for that bucket alone and kept when the batch gets faster by more than
+       `min_gain`.
+    Installs the table and the pixels per thread, and returns (table, pixels
+    per thread, {"global": {candidate: ms}, bucket: {band rows: ms}})."""
     import torch
     import resvg_gb300 as R
-    groups = {}
-    for i, t in enumerate(trees):
-        groups.setdefault(bucket_of(widths[i], scene_draws(t)), []).append(i)
     stream = torch.cuda.Stream()
     saved = R.get_tuning()
-    table, timings = [], {}
+    args = (trees, widths, heights, device_ptrs, stream, reps)
+    timings = {"global": {}}
     try:
-        for wb in WIDTH_BUCKETS:
-            for db in DRAW_BUCKETS:
-                idx = groups.get((wb, db), [])[:per_bucket]
-                if not idx:
+        R.set_tuning_table([])
+        for b, px in TUNING_CANDIDATES:
+            R.set_tuning(b, px)
+            timings["global"][(b, px)] = _time_scene(R, torch, *args)
+        (b0, px0), best = min(timings["global"].items(), key=lambda kv: kv[1])
+        cost = {}
+        for i, t in enumerate(trees):
+            d = scene_draws(t)
+            key = bucket_of(widths[i], d)
+            cost[key] = cost.get(key, 0.0) + scene_cost(widths[i], heights[i], d)
+        total = sum(cost.values()) or 1.0
+        # a table entry for every bucket, starting from the global band height
+        # (band rows 0 keeps the per-stream rule of that candidate)
+        table = {(wb, db): b0 for wb in WIDTH_BUCKETS for db in DRAW_BUCKETS}
+
+        def install():
+            R.set_tuning_table([(wb, db, table[(wb, db)]) for wb in WIDTH_BUCKETS for db in DRAW_BUCKETS])
+        R.set_tuning(0, px0)
+        install()
+        for key in sorted(cost, key=cost.get, reverse=True):
+            if cost[key] / total < min_share:
+                break
+            res = {table[key]: best}
+            for b in BAND_CANDIDATES:
+                if b == table[key]:
                     continue
-                sub = ([trees[i] for i in idx], [widths[i] for i in idx], [heights[i] for i in idx],
-                       [device_ptrs[i] for i in idx])
-                res = {}
-                for b in BAND_CANDIDATES:
-                    R.set_tuning(b, 0)
-                    res[b] = _time_scene(R, torch, *sub, stream, reps)
-                timings[(wb, db)] = res
-                table.append((wb, db, min(res, key=res.get)))
-        R.set_tuning(0, 0)
-        R.set_tuning_table(table)
-        px_ms = {}
-        for px in PX_CANDIDATES:
-            R.set_tuning(0, px)
-            px_ms[px] = _time_scene(R, torch, trees, widths, heights, device_ptrs, stream, reps)
-        best_px = min(px_ms, key=px_ms.get)
-        R.set_tuning(0, best_px)
+                keep = table[key]
+                table[key] = b
+                install()
+                res[b] = _time_scene(R, torch, *args)
+                if res[b] < best * (1.0 - min_gain):
+                    best = res[b]
+                else:
+                    table[key] = keep
+            install()
+            timings[key] = res
+        entries = [(wb, db, table[(wb, db)]) for wb in WIDTH_BUCKETS for db in DRAW_BUCKETS]
     except Exception:
         R.set_tuning(*saved)
         raise
-    timings["px"] = px_ms
-    return table, best_px, timings
+    return entries, px0, timings
 
 
 def scene_cost(width: float, height: float, paths: int) -> float:

@@ -146,6 +146,10 @@ struct BufScratch : FilterScratch {
     }
 };
 
+// rgpu_render_batch pipelines batches of at least this many scenes in this many chunks.
+constexpr uint32_t kPipeMinScenes = 64;
+constexpr uint32_t kPipeChunks = 8;
+
 // A flattened submission with its work decomposition.
 constexpr uint32_t kSpanOvf = 64;  // spans one sub-scanline of one draw may hold in the raster kernel
 
@@ -187,6 +191,15 @@ struct RasterTimer {
     }
 };
 
+// One stage of rgpu_render_batch's pipeline: while the device renders the
+// chunk in one slot, the host flattens and uploads the next into the other.
+struct PipeSlot {
+    Buffers buf;
+    HostBuf staging;
+    RasterTimer timer;
+    cudaEvent_t done = nullptr;  // the slot's uploads and kernels have run
+};
+
 struct Context {
     std::mutex mu;
     int device = -1;
@@ -197,6 +210,9 @@ struct Context {
     DevBuf surface;
     HostBuf staging;
     Tuning tuning;
+    PipeSlot pipe[2];
+    HostBuf pipe_err;            // error words of the pipelined chunks, read back asynchronously
+    uint32_t batch_chunks = 0;   // 0: automatic; else the chunk count of rgpu_render_batch
 };
 
 Context &ctx() {
@@ -238,12 +254,12 @@ int ensure_device(Context &c) {
 }
 
 template <class T>
-int upload(Context &c, DevBuf &d, const std::vector<T> &v, size_t &stage_off, cudaStream_t s) {
+int upload(HostBuf &staging, DevBuf &d, const std::vector<T> &v, size_t &stage_off, cudaStream_t s) {
     size_t bytes = v.size() * sizeof(T);
     CK(d.ensure(bytes ? bytes : 16));
     if (!bytes) return RGPU_OK;
-    std::memcpy((char *)c.staging.p + stage_off, v.data(), bytes);
-    CK(cudaMemcpyAsync(d.p, (char *)c.staging.p + stage_off, bytes, cudaMemcpyHostToDevice, s));
+    std::memcpy((char *)staging.p + stage_off, v.data(), bytes);
+    CK(cudaMemcpyAsync(d.p, (char *)staging.p + stage_off, bytes, cudaMemcpyHostToDevice, s));
     stage_off += (bytes + 255) & ~(size_t)255;
     g_stats.h2d_bytes += bytes;
     return RGPU_OK;
@@ -325,7 +341,8 @@ int plan_scene(Context &c, Plan &p) {
     return RGPU_OK;
 }
 
-int upload_plan(Context &c, Buffers &b, Plan &p, cudaStream_t s) {
+int upload_plan(Context &c, Buffers &b, Plan &p, cudaStream_t s, HostBuf *staging_buf = nullptr) {
+    HostBuf &staging = staging_buf ? *staging_buf : c.staging;
     SceneBuild &sb = p.sb;
     if (b.surf.size() < sb.surfaces.size()) b.surf.resize(sb.surfaces.size());
     for (size_t i = 0; i < sb.surfaces.size(); i++) {
@@ -349,21 +366,21 @@ int upload_plan(Context &c, Buffers &b, Plan &p, cudaStream_t s) {
                    rup(sb.streams.size() * sizeof(StreamRec)) + rup(p.items.size() * sizeof(WorkItem)) +
                    rup(sb.hairs.size() * sizeof(HairRec)) + rup(sb.hair_spans.size() * sizeof(HairSpan)) +
                    rup(sb.fill_cmds.size() * 4) + 4096;
-    CK(c.staging.ensure(stage));
+    CK(staging.ensure(stage));
     size_t off = 0;
     int r;
-    if ((r = upload(c, b.verbs, sb.verbs, off, s))) return r;
-    if ((r = upload(c, b.pts, sb.pts, off, s))) return r;
-    if ((r = upload(c, b.draws, sb.draws, off, s))) return r;
-    if ((r = upload(c, b.paints, sb.paints, off, s))) return r;
-    if ((r = upload(c, b.grads, sb.grads, off, s))) return r;
-    if ((r = upload(c, b.layers, sb.layers, off, s))) return r;
-    if ((r = upload(c, b.cmds, sb.cmds, off, s))) return r;
-    if ((r = upload(c, b.streams, sb.streams, off, s))) return r;
-    if ((r = upload(c, b.items, p.items, off, s))) return r;
-    if ((r = upload(c, b.hairs, sb.hairs, off, s))) return r;
-    if ((r = upload(c, b.hair_spans, sb.hair_spans, off, s))) return r;
-    if ((r = upload(c, b.fill_cmds, sb.fill_cmds, off, s))) return r;
+    if ((r = upload(staging, b.verbs, sb.verbs, off, s))) return r;
+    if ((r = upload(staging, b.pts, sb.pts, off, s))) return r;
+    if ((r = upload(staging, b.draws, sb.draws, off, s))) return r;
+    if ((r = upload(staging, b.paints, sb.paints, off, s))) return r;
+    if ((r = upload(staging, b.grads, sb.grads, off, s))) return r;
+    if ((r = upload(staging, b.layers, sb.layers, off, s))) return r;
+    if ((r = upload(staging, b.cmds, sb.cmds, off, s))) return r;
+    if ((r = upload(staging, b.streams, sb.streams, off, s))) return r;
+    if ((r = upload(staging, b.items, p.items, off, s))) return r;
+    if ((r = upload(staging, b.hairs, sb.hairs, off, s))) return r;
+    if ((r = upload(staging, b.hair_spans, sb.hair_spans, off, s))) return r;
+    if ((r = upload(staging, b.fill_cmds, sb.fill_cmds, off, s))) return r;
     // fixed-size work buffers
     uint64_t nsegs = sb.nsegs;
     CK(b.tpts.ensure(std::max<uint64_t>(sb.ntpts, 1) * 8));
@@ -749,12 +766,91 @@ int rgpu_render_batch(const resvg_render_tree *const *trees, const resvg_transfo
     int r = ensure_device(c);
     if (r) return r;
     cudaStream_t s = stream ? (cudaStream_t)stream : c.stream;
-    Plan p;
-    if ((r = build_batch(p, trees, transforms, count, widths, heights, device_pixmaps, nullptr))) return r;
-    if ((r = plan_scene(c, p))) return r;
-    if ((r = upload_plan(c, c.buf, p, s))) return r;
-    if ((r = enqueue_plan(c, c.buf, p, s, &c.timer))) return r;
-    return check_err(c.buf, s, &c.timer);
+    uint32_t nch = c.batch_chunks ? c.batch_chunks : (count >= kPipeMinScenes ? kPipeChunks : 1u);
+    nch = std::min(nch, count);
+    if (nch <= 1) {
+        Plan p;
+        if ((r = build_batch(p, trees, transforms, count, widths, heights, device_pixmaps, nullptr))) return r;
+        if ((r = plan_scene(c, p))) return r;
+        if ((r = upload_plan(c, c.buf, p, s))) return r;
+        if ((r = enqueue_plan(c, c.buf, p, s, &c.timer))) return r;
+        return check_err(c.buf, s, &c.timer);
+    }
+    // Pipelined: the batch is cut into `nch` contiguous chunks of about equal
+    // estimated cost (pixels x paths; the first one half as large, so the
+    // device starts early).  The host flattens and uploads chunk k + 1 into
+    // one slot while the device renders chunk k from the other; every chunk
+    // is an ordinary submission, so the pixels are those of one submission.
+    for (uint32_t i = 0; i < count; i++)
+        if (!trees[i]) { set_error("invalid batch entry %u", i); return RGPU_ERR_INVALID_ARG; }
+    std::vector<double> cum(count + 1, 0.0);
+    for (uint32_t i = 0; i < count; i++) {
+        const rgpu_tree *tr = trees[i];
+        cum[i + 1] = cum[i] + (double)widths[i] * (double)heights[i] * (double)std::max<size_t>(1, tr->paths.size());
+    }
+    std::vector<uint32_t> cut(nch + 1, count);
+    cut[0] = 0;
+    {
+        const double unit = cum[count] / (nch - 0.5);  // the first chunk takes half a unit
+        uint32_t i = 0;
+        for (uint32_t k = 1; k < nch; k++) {
+            const double target = unit * (k - 0.5);
+            while (i < count && cum[i + 1] <= target) i++;
+            cut[k] = std::max(cut[k - 1] + 1, std::min(i + 1, count - (nch - k)));
+            i = cut[k];
+        }
+    }
+    CK(c.pipe_err.ensure(nch * sizeof(uint32_t)));
+    uint32_t *herr = (uint32_t *)c.pipe_err.p;
+    for (auto &sl : c.pipe)
+        if (!sl.done) CK(cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming));
+    g_stats.raster_ms = 0.0f;
+    float raster_ms = 0.0f;
+    rgpu_stats acc{};
+    for (uint32_t k = 0; k < nch; k++) {
+        PipeSlot &sl = c.pipe[k & 1u];
+        // the slot's previous chunk (k - 2) has finished with its buffers and staging
+        CK(cudaEventSynchronize(sl.done));
+        if (k >= 2 && sl.timer.used) {
+            for (int t = 0; t < sl.timer.used; t++) {
+                float ms = 0.0f;
+                if (cudaEventElapsedTime(&ms, sl.timer.start[t], sl.timer.stop[t]) == cudaSuccess) raster_ms += ms;
+            }
+            sl.timer.used = 0;
+        }
+        Plan p;
+        const uint32_t a = cut[k], n = cut[k + 1] - cut[k];
+        std::memset(&g_stats, 0, sizeof(g_stats));
+        if ((r = build_batch(p, trees + a, transforms + a, n, widths + a, heights + a, device_pixmaps + a, nullptr)))
+            return r;
+        if ((r = plan_scene(c, p))) return r;
+        if ((r = upload_plan(c, sl.buf, p, s, &sl.staging))) return r;
+        if ((r = enqueue_plan(c, sl.buf, p, s, &sl.timer))) return r;
+        CK(cudaMemcpyAsync(herr + k, sl.buf.err.p, 4, cudaMemcpyDeviceToHost, s));
+        CK(cudaEventRecord(sl.done, s));
+        acc.draws += g_stats.draws;
+        acc.edges += g_stats.edges;
+        acc.work_items += g_stats.work_items;
+        acc.kernel_launches += g_stats.kernel_launches;
+        acc.h2d_bytes += g_stats.h2d_bytes;
+    }
+    CK(cudaStreamSynchronize(s));
+    for (auto &sl : c.pipe) {
+        for (int t = 0; t < sl.timer.used; t++) {
+            float ms = 0.0f;
+            if (cudaEventElapsedTime(&ms, sl.timer.start[t], sl.timer.stop[t]) == cudaSuccess) raster_ms += ms;
+        }
+        sl.timer.used = 0;
+    }
+    cudaGetLastError();
+    g_stats = acc;
+    g_stats.raster_ms = raster_ms;
+    for (uint32_t k = 0; k < nch; k++)
+        if (herr[k]) {
+            set_error("raster kernel reported error flags 0x%x (chunk %u of %u)", herr[k], k, nch);
+            return RGPU_ERR_DEVICE_FAULT;
+        }
+    return RGPU_OK;
 }
 
 int rgpu_scene_prepare(const resvg_render_tree *const *trees, const resvg_transform *transforms, uint32_t count,
@@ -989,14 +1085,27 @@ int rgpu_test_fail_allocations(uint32_t count) {
     return RGPU_OK;
 }
 
+int rgpu_set_batch_chunks(uint32_t chunks) {
+    Context &c = ctx();
+    std::lock_guard<std::mutex> lock(c.mu);
+    c.batch_chunks = chunks;
+    return RGPU_OK;
+}
+
 int rgpu_trim(void) {
     Context &c = ctx();
     std::lock_guard<std::mutex> lock(c.mu);
     if (c.device < 0) return RGPU_OK;
-    if (c.stream) cudaStreamSynchronize(c.stream);
+    cudaDeviceSynchronize();  // pipelined batches may still run on a caller's stream
+    cudaGetLastError();
     c.buf.release();
     c.surface.release();
     c.staging.release();
+    for (auto &sl : c.pipe) {
+        sl.buf.release();
+        sl.staging.release();
+    }
+    c.pipe_err.release();
     return RGPU_OK;
 }
 
@@ -1047,6 +1156,14 @@ int rgpu_filter_iir_blur(uint8_t *img, uint32_t w, uint32_t h, double sx, double
     CK(g_fplane.ensure((size_t)w * h * 8 * 4));  // four f64 planes
     CK(filter_iir_blur((uint32_t *)img, g_fplane.as<double>(), (int)w, (int)h, sx, sy, s));
     if (!stream) CK(cudaStreamSynchronize(s));  // a caller stream: asynchronous
+    return RGPU_OK;
+}
+
+int rgpu_set_iir_precision(uint32_t mode) {
+    if (mode > 1) { set_error("IIR precision: 0 (f64, bit-exact) or 1 (f32 chunked scan)"); return RGPU_ERR_INVALID_ARG; }
+    Context &c = ctx();
+    std::lock_guard<std::mutex> lock(c.mu);
+    filter_set_iir_fast(mode == 1);
     return RGPU_OK;
 }
 

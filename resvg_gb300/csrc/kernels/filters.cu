@@ -739,6 +739,142 @@ cudaError_t filter_box_blur(uint32_t *img, uint32_t *tmp, int w, int h, double s
     return cudaGetLastError();
 }
 
+// ---- IIR blur, FP32 chunked-scan mode (opt-in; within 1/255 of the f64 path).
+// Each line's first-order recursions (rightwards y[i] = x[i] + d y[i-1], then
+// leftwards y[i] = y[i] + d y[i+1], `steps` times) run in parallel: a line is
+// held by one 256-thread CTA, each thread owning E consecutive values in
+// registers; a thread first runs the recursion over its chunk from zero, the
+// chunk-end values are scanned across the CTA (the carry into chunk t is
+// end(t-1) + d^E carry(t-1)), and value k of a chunk then gets d^(k+1) carry.
+// Columns are rows of the transposed planes.
+constexpr int kIirLine = 256;
+constexpr int kIirFastMaxE = 16;  // lines of up to 4096 values
+bool g_iir_fast = false;
+
+// Exclusive scan of y_t = e_t + D y_(t-1) over the 256 threads of the CTA, in
+// thread order (reverse = false) or from the last thread down (reverse = true):
+// the carry a thread's chunk receives.
+__device__ float iir_block_carry(float e, float D, bool reverse, float *tot) {
+    const int t = reverse ? kIirLine - 1 - (int)threadIdx.x : (int)threadIdx.x;
+    const int lane = t & 31, warp = t >> 5;
+    // threads are renumbered by t; lanes of a hardware warp keep their order
+    // or reverse it as a whole, so shuffles run on t's lane
+    const unsigned full = 0xffffffffu;
+    float v = e, Dk = D;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const int src_hw = reverse ? (int)threadIdx.x + off : (int)threadIdx.x - off;
+        const float u = __shfl_sync(full, v, src_hw & 31);
+        if (lane >= off) v = v + Dk * u;
+        Dk = Dk * Dk;  // D^(2 off)
+    }
+    // Dk = D^32 now; warp totals, then the carry into each warp
+    if (lane == 31) tot[warp] = v;
+    __syncthreads();
+    float cw = 0.0f;
+    for (int k = 0; k < warp; k++) cw = tot[k] + Dk * cw;
+    // inclusive value of this thread, then the previous thread's (exclusive)
+    float dl = D;  // D^(lane + 1)
+    for (int k = 0; k < lane; k++) dl = dl * D;
+    const float incl = v + dl * cw;
+    const int src_hw = reverse ? (int)threadIdx.x + 1 : (int)threadIdx.x - 1;
+    float prev = __shfl_sync(full, incl, src_hw & 31);
+    __syncthreads();  // tot[] is reused by the next scan
+    return lane == 0 ? cw : prev;
+}
+
+__global__ void __launch_bounds__(kIirLine) k_iir_fast_lines(float *planes, int len, float d, int steps) {
+    __shared__ float tot[kIirLine / 32];
+    float *line = planes + (size_t)blockIdx.x * len;
+    const int E = (len + kIirLine - 1) / kIirLine;
+    const int first = (int)threadIdx.x * E;
+    float v[kIirFastMaxE];
+#pragma unroll
+    for (int k = 0; k < kIirFastMaxE; k++) v[k] = (k < E && first + k < len) ? line[first + k] : 0.0f;
+    float dE = 1.0f;
+    for (int k = 0; k < E; k++) dE = dE * d;
+    for (int st = 0; st < steps; st++) {
+        // rightwards
+        float y = 0.0f;
+#pragma unroll
+        for (int k = 0; k < kIirFastMaxE; k++)
+            if (k < E) { y = v[k] + d * y; v[k] = y; }
+        float c = iir_block_carry(y, dE, false, tot);
+        float p = d;
+#pragma unroll
+        for (int k = 0; k < kIirFastMaxE; k++)
+            if (k < E) { v[k] = (first + k < len) ? v[k] + p * c : 0.0f; p = p * d; }
+        // leftwards
+        y = 0.0f;
+#pragma unroll
+        for (int k = kIirFastMaxE - 1; k >= 0; k--)
+            if (k < E) { y = v[k] + d * y; v[k] = y; }
+        c = iir_block_carry(y, dE, true, tot);
+        p = d;
+#pragma unroll
+        for (int k = kIirFastMaxE - 1; k >= 0; k--)
+            if (k < E) { v[k] = v[k] + p * c; p = p * d; }
+    }
+#pragma unroll
+    for (int k = 0; k < kIirFastMaxE; k++)
+        if (k < E && first + k < len) line[first + k] = v[k];
+}
+
+__global__ void k_iir_fast_load(const uint32_t *img, float *planes, size_t n) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t p = img[i];
+#pragma unroll
+    for (int ch = 0; ch < 4; ch++) planes[(size_t)ch * n + i] = (float)chn(p, ch) / 255.0f;
+}
+
+__global__ void k_iir_fast_store(uint32_t *img, const float *planes, size_t n, float post) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t o = 0;
+#pragma unroll
+    for (int ch = 0; ch < 4; ch++) o |= sat_u8f(planes[(size_t)ch * n + i] * post * 255.0f) << (8 * ch);
+    img[i] = o;
+}
+
+// 4 planes of h rows x w columns -> 4 planes of w rows x h columns
+__global__ void k_iir_transpose(const float *src, float *dst, int w, int h) {
+    __shared__ float tile[32][33];
+    const size_t n = (size_t)w * h;
+    const float *sp = src + (size_t)blockIdx.z * n;
+    float *dp = dst + (size_t)blockIdx.z * n;
+    const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
+    for (int j = threadIdx.y; j < 32; j += 8) {
+        const int x = x0 + threadIdx.x, y = y0 + j;
+        if (x < w && y < h) tile[j][threadIdx.x] = sp[(size_t)y * w + x];
+    }
+    __syncthreads();
+    for (int j = threadIdx.y; j < 32; j += 8) {
+        const int x = y0 + threadIdx.x, y = x0 + j;  // dst is h wide, w tall
+        if (x < h && y < w) dp[(size_t)y * h + x] = tile[threadIdx.x][j];
+    }
+}
+
+void filter_set_iir_fast(bool on) { g_iir_fast = on; }
+bool filter_iir_fast() { return g_iir_fast; }
+
+// buf: 32 bytes per pixel (the f64 mode's four planes), here 2 x 4 f32 planes
+static cudaError_t iir_blur_fast(uint32_t *img, float *a, float *b, int w, int h, double dx, double dy, bool bx,
+                                 bool by, double post, cudaStream_t s) {
+    const int steps = 4;
+    const size_t n = (size_t)w * h;
+    k_iir_fast_load<<<nblk(n, 256), 256, 0, s>>>(img, a, n);
+    if (bx) k_iir_fast_lines<<<(unsigned)(4 * h), kIirLine, 0, s>>>(a, w, (float)dx, steps);
+    if (by) {
+        const dim3 blk(32, 8);
+        k_iir_transpose<<<dim3((w + 31) / 32, (h + 31) / 32, 4), blk, 0, s>>>(a, b, w, h);
+        k_iir_fast_lines<<<(unsigned)(4 * w), kIirLine, 0, s>>>(b, h, (float)dy, steps);
+        k_iir_transpose<<<dim3((h + 31) / 32, (w + 31) / 32, 4), blk, 0, s>>>(b, a, h, w);
+    }
+    k_iir_fast_store<<<nblk(n, 256), 256, 0, s>>>(img, a, n, (float)post);
+    return cudaGetLastError();
+}
+
 cudaError_t filter_iir_blur(uint32_t *img, double *buf, int w, int h, double sx, double sy, cudaStream_t s) {
     const int steps = 4;
     double lx = 1.0, dx = 1.0, ly = 1.0, dy = 1.0;
@@ -747,6 +883,9 @@ cudaError_t filter_iir_blur(uint32_t *img, double *buf, int w, int h, double sx,
     double post = pow(sqrt(dx * dy) / sqrt(lx * ly), 2 * steps);
     size_t n = (size_t)w * h;
     if (n == 0) return cudaSuccess;
+    if (g_iir_fast && w <= kIirLine * kIirFastMaxE && h <= kIirLine * kIirFastMaxE)
+        return iir_blur_fast(img, reinterpret_cast<float *>(buf), reinterpret_cast<float *>(buf) + 4 * n, w, h, dx,
+                             dy, sx > 0.0, sy > 0.0, post, s);
     // buf holds four planes of n doubles
     k_iir_load4<<<nblk(n, 256), 256, 0, s>>>(img, buf, n);
     if (sx > 0.0) k_iir_rows4<<<nblk((size_t)4 * h, 64), 64, 0, s>>>(buf, w, h, dx, steps);

@@ -50,8 +50,13 @@ void box_sizes(float sigma, int sizes[5]);
 // same (fully transparent) result and are clamped to it.
 constexpr double kBoxSigmaMax = 1.0e8;
 cudaError_t filter_box_blur(uint32_t *img, uint32_t *tmp, int w, int h, double sx, double sy, cudaStream_t s);
-// buf: scratch for four f64 planes of w * h values
+// buf: scratch for four f64 planes of w * h values (32 bytes per pixel)
 cudaError_t filter_iir_blur(uint32_t *img, double *buf, int w, int h, double sx, double sy, cudaStream_t s);
+// IIR precision: false (default) the reference's f64 recursions in its order,
+// bit-exact; true an FP32 chunked parallel scan (lines up to 4096 values, else
+// f64), within 1 of the f64 result per channel.
+void filter_set_iir_fast(bool on);
+bool filter_iir_fast();
 cudaError_t filter_color_matrix(uint32_t *img, size_t n, int kind, const float *values, cudaStream_t s);
 cudaError_t filter_morphology(uint32_t *img, uint32_t *tmp, int w, int h, bool dilate, float rx, float ry,
                               cudaStream_t s);

@@ -241,10 +241,12 @@ __device__ __forceinline__ bool gradient_eval(const GradRec &g, int32_t px, int3
     } else if (g.flags & GRAD_PAD_CLAMP) {
         t = fminf(fmaxf(t, 0.0f), 1.0f);
     }
+    // the interval: how many of t[1..n) are <= t; t[] is non-decreasing (the
+    // host makes the stop positions monotonic), so the scan stops at the first
+    // larger value
     uint32_t idx = 0;
     if (!(g.flags & GRAD_TWO_STOP)) {
-        for (uint32_t i = 1; i < g.n; i++)
-            if (t >= g.t[i]) idx++;
+        while (idx + 1 < g.n && t >= g.t[idx + 1]) idx++;
     }
     const float4 fv = reinterpret_cast<const float4 *>(g.f)[idx];
     const float4 bv = reinterpret_cast<const float4 *>(g.b)[idx];

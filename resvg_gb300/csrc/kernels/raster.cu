@@ -50,7 +50,9 @@ struct ItemInfo {
 // and draw origins, and per (slot, row) the alpha runs.  Two of them alternate:
 // the producers fill one while the consumers shade from the other.
 struct WinBuf {
-    uint16_t run_cnt[kMaxPairs];  // alpha runs per (slot, row), including the closing sentinel
+    // alpha runs per (slot, row), including the closing sentinel; the upper
+    // half stays zero: a consumer that gave up on a window reads its counts there
+    uint16_t run_cnt[2 * kMaxPairs];
     int2 run_ext[kMaxPairs];      // [first, last) layer x with non-zero coverage per (slot, row)
     int2 runs[kMaxPairs * kRunStride];
     PaintRec paint[kMaxSlots + 1];   // paints of the window's draws; [kMaxSlots] of buffer 0: the hairline's
@@ -64,6 +66,7 @@ struct VmShared {
     unsigned long long mb_ready[2];  // mbarriers: window in buffer b produced (kProducers arrivals)
     unsigned long long mb_free[2];   // buffer b consumed (kThreads arrivals)
     int32_t abort;                   // set on an error: the rest of the launch skips work and waits
+    int32_t cabort;                  // consumers only: set (for good) by a consumer that has seen an abort
     unsigned long long mb_item_ready[2];  // item ring entry filled (1 arrival: producer 0)
     unsigned long long mb_item_free[2];   // item ring entry done with (kThreads arrivals)
     int4 rects[kMaxDepth];       // layer-stack rects (x, y, w, h) by depth, the top one at [depth]
@@ -108,15 +111,6 @@ __device__ __forceinline__ bool mb_wait(unsigned long long *mb, uint32_t parity,
 // barriers of the consumer threads only (named barrier 1) and of the producer
 // threads only (named barrier 2)
 __device__ __forceinline__ void consumer_sync() { asm volatile("bar.sync 1, %0;" ::"n"(kThreads) : "memory"); }
-// consumer barrier that also ORs a predicate over the consumer threads
-__device__ __forceinline__ bool consumer_sync_or(bool v) {
-    uint32_t r;
-    asm volatile("{ .reg .pred pi, po; setp.ne.u32 pi, %1, 0; bar.red.or.pred po, 1, %2, pi; selp.u32 %0, 1, 0, po; }"
-                 : "=r"(r)
-                 : "r"((uint32_t)v), "n"(kThreads)
-                 : "memory");
-    return r != 0;
-}
 __device__ __forceinline__ void producer_sync() { asm volatile("bar.sync 2, %0;" ::"n"(kProducers) : "memory"); }
 
 __device__ __forceinline__ int32_t round16(int32_t x) { return (int32_t)((uint32_t)x + 0x8000u) >> 16; }
@@ -396,8 +390,9 @@ __device__ __forceinline__ void produce_window(VmShared &sh, const ItemInfo &itm
             for (int w = lane; w < (int)(sizeof(GradRec) / 4); w += 32) ((uint32_t *)&wb.grad[k])[w] = src[w];
         }
     }
-    // tasks 2 pt and 2 pt + 1: the same slot (S is even)
-    const int u0 = 2 * pt, k = u0 / S, j0 = u0 % S;
+    // tasks 2 pt and 2 pt + 1: the same slot (S = 4 x band rows, a power of two)
+    const int Sshift = 31 - __clz(S);
+    const int u0 = 2 * pt, k = u0 >> Sshift, j0 = u0 & (S - 1);
     DrawRec dr;
     if (k < (int)nsl) {
         const uint32_t di = cmds[st.cmd_off + flist[k]].a;
@@ -453,7 +448,9 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
         mb_init(&sh.mb_item_free[0], kThreads);
         mb_init(&sh.mb_item_free[1], kThreads);
         sh.abort = 0;
+        sh.cabort = 0;
     }
+    if (tid < 2 * kMaxPairs) sh.win[tid / kMaxPairs].run_cnt[kMaxPairs + tid % kMaxPairs] = 0;
     __syncthreads();
     uint32_t win_base = 0;  // windows produced and consumed by this CTA so far
 
@@ -465,6 +462,10 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
             const uint32_t is = seq & 1u;
             if (pt == 0) {
                 if (seq >= 2) mb_wait(&sh.mb_item_free[is], ((seq >> 1) - 1u) & 1u, err, &sh.abort, wait_limit);
+                // a wait that returned because of an abort is ordered before the
+                // entry is overwritten: a consumer that sees part of the new
+                // entry also sees the abort
+                __threadfence_block();
                 ItemInfo &w = sh.items[is];
                 const int32_t idx = (int32_t)atomicAdd(item_counter, 1u);
                 w.idx = idx;
@@ -498,38 +499,45 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
         return;
     }
 
-    // set (per thread, for good) once a wait failed or the CTA aborted: the
-    // thread then reads no window and writes no pixel, and only drains the
-    // item queue.  Control flow stays the same in every consumer thread, so
-    // the consumer barriers still match.
-    bool dead = false;
+    // After an abort (a wait that ran out sets `abort`, and every later wait
+    // returns at once) a window buffer may hold a window that was not
+    // produced.  A consumer that sees the abort at a window reads that
+    // window's run counts from the zero half of `run_cnt`, so every fill is
+    // skipped without touching the window, and stores no pixel; it runs the
+    // command list like the others so the consumer barriers still match.  At
+    // the next item every consumer stops: the decision is taken at the item
+    // barrier from `cabort`, which only consumers write, only before that
+    // barrier, and never clear, so all of them read the same value.
     for (uint32_t seq = 0;; seq++) {
         const uint32_t is = seq & 1u;
-        dead |= !mb_wait(&sh.mb_item_ready[is], (seq >> 1) & 1u, err, &sh.abort, wait_limit);
+        mb_wait(&sh.mb_item_ready[is], (seq >> 1) & 1u, err, &sh.abort, wait_limit);
         if (tid == 0) {
             sh.cur = sh.items[is];
             sh.rects[0] = make_int4(0, 0, sh.cur.st.out_w, sh.cur.st.out_h);
+            __threadfence_block();  // the copy, then the abort flag (see the producers' fence)
         }
-        // After an abort the producers no longer wait for the ring entry to be
-        // released, so the copy may mix two items: every consumer then skips
-        // the item (one decision for all of them, taken at this barrier).
-        const bool skip_item = consumer_sync_or(dead || *(volatile int32_t *)&sh.abort != 0);
+        if (*(volatile int32_t *)&sh.abort != 0) *(volatile int32_t *)&sh.cabort = 1;
+        consumer_sync();
+        const bool stop = *(volatile int32_t *)&sh.cabort != 0;
         mb_arrive(&sh.mb_item_free[is]);  // the entry is copied: the producers may refill it
-        if (sh.cur.idx >= (int32_t)nitems) break;
-        if (skip_item) {
-            dead = true;
-            continue;
-        }
+        // After an abort the producers stop waiting for ring entries to be
+        // released, so the copy may mix two items: nobody uses it.  The
+        // producers' remaining waits return at once, so the launch ends.
+        if (stop || sh.cur.idx >= (int32_t)nitems) break;
         const WorkItem &wi = sh.cur.wi;
         const StreamRec &st = sh.cur.st;
         const int BH = (int)st.band_rows;
         const int S = 4 * BH;                 // scanline slots per draw (sub-scanlines for AA)
-        const int K = min(kThreads / S, kMaxSlots);
-        const uint32_t nwin = (st.fill_cnt + (uint32_t)K - 1) / (uint32_t)K;
+        const int K = min(kThreads / S, kMaxSlots);  // a power of two: 8, 16 or 32
+        const int Kshift = 31 - __clz(K);
+        const uint32_t nwin = (st.fill_cnt + (uint32_t)K - 1) >> Kshift;
         // ---- consumers
         const int tpr = kThreads / BH;        // threads per pixel row
         const int row = tid / tpr;
         const int lr = tid % tpr;             // lane within the row: pixel x = x0 + i*tpr + lr
+        // Lane-interleaved pixels: at each step i the 32 lanes of a warp shade 32
+        // neighbouring pixels, which mostly share a run and take the same branches.
+        const int tpr_sh = 31 - __clz(tpr);    // tpr is a power of two
         const int32_t cy = (int32_t)wi.band * BH + row;
         const bool row_ok = cy < st.out_h;
         uint8_t *out = (uint8_t *)(uintptr_t)st.out_ptr;
@@ -542,19 +550,21 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
         int32_t depth = 0;
         int32_t slot_next = 0;
         uint32_t cur_b = 0;      // window buffer of the current fills
+        int32_t cnt_off = 0;     // kMaxPairs after an abort: run counts from the zero half
         uint32_t fill_seen = 0;  // fill commands of the stream before the current one
 
         for (uint32_t ci = 0; ci < st.cmd_cnt; ci++) {
             const Cmd c = cmds[st.cmd_off + ci];
             if (c.op == CMD_FILL || c.op == CMD_APPLY_REGION || c.op == CMD_HAIR) {
-                if (c.op != CMD_HAIR && fill_seen % (uint32_t)K == 0) {
+                if (c.op != CMD_HAIR && (fill_seen & (uint32_t)(K - 1)) == 0) {
                     // ---- the next window: release the previous buffer, wait for this one
-                    const uint32_t gw = win_base + fill_seen / (uint32_t)K;
+                    const uint32_t gw = win_base + (fill_seen >> Kshift);
                     if (fill_seen) mb_arrive(&sh.mb_free[(gw - 1u) & 1u]);
-                    dead |= !mb_wait(&sh.mb_ready[gw & 1u], (gw >> 1) & 1u, err, &sh.abort, wait_limit);
-                    // producers skip windows after an abort but still arrive
-                    dead |= *(volatile int32_t *)&sh.abort != 0;
+                    mb_wait(&sh.mb_ready[gw & 1u], (gw >> 1) & 1u, err, &sh.abort, wait_limit);
+                    // a failed wait sets `abort`; producers skip windows after
+                    // an abort but still arrive
                     cur_b = gw & 1u;
+                    cnt_off = *(volatile int32_t *)&sh.abort != 0 ? kMaxPairs : 0;
                     slot_next = 0;
                 }
                 // ---- phase B: coverage + shading, one pixel per (thread, i).  A hairline
@@ -593,21 +603,23 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
                 } else {
                     fill_seen++;
                     slot = slot_next++;
-                    if (dead) continue;  // the window may not have been produced
                     const int pair = slot * BH + row;
-                    // one entry: the closing sentinel alone, nothing covered on this row
+                    // one entry: the closing sentinel alone, nothing covered on this
+                    // row; none: the window is not read after an abort
                     const WinBuf &wb = sh.win[cur_b];
-                    if (c.op == CMD_FILL && wb.run_cnt[pair] <= 1) continue;
+                    const uint32_t rc = wb.run_cnt[pair + cnt_off];
+                    if (rc == 0u || (rc == 1u && c.op == CMD_FILL)) continue;
                     const int4 geo = wb.slot_geo[slot];
                     ox = geo.y; oy = geo.z;
                     rp = run_base(wb, rovf + (size_t)cur_b * kMaxPairs * rovf_cap, rovf_cap, pair);
                     if (c.op == CMD_FILL) {
-                        // pixel i sits at layer x = x0 - ox + lr + i * tpr
+                        // pixel i sits at layer x = x0 - ox + lr + i * tpr; only
+                        // [first, last) of the row has coverage
                         const int2 e = wb.run_ext[pair];
                         const int32_t b0 = wi.x0 - ox + lr;
                         const int32_t n0 = e.x - b0, n1 = e.y - b0;
-                        i_lo = n0 <= 0 ? 0 : (n0 + tpr - 1) / tpr;
-                        i_hi = n1 <= 0 ? 0 : min(PX, (n1 + tpr - 1) / tpr);
+                        i_lo = n0 <= 0 ? 0 : (n0 + tpr - 1) >> tpr_sh;
+                        i_hi = n1 <= 0 ? 0 : min(PX, (n1 + tpr - 1) >> tpr_sh);
                     }
                 }
                 const WinBuf &pb = sh.win[hair ? 0u : cur_b];
@@ -726,7 +738,7 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
         if (nwin) mb_arrive(&sh.mb_free[(win_base + nwin - 1u) & 1u]);
         win_base += nwin;
         if (depth != 0) atomicOr(err, 8u);
-        if (!dead)
+        if (*(volatile int32_t *)&sh.abort == 0)
             for (int i = 0; i < PX; i++) {
                 const int32_t x = wi.x0 + i * tpr + lr;
                 if (row_ok && x < wi.x1) *(uint32_t *)(out + (size_t)cy * st.out_stride + 4 * (size_t)x) = layer[i * kThreads + tid];

@@ -138,6 +138,24 @@ def test_render_batch_one_submission(batch_case):
     _compare_all(db, refs, "rgpu_render_batch")
 
 
+@pytest.mark.parametrize("chunks", [2, 5, 32])
+def test_render_batch_pipelined_chunks(batch_case, chunks):
+    """rgpu_render_batch with the host/device pipeline forced to `chunks`
+    chunks (two slots alternating, the host flattening a chunk while the
+    device renders the previous one): every scene equals the oracle."""
+    torch = _torch()
+    trees, refs = batch_case
+    db = _DeviceBatch(trees)
+    stream = torch.cuda.Stream()
+    R.set_batch_chunks(chunks)
+    try:
+        R.render_batch(trees, [IDENT] * len(trees), db.ws, db.hs, db.ptrs, stream.cuda_stream)
+        torch.cuda.synchronize()
+    finally:
+        R.set_batch_chunks(0)
+    _compare_all(db, refs, "rgpu_render_batch in %d chunks" % chunks)
+
+
 def test_plain_per_scene_device_calls(batch_case):
     torch = _torch()
     trees, refs = batch_case
@@ -205,8 +223,9 @@ def test_autotuned_tuning_renders_exactly(tuning_case):
 
 
 def test_tuning_table_autotuner_renders_exactly(tuning_case):
-    """The bench's autotuner: band rows per (width, draws) bucket, then pixels
-    per thread; the batch it tunes renders bit-exactly under the table."""
+    """The bench's autotuner: a global (band rows, pixels per thread) choice,
+    then band rows refined per (width, draws) bucket; the batch it tunes
+    renders bit-exactly under the resulting table."""
     import torch
     from resvg_gb300 import batch as BT
     trees, refs = tuning_case
@@ -214,9 +233,10 @@ def test_tuning_table_autotuner_renders_exactly(tuning_case):
     try:
         db = _DeviceBatch(trees)
         table, px, timings = BT.autotune_table(trees, db.ws, db.hs, db.ptrs, reps=1)
-        assert table and px in BT.PX_CANDIDATES
+        assert table and px in {p for _, p in TUNING_CANDIDATES}
         assert R.get_tuning_table() == [tuple(e) for e in table]
-        assert all(b in BT.BAND_CANDIDATES for _, _, b in table)
+        assert all(b in (0,) + BT.BAND_CANDIDATES for _, _, b in table)
+        assert timings["global"] and R.get_tuning() == (0, px)
         scene = R.Scene(trees, [IDENT] * len(trees), db.ws, db.hs, db.ptrs)
         for _ in range(3):
             db.buf.zero_()

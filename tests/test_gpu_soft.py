@@ -127,3 +127,61 @@ def test_config4_shape_runs(gpu):
     for k in GROUPS:
         assert bool(grads[k].isfinite().all())
     assert float(grads["points"].abs().sum()) > 0
+
+
+@pytest.fixture(scope="module")
+def slice_case(gpu):
+    """Four scenes of the config-4 shape (256^2, 64 paths of 2-8 cubic
+    segments, four-stop gradients, per-scene blur): the same generator and
+    sizes as the 256-scene batch, a slice the FP64 reference finishes in
+    seconds."""
+    import torch
+    a = soft.make_scenes(seed=4, scenes=4, size=256, paths=64)
+    t = soft.perturb(a, seed=5)
+    sc, tgt = soft.Scenes(a), soft.Scenes(t)
+    _, target = soft.forward(tgt)
+    torch.cuda.synchronize()
+    return a, sc, target
+
+
+def test_config4_slice_forward_matches_fp64(slice_case, oracle_mod):
+    a, sc, _ = slice_case
+    image, blurred = soft.forward(sc)
+    im64, bl64 = oracle_mod.soft_forward(a)
+    assert np.abs(image.cpu().numpy() - im64).max() <= 2e-4
+    assert np.abs(blurred.cpu().numpy() - bl64).max() <= 2e-4
+
+
+@pytest.mark.parametrize("group", GROUPS + ["all"])
+def test_config4_slice_adjoint_matches_fp64_forward_mode(slice_case, oracle_mod, group):
+    """Directional derivatives of the loss at full scene size: the GPU
+    adjoint against the FP64 forward-mode derivative, 1e-3 relative."""
+    a, sc, target = slice_case
+    loss, grads = _adjoint(sc, target)
+    rng = np.random.default_rng(17)
+    groups = GROUPS if group == "all" else [group]
+    v = {k: rng.normal(size=a[k].shape) for k in groups}
+    adj = sum(float((grads[k].double().cpu().numpy() * v[k]).sum()) for k in groups)
+    loss64, ref = oracle_mod.soft_dloss(a, target.cpu().numpy(), v)
+    assert loss == pytest.approx(loss64, rel=1e-4)
+    assert adj == pytest.approx(ref, rel=1e-3), (adj, ref)
+
+
+@pytest.mark.parametrize("group", ["points", "colors", "sigma", "opacity"])
+def test_config4_slice_adjoint_matches_central_fd(slice_case, oracle_mod, group):
+    """Central differences (step 1e-3) of the FP64 forward at full scene
+    size, 1e-3 relative."""
+    a, sc, target = slice_case
+    _, grads = _adjoint(sc, target)
+    rng = np.random.default_rng(23)
+    v = rng.normal(size=a[group].shape)
+    tgt = target.double().cpu().numpy()
+
+    def L(sign):
+        p = dict(a)
+        p[group] = (a[group].astype(np.float64) + sign * 1e-3 * v).astype(np.float32)
+        return float(((oracle_mod.soft_forward(p)[1] - tgt) ** 2).mean()), p[group]
+    lp, xp = L(+1)
+    lm, xm = L(-1)
+    adj = float((grads[group].double().cpu().numpy() * (xp.astype(np.float64) - xm.astype(np.float64))).sum())
+    assert lp - lm == pytest.approx(adj, rel=1e-3)
