@@ -183,14 +183,23 @@ def peaks():
         return 6800.0, "fallback"
 
 
+def _raster_profile():
+    try:
+        with open(os.path.join(ROOT, "profiles", "raster_traffic.json")) as fh:
+            return json.load(fh)
+    except Exception:
+        return {}
+
+
 def profiled_traffic(key):
     """DRAM bytes per raster launch from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", "raster_traffic.json")
-    try:
-        with open(path) as fh:
-            return json.load(fh).get(key)
-    except Exception:
-        return None
+    return _raster_profile().get(key)
+
+
+def profiled_issue(key):
+    """The raster kernel's issue-rate roof from the committed ncu summary:
+    warp instructions issued / (elapsed SM cycles x 4 schedulers x SMs)."""
+    return _raster_profile().get("issue", {}).get(key)
 
 
 def host_threads():
@@ -517,7 +526,7 @@ def run_batched(args, rank, world):
         "raster_ms": rms,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind, "traffic": profiled_traffic("config3"), "kernel": "k_raster (band VM)",
-                     "algorithmic_bytes": alg_bytes},
+                     "algorithmic_bytes": alg_bytes, "issue_roof": profiled_issue("config3")},
         "e2e": {"value": n_total * 1e3 / e2e_ms, "unit": "scenes/s", "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": int(st["h2d_bytes"]), "d2h_bytes_per_step": int(total),
                 "how": "rgpu_render_batch (host flatten + record upload + kernels) + read-back of every pixmap"},
@@ -739,7 +748,8 @@ def run_plain(args, rank, world):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,
                      "traffic": profiled_traffic("config%d" % args.config),
-                     "kernel": "k_raster (band VM)", "algorithmic_bytes": alg_bytes},
+                     "kernel": "k_raster (band VM)", "algorithmic_bytes": alg_bytes,
+                     "issue_roof": profiled_issue("config%d" % args.config)},
         "e2e": {"value": 1e3 / e2e_ms, "unit": "scenes/s", "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": int(st["h2d_bytes"]), "d2h_bytes_per_step": int(st["d2h_bytes"])},
         "gpu_launches": int(info["kernel_launches"]) * args.steps,
@@ -765,6 +775,19 @@ def run_profile(args):
     from resvg_gb300 import build as B
     B.build()
     R.init(0)
+    if args.config == 4:
+        # forward + loss + adjoint of the 256-scene batch, twice (launches 2 onwards are the second step)
+        from resvg_gb300 import soft
+        a = soft.make_scenes(seed=SEED, scenes=256, size=256, paths=64)
+        sc, tgt = soft.Scenes(a), soft.Scenes(soft.perturb(a, seed=SEED + 1000))
+        _, target = soft.forward(tgt)
+        for _ in range(2):
+            image, blurred = soft.forward(sc)
+            loss, g = soft.mse(blurred, target)
+            soft.backward(sc, image, g)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile": "config4", "scenes": 256, "loss": loss}), flush=True)
+        return
     if args.config == 3:
         trees = [R.Tree.generate(3, seed=SEED, index=i) for i in range(args.scenes)]
     else:

@@ -151,8 +151,8 @@ struct Runner {
     // a private copy of `in` in colour space `lin`
     Img private_in(Img in, bool lin) {
         uint32_t *o = fresh();
-        ck(filter_copy(in.p, o, in.n(), s));
-        if (in.linear != lin) ck(filter_color_space(o, in.n(), lin, s));
+        if (in.linear != lin) ck(filter_color_space_copy(in.p, o, in.n(), lin, s));
+        else ck(filter_copy(in.p, o, in.n(), s));
         return Img{o, lin, in.w, in.h};
     }
     Img in_space(Img in, bool lin) { return in.linear == lin ? in : private_in(in, lin); }
@@ -225,17 +225,21 @@ int run_filter_job(const FilterJob &job, uint32_t *content, uint32_t *result, Fi
                 break;
             }
             case RGPU_FE_COLOR_MATRIX: {
-                res = r.private_in(input(p.in1), lin);
-                r.ck(filter_color_matrix(res.p, res.n(), p.i[0], p.f, s));
+                // out of place from the input in the primitive's space: the
+                // reference's copy-then-modify without the copy pass
+                Img in = r.in_space(input(p.in1), lin);
+                res = Img{r.fresh(), lin, in.w, in.h};
+                r.ck(filter_color_matrix_to(in.p, res.p, res.n(), p.i[0], p.f, s));
                 break;
             }
             case RGPU_FE_MORPHOLOGY: {
-                res = r.private_in(input(p.in1), lin);
+                Img in = r.in_space(input(p.in1), lin);
+                res = Img{r.fresh(), lin, in.w, in.h};
                 float sx = std::sqrt(job.ts.sx * job.ts.sx + job.ts.kx * job.ts.kx);
                 float sy = std::sqrt(job.ts.ky * job.ts.ky + job.ts.sy * job.ts.sy);
                 float rx = p.f[0] * sx, ry = p.f[1] * sy;
                 if (!(rx > 0.0f && ry > 0.0f)) r.ck(filter_fill(res.p, res.n(), 0u, s));
-                else r.ck(filter_morphology(res.p, r.fresh(), res.w, res.h, p.i[0] == 1, rx, ry, s));
+                else r.ck(filter_morphology_to(in.p, res.p, r.fresh(), res.w, res.h, p.i[0] == 1, rx, ry, s));
                 break;
             }
             case RGPU_FE_COMPOSITE: {
@@ -243,7 +247,8 @@ int run_filter_job(const FilterJob &job, uint32_t *content, uint32_t *result, Fi
                 // arithmetic form pairs pixels by index, the others draw both
                 // inputs at the origin
                 Img a = r.in_space(input(p.in1), lin), b = r.in_space(input(p.in2), lin);
-                res = r.blank(rw, rh, lin);
+                if (p.i[0] == RGPU_OP_ARITHMETIC) res = Img{r.fresh(), lin, rw, rh};  // every pixel is written
+                else res = r.blank(rw, rh, lin);
                 if (p.i[0] == RGPU_OP_ARITHMETIC) {
                     const float k[4] = {p.f[0], p.f[1], p.f[2], p.f[3]};
                     if (a.n() < res.n() || b.n() < res.n()) { why = "arithmetic composite of images smaller than the region"; break; }
@@ -496,8 +501,8 @@ int run_filter_job(const FilterJob &job, uint32_t *content, uint32_t *result, Fi
             // cleared, the result drawn at the origin
             Img last = results.back();
             if (last.w == job.w && last.h == job.h) {
-                r.ck(filter_copy(last.p, dst, r.n, s));
-                if (last.linear) r.ck(filter_color_space(dst, r.n, false, s));
+                if (last.linear) r.ck(filter_color_space_copy(last.p, dst, r.n, false, s));
+                else r.ck(filter_copy(last.p, dst, r.n, s));
             } else {
                 Img srgb = last.linear ? r.private_in(last, false) : last;
                 r.ck(filter_fill(dst, r.n, 0u, s));

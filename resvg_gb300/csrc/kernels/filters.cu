@@ -121,6 +121,19 @@ __global__ void k_color_space(uint32_t *img, size_t n, int to_linear) {
     auto g = [t](uint32_t p) { return tab_px(t, p); };
     RGPU_MAP4(img, n, g);
 }
+// the same conversion from `src` into `dst` (a private copy in the other space, one pass)
+__global__ void k_color_space_copy(const uint32_t *src, uint32_t *dst, size_t n, int to_linear) {
+    const int t = to_linear ? TAB_TO_LINEAR : TAB_TO_SRGB;
+    const size_t i = 4 * ((size_t)blockIdx.x * blockDim.x + threadIdx.x);
+    if (i >= n) return;
+    if (vec4(src, i, n) && vec4(dst, i, n)) {
+        uint4 v = *reinterpret_cast<const uint4 *>(src + i);
+        v.x = tab_px(t, v.x); v.y = tab_px(t, v.y); v.z = tab_px(t, v.z); v.w = tab_px(t, v.w);
+        *reinterpret_cast<uint4 *>(dst + i) = v;
+    } else {
+        for (size_t k = i; k < n && k < i + 4; k++) dst[k] = tab_px(t, src[k]);
+    }
+}
 
 // One box pass along lines: line l, element k at base + l*lstride + k*stride.
 // Each thread produces `seg` consecutive outputs with a zero-padded sliding
@@ -221,13 +234,19 @@ __global__ void k_iir_store4(uint32_t *img, const double *planes, size_t n, doub
     img[i] = o;
 }
 
+// c / 255 in f32 for every u8 c, the IEEE quotient (host division is IEEE
+// too): kernels read it from shared memory instead of dividing per channel.
+__device__ float g_unit[256];
+__device__ __forceinline__ void load_unit(float *u) {
+    for (int k = threadIdx.x; k < 256; k += blockDim.x) u[k] = g_unit[k];
+}
 // ---- colour matrix (color_matrix.rs), demultiply and multiply fused
 struct CmParams { int kind; float m[20]; };
 __device__ __forceinline__ uint32_t from_normalized(float c) { return sat_u8f(f32_bound(0.0f, c, 1.0f) * 255.0f); }
-__device__ __forceinline__ uint32_t color_matrix_px(uint32_t px, const CmParams &cp) {
+// `unit[c]` = c / 255 (the IEEE quotient, from a table instead of a division per channel)
+__device__ __forceinline__ uint32_t color_matrix_px(uint32_t px, const CmParams &cp, const float *unit) {
     uint32_t p = tab_px(TAB_DEMUL, px);
-    float r = (float)chn(p, 0) / 255.0f, g = (float)chn(p, 1) / 255.0f, b = (float)chn(p, 2) / 255.0f,
-          a = (float)chn(p, 3) / 255.0f;
+    float r = unit[chn(p, 0)], g = unit[chn(p, 1)], b = unit[chn(p, 2)], a = unit[chn(p, 3)];
     const float *m = cp.m;
     uint32_t o;
     if (cp.kind == 0) {
@@ -245,9 +264,20 @@ __device__ __forceinline__ uint32_t color_matrix_px(uint32_t px, const CmParams 
     }
     return tab_px(TAB_MUL, o);
 }
-__global__ void k_color_matrix(uint32_t *img, size_t n, CmParams cp) {
-    auto f = [&cp](uint32_t p) { return color_matrix_px(p, cp); };
-    RGPU_MAP4(img, n, f);
+__global__ void k_color_matrix(const uint32_t *src, uint32_t *dst, size_t n, CmParams cp) {
+    __shared__ float u[256];
+    load_unit(u);
+    __syncthreads();
+    const size_t i = 4 * ((size_t)blockIdx.x * blockDim.x + threadIdx.x);
+    if (i >= n) return;
+    if (vec4(src, i, n) && vec4(dst, i, n)) {
+        uint4 v = *reinterpret_cast<const uint4 *>(src + i);
+        v.x = color_matrix_px(v.x, cp, u); v.y = color_matrix_px(v.y, cp, u);
+        v.z = color_matrix_px(v.z, cp, u); v.w = color_matrix_px(v.w, cp, u);
+        *reinterpret_cast<uint4 *>(dst + i) = v;
+    } else {
+        for (size_t k = i; k < n && k < i + 4; k++) dst[k] = color_matrix_px(src[k], cp, u);
+    }
 }
 
 // ---- morphology: window [x - tx, x - tx + cols) x [y - ty, y - ty + rows),
@@ -278,12 +308,6 @@ __device__ __forceinline__ bool approx_zero_ulps4(float v) {
     int32_t a = __float_as_int(v);
     if (a < 0) return v == 0.0f;
     return a <= 4;
-}
-// c / 255 in f32 for every u8 c, the IEEE quotient (host division is IEEE
-// too): kernels read it from shared memory instead of dividing per channel.
-__device__ float g_unit[256];
-__device__ __forceinline__ void load_unit(float *u) {
-    for (int k = threadIdx.x; k < 256; k += blockDim.x) u[k] = g_unit[k];
 }
 __device__ __forceinline__ uint32_t arithmetic_px(uint32_t c1, uint32_t c2, float k1, float k2, float k3, float k4,
                                                   const float *u) {
@@ -371,6 +395,14 @@ cudaError_t filter_color_space(uint32_t *img, size_t n, bool to_linear, cudaStre
     cudaError_t e = ensure_luts();
     if (e != cudaSuccess || n == 0) return e;
     k_color_space<<<nblk((n + 3) / 4, 256), 256, 0, s>>>(img, n, to_linear ? 1 : 0);
+    return cudaGetLastError();
+}
+
+cudaError_t filter_color_space_copy(const uint32_t *src, uint32_t *dst, size_t n, bool to_linear, cudaStream_t s) {
+    cudaError_t e = ensure_luts();
+    if (e != cudaSuccess) return e;
+    if (n == 0) return cudaSuccess;
+    k_color_space_copy<<<nblk((n + 3) / 4, 256), 256, 0, s>>>(src, dst, n, to_linear ? 1 : 0);
     return cudaGetLastError();
 }
 
@@ -825,7 +857,7 @@ __global__ void k_iir_fast_load(const uint32_t *img, float *planes, size_t n) {
     if (i >= n) return;
     const uint32_t p = img[i];
 #pragma unroll
-    for (int ch = 0; ch < 4; ch++) planes[(size_t)ch * n + i] = (float)chn(p, ch) / 255.0f;
+    for (int ch = 0; ch < 4; ch++) planes[(size_t)ch * n + i] = __ldg(&g_unit[chn(p, ch)]);
 }
 
 __global__ void k_iir_fast_store(uint32_t *img, const float *planes, size_t n, float post) {
@@ -863,6 +895,8 @@ static cudaError_t iir_blur_fast(uint32_t *img, float *a, float *b, int w, int h
                                  bool by, double post, cudaStream_t s) {
     const int steps = 4;
     const size_t n = (size_t)w * h;
+    cudaError_t te = ensure_luts();  // the c / 255 table the load reads
+    if (te != cudaSuccess) return te;
     k_iir_fast_load<<<nblk(n, 256), 256, 0, s>>>(img, a, n);
     if (bx) k_iir_fast_lines<<<(unsigned)(4 * h), kIirLine, 0, s>>>(a, w, (float)dx, steps);
     if (by) {
@@ -895,6 +929,11 @@ cudaError_t filter_iir_blur(uint32_t *img, double *buf, int w, int h, double sx,
 }
 
 cudaError_t filter_color_matrix(uint32_t *img, size_t n, int kind, const float *values, cudaStream_t s) {
+    return filter_color_matrix_to(img, img, n, kind, values, s);
+}
+
+cudaError_t filter_color_matrix_to(const uint32_t *src, uint32_t *dst, size_t n, int kind, const float *values,
+                                   cudaStream_t s) {
     CmParams cp;
     cp.kind = 0;
     for (int i = 0; i < 20; i++) cp.m[i] = 0.0f;
@@ -925,11 +964,40 @@ cudaError_t filter_color_matrix(uint32_t *img, size_t n, int kind, const float *
     if (n == 0) return cudaSuccess;
     cudaError_t te = ensure_luts();
     if (te != cudaSuccess) return te;
-    k_color_matrix<<<nblk((n + 3) / 4, 256), 256, 0, s>>>(img, n, cp);
+    k_color_matrix<<<nblk((n + 3) / 4, 256), 256, 0, s>>>(src, dst, n, cp);
     return cudaGetLastError();
 }
 
 // morphology.rs: window columns = min(2*ceil(rx), w), rows likewise, target = floor(n/2)
+cudaError_t filter_morphology_to(const uint32_t *src, uint32_t *dst, uint32_t *tmp, int w, int h, bool dilate,
+                                 float rx, float ry, cudaStream_t s) {
+    int cols = (int)fminf(ceilf(rx) * 2.0f, (float)w), rows = (int)fminf(ceilf(ry) * 2.0f, (float)h);
+    int txc = (int)floorf((float)cols / 2.0f), tyr = (int)floorf((float)rows / 2.0f);
+    size_t n = (size_t)w * h;
+    if (n == 0) return cudaSuccess;
+    cudaError_t ae = box_attrs();
+    if (ae != cudaSuccess) return ae;
+    if (cols <= kMorphPairMaxTaps && rows <= kMorphPairMaxTaps) {
+        dim3 g((unsigned)((w + kPairTX - 1) / kPairTX), (unsigned)((h + kPairTY - 1) / kPairTY));
+        k_morph_vh<<<g, 256, morph_pair_smem(cols, rows), s>>>(src, dst, w, h, cols, rows, txc, tyr, dilate ? 1 : 0);
+        return cudaGetLastError();
+    }
+    // separate passes: rows src -> tmp, columns tmp -> dst
+    if (cols <= kMorphMaxTaps) {
+        dim3 g((unsigned)((w + kBoxT - 1) / kBoxT), (unsigned)((h + 31) / 32));
+        k_morph_h<<<g, 256, morph_h_smem(cols), s>>>(src, tmp, w, h, cols, txc, dilate ? 1 : 0);
+    } else {
+        k_morph_pass<<<nblk(n, 256), 256, 0, s>>>(src, tmp, w, h, 1, (size_t)w, cols, txc, dilate ? 1 : 0);
+    }
+    if (rows <= kMorphMaxTaps) {
+        dim3 g((unsigned)((w + 31) / 32), (unsigned)((h + kBoxT - 1) / kBoxT));
+        k_morph_v<<<g, 256, morph_v_smem(rows), s>>>(tmp, dst, w, h, rows, tyr, dilate ? 1 : 0);
+    } else {
+        k_morph_pass<<<nblk(n, 256), 256, 0, s>>>(tmp, dst, h, w, (size_t)w, 1, rows, tyr, dilate ? 1 : 0);
+    }
+    return cudaGetLastError();
+}
+
 cudaError_t filter_morphology(uint32_t *img, uint32_t *tmp, int w, int h, bool dilate, float rx, float ry,
                               cudaStream_t s) {
     int cols = (int)fminf(ceilf(rx) * 2.0f, (float)w), rows = (int)fminf(ceilf(ry) * 2.0f, (float)h);

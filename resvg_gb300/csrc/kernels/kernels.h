@@ -45,6 +45,8 @@ int raster_max_pairs();  // (draw, row) pairs of one phase-A window
 
 // filters.cu
 cudaError_t filter_color_space(uint32_t *img, size_t n, bool to_linear, cudaStream_t s);
+// the conversion of `src` written to `dst` (one pass instead of a copy and a conversion)
+cudaError_t filter_color_space_copy(const uint32_t *src, uint32_t *dst, size_t n, bool to_linear, cudaStream_t s);
 void box_sizes(float sigma, int sizes[5]);
 // Largest standard deviation the box blur computes with; larger ones give the
 // same (fully transparent) result and are clamped to it.
@@ -58,6 +60,11 @@ cudaError_t filter_iir_blur(uint32_t *img, double *buf, int w, int h, double sx,
 void filter_set_iir_fast(bool on);
 bool filter_iir_fast();
 cudaError_t filter_color_matrix(uint32_t *img, size_t n, int kind, const float *values, cudaStream_t s);
+// out of place: `src` (read only) to `dst`; the same pixels as the in-place form
+cudaError_t filter_color_matrix_to(const uint32_t *src, uint32_t *dst, size_t n, int kind, const float *values,
+                                   cudaStream_t s);
+cudaError_t filter_morphology_to(const uint32_t *src, uint32_t *dst, uint32_t *tmp, int w, int h, bool dilate,
+                                 float rx, float ry, cudaStream_t s);
 cudaError_t filter_morphology(uint32_t *img, uint32_t *tmp, int w, int h, bool dilate, float rx, float ry,
                               cudaStream_t s);
 cudaError_t filter_arithmetic(const uint32_t *a, const uint32_t *b, uint32_t *dst, size_t n, const float k[4],

@@ -191,6 +191,13 @@ struct RowShared {
     int warp_count[kThreads / 32];
     float sbuf[kThreads * kMaxPx];  // adjoint: suffix sums of dL/dA over the row, by pixel x
     float dbuf[kThreads * kMaxPx];  // adjoint: dL/dA by pixel x
+    // row areas in 2^-40 fixed point, so the sums are exact whatever the order:
+    // lines wholly left of a pixel (a difference array, then a prefix sum), and
+    // the partial contributions of the lines crossing the pixel's column span
+    long long full[kThreads * kMaxPx];
+    long long part[kThreads * kMaxPx];
+    long long wtot[kThreads / 32];
+    float wtotf[kThreads / 32];
 };
 
 __device__ __forceinline__ uint32_t path_vbase(const rgpu_soft_batch &B, uint32_t j) { return kFlat * B.seg_offset[j]; }
@@ -228,13 +235,123 @@ __device__ void gather_crossings(RowShared &sh, const float2 *verts, uint32_t vb
     }
 }
 
-__device__ __forceinline__ float area_at(const RowShared &sh, float px) {
-    float A = 0.0f;
-    for (int i = 0; i < sh.ncross; i++) {
-        const float4 c = sh.cross[i];
-        A += c.z * mean_right<float>(c.x - px, c.y - px);
+constexpr float kFix = 1099511627776.0f;  // 2^40
+
+// The area A(x) = sum over the crossing lines of sdy * mean_right(xl - x, xh - x)
+// for every pixel x of the row, by line instead of by pixel: a line adds sdy
+// in full to every pixel from ceil(max(xl, xh)) on (there mean_right is 1),
+// and evaluates mean_right only over the pixels its x range touches (from
+// floor(min(xl, xh)); 0 left of them).  The per-pixel loop over all lines
+// costs W x lines; this costs W + the lines' pixel spans.  Sums are taken in
+// 2^-40 fixed point with 64-bit shared atomics, so they do not depend on the
+// order lines are added in.  All threads call it; A[k] is pixel tid + k x kThreads.
+__device__ void row_areas(RowShared &sh, int W, float A[kMaxPx]) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int x = tid; x < W; x += kThreads) {
+        sh.full[x] = 0;
+        sh.part[x] = 0;
     }
-    return A;
+    __syncthreads();
+    for (int ci = warp; ci < sh.ncross; ci += kThreads / 32) {
+        const float4 c = sh.cross[ci];
+        const float xmin = fminf(c.x, c.y), xmax = fmaxf(c.x, c.y);
+        const int xr = (int)ceilf(fminf(fmaxf(xmax, -1.0f), (float)W));  // first pixel with mean_right = 1
+        if (lane == 0 && xr < W)
+            atomicAdd((unsigned long long *)&sh.full[max(xr, 0)], (unsigned long long)__float2ll_rn(c.z * kFix));
+        const int x_lo = max((int)floorf(fminf(fmaxf(xmin, -1.0f), (float)W)), 0);
+        const int x_hi = min(xr, W) - 1;
+        for (int x = x_lo + lane; x <= x_hi; x += 32) {
+            const float v = c.z * mean_right<float>(c.x - (float)x, c.y - (float)x);
+            if (v != 0.0f) atomicAdd((unsigned long long *)&sh.part[x], (unsigned long long)__float2ll_rn(v * kFix));
+        }
+    }
+    __syncthreads();
+    // inclusive prefix sum of `full`: each thread a run of kMaxPx pixels
+    long long v[kMaxPx];
+    long long run = 0;
+    const int base = tid * kMaxPx;
+#pragma unroll
+    for (int k = 0; k < kMaxPx; k++) {
+        run += base + k < W ? sh.full[base + k] : 0;
+        v[k] = run;
+    }
+    long long sc = run;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const long long t = __shfl_up_sync(0xffffffffu, sc, o);
+        if (lane >= o) sc += t;
+    }
+    if (lane == 31) sh.wtot[warp] = sc;
+    __syncthreads();
+    long long off = sc - run;
+    for (int w = 0; w < warp; w++) off += sh.wtot[w];
+#pragma unroll
+    for (int k = 0; k < kMaxPx; k++)
+        if (base + k < W) sh.full[base + k] = v[k] + off;
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kMaxPx; k++) {
+        const int x = tid + k * kThreads;
+        A[k] = x < W ? __ll2float_rn(sh.full[x] + sh.part[x]) * (1.0f / kFix) : 0.0f;
+    }
+    __syncthreads();  // the accumulators are read before the next path clears them
+}
+
+// sbuf[x] = sum of dbuf[q] for q >= x, x < W: a block-wide scan over the
+// reversed row (each thread a run of kMaxPx pixels from the right), ending
+// with a barrier.
+__device__ void suffix_sums(RowShared &sh, int W) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    float v[kMaxPx];
+    float run = 0.0f;
+    const int base = tid * kMaxPx;  // reversed position y = W - 1 - x
+#pragma unroll
+    for (int k = 0; k < kMaxPx; k++) {
+        const int y = base + k;
+        run += y < W ? sh.dbuf[W - 1 - y] : 0.0f;
+        v[k] = run;
+    }
+    float sc = run;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const float t = __shfl_up_sync(0xffffffffu, sc, o);
+        if (lane >= o) sc += t;
+    }
+    if (lane == 31) sh.wtotf[warp] = sc;
+    __syncthreads();
+    float off = 0.0f;
+    for (int w = 0; w < warp; w++) off += sh.wtotf[w];
+    off += sc - run;
+#pragma unroll
+    for (int k = 0; k < kMaxPx; k++) {
+        const int y = base + k;
+        if (y < W) sh.sbuf[W - 1 - y] = v[k] + off;
+    }
+    __syncthreads();
+}
+
+// A(x) for this thread's pixels: summed per pixel over the row's lines when
+// they are few (lines x pixels per thread <= kLineLoopMax: cheaper than
+// row_areas' four barriers), else by row_areas.  The choice depends only on
+// shared values, so every thread takes the same branch.
+constexpr int kLineLoopMax = 24;
+__device__ void areas(RowShared &sh, int W, float A[kMaxPx]) {
+    const int ppt = (W + kThreads - 1) / kThreads;
+    if (sh.ncross * ppt > kLineLoopMax) {
+        row_areas(sh, W, A);
+        return;
+    }
+#pragma unroll
+    for (int k = 0; k < kMaxPx; k++) {
+        const int x = (int)threadIdx.x + k * kThreads;
+        float a = 0.0f;
+        if (x < W)
+            for (int i = 0; i < sh.ncross; i++) {
+                const float4 c = sh.cross[i];
+                a += c.z * mean_right<float>(c.x - (float)x, c.y - (float)x);
+            }
+        A[k] = a;
+    }
 }
 
 // ---- forward: one CTA per (scene, row)
@@ -252,11 +369,13 @@ __global__ void __launch_bounds__(kThreads) k_forward(rgpu_soft_batch B, const f
         gather_crossings(sh, verts, path_vbase(B, j), path_nverts(B, j), (float)py);
         if (threadIdx.x == 0 && sh.ncross >= kMaxCross) atomicOr(overflow, 1u);
         if (sh.ncross > 0) {
+            float Ar[kMaxPx];
+            areas(sh, W, Ar);
 #pragma unroll
             for (int k = 0; k < kMaxPx; k++) {
                 const int x = (int)threadIdx.x + k * kThreads;
                 if (x >= W) continue;
-                const float A = area_at(sh, (float)x);
+                const float A = Ar[k];
                 const float c = fminf(fabsf(A), 1.0f);
                 if (c == 0.0f) continue;
                 const PaintOut po = eval_paint(B, j, (float)x + 0.5f, (float)py + 0.5f);
@@ -416,7 +535,7 @@ __device__ __forceinline__ float warp_sum(float v) {
     return v;
 }
 
-__global__ void __launch_bounds__(kThreads) k_backward(rgpu_soft_batch B, rgpu_soft_grads G, const float2 *verts,
+__global__ void __launch_bounds__(kThreads, 3) k_backward(rgpu_soft_batch B, rgpu_soft_grads G, const float2 *verts,
                                                        const float4 *grad_image, float *scratch_area,
                                                        float4 *scratch_color, float2 *vgrad, uint32_t *row_counter,
                                                        uint32_t *overflow) {
@@ -444,14 +563,17 @@ __global__ void __launch_bounds__(kThreads) k_backward(rgpu_soft_batch B, rgpu_s
             const uint32_t j = s * P + p;
             gather_crossings(sh, verts, path_vbase(B, j), path_nverts(B, j), (float)py);
             if (tid == 0 && sh.ncross >= kMaxCross) atomicOr(overflow, 1u);
+            float Ar[kMaxPx] = {0.0f, 0.0f, 0.0f, 0.0f};
+            if (sh.ncross > 0) areas(sh, W, Ar);
 #pragma unroll
             for (int k = 0; k < kMaxPx; k++) {
                 const int x = tid + k * kThreads;
                 const size_t si = ((size_t)p * kMaxPx + k) * kThreads + tid;
-                float A = 0.0f;
-                if (x < W && sh.ncross > 0) A = area_at(sh, (float)x);
-                areaS[si] = A;
-                colS[si] = C[k];
+                const float A = x < W ? Ar[k] : 0.0f;
+                if (x < W) {  // scratch only for the row's pixels
+                    areaS[si] = A;
+                    colS[si] = C[k];
+                }
                 const float c = fminf(fabsf(A), 1.0f);
                 if (x < W && c != 0.0f) {
                     const PaintOut po = eval_paint(B, j, (float)x + 0.5f, (float)py + 0.5f);
@@ -481,7 +603,7 @@ __global__ void __launch_bounds__(kThreads) k_backward(rgpu_soft_batch B, rgpu_s
             for (int k = 0; k < kMaxPx; k++) {
                 const int x = tid + k * kThreads;
                 const size_t si = ((size_t)p * kMaxPx + k) * kThreads + tid;
-                const float A = areaS[si];
+                const float A = x < W ? areaS[si] : 0.0f;
                 const float c = fminf(fabsf(A), 1.0f);
                 float dA = 0.0f;
                 if (x < W && c != 0.0f) {
@@ -531,7 +653,7 @@ __global__ void __launch_bounds__(kThreads) k_backward(rgpu_soft_batch B, rgpu_s
                     const float dcA = (fabsf(A) < 1.0f) ? (A > 0.0f ? 1.0f : (A < 0.0f ? -1.0f : 0.0f)) : 0.0f;
                     dA = dc * dcA;
                 }
-                areaS[si] = dA;
+                if (x < W) areaS[si] = dA;
             }
             // reduce the paint gradients of this path over the row
             if (tid < kAcc) pacc[tid] = 0.0f;
@@ -560,24 +682,11 @@ __global__ void __launch_bounds__(kThreads) k_backward(rgpu_soft_batch B, rgpu_s
 #pragma unroll
             for (int k = 0; k < kMaxPx; k++) {
                 const size_t si = ((size_t)p * kMaxPx + k) * kThreads + tid;
-                sh.dbuf[k * kThreads + tid] = areaS[si];
+                const int x = tid + k * kThreads;
+                sh.dbuf[x] = x < W ? areaS[si] : 0.0f;
             }
             __syncthreads();
-            if (warp == 0) {
-                float carry = 0.0f;
-                for (int base = ((W - 1) / 32) * 32; base >= 0; base -= 32) {
-                    const int x = base + 31 - lane;  // lane 0 holds the right-most pixel of the chunk
-                    float v = x < W ? sh.dbuf[x] : 0.0f;
-                    for (int o = 1; o < 32; o <<= 1) {
-                        const float t = __shfl_up_sync(0xffffffffu, v, o);
-                        if (lane >= o) v += t;
-                    }
-                    v += carry;
-                    if (x < W) sh.sbuf[x] = v;
-                    carry = __shfl_sync(0xffffffffu, v, 31);
-                }
-            }
-            __syncthreads();
+            suffix_sums(sh, W);
             gather_crossings(sh, verts, path_vbase(B, j), path_nverts(B, j), (float)py);
             auto S = [&](int x) -> float { return x >= W ? 0.0f : sh.sbuf[max(x, 0)]; };
             const uint32_t vb = path_vbase(B, j), nv = path_nverts(B, j);
@@ -591,30 +700,27 @@ __global__ void __launch_bounds__(kThreads) k_backward(rgpu_soft_batch B, rgpu_s
                 x_lo = max(x_lo, 0);
                 x_hi = min(x_hi, W - 1);
                 float g[4] = {0.f, 0.f, 0.f, 0.f};
-                for (int x = x_lo + lane; x <= x_hi; x += 32) {
-                    const float d = sh.dbuf[x];
-                    if (d == 0.0f) continue;
-                    D4 X0 = mk(a.x), Y0 = mk(a.y), X1 = mk(b.x), Y1 = mk(b.y);
-                    X0.d[0] = 1.f; Y0.d[1] = 1.f; X1.d[2] = 1.f; Y1.d[3] = 1.f;
-                    D4 xl, xh, sdy;
-                    if (clip_row<D4>(X0, Y0, X1, Y1, (float)py, &xl, &xh, &sdy)) {
+                // the line clipped to the row, with derivatives in its end
+                // coordinates (the same for every pixel of the row)
+                D4 X0 = mk(a.x), Y0 = mk(a.y), X1 = mk(b.x), Y1 = mk(b.y);
+                X0.d[0] = 1.f; Y0.d[1] = 1.f; X1.d[2] = 1.f; Y1.d[3] = 1.f;
+                D4 xl, xh, sdy;
+                const bool crosses = clip_row<D4>(X0, Y0, X1, Y1, (float)py, &xl, &xh, &sdy);
+                if (crosses)
+                    for (int x = x_lo + lane; x <= x_hi; x += 32) {
+                        const float d = sh.dbuf[x];
+                        if (d == 0.0f) continue;
                         const D4 v = sdy * mean_right<D4>(xl - (float)x, xh - (float)x);
 #pragma unroll
                         for (int q = 0; q < 4; q++) g[q] += d * v.d[q];
                     }
-                }
                 // pixels right of the line: area = sdy, weighted by the suffix sum
                 const int xr = max((int)ceilf(xmax), 0);
-                if (lane == 0 && xr < W) {
+                if (crosses && lane == 0 && xr < W) {
                     const float sr = S(xr);
                     if (sr != 0.0f) {
-                        D4 X0 = mk(a.x), Y0 = mk(a.y), X1 = mk(b.x), Y1 = mk(b.y);
-                        X0.d[0] = 1.f; Y0.d[1] = 1.f; X1.d[2] = 1.f; Y1.d[3] = 1.f;
-                        D4 xl, xh, sdy;
-                        if (clip_row<D4>(X0, Y0, X1, Y1, (float)py, &xl, &xh, &sdy)) {
 #pragma unroll
-                            for (int q = 0; q < 4; q++) g[q] += sr * sdy.d[q];
-                        }
+                        for (int q = 0; q < 4; q++) g[q] += sr * sdy.d[q];
                     }
                 }
 #pragma unroll
