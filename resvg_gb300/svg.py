@@ -1154,7 +1154,7 @@ INHERITED = {"fill", "fill-opacity", "fill-rule", "stroke", "stroke-width", "str
              "shape-rendering", "clip-rule", "color", "color-interpolation-filters", "paint-order", "font-size"}
 NON_INHERITED = {"opacity", "clip-path", "mask", "filter", "mix-blend-mode", "isolation", "display",
                  "stop-color", "stop-opacity", "flood-color", "flood-opacity", "transform"}
-UNSUPPORTED_ELEMS = {"text", "switch", "foreignObject", "tspan", "textPath", "symbol",
+UNSUPPORTED_ELEMS = {"text", "switch", "foreignObject", "tspan", "textPath",
                      "animate", "set"}
 BLEND = {"normal": "source-over", "multiply": "multiply", "screen": "screen", "overlay": "overlay",
          "darken": "darken", "lighten": "lighten", "color-dodge": "color-dodge", "color-burn": "color-burn",
@@ -1285,6 +1285,7 @@ class Loader:
         # or "server" for a gradient or pattern
         self.marker_stack = []
         self.ctx = None
+        self.use_size = (None, None)  # width / height of the <use> instancing an <svg>
         self.solid_ids = set()
         self.ids_out = {}  # SVG id -> the oracle's node id ("<group>" or "p<path>")
 
@@ -1438,7 +1439,7 @@ class Builder(Loader):
     def node(self, e, parent, transform_extra=IDENT):
         tag = _tag(e)
         if tag in ("defs", "linearGradient", "radialGradient", "clipPath", "mask", "filter", "title", "desc",
-                   "metadata", "stop", "pattern", "style", "marker"):
+                   "metadata", "stop", "pattern", "style", "marker", "symbol"):
             return
         if not self.visible(e):
             return
@@ -1457,9 +1458,10 @@ class Builder(Loader):
                 return
             x = self.num(e, "x", 0.0, self.vbw)
             y = self.num(e, "y", 0.0, self.vbh)
+            if _tag(ref) == "symbol":
+                self.use_symbol(e, ref, parent, ts, x, y)
+                return
             ts = mat_mul(ts, (1, 0, 0, 1, x, y))
-            if _tag(ref) == "svg" or _tag(ref) == "symbol":
-                raise Unsupported("use of svg/symbol")
         g = self.group_for(e, parent, ts)
         if g is None:
             return
@@ -1477,13 +1479,19 @@ class Builder(Loader):
             # use_node.rs convert: the <use> element's fill and stroke are the
             # context paints of what it instances
             ctx = (self.context_paint(e, "fill"), self.context_paint(e, "stroke"))
-            saved, saved_ctx = self.parent.get(ref), self.ctx
+            saved, saved_ctx, saved_us = self.parent.get(ref), self.ctx, self.use_size
+            if _tag(ref) == "svg":
+                # use_node.rs: the <use>'s width / height, when given, replace
+                # the referenced <svg>'s (each <use> resets both)
+                self.use_size = (self.num(e, "width", None, self.vbw) if e.get("width") is not None else None,
+                                 self.num(e, "height", None, self.vbh) if e.get("height") is not None else None)
             self.parent[ref] = e
             self.ctx = ctx
             try:
                 self.node(ref, g)
             finally:
                 self.ctx = saved_ctx
+                self.use_size = saved_us
                 if saved is None:
                     self.parent.pop(ref, None)
                 else:
@@ -1497,9 +1505,14 @@ class Builder(Loader):
         """A nested <svg> as usvg converts it (use_node.rs:163-211, 295-371): its
         content under translate(x, y) and the viewBox transform, in a new
         viewport for percentages, clipped to (x, y, width, height) unless
-        overflow is visible / auto or width and height are not both given."""
+        overflow is visible / auto or width and height are not both given.
+        Inside a <use>, the <use>'s width / height replace the element's, and
+        then the clip applies even without the element's own width and height."""
         x, y = self.num(e, "x", 0.0, self.vbw), self.num(e, "y", 0.0, self.vbh)
         w, h = self.num(e, "width", self.vbw, self.vbw), self.num(e, "height", self.vbh, self.vbh)
+        us = self.use_size
+        w = us[0] if us[0] is not None else w
+        h = us[1] if us[1] is not None else h
         vb = numbers(e.get("viewBox")) if e.get("viewBox") is not None else None
         if vb is not None and (len(vb) != 4 or not (vb[2] > 0 and vb[3] > 0)):
             vb = None
@@ -1509,8 +1522,8 @@ class Builder(Loader):
         new_vb = (vb[2], vb[3]) if vb is not None else ((w, h) if w > 0 and h > 0 else (self.vbw, self.vbh))
         ov = (self.attrs(e).get("overflow") or "").strip()
         parent = g
-        if ov not in ("visible", "auto") and e.get("width") is not None and e.get("height") is not None \
-                and w > 0 and h > 0:
+        sized = (e.get("width") is not None and e.get("height") is not None) or us != (None, None)
+        if ov not in ("visible", "auto") and sized and w > 0 and h > 0 and math.isfinite(w) and math.isfinite(h):
             root = self.tree.add_group(-1, _group())
             self.rect_path(root, (x, y, w, h), self.solid(((0, 0, 0), 1.0)))
             c = A.Clip()
@@ -1526,6 +1539,69 @@ class Builder(Loader):
                 self.node(c, inner)
         finally:
             self.vbw, self.vbh = saved
+
+    def use_symbol(self, e, sym, parent, ts_use, x, y):
+        """<use> of a <symbol> as usvg converts it (use_node.rs convert,
+        linked_to_symbol): percentages inside the symbol resolve against the
+        <use>'s width / height when given; the symbol's content goes under
+        translate(x, y) and the fit of the symbol's viewBox into the <use>'s
+        size (100% by default); unless the symbol's overflow is visible / auto
+        it is clipped to (x, y, width, height) of the <use>, in a group that
+        carries the <use>'s transform, the <use>'s own group inside it without
+        one; otherwise the <use>'s transform moves onto the symbol's group.
+        The symbol's own transform attribute is not used."""
+        n = e
+        while n is not None:  # a <use> inside what it references: not rendered
+            if n is sym:
+                return
+            n = self.parent.get(n)
+        vbw, vbh = self.vbw, self.vbh
+        nw = self.num(e, "width", vbw, vbw) if e.get("width") is not None else vbw
+        nh = self.num(e, "height", vbh, vbh) if e.get("height") is not None else vbh
+        if not (nw > 0 and nh > 0 and math.isfinite(nw) and math.isfinite(nh)):
+            nw, nh = vbw, vbh
+        ctx = (self.context_paint(e, "fill"), self.context_paint(e, "stroke"))
+        saved_parent, saved_ctx = self.parent.get(sym), self.ctx
+        self.vbw, self.vbh = nw, nh
+        self.parent[sym] = e
+        self.ctx = ctx
+        try:
+            uw, uh = self.num(e, "width", nw, nw), self.num(e, "height", nh, nh)
+            new_ts = (1.0, 0.0, 0.0, 1.0, x, y)
+            vb = numbers(sym.get("viewBox")) if sym.get("viewBox") is not None else None
+            if vb is not None and (len(vb) != 4 or not (vb[2] > 0 and vb[3] > 0)):
+                vb = None
+            if vb is not None and uw > 0 and uh > 0:
+                new_ts = mat_mul(new_ts, view_box_transform(vb, sym.get("preserveAspectRatio") or "", uw, uh))
+            ov = (self.attrs(sym).get("overflow") or "").strip()
+            if ov not in ("visible", "auto") and uw > 0 and uh > 0 and math.isfinite(uw) and math.isfinite(uh):
+                cx, cy = self.num(e, "x", 0.0, nw), self.num(e, "y", 0.0, nh)
+                root = self.tree.add_group(-1, _group())
+                self.rect_path(root, (cx, cy, uw, uh), self.solid(((0, 0, 0), 1.0)))
+                c = A.Clip()
+                c.transform = _tf(IDENT)
+                c.clip_path = -1
+                c.root = root
+                cg = self.tree.add_group(parent, _group(transform=_tf(ts_use), clip_path=self.tree.add_clip(c)))
+                gu = self.group_for(e, cg, IDENT)
+                sym_ts = new_ts
+            else:
+                gu = self.group_for(e, parent, IDENT)
+                sym_ts = mat_mul(ts_use, new_ts)
+            if gu is None:
+                return
+            gs = self.group_for(sym, gu, sym_ts)
+            if gs is None:
+                return
+            for c in sym:
+                self.node(c, gs)
+        finally:
+            self.vbw, self.vbh = vbw, vbh
+            self.ctx = saved_ctx
+            if saved_parent is None:
+                self.parent.pop(sym, None)
+            else:
+                self.parent[sym] = saved_parent
 
     def group_for(self, e, parent, ts):
         """Creates the group an element needs (transform, opacity, clip, mask,
@@ -1932,11 +2008,21 @@ class Builder(Loader):
             prev = o
             o = max(0.0, min(1.0, o))
             col = sa.get("stop-color", "black")
+            sop_v = sa.get("stop-opacity", "1")
+            # `inherit` on these non-inherited properties takes the direct
+            # parent's value, else the initial one (svgtree resolve_inherit)
+            par = self.attrs(self.parent[s]) if self.parent.get(s) is not None else {}
+            if col.strip() == "inherit":
+                col = par.get("stop-color", "black")
+                col = "black" if col.strip() == "inherit" else col
+            if sop_v.strip() == "inherit":
+                sop_v = par.get("stop-opacity", "1")
+                sop_v = "1" if sop_v.strip() == "inherit" else sop_v
             # currentColor: the `color` the stop inherits through its ancestors
             cur_s = self.get(s, "color")
             cur_c = parse_color(cur_s) if cur_s is not None else None
             c = parse_color(col, cur_c[0] if cur_c else (0, 0, 0)) or ((0, 0, 0), 0.0)
-            sop = sa.get("stop-opacity", "1").strip()
+            sop = sop_v.strip()
             sop = float(sop[:-1]) / 100 if sop.endswith("%") else float(sop)
             stops.append([float(np.float32(o)), c[0], c[1] * max(0.0, min(1.0, sop))])
         if not stops:
@@ -2302,10 +2388,12 @@ class Builder(Loader):
             tag = _tag(c)
             if tag in ("title", "desc"):
                 continue
-            if tag not in ("path", "rect", "circle", "ellipse", "line", "polyline", "polygon", "use", "g"):
-                raise Unsupported("clip child " + tag)
-            if tag == "g":
-                raise Unsupported("clip child g")
+            if tag == "text":
+                raise Unsupported("clip child text")
+            # converter.rs convert_clip_path_elements: only shapes and <use>
+            # (of a shape) draw; <g>, <image>, <switch> and the rest are skipped
+            if tag not in ("path", "rect", "circle", "ellipse", "line", "polyline", "polygon", "use"):
+                continue
             self.clip_child(c, root)
         c = A.Clip()
         c.transform = _tf(ts)
@@ -2331,7 +2419,9 @@ class Builder(Loader):
             target = self.href(e)
             if target is None or _tag(target) not in ("path", "rect", "circle", "ellipse", "line", "polyline",
                                                       "polygon"):
-                raise Unsupported("clip use")
+                if target is not None and _tag(target) == "text":
+                    raise Unsupported("clip use of text")
+                return  # a <use> of anything but a shape draws nothing in a clip path
             ts = mat_mul(ts, (1, 0, 0, 1, self.num(e, "x", 0.0, self.vbw), self.num(e, "y", 0.0, self.vbh)))
         parent = root
         cp = self.ref(a.get("clip-path") if (e, "clip-path") not in self.no_link else None)

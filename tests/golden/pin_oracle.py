@@ -53,7 +53,7 @@ CATEGORIES = [
     "filters/feDistantLight", "filters/fePointLight", "filters/feSpotLight",
     "filters/filter-functions", "filters/feComponentTransfer", "filters/feDropShadow",
     "filters/feTurbulence", "filters/feTile", "filters/feDisplacementMap", "filters/feImage",
-    "paint-servers/pattern", "structure/image", "painting/marker", "painting/context",
+    "paint-servers/pattern", "structure/image", "painting/marker", "painting/context", "structure/symbol",
 ]
 IMAGE_SIZE = 300
 FIXTURES_PER_DIR = 4
