@@ -360,11 +360,15 @@ def parse_filter_list(value):
             return None
 
 
+class InvalidLength(Unsupported):
+    """A length svgtypes does not parse (an unknown unit or stray text)."""
+
+
 def parse_length(s, ref=0.0, font_size=12.0):
     s = s.strip()
     m = re.match(r"(" + NUM + r")\s*([a-z%]*)$", s)
     if not m:
-        raise Unsupported("length " + s)
+        raise InvalidLength("length " + s)
     v, u = float(m.group(1)), m.group(2)
     if u in ("", "px"):
         return v
@@ -384,7 +388,7 @@ def parse_length(s, ref=0.0, font_size=12.0):
         return v * 4.0 / 3.0
     if u == "pc":
         return v * 16.0
-    raise Unsupported("unit " + u)
+    raise InvalidLength("unit " + u)
 
 
 _CSS_NOT_PRESENTATION = {"x", "y", "width", "height", "rx", "ry", "cx", "cy", "r", "d", "points", "x1", "y1",
@@ -1366,7 +1370,7 @@ class Loader:
             return None
         m = re.match(r"url\(\s*['\"]?#([^'\")]+)['\"]?\s*\)", value.strip())
         if not m:
-            raise Unsupported("reference " + value)
+            return None  # not a link (e.g. a CSS shape function): svgtree reads no link
         return self.ids.get(m.group(1), "missing")
 
 
@@ -1713,7 +1717,14 @@ class Builder(Loader):
         tag = _tag(e)
         a = self.attrs(e)
         fsz = self.font_size(e) if any(("em" in v or "ex" in v) for v in a.values()) else 12.0
-        L = lambda n, d, ref: parse_length(a[n], ref, fsz) if n in a else d  # noqa: E731
+        def L(n, d, ref):
+            # an attribute that does not parse as a length is ignored (the default applies)
+            if n not in a:
+                return d
+            try:
+                return parse_length(a[n], ref, fsz)
+            except InvalidLength:
+                return d
         b = PathB()
         if tag == "path":
             b = parse_path_data(a.get("d", ""))
