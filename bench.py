@@ -643,11 +643,21 @@ def run_soft(args, rank, world):
         "gpu_launches": 12 * args.steps,
         "clocks": clk.summary(),
     }
-    peak, peak_kind = peaks()
+    # FP32-bound work: the flops of one step counted by ncu (profiles/soft_config4.json) over the
+    # step time, against the nominal FP32 rate (152 SMs x 128 lanes x 2 x 2.07 GHz; no measured figure)
+    try:
+        with open(os.path.join(ROOT, "profiles", "soft_config4.json")) as fh:
+            flop = float(json.load(fh)["flop_per_step"])
+    except Exception:
+        flop = None
+    peak_f = 152 * 128 * 2 * 2.07e9 / 1e12
     alg_bytes = 2 * h2d + 3 * 256 * 256 * 256 * 16
-    line["roofline"] = {"bound": "hbm", "achieved": alg_bytes / (ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
-                        "frac": alg_bytes / (ms * 1e-3) / 1e9 / peak, "peak_kind": peak_kind, "traffic": None,
-                        "kernel": "soft forward + adjoint (one step)", "algorithmic_bytes": alg_bytes}
+    achieved_f = flop / (ms * 1e-3) / 1e12 if flop else None
+    line["roofline"] = {"bound": "fp32", "achieved": achieved_f, "peak": peak_f, "unit": "TFLOP/s",
+                        "frac": achieved_f / peak_f if achieved_f else None, "peak_kind": "nominal",
+                        "traffic": None, "kernel": "soft forward + adjoint (one step)",
+                        "flop_per_step": flop, "flop_source": "ncu FP32 op counters, profiles/soft_config4.md",
+                        "algorithmic_bytes": alg_bytes}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_soft(a, t)
     if rank == 0:

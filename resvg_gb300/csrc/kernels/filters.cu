@@ -95,6 +95,9 @@ __device__ uint8_t g_tab[4][256 * 256];
 __device__ __forceinline__ uint32_t tab(int t, uint32_t a, uint32_t c) { return __ldg(&g_tab[t][(a << 8) | c]); }
 __device__ __forceinline__ uint32_t tab_px(int t, uint32_t p) {
     const uint32_t a = p >> 24;
+    // demultiply and multiply by an alpha of 255 keep every channel (the
+    // table rows for a = 255 are the identity): opaque pixels skip the lookups
+    if ((t == TAB_DEMUL || t == TAB_MUL) && a == 255u) return p;
     return tab(t, a, p & 0xFFu) | (tab(t, a, (p >> 8) & 0xFFu) << 8) | (tab(t, a, (p >> 16) & 0xFFu) << 16) | (a << 24);
 }
 

@@ -850,7 +850,11 @@ extern "C" int rgpu_soft_backward(const rgpu_soft_batch *b, const float *image, 
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const uint32_t ctas = (uint32_t)std::max(1, sms) * 2;
+    // persistent CTAs taking rows from a counter: as many as fit on the GPU at once
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_backward, kThreads, 0) != cudaSuccess || per_sm < 1)
+        per_sm = 2;
+    const uint32_t ctas = (uint32_t)std::max(1, sms) * (uint32_t)per_sm;
     cudaError_t e = flatten(*b, s);
     if (e == cudaSuccess) e = g_vgrad.ensure(nverts * sizeof(float2));
     if (e == cudaSuccess) e = g_tmp0.ensure(npx * sizeof(float4));
