@@ -394,7 +394,7 @@ int upload_plan(Context &c, Buffers &b, Plan &p, cudaStream_t s, HostBuf *stagin
     size_t stack_words = (size_t)p.max_depth * raster_threads() * p.px;
     CK(b.stack.ensure((size_t)p.grid * stack_words * 4));
     CK(b.span_ovf.ensure((size_t)p.grid * raster_threads() * kSpanOvf * 8));
-    CK(b.run_ovf.ensure((size_t)p.grid * 2 * raster_max_pairs() * p.run_cap * 8));  // two window buffers
+    CK(b.run_ovf.ensure((size_t)p.grid * raster_window_buffers() * raster_max_pairs() * p.run_cap * 8));
     CK(b.err.ensure(16));
     CK(b.counter.ensure(4 * (sb.max_level + 1)));
     return RGPU_OK;

@@ -42,6 +42,7 @@ void raster_set_wait_limit(uint32_t rounds);
 uint32_t raster_wait_limit();
 void raster_set_withhold(bool on);
 int raster_max_pairs();  // (draw, row) pairs of one phase-A window
+int raster_window_buffers();  // phase-A window buffers per CTA (each with its own run-overflow area)
 
 // filters.cu
 cudaError_t filter_color_space(uint32_t *img, size_t n, bool to_linear, cudaStream_t s);

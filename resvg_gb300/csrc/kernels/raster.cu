@@ -310,6 +310,60 @@ __device__ void merge_runs(VmShared &sh, WinBuf &wb, const int2 *ovf, uint32_t o
     wb.run_ext[pair] = make_int2(w.first, w.last);
 }
 
+// The anti-aliased merge of one (slot, row) by the two neighbouring producer
+// lanes that ran its phase A: each lane walks two of the row's four
+// sub-scanline span lists (`half` 0: sub-scanlines 0, 1; 1: 2, 3), and at
+// every coverage change the lanes add their partial coverage and take the
+// nearer next change through shuffles, so both step through the same
+// positions; the even lane writes the runs.  The result is the one-lane
+// merge's (the sum of the four lists' contributions and the minimum of their
+// next changes do not depend on the split).
+__device__ void merge_runs_aa2(VmShared &sh, WinBuf &wb, const int2 *ovf, uint32_t ovf_cap, int2 *rovf,
+                               uint32_t rovf_cap, int pair, int sj0, int half, int32_t lo, int32_t hi, uint32_t *err) {
+    const unsigned mask = 3u << ((threadIdx.x & 31u) & ~1u);
+    RunWriter w{&wb.runs[pair * kRunStride], rovf + (size_t)pair * rovf_cap, rovf_cap, 0, 0, INT32_MAX, INT32_MIN};
+    const int2 *L[2];
+    int n[2], q[2];
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+        n[j] = sh.span_cnt[sj0 + 2 * half + j];
+        L[j] = span_base(sh, ovf, ovf_cap, sj0 + 2 * half + j, n[j]);
+        q[j] = 0;
+    }
+    int32_t x = lo;
+    while (x < hi) {
+        int32_t nxt = hi;
+        uint32_t sum = 0;
+        const int32_t p0 = x << 2;
+#pragma unroll
+        for (int j = 0; j < 2; j++) {
+            while (q[j] < n[j] && L[j][q[j]].y <= p0) q[j]++;
+            for (int k = q[j]; k < n[j]; k++) {
+                const int2 a = L[j][k];
+                if (a.x >= p0 + 4) { nxt = min(nxt, a.x >> 2); break; }
+                const int32_t ov = min(a.y, p0 + 4) - max(a.x, p0);
+                if (ov == 4) {  // full from here up to the pixel holding the span's end
+                    sum += (half == 1 && j == 1) ? 63u : 64u;
+                    nxt = min(nxt, a.y >> 2);
+                } else {
+                    sum += (uint32_t)ov * 16u;
+                    nxt = min(nxt, x + 1);
+                }
+            }
+        }
+        sum += __shfl_xor_sync(mask, sum, 1);
+        nxt = min(nxt, __shfl_xor_sync(mask, nxt, 1));
+        if (half == 0) w.set(x, (int32_t)min(sum, 255u), err);
+        x = nxt;
+    }
+    if (half == 0) {
+        w.set(hi, 0, err);
+        w.put(INT32_MAX, 0, err);
+        wb.run_cnt[pair] = (uint16_t)min(w.n, (int)rovf_cap);
+        wb.run_ext[pair] = make_int2(w.first, w.last);
+    }
+}
+
 __device__ __forceinline__ const int2 *run_base(const WinBuf &wb, const int2 *rovf, uint32_t rovf_cap, int pair) {
     return wb.run_cnt[pair] <= kRunCap ? &wb.runs[pair * kRunStride] : rovf + (size_t)pair * rovf_cap;
 }
@@ -379,9 +433,16 @@ __device__ __forceinline__ void produce_window(VmShared &sh, const ItemInfo &itm
     const uint32_t nsl = min((uint32_t)K, st.fill_cnt - wfirst);
     const uint32_t *flist = fill_cmds + st.fill_off + wfirst;
     const int pw = pt >> 5, lane = pt & 31;
+    // lane j fetches slot j's draw and paint indices (one wave of dependent
+    // loads per warp instead of one per slot); the slots' users shuffle them
+    uint32_t my_di = 0, my_pi = 0;
+    if (lane < (int)nsl) {
+        my_di = cmds[st.cmd_off + flist[lane]].a;
+        my_pi = draws[my_di].paint;
+    }
     for (uint32_t k = (uint32_t)pw; k < nsl; k += kProducers / 32) {
-        const uint32_t di = cmds[st.cmd_off + flist[k]].a;
-        const uint32_t pi = draws[di].paint;
+        const uint32_t di = __shfl_sync(0xffffffffu, my_di, (int)k);
+        const uint32_t pi = __shfl_sync(0xffffffffu, my_pi, (int)k);
         if (lane < (int)(sizeof(PaintRec) / 4))
             ((uint32_t *)&wb.paint[k])[lane] = ((const uint32_t *)&paints[pi])[lane];
         if (lane == 0) wb.slot_geo[k] = make_int4(0, draws[di].ox, draws[di].oy, 0);
@@ -393,9 +454,10 @@ __device__ __forceinline__ void produce_window(VmShared &sh, const ItemInfo &itm
     // tasks 2 pt and 2 pt + 1: the same slot (S = 4 x band rows, a power of two)
     const int Sshift = 31 - __clz(S);
     const int u0 = 2 * pt, k = u0 >> Sshift, j0 = u0 & (S - 1);
+    const uint32_t kdi = __shfl_sync(0xffffffffu, my_di, k & 31);
     DrawRec dr;
     if (k < (int)nsl) {
-        const uint32_t di = cmds[st.cmd_off + flist[k]].a;
+        const uint32_t di = kdi;
         dr = draws[di];
         const uint32_t slot = st.bin_off + wi.band * st.draw_cnt + (di - st.draw_off);
         const EdgeRec *bl = bins + bin_offsets[slot];
@@ -412,14 +474,17 @@ __device__ __forceinline__ void produce_window(VmShared &sh, const ItemInfo &itm
         }
     }
     __syncwarp();
-    if (k < (int)nsl && (j0 & 3) == 0) {
+    if (k < (int)nsl) {
+        // row r2's four sub-scanlines are tasks 4 r2 .. 4 r2 + 3: two lanes
         const int r2 = j0 >> 2;
         const int32_t ly = (int32_t)wi.band * BH + r2 - dr.oy;
         int32_t lo = max(dr.sect_l, wi.x0 - dr.ox), hi = min(dr.sect_r, wi.x1 - dr.ox);
         if (!dr.valid || ly < dr.sect_t || ly >= dr.sect_b || (int32_t)wi.band * BH + r2 >= st.out_h) hi = lo;
-        if (r2 < BH)
-            merge_runs(sh, wb, ovf, ovf_cap, rovf, rovf_cap, k * BH + r2, k * S + (dr.shift ? j0 : r2), dr.shift != 0,
-                       lo, hi, err);
+        if (dr.shift)
+            merge_runs_aa2(sh, wb, ovf, ovf_cap, rovf, rovf_cap, k * BH + r2, k * S + (j0 & ~3), (j0 >> 1) & 1, lo,
+                           hi, err);
+        else if ((j0 & 3) == 0 && r2 < BH)
+            merge_runs(sh, wb, ovf, ovf_cap, rovf, rovf_cap, k * BH + r2, k * S + r2, false, lo, hi, err);
     }
     __syncwarp();  // the merge has read the spans before the next window's phase A overwrites them
 }
@@ -760,6 +825,7 @@ size_t raster_smem_bytes() { return raster_smem_bytes_px(16); }
 size_t raster_stack_words_per_cta(int px) { return (size_t)kMaxDepth * kThreads * px; }
 int raster_threads() { return kThreads; }
 int raster_max_pairs() { return kMaxPairs; }
+int raster_window_buffers() { return 2; }
 
 cudaError_t raster_init() {
     return cudaFuncSetAttribute(k_raster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)raster_smem_bytes_px(16));
