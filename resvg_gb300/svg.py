@@ -1202,7 +1202,7 @@ class Loader:
             if (n, name) in self.no_link:
                 return None
             v = self.attrs(n).get(name)
-            m = re.match(r"\s*url\(\s*['\"]?#([^'\")]+)['\"]?\s*\)", v or "")
+            m = re.match(r"\s*url\(\s*['\"]?#([^'\")\s]+)\s*['\"]?\s*\)", v or "")
             return self.ids.get(m.group(1)) if m else None
         for tag, name in (("clipPath", "clip-path"), ("mask", "mask")):
             nodes = [n for n in self.root.iter() if isinstance(n.tag, str) and _tag(n) == tag]
@@ -1238,7 +1238,7 @@ class Loader:
             if (n, which) in self.no_paint:
                 return None
             v = self.attrs(n).get(which)
-            m = re.match(r"\s*url\(\s*['\"]?#([^'\")]+)['\"]?\s*\)", v or "")
+            m = re.match(r"\s*url\(\s*['\"]?#([^'\")\s]+)\s*['\"]?\s*\)", v or "")
             t = self.ids.get(m.group(1)) if m else None
             return t if t is not None and _tag(t) == "pattern" else None
         for pat in self.root.iter():
@@ -1368,7 +1368,7 @@ class Loader:
     def ref(self, value):
         if not value or value.strip() == "none":
             return None
-        m = re.match(r"url\(\s*['\"]?#([^'\")]+)['\"]?\s*\)", value.strip())
+        m = re.match(r"url\(\s*['\"]?#([^'\")\s]+)\s*['\"]?\s*\)", value.strip())
         if not m:
             return None  # not a link (e.g. a CSS shape function): svgtree reads no link
         return self.ids.get(m.group(1), "missing")
@@ -1424,6 +1424,7 @@ class Builder(Loader):
         root = self.tree.add_group(-1, _group())
         if root_ts != IDENT:
             root = self.tree.add_group(root, _group(transform=_tf(root_ts)))
+        self.background(svg, root, vb if vb and len(vb) == 4 else (0.0, 0.0, W, H))
         # the root <svg> is a group of its own (opacity, clip-path, mask, filter,
         # display) inside the viewBox transform, as usvg converts it
         if self.attrs(svg).get("display", "").strip() != "none":
@@ -1434,6 +1435,30 @@ class Builder(Loader):
         self.tree.finalize()
         self.tree.ids = self.ids_out
         return self.tree
+
+    def background(self, svg, parent, rect):
+        """usvg converter.rs:393-400 and 504-521: the root's non-standard
+        background-color (a presentation attribute), when it parses as a plain
+        colour, becomes a filled rect of the viewBox drawn before everything
+        else, its alpha carried as the fill opacity."""
+        v = self.attrs(svg).get("background-color")
+        if v is None or v.strip().lower() in ("none", "currentcolor") or v.strip().startswith("url("):
+            return
+        try:
+            c = parse_color(v)
+        except InvalidColor:
+            return
+        if c is None:
+            return
+        path = A.Path()
+        path.fill_paint = self.solid(c)
+        path.fill_opacity = float(np.float32(round(c[1] * 255) / 255.0))
+        path.fill_rule = A.NONZERO
+        path.stroke_paint, path.stroke_width = -1, 1.0
+        path.visible, path.anti_alias = 1, 1
+        x, y, w, h = rect
+        self.tree.add_path(parent, path, [A.MOVE, A.LINE, A.LINE, A.LINE, A.CLOSE],
+                           [(x, y), (x + w, y), (x + w, y + h), (x, y + h)])
 
     def visible(self, e):
         if self.attrs(e).get("display", "").strip() == "none":
@@ -1842,7 +1867,7 @@ class Builder(Loader):
                 raise Unsupported("context paint server")
             return c, opacity
         if v.startswith("url("):
-            m = re.match(r"url\(\s*['\"]?#([^'\")]+)['\"]?\s*\)\s*(.*)$", v)
+            m = re.match(r"url\(\s*['\"]?#([^'\")\s]+)\s*['\"]?\s*\)\s*(.*)$", v)
             if not m:
                 return invalid
             ref = self.ids.get(m.group(1))
@@ -1972,7 +1997,7 @@ class Builder(Loader):
                 return None
         v = (self.get(e, which) or "").strip()
         if v.startswith("url("):
-            m = re.match(r"url\(\s*['\"]?#([^'\")]+)['\"]?\s*\)", v)
+            m = re.match(r"url\(\s*['\"]?#([^'\")\s]+)\s*['\"]?\s*\)", v)
             ref = self.ids.get(m.group(1)) if m else None
             if ref is not None and _tag(ref) in ("linearGradient", "radialGradient", "pattern"):
                 return "server"
@@ -2100,6 +2125,26 @@ class Builder(Loader):
                 # paint_server.rs convert_radial: a non-positive r paints the last stop
                 c = stops[-1]
                 return self.solid((c[1], 1.0)), opacity * c[2]
+            # The two-point conical constructor's concentric cases (Skia's
+            # MakeTwoPointConical, kept by tiny-skia's RadialGradient::new): with
+            # focus and centre within 2^-15 of each other, equal radii leave an
+            # infinitely thin ring at r (Pad: the first colour inside it, the last
+            # outside; a tiny r: the last colour), and a zero focal radius is a
+            # plain radial gradient.
+            tol = 1.0 / 32768.0
+            f32 = np.float32
+            if len(stops) >= 2 and abs(f32(p.fx) - f32(p.cx)) <= tol and abs(f32(p.fy) - f32(p.cy)) <= tol:
+                if abs(f32(p.fr) - f32(p.r_)) <= tol:
+                    if spread != 0:
+                        raise Unsupported("degenerate concentric gradient with repeat/reflect")
+                    if not f32(p.r_) > tol:
+                        c = stops[-1]
+                        return self.solid((c[1], 1.0)), opacity * c[2]
+                    first, last = stops[0], stops[-1]
+                    stops = [[0.0, first[1], first[2]], [1.0, first[1], first[2]], [1.0, last[1], last[2]]]
+                    p.cx, p.cy, p.fr = p.fx, p.fy, 0.0
+                elif abs(f32(p.fr)) <= tol:
+                    p.cx, p.cy, p.fr = p.fx, p.fy, 0.0
         p.transform = _tf(gts)
         if len(stops) == 1:
             c = stops[0]
@@ -2215,7 +2260,7 @@ class Builder(Loader):
             v = self.get(e, "marker-" + kind)
             if not v or v.strip() == "none":
                 continue
-            m = re.match(r"\s*url\(\s*['\"]?#([^'\")]+)['\"]?\s*\)", v)
+            m = re.match(r"\s*url\(\s*['\"]?#([^'\")\s]+)\s*['\"]?\s*\)", v)
             ref = self.ids.get(m.group(1)) if m else None
             if ref is None or _tag(ref) != "marker" or any(ref is x for x in self.marker_stack):
                 continue

@@ -81,7 +81,15 @@ def pixel_diff(expected, actual):
 
 
 def collect(root):
+    """The suite's tests in CATEGORIES: an SVG with its golden PNG that
+    crates/resvg/tests/integration/render.rs runs (a few files in the tree,
+    e.g. structure/svg/no-size, have no test there and are left out)."""
+    import re
     base = os.path.join(root, "crates", "resvg", "tests", "tests")
+    listed = None
+    rs = os.path.join(root, "crates", "resvg", "tests", "integration", "render.rs")
+    if os.path.exists(rs):
+        listed = set(re.findall(r'render\("tests/([^"]+)"\)', open(rs).read()))
     out = []
     for cat in CATEGORIES:
         top = os.path.join(base, cat)
@@ -89,6 +97,8 @@ def collect(root):
             sub = os.path.relpath(d, base)
             for name in sorted(files):
                 if name.endswith(".svg") and os.path.exists(os.path.join(d, name[:-4] + ".png")):
+                    if listed is not None and f"{sub}/{name[:-4]}" not in listed:
+                        continue
                     out.append((sub, name[:-4], os.path.join(d, name)))
     return out
 

@@ -150,3 +150,61 @@ def test_front_end_keeps_svg_ids():
     assert tree.find_node("box")[0] == A.NODE_PATH
     assert tree.find_node("dot")[0] == A.NODE_PATH
     assert tree.find_node("nope") is None
+
+
+def _paths(tree):
+    v = tree.view().contents
+    out = []
+    for i in range(v.path_count):
+        p = v.paths[i]
+        pts = [v.points[j] for j in range(p.point_offset * 2, (p.point_offset + p.point_count) * 2)]
+        out.append((p, pts))
+    return v, out
+
+
+def test_root_background_color_is_a_viewbox_rect():
+    """usvg converter.rs:393-521: a plain-colour background-color on the root
+    becomes the first path, a rect of the viewBox with the alpha as opacity;
+    none, currentColor and links add nothing."""
+    tree = svg.load_svg('<svg xmlns="http://www.w3.org/2000/svg" viewBox="10 20 200 100" width="400" '
+                        'style="background-color: #0000ff80"><rect width="5" height="5"/></svg>')
+    v, paths = _paths(tree)
+    assert len(paths) == 2
+    p, pts = paths[0]
+    assert pts == [10.0, 20.0, 210.0, 20.0, 210.0, 120.0, 10.0, 120.0]
+    assert p.fill_opacity == pytest.approx(128 / 255, abs=1e-7)
+    paint = v.paints[p.fill_paint]
+    assert (paint.r, paint.g, paint.b) == (0, 0, 255)
+    for bg in ("none", "currentColor", "url(#x)", "#12"):
+        tree = svg.load_svg('<svg xmlns="http://www.w3.org/2000/svg" width="50" height="50" '
+                            f'background-color="{bg}"><rect width="5" height="5"/></svg>')
+        assert len(_paths(tree)[1]) == 1
+
+
+def test_url_reference_allows_spaces():
+    tree = svg.load_svg('<svg xmlns="http://www.w3.org/2000/svg" width="50" height="50">'
+                        '<linearGradient id="lg1"><stop offset="0"/><stop offset="1" stop-color="white"/>'
+                        '</linearGradient><rect width="40" height="40" fill="  url(  #lg1   )  "/></svg>')
+    v, paths = _paths(tree)
+    assert v.paints[paths[0][0].fill_paint].kind == A.PAINT_LINEAR
+
+
+def test_concentric_equal_radii_radial_is_a_ring():
+    """The two-point conical constructor's degenerate case: focus = centre and
+    fr = r under pad spread become a plain radial gradient of radius r whose
+    stops are (0, first), (1, first), (1, last)."""
+    tree = svg.load_svg('<svg xmlns="http://www.w3.org/2000/svg" width="50" height="50">'
+                        '<radialGradient id="g" fr="0.5"><stop offset="0.2" stop-color="black"/>'
+                        '<stop offset="0.5" stop-color="red"/><stop offset="1" stop-color="white"/>'
+                        '</radialGradient><rect width="40" height="40" fill="url(#g)"/></svg>')
+    v, paths = _paths(tree)
+    paint = v.paints[paths[0][0].fill_paint]
+    assert paint.kind == A.PAINT_RADIAL and paint.fr == 0.0 and paint.r_ == pytest.approx(0.5)
+    stops = [v.stops[paint.stop_offset + i] for i in range(paint.stop_count)]
+    assert [s.offset for s in stops] == [0.0, 1.0, 1.0]
+    assert [(s.r, s.g, s.b) for s in stops] == [(0, 0, 0), (0, 0, 0), (255, 255, 255)]
+    with pytest.raises(svg.Unsupported):
+        svg.load_svg('<svg xmlns="http://www.w3.org/2000/svg" width="50" height="50">'
+                     '<radialGradient id="g" fr="0.5" spreadMethod="repeat"><stop offset="0"/>'
+                     '<stop offset="1" stop-color="white"/></radialGradient>'
+                     '<rect width="40" height="40" fill="url(#g)"/></svg>')
