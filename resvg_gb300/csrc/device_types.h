@@ -12,21 +12,30 @@
 // builds fixed-point edges, bins them into row bands and rasterises.
 #pragma once
 #include <stdint.h>
+#include <stddef.h>
 
 namespace rgpu {
 
 constexpr int kMaxGradStops = 12;   // intervals incl. the two constant ends (<= 10 stops after padding)
 
+// Laid out so that a gradient of n intervals is the record's first
+// 112 + 32 n bytes (the header, the stop positions, then per interval the
+// factor and bias rows): shading touches only that prefix.
 struct alignas(16) GradRec {
-    float f[kMaxGradStops][4];   // per stop interval: colour = t * f + b (16-byte rows: one vector load)
-    float b[kMaxGradStops][4];
     float ts[6];         // device pixel -> unit gradient space (sx, ky, kx, sy, tx, ty)
     uint32_t flags;      // see GRAD_* below
     uint32_t spread;     // rgpu_spread
     uint32_t n;          // number of t_values / factors / biases
     float fr0, fr1, cdx, cdy;  // two-point conical parameters (unit space)
+    uint32_t _pad[3];
     float t[kMaxGradStops];
+    struct Row {
+        float f[4];      // colour = t * f + b (16-byte rows: one vector load each)
+        float b[4];
+    } iv[kMaxGradStops];
 };
+static_assert(sizeof(GradRec) == 496 && offsetof(GradRec, t) == 64 && offsetof(GradRec, iv) == 112,
+              "GradRec prefix layout");
 enum : uint32_t {
     GRAD_TWO_STOP = 1, GRAD_PAD_CLAMP = 2, GRAD_PREMUL = 4, GRAD_RADIAL_SIMPLE = 8, GRAD_RADIAL_CONICAL = 16
 };
@@ -40,16 +49,27 @@ struct ImageRec {
 };
 static_assert(sizeof(ImageRec) <= sizeof(GradRec), "ImageRec fits a GradRec slot");
 
+// A gradient paint carries copies of its record's transform, flags, spread and
+// interval count in place of the uniform colours, so that the raster kernel
+// reads them from the paint it already holds in shared memory and goes to the
+// GradRec only for the stop positions and colour rows.
 struct PaintRec {
     uint32_t kind;       // 0 solid, 1 gradient, 2 image (ImageRec in the GradRec slot)
     uint32_t blend;      // rgpu_blend after tiny-skia's strength reduction
     uint32_t flags;      // PAINT_* below
     uint32_t grad;       // index into GradRec when kind != 0
-    uint16_t rgba16[4];  // lowp uniform colour
-    float colorf[4];     // highp uniform colour (premultiplied)
+    union {
+        struct {
+            uint16_t rgba16[4];  // lowp uniform colour
+            float colorf[4];     // highp uniform colour (premultiplied)
+        };
+        float gts[6];            // kind 1: GradRec::ts
+    };
     uint8_t memset_rgba[4];
-    uint32_t _pad;
+    uint32_t gmeta;      // kind 1: GradRec flags | spread << 8 | n << 16
 };
+static_assert(sizeof(PaintRec) == 48 && offsetof(PaintRec, gts) == 16 && offsetof(PaintRec, colorf) == 24,
+              "PaintRec layout");
 enum : uint32_t { PAINT_LOWP = 1, PAINT_MEMSET = 2, PAINT_SKIP = 4 };
 
 struct DrawRec {

@@ -121,8 +121,8 @@ bool make_grad(const Shader &sh, GradRec &g) {
         ColorF c0 = st[0].c, c1 = st[1].c;
         g.n = 1;
         g.t[0] = 0;
-        g.f[0][0] = c1.r - c0.r; g.f[0][1] = c1.g - c0.g; g.f[0][2] = c1.b - c0.b; g.f[0][3] = c1.a - c0.a;
-        g.b[0][0] = c0.r; g.b[0][1] = c0.g; g.b[0][2] = c0.b; g.b[0][3] = c0.a;
+        g.iv[0].f[0] = c1.r - c0.r; g.iv[0].f[1] = c1.g - c0.g; g.iv[0].f[2] = c1.b - c0.b; g.iv[0].f[3] = c1.a - c0.a;
+        g.iv[0].b[0] = c0.r; g.iv[0].b[1] = c0.g; g.iv[0].b[2] = c0.b; g.iv[0].b[3] = c0.a;
     } else {
         auto eq = [](ColorF a, ColorF b) { return a.r == b.r && a.g == b.g && a.b == b.b && a.a == b.a; };
         size_t first = eq(st[0].c, st[1].c) ? 1 : 0;
@@ -130,7 +130,7 @@ bool make_grad(const Shader &sh, GradRec &g) {
         uint32_t n = 0;
         auto push = [&](const float f[4], const float b[4], float t) {
             if (n >= (uint32_t)kMaxGradStops) { n = kMaxGradStops + 1; return; }
-            for (int k = 0; k < 4; k++) { g.f[n][k] = f[k]; g.b[n][k] = b[k]; }
+            for (int k = 0; k < 4; k++) { g.iv[n].f[k] = f[k]; g.iv[n].b[k] = b[k]; }
             g.t[n] = t;
             n++;
         };
@@ -229,6 +229,8 @@ struct Flattener {
             sb.grads.push_back(g);
             pr.kind = 1;
             pr.grad = (uint32_t)sb.grads.size() - 1;
+            for (int i = 0; i < 6; i++) pr.gts[i] = g.ts[i];
+            pr.gmeta = g.flags | g.spread << 8 | g.n << 16;
         }
         if (blend == RGPU_BLEND_CLEAR && !aa) {
             blend = RGPU_BLEND_SOURCE;

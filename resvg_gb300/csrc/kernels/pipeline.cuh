@@ -200,73 +200,93 @@ __device__ __forceinline__ void blend_sep(uint32_t mode, const float *s, const f
 }
 
 // Gradient colour at device pixel (px, py) (premultiplied f32); false when the
-// pixel lies in a two-point-conical region with no circle through it.
-__device__ __forceinline__ bool gradient_eval(const GradRec &g, int32_t px, int32_t py, float *c,
-                                              bool premul_stage = true) {
+// pixel lies in a two-point-conical region with no circle through it. The
+// transform, flags, spread and interval count come from the paint (held in
+// shared memory by the raster kernel); the rest from g, a record in global
+// memory that no kernel writes while this one runs, so it is read through the
+// read-only data path (__ldg).
+__device__ __forceinline__ bool gradient_eval(const PaintRec &pr, const GradRec &g, int32_t px, int32_t py,
+                                              float *c, bool premul_stage = true) {
+    const uint32_t meta = pr.gmeta;
+    const uint32_t gflags = meta & 0xFFu, gspread = (meta >> 8) & 0xFFu, gn = meta >> 16;
     float x = (float)px + 0.5f, y = (float)py + 0.5f;
-    float tx = x * g.ts[0] + y * g.ts[2] + g.ts[4];
-    float ty = x * g.ts[1] + y * g.ts[3] + g.ts[5];
+    float tx = x * pr.gts[0] + y * pr.gts[2] + pr.gts[4];
+    float ty = x * pr.gts[1] + y * pr.gts[3] + pr.gts[5];
     float t;
-    if (g.flags & GRAD_RADIAL_SIMPLE) {
+    if (gflags & GRAD_RADIAL_SIMPLE) {
         t = __fsqrt_rn(tx * tx + ty * ty);
-    } else if (g.flags & GRAD_RADIAL_CONICAL) {
-        float dr = g.fr1 - g.fr0;
-        float a = g.cdx * g.cdx + g.cdy * g.cdy - dr * dr;
-        float b = tx * g.cdx + ty * g.cdy + g.fr0 * dr;
-        float cc = tx * tx + ty * ty - g.fr0 * g.fr0;
+    } else if (gflags & GRAD_RADIAL_CONICAL) {
+        float dr = __ldg(&g.fr1) - __ldg(&g.fr0);
+        float a = __ldg(&g.cdx) * __ldg(&g.cdx) + __ldg(&g.cdy) * __ldg(&g.cdy) - dr * dr;
+        float b = tx * __ldg(&g.cdx) + ty * __ldg(&g.cdy) + __ldg(&g.fr0) * dr;
+        float cc = tx * tx + ty * ty - __ldg(&g.fr0) * __ldg(&g.fr0);
         if (a == 0.0f) {
             if (b == 0.0f) return false;
             t = __fdiv_rn(cc, 2.0f * b);
-            if (g.fr0 + t * dr < 0.0f) return false;
+            if (__ldg(&g.fr0) + t * dr < 0.0f) return false;
         } else {
             float disc = b * b - a * cc;
             if (disc < 0.0f) return false;
             float sq = __fsqrt_rn(disc);
             float t1 = __fdiv_rn(b + sq, a), t2 = __fdiv_rn(b - sq, a);
             float hi = fmaxf(t1, t2), lo = fminf(t1, t2);
-            if (g.fr0 + hi * dr >= 0.0f) t = hi;
-            else if (g.fr0 + lo * dr >= 0.0f) t = lo;
+            if (__ldg(&g.fr0) + hi * dr >= 0.0f) t = hi;
+            else if (__ldg(&g.fr0) + lo * dr >= 0.0f) t = lo;
             else return false;
         }
     } else {
         t = tx;
     }
-    if (g.spread == RGPU_SPREAD_REFLECT) {
+    if (gspread == RGPU_SPREAD_REFLECT) {
         float u = t - 1.0f;
         t = fabsf(u - 2.0f * floorf(u * 0.5f) - 1.0f);
         t = fminf(fmaxf(t, 0.0f), 1.0f);
-    } else if (g.spread == RGPU_SPREAD_REPEAT) {
+    } else if (gspread == RGPU_SPREAD_REPEAT) {
         t = t - floorf(t);
         t = fminf(fmaxf(t, 0.0f), 1.0f);
-    } else if (g.flags & GRAD_PAD_CLAMP) {
+    } else if (gflags & GRAD_PAD_CLAMP) {
         t = fminf(fmaxf(t, 0.0f), 1.0f);
     }
-    // the interval: how many of t[1..n) are <= t; t[] is non-decreasing (the
-    // host makes the stop positions monotonic), so the scan stops at the first
-    // larger value
+    // the interval: how many of t[1..n) are <= t. t[] is non-decreasing (the
+    // host makes the stop positions monotonic), so this count is the index a
+    // scan that stops at the first larger value finds; counting needs no
+    // chain of dependent loads: t[] is read as up to three 16-byte vectors
     uint32_t idx = 0;
-    if (!(g.flags & GRAD_TWO_STOP)) {
-        while (idx + 1 < g.n && t >= g.t[idx + 1]) idx++;
+    if (!(gflags & GRAD_TWO_STOP)) {
+        const float4 *tv = reinterpret_cast<const float4 *>(g.t);
+        const float4 q0 = __ldg(tv);
+        idx = (uint32_t)(1u < gn && t >= q0.y) + (uint32_t)(2u < gn && t >= q0.z) + (uint32_t)(3u < gn && t >= q0.w);
+        if (gn > 4u) {
+            const float4 q1 = __ldg(tv + 1);
+            idx += (uint32_t)(t >= q1.x) + (uint32_t)(5u < gn && t >= q1.y) + (uint32_t)(6u < gn && t >= q1.z) +
+                   (uint32_t)(7u < gn && t >= q1.w);
+            if (gn > 8u) {
+                const float4 q2 = __ldg(tv + 2);
+                idx += (uint32_t)(t >= q2.x) + (uint32_t)(9u < gn && t >= q2.y) + (uint32_t)(10u < gn && t >= q2.z) +
+                       (uint32_t)(11u < gn && t >= q2.w);
+            }
+        }
     }
-    const float4 fv = reinterpret_cast<const float4 *>(g.f)[idx];
-    const float4 bv = reinterpret_cast<const float4 *>(g.b)[idx];
+    const float4 fv = __ldg(reinterpret_cast<const float4 *>(g.iv[idx].f));
+    const float4 bv = __ldg(reinterpret_cast<const float4 *>(g.iv[idx].b));
     c[0] = t * fv.x + bv.x;
     c[1] = t * fv.y + bv.y;
     c[2] = t * fv.z + bv.z;
     c[3] = t * fv.w + bv.w;
-    if ((g.flags & GRAD_PREMUL) && premul_stage) { c[0] *= c[3]; c[1] *= c[3]; c[2] *= c[3]; }
+    if ((gflags & GRAD_PREMUL) && premul_stage) { c[0] *= c[3]; c[1] *= c[3]; c[2] *= c[3]; }
     return true;
 }
 
 // lowp gradient colour (pipeline/lowp.rs gradient / evenly_spaced_2_stop_gradient
 // + premultiply): the f32 interpolation is clamped, rounded to u16 by
 // truncating v * 255 + 0.5, then premultiplied with div255.
-__device__ __forceinline__ void gradient_eval_lowp(const GradRec &g, int32_t px, int32_t py, uint16_t s[4]) {
+__device__ __forceinline__ void gradient_eval_lowp(const PaintRec &pr, const GradRec &g, int32_t px, int32_t py,
+                                                   uint16_t s[4]) {
     float c[4];
-    gradient_eval(g, px, py, c, false);
+    gradient_eval(pr, g, px, py, c, false);
 #pragma unroll
     for (int k = 0; k < 4; k++) s[k] = (uint16_t)(fminf(fmaxf(c[k], 0.0f), 1.0f) * 255.0f + 0.5f);
-    if (g.flags & GRAD_PREMUL) {
+    if (pr.gmeta & GRAD_PREMUL) {
 #pragma unroll
         for (int k = 0; k < 3; k++) s[k] = div255((uint16_t)(s[k] * s[3]));
     }
@@ -278,16 +298,16 @@ __device__ __forceinline__ void gradient_eval_lowp(const GradRec &g, int32_t px,
 __device__ __forceinline__ uint32_t div255_2(uint32_t v) { return ((v + 0x00FF00FFu) >> 8) & 0x00FF00FFu; }
 
 // lowp gradient colour as two lane pairs (same arithmetic as gradient_eval_lowp).
-__device__ __forceinline__ void gradient_eval_lowp2(const GradRec &g, int32_t px, int32_t py, uint32_t &rb,
-                                                    uint32_t &ga) {
+__device__ __forceinline__ void gradient_eval_lowp2(const PaintRec &pr, const GradRec &g, int32_t px, int32_t py,
+                                                    uint32_t &rb, uint32_t &ga) {
     float c[4];
-    gradient_eval(g, px, py, c, false);
+    gradient_eval(pr, g, px, py, c, false);
     uint32_t s[4];
 #pragma unroll
     for (int k = 0; k < 4; k++) s[k] = (uint32_t)(fminf(fmaxf(c[k], 0.0f), 1.0f) * 255.0f + 0.5f);
     rb = s[0] | s[2] << 16;
     ga = s[1] | s[3] << 16;
-    if (g.flags & GRAD_PREMUL) {
+    if (pr.gmeta & GRAD_PREMUL) {
         rb = div255_2(rb * s[3]);
         ga = (div255_2(ga * s[3]) & 0xFFFFu) | s[3] << 16;
     }
@@ -305,7 +325,7 @@ __device__ __forceinline__ uint32_t shade_pixel_slow(const PaintRec &pr, const G
     const uint32_t blend = pr.blend;
     if (pr.flags & PAINT_LOWP) {
         uint16_t s[4] = {pr.rgba16[0], pr.rgba16[1], pr.rgba16[2], pr.rgba16[3]};
-        if (pr.kind != 0) gradient_eval_lowp(*grad, lx, ly, s);
+        if (pr.kind != 0) gradient_eval_lowp(pr, *grad, lx, ly, s);
         uint16_t d[4] = {(uint16_t)ch(dst, 0), (uint16_t)ch(dst, 1), (uint16_t)ch(dst, 2), (uint16_t)ch(dst, 3)};
         uint16_t o[4];
         if (cov == 255) {
@@ -338,7 +358,7 @@ __device__ __forceinline__ uint32_t shade_pixel_slow(const PaintRec &pr, const G
         s = __ldg(reinterpret_cast<const float4 *>(im.ptr) + (uint32_t)(ly * im.bw + lx));
     } else {
         float c[4];
-        if (gradient_eval(*grad, lx, ly, c)) s = make_float4(c[0], c[1], c[2], c[3]);
+        if (gradient_eval(pr, *grad, lx, ly, c)) s = make_float4(c[0], c[1], c[2], c[3]);
         else s = make_float4(0.f, 0.f, 0.f, 0.f);
     }
     const float4 d = unpack_f(dst);
@@ -369,7 +389,7 @@ __device__ __forceinline__ uint32_t shade_pixel(const PaintRec &pr, const GradRe
     if ((pr.flags & PAINT_LOWP) && blend == RGPU_BLEND_SOURCE_OVER) {
         // lowp source-over (pre-scaled by coverage), two lanes per register
         uint32_t rb, ga;
-        if (pr.kind != 0) gradient_eval_lowp2(*grad, lx, ly, rb, ga);
+        if (pr.kind != 0) gradient_eval_lowp2(pr, *grad, lx, ly, rb, ga);
         else {
             const uint32_t w0 = *reinterpret_cast<const uint32_t *>(&pr.rgba16[0]);
             const uint32_t w1 = *reinterpret_cast<const uint32_t *>(&pr.rgba16[2]);

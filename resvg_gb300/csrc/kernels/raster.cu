@@ -33,6 +33,7 @@ constexpr int kSpanStride = kSpanCap + 1;  // padded: neighbouring lists start i
 constexpr int kMaxDepth = 48;    // layer stack depth
 
 constexpr int kMaxSlots = 32;   // draws per phase-A window
+constexpr uint32_t kWinBufs = 3;  // window buffers: the producers run up to two windows ahead
 constexpr int kMaxPairs = kThreads / 4;  // (slot, row) pairs per window: K x BH <= kThreads / 4
 constexpr int kRunCap = 32;     // alpha runs per (slot, row) kept in shared memory
 constexpr int kRunStride = kRunCap + 1;
@@ -46,9 +47,9 @@ struct ItemInfo {
     StreamRec st;
 };
 
-// One phase-A window as the consumers read it: the window's paints, gradients
-// and draw origins, and per (slot, row) the alpha runs.  Two of them alternate:
-// the producers fill one while the consumers shade from the other.
+// One phase-A window as the consumers read it: the window's paints and draw
+// origins, and per (slot, row) the alpha runs.  kWinBufs of them rotate: the
+// producers fill the next ones while the consumers shade from the oldest.
 struct WinBuf {
     // alpha runs per (slot, row), including the closing sentinel; the upper
     // half stays zero: a consumer that gave up on a window reads its counts there
@@ -57,14 +58,14 @@ struct WinBuf {
     int2 runs[kMaxPairs * kRunStride];
     PaintRec paint[kMaxSlots + 1];   // paints of the window's draws; [kMaxSlots] of buffer 0: the hairline's
     int4 slot_geo[kMaxSlots];    // (unused, ox, oy, unused) per slot
-    GradRec grad[kMaxSlots + 1];     // gradients of the window's draws (and the hairline's)
+
 };
 struct VmShared {
     uint16_t span_cnt[kThreads];  // producer-private: spans per (slot, sub-scanline) task
     int2 spans[kThreads * kSpanStride];
-    WinBuf win[2];
-    unsigned long long mb_ready[2];  // mbarriers: window in buffer b produced (kProducers arrivals)
-    unsigned long long mb_free[2];   // buffer b consumed (kThreads arrivals)
+    WinBuf win[kWinBufs];
+    unsigned long long mb_ready[kWinBufs];  // mbarriers: window in buffer b produced (kProducers arrivals)
+    unsigned long long mb_free[kWinBufs];   // buffer b consumed (kThreads arrivals)
     int32_t abort;                   // set on an error: the rest of the launch skips work and waits
     int32_t cabort;                  // consumers only: set (for good) by a consumer that has seen an abort
     unsigned long long mb_item_ready[2];  // item ring entry filled (1 arrival: producer 0)
@@ -415,14 +416,14 @@ __device__ __forceinline__ uint32_t hair_cov(const HairSpan *hsp, int32_t px, in
 }
 
 // One phase-A window by the producer threads (pt = 0 .. kProducers-1) into
-// buffer wb: stage the window's paints, gradients and draw origins, run phase
+// buffer wb: stage the window's paints and draw origins, run phase
 // A for two (slot, sub-scanline) tasks per thread, then merge each (slot, row)
 // into alpha runs (a row's tasks sit in one warp, so a warp barrier orders
 // them).
 __device__ __forceinline__ void produce_window(VmShared &sh, const ItemInfo &itm, WinBuf &wb, int pt, uint32_t wfirst,
                                                const Cmd *cmds,
                                                const uint32_t *fill_cmds, const DrawRec *draws,
-                                               const PaintRec *paints, const GradRec *grads, const EdgeRec *bins,
+                                               const PaintRec *paints, const EdgeRec *bins,
                                                const uint32_t *bin_offsets, const uint32_t *bin_counts, int2 *ovf,
                                                uint32_t ovf_cap, int2 *rovf, uint32_t rovf_cap, uint32_t *err) {
     const WorkItem &wi = itm.wi;
@@ -446,10 +447,6 @@ __device__ __forceinline__ void produce_window(VmShared &sh, const ItemInfo &itm
         if (lane < (int)(sizeof(PaintRec) / 4))
             ((uint32_t *)&wb.paint[k])[lane] = ((const uint32_t *)&paints[pi])[lane];
         if (lane == 0) wb.slot_geo[k] = make_int4(0, draws[di].ox, draws[di].oy, 0);
-        if (paints[pi].kind != 0) {
-            const uint32_t *src = (const uint32_t *)&grads[paints[pi].grad];
-            for (int w = lane; w < (int)(sizeof(GradRec) / 4); w += 32) ((uint32_t *)&wb.grad[k])[w] = src[w];
-        }
     }
     // tasks 2 pt and 2 pt + 1: the same slot (S = 4 x band rows, a power of two)
     const int Sshift = 31 - __clz(S);
@@ -502,12 +499,12 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
     uint32_t *stack = stack_scratch + (size_t)blockIdx.x * stack_depth * kThreads * PX;
     int2 *ovf = span_ovf + (size_t)blockIdx.x * kThreads * ovf_cap;
     // two run-overflow areas per CTA, one per window buffer
-    int2 *rovf = run_ovf + (size_t)blockIdx.x * 2 * kMaxPairs * rovf_cap;
+    int2 *rovf = run_ovf + (size_t)blockIdx.x * kWinBufs * kMaxPairs * rovf_cap;
     if (tid == 0) {
-        mb_init(&sh.mb_ready[0], kProducers);
-        mb_init(&sh.mb_ready[1], kProducers);
-        mb_init(&sh.mb_free[0], kThreads);
-        mb_init(&sh.mb_free[1], kThreads);
+        for (uint32_t b = 0; b < kWinBufs; b++) {
+            mb_init(&sh.mb_ready[b], kProducers);
+            mb_init(&sh.mb_free[b], kThreads);
+        }
         mb_init(&sh.mb_item_ready[0], 1);
         mb_init(&sh.mb_item_ready[1], 1);
         mb_init(&sh.mb_item_free[0], kThreads);
@@ -515,7 +512,7 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
         sh.abort = 0;
         sh.cabort = 0;
     }
-    if (tid < 2 * kMaxPairs) sh.win[tid / kMaxPairs].run_cnt[kMaxPairs + tid % kMaxPairs] = 0;
+    if (tid < (int)kWinBufs * kMaxPairs) sh.win[tid / kMaxPairs].run_cnt[kMaxPairs + tid % kMaxPairs] = 0;
     __syncthreads();
     uint32_t win_base = 0;  // windows produced and consumed by this CTA so far
 
@@ -547,12 +544,12 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
             const int K = min(kThreads / S, kMaxSlots);
             const uint32_t nwin = (itm.st.fill_cnt + (uint32_t)K - 1) / (uint32_t)K;
             for (uint32_t w = 0; w < nwin; w++) {
-                const uint32_t gw = win_base + w, b = gw & 1u;
-                if (gw >= 2) mb_wait(&sh.mb_free[b], ((gw >> 1) - 1u) & 1u, err, &sh.abort, wait_limit);
+                const uint32_t gw = win_base + w, b = gw % kWinBufs;
+                if (gw >= kWinBufs) mb_wait(&sh.mb_free[b], (gw / kWinBufs - 1u) & 1u, err, &sh.abort, wait_limit);
                 // one decision per warp: produce_window synchronises its warps
                 const bool skip = __any_sync(0xffffffffu, *(volatile int32_t *)&sh.abort != 0);
                 if (!skip)
-                    produce_window(sh, itm, sh.win[b], pt, w * (uint32_t)K, cmds, fill_cmds, draws, paints, grads,
+                    produce_window(sh, itm, sh.win[b], pt, w * (uint32_t)K, cmds, fill_cmds, draws, paints,
                                    bins, bin_offsets, bin_counts, ovf, ovf_cap,
                                    rovf + (size_t)b * kMaxPairs * rovf_cap, rovf_cap, err);
                 // failure-detection test hook: CTA 0 never completes its first
@@ -624,11 +621,11 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
                 if (c.op != CMD_HAIR && (fill_seen & (uint32_t)(K - 1)) == 0) {
                     // ---- the next window: release the previous buffer, wait for this one
                     const uint32_t gw = win_base + (fill_seen >> Kshift);
-                    if (fill_seen) mb_arrive(&sh.mb_free[(gw - 1u) & 1u]);
-                    mb_wait(&sh.mb_ready[gw & 1u], (gw >> 1) & 1u, err, &sh.abort, wait_limit);
+                    if (fill_seen) mb_arrive(&sh.mb_free[(gw - 1u) % kWinBufs]);
+                    mb_wait(&sh.mb_ready[gw % kWinBufs], (gw / kWinBufs) & 1u, err, &sh.abort, wait_limit);
                     // a failed wait sets `abort`; producers skip windows after
                     // an abort but still arrive
-                    cur_b = gw & 1u;
+                    cur_b = gw % kWinBufs;
                     cnt_off = *(volatile int32_t *)&sh.abort != 0 ? kMaxPairs : 0;
                     slot_next = 0;
                 }
@@ -656,10 +653,6 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
                     consumer_sync();  // the previous hairline's pixels are done with the slot
                     slot = kMaxSlots;  // the spare slot of buffer 0 (producers never write it)
                     if (tid == 0) sh.win[0].paint[slot] = paints[hr.paint];
-                    const PaintRec &gp = paints[hr.paint];
-                    if (gp.kind != 0)
-                        for (int w = tid; w < (int)(sizeof(GradRec) / 4); w += kThreads)
-                            ((uint32_t *)&sh.win[0].grad[slot])[w] = ((const uint32_t *)&grads[gp.grad])[w];
                     consumer_sync();
                     if (sh.win[0].paint[slot].flags & PAINT_SKIP) continue;
                     ox = hr.ox; oy = hr.oy;
@@ -689,7 +682,10 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
                 }
                 const WinBuf &pb = sh.win[hair ? 0u : cur_b];
                 const PaintRec &pr = pb.paint[slot];
-                const GradRec *gr = &pb.grad[slot];  // read only for gradient paints
+                // gradient and image records are read from global memory through the
+                // read-only path: not staging them leaves the producers less work and
+                // shared memory for a third window buffer
+                const GradRec *gr = grads + pr.grad;
                 const int32_t ly = cy - oy;
                 const int32_t lrow0 = (int32_t)wi.band * BH - oy;
 #pragma unroll 1
@@ -800,7 +796,7 @@ k_raster(int PX, const StreamRec *streams, const WorkItem *items, uint32_t nitem
                 break;
             }
         }
-        if (nwin) mb_arrive(&sh.mb_free[(win_base + nwin - 1u) & 1u]);
+        if (nwin) mb_arrive(&sh.mb_free[(win_base + nwin - 1u) % kWinBufs]);
         win_base += nwin;
         if (depth != 0) atomicOr(err, 8u);
         if (*(volatile int32_t *)&sh.abort == 0)
@@ -825,7 +821,7 @@ size_t raster_smem_bytes() { return raster_smem_bytes_px(16); }
 size_t raster_stack_words_per_cta(int px) { return (size_t)kMaxDepth * kThreads * px; }
 int raster_threads() { return kThreads; }
 int raster_max_pairs() { return kMaxPairs; }
-int raster_window_buffers() { return 2; }
+int raster_window_buffers() { return (int)kWinBufs; }
 
 cudaError_t raster_init() {
     return cudaFuncSetAttribute(k_raster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)raster_smem_bytes_px(16));
