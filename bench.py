@@ -427,9 +427,7 @@ def run_batched(args, rank, world):
         s1.record(stream)
         return s0, s1
 
-    for _ in range(args.warmup):
-        step()
-        scene.check()
+    stroke = warmup_with_stroke_record(step, scene, args.warmup)
     info = scene.info()
     if world > 1:
         torch.distributed.barrier()
@@ -516,7 +514,7 @@ def run_batched(args, rank, world):
                               "autotune_s": tune_s,
                               "buckets": "width <= %s x draws <= %s" % (list(BT.WIDTH_BUCKETS),
                                                                         list(BT.DRAW_BUCKETS))},
-                   "prepare_s": prep_s, "l2": "outputs %.1f GB > L2 (129 MB)" % (total / 1e9),
+                   "prepare_s": prep_s, "stroke": stroke, "l2": "outputs %.1f GB > L2 (129 MB)" % (total / 1e9),
                    "graph_replay": True},
         "mpix_s": value * out_px / n / 1e6 if n else 0.0,
         "plain": {"value": plain_value, "unit": "scenes/s", "sample_scenes": len(psamp),
@@ -695,9 +693,7 @@ def run_plain(args, rank, world):
         s1.record(stream)
         return s0, s1
 
-    for _ in range(args.warmup):
-        step()
-        scene.check()
+    stroke = warmup_with_stroke_record(step, scene, args.warmup)
     info = scene.info()
     if world > 1:
         torch.distributed.barrier()
@@ -751,7 +747,7 @@ def run_plain(args, rank, world):
         "config": {"workload": "config%d: %s" % (args.config, CONFIG_DESC.get(args.config, "")),
                    "canvas": [w, h], "draws": info["draws"], "edges": info["edges"],
                    "binned_edges": info["binned_edges"], "work_items": info["work_items"],
-                   "l2": "flushed between steps (256 MB write)", "graph_replay": True},
+                   "l2": "flushed between steps (256 MB write)", "graph_replay": True, "stroke": stroke},
         "mpix_s": value * out_px / 1e6,
         "raster_ms": rms,
         "wall_s_timed_region": t_wall,
@@ -775,6 +771,25 @@ def run_plain(args, rank, world):
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def warmup_with_stroke_record(step, scene, warmup):
+    """Runs the warm-up renders; the first one is the prepared scene's sizing
+    render, which strokes every path that has no outline yet on the device
+    (kernels/stroke.cu) and keeps the outlines for the renders after it.
+    Returns that pass's record: paths stroked and the stroke kernel's time."""
+    import resvg_gb300 as R
+    rec = None
+    s0 = R.stats()
+    for k in range(warmup):
+        step()
+        scene.check()
+        if k == 0:
+            s1 = R.stats()
+            rec = {"jobs": int(s1["stroke_jobs"] - s0["stroke_jobs"]),
+                   "device_ms": float(s1["stroke_ms"] - s0["stroke_ms"]),
+                   "when": "first (sizing) render; later renders and graph replays reuse the outlines"}
+    return rec
 
 
 def run_profile(args):

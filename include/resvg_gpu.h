@@ -198,11 +198,40 @@ int rgpu_set_batch_chunks(uint32_t chunks);
  * the largest render seen and are otherwise kept for reuse). */
 int rgpu_trim(void);
 
+/* Where stroke outlines are built when a tree is rendered: 1 (the default) on
+ * the device, one thread per stroked path; 0 on the host.  Both run the same
+ * stroker (tiny-skia-path's Path::stroke, called from resvg's
+ * crates/resvg/src/path.rs:113 through Pixmap::stroke_path) and give
+ * identical outlines.  Dashing (Path::dash, path.rs:106-111) stays on the
+ * host either way. */
+int rgpu_set_stroke_mode(int on_device);
+
+/* Strokes `count` paths and returns their outlines (the path to fill with the
+ * non-zero rule), as tiny-skia-path's Path::stroke(stroke, res_scale) does.
+ * Path i is verbs[verb_off, verb_off + verb_cnt) with points
+ * pts[2 * pt_off, 2 * (pt_off + pt_cnt)).  The outlines are written one after
+ * another to out_verbs / out_pts (x, y pairs), out_counts[2i] and
+ * out_counts[2i + 1] receiving path i's verb and point counts (0 when the
+ * stroke produces nothing).  on_device selects the device stroker (1) or the
+ * host one (0).  RGPU_ERR_CAPACITY when the outlines exceed verb_cap verbs or
+ * pt_cap points. */
+typedef struct rgpu_stroke_desc {
+    uint32_t verb_off, verb_cnt, pt_off, pt_cnt;
+    float width, miter_limit, res_scale;
+    uint32_t cap;   /* rgpu_cap */
+    uint32_t join;  /* rgpu_join */
+} rgpu_stroke_desc;
+int rgpu_stroke_paths(const rgpu_stroke_desc *descs, uint32_t count, const uint8_t *verbs, uint32_t verb_count,
+                      const float *pts, uint32_t pt_count, int on_device, uint8_t *out_verbs, uint32_t verb_cap,
+                      float *out_pts, uint32_t pt_cap, uint32_t *out_counts);
+
 /* Per-call statistics of the last render on this thread (for benchmarking). */
 typedef struct rgpu_stats {
     uint64_t draws, edges, crossings_capacity, work_items, kernel_launches;
     uint64_t h2d_bytes, d2h_bytes;
     float raster_ms;         /* device time of the raster kernel (CUDA events) */
+    float stroke_ms;         /* device time of the stroke kernel's last pass when it ran (CUDA events) */
+    uint64_t stroke_jobs;    /* paths stroked on the device */
 } rgpu_stats;
 int rgpu_get_stats(rgpu_stats *s);
 

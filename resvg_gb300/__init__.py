@@ -308,6 +308,67 @@ def set_batch_chunks(chunks: int) -> None:
     check(L.rgpu_set_batch_chunks(int(chunks)))
 
 
+def set_stroke_mode(on_device: bool) -> None:
+    """Build stroke outlines on the device (default) or on the host; both run
+    the same stroker and give identical outlines."""
+    L = lib()
+    L.rgpu_set_stroke_mode.restype = C.c_int
+    L.rgpu_set_stroke_mode.argtypes = [C.c_int]
+    check(L.rgpu_set_stroke_mode(1 if on_device else 0))
+
+
+class StrokeDesc(C.Structure):
+    _fields_ = [("verb_off", C.c_uint32), ("verb_cnt", C.c_uint32), ("pt_off", C.c_uint32), ("pt_cnt", C.c_uint32),
+                ("width", C.c_float), ("miter_limit", C.c_float), ("res_scale", C.c_float),
+                ("cap", C.c_uint32), ("join", C.c_uint32)]
+
+
+def stroke_paths(paths, on_device: bool = True):
+    """tiny-skia's Path::stroke for many paths at once (rgpu_stroke_paths).
+    `paths`: (verbs, points (n, 2), width, miter_limit, cap, join, res_scale)
+    tuples.  Returns one (verbs uint8, points float32 (m, 2)) outline per path
+    (empty arrays when the stroke produces nothing)."""
+    L = lib()
+    L.rgpu_stroke_paths.restype = C.c_int
+    P = C.c_void_p
+    L.rgpu_stroke_paths.argtypes = [C.POINTER(StrokeDesc), C.c_uint32, P, C.c_uint32, P, C.c_uint32, C.c_int,
+                                    P, C.c_uint32, P, C.c_uint32, P]
+    n = len(paths)
+    descs = (StrokeDesc * max(n, 1))()
+    vs, ps = [], []
+    vo = po = 0
+    for i, (v, pt, width, miter, cap, join, rs) in enumerate(paths):
+        v = np.ascontiguousarray(np.asarray(v, dtype=np.uint8))
+        pt = np.ascontiguousarray(np.asarray(pt, dtype=np.float32).reshape(-1, 2))
+        descs[i] = StrokeDesc(vo, len(v), po, len(pt), width, miter, rs, cap, join)
+        vs.append(v)
+        ps.append(pt)
+        vo += len(v)
+        po += len(pt)
+    verbs = np.concatenate(vs) if vs else np.zeros(1, np.uint8)
+    pts = np.concatenate(ps) if ps else np.zeros((1, 2), np.float32)
+    vcap, pcap = 64 * max(vo, 1) + 256 * n + 64, 64 * max(po, 1) + 256 * n + 64
+    while True:
+        ov = np.zeros(vcap, np.uint8)
+        op = np.zeros((pcap, 2), np.float32)
+        counts = np.zeros(2 * max(n, 1), np.uint32)
+        r = L.rgpu_stroke_paths(descs, n, verbs.ctypes.data, len(verbs), pts.ctypes.data, len(pts),
+                                1 if on_device else 0, ov.ctypes.data, vcap, op.ctypes.data, pcap,
+                                counts.ctypes.data)
+        if r == 5:  # RGPU_ERR_CAPACITY: larger output arrays
+            vcap, pcap = 4 * vcap, 4 * pcap
+            continue
+        check(r, "rgpu_stroke_paths")
+        break
+    out, a, b = [], 0, 0
+    for i in range(n):
+        nv, np_ = int(counts[2 * i]), int(counts[2 * i + 1])
+        out.append((ov[a:a + nv].copy(), op[b:b + np_].copy()))
+        a += nv
+        b += np_
+    return out
+
+
 def set_tuning_table(entries) -> None:
     """Band rows per (max stream width, max stream draws) bucket, used for
     streams whose band rows the tuning leaves automatic: entries are

@@ -107,7 +107,8 @@ class TuningEntry(C.Structure):
 class Stats(C.Structure):
     _fields_ = [("draws", C.c_uint64), ("edges", C.c_uint64), ("crossings_capacity", C.c_uint64),
                 ("work_items", C.c_uint64), ("kernel_launches", C.c_uint64),
-                ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64), ("raster_ms", f32)]
+                ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64), ("raster_ms", f32),
+                ("stroke_ms", f32), ("stroke_jobs", C.c_uint64)]
 
 
 class SoftBatch(C.Structure):

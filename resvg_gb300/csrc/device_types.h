@@ -91,7 +91,35 @@ struct DrawRec {
     int32_t start_y, stop_y, right_clip, super_left;  // scan range in (sub)scanline units
     uint32_t edge_base, edge_count;
 };
-enum : uint32_t { DRAW_EVENODD = 1, DRAW_AA = 2 };
+enum : uint32_t {
+    DRAW_EVENODD = 1,
+    DRAW_AA = 2,
+    DRAW_STROKED = 4,  // the geometry is a stroke outline built on the device (stroke arrays)
+};
+
+// One path stroked on the device (tiny-skia's Path::stroke, one thread per
+// job): the source path in the scene's geometry arrays, the stroke, and the
+// slice of the stroke arrays its outline is written to.  The thread writes the
+// outline's verb and point counts into draws[draw]; an outline that does not
+// fit its slice sets its status word instead and draws nothing.
+struct StrokeJob {
+    uint32_t src_verb_off, src_verb_cnt, src_pt_off, src_pt_cnt;
+    float width, miter_limit, res_scale;
+    uint32_t cap_join;     // rgpu_cap | rgpu_join << 8
+    uint32_t draw;         // the DrawRec that fills the outline
+    uint32_t verb_off, verb_cap;  // outline slice: verbs
+    uint32_t pt_off, pt_cap;      // outline slice: points (x, y pairs)
+    uint32_t seg_off;      // segment scratch: 2 * src_verb_cnt + 1 entries
+    uint32_t _pad[2];
+};
+static_assert(sizeof(StrokeJob) == 64, "StrokeJob layout");
+
+// One outline moved from its sizing slice to its exact slice.
+struct StrokeMove {
+    uint32_t src_verb, dst_verb, verbs;
+    uint32_t src_pt, dst_pt, pts;
+    uint32_t draw;
+};
 
 struct SegRec {
     uint32_t draw;

@@ -14,6 +14,11 @@
 #include <thread>
 
 namespace rgpu {
+
+static std::atomic<bool> g_device_stroke{true};
+void set_device_stroke(bool on) { g_device_stroke.store(on); }
+bool device_stroke_enabled() { return g_device_stroke.load(); }
+
 namespace {
 
 struct ColorF { float r, g, b, a; };
@@ -462,7 +467,46 @@ struct Flattener {
             if (hairline(pi, sh, blend, ts, tg, rs)) return;
             if (!paint_rec(sh, blend, p.anti_alias != 0, ts, pr)) return;
         }
-        auto outline = tree.stroke_outline(pi, rs);
+        bool cached = false;
+        std::shared_ptr<PathData> outline;
+        if (device_stroke_enabled()) outline = tree.cached_stroke_outline(pi, rs, &cached);
+        if (device_stroke_enabled() && !cached) {
+            // stroked on the device (kernels/stroke.cu): a job over the source
+            // path, whose outline the draw fills; the outline then goes to the
+            // tree's cache for later flattens
+            if (!(p.stroke_width > 0)) return;
+            uint32_t sv = tree_verb_base + p.verb_offset, sp = tree_pt_base + p.point_offset;
+            uint32_t nv = p.verb_count, np = p.point_count;
+            if (p.dash_count) {
+                // dash.rs on the host; the dashed path is the stroker's source
+                PathData dashed;
+                if (dash_path(t.verbs + p.verb_offset, p.verb_count, t.points + 2 * (size_t)p.point_offset,
+                              p.point_count, t.dashes + p.dash_offset, p.dash_count, p.dash_phase, rs, dashed)) {
+                    if (dashed.empty()) return;
+                    sv = (uint32_t)sb.verbs.size();
+                    sp = (uint32_t)(sb.pts.size() / 2);
+                    nv = (uint32_t)dashed.verbs.size();
+                    np = (uint32_t)(dashed.pts.size() / 2);
+                    sb.verbs.insert(sb.verbs.end(), dashed.verbs.begin(), dashed.verbs.end());
+                    sb.pts.insert(sb.pts.end(), dashed.pts.begin(), dashed.pts.end());
+                }
+            }
+            StrokeJob j;
+            std::memset(&j, 0, sizeof(j));
+            j.src_verb_off = sv; j.src_verb_cnt = nv;
+            j.src_pt_off = sp; j.src_pt_cnt = np;
+            j.width = p.stroke_width;
+            j.miter_limit = p.miter_limit;
+            j.res_scale = rs;
+            j.cap_join = (p.line_cap & 0xFFu) | (p.line_join & 0xFFu) << 8;
+            j.draw = (uint32_t)cur->draws.size();
+            cur->strokes.push_back(j);
+            cur->stroke_keys.push_back(StrokeKey{&tree, pi, rs});
+            emit_draw(CMD_FILL, 0, 0, 0, 0, ts, tg, RGPU_NONZERO, p.anti_alias != 0, add_paint(pr));
+            cur->draws.back().flags |= DRAW_STROKED;
+            return;
+        }
+        if (!cached) outline = tree.stroke_outline(pi, rs);
         if (!outline || outline->verbs.empty()) return;
         uint32_t vo = (uint32_t)sb.verbs.size(), po = (uint32_t)(sb.pts.size() / 2);
         sb.verbs.insert(sb.verbs.end(), outline->verbs.begin(), outline->verbs.end());
@@ -711,6 +755,11 @@ uint32_t SceneBuild::append_stream(StreamBuild &b) {
         ntpts += d.pt_cnt;
         draws.push_back(d);
     }
+    for (auto j : b.strokes) {
+        j.draw += st.draw_off;
+        stroke_jobs.push_back(j);
+    }
+    stroke_keys.insert(stroke_keys.end(), b.stroke_keys.begin(), b.stroke_keys.end());
     for (auto c : b.cmds) {
         if (c.op == CMD_FILL || c.op == CMD_APPLY_REGION) c.a += st.draw_off;
         cmds.push_back(c);
@@ -726,14 +775,14 @@ void SceneBuild::merge(std::vector<SceneBuild> &parts, unsigned threads) {
     // one after another into one build.  Arrays are sized first, then each part
     // is copied into its ranges with the index fix-ups, parts in parallel.
     struct Off {
-        size_t verbs, pts, draws, paints, grads, layers, cmds, streams, surfaces, jobs, fe, patterns, hairs, hspans;
+        size_t verbs, pts, draws, paints, grads, layers, cmds, streams, surfaces, jobs, fe, patterns, hairs, hspans, strokes;
         uint64_t nsegs, ntpts;
     };
     const size_t n = parts.size();
     std::vector<Off> off(n + 1);
     Off cur{verbs.size(), pts.size(), draws.size(), paints.size(), grads.size(), layers.size(), cmds.size(),
             streams.size(), surfaces.size(), jobs.size(), fe_images.size(), patterns.size(), hairs.size(),
-            hair_spans.size(), nsegs, ntpts};
+            hair_spans.size(), stroke_jobs.size(), nsegs, ntpts};
     for (size_t k = 0; k < n; k++) {
         const SceneBuild &o = parts[k];
         off[k] = cur;
@@ -741,7 +790,7 @@ void SceneBuild::merge(std::vector<SceneBuild> &parts, unsigned threads) {
         cur.paints += o.paints.size(); cur.grads += o.grads.size(); cur.layers += o.layers.size();
         cur.cmds += o.cmds.size(); cur.streams += o.streams.size(); cur.surfaces += o.surfaces.size();
         cur.jobs += o.jobs.size(); cur.fe += o.fe_images.size(); cur.patterns += o.patterns.size();
-        cur.hairs += o.hairs.size(); cur.hspans += o.hair_spans.size();
+        cur.hairs += o.hairs.size(); cur.hspans += o.hair_spans.size(); cur.strokes += o.stroke_jobs.size();
         cur.nsegs += o.nsegs; cur.ntpts += o.ntpts;
         max_level = std::max(max_level, o.max_level);
     }
@@ -749,7 +798,8 @@ void SceneBuild::merge(std::vector<SceneBuild> &parts, unsigned threads) {
     verbs.resize(cur.verbs); pts.resize(cur.pts); draws.resize(cur.draws); paints.resize(cur.paints);
     grads.resize(cur.grads); layers.resize(cur.layers); cmds.resize(cur.cmds); streams.resize(cur.streams);
     surfaces.resize(cur.surfaces); jobs.resize(cur.jobs); fe_images.resize(cur.fe); patterns.resize(cur.patterns);
-    hairs.resize(cur.hairs); hair_spans.resize(cur.hspans);
+    hairs.resize(cur.hairs); hair_spans.resize(cur.hspans); stroke_jobs.resize(cur.strokes);
+    stroke_keys.resize(cur.strokes);
     nsegs = cur.nsegs;
     ntpts = cur.ntpts;
     auto copy_part = [&](size_t k) {
@@ -777,6 +827,14 @@ void SceneBuild::merge(std::vector<SceneBuild> &parts, unsigned threads) {
             paints[b.paints + i] = q;
         }
         std::copy(o.grads.begin(), o.grads.end(), grads.begin() + b.grads);
+        for (size_t i = 0; i < o.stroke_jobs.size(); i++) {
+            StrokeJob j = o.stroke_jobs[i];
+            j.src_verb_off += V;
+            j.src_pt_off += P;
+            j.draw += D;
+            stroke_jobs[b.strokes + i] = j;
+        }
+        std::copy(o.stroke_keys.begin(), o.stroke_keys.end(), stroke_keys.begin() + b.strokes);
         for (size_t i = 0; i < o.layers.size(); i++) {
             LayerRec l = o.layers[i];
             if (l.surf >= 0) l.surf += (int32_t)SU;

@@ -56,8 +56,18 @@ struct FeImageReq {
     uint32_t surface;
 };
 
+// A device stroke job's entry in its tree's outline cache: once the device
+// has built the outline, later flattens of the tree reuse it.
+struct StrokeKey {
+    Tree *tree;
+    uint32_t path;
+    float res_scale;
+};
+
 struct StreamBuild {
     std::vector<DrawRec> draws;     // seg_base / tpt_base / stream assigned on append
+    std::vector<StrokeJob> strokes; // draw = index within this stream; outline slices set by the plan
+    std::vector<StrokeKey> stroke_keys;  // per stroke job: where its outline is cached
     std::vector<Cmd> cmds;          // FILL / APPLY_REGION: a = draw index within this stream
     std::vector<LayerRec> layers;
     int32_t out_w = 0, out_h = 0;
@@ -84,6 +94,8 @@ struct SceneBuild {
     std::vector<uint32_t> fill_cmds;  // per stream: its fill / region command indices (plan_scene)
     std::vector<uint8_t> verbs;
     std::vector<float> pts;
+    std::vector<StrokeJob> stroke_jobs;  // paths stroked on the device (their draws carry DRAW_STROKED)
+    std::vector<StrokeKey> stroke_keys;  // per job: the tree outline cache entry it fills
     uint64_t nsegs = 0, ntpts = 0;
     uint32_t max_level = 0;
     std::string error;
@@ -103,5 +115,10 @@ struct SceneBuild {
     // trees be flattened on separate threads.
     void merge(std::vector<SceneBuild> &parts, unsigned threads);
 };
+
+// Where stroke outlines are built: on the device by kernels/stroke.cu (the
+// default) or on the host by stroke.cpp (the same stroker source).
+void set_device_stroke(bool on);
+bool device_stroke_enabled();
 
 }  // namespace rgpu

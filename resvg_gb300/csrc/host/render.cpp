@@ -115,12 +115,16 @@ struct Buffers {
     DevBuf edges, edge_draw, bin_counts, bin_offsets, bins;
     DevBuf stack, span_ovf, run_ovf, err, counter, fill_cmds;
     DevBuf hairs, hair_spans;
+    // device stroking: jobs, outlines, builder scratch, segment scratch,
+    // per-job status, per-draw sizes and bases
+    DevBuf sjobs, sverbs, spts, sscr_verbs, sscr_pts, ssegs, sstatus, dsizes, dbases;
     std::vector<DevBuf> surf, img;   // internal surfaces (filter content/results) and filter images
     DevBuf plane;                    // f64 plane of the IIR blur
     void release() {
         DevBuf *all[] = {&verbs, &pts, &draws, &paints, &grads, &layers, &cmds, &streams, &items, &tpts, &segs,
                          &seg_counts, &seg_offsets, &scan_scratch, &totals, &edges, &edge_draw, &bin_counts,
-                         &bin_offsets, &bins, &stack, &span_ovf, &run_ovf, &err, &counter, &fill_cmds, &plane, &hairs, &hair_spans};
+                         &bin_offsets, &bins, &stack, &span_ovf, &run_ovf, &err, &counter, &fill_cmds, &plane, &hairs, &hair_spans,
+                         &sjobs, &sverbs, &spts, &sscr_verbs, &sscr_pts, &ssegs, &sstatus, &dsizes, &dbases};
         for (DevBuf *b : all) b->release();
         for (auto &b : surf) b.release();
         for (auto &b : img) b.release();
@@ -163,6 +167,16 @@ struct Plan {
     uint32_t grid = 1;
     uint32_t run_cap = 0;              // alpha-run overflow entries per (draw, row) pair
     uint32_t nedges = 0, nbinned = 0;  // known after the first (sizing) run
+    // segment slots and transformed points: the build's own counts, or with
+    // device-stroked paths the device's totals (known after the sizing run)
+    uint64_t nsegs = 0, ntpts = 0;
+    // device stroking: per job the outline slice (verbs, points); the layout's
+    // totals in the stroke arrays and the segment scratch
+    std::vector<uint32_t> svcap, spcap;
+    uint64_t sverbs = 0, spts = 0, ssegs = 0;
+    // the outlines, their DrawRec counts and the draws' bases are in device
+    // memory since the last upload: renders (and graph replays) reuse them
+    bool strokes_ready = false;
     bool sized = false;
 };
 
@@ -249,6 +263,7 @@ int ensure_device(Context &c) {
     c.sms = prop.multiProcessorCount;
     CK(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
     CK(raster_init());
+    CK(stroke_warmup(c.stream));
     c.device = dev;
     return RGPU_OK;
 }
@@ -284,8 +299,75 @@ uint32_t pick_bh(int32_t w, uint32_t draws, uint32_t px, const Tuning &tu) {
 }
 
 // Host-side work decomposition of a flattened submission.
+// Places each stroke job's outline slice (p.svcap / p.spcap) and segment
+// scratch in the stroke arrays.
+int layout_strokes(Plan &p) {
+    uint64_t v = 0, q = 0, g = 0;
+    auto &jobs = p.sb.stroke_jobs;
+    for (size_t i = 0; i < jobs.size(); i++) {
+        StrokeJob &j = jobs[i];
+        j.verb_off = (uint32_t)v;
+        j.verb_cap = p.svcap[i];
+        j.pt_off = (uint32_t)q;
+        j.pt_cap = p.spcap[i];
+        j.seg_off = (uint32_t)g;
+        v += j.verb_cap;
+        q += j.pt_cap;
+        g += 2ull * j.src_verb_cnt + 1;
+        if (v > 0x7FFFFFFFull || q > 0x3FFFFFFFull || g > 0x7FFFFFFFull) {
+            set_error("stroke outlines exceed the stroke arrays' index range");
+            return RGPU_ERR_CAPACITY;
+        }
+    }
+    p.sverbs = v;
+    p.spts = q;
+    p.ssegs = g;
+    return RGPU_OK;
+}
+
 int plan_scene(Context &c, Plan &p) {
     SceneBuild &sb = p.sb;
+    if (sb.stroke_jobs.empty()) {
+        p.nsegs = sb.nsegs;
+        p.ntpts = sb.ntpts;
+    }
+    if (!sb.stroke_jobs.empty() && p.svcap.size() != sb.stroke_jobs.size()) {
+        // one thread strokes one path, so the 32 paths of a warp run in step
+        // only as far as their control flow agrees: order the jobs by source
+        // verb count and cap / join (each keeps its draw and cache entry)
+        {
+            const size_t nj = sb.stroke_jobs.size();
+            std::vector<uint32_t> ord(nj);
+            for (size_t i = 0; i < nj; i++) ord[i] = (uint32_t)i;
+            auto key = [&](uint32_t i) {
+                const StrokeJob &j = sb.stroke_jobs[i];
+                return ((uint64_t)j.src_verb_cnt << 32) | j.cap_join;
+            };
+            std::stable_sort(ord.begin(), ord.end(), [&](uint32_t a, uint32_t b) { return key(a) < key(b); });
+            std::vector<StrokeJob> jobs(nj);
+            for (size_t i = 0; i < nj; i++) jobs[i] = sb.stroke_jobs[ord[i]];
+            sb.stroke_jobs.swap(jobs);
+            if (sb.stroke_keys.size() == nj) {
+                std::vector<StrokeKey> keys(nj);
+                for (size_t i = 0; i < nj; i++) keys[i] = sb.stroke_keys[ord[i]];
+                sb.stroke_keys.swap(keys);
+            }
+        }
+        // first slices: outlines measured on the benchmark scenes average 15
+        // verbs and 12 points per source verb and point (at most 29 and 24);
+        // a larger outline is given a larger slice by the sizing run
+        p.svcap.resize(sb.stroke_jobs.size());
+        p.spcap.resize(sb.stroke_jobs.size());
+        for (size_t i = 0; i < sb.stroke_jobs.size(); i++) {
+            p.svcap[i] = 32u * sb.stroke_jobs[i].src_verb_cnt + 64u;
+            p.spcap[i] = 32u * sb.stroke_jobs[i].src_pt_cnt + 128u;
+        }
+        p.sized = false;
+    }
+    if (!sb.stroke_jobs.empty()) {
+        int r = layout_strokes(p);
+        if (r) return r;
+    }
     p.px = pick_px(sb, c.tuning);
     p.items.clear();
     p.nbins = 0;
@@ -341,6 +423,168 @@ int plan_scene(Context &c, Plan &p) {
     return RGPU_OK;
 }
 
+int ensure_stroke_buffers(Buffers &b, Plan &p) {
+    if (p.sb.stroke_jobs.empty()) return RGPU_OK;
+    const size_t nd = p.sb.draws.size();
+    CK(b.sverbs.ensure(std::max<uint64_t>(p.sverbs, 1)));
+    CK(b.spts.ensure(std::max<uint64_t>(p.spts, 1) * 8));
+    CK(b.sscr_verbs.ensure(std::max<uint64_t>(2 * p.sverbs, 1)));
+    CK(b.sscr_pts.ensure(std::max<uint64_t>(2 * p.spts, 1) * 8));
+    CK(b.ssegs.ensure(std::max<uint64_t>(p.ssegs, 1) * stroke_seg_bytes()));
+    CK(b.sstatus.ensure(p.sb.stroke_jobs.size() * 8));
+    CK(b.dsizes.ensure((nd + 1) * 8));
+    CK(b.dbases.ensure((nd + 1) * 8));
+    return RGPU_OK;
+}
+
+int ensure_segment_buffers(Buffers &b, Plan &p) {
+    const uint64_t nsegs = p.nsegs;
+    CK(b.tpts.ensure(std::max<uint64_t>(p.ntpts, 1) * 8));
+    CK(b.segs.ensure(std::max<uint64_t>(nsegs, 1) * sizeof(SegRec)));
+    CK(b.seg_counts.ensure((nsegs + 1) * 4));
+    CK(b.seg_offsets.ensure((nsegs + 1) * 4));
+    CK(b.scan_scratch.ensure(scan_scratch_words(std::max<uint64_t>({nsegs + 1, p.nbins + 1, p.sb.draws.size() + 1})) * 4));
+    return RGPU_OK;
+}
+
+// One device stroking pass: every job's outline into its slice (the counts
+// into its DrawRec), then the per-draw segment and point bases.
+int stroke_pass(Buffers &b, Plan &p, cudaStream_t s) {
+    SceneBuild &sb = p.sb;
+    const uint32_t nj = (uint32_t)sb.stroke_jobs.size(), nd = (uint32_t)sb.draws.size();
+    uint32_t *totals = b.totals.as<uint32_t>();
+    uint32_t *sz = b.dsizes.as<uint32_t>(), *bs = b.dbases.as<uint32_t>();
+    CK(launch_stroke(b.sjobs.as<StrokeJob>(), nj, b.verbs.as<uint8_t>(), b.pts.as<float>(), b.sverbs.as<uint8_t>(),
+                     b.spts.as<float>(), b.sscr_verbs.as<uint8_t>(), b.sscr_pts.as<float>(), b.ssegs.p,
+                     b.draws.as<DrawRec>(), b.sstatus.as<uint32_t>(), s));
+    CK(launch_draw_sizes(b.draws.as<DrawRec>(), nd, sz, sz + (nd + 1), s));
+    CK(launch_exclusive_scan(sz, bs, nd, b.scan_scratch.as<uint32_t>(), totals + 2, s));
+    CK(launch_exclusive_scan(sz + (nd + 1), bs + (nd + 1), nd, b.scan_scratch.as<uint32_t>(), totals + 3, s));
+    CK(launch_draw_bases(b.draws.as<DrawRec>(), nd, bs, bs + (nd + 1), s));
+    g_stats.kernel_launches += 5;
+    return RGPU_OK;
+}
+
+// Copies the outlines the device built into their trees' outline caches, so
+// that flattening the same trees again reuses them instead of new jobs.
+int cache_outlines(Buffers &b, Plan &p, cudaStream_t s) {
+    SceneBuild &sb = p.sb;
+    const size_t nj = sb.stroke_jobs.size();
+    if (sb.stroke_keys.size() != nj) return RGPU_OK;
+    std::vector<uint8_t> hv(p.sverbs);
+    std::vector<float> hp(2 * p.spts);
+    if (p.sverbs) CK(cudaMemcpyAsync(hv.data(), b.sverbs.p, p.sverbs, cudaMemcpyDeviceToHost, s));
+    if (p.spts) CK(cudaMemcpyAsync(hp.data(), b.spts.p, p.spts * 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    g_stats.d2h_bytes += p.sverbs + p.spts * 8;
+    auto store = [&](size_t a, size_t e) {
+        for (size_t j = a; j < e; j++) {
+            const StrokeJob &jb = sb.stroke_jobs[j];
+            std::shared_ptr<PathData> out;
+            if (jb.verb_cap > 1) {
+                out = std::make_shared<PathData>();
+                out->verbs.assign(hv.begin() + jb.verb_off, hv.begin() + jb.verb_off + jb.verb_cap);
+                out->pts.assign(hp.begin() + 2 * (size_t)jb.pt_off, hp.begin() + 2 * ((size_t)jb.pt_off + jb.pt_cap));
+            }
+            const StrokeKey &k = sb.stroke_keys[j];
+            k.tree->store_stroke_outline(k.path, k.res_scale, std::move(out));
+        }
+    };
+    // contiguous ranges: a tree's jobs are adjacent, so threads rarely share a cache
+    const size_t nt = std::min<size_t>(std::max(1u, std::thread::hardware_concurrency()), nj / 4096 + 1);
+    std::vector<std::thread> pool;
+    for (size_t k = 1; k < nt; k++) pool.emplace_back(store, nj * k / nt, nj * (k + 1) / nt);
+    store(0, nj / nt);
+    for (auto &t : pool) t.join();
+    return RGPU_OK;
+}
+
+// Device stroking with the sizing run: outlines that outgrow their slice are
+// stroked again with four times the room until all fit, then every slice is
+// cut to its outline's exact size and the outlines are built once more in
+// that layout, which later renders (and graph replays) reuse.
+int run_strokes(Buffers &b, Plan &p, cudaStream_t s) {
+    int r;
+    if (p.sized) return stroke_pass(b, p, s);
+    SceneBuild &sb = p.sb;
+    const size_t nj = sb.stroke_jobs.size();
+    std::vector<uint32_t> st(2 * nj);
+    auto reupload = [&]() -> int {
+        int rr = layout_strokes(p);
+        if (rr) return rr;
+        if ((rr = ensure_stroke_buffers(b, p))) return rr;
+        CK(b.sjobs.ensure(nj * sizeof(StrokeJob)));
+        CK(cudaMemcpyAsync(b.sjobs.p, sb.stroke_jobs.data(), nj * sizeof(StrokeJob), cudaMemcpyHostToDevice, s));
+        CK(cudaStreamSynchronize(s));
+        return RGPU_OK;
+    };
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    const bool timed = cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess;
+    for (int round = 0;; round++) {
+        if (timed && round == 0) CK(cudaEventRecord(e0, s));
+        if ((r = stroke_pass(b, p, s))) return r;
+        if (timed && round == 0) CK(cudaEventRecord(e1, s));
+        CK(cudaMemcpyAsync(st.data(), b.sstatus.p, nj * 8, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        bool grow = false;
+        for (size_t j = 0; j < nj; j++)
+            if (st[2 * j] & 0x80000000u) {
+                grow = true;
+                p.svcap[j] = (uint32_t)std::min<uint64_t>(4ull * p.svcap[j], 0x10000000ull);
+                p.spcap[j] = (uint32_t)std::min<uint64_t>(4ull * p.spcap[j], 0x10000000ull);
+            }
+        if (!grow) break;
+        if (round >= 6) {
+            set_error("a stroke outline outgrew its slice after repeated growth");
+            return RGPU_ERR_CAPACITY;
+        }
+        if ((r = reupload())) return r;
+    }
+    // every outline fits: move each to a slice of its exact size in the
+    // scratch arrays, which then become the outline arrays
+    std::vector<StrokeMove> moves(nj);
+    for (size_t j = 0; j < nj; j++) {
+        moves[j].src_verb = sb.stroke_jobs[j].verb_off;
+        moves[j].src_pt = sb.stroke_jobs[j].pt_off;
+        moves[j].verbs = st[2 * j];
+        moves[j].pts = st[2 * j + 1];
+        moves[j].draw = sb.stroke_jobs[j].draw;
+        p.svcap[j] = st[2 * j];
+        p.spcap[j] = st[2 * j + 1];
+    }
+    if ((r = layout_strokes(p))) return r;
+    for (size_t j = 0; j < nj; j++) {
+        moves[j].dst_verb = sb.stroke_jobs[j].verb_off;
+        moves[j].dst_pt = sb.stroke_jobs[j].pt_off;
+    }
+    DevBuf dmoves;
+    CK(dmoves.ensure(nj * sizeof(StrokeMove)));
+    CK(cudaMemcpyAsync(dmoves.p, moves.data(), nj * sizeof(StrokeMove), cudaMemcpyHostToDevice, s));
+    CK(launch_stroke_gather(dmoves.as<StrokeMove>(), (uint32_t)nj, b.sverbs.as<uint8_t>(), b.spts.as<float>(),
+                            b.sscr_verbs.as<uint8_t>(), b.sscr_pts.as<float>(), b.draws.as<DrawRec>(), s));
+    CK(cudaMemcpyAsync(b.sjobs.p, sb.stroke_jobs.data(), nj * sizeof(StrokeJob), cudaMemcpyHostToDevice, s));
+    CK(cudaStreamSynchronize(s));
+    dmoves.release();
+    std::swap(b.sverbs, b.sscr_verbs);
+    std::swap(b.spts, b.sscr_pts);
+    if ((r = ensure_stroke_buffers(b, p))) return r;
+    uint32_t tot[2] = {0, 0};
+    CK(cudaMemcpyAsync(tot, b.totals.as<uint32_t>() + 2, 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    p.nsegs = tot[0];
+    p.ntpts = tot[1];
+    g_stats.stroke_jobs += nj;
+    if (timed) {
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess) g_stats.stroke_ms += ms;
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaGetLastError();
+    if ((r = cache_outlines(b, p, s))) return r;
+    return ensure_segment_buffers(b, p);
+}
+
 int upload_plan(Context &c, Buffers &b, Plan &p, cudaStream_t s, HostBuf *staging_buf = nullptr) {
     HostBuf &staging = staging_buf ? *staging_buf : c.staging;
     SceneBuild &sb = p.sb;
@@ -365,7 +609,7 @@ int upload_plan(Context &c, Buffers &b, Plan &p, cudaStream_t s, HostBuf *stagin
                    rup(sb.layers.size() * sizeof(LayerRec)) + rup(sb.cmds.size() * sizeof(Cmd)) +
                    rup(sb.streams.size() * sizeof(StreamRec)) + rup(p.items.size() * sizeof(WorkItem)) +
                    rup(sb.hairs.size() * sizeof(HairRec)) + rup(sb.hair_spans.size() * sizeof(HairSpan)) +
-                   rup(sb.fill_cmds.size() * 4) + 4096;
+                   rup(sb.fill_cmds.size() * 4) + rup(sb.stroke_jobs.size() * sizeof(StrokeJob)) + 4096;
     CK(staging.ensure(stage));
     size_t off = 0;
     int r;
@@ -381,14 +625,15 @@ int upload_plan(Context &c, Buffers &b, Plan &p, cudaStream_t s, HostBuf *stagin
     if ((r = upload(staging, b.hairs, sb.hairs, off, s))) return r;
     if ((r = upload(staging, b.hair_spans, sb.hair_spans, off, s))) return r;
     if ((r = upload(staging, b.fill_cmds, sb.fill_cmds, off, s))) return r;
-    // fixed-size work buffers
-    uint64_t nsegs = sb.nsegs;
-    CK(b.tpts.ensure(std::max<uint64_t>(sb.ntpts, 1) * 8));
-    CK(b.segs.ensure(std::max<uint64_t>(nsegs, 1) * sizeof(SegRec)));
-    CK(b.seg_counts.ensure((nsegs + 1) * 4));
-    CK(b.seg_offsets.ensure((nsegs + 1) * 4));
+    if ((r = upload(staging, b.sjobs, sb.stroke_jobs, off, s))) return r;
+    if ((r = ensure_stroke_buffers(b, p))) return r;
+    p.strokes_ready = false;  // the draws just uploaded carry no outline counts
+    // fixed-size work buffers (with device-stroked paths the segment counts
+    // are the device's, so these follow the sizing run)
+    if (sb.stroke_jobs.empty() || p.sized)
+        if ((r = ensure_segment_buffers(b, p))) return r;
     CK(b.totals.ensure(64));
-    CK(b.scan_scratch.ensure(scan_scratch_words(std::max<uint64_t>(nsegs + 1, p.nbins + 1)) * 4));
+    CK(b.scan_scratch.ensure(scan_scratch_words(std::max<uint64_t>({p.nsegs + 1, p.nbins + 1, sb.draws.size() + 1})) * 4));
     CK(b.bin_counts.ensure((p.nbins + 1) * 4));
     CK(b.bin_offsets.ensure((p.nbins + 1) * 4));
     size_t stack_words = (size_t)p.max_depth * raster_threads() * p.px;
@@ -406,10 +651,15 @@ int upload_plan(Context &c, Buffers &b, Plan &p, cudaStream_t s, HostBuf *stagin
 int enqueue_plan(Context &c, Buffers &b, Plan &p, cudaStream_t s, RasterTimer *tm) {
     SceneBuild &sb = p.sb;
     uint32_t ndraws = (uint32_t)sb.draws.size();
-    uint64_t nsegs = sb.nsegs;
+    if (!sb.stroke_jobs.empty() && !p.strokes_ready) {
+        int r = run_strokes(b, p, s);
+        if (r) return r;
+        p.strokes_ready = true;
+    }
+    uint64_t nsegs = p.nsegs;
     uint32_t *totals = b.totals.as<uint32_t>();
-    CK(launch_draw_setup(b.draws.as<DrawRec>(), ndraws, b.verbs.as<uint8_t>(), b.pts.as<float>(), b.tpts.p,
-                         b.segs.as<SegRec>(), s));
+    CK(launch_draw_setup(b.draws.as<DrawRec>(), ndraws, b.verbs.as<uint8_t>(), b.pts.as<float>(),
+                         b.sverbs.as<uint8_t>(), b.spts.as<float>(), b.tpts.p, b.segs.as<SegRec>(), s));
     CK(cudaMemsetAsync(b.seg_counts.p, 0, (nsegs + 1) * 4, s));
     CK(launch_edges(false, b.segs.as<SegRec>(), (uint32_t)nsegs, b.draws.as<DrawRec>(), b.tpts.p,
                     b.seg_counts.as<uint32_t>(), nullptr, nullptr, nullptr, 0, s));
@@ -939,7 +1189,7 @@ int rgpu_scene_info(const rgpu_scene *sc, rgpu_scene_stats *st) {
     st->streams = p.sb.streams.size();
     st->draws = p.sb.draws.size();
     st->commands = p.sb.cmds.size();
-    st->segments = p.sb.nsegs;
+    st->segments = p.nsegs;
     st->edges = p.nedges;
     st->binned_edges = p.nbinned;
     st->work_items = p.items.size();
@@ -1106,6 +1356,109 @@ int rgpu_trim(void) {
         sl.staging.release();
     }
     c.pipe_err.release();
+    return RGPU_OK;
+}
+
+int rgpu_set_stroke_mode(int on_device) {
+    set_device_stroke(on_device != 0);
+    return RGPU_OK;
+}
+
+int rgpu_stroke_paths(const rgpu_stroke_desc *descs, uint32_t count, const uint8_t *verbs, uint32_t verb_count,
+                      const float *pts, uint32_t pt_count, int on_device, uint8_t *out_verbs, uint32_t verb_cap,
+                      float *out_pts, uint32_t pt_cap, uint32_t *out_counts) {
+    g_last_error.clear();
+    if ((count && (!descs || !verbs || !pts || !out_counts)) || (verb_cap && !out_verbs) || (pt_cap && !out_pts)) {
+        set_error("invalid arguments");
+        return RGPU_ERR_INVALID_ARG;
+    }
+    for (uint32_t i = 0; i < count; i++) {
+        const rgpu_stroke_desc &d = descs[i];
+        if ((uint64_t)d.verb_off + d.verb_cnt > verb_count || (uint64_t)d.pt_off + d.pt_cnt > pt_count) {
+            set_error("path %u lies outside the verb / point arrays", i);
+            return RGPU_ERR_INVALID_ARG;
+        }
+    }
+    uint64_t vo = 0, po = 0;
+    auto put = [&](uint32_t i, const uint8_t *v, uint32_t nv, const float *q, uint32_t np) -> int {
+        if (vo + nv > verb_cap || po + np > pt_cap) {
+            set_error("the outlines exceed the output arrays");
+            return RGPU_ERR_CAPACITY;
+        }
+        std::memcpy(out_verbs + vo, v, nv);
+        std::memcpy(out_pts + 2 * po, q, (size_t)np * 8);
+        vo += nv;
+        po += np;
+        out_counts[2 * i] = nv;
+        out_counts[2 * i + 1] = np;
+        return RGPU_OK;
+    };
+    if (!on_device) {
+        for (uint32_t i = 0; i < count; i++) {
+            const rgpu_stroke_desc &d = descs[i];
+            StrokeStyle st;
+            st.width = d.width;
+            st.miter_limit = d.miter_limit;
+            st.cap = d.cap;
+            st.join = d.join;
+            PathData o;
+            if (!stroke_path(verbs + d.verb_off, d.verb_cnt, pts + 2 * (size_t)d.pt_off, d.pt_cnt, st, d.res_scale, o))
+                o = PathData();
+            int r = put(i, o.verbs.data(), (uint32_t)o.verbs.size(), o.pts.data(), (uint32_t)(o.pts.size() / 2));
+            if (r) return r;
+        }
+        return RGPU_OK;
+    }
+    Context &c = ctx();
+    std::lock_guard<std::mutex> lock(c.mu);
+    int r = ensure_device(c);
+    if (r) return r;
+    if (!count) return RGPU_OK;
+    cudaStream_t s = c.stream;
+    // one job per path over a standalone plan: every job has its own DrawRec
+    static Buffers b;
+    Plan p;
+    p.sb.verbs.assign(verbs, verbs + verb_count);
+    p.sb.pts.assign(pts, pts + 2 * (size_t)pt_count);
+    p.sb.draws.resize(count);
+    std::memset(p.sb.draws.data(), 0, count * sizeof(DrawRec));
+    p.sb.stroke_jobs.resize(count);
+    for (uint32_t i = 0; i < count; i++) {
+        const rgpu_stroke_desc &d = descs[i];
+        StrokeJob &j = p.sb.stroke_jobs[i];
+        std::memset(&j, 0, sizeof(j));
+        j.src_verb_off = d.verb_off; j.src_verb_cnt = d.verb_cnt;
+        j.src_pt_off = d.pt_off; j.src_pt_cnt = d.pt_cnt;
+        j.width = d.width; j.miter_limit = d.miter_limit; j.res_scale = d.res_scale;
+        j.cap_join = (d.cap & 0xFFu) | (d.join & 0xFFu) << 8;
+        j.draw = i;
+    }
+    if ((r = plan_scene(c, p))) return r;
+    CK(b.verbs.ensure(std::max<size_t>(p.sb.verbs.size(), 1)));
+    CK(b.pts.ensure(std::max<size_t>(p.sb.pts.size(), 1) * 4));
+    CK(b.draws.ensure(count * sizeof(DrawRec)));
+    CK(b.sjobs.ensure(count * sizeof(StrokeJob)));
+    CK(b.totals.ensure(64));
+    CK(b.scan_scratch.ensure(scan_scratch_words((uint64_t)count + 1) * 4));
+    if ((r = ensure_stroke_buffers(b, p))) return r;
+    CK(cudaMemcpyAsync(b.verbs.p, p.sb.verbs.data(), p.sb.verbs.size(), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(b.pts.p, p.sb.pts.data(), p.sb.pts.size() * 4, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(b.draws.p, p.sb.draws.data(), count * sizeof(DrawRec), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(b.sjobs.p, p.sb.stroke_jobs.data(), count * sizeof(StrokeJob), cudaMemcpyHostToDevice, s));
+    if ((r = run_strokes(b, p, s))) return r;
+    std::vector<uint8_t> hv(p.sverbs);
+    std::vector<float> hp(2 * p.spts);
+    if (p.sverbs) CK(cudaMemcpyAsync(hv.data(), b.sverbs.p, p.sverbs, cudaMemcpyDeviceToHost, s));
+    if (p.spts) CK(cudaMemcpyAsync(hp.data(), b.spts.p, p.spts * 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    // the plan orders jobs by shape; job.draw is the path's index
+    std::vector<uint32_t> job_of(count);
+    for (uint32_t k = 0; k < count; k++) job_of[p.sb.stroke_jobs[k].draw] = k;
+    for (uint32_t i = 0; i < count; i++) {
+        const StrokeJob &j = p.sb.stroke_jobs[job_of[i]];
+        // a job whose stroke produced nothing has an empty slice
+        if ((r = put(i, hv.data() + j.verb_off, j.verb_cap, hp.data() + 2 * (size_t)j.pt_off, j.pt_cap))) return r;
+    }
     return RGPU_OK;
 }
 

@@ -146,6 +146,22 @@ bool hairline_source_view(const rgpu_tree_view &t, uint32_t pi, float res_scale,
     return !out.verbs.empty();
 }
 
+std::shared_ptr<PathData> Tree::cached_stroke_outline(uint32_t pi, float rs, bool *found) {
+    uint32_t bits;
+    std::memcpy(&bits, &rs, 4);
+    std::lock_guard<std::mutex> g(cache_mu);
+    auto it = stroke_cache.find(std::make_pair(pi, bits));
+    *found = it != stroke_cache.end();
+    return *found ? it->second : nullptr;
+}
+
+void Tree::store_stroke_outline(uint32_t pi, float rs, std::shared_ptr<PathData> out) {
+    uint32_t bits;
+    std::memcpy(&bits, &rs, 4);
+    std::lock_guard<std::mutex> g(cache_mu);
+    stroke_cache[std::make_pair(pi, bits)] = std::move(out);
+}
+
 std::shared_ptr<PathData> Tree::stroke_outline(uint32_t pi, float rs) {
     uint32_t bits;
     std::memcpy(&bits, &rs, 4);

@@ -63,6 +63,11 @@ struct Tree {
     // Stroke outline of path `pi` (dashing applied) at resolution scale `rs`;
     // null when the stroke produces nothing.
     std::shared_ptr<PathData> stroke_outline(uint32_t pi, float rs);
+    // The cached outline without computing one: *found tells a cached "no
+    // outline" (nullptr) from a miss.  store_* fills the cache (outlines the
+    // device built).
+    std::shared_ptr<PathData> cached_stroke_outline(uint32_t pi, float rs, bool *found);
+    void store_stroke_outline(uint32_t pi, float rs, std::shared_ptr<PathData> out);
 };
 
 // Stroke outline for a path of any tree view (used by the oracle too).

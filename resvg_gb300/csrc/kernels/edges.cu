@@ -24,11 +24,15 @@ using dev::Pt;
 
 __device__ __forceinline__ bool nearly_zero(float v) { return fabsf(v) <= (1.0f / 4096.0f); }
 
-__global__ void k_draw_setup(DrawRec *draws, uint32_t ndraws, const uint8_t *verbs, const float *pts, Pt *tpts,
-                             SegRec *segs) {
+__global__ void k_draw_setup(DrawRec *draws, uint32_t ndraws, const uint8_t *scene_verbs, const float *scene_pts,
+                             const uint8_t *stroke_verbs, const float *stroke_pts, Pt *tpts, SegRec *segs) {
     uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
     if (d >= ndraws) return;
     DrawRec dr = draws[d];
+    // a stroke outline built on the device lives in the stroke arrays
+    const bool stroked = (dr.flags & DRAW_STROKED) != 0;
+    const uint8_t *verbs = stroked ? stroke_verbs : scene_verbs;
+    const float *pts = stroked ? stroke_pts : scene_pts;
     dr.valid = 0;
     dr.edge_base = 0;
     dr.edge_count = 0;
@@ -294,10 +298,12 @@ inline uint32_t blocks_for(uint64_t n, uint32_t t) { return (uint32_t)((n + t - 
 }  // namespace
 
 // ---------------------------------------------------------------- host launchers
-cudaError_t launch_draw_setup(DrawRec *draws, uint32_t ndraws, const uint8_t *verbs, const float *pts, void *tpts,
-                              SegRec *segs, cudaStream_t s) {
+cudaError_t launch_draw_setup(DrawRec *draws, uint32_t ndraws, const uint8_t *verbs, const float *pts,
+                              const uint8_t *stroke_verbs, const float *stroke_pts, void *tpts, SegRec *segs,
+                              cudaStream_t s) {
     if (!ndraws) return cudaSuccess;
-    k_draw_setup<<<blocks_for(ndraws, 128), 128, 0, s>>>(draws, ndraws, verbs, pts, (Pt *)tpts, segs);
+    k_draw_setup<<<blocks_for(ndraws, 128), 128, 0, s>>>(draws, ndraws, verbs, pts, stroke_verbs, stroke_pts,
+                                                         (Pt *)tpts, segs);
     return cudaGetLastError();
 }
 cudaError_t launch_edges(bool emit, const SegRec *segs, uint32_t nsegs, const DrawRec *draws, const void *tpts,

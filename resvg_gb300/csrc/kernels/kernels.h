@@ -8,9 +8,24 @@
 
 namespace rgpu {
 
+// stroke.cu: device-side stroking (one thread per stroked path) and the
+// per-draw segment / point bases that follow from the outlines' sizes
+size_t stroke_seg_bytes();
+cudaError_t stroke_warmup(cudaStream_t s);
+cudaError_t launch_stroke(const StrokeJob *jobs, uint32_t njobs, const uint8_t *src_verbs, const float *src_pts,
+                          uint8_t *out_verbs, float *out_pts, uint8_t *scr_verbs, float *scr_pts, void *segs,
+                          DrawRec *draws, uint32_t *status, cudaStream_t s);
+cudaError_t launch_stroke_gather(const StrokeMove *moves, uint32_t n, const uint8_t *src_verbs, const float *src_pts,
+                                 uint8_t *dst_verbs, float *dst_pts, DrawRec *draws, cudaStream_t s);
+cudaError_t launch_draw_sizes(const DrawRec *draws, uint32_t ndraws, uint32_t *seg_sizes, uint32_t *tpt_sizes,
+                              cudaStream_t s);
+cudaError_t launch_draw_bases(DrawRec *draws, uint32_t ndraws, const uint32_t *seg_base, const uint32_t *tpt_base,
+                              cudaStream_t s);
+
 // edges.cu
-cudaError_t launch_draw_setup(DrawRec *draws, uint32_t ndraws, const uint8_t *verbs, const float *pts, void *tpts,
-                              SegRec *segs, cudaStream_t s);
+cudaError_t launch_draw_setup(DrawRec *draws, uint32_t ndraws, const uint8_t *verbs, const float *pts,
+                              const uint8_t *stroke_verbs, const float *stroke_pts, void *tpts, SegRec *segs,
+                              cudaStream_t s);
 cudaError_t launch_edges(bool emit, const SegRec *segs, uint32_t nsegs, const DrawRec *draws, const void *tpts,
                          uint32_t *counts, const uint32_t *offsets, EdgeRec *edges, uint32_t *edge_draw,
                          uint32_t edge_cap, cudaStream_t s);

@@ -232,6 +232,23 @@ pub struct rgpu_stats {
     pub h2d_bytes: u64,
     pub d2h_bytes: u64,
     pub raster_ms: f32,
+    pub stroke_ms: f32,
+    pub stroke_jobs: u64,
+}
+
+/// One path for `rgpu_stroke_paths` (tiny-skia-path's `Path::stroke`).
+#[repr(C)]
+#[derive(Clone, Copy, Debug, Default)]
+pub struct rgpu_stroke_desc {
+    pub verb_off: u32,
+    pub verb_cnt: u32,
+    pub pt_off: u32,
+    pub pt_cnt: u32,
+    pub width: f32,
+    pub miter_limit: f32,
+    pub res_scale: f32,
+    pub cap: u32,
+    pub join: u32,
 }
 
 #[link(name = "resvg_gb300")]
@@ -340,6 +357,21 @@ extern "C" {
     pub fn rgpu_get_stats(s: *mut rgpu_stats) -> c_int;
     pub fn rgpu_set_wait_limit(rounds: u32) -> c_int;
     pub fn rgpu_trim() -> c_int;
+    pub fn rgpu_set_stroke_mode(on_device: c_int) -> c_int;
+    pub fn rgpu_stroke_paths(
+        descs: *const rgpu_stroke_desc,
+        count: u32,
+        verbs: *const u8,
+        verb_count: u32,
+        pts: *const f32,
+        pt_count: u32,
+        on_device: c_int,
+        out_verbs: *mut u8,
+        verb_cap: u32,
+        out_pts: *mut f32,
+        pt_cap: u32,
+        out_counts: *mut u32,
+    ) -> c_int;
 }
 
 // ---------------------------------------------------------------- safe layer

@@ -44,5 +44,7 @@ def test_repr_c_structs_match_the_header():
              "rgpu_node": A.Node, "rgpu_group": A.Group, "rgpu_clip": A.Clip, "rgpu_mask": A.Mask,
              "rgpu_primitive": A.Primitive, "rgpu_filter": A.Filter, "resvg_transform": A.ResvgTransform,
              "rgpu_tuning": A.Tuning, "rgpu_stats": A.Stats}
+    import resvg_gb300 as R
+    pairs["rgpu_stroke_desc"] = R.StrokeDesc
     for rust, cstruct in pairs.items():
         assert _rust_struct_fields(rust) == [f[0] for f in cstruct._fields_], rust
