@@ -200,16 +200,19 @@ int rgpu_trim(void);
 
 /* Where stroke outlines are built when a tree is rendered: 1 (the default) on
  * the device, one thread per stroked path; 0 on the host.  Both run the same
- * stroker (tiny-skia-path's Path::stroke, called from resvg's
- * crates/resvg/src/path.rs:113 through Pixmap::stroke_path) and give
- * identical outlines.  Dashing (Path::dash, path.rs:106-111) stays on the
- * host either way. */
+ * dasher and stroker (tiny-skia-path's Path::dash and Path::stroke, called
+ * from resvg's crates/resvg/src/path.rs:106-113 through Pixmap::stroke_path)
+ * and give identical outlines. */
 int rgpu_set_stroke_mode(int on_device);
 
 /* Strokes `count` paths and returns their outlines (the path to fill with the
- * non-zero rule), as tiny-skia-path's Path::stroke(stroke, res_scale) does.
- * Path i is verbs[verb_off, verb_off + verb_cnt) with points
- * pts[2 * pt_off, 2 * (pt_off + pt_cnt)).  The outlines are written one after
+ * non-zero rule), as resvg's stroke_path does through tiny-skia-path:
+ * Path::dash(dash, res_scale) when the path is dashed (an invalid dash array
+ * strokes the undashed path, a dashing that leaves nothing gives no outline),
+ * then Path::stroke(stroke, res_scale).  Path i is verbs[verb_off, verb_off +
+ * verb_cnt) with points pts[2 * pt_off, 2 * (pt_off + pt_cnt)), dashed by
+ * dashes[dash_off, dash_off + dash_cnt) from dash_phase (dash_cnt 0: not
+ * dashed).  The outlines are written one after
  * another to out_verbs / out_pts (x, y pairs), out_counts[2i] and
  * out_counts[2i + 1] receiving path i's verb and point counts (0 when the
  * stroke produces nothing).  on_device selects the device stroker (1) or the
@@ -220,10 +223,12 @@ typedef struct rgpu_stroke_desc {
     float width, miter_limit, res_scale;
     uint32_t cap;   /* rgpu_cap */
     uint32_t join;  /* rgpu_join */
+    uint32_t dash_off, dash_cnt;
+    float dash_phase;
 } rgpu_stroke_desc;
 int rgpu_stroke_paths(const rgpu_stroke_desc *descs, uint32_t count, const uint8_t *verbs, uint32_t verb_count,
-                      const float *pts, uint32_t pt_count, int on_device, uint8_t *out_verbs, uint32_t verb_cap,
-                      float *out_pts, uint32_t pt_cap, uint32_t *out_counts);
+                      const float *pts, uint32_t pt_count, const float *dashes, uint32_t dash_count, int on_device,
+                      uint8_t *out_verbs, uint32_t verb_cap, float *out_pts, uint32_t pt_cap, uint32_t *out_counts);
 
 /* Per-call statistics of the last render on this thread (for benchmarking). */
 typedef struct rgpu_stats {

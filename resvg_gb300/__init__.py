@@ -320,41 +320,49 @@ def set_stroke_mode(on_device: bool) -> None:
 class StrokeDesc(C.Structure):
     _fields_ = [("verb_off", C.c_uint32), ("verb_cnt", C.c_uint32), ("pt_off", C.c_uint32), ("pt_cnt", C.c_uint32),
                 ("width", C.c_float), ("miter_limit", C.c_float), ("res_scale", C.c_float),
-                ("cap", C.c_uint32), ("join", C.c_uint32)]
+                ("cap", C.c_uint32), ("join", C.c_uint32), ("dash_off", C.c_uint32), ("dash_cnt", C.c_uint32),
+                ("dash_phase", C.c_float)]
 
 
 def stroke_paths(paths, on_device: bool = True):
-    """tiny-skia's Path::stroke for many paths at once (rgpu_stroke_paths).
-    `paths`: (verbs, points (n, 2), width, miter_limit, cap, join, res_scale)
-    tuples.  Returns one (verbs uint8, points float32 (m, 2)) outline per path
-    (empty arrays when the stroke produces nothing)."""
+    """tiny-skia's Path::dash + Path::stroke for many paths at once
+    (rgpu_stroke_paths).  `paths`: (verbs, points (n, 2), width, miter_limit,
+    cap, join, res_scale[, dashes, dash_phase]) tuples.  Returns one (verbs
+    uint8, points float32 (m, 2)) outline per path (empty arrays when the
+    stroke produces nothing)."""
     L = lib()
     L.rgpu_stroke_paths.restype = C.c_int
     P = C.c_void_p
-    L.rgpu_stroke_paths.argtypes = [C.POINTER(StrokeDesc), C.c_uint32, P, C.c_uint32, P, C.c_uint32, C.c_int,
-                                    P, C.c_uint32, P, C.c_uint32, P]
+    L.rgpu_stroke_paths.argtypes = [C.POINTER(StrokeDesc), C.c_uint32, P, C.c_uint32, P, C.c_uint32, P, C.c_uint32,
+                                    C.c_int, P, C.c_uint32, P, C.c_uint32, P]
     n = len(paths)
     descs = (StrokeDesc * max(n, 1))()
-    vs, ps = [], []
-    vo = po = 0
-    for i, (v, pt, width, miter, cap, join, rs) in enumerate(paths):
+    vs, ps, ds = [], [], []
+    vo = po = do = 0
+    for i, path in enumerate(paths):
+        v, pt, width, miter, cap, join, rs = path[:7]
+        dash = np.asarray(path[7] if len(path) > 7 and path[7] is not None else [], np.float32).reshape(-1)
+        phase = float(path[8]) if len(path) > 8 else 0.0
         v = np.ascontiguousarray(np.asarray(v, dtype=np.uint8))
         pt = np.ascontiguousarray(np.asarray(pt, dtype=np.float32).reshape(-1, 2))
-        descs[i] = StrokeDesc(vo, len(v), po, len(pt), width, miter, rs, cap, join)
+        descs[i] = StrokeDesc(vo, len(v), po, len(pt), width, miter, rs, cap, join, do, len(dash), phase)
         vs.append(v)
         ps.append(pt)
+        ds.append(dash)
         vo += len(v)
         po += len(pt)
+        do += len(dash)
     verbs = np.concatenate(vs) if vs else np.zeros(1, np.uint8)
     pts = np.concatenate(ps) if ps else np.zeros((1, 2), np.float32)
+    dashes = np.concatenate(ds + [np.zeros(1, np.float32)]).astype(np.float32)
     vcap, pcap = 64 * max(vo, 1) + 256 * n + 64, 64 * max(po, 1) + 256 * n + 64
     while True:
         ov = np.zeros(vcap, np.uint8)
         op = np.zeros((pcap, 2), np.float32)
         counts = np.zeros(2 * max(n, 1), np.uint32)
         r = L.rgpu_stroke_paths(descs, n, verbs.ctypes.data, len(verbs), pts.ctypes.data, len(pts),
-                                1 if on_device else 0, ov.ctypes.data, vcap, op.ctypes.data, pcap,
-                                counts.ctypes.data)
+                                dashes.ctypes.data, len(dashes), 1 if on_device else 0, ov.ctypes.data, vcap,
+                                op.ctypes.data, pcap, counts.ctypes.data)
         if r == 5:  # RGPU_ERR_CAPACITY: larger output arrays
             vcap, pcap = 4 * vcap, 4 * pcap
             continue

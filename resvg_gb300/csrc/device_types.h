@@ -97,11 +97,12 @@ enum : uint32_t {
     DRAW_STROKED = 4,  // the geometry is a stroke outline built on the device (stroke arrays)
 };
 
-// One path stroked on the device (tiny-skia's Path::stroke, one thread per
-// job): the source path in the scene's geometry arrays, the stroke, and the
-// slice of the stroke arrays its outline is written to.  The thread writes the
-// outline's verb and point counts into draws[draw]; an outline that does not
-// fit its slice sets its status word instead and draws nothing.
+// One path stroked on the device (tiny-skia's Path::dash and Path::stroke,
+// one thread per job): the source path in the scene's geometry arrays, the
+// dash array (dash_cnt 0: not dashed) and the stroke, and the slices of the
+// stroke arrays the job works in.  The thread writes the outline's verb and
+// point counts into draws[draw]; a job that outgrows a slice sets its status
+// word instead and draws nothing.
 struct StrokeJob {
     uint32_t src_verb_off, src_verb_cnt, src_pt_off, src_pt_cnt;
     float width, miter_limit, res_scale;
@@ -109,10 +110,14 @@ struct StrokeJob {
     uint32_t draw;         // the DrawRec that fills the outline
     uint32_t verb_off, verb_cap;  // outline slice: verbs
     uint32_t pt_off, pt_cap;      // outline slice: points (x, y pairs)
-    uint32_t seg_off;      // segment scratch: 2 * src_verb_cnt + 1 entries
-    uint32_t _pad[2];
+    uint32_t seg_off, seg_cap;    // segment scratch of the path being stroked
+    uint32_t dash_off, dash_cnt;  // dash intervals in the dash array
+    float dash_phase;
+    uint32_t dverb_off, dverb_cap, dpt_off, dpt_cap;  // the dashed path (scratch)
+    uint32_t mseg_off, mseg_cap, mpt_off, mpt_cap;    // one measured contour (scratch)
+    uint32_t _pad[6];
 };
-static_assert(sizeof(StrokeJob) == 64, "StrokeJob layout");
+static_assert(sizeof(StrokeJob) == 128, "StrokeJob layout");
 
 // One outline moved from its sizing slice to its exact slice.
 struct StrokeMove {

@@ -475,26 +475,17 @@ struct Flattener {
             // path, whose outline the draw fills; the outline then goes to the
             // tree's cache for later flattens
             if (!(p.stroke_width > 0)) return;
-            uint32_t sv = tree_verb_base + p.verb_offset, sp = tree_pt_base + p.point_offset;
-            uint32_t nv = p.verb_count, np = p.point_count;
-            if (p.dash_count) {
-                // dash.rs on the host; the dashed path is the stroker's source
-                PathData dashed;
-                if (dash_path(t.verbs + p.verb_offset, p.verb_count, t.points + 2 * (size_t)p.point_offset,
-                              p.point_count, t.dashes + p.dash_offset, p.dash_count, p.dash_phase, rs, dashed)) {
-                    if (dashed.empty()) return;
-                    sv = (uint32_t)sb.verbs.size();
-                    sp = (uint32_t)(sb.pts.size() / 2);
-                    nv = (uint32_t)dashed.verbs.size();
-                    np = (uint32_t)(dashed.pts.size() / 2);
-                    sb.verbs.insert(sb.verbs.end(), dashed.verbs.begin(), dashed.verbs.end());
-                    sb.pts.insert(sb.pts.end(), dashed.pts.begin(), dashed.pts.end());
-                }
-            }
             StrokeJob j;
             std::memset(&j, 0, sizeof(j));
-            j.src_verb_off = sv; j.src_verb_cnt = nv;
-            j.src_pt_off = sp; j.src_pt_cnt = np;
+            j.src_verb_off = tree_verb_base + p.verb_offset; j.src_verb_cnt = p.verb_count;
+            j.src_pt_off = tree_pt_base + p.point_offset; j.src_pt_cnt = p.point_count;
+            if (p.dash_count) {
+                // dash.rs on the device too: the job dashes, then strokes the dashed path
+                j.dash_off = (uint32_t)sb.dashes.size();
+                j.dash_cnt = p.dash_count;
+                j.dash_phase = p.dash_phase;
+                sb.dashes.insert(sb.dashes.end(), t.dashes + p.dash_offset, t.dashes + p.dash_offset + p.dash_count);
+            }
             j.width = p.stroke_width;
             j.miter_limit = p.miter_limit;
             j.res_scale = rs;
@@ -775,14 +766,15 @@ void SceneBuild::merge(std::vector<SceneBuild> &parts, unsigned threads) {
     // one after another into one build.  Arrays are sized first, then each part
     // is copied into its ranges with the index fix-ups, parts in parallel.
     struct Off {
-        size_t verbs, pts, draws, paints, grads, layers, cmds, streams, surfaces, jobs, fe, patterns, hairs, hspans, strokes;
+        size_t verbs, pts, draws, paints, grads, layers, cmds, streams, surfaces, jobs, fe, patterns, hairs, hspans, strokes,
+            dashes;
         uint64_t nsegs, ntpts;
     };
     const size_t n = parts.size();
     std::vector<Off> off(n + 1);
     Off cur{verbs.size(), pts.size(), draws.size(), paints.size(), grads.size(), layers.size(), cmds.size(),
             streams.size(), surfaces.size(), jobs.size(), fe_images.size(), patterns.size(), hairs.size(),
-            hair_spans.size(), stroke_jobs.size(), nsegs, ntpts};
+            hair_spans.size(), stroke_jobs.size(), dashes.size(), nsegs, ntpts};
     for (size_t k = 0; k < n; k++) {
         const SceneBuild &o = parts[k];
         off[k] = cur;
@@ -791,6 +783,7 @@ void SceneBuild::merge(std::vector<SceneBuild> &parts, unsigned threads) {
         cur.cmds += o.cmds.size(); cur.streams += o.streams.size(); cur.surfaces += o.surfaces.size();
         cur.jobs += o.jobs.size(); cur.fe += o.fe_images.size(); cur.patterns += o.patterns.size();
         cur.hairs += o.hairs.size(); cur.hspans += o.hair_spans.size(); cur.strokes += o.stroke_jobs.size();
+        cur.dashes += o.dashes.size();
         cur.nsegs += o.nsegs; cur.ntpts += o.ntpts;
         max_level = std::max(max_level, o.max_level);
     }
@@ -800,6 +793,7 @@ void SceneBuild::merge(std::vector<SceneBuild> &parts, unsigned threads) {
     surfaces.resize(cur.surfaces); jobs.resize(cur.jobs); fe_images.resize(cur.fe); patterns.resize(cur.patterns);
     hairs.resize(cur.hairs); hair_spans.resize(cur.hspans); stroke_jobs.resize(cur.strokes);
     stroke_keys.resize(cur.strokes);
+    dashes.resize(cur.dashes);
     nsegs = cur.nsegs;
     ntpts = cur.ntpts;
     auto copy_part = [&](size_t k) {
@@ -832,8 +826,10 @@ void SceneBuild::merge(std::vector<SceneBuild> &parts, unsigned threads) {
             j.src_verb_off += V;
             j.src_pt_off += P;
             j.draw += D;
+            if (j.dash_cnt) j.dash_off += (uint32_t)b.dashes;
             stroke_jobs[b.strokes + i] = j;
         }
+        std::copy(o.dashes.begin(), o.dashes.end(), dashes.begin() + b.dashes);
         std::copy(o.stroke_keys.begin(), o.stroke_keys.end(), stroke_keys.begin() + b.strokes);
         for (size_t i = 0; i < o.layers.size(); i++) {
             LayerRec l = o.layers[i];

@@ -96,6 +96,7 @@ struct SceneBuild {
     std::vector<float> pts;
     std::vector<StrokeJob> stroke_jobs;  // paths stroked on the device (their draws carry DRAW_STROKED)
     std::vector<StrokeKey> stroke_keys;  // per job: the tree outline cache entry it fills
+    std::vector<float> dashes;           // dash intervals of the stroke jobs
     uint64_t nsegs = 0, ntpts = 0;
     uint32_t max_level = 0;
     std::string error;

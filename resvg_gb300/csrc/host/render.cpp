@@ -118,13 +118,15 @@ struct Buffers {
     // device stroking: jobs, outlines, builder scratch, segment scratch,
     // per-job status, per-draw sizes and bases
     DevBuf sjobs, sverbs, spts, sscr_verbs, sscr_pts, ssegs, sstatus, dsizes, dbases;
+    DevBuf sdash, sdverbs, sdpts, smsegs, smpts;  // dash intervals, dashed paths, measured contours
     std::vector<DevBuf> surf, img;   // internal surfaces (filter content/results) and filter images
     DevBuf plane;                    // f64 plane of the IIR blur
     void release() {
         DevBuf *all[] = {&verbs, &pts, &draws, &paints, &grads, &layers, &cmds, &streams, &items, &tpts, &segs,
                          &seg_counts, &seg_offsets, &scan_scratch, &totals, &edges, &edge_draw, &bin_counts,
                          &bin_offsets, &bins, &stack, &span_ovf, &run_ovf, &err, &counter, &fill_cmds, &plane, &hairs, &hair_spans,
-                         &sjobs, &sverbs, &spts, &sscr_verbs, &sscr_pts, &ssegs, &sstatus, &dsizes, &dbases};
+                         &sjobs, &sverbs, &spts, &sscr_verbs, &sscr_pts, &ssegs, &sstatus, &dsizes, &dbases,
+                         &sdash, &sdverbs, &sdpts, &smsegs, &smpts};
         for (DevBuf *b : all) b->release();
         for (auto &b : surf) b.release();
         for (auto &b : img) b.release();
@@ -173,7 +175,8 @@ struct Plan {
     // device stroking: per job the outline slice (verbs, points); the layout's
     // totals in the stroke arrays and the segment scratch
     std::vector<uint32_t> svcap, spcap;
-    uint64_t sverbs = 0, spts = 0, ssegs = 0;
+    std::vector<uint32_t> sscale;  // per job: growth of its slices (1, 4, 16, ...)
+    uint64_t sverbs = 0, spts = 0, ssegs = 0, sdverbs = 0, sdpts = 0, smsegs = 0, smpts = 0;
     // the outlines, their DrawRec counts and the draws' bases are in device
     // memory since the last upload: renders (and graph replays) reuse them
     bool strokes_ready = false;
@@ -299,22 +302,55 @@ uint32_t pick_bh(int32_t w, uint32_t draws, uint32_t px, const Tuning &tu) {
 }
 
 // Host-side work decomposition of a flattened submission.
-// Places each stroke job's outline slice (p.svcap / p.spcap) and segment
-// scratch in the stroke arrays.
+// First slice sizes of a job at growth `sc`: outlines measured on the
+// benchmark scenes average 15 verbs and 12 points per source verb and point
+// (at most 29 and 24); a dashed path is sized from the source too, and its
+// outline from the dashed path.  A job that outgrows a slice is given four
+// times the room by the sizing run.
+void first_slices(const StrokeJob &j, uint32_t sc, uint32_t *vcap, uint32_t *pcap) {
+    uint64_t v = 32ull * j.src_verb_cnt + 64, q = 32ull * j.src_pt_cnt + 128;
+    if (j.dash_cnt) {
+        v = 16ull * (64ull * j.src_verb_cnt + 256);
+        q = 16ull * (64ull * j.src_pt_cnt + 512);
+    }
+    *vcap = (uint32_t)std::min<uint64_t>(v * sc, 0x10000000ull);
+    *pcap = (uint32_t)std::min<uint64_t>(q * sc, 0x10000000ull);
+}
+
+// Places each stroke job's slices (outline: p.svcap / p.spcap; the rest from
+// the job's growth p.sscale) in the stroke arrays.
 int layout_strokes(Plan &p) {
-    uint64_t v = 0, q = 0, g = 0;
+    uint64_t v = 0, q = 0, g = 0, dv = 0, dq = 0, ms = 0, mq = 0;
     auto &jobs = p.sb.stroke_jobs;
     for (size_t i = 0; i < jobs.size(); i++) {
         StrokeJob &j = jobs[i];
+        const uint64_t sc = p.sscale[i];
         j.verb_off = (uint32_t)v;
         j.verb_cap = p.svcap[i];
         j.pt_off = (uint32_t)q;
         j.pt_cap = p.spcap[i];
+        uint64_t seg_cap = 2ull * j.src_verb_cnt + 1;
+        j.dverb_off = (uint32_t)dv; j.dpt_off = (uint32_t)dq;
+        j.mseg_off = (uint32_t)ms; j.mpt_off = (uint32_t)mq;
+        j.dverb_cap = j.dpt_cap = j.mseg_cap = j.mpt_cap = 0;
+        if (j.dash_cnt) {
+            j.dverb_cap = (uint32_t)std::min<uint64_t>((64ull * j.src_verb_cnt + 256) * sc, 0x10000000ull);
+            j.dpt_cap = (uint32_t)std::min<uint64_t>((64ull * j.src_pt_cnt + 512) * sc, 0x10000000ull);
+            j.mseg_cap = (uint32_t)std::min<uint64_t>((64ull * j.src_verb_cnt + 64) * sc, 0x10000000ull);
+            j.mpt_cap = j.src_pt_cnt + 2;  // a contour's points and its closing point
+            seg_cap = std::max<uint64_t>(seg_cap, 2ull * j.dverb_cap + 1);
+        }
         j.seg_off = (uint32_t)g;
+        j.seg_cap = (uint32_t)seg_cap;
         v += j.verb_cap;
         q += j.pt_cap;
-        g += 2ull * j.src_verb_cnt + 1;
-        if (v > 0x7FFFFFFFull || q > 0x3FFFFFFFull || g > 0x7FFFFFFFull) {
+        g += seg_cap;
+        dv += j.dverb_cap;
+        dq += j.dpt_cap;
+        ms += j.mseg_cap;
+        mq += j.mpt_cap;
+        if (v > 0x7FFFFFFFull || q > 0x3FFFFFFFull || g > 0x7FFFFFFFull || dv > 0x7FFFFFFFull ||
+            dq > 0x3FFFFFFFull || ms > 0x3FFFFFFFull || mq > 0x3FFFFFFFull) {
             set_error("stroke outlines exceed the stroke arrays' index range");
             return RGPU_ERR_CAPACITY;
         }
@@ -322,6 +358,10 @@ int layout_strokes(Plan &p) {
     p.sverbs = v;
     p.spts = q;
     p.ssegs = g;
+    p.sdverbs = dv;
+    p.sdpts = dq;
+    p.smsegs = ms;
+    p.smpts = mq;
     return RGPU_OK;
 }
 
@@ -358,10 +398,8 @@ int plan_scene(Context &c, Plan &p) {
         // a larger outline is given a larger slice by the sizing run
         p.svcap.resize(sb.stroke_jobs.size());
         p.spcap.resize(sb.stroke_jobs.size());
-        for (size_t i = 0; i < sb.stroke_jobs.size(); i++) {
-            p.svcap[i] = 32u * sb.stroke_jobs[i].src_verb_cnt + 64u;
-            p.spcap[i] = 32u * sb.stroke_jobs[i].src_pt_cnt + 128u;
-        }
+        p.sscale.assign(sb.stroke_jobs.size(), 1u);
+        for (size_t i = 0; i < sb.stroke_jobs.size(); i++) first_slices(sb.stroke_jobs[i], 1, &p.svcap[i], &p.spcap[i]);
         p.sized = false;
     }
     if (!sb.stroke_jobs.empty()) {
@@ -431,6 +469,11 @@ int ensure_stroke_buffers(Buffers &b, Plan &p) {
     CK(b.sscr_verbs.ensure(std::max<uint64_t>(2 * p.sverbs, 1)));
     CK(b.sscr_pts.ensure(std::max<uint64_t>(2 * p.spts, 1) * 8));
     CK(b.ssegs.ensure(std::max<uint64_t>(p.ssegs, 1) * stroke_seg_bytes()));
+    CK(b.sdash.ensure(std::max<size_t>(p.sb.dashes.size(), 1) * 4));
+    CK(b.sdverbs.ensure(std::max<uint64_t>(p.sdverbs, 1)));
+    CK(b.sdpts.ensure(std::max<uint64_t>(p.sdpts, 1) * 8));
+    CK(b.smsegs.ensure(std::max<uint64_t>(p.smsegs, 1) * stroke_mseg_bytes()));
+    CK(b.smpts.ensure(std::max<uint64_t>(p.smpts, 1) * 8));
     CK(b.sstatus.ensure(p.sb.stroke_jobs.size() * 8));
     CK(b.dsizes.ensure((nd + 1) * 8));
     CK(b.dbases.ensure((nd + 1) * 8));
@@ -454,9 +497,22 @@ int stroke_pass(Buffers &b, Plan &p, cudaStream_t s) {
     const uint32_t nj = (uint32_t)sb.stroke_jobs.size(), nd = (uint32_t)sb.draws.size();
     uint32_t *totals = b.totals.as<uint32_t>();
     uint32_t *sz = b.dsizes.as<uint32_t>(), *bs = b.dbases.as<uint32_t>();
-    CK(launch_stroke(b.sjobs.as<StrokeJob>(), nj, b.verbs.as<uint8_t>(), b.pts.as<float>(), b.sverbs.as<uint8_t>(),
-                     b.spts.as<float>(), b.sscr_verbs.as<uint8_t>(), b.sscr_pts.as<float>(), b.ssegs.p,
-                     b.draws.as<DrawRec>(), b.sstatus.as<uint32_t>(), s));
+    StrokeBuffers sbuf;
+    sbuf.src_verbs = b.verbs.as<uint8_t>();
+    sbuf.src_pts = b.pts.as<float>();
+    sbuf.dashes = b.sdash.as<float>();
+    sbuf.out_verbs = b.sverbs.as<uint8_t>();
+    sbuf.out_pts = b.spts.as<float>();
+    sbuf.scr_verbs = b.sscr_verbs.as<uint8_t>();
+    sbuf.scr_pts = b.sscr_pts.as<float>();
+    sbuf.segs = b.ssegs.p;
+    sbuf.dash_verbs = b.sdverbs.as<uint8_t>();
+    sbuf.dash_pts = b.sdpts.as<float>();
+    sbuf.msegs = b.smsegs.p;
+    sbuf.mpts = b.smpts.as<float>();
+    sbuf.draws = b.draws.as<DrawRec>();
+    sbuf.status = b.sstatus.as<uint32_t>();
+    CK(launch_stroke(b.sjobs.as<StrokeJob>(), nj, sbuf, s));
     CK(launch_draw_sizes(b.draws.as<DrawRec>(), nd, sz, sz + (nd + 1), s));
     CK(launch_exclusive_scan(sz, bs, nd, b.scan_scratch.as<uint32_t>(), totals + 2, s));
     CK(launch_exclusive_scan(sz + (nd + 1), bs + (nd + 1), nd, b.scan_scratch.as<uint32_t>(), totals + 3, s));
@@ -530,8 +586,8 @@ int run_strokes(Buffers &b, Plan &p, cudaStream_t s) {
         for (size_t j = 0; j < nj; j++)
             if (st[2 * j] & 0x80000000u) {
                 grow = true;
-                p.svcap[j] = (uint32_t)std::min<uint64_t>(4ull * p.svcap[j], 0x10000000ull);
-                p.spcap[j] = (uint32_t)std::min<uint64_t>(4ull * p.spcap[j], 0x10000000ull);
+                p.sscale[j] = (uint32_t)std::min<uint64_t>(4ull * p.sscale[j], 1u << 24);
+                first_slices(sb.stroke_jobs[j], p.sscale[j], &p.svcap[j], &p.spcap[j]);
             }
         if (!grow) break;
         if (round >= 6) {
@@ -609,7 +665,8 @@ int upload_plan(Context &c, Buffers &b, Plan &p, cudaStream_t s, HostBuf *stagin
                    rup(sb.layers.size() * sizeof(LayerRec)) + rup(sb.cmds.size() * sizeof(Cmd)) +
                    rup(sb.streams.size() * sizeof(StreamRec)) + rup(p.items.size() * sizeof(WorkItem)) +
                    rup(sb.hairs.size() * sizeof(HairRec)) + rup(sb.hair_spans.size() * sizeof(HairSpan)) +
-                   rup(sb.fill_cmds.size() * 4) + rup(sb.stroke_jobs.size() * sizeof(StrokeJob)) + 4096;
+                   rup(sb.fill_cmds.size() * 4) + rup(sb.stroke_jobs.size() * sizeof(StrokeJob)) +
+                   rup(sb.dashes.size() * 4) + 4096;
     CK(staging.ensure(stage));
     size_t off = 0;
     int r;
@@ -626,6 +683,7 @@ int upload_plan(Context &c, Buffers &b, Plan &p, cudaStream_t s, HostBuf *stagin
     if ((r = upload(staging, b.hair_spans, sb.hair_spans, off, s))) return r;
     if ((r = upload(staging, b.fill_cmds, sb.fill_cmds, off, s))) return r;
     if ((r = upload(staging, b.sjobs, sb.stroke_jobs, off, s))) return r;
+    if ((r = upload(staging, b.sdash, sb.dashes, off, s))) return r;
     if ((r = ensure_stroke_buffers(b, p))) return r;
     p.strokes_ready = false;  // the draws just uploaded carry no outline counts
     // fixed-size work buffers (with device-stroked paths the segment counts
@@ -1365,8 +1423,8 @@ int rgpu_set_stroke_mode(int on_device) {
 }
 
 int rgpu_stroke_paths(const rgpu_stroke_desc *descs, uint32_t count, const uint8_t *verbs, uint32_t verb_count,
-                      const float *pts, uint32_t pt_count, int on_device, uint8_t *out_verbs, uint32_t verb_cap,
-                      float *out_pts, uint32_t pt_cap, uint32_t *out_counts) {
+                      const float *pts, uint32_t pt_count, const float *dashes, uint32_t dash_count, int on_device,
+                      uint8_t *out_verbs, uint32_t verb_cap, float *out_pts, uint32_t pt_cap, uint32_t *out_counts) {
     g_last_error.clear();
     if ((count && (!descs || !verbs || !pts || !out_counts)) || (verb_cap && !out_verbs) || (pt_cap && !out_pts)) {
         set_error("invalid arguments");
@@ -1374,8 +1432,9 @@ int rgpu_stroke_paths(const rgpu_stroke_desc *descs, uint32_t count, const uint8
     }
     for (uint32_t i = 0; i < count; i++) {
         const rgpu_stroke_desc &d = descs[i];
-        if ((uint64_t)d.verb_off + d.verb_cnt > verb_count || (uint64_t)d.pt_off + d.pt_cnt > pt_count) {
-            set_error("path %u lies outside the verb / point arrays", i);
+        if ((uint64_t)d.verb_off + d.verb_cnt > verb_count || (uint64_t)d.pt_off + d.pt_cnt > pt_count ||
+            (d.dash_cnt && (!dashes || (uint64_t)d.dash_off + d.dash_cnt > dash_count))) {
+            set_error("path %u lies outside the verb / point / dash arrays", i);
             return RGPU_ERR_INVALID_ARG;
         }
     }
@@ -1401,9 +1460,19 @@ int rgpu_stroke_paths(const rgpu_stroke_desc *descs, uint32_t count, const uint8
             st.miter_limit = d.miter_limit;
             st.cap = d.cap;
             st.join = d.join;
-            PathData o;
-            if (!stroke_path(verbs + d.verb_off, d.verb_cnt, pts + 2 * (size_t)d.pt_off, d.pt_cnt, st, d.res_scale, o))
-                o = PathData();
+            PathData o, dashed;
+            const uint8_t *sv = verbs + d.verb_off;
+            const float *sp = pts + 2 * (size_t)d.pt_off;
+            size_t nv = d.verb_cnt, np = d.pt_cnt;
+            bool draw = true;
+            if (d.dash_cnt && dash_path(sv, nv, sp, np, dashes + d.dash_off, d.dash_cnt, d.dash_phase, d.res_scale, dashed)) {
+                draw = !dashed.empty();
+                sv = dashed.verbs.data();
+                sp = dashed.pts.data();
+                nv = dashed.verbs.size();
+                np = dashed.pts.size() / 2;
+            }
+            if (!draw || !stroke_path(sv, nv, sp, np, st, d.res_scale, o)) o = PathData();
             int r = put(i, o.verbs.data(), (uint32_t)o.verbs.size(), o.pts.data(), (uint32_t)(o.pts.size() / 2));
             if (r) return r;
         }
@@ -1432,6 +1501,12 @@ int rgpu_stroke_paths(const rgpu_stroke_desc *descs, uint32_t count, const uint8
         j.width = d.width; j.miter_limit = d.miter_limit; j.res_scale = d.res_scale;
         j.cap_join = (d.cap & 0xFFu) | (d.join & 0xFFu) << 8;
         j.draw = i;
+        if (d.dash_cnt) {
+            j.dash_off = (uint32_t)p.sb.dashes.size();
+            j.dash_cnt = d.dash_cnt;
+            j.dash_phase = d.dash_phase;
+            p.sb.dashes.insert(p.sb.dashes.end(), dashes + d.dash_off, dashes + d.dash_off + d.dash_cnt);
+        }
     }
     if ((r = plan_scene(c, p))) return r;
     CK(b.verbs.ensure(std::max<size_t>(p.sb.verbs.size(), 1)));
@@ -1445,6 +1520,8 @@ int rgpu_stroke_paths(const rgpu_stroke_desc *descs, uint32_t count, const uint8
     CK(cudaMemcpyAsync(b.pts.p, p.sb.pts.data(), p.sb.pts.size() * 4, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(b.draws.p, p.sb.draws.data(), count * sizeof(DrawRec), cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(b.sjobs.p, p.sb.stroke_jobs.data(), count * sizeof(StrokeJob), cudaMemcpyHostToDevice, s));
+    if (!p.sb.dashes.empty())
+        CK(cudaMemcpyAsync(b.sdash.p, p.sb.dashes.data(), p.sb.dashes.size() * 4, cudaMemcpyHostToDevice, s));
     if ((r = run_strokes(b, p, s))) return r;
     std::vector<uint8_t> hv(p.sverbs);
     std::vector<float> hp(2 * p.spts);

@@ -12,9 +12,25 @@ namespace rgpu {
 // per-draw segment / point bases that follow from the outlines' sizes
 size_t stroke_seg_bytes();
 cudaError_t stroke_warmup(cudaStream_t s);
-cudaError_t launch_stroke(const StrokeJob *jobs, uint32_t njobs, const uint8_t *src_verbs, const float *src_pts,
-                          uint8_t *out_verbs, float *out_pts, uint8_t *scr_verbs, float *scr_pts, void *segs,
-                          DrawRec *draws, uint32_t *status, cudaStream_t s);
+// the arrays a stroking pass reads and writes (slices per job in StrokeJob)
+struct StrokeBuffers {
+    const uint8_t *src_verbs;
+    const float *src_pts;
+    const float *dashes;
+    uint8_t *out_verbs;
+    float *out_pts;
+    uint8_t *scr_verbs;
+    float *scr_pts;
+    void *segs;
+    uint8_t *dash_verbs;
+    float *dash_pts;
+    void *msegs;
+    float *mpts;
+    DrawRec *draws;
+    uint32_t *status;
+};
+size_t stroke_mseg_bytes();
+cudaError_t launch_stroke(const StrokeJob *jobs, uint32_t njobs, const StrokeBuffers &b, cudaStream_t s);
 cudaError_t launch_stroke_gather(const StrokeMove *moves, uint32_t n, const uint8_t *src_verbs, const float *src_pts,
                                  uint8_t *dst_verbs, float *dst_pts, DrawRec *draws, cudaStream_t s);
 cudaError_t launch_draw_sizes(const DrawRec *draws, uint32_t ndraws, uint32_t *seg_sizes, uint32_t *tpt_sizes,

@@ -17,7 +17,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include "kernels.h"
-#include "../host/stroke_core.h"
+#include "../host/dash_core.h"
 
 namespace rgpu {
 namespace {
@@ -47,10 +47,32 @@ struct SliceTraits {
 };
 using DevStroker = sk::StrokerT<SliceTraits>;
 
-__global__ void __launch_bounds__(128) k_stroke(const StrokeJob *jobs, uint32_t njobs, const uint8_t *src_verbs,
-                                                 const float *src_pts, uint8_t *out_verbs, float *out_pts,
-                                                 uint8_t *scr_verbs, float *scr_pts, sk::Seg *segs, DrawRec *draws,
-                                                 uint32_t *status) {
+// Device-side arrays a stroke job works in (the job holds its slices).
+struct StrokeArrays {
+    const uint8_t *src_verbs;
+    const float *src_pts;
+    const float *dashes;
+    uint8_t *out_verbs;
+    float *out_pts;
+    uint8_t *scr_verbs;   // inner offset path + cusp circles: twice the outline slice
+    float *scr_pts;
+    sk::Seg *segs;
+    uint8_t *dash_verbs;  // the dashed path
+    float *dash_pts;
+    sk::MSeg *msegs;      // one measured contour
+    float *mpts;
+    DrawRec *draws;
+    uint32_t *status;
+};
+
+template <class T> __device__ __forceinline__ void bind_vec(SliceVec<T> &v, T *p, uint32_t cap, uint32_t *ovf) {
+    v.p = p;
+    v.cap = cap;
+    v.ovf = ovf;
+    v.n = 0;
+}
+
+__global__ void __launch_bounds__(128) k_stroke(const StrokeJob *jobs, uint32_t njobs, StrokeArrays a) {
     const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= njobs) return;
     const StrokeJob jb = jobs[j];
@@ -58,39 +80,60 @@ __global__ void __launch_bounds__(128) k_stroke(const StrokeJob *jobs, uint32_t 
     uint32_t nv = 0, np = 0;
     // slices of at least one entry: the builders' back() needs one
     if (jb.verb_cap > 0 && jb.pt_cap > 0) {
-        const long ns = sk::build_segments(src_verbs + jb.src_verb_off, jb.src_verb_cnt,
-                                           src_pts + 2 * (size_t)jb.src_pt_off, segs + jb.seg_off);
-        if (ns >= 0) {
-            DevStroker skr;
-            auto bind = [&](sk::BuilderT<SliceTraits> &b, uint8_t *v, float *p) {
-                b.verbs.p = v;
-                b.verbs.cap = jb.verb_cap;
-                b.verbs.ovf = &ovf;
-                b.pts.p = reinterpret_cast<sk::Pt *>(p);
-                b.pts.cap = jb.pt_cap;
-                b.pts.ovf = &ovf;
-            };
-            bind(skr.outer, out_verbs + jb.verb_off, out_pts + 2 * (size_t)jb.pt_off);
-            bind(skr.inner, scr_verbs + 2 * (size_t)jb.verb_off, scr_pts + 4 * (size_t)jb.pt_off);
-            bind(skr.cusper, scr_verbs + 2 * (size_t)jb.verb_off + jb.verb_cap,
-                 scr_pts + 4 * (size_t)jb.pt_off + 2 * (size_t)jb.pt_cap);
-            sk::StrokeParams sp;
-            sp.width = jb.width;
-            sp.miter_limit = jb.miter_limit;
-            sp.cap = jb.cap_join & 0xFFu;
-            sp.join = jb.cap_join >> 8;
-            sp.res_scale = jb.res_scale;
-            if (sk::stroke_segments(skr, segs + jb.seg_off, (size_t)ns, sp)) {
-                nv = skr.outer.verbs.n;
-                np = skr.outer.pts.n;
+        // the path to stroke: the source, or its dashed copy (dash.rs)
+        const uint8_t *pv = a.src_verbs + jb.src_verb_off;
+        const float *pp = a.src_pts + 2 * (size_t)jb.src_pt_off;
+        size_t pnv = jb.src_verb_cnt;
+        bool any = true;
+        if (jb.dash_cnt > 0 && jb.dverb_cap > 0 && jb.dpt_cap > 0 && jb.mseg_cap > 0 && jb.mpt_cap > 0) {
+            sk::ContourT<SliceTraits> c;
+            bind_vec(c.segs, a.msegs + jb.mseg_off, jb.mseg_cap, &ovf);
+            bind_vec(c.pts, reinterpret_cast<sk::Pt *>(a.mpts) + jb.mpt_off, jb.mpt_cap, &ovf);
+            sk::BuilderT<SliceTraits> db;
+            bind_vec(db.verbs, a.dash_verbs + jb.dverb_off, jb.dverb_cap, &ovf);
+            bind_vec(db.pts, reinterpret_cast<sk::Pt *>(a.dash_pts) + jb.dpt_off, jb.dpt_cap, &ovf);
+            const int r = sk::dash_run(pv, pnv, pp, a.dashes + jb.dash_off, jb.dash_cnt, jb.dash_phase, jb.res_scale, c,
+                                       db);
+            if (r == 0) {
+                any = false;  // dashing left nothing, or gave up: nothing is drawn
+            } else if (r > 0) {
+                pv = db.verbs.p;
+                pp = reinterpret_cast<const float *>(db.pts.p);
+                pnv = db.verbs.n;
+            }
+        }
+        // a path of n verbs makes at most 2n segments
+        if (any && !ovf && 2 * pnv + 1 > jb.seg_cap) ovf = 1u;
+        if (any && !ovf) {
+            const long ns = sk::build_segments(pv, pnv, pp, a.segs + jb.seg_off);
+            if (ns >= 0) {
+                DevStroker skr;
+                auto bind = [&](sk::BuilderT<SliceTraits> &bd, uint8_t *v, float *p) {
+                    bind_vec(bd.verbs, v, jb.verb_cap, &ovf);
+                    bind_vec(bd.pts, reinterpret_cast<sk::Pt *>(p), jb.pt_cap, &ovf);
+                };
+                bind(skr.outer, a.out_verbs + jb.verb_off, a.out_pts + 2 * (size_t)jb.pt_off);
+                bind(skr.inner, a.scr_verbs + 2 * (size_t)jb.verb_off, a.scr_pts + 4 * (size_t)jb.pt_off);
+                bind(skr.cusper, a.scr_verbs + 2 * (size_t)jb.verb_off + jb.verb_cap,
+                     a.scr_pts + 4 * (size_t)jb.pt_off + 2 * (size_t)jb.pt_cap);
+                sk::StrokeParams sp;
+                sp.width = jb.width;
+                sp.miter_limit = jb.miter_limit;
+                sp.cap = jb.cap_join & 0xFFu;
+                sp.join = jb.cap_join >> 8;
+                sp.res_scale = jb.res_scale;
+                if (sk::stroke_segments(skr, a.segs + jb.seg_off, (size_t)ns, sp)) {
+                    nv = skr.outer.verbs.n;
+                    np = skr.outer.pts.n;
+                }
             }
         }
     }
     // the outline's size; after an overflow only a flag (the counts ran on
-    // clamped reads) and the host grows the slice
-    status[2 * j] = ovf ? (nv | 0x80000000u) : nv;
-    status[2 * j + 1] = np;
-    DrawRec &d = draws[jb.draw];
+    // clamped reads) and the host grows the slices
+    a.status[2 * j] = ovf ? (nv | 0x80000000u) : nv;
+    a.status[2 * j + 1] = np;
+    DrawRec &d = a.draws[jb.draw];
     d.verb_off = jb.verb_off;
     d.pt_off = jb.pt_off;
     d.verb_cnt = ovf ? 0u : nv;
@@ -133,6 +176,7 @@ __global__ void k_stroke_gather(const StrokeMove *moves, uint32_t n, const uint8
 }  // namespace
 
 size_t stroke_seg_bytes() { return sizeof(sk::Seg); }
+size_t stroke_mseg_bytes() { return sizeof(sk::MSeg); }
 
 // One launch of k_stroke over an empty job at start-up: the kernel's 6.5 KB of
 // per-thread local memory is reserved then, not inside the first render.
@@ -146,7 +190,10 @@ cudaError_t stroke_warmup(cudaStream_t s) {
     uint32_t *status = reinterpret_cast<uint32_t *>(reinterpret_cast<char *>(mem) + sizeof(StrokeJob) + sizeof(DrawRec));
     if (e == cudaSuccess) {
         // verb_cap = 0: the thread strokes nothing and writes empty counts
-        k_stroke<<<1, 32, 0, s>>>(job, 1, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, draw, status);
+        StrokeArrays a{};
+        a.draws = draw;
+        a.status = status;
+        k_stroke<<<1, 32, 0, s>>>(job, 1, a);
         e = cudaGetLastError();
     }
     cudaError_t e2 = cudaStreamSynchronize(s);
@@ -161,12 +208,24 @@ cudaError_t launch_stroke_gather(const StrokeMove *moves, uint32_t n, const uint
     return cudaGetLastError();
 }
 
-cudaError_t launch_stroke(const StrokeJob *jobs, uint32_t njobs, const uint8_t *src_verbs, const float *src_pts,
-                          uint8_t *out_verbs, float *out_pts, uint8_t *scr_verbs, float *scr_pts, void *segs,
-                          DrawRec *draws, uint32_t *status, cudaStream_t s) {
+cudaError_t launch_stroke(const StrokeJob *jobs, uint32_t njobs, const StrokeBuffers &b, cudaStream_t s) {
     if (!njobs) return cudaSuccess;
-    k_stroke<<<(njobs + 127) / 128, 128, 0, s>>>(jobs, njobs, src_verbs, src_pts, out_verbs, out_pts, scr_verbs,
-                                                 scr_pts, reinterpret_cast<sk::Seg *>(segs), draws, status);
+    StrokeArrays a;
+    a.src_verbs = b.src_verbs;
+    a.src_pts = b.src_pts;
+    a.dashes = b.dashes;
+    a.out_verbs = b.out_verbs;
+    a.out_pts = b.out_pts;
+    a.scr_verbs = b.scr_verbs;
+    a.scr_pts = b.scr_pts;
+    a.segs = reinterpret_cast<sk::Seg *>(b.segs);
+    a.dash_verbs = b.dash_verbs;
+    a.dash_pts = b.dash_pts;
+    a.msegs = reinterpret_cast<sk::MSeg *>(b.msegs);
+    a.mpts = b.mpts;
+    a.draws = b.draws;
+    a.status = b.status;
+    k_stroke<<<(njobs + 127) / 128, 128, 0, s>>>(jobs, njobs, a);
     return cudaGetLastError();
 }
 

@@ -249,6 +249,9 @@ pub struct rgpu_stroke_desc {
     pub res_scale: f32,
     pub cap: u32,
     pub join: u32,
+    pub dash_off: u32,
+    pub dash_cnt: u32,
+    pub dash_phase: f32,
 }
 
 #[link(name = "resvg_gb300")]
@@ -365,6 +368,8 @@ extern "C" {
         verb_count: u32,
         pts: *const f32,
         pt_count: u32,
+        dashes: *const f32,
+        dash_count: u32,
         on_device: c_int,
         out_verbs: *mut u8,
         verb_cap: u32,

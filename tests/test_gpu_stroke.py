@@ -151,3 +151,41 @@ def test_prepared_scene_replays_device_outlines(R):
         for t, (w, h), s in zip(trees, sizes, surfs):
             ref = oracle.render(t.view(), (1, 0, 0, 1, 0, 0), w, h).reshape(h, w, 4)
             assert np.array_equal(s.cpu().numpy(), ref)
+
+
+def _random_dashed(rng, n):
+    out = []
+    for i, (v, p, w, m, cap, join, rs) in enumerate(_random_paths(rng, n)):
+        k = int(rng.choice([2, 2, 4, 6, 3]))          # an odd count is invalid: stroked undashed
+        dash = rng.uniform(0.0, 15.0, k).astype(np.float32)
+        if i % 13 == 0:
+            dash[:] = 0.0                               # all zero: invalid
+        if i % 17 == 0:
+            dash[0] = -1.0                              # negative: invalid
+        if i % 5 == 0:
+            dash[0] = 0.0                               # zero-length dashes
+        phase = float(rng.uniform(-40, 40))
+        out.append((v, p, w, m, cap, join, rs, dash, phase))
+    return out
+
+
+def test_device_dashing_equals_host_random(R):
+    rng = np.random.default_rng(7)
+    paths = _random_dashed(rng, 3000)
+    dev = R.stroke_paths(paths, on_device=True)
+    host = R.stroke_paths(paths, on_device=False)
+    diff = [i for i in range(len(paths)) if not _same(dev[i], host[i])]
+    assert not diff, f"{len(diff)} of {len(paths)} dashed outlines differ, first {diff[:5]}"
+    assert sum(len(h[0]) > 0 for h in host) > 2000
+
+
+def test_dashing_that_outgrows_its_slices_and_gives_up(R):
+    line = ([A_MOVE, A_LINE], np.array([[0, 0], [3000, 0]], np.float32))
+    curve = ([A_MOVE, A_CUBIC], np.array([[0, 0], [900, 400], [-500, 800], [1200, 1200]], np.float32))
+    paths = [line + (2.0, 4.0, 1, 2, 1.0, [0.75, 0.75], 0.3),      # 2000 dashes: several times the first slice
+             curve + (3.0, 4.0, 0, 0, 2.0, [1.0, 2.0, 0.5, 1.5], -7.0),
+             line + (1.0, 4.0, 0, 0, 1.0, [0.001, 0.001], 0.0)]    # 1.5 M dashes: dashing gives up
+    dev = R.stroke_paths(paths, on_device=True)
+    host = R.stroke_paths(paths, on_device=False)
+    assert all(_same(d, h) for d, h in zip(dev, host))
+    assert len(host[0][0]) > 4000 and len(host[2][0]) == 0
