@@ -119,6 +119,7 @@ struct Buffers {
     // per-job status, per-draw sizes and bases
     DevBuf sjobs, sverbs, spts, sscr_verbs, sscr_pts, ssegs, sstatus, dsizes, dbases;
     DevBuf sdash, sdverbs, sdpts, smsegs, smpts;  // dash intervals, dashed paths, measured contours
+    DevBuf smoves;                                // the sizing run's outline moves
     std::vector<DevBuf> surf, img;   // internal surfaces (filter content/results) and filter images
     DevBuf plane;                    // f64 plane of the IIR blur
     void release() {
@@ -126,7 +127,7 @@ struct Buffers {
                          &seg_counts, &seg_offsets, &scan_scratch, &totals, &edges, &edge_draw, &bin_counts,
                          &bin_offsets, &bins, &stack, &span_ovf, &run_ovf, &err, &counter, &fill_cmds, &plane, &hairs, &hair_spans,
                          &sjobs, &sverbs, &spts, &sscr_verbs, &sscr_pts, &ssegs, &sstatus, &dsizes, &dbases,
-                         &sdash, &sdverbs, &sdpts, &smsegs, &smpts};
+                         &sdash, &sdverbs, &sdpts, &smsegs, &smpts, &smoves};
         for (DevBuf *b : all) b->release();
         for (auto &b : surf) b.release();
         for (auto &b : img) b.release();
@@ -236,6 +237,23 @@ Context &ctx() {
     static Context c;
     return c;
 }
+
+// Outline-cache writebacks run on their own threads while the device works
+// on; every render entry point joins them before it returns (so a tree is
+// never written after the call that stroked it).
+std::mutex g_wb_mu;
+std::vector<std::thread> g_writebacks;
+void join_writebacks() {
+    std::vector<std::thread> ts;
+    {
+        std::lock_guard<std::mutex> g(g_wb_mu);
+        ts.swap(g_writebacks);
+    }
+    for (auto &t : ts) t.join();
+}
+struct WritebackJoin {
+    ~WritebackJoin() { join_writebacks(); }
+};
 
 #define CK(expr)                                                                                  \
     do {                                                                                          \
@@ -527,31 +545,37 @@ int cache_outlines(Buffers &b, Plan &p, cudaStream_t s) {
     SceneBuild &sb = p.sb;
     const size_t nj = sb.stroke_jobs.size();
     if (sb.stroke_keys.size() != nj) return RGPU_OK;
-    std::vector<uint8_t> hv(p.sverbs);
-    std::vector<float> hp(2 * p.spts);
-    if (p.sverbs) CK(cudaMemcpyAsync(hv.data(), b.sverbs.p, p.sverbs, cudaMemcpyDeviceToHost, s));
-    if (p.spts) CK(cudaMemcpyAsync(hp.data(), b.spts.p, p.spts * 8, cudaMemcpyDeviceToHost, s));
+    auto hv = std::make_shared<std::vector<uint8_t>>(p.sverbs);
+    auto hp = std::make_shared<std::vector<float>>(2 * p.spts);
+    if (p.sverbs) CK(cudaMemcpyAsync(hv->data(), b.sverbs.p, p.sverbs, cudaMemcpyDeviceToHost, s));
+    if (p.spts) CK(cudaMemcpyAsync(hp->data(), b.spts.p, p.spts * 8, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     g_stats.d2h_bytes += p.sverbs + p.spts * 8;
-    auto store = [&](size_t a, size_t e) {
+    // the slices and keys the inserts need, copied: the plan lives on
+    struct Slice { uint32_t vo, vn, po, pn; };
+    auto slices = std::make_shared<std::vector<Slice>>(nj);
+    auto keys = std::make_shared<std::vector<StrokeKey>>(sb.stroke_keys);
+    for (size_t j = 0; j < nj; j++) {
+        const StrokeJob &jb = sb.stroke_jobs[j];
+        (*slices)[j] = Slice{jb.verb_off, jb.verb_cap, jb.pt_off, jb.pt_cap};
+    }
+    auto store = [hv, hp, slices, keys](size_t a, size_t e) {
         for (size_t j = a; j < e; j++) {
-            const StrokeJob &jb = sb.stroke_jobs[j];
+            const Slice &sl = (*slices)[j];
             std::shared_ptr<PathData> out;
-            if (jb.verb_cap > 1) {
+            if (sl.vn > 1) {
                 out = std::make_shared<PathData>();
-                out->verbs.assign(hv.begin() + jb.verb_off, hv.begin() + jb.verb_off + jb.verb_cap);
-                out->pts.assign(hp.begin() + 2 * (size_t)jb.pt_off, hp.begin() + 2 * ((size_t)jb.pt_off + jb.pt_cap));
+                out->verbs.assign(hv->begin() + sl.vo, hv->begin() + sl.vo + sl.vn);
+                out->pts.assign(hp->begin() + 2 * (size_t)sl.po, hp->begin() + 2 * ((size_t)sl.po + sl.pn));
             }
-            const StrokeKey &k = sb.stroke_keys[j];
+            const StrokeKey &k = (*keys)[j];
             k.tree->store_stroke_outline(k.path, k.res_scale, std::move(out));
         }
     };
     // contiguous ranges: a tree's jobs are adjacent, so threads rarely share a cache
-    const size_t nt = std::min<size_t>(std::max(1u, std::thread::hardware_concurrency()), nj / 4096 + 1);
-    std::vector<std::thread> pool;
-    for (size_t k = 1; k < nt; k++) pool.emplace_back(store, nj * k / nt, nj * (k + 1) / nt);
-    store(0, nj / nt);
-    for (auto &t : pool) t.join();
+    const size_t nt = std::min<size_t>(std::max(1u, std::thread::hardware_concurrency() / 2), nj / 4096 + 1);
+    std::lock_guard<std::mutex> g(g_wb_mu);
+    for (size_t k = 0; k < nt; k++) g_writebacks.emplace_back(store, nj * k / nt, nj * (k + 1) / nt);
     return RGPU_OK;
 }
 
@@ -613,14 +637,12 @@ int run_strokes(Buffers &b, Plan &p, cudaStream_t s) {
         moves[j].dst_verb = sb.stroke_jobs[j].verb_off;
         moves[j].dst_pt = sb.stroke_jobs[j].pt_off;
     }
-    DevBuf dmoves;
-    CK(dmoves.ensure(nj * sizeof(StrokeMove)));
-    CK(cudaMemcpyAsync(dmoves.p, moves.data(), nj * sizeof(StrokeMove), cudaMemcpyHostToDevice, s));
-    CK(launch_stroke_gather(dmoves.as<StrokeMove>(), (uint32_t)nj, b.sverbs.as<uint8_t>(), b.spts.as<float>(),
+    CK(b.smoves.ensure(nj * sizeof(StrokeMove)));
+    // pageable sources: the copies are staged before the calls return
+    CK(cudaMemcpyAsync(b.smoves.p, moves.data(), nj * sizeof(StrokeMove), cudaMemcpyHostToDevice, s));
+    CK(launch_stroke_gather(b.smoves.as<StrokeMove>(), (uint32_t)nj, b.sverbs.as<uint8_t>(), b.spts.as<float>(),
                             b.sscr_verbs.as<uint8_t>(), b.sscr_pts.as<float>(), b.draws.as<DrawRec>(), s));
     CK(cudaMemcpyAsync(b.sjobs.p, sb.stroke_jobs.data(), nj * sizeof(StrokeJob), cudaMemcpyHostToDevice, s));
-    CK(cudaStreamSynchronize(s));
-    dmoves.release();
     std::swap(b.sverbs, b.sscr_verbs);
     std::swap(b.spts, b.sscr_pts);
     if ((r = ensure_stroke_buffers(b, p))) return r;
@@ -833,6 +855,7 @@ int render_host(const rgpu_tree *tree, const resvg_transform &ts, uint32_t w, ui
     }
     Context &c = ctx();
     std::lock_guard<std::mutex> lock(c.mu);
+    WritebackJoin writebacks;  // joined before the lock is released
     int r = ensure_device(c);
     if (r) return r;
     cudaStream_t s = c.stream;
@@ -1049,6 +1072,7 @@ int rgpu_render_device(const resvg_render_tree *tree, resvg_transform ts, uint32
     }
     Context &c = ctx();
     std::lock_guard<std::mutex> lock(c.mu);
+    WritebackJoin writebacks;  // joined before the lock is released
     int r = ensure_device(c);
     if (r) return r;
     cudaStream_t s = stream ? (cudaStream_t)stream : c.stream;
@@ -1071,6 +1095,7 @@ int rgpu_render_batch(const resvg_render_tree *const *trees, const resvg_transfo
     }
     Context &c = ctx();
     std::lock_guard<std::mutex> lock(c.mu);
+    WritebackJoin writebacks;  // joined before the lock is released
     int r = ensure_device(c);
     if (r) return r;
     cudaStream_t s = stream ? (cudaStream_t)stream : c.stream;
@@ -1197,6 +1222,7 @@ int rgpu_scene_render(rgpu_scene *sc, void *stream) {
     if (!sc) { set_error("invalid arguments"); return RGPU_ERR_INVALID_ARG; }
     Context &c = ctx();
     std::lock_guard<std::mutex> lock(c.mu);
+    WritebackJoin writebacks;  // joined before the lock is released
     cudaStream_t s = stream ? (cudaStream_t)stream : c.stream;
     sc->last_stream = s;
     int r;
