@@ -674,9 +674,19 @@ def run_plain(args, rank, world):
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
     torch.cuda.set_device(dev)
     R.init(0)
+    from resvg_gb300 import batch as BT
     tree = R.Tree.generate(args.config, seed=SEED, index=rank, scale=args.scale)
     w, h = (int(v) for v in tree.size)
     surface = torch.zeros((h, w, 4), dtype=torch.uint8, device=dev)
+    # the product's autotuner (rgpu_autotune) picks band rows and pixels per
+    # thread for this scene, on a copy of the tree: the timed tree's own first
+    # render is the one that strokes its paths
+    t0 = time.perf_counter()
+    tune_tree = R.Tree.generate(args.config, seed=SEED, index=rank, scale=args.scale)
+    best_tuning, tune_ms = R.autotune([tune_tree], [IDENT], [w], [h], [surface.data_ptr()], BT.TUNING_CANDIDATES,
+                                      reps=3)
+    tune_s = time.perf_counter() - t0
+    del tune_tree
     stream = torch.cuda.Stream(device=dev)
     torch.cuda.set_stream(stream)
     sh = stream.cuda_stream
@@ -747,7 +757,10 @@ def run_plain(args, rank, world):
         "config": {"workload": "config%d: %s" % (args.config, CONFIG_DESC.get(args.config, "")),
                    "canvas": [w, h], "draws": info["draws"], "edges": info["edges"],
                    "binned_edges": info["binned_edges"], "work_items": info["work_items"],
-                   "l2": "flushed between steps (256 MB write)", "graph_replay": True, "stroke": stroke},
+                   "l2": "flushed between steps (256 MB write)", "graph_replay": True, "stroke": stroke,
+                   "tuning": {"band_rows": best_tuning[0], "pixels_per_thread": best_tuning[1],
+                              "autotune_ms": tune_ms, "autotune_s": tune_s,
+                              "candidates": [list(c) for c in BT.TUNING_CANDIDATES]}},
         "mpix_s": value * out_px / 1e6,
         "raster_ms": rms,
         "wall_s_timed_region": t_wall,
