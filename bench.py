@@ -79,6 +79,9 @@ def parse(argv=None):
     ap.add_argument("--profile", action="store_true",
                     help="for ncu captures: prepare the workload, render it twice (the sizing render, then the "
                          "one to capture, k_raster launches 1 + levels onwards) and exit")
+    ap.add_argument("--tuning", type=str, default="",
+                    help="with --profile: band rows and pixels per thread ('4,8'), the choice the timed run's "
+                         "autotuner made (the bench line's config.tuning)")
     return ap.parse_args(argv)
 
 
@@ -826,6 +829,9 @@ def run_profile(args):
         torch.cuda.synchronize()
         print(json.dumps({"profile": "config4", "scenes": 256, "loss": loss}), flush=True)
         return
+    if args.tuning:
+        band_rows, px = (int(v) for v in args.tuning.split(","))
+        R.set_tuning(band_rows, px)
     if args.config == 3:
         trees = [R.Tree.generate(3, seed=SEED, index=i) for i in range(args.scenes)]
     else:
@@ -844,7 +850,7 @@ def run_profile(args):
         scene.render()
         ms.append(scene.check())
     print(json.dumps({"profile": "config%d" % args.config, "scenes": len(trees), "raster_ms": ms,
-                      "info": scene.info()}), flush=True)
+                      "tuning": R.get_tuning(), "info": scene.info()}), flush=True)
 
 
 def main():

@@ -225,7 +225,8 @@ cudaError_t launch_stroke(const StrokeJob *jobs, uint32_t njobs, const StrokeBuf
     a.mpts = b.mpts;
     a.draws = b.draws;
     a.status = b.status;
-    k_stroke<<<(njobs + 127) / 128, 128, 0, s>>>(jobs, njobs, a);
+    // one warp per block: the jobs of a warp diverge, so a small pass spreads its warps over the SMs
+    k_stroke<<<(njobs + 31) / 32, 32, 0, s>>>(jobs, njobs, a);
     return cudaGetLastError();
 }
 
