@@ -16,8 +16,9 @@ These workloads run tiny-skia's lowp pipeline (solid colours, linear and
 simple radial gradients, source-over, the integer clip and mask passes), the
 integer box blur, and the IIR blur with the reference's f64 operations in the
 reference's order.  The 2048^2 filter chain converts to linearRGB and back and
-runs the colour matrix and arithmetic composite in f32; the benchmark spec allows
-1/255 there, and this test asserts the tighter bound the device reaches.
+runs the colour matrix and arithmetic composite in f32; the floating-point
+tolerance of the filter path is 1/255 there, and this test asserts the
+tighter bound the device reaches.
 """
 import os
 
