@@ -1158,8 +1158,18 @@ INHERITED = {"fill", "fill-opacity", "fill-rule", "stroke", "stroke-width", "str
              "shape-rendering", "clip-rule", "color", "color-interpolation-filters", "paint-order", "font-size"}
 NON_INHERITED = {"opacity", "clip-path", "mask", "filter", "mix-blend-mode", "isolation", "display",
                  "stop-color", "stop-opacity", "flood-color", "flood-opacity", "transform"}
-UNSUPPORTED_ELEMS = {"text", "switch", "foreignObject", "tspan", "textPath",
+UNSUPPORTED_ELEMS = {"text", "foreignObject", "tspan", "textPath",
                      "animate", "set"}
+# usvg's element ids (svgtree/names.rs EId): any other element, or one of
+# another namespace, is dropped with its children (svgtree/parse.rs
+# parse_tag_name / parse_xml_node)
+KNOWN_ELEMS = {
+    "a", "circle", "clipPath", "defs", "ellipse", "feBlend", "feColorMatrix", "feComponentTransfer", "feComposite",
+    "feConvolveMatrix", "feDiffuseLighting", "feDisplacementMap", "feDistantLight", "feDropShadow", "feFlood",
+    "feFuncA", "feFuncB", "feFuncG", "feFuncR", "feGaussianBlur", "feImage", "feMerge", "feMergeNode",
+    "feMorphology", "feOffset", "fePointLight", "feSpecularLighting", "feSpotLight", "feTile", "feTurbulence",
+    "filter", "g", "image", "line", "linearGradient", "marker", "mask", "path", "pattern", "polygon", "polyline",
+    "radialGradient", "rect", "stop", "style", "svg", "switch", "symbol", "text", "textPath", "tref", "tspan", "use"}
 BLEND = {"normal": "source-over", "multiply": "multiply", "screen": "screen", "overlay": "overlay",
          "darken": "darken", "lighten": "lighten", "color-dodge": "color-dodge", "color-burn": "color-burn",
          "hard-light": "hard-light", "soft-light": "soft-light", "difference": "difference",
@@ -1467,6 +1477,8 @@ class Builder(Loader):
 
     def node(self, e, parent, transform_extra=IDENT):
         tag = _tag(e)
+        if tag not in KNOWN_ELEMS:
+            return
         if tag in ("defs", "linearGradient", "radialGradient", "clipPath", "mask", "filter", "title", "desc",
                    "metadata", "stop", "pattern", "style", "marker", "symbol"):
             return
@@ -1483,8 +1495,8 @@ class Builder(Loader):
             return
         if tag == "use":
             ref = self.href(e)
-            if ref is None:
-                return
+            if ref is None or _tag(ref) not in KNOWN_ELEMS:
+                return  # svgtree: a use linked to no SVG element is dropped
             x = self.num(e, "x", 0.0, self.vbw)
             y = self.num(e, "y", 0.0, self.vbh)
             if _tag(ref) == "symbol":
@@ -1724,8 +1736,8 @@ class Builder(Loader):
                     max(b[3] for b in boxes))
         if tag == "use":
             ref = self.href(e)
-            if ref is None:
-                return None
+            if ref is None or _tag(ref) not in KNOWN_ELEMS:
+                return  # svgtree: a use linked to no SVG element is dropped None
             b = self.element_bbox(ref)
             if b is None:
                 return None
