@@ -633,6 +633,32 @@ def parse_angle_deg(s):
     return v
 
 
+def parse_transform_origin(s):
+    """svgtypes TransformOrigin (CSS transform-origin): one to three values,
+    keywords (left / center / right, top / bottom) or lengths; a single value
+    sets x (or y for top / bottom) with the other at center; a y keyword first
+    swaps the pair; a third value (z) is ignored.  Returns the (x, y) lengths
+    as strings, or None when the value does not parse."""
+    toks = (s or "").replace(",", " ").split()
+    if not 1 <= len(toks) <= 3:
+        return None
+    kw = {"left": "0%", "center": "50%", "right": "100%", "top": "0%", "bottom": "100%"}
+
+    def ok(t):
+        return t in kw or re.fullmatch(NUM + r"(px|%|em|ex|in|cm|mm|pt|pc)?", t) is not None
+    if not all(ok(t) for t in toks[:2]):
+        return None
+    if len(toks) == 1:
+        t = toks[0]
+        return ("50%", kw[t]) if t in ("top", "bottom") else (kw.get(t, t), "50%")
+    x, y = toks[0], toks[1]
+    if x in ("top", "bottom") or y in ("left", "right"):
+        x, y = y, x
+    if x in ("top", "bottom") or y in ("left", "right"):
+        return None
+    return kw.get(x, x), kw.get(y, y)
+
+
 def parse_transform(s):
     ts = IDENT
     for name, args in re.findall(r"(\w+)\s*\(([^)]*)\)", s or ""):
@@ -1446,6 +1472,33 @@ class Builder(Loader):
         self.tree.ids = self.ids_out
         return self.tree
 
+    def transform_of(self, e, attr="transform", value=None):
+        """An element's transform with its transform-origin (converter.rs
+        resolve_transform): translate(origin) . transform . translate(-origin),
+        the origin's lengths and percentages in user space (percentages of the
+        viewBox).  transform-origin is a presentation attribute but not
+        inherited; one that does not parse is ignored."""
+        ts = parse_transform(value if value is not None else (self.attrs(e).get(attr, "") or ""))
+        o = self.own_attr(e, "transform-origin")
+        if o is None:
+            return ts
+        xy = parse_transform_origin(o)
+        if xy is None:
+            return ts
+        fsz = self.font_size(e)
+        try:
+            dx = parse_length(xy[0], self.vbw, fsz)
+            dy = parse_length(xy[1], self.vbh, fsz)
+        except (ValueError, Unsupported):
+            return ts
+        return mat_mul(mat_mul((1.0, 0.0, 0.0, 1.0, dx, dy), ts), (1.0, 0.0, 0.0, 1.0, -dx, -dy))
+
+    def own_attr(self, e, name):
+        """A non-inherited presentation attribute: from the element's style or
+        attribute, not from its ancestors."""
+        v = self.attrs(e).get(name)
+        return v.strip() if isinstance(v, str) else None
+
     def background(self, svg, parent, rect):
         """usvg converter.rs:393-400 and 504-521: the root's non-standard
         background-color (a presentation attribute), when it parses as a plain
@@ -1487,7 +1540,7 @@ class Builder(Loader):
         if tag not in ("g", "path", "rect", "circle", "ellipse", "line", "polyline", "polygon", "use", "svg", "a",
                        "image"):
             raise Unsupported("element " + tag)
-        ts = parse_transform(self.attrs(e).get("transform", ""))
+        ts = self.transform_of(e)
         if transform_extra != IDENT:
             ts = mat_mul(transform_extra, ts)
         if tag == "image":
@@ -1729,7 +1782,7 @@ class Builder(Loader):
                 b = self.element_bbox(c)
                 if b is None:
                     continue
-                boxes.append(_map_box(parse_transform(self.attrs(c).get("transform", "")), b))
+                boxes.append(_map_box(self.transform_of(c), b))
             if not boxes:
                 return None
             return (min(b[0] for b in boxes), min(b[1] for b in boxes), max(b[2] for b in boxes),
@@ -1737,11 +1790,11 @@ class Builder(Loader):
         if tag == "use":
             ref = self.href(e)
             if ref is None or _tag(ref) not in KNOWN_ELEMS:
-                return  # svgtree: a use linked to no SVG element is dropped None
+                return None  # svgtree: a use linked to no SVG element is dropped
             b = self.element_bbox(ref)
             if b is None:
                 return None
-            t = parse_transform(self.attrs(ref).get("transform", ""))
+            t = self.transform_of(ref)
             t = mat_mul((1, 0, 0, 1, self.num(e, "x", 0.0, self.vbw), self.num(e, "y", 0.0, self.vbh)), t)
             return _map_box(t, b)
         geo = self.geometry(e)
@@ -1939,7 +1992,7 @@ class Builder(Loader):
         cunits = (attr("patternContentUnits") or "userSpaceOnUse").strip()
         obb = units != "userSpaceOnUse"
         cobb = cunits == "objectBoundingBox"
-        pts = parse_transform(attr("patternTransform") or "")
+        pts = self.transform_of(ref, value=attr("patternTransform") or "")
         if abs(pts[0] * pts[3] - pts[1] * pts[2]) <= 0.0 or not all(math.isfinite(v) for v in pts):
             pts = (1.0, 0.0, 0.0, 1.0, 0.0, 0.0)  # a non-invertible patternTransform reads as none
 
@@ -2098,7 +2151,7 @@ class Builder(Loader):
                 stops[i][0] = o1
         units = self.grad_attr(ref, "gradientUnits", chain) or "objectBoundingBox"
         spread = {"pad": 0, "reflect": 1, "repeat": 2}.get((self.grad_attr(ref, "spreadMethod", chain) or "pad").strip(), 0)
-        gts = parse_transform(self.grad_attr(ref, "gradientTransform", chain) or "")
+        gts = self.transform_of(ref, value=self.grad_attr(ref, "gradientTransform", chain) or "")
         if abs(gts[0] * gts[3] - gts[1] * gts[2]) <= 0.0 or not all(math.isfinite(v) for v in gts):
             gts = (1.0, 0.0, 0.0, 1.0, 0.0, 0.0)  # a non-invertible gradientTransform reads as none
         p = A.Paint()
@@ -2446,7 +2499,7 @@ class Builder(Loader):
         if _tag(ce) != "clipPath":
             return None
         units = (ce.get("clipPathUnits") or "userSpaceOnUse").strip()
-        ts = parse_transform(ce.get("transform", ""))
+        ts = self.transform_of(ce, value=ce.get("transform", ""))
         if units == "objectBoundingBox":
             if bbox is None or bbox[2] <= bbox[0] or bbox[3] <= bbox[1]:
                 return None
@@ -2481,7 +2534,7 @@ class Builder(Loader):
         if not self.visible(e):
             return
         a = self.attrs(e)
-        ts = parse_transform(a.get("transform", ""))
+        ts = self.transform_of(e)
         target = e
         if _tag(e) == "use":
             target = self.href(e)

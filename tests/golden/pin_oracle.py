@@ -54,6 +54,7 @@ CATEGORIES = [
     "filters/filter-functions", "filters/feComponentTransfer", "filters/feDropShadow",
     "filters/feTurbulence", "filters/feTile", "filters/feDisplacementMap", "filters/feImage",
     "paint-servers/pattern", "structure/image", "painting/marker", "painting/context", "structure/symbol",
+    "structure/transform-origin",
 ]
 IMAGE_SIZE = 300
 FIXTURES_PER_DIR = 4
