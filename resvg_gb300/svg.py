@@ -633,6 +633,46 @@ def parse_angle_deg(s):
     return v
 
 
+# Attributes CSS cannot set: svgtree/parse.rs takes only presentation
+# attributes from style sheets and style attributes (geometry and element
+# attributes are left to the XML attributes)
+NOT_PRESENTATION = {
+    "x", "y", "width", "height", "r", "rx", "ry", "cx", "cy", "fx", "fy", "fr", "d", "points", "x1", "y1", "x2",
+    "y2", "offset", "viewBox", "preserveAspectRatio", "gradientUnits", "gradientTransform", "spreadMethod",
+    "patternUnits", "patternContentUnits", "patternTransform", "clipPathUnits", "maskUnits", "maskContentUnits",
+    "filterUnits", "primitiveUnits", "refX", "refY", "markerWidth", "markerHeight", "markerUnits", "orient", "href",
+    "id", "class", "pathLength"}
+
+# switch.rs FEATURES: the SVG 1.1 feature strings usvg supports
+SVG_FEATURES = {"http://www.w3.org/TR/SVG11/feature#" + f for f in (
+    "SVGDOM-static", "SVG-static", "CoreAttribute", "Structure", "BasicStructure", "ContainerAttribute",
+    "ConditionalProcessing", "Image", "Style", "Shape", "Text", "BasicText", "PaintAttribute",
+    "BasicPaintAttribute", "OpacityAttribute", "GraphicsAttribute", "BasicGraphicsAttribute", "Marker", "Gradient",
+    "Pattern", "Clip", "BasicClip", "Mask", "Filter", "BasicFilter", "XlinkAttribute")}
+LANGUAGES = ("en",)  # usvg Options::languages default
+
+
+def condition_passed(e):
+    """switch.rs is_condition_passed: no requiredExtensions, every
+    requiredFeatures string supported, and a systemLanguage entry equal to a
+    user language or to one followed by '-'."""
+    if e.get("requiredExtensions") is not None:
+        return False
+    rf = e.get("requiredFeatures")
+    if rf is not None and any(f not in SVG_FEATURES for f in rf.split(" ")):
+        return False
+    sl = e.get("systemLanguage")
+    if sl is not None:
+        for lang in sl.split(","):
+            lang = lang.strip()
+            if lang in LANGUAGES:
+                return True
+            if "-" in lang and lang[:lang.index("-")] in LANGUAGES:
+                return True
+        return False
+    return True
+
+
 def parse_transform_origin(s):
     """svgtypes TransformOrigin (CSS transform-origin): one to three values,
     keywords (left / center / right, top / bottom) or lengths; a single value
@@ -1316,8 +1356,6 @@ class Loader:
         for e in self.root.iter():
             if _tag(e) in UNSUPPORTED_ELEMS:
                 raise Unsupported("element " + _tag(e))
-            if e.get("systemLanguage") is not None:
-                raise Unsupported("systemLanguage")
         self.clip_cache, self.mask_cache, self.filter_cache = {}, {}, {}
         # markers being converted (a marker inside its own content is skipped;
         # nodes made for markers carry no id), and the (fill, stroke) that
@@ -1343,12 +1381,14 @@ class Loader:
             for kk in (("marker-start", "marker-mid", "marker-end") if k == "marker" else (k,)):
                 d[kk] = v
         for k, v, imp in self.css.get(e, ()):
-            put(important if imp else a, k, v)
+            if k not in NOT_PRESENTATION:
+                put(important if imp else a, k, v)
         if st:
-            for part in st.split(";"):
+            for part in re.sub(r"/\*.*?\*/", "", st, flags=re.S).split(";"):
                 if ":" in part:
                     k, v = part.split(":", 1)
-                    put(a, k.strip(), v.strip())
+                    if k.strip() not in NOT_PRESENTATION:
+                        put(a, k.strip(), v.strip())
         a.update(important)
         return a
 
@@ -1463,7 +1503,9 @@ class Builder(Loader):
         self.background(svg, root, vb if vb and len(vb) == 4 else (0.0, 0.0, W, H))
         # the root <svg> is a group of its own (opacity, clip-path, mask, filter,
         # display) inside the viewBox transform, as usvg converts it
-        if self.attrs(svg).get("display", "").strip() != "none":
+        # converter.rs convert_doc: a root that is not visible (display:none or
+        # failed conditions) leaves the tree empty
+        if self.attrs(svg).get("display", "").strip() != "none" and condition_passed(svg):
             g = self.group_for(svg, root, IDENT)
             if g is not None:
                 for c in svg:
@@ -1524,9 +1566,11 @@ class Builder(Loader):
                            [(x, y), (x + w, y), (x + w, y + h), (x, y + h)])
 
     def visible(self, e):
+        """usvg is_visible_element: not display:none and the conditional
+        attributes pass (switch.rs is_condition_passed)."""
         if self.attrs(e).get("display", "").strip() == "none":
             return False
-        return True
+        return condition_passed(e)
 
     def node(self, e, parent, transform_extra=IDENT):
         tag = _tag(e)
@@ -1538,7 +1582,7 @@ class Builder(Loader):
         if not self.visible(e):
             return
         if tag not in ("g", "path", "rect", "circle", "ellipse", "line", "polyline", "polygon", "use", "svg", "a",
-                       "image"):
+                       "image", "switch"):
             raise Unsupported("element " + tag)
         ts = self.transform_of(e)
         if transform_extra != IDENT:
@@ -1562,6 +1606,13 @@ class Builder(Loader):
         if tag in ("g", "a"):
             for c in e:
                 self.node(c, g)
+        elif tag == "switch":
+            # switch.rs: the first child element whose conditions pass
+            for c in e:
+                # unknown elements are not in usvg's tree, so never the chosen child
+                if isinstance(c.tag, str) and _tag(c) in KNOWN_ELEMS and condition_passed(c):
+                    self.node(c, g)
+                    break
         elif tag == "use":
             # the instanced element inherits from the <use>, not from where it
             # is defined
@@ -1709,7 +1760,7 @@ class Builder(Loader):
         # mix-blend-mode and isolation count only as CSS properties (style), not as
         # presentation attributes
         css = {}
-        for part in (e.get("style") or "").split(";"):
+        for part in re.sub(r"/\*.*?\*/", "", e.get("style") or "", flags=re.S).split(";"):
             if ":" in part:
                 k, v = part.split(":", 1)
                 css[k.strip()] = v.strip()

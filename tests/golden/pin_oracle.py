@@ -54,7 +54,9 @@ CATEGORIES = [
     "filters/filter-functions", "filters/feComponentTransfer", "filters/feDropShadow",
     "filters/feTurbulence", "filters/feTile", "filters/feDisplacementMap", "filters/feImage",
     "paint-servers/pattern", "structure/image", "painting/marker", "painting/context", "structure/symbol",
-    "structure/transform-origin",
+    "structure/transform-origin", "filters/enable-background", "structure/switch", "structure/systemLanguage",
+    "filters/flood-color", "filters/flood-opacity", "structure/defs", "painting/overflow", "structure/a",
+    "painting/image-rendering", "structure/style-attribute", "masking/clip",
 ]
 IMAGE_SIZE = 300
 FIXTURES_PER_DIR = 4
