@@ -2772,11 +2772,22 @@ class Builder(Loader):
             p.f[11] = fa(light, "limitingConeAngle", np.nan)
         return True
 
+    def own_value(self, e, name):
+        """A non-inherited attribute's value; `inherit` takes the direct
+        parent's (svgtree/parse.rs resolve_inherit), None when it has none."""
+        v = self.attrs(e).get(name)
+        if v is not None and v.strip() == "inherit":
+            p = self.parent.get(e)
+            v = self.attrs(p).get(name) if p is not None else None
+            if v is not None and v.strip() == "inherit":
+                v = None
+        return v
+
     def attr_color(self, e, name):
         """An element's own colour attribute as svgtypes parses it and usvg splits
         it: ((r, g, b), alpha) with the alpha stored as u8; black when absent or
         invalid."""
-        v = self.attrs(e).get(name)
+        v = self.own_value(e, name)
         try:
             c = parse_color(v) if v is not None and v.strip().lower() != "currentcolor" else None
         except (InvalidColor, Unsupported):
@@ -3114,9 +3125,9 @@ class Builder(Loader):
                     p.f[k] = float(c.get(n, "0"))
             elif tag == "feFlood":
                 p.kind = A.FE_FLOOD
-                col = parse_color(self.attrs(c).get("flood-color", "black")) or ((0, 0, 0), 0.0)
+                col = parse_color(self.own_value(c, "flood-color") or "black") or ((0, 0, 0), 0.0)
                 p.i[0], p.i[1], p.i[2] = col[0]
-                fo = self.attrs(c).get("flood-opacity", "1").strip()
+                fo = (self.own_value(c, "flood-opacity") or "1").strip()
                 fo = float(fo[:-1]) / 100 if fo.endswith("%") else float(fo)
                 p.f[0] = max(0.0, min(1.0, fo)) * col[1]
             elif tag == "feOffset":
