@@ -1764,9 +1764,8 @@ class Builder(Loader):
             if ":" in part:
                 k, v = part.split(":", 1)
                 css[k.strip()] = v.strip()
-        blend = BLEND.get(css.get("mix-blend-mode", "normal").strip(), None)
-        if blend is None:
-            raise Unsupported("blend mode")
+        # a value that is not a blend mode reads as normal (the attribute does not parse)
+        blend = BLEND.get(css.get("mix-blend-mode", "normal").strip(), BLEND["normal"])
         isolate = css.get("isolation", "auto").strip() == "isolate"
         # svgtree drops a clip-path / mask attribute whose link has no element
         clip = None if clip == "missing" else clip
